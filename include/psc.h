@@ -1,0 +1,144 @@
+/*
+ * psc.h — C ABI of the GB300 pseudo-spectral lattice evolution (libpsc.so).
+ *
+ * The reference (PSpectCosmo) has no library interface: its path is a set of free
+ * functions on global arrays, configured at compile time. This header is the
+ * drop-in boundary for that path. Each entry point says which reference routine
+ * it replaces (file:line inside the reference project).
+ *
+ *   compile-time parameters.h / model.h   -> psc_params (run-time values, same names)
+ *   initialize() + initialize_GW()        -> psc_init_ic
+ *   evolve_VV_k_nopad(dt) / evolve_VV(dt) -> psc_step
+ *   spectra(), energy(), meansvars(), scale() -> psc_spectra, psc_energies, psc_means
+ *   global arrays f_k, pi_k, u_k, pi_u_k, a, ad, add -> psc_get_state / psc_set_state
+ *
+ * Conventions: every call returns PSC_OK (0) or a negative PSC_ERR_* code and
+ * never throws or exits; psc_strerror names the code and psc_last_error gives the
+ * message of the last failure on the calling thread. A handle owns its device
+ * memory and one CUDA stream; calls on one handle must not run concurrently.
+ * Complex arrays are interleaved (re, im) doubles in the reference's FFTW layout:
+ * [N][N][N/2+1] with the last index fastest, one block of N*N*(N/2+1) complex per
+ * field or tensor component. Real arrays are [N][N][N] doubles. Host buffers are
+ * always FP64, whatever precision the device evolves in.
+ */
+#ifndef PSC_H
+#define PSC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PSC_OK 0
+#define PSC_ERR_CONFIG (-1)     /* unsupported parameter (N not a power of two in [8,1024], ...) */
+#define PSC_ERR_ARG (-2)        /* null pointer / bad argument */
+#define PSC_ERR_CUDA (-3)       /* a CUDA runtime call failed */
+#define PSC_ERR_NONFINITE (-4)  /* the on-device finite check tripped (NaN/Inf in the background) */
+#define PSC_ERR_TIMEOUT (-5)    /* a bounded device-side wait gave up */
+#define PSC_ERR_STATE (-6)      /* call out of order (e.g. step before state is set) */
+#define PSC_ERR_NOMEM (-7)      /* device allocation failed */
+
+#define PSC_MODEL_PHI2 0      /* V = phi^2/2 (reference model.h:35-99) */
+#define PSC_MODEL_PHI2CHI2 1  /* V = phi^2/2 + gsq phi^2 chi^2 / 2 (two-field preheating) */
+
+/*
+ * Run configuration: the reference's compile-time parameters.h / model.h surface as
+ * run-time values. Field names follow parameters.h.
+ */
+typedef struct psc_params {
+    int N;                  /* parameters.h:22   points per lattice edge: power of two, 8..1024 */
+    int nflds;              /* parameters.h:20   number of scalar fields: 1 or 2 */
+    int vv;                 /* parameters.h:10   integrator: 2 (velocity Verlet), 4, 6, 8, 10 (Yoshida) */
+    int alpha;              /* parameters.h:120  time variable exponent (0 = cosmic time) */
+    int expansion;          /* parameters.h:67   must be 2 (self-consistent Friedmann) for evolution */
+    int simulate_inflation; /* parameters.h:17   fixed-amplitude ICs + R_Q2C mask in K, G */
+    int spectral;           /* parameters.h:12   1: evolve_VV_k_nopad semantics, 0: evolve_VV (real space) */
+    int with_gw;            /* parameters.h:15   evolve the tensor perturbations u_ij (needs spectral = 0) */
+    int precision;          /* 64: FP64 state (the plain method) or 32: FP32 state, FP64 background */
+    int model;              /* PSC_MODEL_* (model.h) */
+    int seed;               /* parameters.h:65   Park-Miller seed (rand_uniform, initialize.cpp:13) */
+    int reserved0;
+    double kIR;             /* parameters.h:27   smallest lattice wavenumber (program units) */
+    double a0;              /* parameters.h:29   initial scale factor */
+    double MPl;             /* parameters.h:121  Planck mass */
+    double m_in_MPl;        /* parameters.h:110  mass in Planck units (omegaStar = m_in_MPl * fStar) */
+    double fStar;           /* parameters.h:127  field unit (0 => MPl) */
+    double epsilon;         /* parameters.h:39   R_Q2C threshold of the K, G mask */
+    double gsq;             /* two-field coupling g^2 in program units */
+    double initfield[2];    /* parameters.h:123  initial homogeneous fields */
+    double initderivs[2];   /* parameters.h:124  initial homogeneous field derivatives */
+    double kcutoff;         /* parameters.h:30   initial low-pass cut (0 = none) */
+} psc_params;
+
+typedef struct psc_handle psc_handle;
+
+/* Fill *p with the reference's shipped parameters.h / model.h values (N = 64,
+ * one field, VV = 2, kIR = 25, phi0 = 11, spectral path, FP64). */
+void psc_default_params(psc_params *p);
+
+/* Allocate device state for one lattice (replaces the allocation block of the
+ * reference main, pspectcosmo.cpp:253-282). Validates the configuration. */
+int psc_create(const psc_params *p, psc_handle **out);
+void psc_destroy(psc_handle *h);
+
+/* Initial conditions with the reference's RNG stream and mode order
+ * (initialize.cpp:562-810 and, with GWs, initialize_GW initialize.cpp:341-470).
+ * Generates on the host in FP64, uploads, and computes a'' as
+ * kernel_a_k_nopad / kernel_a (evolution.cpp:1061, 421). */
+int psc_init_ic(psc_handle *h);
+
+/* Replace the state. f_k, pi_k: nflds blocks; u_k, pi_u_k: 6 blocks (components
+ * 00,01,02,11,12,22) or NULL when GWs are off. add < 0 is not special: the value
+ * is taken as given. Equivalent to writing the reference's globals. */
+int psc_set_state(psc_handle *h, const double *f_k, const double *pi_k, double a, double ad, double add,
+                  const double *u_k, const double *pi_u_k);
+int psc_get_state(psc_handle *h, double *f_k, double *pi_k, double *a, double *ad, double *add,
+                  double *u_k, double *pi_u_k);
+int psc_get_time(psc_handle *h, double *t);
+int psc_set_time(psc_handle *h, double t);
+
+/* Advance nsteps steps of size dt: evolve_VV_k_nopad (evolution.cpp:1131-1198)
+ * when spectral = 1, evolve_VV (evolution.cpp:607-694) when spectral = 0. The
+ * step sequence is captured in a CUDA graph. Returns PSC_ERR_NONFINITE if the
+ * background became non-finite (the reference aborts in meansvars/scale,
+ * output.cpp:450-454, 480-483). */
+int psc_step(psc_handle *h, double dt, int nsteps);
+
+/* Real-space fields f, pi_f ([nflds][N^3], what meansvars() reads after its c2r,
+ * output.cpp:396-424). Either pointer may be NULL. */
+int psc_get_fields_real(psc_handle *h, double *f, double *pi_f);
+
+/* Radial-bin spectra of spectra() (output.cpp:490-705, 780-1062). Arrays have
+ * maxnumbins = (int)(sqrt(3) N/2) + 2 entries (parameters.h:25); pass NULL for
+ * any output not needed. numpoints[l] counts modes in bin l (bit-exact integer);
+ * f2/pi2/n2 are the per-bin MEANS the reference computes before printing,
+ * [nflds][maxnumbins]; h2/hdot2 are the GW per-bin means ([maxnumbins]); gw_numpoints
+ * the GW bin counts. */
+int psc_maxnumbins(int N);
+int psc_spectra(psc_handle *h, int32_t *numpoints, double *f2, double *pi2, double *n2, int32_t *gw_numpoints,
+                double *h2, double *hdot2, double *hdot2_zero);
+
+/* Energy components of energy_density() (output.cpp:57-115): per field K and G
+ * ([nflds] each, masked by R_Q2C on the spectral path), per potential term V
+ * ([num_potential_terms]), their total, the Friedmann-constraint violation of
+ * energy() (output.cpp:1178-1185) and the GW energy density rho_GW of spectra()
+ * (output.cpp:1030-1060; 0 without GWs). Any pointer may be NULL. */
+int psc_energies(psc_handle *h, double *K, double *G, double *V, double *total, double *friedmann_violation,
+                 double *rho_gw);
+
+/* meansvars() (output.cpp:380-461): per field <f>, a^(alpha-3)<pi>, <f^2>,
+ * a^(2(alpha-3))<pi^2>, rms(f), a^(alpha-3) rms(pi); out has 6*nflds doubles. */
+int psc_means(psc_handle *h, double *out);
+
+/* Device-time of the last psc_step call (CUDA events on the handle's stream), ms. */
+int psc_last_step_ms(psc_handle *h, float *ms);
+
+const char *psc_strerror(int code);
+const char *psc_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

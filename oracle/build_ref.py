@@ -1,0 +1,136 @@
+"""Build recipe for oracle/_ref: the reference's OWN sources compiled as the CPU oracle.
+
+Test infrastructure only. The reference (JieJiang-Cosmology/PSpectCosmo) is configured
+at compile time through parameters.h and model.h, so each configuration is a separate
+build:
+
+  1. the four reference .cpp files and pspectcosmo.h are copied, unchanged, from the
+     reference checkout into oracle/_ref/<config>/ (git-ignored). They must sit next to
+     the per-config headers because pspectcosmo.h:24 includes "parameters.h" with quotes;
+  2. parameters.h is the reference's own file with the named constants/macros replaced
+     (regex on `const <type> NAME = ...;` and `#define NAME ...`);
+  3. model.h is the reference's own (single-field phi^2) or oracle/models/*.h (the
+     two-field model the benchmark configurations need, written in the same API);
+  4. g++ compiles them against oracle/shim (FFTW/HDF5 API shims over oracle/fft64.c),
+     with pspectcosmo.cpp's main renamed and oracle/ref_harness.cpp as the driver.
+
+Nothing here is run on the GPU machine: the reference checkout exists only where the
+fixtures are generated. Usage: python oracle/build_ref.py [config ...]
+"""
+from __future__ import annotations
+
+import os
+import re
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF = os.environ.get("PSC_REFERENCE_DIR", "/root/reference")
+OUT = os.path.join(HERE, "_ref")
+
+# name -> (model, overrides). Values are C++ source text.
+CONFIGS: dict[str, tuple[str, dict[str, str]]] = {
+    # shipped configuration (parameters.h as is) at N=16 and N=64
+    "spec1_n16": ("phi2", {"N": "16"}),
+    "spec1_n32_vv4": ("phi2", {"N": "32", "VV": "4"}),
+    "spec1_n16_vv6": ("phi2", {"N": "16", "VV": "6"}),
+    "spec1_n64": ("phi2", {}),
+    # two-field preheating (phi0 = 0.193 MPl, phidot0 = -0.142 m MPl, kIR = 1 m)
+    "spec2_n16_vv4": ("phi2chi2", {
+        "N": "16", "VV": "4", "nflds": "2", "kIR": "1",
+        "initfield[]": "{0.193 * MPl, 0.}",
+        "initderivs[]": "{-0.142e-6 * MPl * MPl, 0.}",
+    }),
+    "spec2_n32_vv2": ("phi2chi2", {
+        "N": "32", "VV": "2", "nflds": "2", "kIR": "1",
+        "initfield[]": "{0.193 * MPl, 0.}",
+        "initderivs[]": "{-0.142e-6 * MPl * MPl, 0.}",
+    }),
+    # real-space pseudo-spectral path with gravitational waves (evolve_VV)
+    "gw2_n16_vv4": ("phi2chi2", {
+        "N": "16", "VV": "4", "nflds": "2", "kIR": "1",
+        "SPECTRAL_FLAG": "false", "WITH_GW": "true",
+        "initfield[]": "{0.193 * MPl, 0.}",
+        "initderivs[]": "{-0.142e-6 * MPl * MPl, 0.}",
+    }),
+    "gw1_n16_vv2": ("phi2", {
+        "N": "16", "VV": "2", "SPECTRAL_FLAG": "false", "WITH_GW": "true",
+    }),
+}
+
+MACROS = {"VV", "SPECTRAL_FLAG", "PAD_FLAG", "WITH_GW", "SIMULATE_INFLATION", "SNAPSHOTS_ENERGY",
+          "BIFURCATION", "ANALYTIC_EVOLUTION"}
+
+SOURCES = ["pspectcosmo.cpp", "initialize.cpp", "evolution.cpp", "output.cpp"]
+
+
+def make_parameters(text: str, overrides: dict[str, str]) -> str:
+    for name, value in overrides.items():
+        if name in MACROS:
+            pat = re.compile(r"^(#define\s+%s\s+)\S+" % re.escape(name), re.M)
+            text, n = pat.subn(lambda m: m.group(1) + value, text)
+        else:
+            pat = re.compile(r"^(const\s+[\w:]+\s+%s\s*=\s*)[^;]*;" % re.escape(name), re.M)
+            text, n = pat.subn(lambda m: m.group(1) + value + ";", text)
+        if n != 1:
+            raise SystemExit(f"parameters.h: could not override {name!r} ({n} matches)")
+    return text
+
+
+def build(name: str) -> str:
+    model, overrides = CONFIGS[name]
+    d = os.path.join(OUT, name)
+    os.makedirs(d, exist_ok=True)
+    for s in SOURCES + ["pspectcosmo.h"]:
+        shutil.copyfile(os.path.join(REF, s), os.path.join(d, s))
+    with open(os.path.join(REF, "parameters.h")) as fh:
+        params = make_parameters(fh.read(), overrides)
+    with open(os.path.join(d, "parameters.h"), "w") as fh:
+        fh.write(params)
+    if model == "phi2":
+        shutil.copyfile(os.path.join(REF, "model.h"), os.path.join(d, "model.h"))
+    else:
+        shutil.copyfile(os.path.join(HERE, "models", f"model_{model}.h"), os.path.join(d, "model.h"))
+
+    shim = os.path.join(HERE, "shim")
+    cxx = ["g++", "-O2", "-std=c++17", "-fopenmp", "-w", "-I", d, "-I", shim,
+           "-include", os.path.join(shim, "prec_override.h")]
+    objs = []
+    jobs = []
+    for s in SOURCES:
+        extra = ["-Dmain=reference_main"] if s == "pspectcosmo.cpp" else []
+        o = os.path.join(d, s.replace(".cpp", ".o"))
+        jobs.append(cxx + extra + ["-c", os.path.join(d, s), "-o", o])
+        objs.append(o)
+    o = os.path.join(d, "ref_harness.o")
+    jobs.append(cxx + ["-c", os.path.join(HERE, "ref_harness.cpp"), "-o", o])
+    objs.append(o)
+    for src in (os.path.join(shim, "shim_fftw.c"), os.path.join(HERE, "fft64.c")):
+        o = os.path.join(d, os.path.basename(src).replace(".c", ".o"))
+        jobs.append(["gcc", "-O2", "-std=c11", "-fopenmp", "-I", shim, "-c", src, "-o", o])
+        objs.append(o)
+    with ThreadPoolExecutor(max_workers=os.cpu_count()) as ex:
+        for r in ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), jobs):
+            if r.returncode != 0:
+                raise SystemExit(f"compile failed:\n{' '.join(r.args)}\n{r.stderr}")
+    exe = os.path.join(d, "harness")
+    r = subprocess.run(["g++", "-fopenmp", "-o", exe] + objs + ["-lm", "-lpthread"], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise SystemExit(f"link failed:\n{r.stderr}")
+    return exe
+
+
+def main(argv: list[str]) -> None:
+    if not os.path.isdir(REF):
+        print(f"reference checkout not found at {REF}; nothing to build")
+        return
+    names = argv or list(CONFIGS)
+    with ThreadPoolExecutor(max_workers=4) as ex:
+        for exe in ex.map(build, names):
+            print(exe)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])

@@ -1,0 +1,142 @@
+/*
+ * Harness main for the oracle build of the reference's own sources
+ * (test infrastructure only; compiled by oracle/build_ref.py into oracle/_ref/).
+ *
+ * It replaces the reference's main() (pspectcosmo.cpp:236-742, compiled here as
+ * reference_main and never called) with a fixed-dt driver:
+ *   - replicates the allocation block (pspectcosmo.cpp:253-282) and a = a0, t = 0
+ *     (pspectcosmo.cpp:295-300);
+ *   - calls initialize() (initialize.cpp:562) and, with GWs, initialize_GW()
+ *     (initialize.cpp:341), then save() (output.cpp:1796) as main does
+ *     (pspectcosmo.cpp:489-545);
+ *   - steps evolve_VV_k_nopad(dt) (evolution.cpp:1131) or evolve_VV(dt)
+ *     (evolution.cpp:607) with the FIXED dt given on the command line instead of
+ *     the adaptive calculate_dt (pspectcosmo.cpp:213-233);
+ *   - every `every` steps calls save_Freq() and save_Infreq() (output.cpp:1831,
+ *     1842) and dumps the raw state.
+ * Everything runs on a thread with a 2 GiB stack, because the real-space path
+ * keeps N^3 arrays on the stack (evolution.cpp:612, 441, 581).
+ *
+ * usage: harness NSTEPS DT EVERY      (run inside the output directory)
+ * writes: output/*.txt (reference writers, 17 digits), state_<step>.bin, bg.txt,
+ *         ic_info.txt
+ */
+#include "pspectcosmo.h"
+
+#include <pthread.h>
+#include <cstdio>
+#include <cstdlib>
+
+static long g_nsteps = 0, g_every = 1;
+static double g_dt = 0.0;
+
+static void dump_state(long step) {
+    char name[64];
+    std::snprintf(name, sizeof name, "state_%06ld.bin", step);
+    std::FILE *fp = std::fopen(name, "wb");
+    if (!fp) { std::perror(name); std::exit(3); }
+    int hdr[6] = {0x44435350 /* 'PSCD' */, 1, N, nflds, (int)SPECTRAL_FLAG, (int)WITH_GW};
+    std::fwrite(hdr, sizeof(int), 6, fp);
+    double bg[4] = {t, a, ad, add};
+    std::fwrite(bg, sizeof(double), 4, fp);
+    const size_t modes = (size_t)N * N * (N / 2 + 1);
+    const size_t sites = (size_t)N * N * N;
+    for (int fld = 0; fld < nflds; fld++) std::fwrite(f_k[fld], sizeof(fftw_complex), modes, fp);
+    for (int fld = 0; fld < nflds; fld++) std::fwrite(pi_k[fld], sizeof(fftw_complex), modes, fp);
+    std::fwrite(&f[0][0][0][0], sizeof(double), sites * nflds, fp);
+    std::fwrite(&pi_f[0][0][0][0], sizeof(double), sites * nflds, fp);
+#if WITH_GW
+    std::fwrite(&u[0][0][0][0][0], sizeof(double), sites * 9, fp);
+    std::fwrite(&pi_u[0][0][0][0][0], sizeof(double), sites * 9, fp);
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) std::fwrite(u_k[i][j], sizeof(fftw_complex), modes, fp);
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) std::fwrite(pi_u_k[i][j], sizeof(fftw_complex), modes, fp);
+#endif
+    std::fclose(fp);
+}
+
+static void step_once(double dt_) {
+#if SPECTRAL_FLAG
+    evolve_VV_k_nopad(dt_);
+#else
+    evolve_VV(dt_);
+#endif
+}
+
+static void *run(void *) {
+    checkdirectory();
+    fftw_init_threads();
+    fftw_plan_with_nthreads(n_threads);
+
+    const size_t modes = (size_t)N * N * (N / 2 + 1);
+    Cache_Data_k = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes);
+    R_k = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes);
+    for (int fld = 0; fld < nflds; fld++) {
+        f_k[fld] = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes);
+        pi_k[fld] = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes);
+#if SPECTRAL_FLAG
+        pi_k_half[fld] = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes);
+        V_prime_k[fld] = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes);
+        kernel_f_k[fld] = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes);
+#endif
+    }
+#if WITH_GW
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            u_k[i][j] = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes);
+            pi_u_k[i][j] = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes);
+        }
+#endif
+    dt = g_dt;
+    t0 = 0.;
+    t = t0;
+    a = a0;
+
+    initialize();
+    {
+        std::FILE *fp = std::fopen("ic_info.txt", "w");
+        std::fprintf(fp, "hubble_init %.17g\na %.17g\nad %.17g\nadd %.17g\n", hubble_init, a, ad, add);
+        std::fclose(fp);
+    }
+#if WITH_GW
+    initialize_GW();
+#endif
+    dump_state(0);
+    save();
+
+    std::FILE *bgf = std::fopen("bg.txt", "w");
+    std::fprintf(bgf, "%ld %.17g %.17g %.17g %.17g\n", 0L, t, a, ad, add);
+    for (long s = 1; s <= g_nsteps; s++) {
+        step_once(g_dt);
+        std::fprintf(bgf, "%ld %.17g %.17g %.17g %.17g\n", s, t, a, ad, add);
+        if (s % g_every == 0) {
+            save_Freq();
+            save_Infreq();
+            dump_state(s);
+        }
+    }
+    std::fclose(bgf);
+    return nullptr;
+}
+
+int main(int argc, char **argv) {
+    if (argc < 4) {
+        std::fprintf(stderr, "usage: %s NSTEPS DT EVERY\n", argv[0]);
+        return 2;
+    }
+    g_nsteps = std::atol(argv[1]);
+    g_dt = std::atof(argv[2]);
+    g_every = std::atol(argv[3]);
+    if (g_every < 1) g_every = 1;
+    pthread_attr_t attr;
+    pthread_attr_init(&attr);
+    pthread_attr_setstacksize(&attr, (size_t)2 << 30);
+    pthread_t th;
+    if (pthread_create(&th, &attr, run, nullptr) != 0) {
+        std::fprintf(stderr, "cannot start worker thread\n");
+        return 3;
+    }
+    pthread_join(th, nullptr);
+    return 0;
+}
