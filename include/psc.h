@@ -89,6 +89,13 @@ void psc_destroy(psc_handle *h);
  * kernel_a_k_nopad / kernel_a (evolution.cpp:1061, 421). */
 int psc_init_ic(psc_handle *h);
 
+/* Host-only initial conditions: fills f_k, pi_k (nflds blocks) and, with GWs,
+ * u_k, pi_u_k (6 blocks) exactly as initialize() / initialize_GW() do
+ * (initialize.cpp:562-810, 341-470), without touching a GPU. info (may be NULL)
+ * receives {hubble_init, a, ad, printed a'', kinetic, potential}
+ * (initialize.cpp:649-670). Buffers are overwritten entirely. */
+int psc_generate_ic(const psc_params *p, double *f_k, double *pi_k, double *u_k, double *pi_u_k, double *info);
+
 /* Replace the state. f_k, pi_k: nflds blocks; u_k, pi_u_k: 6 blocks (components
  * 00,01,02,11,12,22) or NULL when GWs are off. add < 0 is not special: the value
  * is taken as given. Equivalent to writing the reference's globals. */

@@ -1,0 +1,72 @@
+"""Build libpsc.so (the CUDA path and its C ABI) in-tree for sm_103a.
+
+Three translation units compiled in parallel with nvcc (the IC generator with the host
+compiler through nvcc), linked into pspectcosmo_gb300/libpsc.so. Rebuilds only when a
+source is newer than the library.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+ROOT = os.path.dirname(HERE)
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libpsc.so")
+SOURCES = ["psc_kernels.cu", "psc_api.cu", "psc_ic.cpp"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _deps():
+    files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(ROOT, "include", "psc.h")]
+    return [f for f in files if os.path.isfile(f)]
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    newest = max(os.path.getmtime(f) for f in _deps() + [os.path.abspath(__file__)])
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    cc = nvcc()
+    common = ["-std=c++17", "-O3", "-Xcompiler", "-fPIC", "-I", CSRC, "-I", os.path.join(ROOT, "include")]
+    jobs = []
+    objs = []
+    for src in SOURCES:
+        obj = os.path.join(BUILD, src + ".o")
+        objs.append(obj)
+        path = os.path.join(CSRC, src)
+        if src.endswith(".cu"):
+            cmd = [cc] + ARCH + common + ["-lineinfo", "-Xptxas", "-O3", "-c", path, "-o", obj]
+            if verbose:
+                cmd += ["-Xptxas", "-v"]
+        else:
+            cmd = [cc] + common + ["-x", "c++", "-c", path, "-o", obj]
+        jobs.append(cmd)
+    with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        results = list(ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), jobs))
+    for r in results:
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed:\n{' '.join(r.args)}\n{r.stdout}\n{r.stderr}")
+        if verbose and r.stderr:
+            sys.stderr.write(r.stderr)
+    tmp = LIB + ".tmp"
+    r = subprocess.run([cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

@@ -1,0 +1,31 @@
+// psc_bg.h — the FP64 background record shared by host and device code.
+#pragma once
+
+namespace psc {
+
+constexpr int kMaxStages = 31;   // Yoshida-10 (pspectcosmo.h:295-297)
+constexpr int kMaxFields = 2;
+constexpr int kMaxTerms = 2;
+
+// FP64 background and per-stage coefficients, resident in device memory so a
+// captured step graph needs no host values. Mirrors the reference globals
+// a, ad, add, t (pspectcosmo.cpp:155-156) and the locals b, b_half, a_half of
+// evolve_VV_k_nopad (evolution.cpp:1131-1198).
+struct DevBG {
+    double a, ad, add, t;           // state at step boundaries
+    double b, b_half;               // within a step (b = a' during the stages)
+    double ad_stale;                // ad at the start of the step: the R_Q2C mask reads the stale global ad
+    double dt;
+    double c_drift;                 // w dt a_half^(alpha-3)            (evolution.cpp:1164-1168)
+    double c_close, c_open;         // closing / next opening half kick  (evolution.cpp:1153-1158, 1184-1189)
+    double norm1, norm2;            // a^(1+alpha), a^(3+alpha)          (evolution.cpp:1099-1100)
+    double hub, apow, a3;           // ad_stale/a, a^(alpha-3), a^(3-alpha) for R_Q2C (evolution.cpp:1047)
+    double K[kMaxFields], G[kMaxFields], V[kMaxTerms];   // last reductions (kinetic, gradient, potential)
+    double w[kMaxStages];
+    // run constants
+    double kIR, kIR2, DFDP, eps, fs_over_mpl2, gsq, inv_n3, inv_n3sq;
+    int s, alpha, nf, nterms, mask, model, nbx, nbz;
+    int stage, steps_left, err, pad;
+};
+
+}  // namespace psc

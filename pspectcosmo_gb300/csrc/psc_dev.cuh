@@ -1,0 +1,221 @@
+// psc_dev.cuh — device-side building blocks of the GB300 lattice step:
+// complex types, the background record, the model, and the shared-memory
+// Stockham FFT engine used by every pass kernel.
+//
+// Layout conventions (match the reference's FFTW arrays, pspectcosmo.h:179-190):
+//   half spectrum  [x][y][kz], kz in [0, N/2], kz fastest, H = N/2 + 1
+//   real lattice   [x][y][z],  z fastest
+// Transforms are unnormalised like FFTW's; the 1/N^3 of every c2r
+// (evolution.cpp:1150, 1176) is applied in the Z-pass epilogue.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "psc_bg.h"
+
+namespace psc {
+
+// ------------------------------------------------------------------ types
+template <typename T> struct CplxOf;
+template <> struct CplxOf<float> { using type = float2; };
+template <> struct CplxOf<double> { using type = double2; };
+template <typename T> using cplx = typename CplxOf<T>::type;
+
+template <typename T> __device__ __forceinline__ cplx<T> mk(T re, T im) { cplx<T> c; c.x = re; c.y = im; return c; }
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { a.x += b.x; a.y += b.y; return a; }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { a.x -= b.x; a.y -= b.y; return a; }
+template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+    C r;
+    r.x = a.x * b.x - a.y * b.y;
+    r.y = a.x * b.y + a.y * b.x;
+    return r;
+}
+template <typename C, typename T> __device__ __forceinline__ C cscale(C a, T s) { a.x *= s; a.y *= s; return a; }
+template <typename C> __device__ __forceinline__ C cconj(C a) { a.y = -a.y; return a; }
+
+
+// ------------------------------------------------------------------ model (model.h)
+// Device mirror of model.h: V, dV/dphi for the shipped phi^2 model
+// (model.h:35-82) and the two-field phi^2 chi^2 model written in the same API.
+struct Model {
+    int kind;   // 0 = phi^2, 1 = phi^2 chi^2
+    double gsq;
+};
+
+template <typename T>
+__device__ __forceinline__ void model_dvdf(const Model &m, const T *v, T *out, int nf) {
+    if (m.kind == 0) {
+        out[0] = v[0];
+    } else {
+        const T g = (T)m.gsq;
+        out[0] = v[0] + g * v[0] * (v[1] * v[1]);
+        if (nf > 1) out[1] = g * (v[0] * v[0]) * v[1];
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void model_potential(const Model &m, const T *v, double *terms) {
+    const double p = (double)v[0];
+    terms[0] += 0.5 * p * p;
+    if (m.kind == 1) {
+        const double c = (double)v[1];
+        terms[1] += 0.5 * m.gsq * p * p * c * c;
+    }
+}
+
+// ------------------------------------------------------------------ FFT engine
+// cos/sin(2 pi k / 16): exact decimal expansions of the algebraic values.
+__host__ __device__ constexpr double cos16(int k) {
+    switch (k & 15) {
+    case 0: return 1.0;
+    case 1: return 0.92387953251128675613;
+    case 2: return 0.70710678118654752440;
+    case 3: return 0.38268343236508977173;
+    case 4: return 0.0;
+    case 5: return -0.38268343236508977173;
+    case 6: return -0.70710678118654752440;
+    case 7: return -0.92387953251128675613;
+    case 8: return -1.0;
+    case 9: return -0.92387953251128675613;
+    case 10: return -0.70710678118654752440;
+    case 11: return -0.38268343236508977173;
+    case 12: return 0.0;
+    case 13: return 0.38268343236508977173;
+    case 14: return 0.70710678118654752440;
+    default: return 0.92387953251128675613;
+    }
+}
+__host__ __device__ constexpr double sin16(int k) { return cos16(k - 4); }
+
+template <int R> __host__ __device__ constexpr int brev(int i) {
+    int r = 0;
+    for (int b = 1, m = R >> 1; b < R; b <<= 1, m >>= 1)
+        if (i & b) r |= m;
+    return r;
+}
+
+// In-register R-point DFT (R = 2, 4, 8, 16), direction DIR = -1 (forward,
+// e^{-2 pi i}) or +1 (backward): bit reversal + radix-2 butterflies with
+// compile-time twiddles.
+template <int R, int DIR, typename C>
+__device__ __forceinline__ void dft(C (&v)[R]) {
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+        const int j = brev<R>(i);
+        if (i < j) { C t = v[i]; v[i] = v[j]; v[j] = t; }
+    }
+#pragma unroll
+    for (int len = 2; len <= R; len <<= 1) {
+#pragma unroll
+        for (int i = 0; i < R; i += len) {
+#pragma unroll
+            for (int k = 0; k < len / 2; ++k) {
+                const int ti = k * (16 / len);
+                C u = v[i + k], x = v[i + k + len / 2], t;
+                if (ti == 0) {
+                    t = x;
+                } else if (ti == 4) {
+                    if (DIR < 0) { t.x = x.y; t.y = -x.x; } else { t.x = -x.y; t.y = x.x; }
+                } else {
+                    using T = decltype(x.x);
+                    const T c = (T)cos16(ti), s = (T)(DIR * sin16(ti));
+                    t.x = x.x * c - x.y * s;
+                    t.y = x.x * s + x.y * c;
+                }
+                v[i + k] = cadd(u, t);
+                v[i + k + len / 2] = csub(u, t);
+            }
+        }
+    }
+}
+
+// One Stockham autosort stage (radix R, span Ns) over a tile of TL lines of
+// length L held in shared memory as s[n * LD + t] (element n of line t).
+// Twiddles come from tw[q] = e^{-2 pi i q / Ntw}, the table of the lattice
+// length; a length-L transform uses every (Ntw/L)-th entry.
+template <typename C, int R, int DIR>
+__device__ __forceinline__ void stockham_stage(const C *__restrict__ src, C *__restrict__ dst, int L, int Ns, int tl_shift,
+                                               int LD, const C *__restrict__ tw, int Ntw) {
+    const int LR = L / R;
+    const int TL = 1 << tl_shift;
+    const int nb = LR << tl_shift;
+    const int tws = Ntw / (Ns * R);
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+        const int t = b & (TL - 1);
+        const int j = b >> tl_shift;
+        const int jm = j & (Ns - 1);
+        C v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[r] = src[(j + r * LR) * LD + t];
+        if (Ns > 1) {
+#pragma unroll
+            for (int r = 1; r < R; ++r) {
+                C w = __ldg(&tw[jm * r * tws]);
+                if (DIR > 0) w.y = -w.y;
+                v[r] = cmul(v[r], w);
+            }
+        }
+        dft<R, DIR>(v);
+        const int idxD = (j - jm) * R + jm;
+#pragma unroll
+        for (int r = 0; r < R; ++r) dst[(idxD + r * Ns) * LD + t] = v[r];
+    }
+}
+
+// Transform all TL lines of a tile (length L, power of two >= 2). Ping-pongs
+// between a and b; returns the buffer holding the result. Begins and ends
+// with a block barrier.
+template <typename C, int DIR>
+__device__ C *fft_tile(C *a, C *b, int L, int tl_shift, int LD, const C *__restrict__ tw, int Ntw) {
+    C *src = a, *dst = b;
+    int Ns = 1, rem = L;
+    while (rem > 1) {
+        __syncthreads();
+        if (rem >= 16) {
+            stockham_stage<C, 16, DIR>(src, dst, L, Ns, tl_shift, LD, tw, Ntw);
+            Ns *= 16; rem >>= 4;
+        } else if (rem == 8) {
+            stockham_stage<C, 8, DIR>(src, dst, L, Ns, tl_shift, LD, tw, Ntw);
+            Ns *= 8; rem >>= 3;
+        } else if (rem == 4) {
+            stockham_stage<C, 4, DIR>(src, dst, L, Ns, tl_shift, LD, tw, Ntw);
+            Ns *= 4; rem >>= 2;
+        } else {
+            stockham_stage<C, 2, DIR>(src, dst, L, Ns, tl_shift, LD, tw, Ntw);
+            Ns *= 2; rem >>= 1;
+        }
+        C *x = src; src = dst; dst = x;
+    }
+    __syncthreads();
+    return src;
+}
+
+// ------------------------------------------------------------------ reductions
+// Block reduction of NV doubles; thread 0 stores out[i * stride + blockIdx.x].
+// Deterministic for a fixed block size.
+template <int NV>
+__device__ __forceinline__ void block_reduce_store(double (&v)[NV], double *out, int stride, int slot) {
+    __shared__ double red[32][NV > 0 ? NV : 1];
+#pragma unroll
+    for (int i = 0; i < NV; ++i)
+        for (int off = 16; off > 0; off >>= 1) v[i] += __shfl_down_sync(0xffffffffu, v[i], off);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int i = 0; i < NV; ++i) red[warp][i] = v[i];
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            double x = lane < nw ? red[lane][i] : 0.0;
+            for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+            if (lane == 0) out[i * stride + slot] = x;
+        }
+    }
+}
+
+__device__ __forceinline__ int pcoord(int i, int N) { return i <= (N >> 1) ? i : i - N; }
+
+}  // namespace psc

@@ -1,0 +1,841 @@
+// psc_kernels.cu — the sm_103a kernels of one pseudo-spectral stage.
+//
+// A stage of evolve_VV_k_nopad (evolution.cpp:1131-1198) / evolve_VV
+// (evolution.cpp:607-694) is one force evaluation here, because the closing
+// half kick of a stage and the opening half kick of the next use the same
+// force (same f and a): the two kicks are applied together in the epilogue of
+// the last pass. Per stage and per field (GW terms in brackets):
+//
+//   k_ifft_x   X-axis inverse pass over f_k; prologue: the drift
+//              f_k += w dt a_half^(alpha-3) pi_half (evolution.cpp:1164-1168);
+//              [also i k_x f_k for the x-derivative (evolution.cpp:484-497)]
+//   k_ifft_y   Y-axis inverse pass [+ i k_y for the y-derivative]
+//   k_zpass    per (x,y) line: c2r along z and 1/N^3 (evolution.cpp:1171-1176)
+//              [+ i k_z for the z-derivative], then pointwise V'(phi, chi)
+//              (evolution.cpp:1103-1109) and <V> (evolution.cpp:1077-1085)
+//              [and S_ab = 2 sum_f d_a f d_b f (evolution.cpp:592-597)], then
+//              r2c along z of every product
+//   k_fft_y    Y-axis forward pass of V' [and S_ab]
+//   k_fft_x_final  X-axis forward pass, then the force
+//              -a^(1+alpha) kIR^2 k^2 f_k - a^(3+alpha) V'_k (evolution.cpp:1115-1127),
+//              the kicks, the masked K and G sums (evolution.cpp:923-1056)
+//              [and for u_ij: the deferred drift, the force a^(1+alpha)(-k^2 u + S)
+//              and the kicks (evolution.cpp:581-601, 635-684)]
+//   k_scalar   one block: reductions -> a'' (evolution.cpp:1087) -> b, and the
+//              next stage's coefficients (evolution.cpp:1141, 1161, 1180, 1193)
+//
+// All passes stage a tile of lines in shared memory and run a Stockham FFT
+// there (psc_dev.cuh), so each pass is one read and one write of its arrays.
+#include "psc_dev.cuh"
+#include "psc_launch.h"
+
+namespace psc {
+
+// ------------------------------------------------------------------ X pass (inverse)
+template <typename T, bool GW, bool DRIFT>
+__global__ void __launch_bounds__(256) k_ifft_x(Geo g, cplx<T> *__restrict__ fk, const cplx<T> *__restrict__ pk,
+                                                cplx<T> *__restrict__ TA, cplx<T> *__restrict__ TB,
+                                                const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw) {
+    using C = cplx<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int sh = g.tlx_shift, TL = 1 << sh, N = g.N;
+    C *b0 = reinterpret_cast<C *>(smem_raw);
+    C *b1 = b0 + TL * N;
+    const long long off = (long long)blockIdx.y * g.modes;
+    const int line0 = blockIdx.x * TL;
+    const long long stride = g.lines_x;
+    const T c = DRIFT ? (T)bg->c_drift : T(0);
+    const int total = TL * N;
+    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+        const int t = idx & (TL - 1), n = idx >> sh, line = line0 + t;
+        C v = mk<T>(0, 0);
+        if (line < g.lines_x) {
+            const long long a = off + n * stride + line;
+            v = fk[a];
+            if (DRIFT) {
+                const C p = pk[a];
+                v.x += c * p.x;
+                v.y += c * p.y;
+                fk[a] = v;
+            }
+        }
+        b0[idx] = v;
+    }
+    C *r = fft_tile<C, +1>(b0, b1, N, sh, TL, tw, N);
+    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+        const int t = idx & (TL - 1), n = idx >> sh, line = line0 + t;
+        if (line < g.lines_x) TA[off + n * stride + line] = r[idx];
+    }
+    if (GW) {
+        __syncthreads();
+        const T kIR = (T)bg->kIR;
+        for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+            const int t = idx & (TL - 1), n = idx >> sh, line = line0 + t;
+            C v = mk<T>(0, 0);
+            if (line < g.lines_x) {
+                const C f = fk[off + n * stride + line];
+                const T kx = (n == (N >> 1)) ? T(0) : kIR * (T)pcoord(n, N);
+                v = mk<T>(-kx * f.y, kx * f.x);
+            }
+            b0[idx] = v;
+        }
+        r = fft_tile<C, +1>(b0, b1, N, sh, TL, tw, N);
+        for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+            const int t = idx & (TL - 1), n = idx >> sh, line = line0 + t;
+            if (line < g.lines_x) TB[off + n * stride + line] = r[idx];
+        }
+    }
+}
+
+// ------------------------------------------------------------------ Y pass helpers
+// Line l = x * H + kz of the Y pass; element y at (x N + y) H + kz.
+__device__ __forceinline__ long long yaddr(const Geo &g, int line, int y) {
+    const int x = line / g.H, kz = line - x * g.H;
+    return ((long long)x * g.N + y) * g.H + kz;
+}
+
+// One Y-axis transform of a tile: src -> dst (may alias), optional i k_y multiplier.
+template <typename T, int DIR>
+__device__ __forceinline__ void ypass_tile(const Geo &g, const cplx<T> *src, cplx<T> *dst, bool deriv, T kIR,
+                                           cplx<T> *b0, cplx<T> *b1, const cplx<T> *__restrict__ tw) {
+    using C = cplx<T>;
+    const int sh = g.tlx_shift, TL = 1 << sh, N = g.N, total = TL * N;
+    const int line0 = blockIdx.x * TL;
+    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+        const int t = idx & (TL - 1), n = idx >> sh, line = line0 + t;
+        C v = mk<T>(0, 0);
+        if (line < g.lines_x) {
+            v = src[yaddr(g, line, n)];
+            if (deriv) {
+                const T ky = (n == (N >> 1)) ? T(0) : kIR * (T)pcoord(n, N);
+                v = mk<T>(-ky * v.y, ky * v.x);
+            }
+        }
+        b0[idx] = v;
+    }
+    C *r = fft_tile<C, DIR>(b0, b1, N, sh, TL, tw, N);
+    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+        const int t = idx & (TL - 1), n = idx >> sh, line = line0 + t;
+        if (line < g.lines_x) dst[yaddr(g, line, n)] = r[idx];
+    }
+    __syncthreads();
+}
+
+template <typename T, bool GW>
+__global__ void __launch_bounds__(256) k_ifft_y(Geo g, cplx<T> *__restrict__ TA, cplx<T> *__restrict__ TB,
+                                                cplx<T> *__restrict__ TC, const DevBG *__restrict__ bg,
+                                                const cplx<T> *__restrict__ tw) {
+    using C = cplx<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int TL = 1 << g.tlx_shift;
+    C *b0 = reinterpret_cast<C *>(smem_raw);
+    C *b1 = b0 + TL * g.N;
+    const long long off = (long long)blockIdx.y * g.modes;
+    const T kIR = (T)bg->kIR;
+    if (GW) {
+        // the y-derivative reads TA before TA is transformed in place
+        ypass_tile<T, +1>(g, TA + off, TC + off, true, kIR, b0, b1, tw);
+        ypass_tile<T, +1>(g, TA + off, TA + off, false, kIR, b0, b1, tw);
+        ypass_tile<T, +1>(g, TB + off, TB + off, false, kIR, b0, b1, tw);
+    } else {
+        ypass_tile<T, +1>(g, TA + off, TA + off, false, kIR, b0, b1, tw);
+    }
+}
+
+// Forward Y pass in place over a list of arrays (blockIdx.y selects the array).
+struct ArrList {
+    void *p[8];
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_fft_y(Geo g, ArrList arrs, const cplx<T> *__restrict__ tw) {
+    using C = cplx<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int TL = 1 << g.tlx_shift;
+    C *b0 = reinterpret_cast<C *>(smem_raw);
+    C *b1 = b0 + TL * g.N;
+    C *a = reinterpret_cast<C *>(arrs.p[blockIdx.y]);
+    ypass_tile<T, -1>(g, a, a, false, T(0), b0, b1, tw);
+}
+
+// ------------------------------------------------------------------ fused Z pass
+// Shared memory: b0, b1 (H rows x ldz) and nslot real-line slots (M rows x ldz,
+// a complex element holding the two real sites 2m and 2m+1).
+template <typename T, bool GW>
+__global__ void __launch_bounds__(256) k_zpass(Geo g, const cplx<T> *__restrict__ TA, const cplx<T> *__restrict__ TB,
+                                               const cplx<T> *__restrict__ TC, cplx<T> *__restrict__ QV,
+                                               cplx<T> *__restrict__ QS, double *__restrict__ partV,
+                                               const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw) {
+    using C = cplx<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int sh = g.tlz_shift, TL = 1 << sh, LD = g.ldz, H = g.H, M = g.M, N = g.N;
+    C *b0 = reinterpret_cast<C *>(smem_raw);
+    C *b1 = b0 + H * LD;
+    C *slots = b1 + H * LD;
+    const int line0 = blockIdx.x * TL;
+    const int nf = g.nf;
+    const int nin = nf * (GW ? 4 : 1);
+    const int nout = nf + (GW ? 6 : 0);
+    const T inv_n3 = (T)bg->inv_n3;
+    const T kIR = (T)bg->kIR;
+
+    // 1. complex-to-real along z of every input line
+    for (int o = 0; o < nin; ++o) {
+        const int fld = GW ? (o >> 2) : o;
+        const int kind = GW ? (o & 3) : 0;   // 0: f, 1: d/dx f, 2: d/dy f, 3: d/dz f
+        const C *src = (kind == 1 ? TB : (kind == 2 ? TC : TA)) + (long long)fld * g.modes;
+        for (int idx = threadIdx.x; idx < TL * H; idx += blockDim.x) {
+            const int t = idx / H, k = idx - t * H, line = line0 + t;
+            C v = mk<T>(0, 0);
+            if (line < g.lines_z) {
+                v = src[(long long)line * H + k];
+                if (kind == 3) {
+                    const T kz = (k < M) ? kIR * (T)k : T(0);
+                    v = mk<T>(-kz * v.y, kz * v.x);
+                }
+            }
+            b1[k * LD + t] = v;
+        }
+        __syncthreads();
+        // pack the half spectrum into an M-point complex transform:
+        // Z[k] = (X[k] + conj X[M-k]) + i w^k (X[k] - conj X[M-k]), w = e^{+2 pi i/N};
+        // Im X[0] and Im X[M] are ignored, as a c2r transform does.
+        for (int idx = threadIdx.x; idx < TL * M; idx += blockDim.x) {
+            const int t = idx & (TL - 1), k = idx >> sh;
+            C x = b1[k * LD + t], y = cconj(b1[(M - k) * LD + t]);
+            if (k == 0) { x.y = T(0); y.y = T(0); }
+            const C s = cadd(x, y), d = csub(x, y);
+            C w = __ldg(&tw[k]);
+            w.y = -w.y;
+            const C td = cmul(w, d);
+            b0[k * LD + t] = mk<T>(s.x - td.y, s.y + td.x);
+        }
+        C *r = fft_tile<C, +1>(b0, b1, M, sh, LD, tw, N);
+        C *so = slots + (size_t)o * M * LD;
+        for (int idx = threadIdx.x; idx < TL * M; idx += blockDim.x) {
+            const int t = idx & (TL - 1), k = idx >> sh;
+            so[k * LD + t] = cscale(r[k * LD + t], inv_n3);
+        }
+        __syncthreads();
+    }
+
+    // 2. pointwise epilogue: V'(f), <V>, anisotropic stress
+    Model mdl;
+    mdl.kind = g.model;
+    mdl.gsq = g.gsq;
+    double pot[kMaxTerms] = {0.0, 0.0};
+    for (int idx = threadIdx.x; idx < TL * M; idx += blockDim.x) {
+        const int t = idx & (TL - 1), k = idx >> sh;
+        if (line0 + t >= g.lines_z) continue;
+        const int e = k * LD + t;
+        C in[8];
+#pragma unroll
+        for (int o = 0; o < 8; ++o)
+            if (o < nin) in[o] = slots[(size_t)o * M * LD + e];
+        C out[8];
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            T f[2], vp[2];
+#pragma unroll
+            for (int fl = 0; fl < 2; ++fl) {
+                if (fl < nf) {
+                    const C c = in[GW ? fl * 4 : fl];
+                    f[fl] = half ? c.y : c.x;
+                } else {
+                    f[fl] = T(0);
+                }
+            }
+            model_dvdf<T>(mdl, f, vp, nf);
+            model_potential<T>(mdl, f, pot);
+#pragma unroll
+            for (int fl = 0; fl < 2; ++fl)
+                if (fl < nf) { if (half) out[fl].y = vp[fl]; else out[fl].x = vp[fl]; }
+            if (GW) {
+                T d[2][3];
+#pragma unroll
+                for (int fl = 0; fl < 2; ++fl)
+#pragma unroll
+                    for (int ax = 0; ax < 3; ++ax)
+                        d[fl][ax] = (fl < nf) ? (half ? in[fl * 4 + 1 + ax].y : in[fl * 4 + 1 + ax].x) : T(0);
+                const int si[6] = {0, 0, 0, 1, 1, 2}, sj[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+                for (int c = 0; c < 6; ++c) {
+                    T sum = T(0);
+#pragma unroll
+                    for (int fl = 0; fl < 2; ++fl)
+                        if (fl < nf) sum += T(2) * d[fl][si[c]] * d[fl][sj[c]];
+                    if (half) out[nf + c].y = sum; else out[nf + c].x = sum;
+                }
+            }
+        }
+#pragma unroll
+        for (int o = 0; o < 8; ++o)
+            if (o < nout) slots[(size_t)o * M * LD + e] = out[o];
+    }
+    block_reduce_store<kMaxTerms>(pot, partV, gridDim.x, blockIdx.x);
+    __syncthreads();
+
+    // 3. real-to-complex along z of every product
+    for (int o = 0; o < nout; ++o) {
+        C *so = slots + (size_t)o * M * LD;
+        C *r = fft_tile<C, -1>(so, b0, M, sh, LD, tw, N);
+        C *dst = (o < nf) ? QV + (long long)o * g.modes : QS + (long long)(o - nf) * g.modes;
+        for (int idx = threadIdx.x; idx < TL * H; idx += blockDim.x) {
+            const int t = idx / H, k = idx - t * H, line = line0 + t;
+            if (line >= g.lines_z) continue;
+            const C zk = r[(k == M ? 0 : k) * LD + t];
+            const C zc = cconj(r[(k == 0 ? 0 : M - k) * LD + t]);
+            const C ev = cscale(cadd(zk, zc), T(0.5));
+            const C dd = cscale(csub(zk, zc), T(0.5));
+            const C od = mk<T>(dd.y, -dd.x);
+            C w;
+            if (k < M) w = __ldg(&tw[k]); else w = mk<T>(T(-1), T(0));
+            dst[(long long)line * H + k] = cadd(ev, cmul(w, od));
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------ X pass (forward) + kick epilogue
+template <typename T, bool GW>
+__global__ void __launch_bounds__(256) k_fft_x_final(Geo g, const cplx<T> *__restrict__ QV, const cplx<T> *__restrict__ QS,
+                                                     const cplx<T> *__restrict__ fk, cplx<T> *__restrict__ pk,
+                                                     cplx<T> *__restrict__ uk, cplx<T> *__restrict__ puk,
+                                                     double *__restrict__ partKG, const DevBG *__restrict__ bg,
+                                                     const cplx<T> *__restrict__ tw) {
+    using C = cplx<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int sh = g.tlx_shift, TL = 1 << sh, N = g.N, H = g.H, M = g.M;
+    C *b0 = reinterpret_cast<C *>(smem_raw);
+    C *b1 = b0 + TL * N;
+    const int job = blockIdx.y;
+    const bool field = job < g.nf;
+    const long long off = (long long)(field ? job : job - g.nf) * g.modes;
+    const C *src = (field ? QV : QS) + off;
+    const int line0 = blockIdx.x * TL;
+    const long long stride = g.lines_x;
+    const int total = TL * N;
+    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+        const int t = idx & (TL - 1), n = idx >> sh, line = line0 + t;
+        b0[idx] = (line < g.lines_x) ? src[n * stride + line] : mk<T>(0, 0);
+    }
+    const C *r = fft_tile<C, -1>(b0, b1, N, sh, TL, tw, N);
+
+    const T norm1 = (T)bg->norm1, norm2 = (T)bg->norm2, kIR2 = (T)bg->kIR2;
+    const T c_close = (T)bg->c_close, c_open = (T)bg->c_open;
+    double accK = 0.0, accG = 0.0;
+    if (field) {
+        const bool mask = g.mask != 0;
+        const T hub = (T)bg->hub, apow = (T)bg->apow, a3 = (T)bg->a3;
+        const T dfdp = (T)bg->DFDP, eps = (T)bg->eps;
+        for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+            const int t = idx & (TL - 1), n = idx >> sh, line = line0 + t;
+            if (line >= g.lines_x) continue;
+            const int y = line / H, kz = line - y * H;
+            const int px = pcoord(n, N), py = pcoord(y, N);
+            const T k2 = (T)(px * px + py * py + kz * kz);
+            const long long a = off + n * stride + line;
+            const C f = fk[a], p = pk[a], q = r[idx];
+            // force (evolution.cpp:1124-1125)
+            const T fl = -norm1 * kIR2 * k2;
+            const C F = mk<T>(fl * f.x - norm2 * q.x, fl * f.y - norm2 * q.y);
+            const C pf = mk<T>(p.x + c_close * F.x, p.y + c_close * F.y);
+            bool inc = true;
+            if (mask && (n | line) != 0) {
+                // R_Q2C (evolution.cpp:1038-1056) with the stale a' of the step
+                const T fm = sqrt(f.x * f.x + f.y * f.y);
+                const T gx = hub * f.x + apow * pf.x, gy = hub * f.y + apow * pf.y;
+                const T R = dfdp / (fm * a3 * sqrt(gx * gx + gy * gy));
+                inc = R < eps;
+            }
+            if (inc) {
+                const double wgt = (kz == 0 || kz == M) ? 1.0 : 2.0;
+                accK += wgt * ((double)pf.x * pf.x + (double)pf.y * pf.y);
+                accG += wgt * (double)k2 * ((double)f.x * f.x + (double)f.y * f.y);
+            }
+            pk[a] = mk<T>(pf.x + c_open * F.x, pf.y + c_open * F.y);
+        }
+        double v[2] = {accK, accG};
+        block_reduce_store<2>(v, partKG + (size_t)(2 * job) * gridDim.x, gridDim.x, blockIdx.x);
+    } else if (GW) {
+        const T c_drift = (T)bg->c_drift;
+        for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+            const int t = idx & (TL - 1), n = idx >> sh, line = line0 + t;
+            if (line >= g.lines_x) continue;
+            const int y = line / H, kz = line - y * H;
+            const int px = pcoord(n, N), py = pcoord(y, N);
+            const T k2 = (T)(px * px + py * py + kz * kz);
+            const long long a = off + n * stride + line;
+            C u = uk[a];
+            const C v = puk[a], q = r[idx];
+            // drift of u_ij deferred from the stage prologue (evolution.cpp:655-662)
+            u.x += c_drift * v.x;
+            u.y += c_drift * v.y;
+            // a^(1+alpha) (lapl u + 2 sum d_i f d_j f)  (evolution.cpp:586-598)
+            const T l = -kIR2 * k2;
+            const C F = mk<T>(norm1 * (l * u.x + q.x), norm1 * (l * u.y + q.y));
+            const C vf = mk<T>(v.x + c_close * F.x, v.y + c_close * F.y);
+            uk[a] = u;
+            puk[a] = mk<T>(vf.x + c_open * F.x, vf.y + c_open * F.y);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ scalar background update
+__device__ void begin_stage(DevBG *bg, int p) {
+    const double w = bg->w[p], dt = bg->dt;
+    const int al = bg->alpha;
+    // evolution.cpp:1141, 1161, 1165, 1180
+    bg->b_half = bg->b + w * dt / 2. * bg->add;
+    const double a_half = bg->a + bg->b_half * w * dt / 2.;
+    bg->c_drift = w * dt * pow(a_half, (double)(al - 3));
+    bg->a = a_half + bg->b_half * w * dt / 2.;
+    bg->norm1 = pow(bg->a, (double)(1 + al));
+    bg->norm2 = pow(bg->a, (double)(3 + al));
+    bg->c_close = w * dt / 2;
+    if (p + 1 < bg->s) bg->c_open = bg->w[p + 1] * dt / 2;
+    else bg->c_open = (bg->steps_left > 1) ? bg->w[0] * dt / 2 : 0.0;
+    bg->hub = bg->ad_stale / bg->a;
+    bg->apow = pow(bg->a, (double)(al - 3));
+    bg->a3 = pow(bg->a, (double)(3 - al));
+    bg->stage = p;
+}
+
+__device__ void eval_coeffs(DevBG *bg) {
+    const int al = bg->alpha;
+    bg->c_drift = 0.0;
+    bg->c_close = 0.0;
+    bg->norm1 = pow(bg->a, (double)(1 + al));
+    bg->norm2 = pow(bg->a, (double)(3 + al));
+    bg->ad_stale = bg->ad;
+    bg->hub = bg->ad / bg->a;
+    bg->apow = pow(bg->a, (double)(al - 3));
+    bg->a3 = pow(bg->a, (double)(3 - al));
+}
+
+// a'' = (1/3)(fStar/MPl)^2 a^(1+2 alpha) ((alpha-2) K + alpha G + (alpha+1) V)  (evolution.cpp:1087)
+__device__ double friedmann_add(const DevBG *bg, double K, double G, double V) {
+    const int al = bg->alpha;
+    return 1. / 3. * bg->fs_over_mpl2 * pow(bg->a, (double)(1 + 2 * al)) * ((al - 2) * K + al * G + (al + 1) * V);
+}
+
+__global__ void __launch_bounds__(512) k_scalar(DevBG *bg, const double *__restrict__ partKG,
+                                                const double *__restrict__ partV, int mode, int p) {
+    __shared__ double red[512];
+    __shared__ double sums[2 * kMaxFields + kMaxTerms];
+    const bool reduce = (mode == SCALAR_END || mode == SCALAR_EVAL_END);
+    if (reduce) {
+        const int nbx = bg->nbx, nbz = bg->nbz, nf = bg->nf, nt = bg->nterms;
+        const int nq = 2 * nf + nt;
+        for (int q = 0; q < nq; ++q) {
+            double acc = 0.0;
+            if (q < 2 * nf) {
+                for (int i = threadIdx.x; i < nbx; i += blockDim.x) acc += partKG[(size_t)q * nbx + i];
+            } else {
+                for (int i = threadIdx.x; i < nbz; i += blockDim.x) acc += partV[(size_t)(q - 2 * nf) * nbz + i];
+            }
+            red[threadIdx.x] = acc;
+            __syncthreads();
+            for (int s = blockDim.x >> 1; s > 0; s >>= 1) {
+                if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+                __syncthreads();
+            }
+            if (threadIdx.x == 0) sums[q] = red[0];
+            __syncthreads();
+        }
+    }
+    if (threadIdx.x != 0) return;
+    if (mode == SCALAR_PRIME) {
+        eval_coeffs(bg);
+        bg->c_open = bg->w[0] * bg->dt / 2;
+        return;
+    }
+    if (mode == SCALAR_EVAL) {
+        eval_coeffs(bg);
+        bg->c_open = 0.0;
+        return;
+    }
+    if (mode == SCALAR_BEGIN) {
+        bg->b = bg->ad;
+        bg->ad_stale = bg->ad;
+        begin_stage(bg, 0);
+        return;
+    }
+    // reductions -> K, G, V (kinetic_energy_k / gradient_energy_k evolution.cpp:966-1034,
+    // V_E evolution.cpp:1077-1085)
+    double K = 0, G = 0, V = 0;
+    const double a = bg->a;
+    for (int f = 0; f < bg->nf; ++f) {
+        const double k = .5 * sums[2 * f] / pow(a, 6.0) * bg->inv_n3sq;
+        double grad = bg->kIR2 * sums[2 * f + 1];
+        grad *= bg->inv_n3;
+        grad /= 2.;
+        const double gq = grad / (a * a) * bg->inv_n3;
+        bg->K[f] = k;
+        bg->G[f] = gq;
+        K += k;
+        G += gq;
+    }
+    for (int tt = 0; tt < bg->nterms; ++tt) {
+        const double v = sums[2 * bg->nf + tt] * bg->inv_n3;
+        bg->V[tt] = v;
+        V += v;
+    }
+    const double add_new = friedmann_add(bg, K, G, V);
+    if (!isfinite(add_new) || !isfinite(bg->a)) bg->err = PSC_ERR_NONFINITE;
+    if (mode == SCALAR_EVAL_END) {
+        if (p == 0) bg->add = add_new;   // p == 1: diagnostics only, a'' kept as set by the caller
+        return;
+    }
+    bg->add = add_new;
+    // SCALAR_END: close stage p (evolution.cpp:1193), then open the next stage or step
+    bg->b = bg->b_half + bg->w[p] * bg->dt / 2. * bg->add;
+    if (p + 1 < bg->s) {
+        begin_stage(bg, p + 1);
+        return;
+    }
+    bg->ad = bg->b;        // evolution.cpp:1196-1197
+    bg->t += bg->dt;
+    bg->steps_left -= 1;
+    if (!isfinite(bg->ad)) bg->err = PSC_ERR_NONFINITE;
+    if (bg->steps_left > 0) {
+        bg->b = bg->ad;
+        bg->ad_stale = bg->ad;
+        begin_stage(bg, 0);
+    }
+}
+
+__global__ void k_set_run(DevBG *bg, double dt, int nsteps) {
+    bg->dt = dt;
+    bg->steps_left = nsteps;
+}
+
+// ------------------------------------------------------------------ real-space view
+template <typename T>
+__global__ void __launch_bounds__(256) k_z_c2r_real(Geo g, const cplx<T> *__restrict__ TA, T *__restrict__ out,
+                                                    const cplx<T> *__restrict__ tw, T inv_n3) {
+    using C = cplx<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int sh = g.tlz_shift, TL = 1 << sh, LD = g.ldz, H = g.H, M = g.M, N = g.N;
+    C *b0 = reinterpret_cast<C *>(smem_raw);
+    C *b1 = b0 + H * LD;
+    const int line0 = blockIdx.x * TL;
+    const long long off = (long long)blockIdx.y * g.modes;
+    const C *src = TA + off;
+    for (int idx = threadIdx.x; idx < TL * H; idx += blockDim.x) {
+        const int t = idx / H, k = idx - t * H, line = line0 + t;
+        b1[k * LD + t] = (line < g.lines_z) ? src[(long long)line * H + k] : mk<T>(0, 0);
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < TL * M; idx += blockDim.x) {
+        const int t = idx & (TL - 1), k = idx >> sh;
+        C x = b1[k * LD + t], y = cconj(b1[(M - k) * LD + t]);
+        if (k == 0) { x.y = T(0); y.y = T(0); }
+        const C s = cadd(x, y), d = csub(x, y);
+        C w = __ldg(&tw[k]);
+        w.y = -w.y;
+        const C td = cmul(w, d);
+        b0[k * LD + t] = mk<T>(s.x - td.y, s.y + td.x);
+    }
+    const C *r = fft_tile<C, +1>(b0, b1, M, sh, LD, tw, N);
+    T *o = out + (long long)blockIdx.y * g.sites;
+    for (int idx = threadIdx.x; idx < TL * N; idx += blockDim.x) {
+        const int t = idx / N, z = idx - t * N, line = line0 + t;
+        if (line >= g.lines_z) continue;
+        const C c = r[(z >> 1) * LD + t];
+        o[(long long)line * N + z] = ((z & 1) ? c.y : c.x) * inv_n3;
+    }
+}
+
+// ------------------------------------------------------------------ spectra
+// Scalar spectra bin sums (output.cpp:626-669): every stored mode, weight 2 for
+// 0 < kz < N/2; bin l = floor(sqrt(px^2 + py^2 + kz^2) + 0.5).
+template <typename T>
+__global__ void k_spectra_scalar(Geo g, const cplx<T> *__restrict__ fk, const cplx<T> *__restrict__ pk,
+                                 const DevBG *__restrict__ bg, int nb, double *__restrict__ acc,
+                                 int *__restrict__ cnt) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double *sF = reinterpret_cast<double *>(smem_raw);
+    double *sP = sF + nb, *sN = sP + nb;
+    int *sC = reinterpret_cast<int *>(sN + nb);
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) { sF[i] = sP[i] = sN[i] = 0.0; sC[i] = 0; }
+    __syncthreads();
+    const int fld = blockIdx.y, N = g.N, H = g.H, M = g.M;
+    const double a = bg->a, hub = bg->ad / a, aop = pow(a, (double)(bg->alpha - 3));
+    const cplx<T> *f = fk + (long long)fld * g.modes, *p = pk + (long long)fld * g.modes;
+    for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < g.modes;
+         m += (long long)gridDim.x * blockDim.x) {
+        const int kz = (int)(m % H);
+        const long long xy = m / H;
+        const int y = (int)(xy % N), x = (int)(xy / N);
+        const int px = pcoord(x, N), py = pcoord(y, N);
+        const int l = (int)floor(sqrt((double)(px * px + py * py + kz * kz)) + 0.5);
+        const double fr = f[m].x, fi = f[m].y, pr = p[m].x, pi = p[m].y;
+        const double w = (kz == 0 || kz == M) ? 1.0 : 2.0;
+        const double nr = aop * pr + hub * fr, ni = aop * pi + hub * fi;
+        atomicAdd(&sF[l], w * (fr * fr + fi * fi));
+        atomicAdd(&sP[l], w * (pr * pr + pi * pi));
+        atomicAdd(&sN[l], w * (nr * nr + ni * ni));
+        atomicAdd(&sC[l], (int)w);
+    }
+    __syncthreads();
+    double *aF = acc + (size_t)fld * 3 * nb;
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+        if (sC[i] == 0) continue;
+        atomicAdd(&aF[i], sF[i]);
+        atomicAdd(&aF[nb + i], sP[i]);
+        atomicAdd(&aF[2 * nb + i], sN[i]);
+        atomicAdd(&cnt[(size_t)fld * nb + i], sC[i]);
+    }
+}
+
+// GW spectra bin sums (output.cpp:780-1025): on the kz = 0 and kz = N/2 planes
+// only the reference's "+" representatives count (weight 2), plus the seven
+// non-zero real corners (weight 1); interior planes have weight 2. Per mode
+// v = P u with P = 1 - khat khat, h^2 += sum |v_ij|^2 - |tr v|^2 / 2.
+template <typename T>
+__global__ void k_spectra_gw(Geo g, const cplx<T> *__restrict__ uk, const cplx<T> *__restrict__ puk,
+                             const DevBG *__restrict__ bg, int nb, double *__restrict__ acc, int *__restrict__ cnt) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double *sH = reinterpret_cast<double *>(smem_raw);
+    double *sD = sH + nb;
+    int *sC = reinterpret_cast<int *>(sD + nb);
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) { sH[i] = sD[i] = 0.0; sC[i] = 0; }
+    __syncthreads();
+    const int N = g.N, H = g.H, M = g.M;
+    const double kIR = bg->kIR;
+    for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < g.modes;
+         m += (long long)gridDim.x * blockDim.x) {
+        const int kz = (int)(m % H);
+        const long long xy = m / H;
+        const int j = (int)(xy % N), i = (int)(xy / N);
+        int w = 2;
+        if (kz == 0 || kz == M) {
+            const bool ie = (i == 0 || i == M), je = (j == 0 || j == M);
+            const bool iin = (i >= 1 && i < M), jlo = (j >= 1 && j < M), jhi = (j > M && j < N);
+            if (ie && je) w = (i == 0 && j == 0 && kz == 0) ? 0 : 1;
+            else if (ie && jlo) w = 2;
+            else if (je && iin) w = 2;
+            else if (iin && (jlo || jhi)) w = 2;
+            else w = 0;
+        }
+        if (w == 0) continue;
+        const int px = pcoord(i, N), py = pcoord(j, N);
+        const int l = (int)floor(sqrt((double)(px * px + py * py + kz * kz)) + 0.5);
+        const double kv[3] = {px * kIR, py * kIR, kz * kIR};
+        const double kn = sqrt(kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2]);
+        const double kh[3] = {kv[0] / kn, kv[1] / kn, kv[2] / kn};
+        double res[2];
+#pragma unroll
+        for (int which = 0; which < 2; ++which) {
+            const cplx<T> *arr = which ? puk : uk;
+            double ur[6], ui[6];
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                const cplx<T> v = arr[(long long)c * g.modes + m];
+                ur[c] = v.x;
+                ui[c] = v.y;
+            }
+            const int sym[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+            double s = 0.0, trr = 0.0, tri = 0.0;
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+#pragma unroll
+                for (int b = 0; b < 3; ++b) {
+                    double vr = 0.0, vi = 0.0;
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        const double P = (a == k ? 1.0 : 0.0) - kh[a] * kh[k];
+                        vr += P * ur[sym[k][b]];
+                        vi += P * ui[sym[k][b]];
+                    }
+                    s += vr * vr + vi * vi;
+                    if (a == b) { trr += vr; tri += vi; }
+                }
+            res[which] = s - (trr * trr + tri * tri) / 2.;
+        }
+        atomicAdd(&sH[l], w * res[0]);
+        atomicAdd(&sD[l], w * res[1]);
+        atomicAdd(&sC[l], w);
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < nb; q += blockDim.x) {
+        if (sC[q] == 0) continue;
+        atomicAdd(&acc[q], sH[q]);
+        atomicAdd(&acc[nb + q], sD[q]);
+        atomicAdd(&cnt[q], sC[q]);
+    }
+}
+
+// ------------------------------------------------------------------ host side
+static int ilog2i(int v) {
+    int l = 0;
+    while ((1 << l) < v) ++l;
+    return l;
+}
+
+void plan(const psc_params &p, LaunchCfg *cfg) {
+    Geo &g = cfg->g;
+    g.N = p.N;
+    g.H = p.N / 2 + 1;
+    g.M = p.N / 2;
+    g.nf = p.nflds;
+    g.gw = p.with_gw ? 1 : 0;
+    g.model = p.model;
+    g.nterms = p.model == PSC_MODEL_PHI2 ? 1 : 2;
+    g.mask = (p.spectral && p.simulate_inflation) ? 1 : 0;
+    g.gsq = p.gsq;
+    g.lines_x = g.N * g.H;
+    g.lines_z = g.N * g.N;
+    g.modes = (long long)g.N * g.N * g.H;
+    g.sites = (long long)g.N * g.N * g.N;
+    const int csize = p.precision == 32 ? 8 : 16;
+    // X/Y passes: a tile of TL lines x N elements, two ping-pong buffers of
+    // <= 32 KiB each (TL >= 8 keeps the strided rows at >= 64 B).
+    int tl = (32768 / csize) / g.N;
+    if (tl < 4) tl = 4;
+    if (tl > 256) tl = 256;
+    while (tl > 1 && tl / 2 >= g.lines_x) tl /= 2;
+    g.tlx_shift = ilog2i(tl);
+    cfg->thr_xy = 256;
+    cfg->smem_xy = (size_t)2 * tl * g.N * csize;
+    cfg->nbx = (g.lines_x + tl - 1) / tl;
+    // Z pass: TLz lines, two H-row buffers + nslot M-row real-line slots.
+    const int nin = g.nf * (g.gw ? 4 : 1), nout = g.nf + (g.gw ? 6 : 0);
+    const int nslot = nin > nout ? nin : nout;
+    int tlz = 32;
+    auto zbytes = [&](int t) { return (size_t)(t + 1) * (2 * g.H + nslot * g.M) * csize; };
+    while (tlz > 1 && zbytes(tlz) > 100 * 1024) tlz /= 2;
+    while (tlz > 1 && tlz / 2 >= g.lines_z) tlz /= 2;
+    g.tlz_shift = ilog2i(tlz);
+    g.ldz = tlz + 1;
+    cfg->thr_z = 256;
+    cfg->smem_z = zbytes(tlz);
+    cfg->nbz = (g.lines_z + tlz - 1) / tlz;
+}
+
+template <typename T>
+static cudaError_t configure_t(const LaunchCfg &cfg) {
+    const int sxy = (int)cfg.smem_xy, sz = (int)cfg.smem_z;
+    cudaError_t e;
+#define SETA(kern, bytes)                                                                                  \
+    e = cudaFuncSetAttribute((const void *)(kern), cudaFuncAttributeMaxDynamicSharedMemorySize, (bytes));  \
+    if (e != cudaSuccess) return e;
+    SETA((k_ifft_x<T, false, true>), sxy);
+    SETA((k_ifft_x<T, true, true>), sxy);
+    SETA((k_ifft_x<T, false, false>), sxy);
+    SETA((k_ifft_x<T, true, false>), sxy);
+    SETA((k_ifft_y<T, false>), sxy);
+    SETA((k_ifft_y<T, true>), sxy);
+    SETA((k_fft_y<T>), sxy);
+    SETA((k_zpass<T, false>), sz);
+    SETA((k_zpass<T, true>), sz);
+    SETA((k_fft_x_final<T, false>), sxy);
+    SETA((k_fft_x_final<T, true>), sxy);
+    SETA((k_z_c2r_real<T>), sz);
+#undef SETA
+    return cudaSuccess;
+}
+
+cudaError_t configure(const LaunchCfg &cfg, int precision) {
+    return precision == 32 ? configure_t<float>(cfg) : configure_t<double>(cfg);
+}
+
+template <typename T>
+static cudaError_t launch_stage_t(const LaunchCfg &cfg, const Buffers &b, int drift, cudaStream_t st) {
+    using C = cplx<T>;
+    const Geo &g = cfg.g;
+    const C *tw = reinterpret_cast<const C *>(b.tw);
+    C *fk = (C *)b.fk, *pk = (C *)b.pk, *uk = (C *)b.uk, *puk = (C *)b.puk;
+    C *TA = (C *)b.TA, *TB = (C *)b.TB, *TC = (C *)b.TC, *QV = (C *)b.QV, *QS = (C *)b.QS;
+    const dim3 gx(cfg.nbx, g.nf);
+    if (g.gw) {
+        if (drift) k_ifft_x<T, true, true><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
+        else k_ifft_x<T, true, false><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
+        k_ifft_y<T, true><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, TA, TB, TC, b.bg, tw);
+        k_zpass<T, true><<<cfg.nbz, cfg.thr_z, cfg.smem_z, st>>>(g, TA, TB, TC, QV, QS, b.partV, b.bg, tw);
+    } else {
+        if (drift) k_ifft_x<T, false, true><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
+        else k_ifft_x<T, false, false><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
+        k_ifft_y<T, false><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, TA, TB, TC, b.bg, tw);
+        k_zpass<T, false><<<cfg.nbz, cfg.thr_z, cfg.smem_z, st>>>(g, TA, TB, TC, QV, QS, b.partV, b.bg, tw);
+    }
+    ArrList al{};
+    int nj = 0;
+    for (int f = 0; f < g.nf; ++f) al.p[nj++] = QV + (long long)f * g.modes;
+    if (g.gw)
+        for (int c = 0; c < 6; ++c) al.p[nj++] = QS + (long long)c * g.modes;
+    k_fft_y<T><<<dim3(cfg.nbx, nj), cfg.thr_xy, cfg.smem_xy, st>>>(g, al, tw);
+    const dim3 gf(cfg.nbx, nj);
+    if (g.gw) k_fft_x_final<T, true><<<gf, cfg.thr_xy, cfg.smem_xy, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw);
+    else k_fft_x_final<T, false><<<gf, cfg.thr_xy, cfg.smem_xy, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stage(const LaunchCfg &cfg, const Buffers &b, int precision, int drift, cudaStream_t st) {
+    return precision == 32 ? launch_stage_t<float>(cfg, b, drift, st) : launch_stage_t<double>(cfg, b, drift, st);
+}
+
+cudaError_t launch_scalar(const LaunchCfg &cfg, const Buffers &b, int mode, int p, cudaStream_t st) {
+    (void)cfg;
+    k_scalar<<<1, 512, 0, st>>>(b.bg, b.partKG, b.partV, mode, p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_set_run(DevBG *bg, double dt, int nsteps, cudaStream_t st) {
+    k_set_run<<<1, 1, 0, st>>>(bg, dt, nsteps);
+    return cudaGetLastError();
+}
+
+template <typename T>
+static cudaError_t launch_c2r_real_t(const LaunchCfg &cfg, const Buffers &b, const void *src, int nsrc,
+                                     cudaStream_t st) {
+    using C = cplx<T>;
+    const Geo &g = cfg.g;
+    const C *tw = reinterpret_cast<const C *>(b.tw);
+    C *TA = (C *)b.TA;
+    // one source array at a time through TA (TA holds nf arrays)
+    for (int s0 = 0; s0 < nsrc; s0 += g.nf) {
+        const int cnt = (nsrc - s0) < g.nf ? (nsrc - s0) : g.nf;
+        const C *s = (const C *)src + (long long)s0 * g.modes;
+        k_ifft_x<T, false, false><<<dim3(cfg.nbx, cnt), cfg.thr_xy, cfg.smem_xy, st>>>(g, (C *)s, nullptr, TA, nullptr,
+                                                                                      b.bg, tw);
+        k_ifft_y<T, false><<<dim3(cfg.nbx, cnt), cfg.thr_xy, cfg.smem_xy, st>>>(g, TA, nullptr, nullptr, b.bg, tw);
+        k_z_c2r_real<T><<<dim3(cfg.nbz, cnt), cfg.thr_z, cfg.smem_z, st>>>(
+            g, TA, (T *)b.real + (long long)s0 * g.sites, tw, (T)(1.0 / (double)g.sites));
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_c2r_real(const LaunchCfg &cfg, const Buffers &b, int precision, const void *src, int nsrc,
+                            cudaStream_t st) {
+    return precision == 32 ? launch_c2r_real_t<float>(cfg, b, src, nsrc, st)
+                           : launch_c2r_real_t<double>(cfg, b, src, nsrc, st);
+}
+
+template <typename T>
+static cudaError_t launch_spectra_t(const LaunchCfg &cfg, const Buffers &b, int nb, cudaStream_t st) {
+    using C = cplx<T>;
+    const Geo &g = cfg.g;
+    const size_t nacc = (size_t)g.nf * 3 * nb + 2 * nb, ncnt = (size_t)g.nf * nb + nb;
+    cudaError_t e = cudaMemsetAsync(b.spec, 0, nacc * sizeof(double), st);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(b.spec_cnt, 0, ncnt * sizeof(int), st);
+    if (e != cudaSuccess) return e;
+    const int blocks = 4 * 152;
+    const size_t sm_s = (size_t)nb * (3 * sizeof(double) + sizeof(int));
+    k_spectra_scalar<T><<<dim3(blocks, g.nf), 256, sm_s, st>>>(g, (const C *)b.fk, (const C *)b.pk, b.bg, nb, b.spec,
+                                                               b.spec_cnt);
+    if (g.gw) {
+        const size_t sm_g = (size_t)nb * (2 * sizeof(double) + sizeof(int));
+        k_spectra_gw<T><<<blocks, 256, sm_g, st>>>(g, (const C *)b.uk, (const C *)b.puk, b.bg, nb,
+                                                   b.spec + (size_t)g.nf * 3 * nb, b.spec_cnt + (size_t)g.nf * nb);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spectra(const LaunchCfg &cfg, const Buffers &b, int precision, int nb, cudaStream_t st) {
+    return precision == 32 ? launch_spectra_t<float>(cfg, b, nb, st) : launch_spectra_t<double>(cfg, b, nb, st);
+}
+
+}  // namespace psc

@@ -1,0 +1,78 @@
+// psc_launch.h — host-side interface between the C-ABI layer (psc_api.cpp) and
+// the CUDA kernels (psc_kernels.cu). No CUDA C++ device code here.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/psc.h"
+
+namespace psc {
+
+struct DevBG;
+
+// Lattice geometry and tiling, passed by value to every pass kernel.
+struct Geo {
+    int N, H, M;                 // edge, half-spectrum length N/2+1, N/2
+    int nf, gw, nterms, mask;    // fields, GW flag, potential terms, R_Q2C mask on
+    int model;                   // PSC_MODEL_*
+    int tlx_shift, tlz_shift;    // log2 lines per tile: X/Y passes, Z pass
+    int ldz;                     // shared-memory leading dimension of the Z pass (lines + 1)
+    int lines_x;                 // N * H  (X-pass and Y-pass line count per array)
+    int lines_z;                 // N * N  (Z-pass line count)
+    long long modes, sites;
+    double gsq;
+};
+
+struct LaunchCfg {
+    Geo g;
+    int thr_xy, thr_z;           // threads per block
+    size_t smem_xy, smem_z;      // dynamic shared memory bytes
+    int nbx;                     // blocks of the X / Y passes (per array)
+    int nbz;                     // blocks of the Z pass
+};
+
+// Device buffers of one lattice. Complex arrays hold cplx<T> of the handle's
+// precision (T = float for 32, double for 64).
+struct Buffers {
+    void *fk, *pk;               // [nf][modes]   f_k, pi_k (pi_half between the stages of a step)
+    void *uk, *puk;              // [6][modes]    u_k, pi_u_k (GW)
+    void *TA, *TB, *TC;          // [nf][modes]   inverse-transform intermediates (f, d/dx f, d/dy f)
+    void *QV, *QS;               // [nf][modes], [6][modes]   forward-transform intermediates (V', S_ab)
+    void *tw;                    // [N] e^{-2 pi i q/N}
+    void *real;                  // [nf][sites] real-space output buffer (optional)
+    double *partKG;              // [2 nf][nbx]   block partial sums of K and G
+    double *partV;               // [nterms][nbz] block partial sums of V
+    double *spec;                // spectra accumulators
+    int *spec_cnt;
+    DevBG *bg;
+};
+
+enum ScalarMode {
+    SCALAR_PRIME = 0,   // coefficients for the opening half kick of a call
+    SCALAR_BEGIN = 1,   // start of a step: b = ad, begin stage 0
+    SCALAR_END = 2,     // end of stage p: reductions -> a'' -> b; begin the next stage/step
+    SCALAR_EVAL = 3,    // coefficients for a pure force/energy evaluation
+    SCALAR_EVAL_END = 4 // reductions of an evaluation -> K, G, V, a''
+};
+
+// Tile sizes, block sizes and shared memory for one configuration.
+void plan(const psc_params &p, LaunchCfg *cfg);
+// Set the dynamic shared-memory limits of the kernels a configuration uses.
+cudaError_t configure(const LaunchCfg &cfg, int precision);
+
+// One force evaluation of a stage: X-iFFT (with the drift when drift != 0),
+// Y-iFFT, fused Z pass (c2r, V' and anisotropic stress, r2c), Y-fFFT and the
+// X-fFFT with the kick epilogue and the K, G reductions.
+cudaError_t launch_stage(const LaunchCfg &cfg, const Buffers &b, int precision, int drift, cudaStream_t st);
+cudaError_t launch_scalar(const LaunchCfg &cfg, const Buffers &b, int mode, int p, cudaStream_t st);
+cudaError_t launch_set_run(DevBG *bg, double dt, int nsteps, cudaStream_t st);
+// Real-space view of nsrc complex arrays (c2r / N^3) into b.real (precision T).
+cudaError_t launch_c2r_real(const LaunchCfg &cfg, const Buffers &b, int precision, const void *src, int nsrc,
+                            cudaStream_t st);
+// Bin sums of the scalar spectra (output.cpp:626-669) and of the GW spectra
+// (output.cpp:780-1025). Layout of b.spec: [nf][3][nb] then GW [2][nb];
+// b.spec_cnt: [nf][nb] then GW [nb]. Zeroes the accumulators first.
+cudaError_t launch_spectra(const LaunchCfg &cfg, const Buffers &b, int precision, int nb, cudaStream_t st);
+
+}  // namespace psc

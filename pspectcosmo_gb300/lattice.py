@@ -1,0 +1,245 @@
+"""Python mirror of the reference's evolution interface over the C ABI (libpsc.so).
+
+The reference drives its path through free functions on global arrays
+(pspectcosmo.h:203-272): initialize(), evolve_VV_k_nopad(dt) / evolve_VV(dt),
+kernel_a_k_nopad(), and the output routines spectra(), energy(), meansvars(),
+scale(). `Lattice` exposes the same operations on one device-resident lattice:
+
+    lat = Lattice(Params.reference_default())
+    lat.initialize()                 # initialize() [+ initialize_GW()]
+    lat.evolve(dt, nsteps)           # nsteps x evolve_VV_k_nopad(dt) / evolve_VV(dt)
+    lat.spectra(), lat.energy(), lat.meansvars(), lat.scale()
+
+Errors from the library raise PscError (the reference exits instead,
+output.cpp:450-454). The CUDA library is required: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .params import Params
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libpsc.so")
+
+PSC_OK = 0
+PSC_ERR_CONFIG = -1
+PSC_ERR_ARG = -2
+PSC_ERR_CUDA = -3
+PSC_ERR_NONFINITE = -4
+PSC_ERR_TIMEOUT = -5
+PSC_ERR_STATE = -6
+PSC_ERR_NOMEM = -7
+
+_lib = None
+
+
+class PscError(RuntimeError):
+    def __init__(self, code: int, where: str):
+        self.code = code
+        msg = _lib.psc_last_error().decode() if _lib else ""
+        name = _lib.psc_strerror(code).decode() if _lib else str(code)
+        super().__init__(f"{where}: {name} ({code}): {msg}")
+
+
+def load_library(path: str | None = None):
+    """Load libpsc.so (built by pspectcosmo_gb300.build). Raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with `python -m pspectcosmo_gb300.build` "
+                           "(the CUDA path has no CPU fallback)")
+    L = ctypes.CDLL(path)
+    P = ctypes.c_void_p
+    D = ctypes.POINTER(ctypes.c_double)
+    I32 = ctypes.POINTER(ctypes.c_int32)
+    PP = ctypes.POINTER(Params)
+    L.psc_default_params.argtypes = [PP]
+    L.psc_default_params.restype = None
+    L.psc_create.argtypes = [PP, ctypes.POINTER(P)]
+    L.psc_destroy.argtypes = [P]
+    L.psc_destroy.restype = None
+    L.psc_init_ic.argtypes = [P]
+    L.psc_generate_ic.argtypes = [PP, D, D, D, D, D]
+    L.psc_set_state.argtypes = [P, D, D, ctypes.c_double, ctypes.c_double, ctypes.c_double, D, D]
+    L.psc_get_state.argtypes = [P, D, D, D, D, D, D, D]
+    L.psc_get_time.argtypes = [P, D]
+    L.psc_set_time.argtypes = [P, ctypes.c_double]
+    L.psc_step.argtypes = [P, ctypes.c_double, ctypes.c_int]
+    L.psc_get_fields_real.argtypes = [P, D, D]
+    L.psc_maxnumbins.argtypes = [ctypes.c_int]
+    L.psc_spectra.argtypes = [P, I32, D, D, D, I32, D, D, D]
+    L.psc_energies.argtypes = [P, D, D, D, D, D, D]
+    L.psc_means.argtypes = [P, D]
+    L.psc_last_step_ms.argtypes = [P, ctypes.POINTER(ctypes.c_float)]
+    L.psc_strerror.argtypes = [ctypes.c_int]
+    L.psc_strerror.restype = ctypes.c_char_p
+    L.psc_last_error.argtypes = []
+    L.psc_last_error.restype = ctypes.c_char_p
+    for name in ("psc_create", "psc_init_ic", "psc_generate_ic", "psc_set_state", "psc_get_state", "psc_get_time",
+                 "psc_set_time", "psc_step", "psc_get_fields_real", "psc_maxnumbins", "psc_spectra", "psc_energies",
+                 "psc_means", "psc_last_step_ms"):
+        getattr(L, name).restype = ctypes.c_int
+    _lib = L
+    return L
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a):
+    return None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+
+
+def _check(rc: int, where: str):
+    if rc != PSC_OK:
+        raise PscError(rc, where)
+
+
+def generate_ic(params: Params):
+    """Host-only initial conditions (initialize() / initialize_GW()) as numpy arrays."""
+    L = load_library()
+    p = params
+    f = np.zeros((p.nflds, p.modes), np.complex128)
+    pi = np.zeros((p.nflds, p.modes), np.complex128)
+    u = np.zeros((6, p.modes), np.complex128) if p.with_gw else None
+    pu = np.zeros((6, p.modes), np.complex128) if p.with_gw else None
+    info = np.zeros(6)
+    _check(L.psc_generate_ic(ctypes.byref(p), _dp(f), _dp(pi), _dp(u), _dp(pu), _dp(info)), "psc_generate_ic")
+    keys = ("hubble_init", "a", "ad", "add_printed", "kinetic", "potential")
+    return f, pi, u, pu, dict(zip(keys, info.tolist()))
+
+
+class Lattice:
+    """One lattice on the current CUDA device (a psc_handle)."""
+
+    def __init__(self, params: Params):
+        self.p = params.copy()
+        self._L = load_library()
+        h = ctypes.c_void_p()
+        _check(self._L.psc_create(ctypes.byref(self.p), ctypes.byref(h)), "psc_create")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.psc_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- initialize() / state -------------------------------------------------
+    def initialize(self):
+        """initialize() (initialize.cpp:562) and, with GWs, initialize_GW() (initialize.cpp:341)."""
+        _check(self._L.psc_init_ic(self._h), "psc_init_ic")
+
+    def set_state(self, f_k, pi_k, a, ad, add, u_k=None, pi_u_k=None):
+        c = lambda x: None if x is None else np.ascontiguousarray(x, np.complex128)
+        f_k, pi_k, u_k, pi_u_k = c(f_k), c(pi_k), c(u_k), c(pi_u_k)
+        _check(self._L.psc_set_state(self._h, _dp(f_k), _dp(pi_k), a, ad, add, _dp(u_k), _dp(pi_u_k)),
+               "psc_set_state")
+
+    def get_state(self):
+        p = self.p
+        f = np.zeros((p.nflds, p.modes), np.complex128)
+        pi = np.zeros((p.nflds, p.modes), np.complex128)
+        u = np.zeros((6, p.modes), np.complex128) if p.with_gw else None
+        pu = np.zeros((6, p.modes), np.complex128) if p.with_gw else None
+        a, ad, add = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        _check(self._L.psc_get_state(self._h, _dp(f), _dp(pi), ctypes.byref(a), ctypes.byref(ad), ctypes.byref(add),
+                                     _dp(u), _dp(pu)), "psc_get_state")
+        return dict(f_k=f, pi_k=pi, u_k=u, pi_u_k=pu, a=a.value, ad=ad.value, add=add.value)
+
+    @property
+    def t(self) -> float:
+        v = ctypes.c_double()
+        _check(self._L.psc_get_time(self._h, ctypes.byref(v)), "psc_get_time")
+        return v.value
+
+    @t.setter
+    def t(self, value: float):
+        _check(self._L.psc_set_time(self._h, float(value)), "psc_set_time")
+
+    def background(self) -> dict:
+        st = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        _check(self._L.psc_get_state(self._h, None, None, *(ctypes.byref(x) for x in st), None, None), "psc_get_state")
+        return dict(t=self.t, a=st[0].value, ad=st[1].value, add=st[2].value)
+
+    # -- evolution ------------------------------------------------------------
+    def evolve(self, dt: float, nsteps: int = 1):
+        """nsteps calls of evolve_VV_k_nopad(dt) (spectral) or evolve_VV(dt) (real space)."""
+        _check(self._L.psc_step(self._h, float(dt), int(nsteps)), "psc_step")
+
+    def last_step_ms(self) -> float:
+        v = ctypes.c_float()
+        _check(self._L.psc_last_step_ms(self._h, ctypes.byref(v)), "psc_last_step_ms")
+        return v.value
+
+    # -- outputs --------------------------------------------------------------
+    def fields_real(self):
+        p = self.p
+        f = np.zeros((p.nflds, p.N, p.N, p.N))
+        pi = np.zeros((p.nflds, p.N, p.N, p.N))
+        _check(self._L.psc_get_fields_real(self._h, _dp(f), _dp(pi)), "psc_get_fields_real")
+        return f, pi
+
+    def spectra_raw(self) -> dict:
+        p = self.p
+        nb = p.maxnumbins
+        out = dict(numpoints=np.zeros((p.nflds, nb), np.int32), f2=np.zeros((p.nflds, nb)),
+                   pi2=np.zeros((p.nflds, nb)), n2=np.zeros((p.nflds, nb)))
+        if p.with_gw:
+            out.update(gw_numpoints=np.zeros(nb, np.int32), h2=np.zeros(nb), hdot2=np.zeros(nb))
+        hz = ctypes.c_double(0.0)
+        _check(self._L.psc_spectra(self._h, _ip(out["numpoints"]), _dp(out["f2"]), _dp(out["pi2"]), _dp(out["n2"]),
+                                   _ip(out.get("gw_numpoints")), _dp(out.get("h2")), _dp(out.get("hdot2")),
+                                   ctypes.byref(hz)), "psc_spectra")
+        out["hdot2_zero"] = hz.value
+        return out
+
+    def energies(self) -> dict:
+        p = self.p
+        K, G, V = np.zeros(p.nflds), np.zeros(p.nflds), np.zeros(p.num_potential_terms)
+        tot, fv, rho = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        _check(self._L.psc_energies(self._h, _dp(K), _dp(G), _dp(V), ctypes.byref(tot), ctypes.byref(fv),
+                                    ctypes.byref(rho)), "psc_energies")
+        return dict(K=K, G=G, V=V, total=tot.value, friedmann_violation=fv.value, rho_gw=rho.value)
+
+    def means(self) -> np.ndarray:
+        out = np.zeros((self.p.nflds, 6))
+        _check(self._L.psc_means(self._h, _dp(out)), "psc_means")
+        return out
+
+    # reference-named output rows (the columns the reference writes)
+    def spectra(self) -> dict:
+        from .outputs import spectra_rows
+
+        return spectra_rows(self.p, self.background(), self.spectra_raw(), self.energies()["total"])
+
+    def energy(self) -> dict:
+        from .outputs import energy_rows
+
+        return energy_rows(self.p, self.background(), self.energies())
+
+    def meansvars(self) -> np.ndarray:
+        return self.means()
+
+    def scale(self) -> list:
+        from .outputs import scale_row
+
+        return scale_row(self.p, self.background())

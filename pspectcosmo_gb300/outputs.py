@@ -1,0 +1,141 @@
+"""Reference output rows and text files computed from the device reductions.
+
+The column formulas follow the reference's writers:
+  spectra_scalar_<f>.txt   output.cpp:671-690   (p, P_f, P_pi, n_k, numpoints)
+  spectra_gws.txt          output.cpp:1041-1052 (p, P_h, dP_rhoGW, reference line, numpoints)
+  energy_gws.txt           output.cpp:1055-1060 (t, rho_GW / rho, rho_GW)
+  average_energies.txt     output.cpp:1163-1168 (t, K_0, G_0, [K_1, G_1], V_terms..., total)
+  average_energy_conservation.txt  output.cpp:1171-1185
+  average_scale_factor.txt output.cpp:467-486
+  average_scalar_<f>.txt   output.cpp:430-461
+Numbers are written with the reference's 6 significant digits (std::scientific,
+setprecision(6)) so existing post-processing scripts read the files unchanged.
+"""
+from __future__ import annotations
+
+import math
+import os
+
+import numpy as np
+
+from .params import MODEL_PHI2, Params
+
+
+def mass_sq_av(p: Params, means: np.ndarray) -> np.ndarray:
+    """<effective_mass(f(x))> over the lattice (output.cpp:571-580); the models'
+    effective masses are linear in the squared fields, so <f^2> suffices."""
+    if p.model == MODEL_PHI2:
+        return np.array([1.0])
+    phi2, chi2 = means[0, 2], means[1, 2]
+    return np.array([1.0 + p.gsq * chi2, p.gsq * phi2])
+
+
+def spectra_rows(p: Params, bg: dict, raw: dict, total: float, means: np.ndarray | None = None) -> dict:
+    a, ad, al = bg["a"], bg["ad"], p.alpha
+    n3 = float(p.sites)
+    nb = p.maxnumbins
+    a_of_pi = a ** (al - 3)
+    out = {}
+    m2 = mass_sq_av(p, means) if means is not None else (np.array([1.0]) if p.model == MODEL_PHI2 else None)
+    for f in range(p.nflds):
+        rows = []
+        for i in range(1, nb):
+            pk = p.kIR * i
+            npt = int(raw["numpoints"][f, i])
+            f2, pi2, n2 = raw["f2"][f, i], raw["pi2"][f, i], raw["n2"][f, i]
+            nd = 0.0
+            if m2 is not None:
+                om2 = abs(pk * pk + a * a * m2[f])
+                if om2 > 0:
+                    om = math.sqrt(om2)
+                    nd = (a * a * p.L ** 3 / 2.0 / n3 ** 2 * (p.f_star / p.omegaStar) ** 2
+                          * (om * f2 + a ** (2 * (1 - al)) / om * n2))
+            rows.append((pk, i / n3 ** 2 * npt * f2, i / n3 ** 2 * npt * a_of_pi ** 2 * pi2, nd, npt))
+        out[f"spectra_scalar_{f}"] = np.array(rows)
+    if p.with_gw:
+        rows = []
+        for i in range(1, nb):
+            npt = int(raw["gw_numpoints"][i])
+            rows.append((p.kIR * i, i / n3 ** 2 * npt * raw["h2"][i],
+                         i / n3 ** 2 / 4.0 / a ** 6 * (p.f_star / p.MPl) ** 2 / total * npt * raw["hdot2"][i],
+                         (p.MPl * p.omegaStar) ** 2 / p.f_star ** 4 * 2 / math.pi ** 2 * ad ** 2 / a ** (2 * al + 2),
+                         npt))
+        out["spectra_gws"] = np.array(rows)
+    return out
+
+
+def energy_rows(p: Params, bg: dict, en: dict) -> dict:
+    vals = []
+    for f in range(p.nflds):
+        vals += [en["K"][f], en["G"][f]]
+    vals += list(en["V"])
+    vals.append(en["total"])
+    return dict(average_energies=np.array([bg["t"]] + vals),
+                average_energy_conservation=np.array([bg["t"], en["friedmann_violation"]]),
+                energy_gws=np.array([bg["t"], en["rho_gw"] / en["total"] if en["total"] else 0.0, en["rho_gw"]]))
+
+
+def scale_row(p: Params, bg: dict) -> list:
+    a, ad, add, al = bg["a"], bg["ad"], bg["add"], p.alpha
+    return [bg["t"], a, ad, ad / a, add, 1 / (a ** (-al) * ad), 1 + al - a * add / ad ** 2]
+
+
+class TextWriter:
+    """Appends the reference's text outputs (output.cpp) in directory `dir_`."""
+
+    def __init__(self, p: Params, dir_: str = "output", ext: str = ".txt"):
+        self.p, self.dir, self.ext = p, dir_, ext
+        os.makedirs(os.path.join(dir_, "Snapshots"), exist_ok=True)
+        self._first_spectra = True
+
+    def _open(self, name):
+        return open(os.path.join(self.dir, name + self.ext), "a")
+
+    @staticmethod
+    def _e(x):
+        return f"{x:15.6e}"
+
+    def save_freq(self, lat):
+        """save_Freq(): meansvars, scale, energy (output.cpp:1831-1840)."""
+        p = self.p
+        bg = lat.background()
+        means = lat.means()
+        for f in range(p.nflds):
+            with self._open(f"average_scalar_{f}") as fh:
+                m = means[f]
+                fh.write(f"{bg['t']:.3f}" + "".join(self._e(v) for v in m) + "\n")
+        if p.expansion == 2:
+            r = scale_row(p, bg)
+            with self._open("average_scale_factor") as fh:
+                fh.write(f"{r[0]:.6f} {r[1]:.6f} {r[2]:.6f} {r[3]:.6f} {r[4]:.6f} {r[5]:15.6e} {r[6]:.6f}\n")
+        en = lat.energies()
+        er = energy_rows(p, bg, en)
+        with self._open("average_energies") as fh:
+            fh.write(f"{bg['t']:.3f}" + "".join(f" {v:.6e}" for v in er["average_energies"][1:]) + "\n")
+        if p.expansion != 1:
+            lhs = bg["ad"] ** 2
+            rhs = (p.f_star / p.MPl) ** 2 * bg["a"] ** (2 * (p.alpha + 1)) * en["total"] / 3.0
+            with self._open("average_energy_conservation") as fh:
+                fh.write(f"{bg['t']:.3f} {en['friedmann_violation']:.8e} {lhs:.6f} {rhs:.6f}\n")
+
+    def save_infreq(self, lat):
+        """spectra() (output.cpp:490-1062)."""
+        p = self.p
+        bg = lat.background()
+        en = lat.energies()
+        rows = spectra_rows(p, bg, lat.spectra_raw(), en["total"], lat.means())
+        for f in range(p.nflds):
+            with self._open(f"spectra_scalar_{f}") as fh:
+                for r in rows[f"spectra_scalar_{f}"]:
+                    fh.write(f"{r[0]:.1f} {r[1]:15.6e} {r[2]:15.6e} {r[3]:15.6e} {int(r[4])}\n")
+                fh.write("\n")
+        with self._open("average_spectra_times") as fh:
+            fh.write(f"{bg['t']:.2f}\n")
+        if p.with_gw:
+            with self._open("spectra_gws") as fh:
+                for r in rows["spectra_gws"]:
+                    fh.write(f"{r[0]:.1f} {r[1]:15.6e} {r[2]:15.6e} {r[3]:15.6e} {int(r[4])}\n")
+                fh.write("\n")
+            with self._open("energy_gws") as fh:
+                rho = en["rho_gw"]
+                fh.write(f"{bg['t']:.2f} {rho / en['total']:.6e} {rho:.6e}\n")

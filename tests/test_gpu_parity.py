@@ -1,0 +1,208 @@
+"""CUDA path (libpsc.so through its C ABI) against the FP64 oracle.
+
+FP64 device path: the plain method; it must match the oracle to 1e-10 relative in the
+fields after the runs below (the spec bar for FP64) and bit for bit in the
+spectrum bin counts. FP32 device path: fields within 2e-4 relative of the oracle
+after the same runs, spectra within 1e-3, background within 1e-6 (measured tolerances,
+written here so a regression shows)."""
+import numpy as np
+import pytest
+
+from golden_util import load, output_rows, params_for, rel
+
+pytestmark = pytest.mark.gpu
+
+RUNS = ["spec1_n16", "spec1_n16_vv6", "spec1_n32_vv4", "spec1_n64_dt1e-4", "spec2_n16_vv4", "spec2_n32_vv2",
+        "gw1_n16_vv2", "gw2_n16_vv4"]
+
+FP32_FIELD_TOL = 2e-4
+FP32_SPEC_TOL = 1e-3
+FP32_BG_TOL = 1e-6
+
+
+def _pair(oracle_mod, run, precision):
+    from pspectcosmo_gb300 import Lattice
+
+    g, meta = load(run)
+    p = params_for(meta, precision)
+    o = oracle_mod.Oracle(p)
+    o.init_ic()
+    lat = Lattice(p)
+    lat.initialize()
+    return g, meta, p, o, lat
+
+
+def _compare_state(lat, o, p, tol_field, tol_bg):
+    st = lat.get_state()
+    of, opi, ou, opu = o.state_k()
+    assert rel(st["f_k"], of) < tol_field, "f_k"
+    assert rel(st["pi_k"], opi) < tol_field, "pi_k"
+    if p.with_gw:
+        assert rel(st["u_k"], ou) < tol_field, "u_k"
+        assert rel(st["pi_u_k"], opu) < tol_field, "pi_u_k"
+    bg = o.bg()
+    assert rel(st["a"], bg["a"]) < tol_bg
+    assert rel(st["ad"], bg["ad"]) < tol_bg
+    assert rel(st["add"], bg["add"]) < max(tol_bg, 1e-11)
+
+
+def _compare_outputs(lat, o, p, tol):
+    r_gpu = output_rows(lat, p)
+    r_orc = output_rows(o, p)
+    for f in range(p.nflds):
+        a, b = r_gpu[f"spectra_scalar_{f}"], r_orc[f"spectra_scalar_{f}"]
+        assert np.array_equal(a[:, 4], b[:, 4]), "bin counts must be bit-exact"
+        for c in (1, 2, 3):
+            assert rel(a[:, c], b[:, c]) < tol, f"spectra col {c}"
+    eg, eo = r_gpu["energies"], r_orc["energies"]
+    assert rel(eg["K"], eo["K"]) < tol and rel(eg["G"], eo["G"]) < tol and rel(eg["V"], eo["V"]) < tol
+    if p.with_gw:
+        a, b = r_gpu["spectra_gws"], r_orc["spectra_gws"]
+        assert np.array_equal(a[:, 4], b[:, 4])
+        for c in (1, 2):
+            assert rel(a[:, c], b[:, c]) < tol, f"GW spectra col {c}"
+        assert rel(eg["rho_gw"], eo["rho_gw"]) < tol
+
+
+@pytest.mark.parametrize("run", RUNS)
+def test_fp64_matches_oracle(oracle_mod, run):
+    g, meta, p, o, lat = _pair(oracle_mod, run, 64)
+    _compare_state(lat, o, p, 1e-13, 1e-13)   # initial conditions + initial a''
+    lat.evolve(meta["dt"], meta["nsteps"])
+    o.step(meta["dt"], meta["nsteps"])
+    _compare_state(lat, o, p, 1e-10, 1e-12)
+    _compare_outputs(lat, o, p, 1e-10)
+    assert abs(lat.t - meta["nsteps"] * meta["dt"]) < 1e-12
+
+
+@pytest.mark.parametrize("run", RUNS)
+def test_fp32_within_stated_tolerance(oracle_mod, run):
+    g, meta, p, o, lat = _pair(oracle_mod, run, 32)
+    lat.evolve(meta["dt"], meta["nsteps"])
+    o.step(meta["dt"], meta["nsteps"])
+    _compare_state(lat, o, p, FP32_FIELD_TOL, FP32_BG_TOL)
+    _compare_outputs(lat, o, p, FP32_SPEC_TOL)
+
+
+def test_fp64_against_reference_golden_directly(oracle_mod):
+    """No oracle in the loop: the device result against the reference's own dump."""
+    g, meta, p, o, lat = _pair(oracle_mod, "spec2_n16_vv4", 64)
+    lat.evolve(meta["dt"], meta["nsteps"])
+    st = lat.get_state()
+    assert rel(st["f_k"], g["fin_f_k"]) < 1e-10 and rel(st["pi_k"], g["fin_pi_k"]) < 1e-10
+    assert rel(st["a"], g["bg"][-1, 2]) < 1e-12
+
+
+def test_fp64_1000_steps_64cubed(oracle_mod):
+    """The shipped configuration (64^3, velocity Verlet, FP64) for 1000 steps, at a
+    stable dt: fields within 1e-10 relative, bin counts exact."""
+    from pspectcosmo_gb300 import Lattice
+    from pspectcosmo_gb300.params import Params
+
+    p = Params.reference_default()
+    o = oracle_mod.Oracle(p)
+    o.init_ic()
+    lat = Lattice(p)
+    lat.initialize()
+    dt = 1e-4
+    for _ in range(4):
+        lat.evolve(dt, 250)
+        o.step(dt, 250)
+    _compare_state(lat, o, p, 1e-10, 1e-12)
+    _compare_outputs(lat, o, p, 1e-10)
+
+
+def test_fp64_shipped_dt_background_track(oracle_mod):
+    """The shipped configuration at the BASELINE dt = 0.002 (unstable at the start):
+    a(t) and a'(t) follow the reference's golden track over 1000 steps."""
+    from pspectcosmo_gb300 import Lattice
+
+    g, meta = load("spec1_n64_dt2e-3")
+    p = params_for(meta, 64)
+    lat = Lattice(p)
+    lat.initialize()
+    worst = 0.0
+    for s in range(50, 1001, 50):
+        lat.evolve(meta["dt"], 50)
+        st = lat.background()
+        worst = max(worst, rel(st["a"], g["bg"][s, 2]), rel(st["ad"], g["bg"][s, 3]))
+    assert worst < 1e-8
+
+
+def test_real_space_view_matches_numpy(oracle_mod):
+    from pspectcosmo_gb300 import Lattice
+    from pspectcosmo_gb300.params import Params
+
+    for prec, tol in ((64, 1e-13), (32, 1e-5)):
+        p = Params.preheating(N=32, precision=prec)
+        lat = Lattice(p)
+        lat.initialize()
+        st = lat.get_state()
+        f, pi = lat.fields_real()
+        N = p.N
+        for fld in range(p.nflds):
+            ref = np.fft.irfftn(st["f_k"][fld].reshape(N, N, N // 2 + 1), s=(N, N, N), axes=(0, 1, 2))
+            assert rel(f[fld], ref) < tol
+            refp = np.fft.irfftn(st["pi_k"][fld].reshape(N, N, N // 2 + 1), s=(N, N, N), axes=(0, 1, 2))
+            assert rel(pi[fld], refp) < tol
+
+
+@pytest.mark.parametrize("N", [8, 128])
+def test_other_lattice_sizes_fp64(oracle_mod, N):
+    from pspectcosmo_gb300 import Lattice
+    from pspectcosmo_gb300.params import Params
+
+    p = Params.preheating(N=N, vv=2)
+    o = oracle_mod.Oracle(p)
+    o.init_ic()
+    lat = Lattice(p)
+    lat.initialize()
+    lat.evolve(0.005, 3)
+    o.step(0.005, 3)
+    _compare_state(lat, o, p, 1e-10, 1e-12)
+
+
+def test_nonfinite_state_is_reported():
+    """A NaN planted in host-side initial data is caught by the device finite check."""
+    from pspectcosmo_gb300 import Lattice, PscError
+    from pspectcosmo_gb300.params import Params
+
+    p = Params.reference_default(N=16)
+    lat = Lattice(p)
+    lat.initialize()
+    st = lat.get_state()
+    f = st["f_k"].copy()
+    f[0, 5] = np.nan
+    lat.set_state(f, st["pi_k"], st["a"], st["ad"], st["add"])
+    with pytest.raises(PscError) as ei:
+        lat.evolve(0.002, 2)
+    assert ei.value.code == -4
+    # the context is still usable
+    lat.set_state(st["f_k"], st["pi_k"], st["a"], st["ad"], st["add"])
+    lat.evolve(0.002, 2)
+
+
+def test_step_before_state_is_rejected():
+    from pspectcosmo_gb300 import Lattice, PscError
+    from pspectcosmo_gb300.params import Params
+
+    lat = Lattice(Params.reference_default(N=16))
+    with pytest.raises(PscError) as ei:
+        lat.evolve(0.002, 1)
+    assert ei.value.code == -6
+
+
+def test_split_calls_equal_one_call(oracle_mod):
+    """evolve(dt, 6) == 6 x evolve(dt, 1) (the opening half kick of a call)."""
+    from pspectcosmo_gb300 import Lattice
+    from pspectcosmo_gb300.params import Params
+
+    p = Params.preheating(N=16, spectral=0, with_gw=1)
+    a, b = Lattice(p), Lattice(p)
+    a.initialize()
+    b.initialize()
+    a.evolve(0.005, 6)
+    for _ in range(6):
+        b.evolve(0.005, 1)
+    sa, sb = a.get_state(), b.get_state()
+    assert rel(sa["f_k"], sb["f_k"]) < 1e-13 and rel(sa["u_k"], sb["u_k"]) < 1e-13
