@@ -1,0 +1,313 @@
+"""Benchmark: site-steps/s of the pseudo-spectral lattice step on GB300.
+
+Workload (the configuration the headline metric is quoted on): 256^3 two-field
+preheating, V = m^2 phi^2/2 + g^2 phi^2 chi^2/2 with g^2 = 2.5e5, gravitational waves on
+(six u_ij, evolve_VV semantics), Yoshida-4, dt = 0.005, FP32 fields with FP64
+background and reductions. Synthetic data: the reference's own seeded initial
+conditions (seed 1), generated on the host. Every array is larger than the 129 MB L2
+(2 GB resident), so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--config preheat_gw_256|preheat_256|inflation_64] [--precision 32|64]
+
+One JSON line (rank 0). `value` is device-timed whole-job site-steps/s (inputs resident
+in HBM); `e2e` is the same metric through the C ABI with host buffers, the state copied
+host->device before the steps and device->host after them, and the background read
+back after every step. `--impl reference` times the CPU restatement of the reference's
+FP64 path (oracle/port) on this machine's host cores.
+Multi-GPU: independent replicas, one lattice per rank (the path does not shard); the
+timed region is bracketed by barriers and the max over ranks is reported.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIGS = {
+    # name: (Params factory kwargs, dt, description)
+    "preheat_gw_256": (dict(kind="preheating", N=256, spectral=0, with_gw=1, vv=4), 0.005,
+                       "256^3 two-field preheating + GW, Yoshida-4"),
+    "preheat_256": (dict(kind="preheating", N=256, spectral=1, with_gw=0, vv=4), 0.005,
+                    "256^3 two-field preheating (spectral path, no GW), Yoshida-4"),
+    "inflation_64": (dict(kind="default", N=64, vv=2), 0.002, "64^3 single-field inflation, velocity Verlet"),
+}
+
+# algorithmic HBM bytes per site-step of the fused dataflow: per stage and field 9C + 2R,
+# GW 36C + 12R (C = P (1 + 2/N) per site for a half-spectrum complex array, R = P)
+def algorithmic_bytes_per_site_step(p) -> float:
+    P = 4 if p.precision == 32 else 8
+    C = P * (1 + 2 / p.N)
+    R = P
+    per_stage = p.nflds * (9 * C + 2 * R) + (36 * C + 12 * R if p.with_gw else 0)
+    return p.stages * per_stage
+
+
+def make_params(name: str, precision: int):
+    from pspectcosmo_gb300.params import Params
+
+    kw, dt, desc = CONFIGS[name]
+    kw = dict(kw)
+    kind = kw.pop("kind")
+    p = Params.preheating(**kw) if kind == "preheating" else Params.reference_default(**kw)
+    p.precision = precision
+    return p, dt, desc
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+        self._t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self._t:
+            self._t.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        return world, rank, local, dist
+    return 1, 0, 0, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, value: float) -> float:
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], device="cuda" if torch.cuda.is_available() else "cpu", dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample(p, dt, budget_s: float = 20.0, threads: int | None = None) -> dict:
+    """The CPU restatement of the reference's FP64 path (oracle/port) on this host:
+    as many Yoshida stages of the same lattice as fit in ~budget_s."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle", "port"))
+    import oracle
+
+    oracle.build()
+    q = p.copy()
+    q.precision = 64
+    threads = threads or os.cpu_count()
+    o = oracle.Oracle(q, threads=threads)
+    o.init_ic()
+    s = o.stages
+    o.step_stages(dt, 1)  # warm-up (page faults, twiddles)
+    done, t0 = 0, time.perf_counter()
+    while True:
+        o.step_stages(dt, 1)
+        done += 1
+        el = time.perf_counter() - t0
+        if el > budget_s or done >= 3 * s:
+            break
+    per_step = el / done * s
+    return {"value": p.sites / per_step, "unit": "site-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{done} Yoshida stage(s) of the {p.N}^3 lattice ({s} per step) in {el:.1f} s, FP64 "
+                      f"restatement (oracle/port) with {threads} threads"}
+
+
+def run_reference(args):
+    world, rank, local, dist = dist_setup()
+    if rank != 0:
+        return
+    p, dt, desc = make_params(args.config, args.precision)
+    budget = max(5.0, min(120.0, 8.0 * args.steps))
+    cs = cpu_sample(p, dt, budget_s=budget)
+    line = {"impl": "reference", "metric": "site-steps/s", "value": cs["value"], "unit": "site-steps/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (reference seeded ICs)",
+            "config": {"workload": desc, "N": p.N, "nflds": p.nflds, "gw": bool(p.with_gw), "vv": p.vv,
+                       "dt": dt, "parallelism": "cpu threads"},
+            "cpu_baseline": cs,
+            "e2e": {"value": cs["value"], "unit": "site-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    world, rank, local, dist = dist_setup()
+    from pspectcosmo_gb300 import Lattice, build
+    from pspectcosmo_gb300.params import Params  # noqa: F401
+
+    build.build()
+    p, dt, desc = make_params(args.config, args.precision)
+    lat = Lattice(p)
+    lat.initialize()
+    st0 = lat.get_state()   # host copy of the initial state (e2e input)
+    # warm-up (graph build, first launches)
+    lat.evolve(dt, args.warmup)
+    lat.set_state(st0["f_k"], st0["pi_k"], st0["a"], st0["ad"], st0["add"], st0["u_k"], st0["pi_u_k"])
+
+    clocks = ClockSampler(local)
+    barrier(dist)
+    clocks.start()
+    barrier(dist)
+    lat.evolve(dt, args.steps)     # device-timed with CUDA events on the lattice's stream
+    barrier(dist)
+    ms = max_over_ranks(dist, lat.last_step_ms())
+    clk = clocks.stop()
+    value = world * p.sites * args.steps / (ms / 1e3)
+
+    # end to end through the C ABI with host buffers
+    import numpy as np  # noqa: F401
+
+    barrier(dist)
+    t0 = time.perf_counter()
+    lat.set_state(st0["f_k"], st0["pi_k"], st0["a"], st0["ad"], st0["add"], st0["u_k"], st0["pi_u_k"])
+    for _ in range(args.steps):
+        lat.evolve(dt, 1)
+        lat.background()
+    out = lat.get_state()
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+    e2e_value = world * p.sites * args.steps / e2e_s
+    csize = 8 if p.precision == 32 else 16
+    state_arrays = 2 * p.nflds + (12 if p.with_gw else 0)
+    state_bytes_host = state_arrays * p.modes * 16   # host buffers are FP64 complex
+    h2d = state_bytes_host / args.steps + 8
+    d2h = state_bytes_host / args.steps + 3 * 8 + 4 + 8
+
+    # per-pass device times and roofline of the dominant pass
+    passes = lat.time_passes(reps=3)
+    pbytes = lat.pass_bytes()
+    peak, peak_kind = measured_peaks()
+    dom = max((k for k in passes if k != "background"), key=lambda k: passes[k])
+    achieved = pbytes[dom] / (passes[dom] / 1e3) / 1e9
+    step_alg = algorithmic_bytes_per_site_step(p) * p.sites
+    step_achieved = step_alg / (ms / 1e3 / args.steps) / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(prof):
+        try:
+            with open(prof) as fh:
+                traffic = json.load(fh).get(f"{args.config}:{dom}")
+        except Exception:
+            traffic = None
+
+    launches_per_stage = 6
+    gpu_launches = 1 + 7 + p.stages * launches_per_stage * args.steps
+
+    if rank == 0:
+        cpu = cpu_sample(p, dt, budget_s=20.0) if (world == 1 and not args.no_cpu) else None
+        line = {
+            "metric": "site-steps/s", "value": value, "unit": "site-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if p.precision == 32 else "f64",
+            "data": "synthetic (reference seeded initial conditions, seed 1)",
+            "config": {"workload": desc, "N": p.N, "nflds": p.nflds, "gw": bool(p.with_gw), "vv": p.vv, "dt": dt,
+                       "precision": f"fp{p.precision} fields, fp64 background/reductions",
+                       "parallelism": f"replicas x{world}" if world > 1 else "single lattice",
+                       "l2": "arrays > 129 MB L2 (no flush needed)"},
+            "e2e": {"value": e2e_value, "unit": "site-steps/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                         "bytes_per_launch": pbytes[dom], "ms_per_launch": passes[dom],
+                         "step": {"algorithmic_bytes_per_site_step": algorithmic_bytes_per_site_step(p),
+                                  "achieved": step_achieved, "frac": step_achieved / peak}},
+            "passes_ms": passes,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": gpu_launches,
+        }
+        print(json.dumps(line), flush=True)
+    lat.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="preheat_gw_256", choices=sorted(CONFIGS))
+    ap.add_argument("--precision", type=int, default=32, choices=[32, 64])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -142,6 +142,19 @@ int psc_means(psc_handle *h, double *out);
 /* Device-time of the last psc_step call (CUDA events on the handle's stream), ms. */
 int psc_last_step_ms(psc_handle *h, float *ms);
 
+/* Per-pass device times of one stage (no reference counterpart; the measurement
+ * hook of the benchmark): runs `reps` force evaluations of the current state with
+ * CUDA events between the kernels on the handle's stream and writes the average
+ * milliseconds of [X inverse pass, Y inverse pass, fused Z pass, Y forward pass,
+ * X forward pass + kick, background update] to ms[0..5]. The state is left as
+ * it was (the evaluations apply zero-length kicks). */
+#define PSC_NPASS 6
+int psc_time_passes(psc_handle *h, int reps, float *ms);
+
+/* Compulsory HBM bytes each of the PSC_NPASS passes moves per launch (the bytes
+ * of the arrays it must read and write once), for roofline accounting. */
+int psc_pass_bytes(psc_handle *h, double *bytes);
+
 const char *psc_strerror(int code);
 const char *psc_last_error(void);
 

@@ -45,6 +45,9 @@ def lib():
         L.orc_hubble_init.restype = ctypes.c_double
         L.orc_hubble_init.argtypes = [P]
         L.orc_step.argtypes = [P, ctypes.c_double]
+        L.orc_step_stages.argtypes = [P, ctypes.c_double, ctypes.c_int]
+        L.orc_stages.argtypes = [P]
+        L.orc_stages.restype = ctypes.c_int
         L.orc_get_bg.argtypes = [P, D, D, D, D]
         L.orc_set_bg.argtypes = [P, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double]
         L.orc_get_state_k.argtypes = [P, D, D, D, D]
@@ -108,6 +111,14 @@ class Oracle:
     def step(self, dt: float, nsteps: int = 1):
         for _ in range(nsteps):
             lib().orc_step(self._h, dt)
+
+    def step_stages(self, dt: float, nstages: int):
+        """Timing sample: the first nstages stages of one step."""
+        lib().orc_step_stages(self._h, dt, nstages)
+
+    @property
+    def stages(self) -> int:
+        return lib().orc_stages(self._h)
 
     def bg(self) -> dict:
         v = [ctypes.c_double() for _ in range(4)]

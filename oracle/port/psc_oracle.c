@@ -587,11 +587,11 @@ static void kernel_field_k(orc_state *s) {
 }
 
 /* evolve_VV_k_nopad, evolution.cpp:1131-1198 */
-static void step_spectral(orc_state *s, double dt) {
+static void step_spectral(orc_state *s, double dt, int nst) {
     const int nf = s->nf;
     const long m2 = 2 * s->modes;
     double b = s->ad, b_half, a_half, norm;
-    for (int p = 0; p < s->s; p++) {
+    for (int p = 0; p < nst; p++) {
         const double w = s->w[p];
         b_half = b + w * dt / 2. * s->add;
         for (int fld = 0; fld < nf; fld++) c2r_norm(s, s->f_k + m2 * fld, s->f + s->sites * fld);
@@ -699,11 +699,11 @@ static void kernel_gw(orc_state *s, int c, double *kern) {
 }
 
 /* evolve_VV, evolution.cpp:607-694 */
-static void step_real(orc_state *s, double dt) {
+static void step_real(orc_state *s, double dt, int nst) {
     const int nf = s->nf;
     const long n = s->sites;
     double b = s->ad, b_half, a_half, a_of_pi;
-    for (int p = 0; p < s->s; p++) {
+    for (int p = 0; p < nst; p++) {
         const double w = s->w[p];
         b_half = b + w * dt / 2. * s->add;
         for (int fld = 0; fld < nf; fld++) {
@@ -746,9 +746,17 @@ static void step_real(orc_state *s, double dt) {
 }
 
 void orc_step(orc_state *s, double dt) {
-    if (s->spectral) step_spectral(s, dt);
-    else step_real(s, dt);
+    if (s->spectral) step_spectral(s, dt, s->s);
+    else step_real(s, dt, s->s);
 }
+
+void orc_step_stages(orc_state *s, double dt, int nstages) {
+    if (nstages > s->s) nstages = s->s;
+    if (s->spectral) step_spectral(s, dt, nstages);
+    else step_real(s, dt, nstages);
+}
+
+int orc_stages(orc_state *s) { return s->s; }
 
 /* ---------------------------------------------------------------- state access */
 void orc_get_bg(orc_state *s, double *t, double *a, double *ad, double *add) {

@@ -28,6 +28,10 @@ double orc_hubble_init(orc_state *s);
 
 /* one step: evolve_VV_k_nopad (spectral) or evolve_VV (real space) */
 void orc_step(orc_state *s, double dt);
+/* the first nstages Yoshida stages of one step (a bounded CPU timing sample; the
+ * state afterwards is not a step boundary) */
+void orc_step_stages(orc_state *s, double dt, int nstages);
+int orc_stages(orc_state *s);
 
 /* background */
 void orc_get_bg(orc_state *s, double *t, double *a, double *ad, double *add);

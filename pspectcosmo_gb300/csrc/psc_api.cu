@@ -485,6 +485,49 @@ int psc_last_step_ms(psc_handle *h, float *ms) {
     return PSC_OK;
 }
 
+int psc_time_passes(psc_handle *h, int reps, float *ms) {
+    if (!h || !ms || reps < 1) return fail(PSC_ERR_ARG, "bad argument");
+    if (!h->have_state) return fail(PSC_ERR_STATE, "no state");
+    cudaEvent_t ev[7];
+    for (int i = 0; i < 7; ++i) CU(cudaEventCreate(&ev[i]));
+    double acc[PSC_NPASS] = {0, 0, 0, 0, 0, 0};
+    // zero-length kicks: the state is unchanged; a'' is kept (diagnostics mode)
+    for (int r = 0; r < reps; ++r) {
+        CU(psc::launch_scalar(h->cfg, h->b, psc::SCALAR_EVAL, 0, h->st));
+        CU(psc::launch_stage_timed(h->cfg, h->b, h->p.precision, 0, psc::SCALAR_EVAL_END, ev, h->st));
+        CU(cudaEventSynchronize(ev[6]));
+        for (int i = 0; i < PSC_NPASS; ++i) {
+            float t = 0.f;
+            CU(cudaEventElapsedTime(&t, ev[i], ev[i + 1]));
+            acc[i] += t;
+        }
+    }
+    for (int i = 0; i < 7; ++i) cudaEventDestroy(ev[i]);
+    for (int i = 0; i < PSC_NPASS; ++i) ms[i] = (float)(acc[i] / reps);
+    h->diag_valid = true;
+    return PSC_OK;
+}
+
+int psc_pass_bytes(psc_handle *h, double *bytes) {
+    if (!h || !bytes) return fail(PSC_ERR_ARG, "bad argument");
+    const psc::Geo &g = h->cfg.g;
+    const double C = (double)g.modes * h->csize, R = (double)g.sites * (h->csize / 2);
+    const int nf = g.nf, gw = g.gw;
+    (void)R;
+    // X inverse: read f_k, pi_half; write f_k, TA [, TB]
+    bytes[0] = nf * (4 + gw) * C;
+    // Y inverse: read TA [, TB]; write TA [, TB, TC]
+    bytes[1] = nf * (gw ? 5 : 2) * C;
+    // fused Z: read TA [, TB, TC]; write QV [, QS]
+    bytes[2] = (nf * (gw ? 3 : 1) + nf + (gw ? 6 : 0)) * C;
+    // Y forward: in place over QV [, QS]
+    bytes[3] = 2.0 * (nf + (gw ? 6 : 0)) * C;
+    // X forward + kick: read QV, f_k, pi; write pi [; read QS, u, pi_u; write u, pi_u]
+    bytes[4] = (4.0 * nf + (gw ? 6 * 5 : 0)) * C;
+    bytes[5] = 0.0;
+    return PSC_OK;
+}
+
 int psc_get_fields_real(psc_handle *h, double *f, double *pi_f) {
     if (!h) return fail(PSC_ERR_ARG, "null handle");
     const psc::Geo &g = h->cfg.g;

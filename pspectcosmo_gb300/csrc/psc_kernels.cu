@@ -742,34 +742,56 @@ cudaError_t configure(const LaunchCfg &cfg, int precision) {
 }
 
 template <typename T>
-static cudaError_t launch_stage_t(const LaunchCfg &cfg, const Buffers &b, int drift, cudaStream_t st) {
+static cudaError_t launch_stage_t(const LaunchCfg &cfg, const Buffers &b, int drift, cudaStream_t st,
+                                  cudaEvent_t *ev = nullptr, int scalar_mode = -1) {
     using C = cplx<T>;
     const Geo &g = cfg.g;
     const C *tw = reinterpret_cast<const C *>(b.tw);
     C *fk = (C *)b.fk, *pk = (C *)b.pk, *uk = (C *)b.uk, *puk = (C *)b.puk;
     C *TA = (C *)b.TA, *TB = (C *)b.TB, *TC = (C *)b.TC, *QV = (C *)b.QV, *QS = (C *)b.QS;
     const dim3 gx(cfg.nbx, g.nf);
+    auto mark = [&](int i) {
+        if (ev) cudaEventRecord(ev[i], st);
+    };
+    mark(0);
     if (g.gw) {
         if (drift) k_ifft_x<T, true, true><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
         else k_ifft_x<T, true, false><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
+        mark(1);
         k_ifft_y<T, true><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, TA, TB, TC, b.bg, tw);
+        mark(2);
         k_zpass<T, true><<<cfg.nbz, cfg.thr_z, cfg.smem_z, st>>>(g, TA, TB, TC, QV, QS, b.partV, b.bg, tw);
     } else {
         if (drift) k_ifft_x<T, false, true><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
         else k_ifft_x<T, false, false><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
+        mark(1);
         k_ifft_y<T, false><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, TA, TB, TC, b.bg, tw);
+        mark(2);
         k_zpass<T, false><<<cfg.nbz, cfg.thr_z, cfg.smem_z, st>>>(g, TA, TB, TC, QV, QS, b.partV, b.bg, tw);
     }
+    mark(3);
     ArrList al{};
     int nj = 0;
     for (int f = 0; f < g.nf; ++f) al.p[nj++] = QV + (long long)f * g.modes;
     if (g.gw)
         for (int c = 0; c < 6; ++c) al.p[nj++] = QS + (long long)c * g.modes;
     k_fft_y<T><<<dim3(cfg.nbx, nj), cfg.thr_xy, cfg.smem_xy, st>>>(g, al, tw);
+    mark(4);
     const dim3 gf(cfg.nbx, nj);
     if (g.gw) k_fft_x_final<T, true><<<gf, cfg.thr_xy, cfg.smem_xy, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw);
     else k_fft_x_final<T, false><<<gf, cfg.thr_xy, cfg.smem_xy, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw);
+    mark(5);
+    if (scalar_mode >= 0) {
+        k_scalar<<<1, 512, 0, st>>>(b.bg, b.partKG, b.partV, scalar_mode, 1);
+        mark(6);
+    }
     return cudaGetLastError();
+}
+
+cudaError_t launch_stage_timed(const LaunchCfg &cfg, const Buffers &b, int precision, int drift, int scalar_mode,
+                               cudaEvent_t *ev, cudaStream_t st) {
+    return precision == 32 ? launch_stage_t<float>(cfg, b, drift, st, ev, scalar_mode)
+                           : launch_stage_t<double>(cfg, b, drift, st, ev, scalar_mode);
 }
 
 cudaError_t launch_stage(const LaunchCfg &cfg, const Buffers &b, int precision, int drift, cudaStream_t st) {

@@ -65,6 +65,10 @@ cudaError_t configure(const LaunchCfg &cfg, int precision);
 // Y-iFFT, fused Z pass (c2r, V' and anisotropic stress, r2c), Y-fFFT and the
 // X-fFFT with the kick epilogue and the K, G reductions.
 cudaError_t launch_stage(const LaunchCfg &cfg, const Buffers &b, int precision, int drift, cudaStream_t st);
+// The same sequence with an event recorded after each pass (ev[0] before the
+// first, ev[i + 1] after pass i; 5 passes + the scalar kernel of `scalar_mode`).
+cudaError_t launch_stage_timed(const LaunchCfg &cfg, const Buffers &b, int precision, int drift, int scalar_mode,
+                               cudaEvent_t *ev, cudaStream_t st);
 cudaError_t launch_scalar(const LaunchCfg &cfg, const Buffers &b, int mode, int p, cudaStream_t st);
 cudaError_t launch_set_run(DevBG *bg, double dt, int nsteps, cudaStream_t st);
 // Real-space view of nsrc complex arrays (c2r / N^3) into b.real (precision T).

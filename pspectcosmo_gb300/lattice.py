@@ -77,13 +77,15 @@ def load_library(path: str | None = None):
     L.psc_energies.argtypes = [P, D, D, D, D, D, D]
     L.psc_means.argtypes = [P, D]
     L.psc_last_step_ms.argtypes = [P, ctypes.POINTER(ctypes.c_float)]
+    L.psc_time_passes.argtypes = [P, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
+    L.psc_pass_bytes.argtypes = [P, D]
     L.psc_strerror.argtypes = [ctypes.c_int]
     L.psc_strerror.restype = ctypes.c_char_p
     L.psc_last_error.argtypes = []
     L.psc_last_error.restype = ctypes.c_char_p
     for name in ("psc_create", "psc_init_ic", "psc_generate_ic", "psc_set_state", "psc_get_state", "psc_get_time",
                  "psc_set_time", "psc_step", "psc_get_fields_real", "psc_maxnumbins", "psc_spectra", "psc_energies",
-                 "psc_means", "psc_last_step_ms"):
+                 "psc_means", "psc_last_step_ms", "psc_time_passes", "psc_pass_bytes"):
         getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L
@@ -189,6 +191,20 @@ class Lattice:
         v = ctypes.c_float()
         _check(self._L.psc_last_step_ms(self._h, ctypes.byref(v)), "psc_last_step_ms")
         return v.value
+
+    PASS_NAMES = ("ifft_x", "ifft_y", "zpass", "fft_y", "fft_x_kick", "background")
+
+    def time_passes(self, reps: int = 5) -> dict:
+        """Average device ms of each pass of one stage (CUDA events on the lattice's stream)."""
+        ms = (ctypes.c_float * 6)()
+        _check(self._L.psc_time_passes(self._h, int(reps), ms), "psc_time_passes")
+        return dict(zip(self.PASS_NAMES, [float(x) for x in ms]))
+
+    def pass_bytes(self) -> dict:
+        """Compulsory HBM bytes per launch of each pass."""
+        b = np.zeros(6)
+        _check(self._L.psc_pass_bytes(self._h, _dp(b)), "psc_pass_bytes")
+        return dict(zip(self.PASS_NAMES, b.tolist()))
 
     # -- outputs --------------------------------------------------------------
     def fields_real(self):
