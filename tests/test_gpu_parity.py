@@ -8,7 +8,8 @@ rounding floor of ~eps * phi0 / dphi ~ 1e-9 per step that the k-space state does
 have. FP32 device path (measured tolerances, written here so a regression shows):
 fields within 2e-4 relative of the oracle, a and a' within 1e-6, a'' within 1e-4
 (a'' = (fStar/MPl)^2 a (V - 2K)/3 cancels), P_f and P_pi within 1e-3, the occupation
-number n_k (|a^(alpha-3) pi + H f|^2 cancels for vacuum modes) within 5e-3."""
+number n_k (|a^(alpha-3) pi + H f|^2 cancels for vacuum modes) within 1e-2; on the
+real-space path n_k is compared at 1e-6 for the same reason."""
 import numpy as np
 import pytest
 
@@ -21,10 +22,11 @@ RUNS = ["spec1_n16", "spec1_n16_vv6", "spec1_n32_vv4", "spec1_n64_dt1e-4", "spec
 
 FP32_FIELD_TOL = 2e-4
 FP32_SPEC_TOL = 1e-3
-FP32_NK_TOL = 5e-3
+FP32_NK_TOL = 1e-2
 FP32_BG_TOL = 1e-6
 FP32_ADD_TOL = 1e-4
 REALSPACE_SPEC_TOL = 1e-7
+REALSPACE_NK_TOL = 1e-6
 
 
 def _pair(oracle_mod, run, precision):
@@ -79,7 +81,10 @@ def test_fp64_matches_oracle(oracle_mod, run):
     lat.evolve(meta["dt"], meta["nsteps"])
     o.step(meta["dt"], meta["nsteps"])
     _compare_state(lat, o, p, 1e-10, 1e-12)
-    _compare_outputs(lat, o, p, 1e-10 if p.spectral else REALSPACE_SPEC_TOL)
+    if p.spectral:
+        _compare_outputs(lat, o, p, 1e-10)
+    else:
+        _compare_outputs(lat, o, p, REALSPACE_SPEC_TOL, REALSPACE_NK_TOL)
     assert abs(lat.t - meta["nsteps"] * meta["dt"]) < 1e-12
 
 
