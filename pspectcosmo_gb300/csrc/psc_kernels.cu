@@ -689,9 +689,31 @@ void plan(const psc_params &p, LaunchCfg *cfg) {
     g.lines_z = g.N * g.N;
     g.modes = (long long)g.N * g.N * g.H;
     g.sites = (long long)g.N * g.N * g.N;
+    g.reg = g.N >= 32 ? 1 : 0;
     const int csize = p.precision == 32 ? 8 : 16;
-    // X/Y passes: a tile of TL lines x N elements, two ping-pong buffers of
-    // <= 32 KiB each (TL >= 8 keeps the strided rows at >= 64 B).
+    const int nin = g.nf * (g.gw ? 4 : 1), nout = g.nf + (g.gw ? 6 : 0);
+    const int nslot = nin > nout ? nin : nout;
+    if (g.reg) {
+        // register engine: P = L/16 threads per line, 256 threads per block
+        const int P = g.N / 16;
+        int tl = 256 / P;
+        while (tl > 1 && tl / 2 >= g.lines_x) tl /= 2;
+        g.tlx_shift = ilog2i(tl);
+        cfg->thr_xy = tl * P;
+        cfg->smem_xy = (size_t)tl * g.N * csize;
+        cfg->nbx = (g.lines_x + tl - 1) / tl;
+        const int Pz = g.M / 16;
+        int tlz = 256 / (nin * Pz);
+        if (tlz < 1) tlz = 1;
+        g.tlz_shift = ilog2i(tlz);
+        g.ldz = 0;
+        cfg->thr_z = nin * tlz * Pz;
+        cfg->smem_z = (size_t)nslot * tlz * (g.M + g.M / 16) * csize;
+        cfg->nbz = (g.lines_z + tlz - 1) / tlz;
+        return;
+    }
+    // generic engine: a tile of TL lines x N elements, two ping-pong buffers of
+    // <= 32 KiB each
     int tl = (32768 / csize) / g.N;
     if (tl < 4) tl = 4;
     if (tl > 256) tl = 256;
@@ -701,8 +723,6 @@ void plan(const psc_params &p, LaunchCfg *cfg) {
     cfg->smem_xy = (size_t)2 * tl * g.N * csize;
     cfg->nbx = (g.lines_x + tl - 1) / tl;
     // Z pass: TLz lines, two H-row buffers + nslot M-row real-line slots.
-    const int nin = g.nf * (g.gw ? 4 : 1), nout = g.nf + (g.gw ? 6 : 0);
-    const int nslot = nin > nout ? nin : nout;
     int tlz = 32;
     auto zbytes = [&](int t) { return (size_t)(t + 1) * (2 * g.H + nslot * g.M) * csize; };
     while (tlz > 1 && zbytes(tlz) > 100 * 1024) tlz /= 2;
@@ -738,6 +758,7 @@ static cudaError_t configure_t(const LaunchCfg &cfg) {
 }
 
 cudaError_t configure(const LaunchCfg &cfg, int precision) {
+    if (cfg.g.reg) return precision == 32 ? reg_configure_f32(cfg) : reg_configure_f64(cfg);
     return precision == 32 ? configure_t<float>(cfg) : configure_t<double>(cfg);
 }
 
@@ -790,11 +811,17 @@ static cudaError_t launch_stage_t(const LaunchCfg &cfg, const Buffers &b, int dr
 
 cudaError_t launch_stage_timed(const LaunchCfg &cfg, const Buffers &b, int precision, int drift, int scalar_mode,
                                cudaEvent_t *ev, cudaStream_t st) {
+    if (cfg.g.reg)
+        return precision == 32 ? reg_stage_f32(cfg, b, drift, st, ev, scalar_mode)
+                               : reg_stage_f64(cfg, b, drift, st, ev, scalar_mode);
     return precision == 32 ? launch_stage_t<float>(cfg, b, drift, st, ev, scalar_mode)
                            : launch_stage_t<double>(cfg, b, drift, st, ev, scalar_mode);
 }
 
 cudaError_t launch_stage(const LaunchCfg &cfg, const Buffers &b, int precision, int drift, cudaStream_t st) {
+    if (cfg.g.reg)
+        return precision == 32 ? reg_stage_f32(cfg, b, drift, st, nullptr, -1)
+                               : reg_stage_f64(cfg, b, drift, st, nullptr, -1);
     return precision == 32 ? launch_stage_t<float>(cfg, b, drift, st) : launch_stage_t<double>(cfg, b, drift, st);
 }
 
@@ -831,6 +858,8 @@ static cudaError_t launch_c2r_real_t(const LaunchCfg &cfg, const Buffers &b, con
 
 cudaError_t launch_c2r_real(const LaunchCfg &cfg, const Buffers &b, int precision, const void *src, int nsrc,
                             cudaStream_t st) {
+    if (cfg.g.reg)
+        return precision == 32 ? reg_c2r_real_f32(cfg, b, src, nsrc, st) : reg_c2r_real_f64(cfg, b, src, nsrc, st);
     return precision == 32 ? launch_c2r_real_t<float>(cfg, b, src, nsrc, st)
                            : launch_c2r_real_t<double>(cfg, b, src, nsrc, st);
 }

@@ -16,6 +16,7 @@ struct Geo {
     int N, H, M;                 // edge, half-spectrum length N/2+1, N/2
     int nf, gw, nterms, mask;    // fields, GW flag, potential terms, R_Q2C mask on
     int model;                   // PSC_MODEL_*
+    int reg;                     // 1: register-engine passes (N >= 32), 0: generic shared-memory engine
     int tlx_shift, tlz_shift;    // log2 lines per tile: X/Y passes, Z pass
     int ldz;                     // shared-memory leading dimension of the Z pass (lines + 1)
     int lines_x;                 // N * H  (X-pass and Y-pass line count per array)
@@ -78,5 +79,15 @@ cudaError_t launch_c2r_real(const LaunchCfg &cfg, const Buffers &b, int precisio
 // (output.cpp:780-1025). Layout of b.spec: [nf][3][nb] then GW [2][nb];
 // b.spec_cnt: [nf][nb] then GW [nb]. Zeroes the accumulators first.
 cudaError_t launch_spectra(const LaunchCfg &cfg, const Buffers &b, int precision, int nb, cudaStream_t st);
+
+// Register-engine passes (psc_reg_f32.cu, psc_reg_f64.cu), N = 32..1024.
+cudaError_t reg_configure_f32(const LaunchCfg &cfg);
+cudaError_t reg_configure_f64(const LaunchCfg &cfg);
+cudaError_t reg_stage_f32(const LaunchCfg &cfg, const Buffers &b, int drift, cudaStream_t st, cudaEvent_t *ev,
+                          int scalar_mode);
+cudaError_t reg_stage_f64(const LaunchCfg &cfg, const Buffers &b, int drift, cudaStream_t st, cudaEvent_t *ev,
+                          int scalar_mode);
+cudaError_t reg_c2r_real_f32(const LaunchCfg &cfg, const Buffers &b, const void *src, int nsrc, cudaStream_t st);
+cudaError_t reg_c2r_real_f64(const LaunchCfg &cfg, const Buffers &b, const void *src, int nsrc, cudaStream_t st);
 
 }  // namespace psc

@@ -1,0 +1,465 @@
+// psc_passes.cuh — the pass kernels on the register-resident FFT engine
+// (psc_fftreg.cuh), templated on precision T and line length L. Used for
+// N >= 32; the generic shared-memory engine of psc_kernels.cu covers N = 8, 16.
+//
+// Thread layout of the X/Y passes (strided lines): TL lines x P = L/16 threads,
+// t fastest, so each of a thread's 16 loads is one coalesced TL-wide row.
+// Thread layout of the Z pass (contiguous lines): (input, line, j) with j
+// fastest, so consecutive threads read consecutive kz of one line; all inputs
+// of a tile are transformed at the same time and meet in shared memory for the
+// pointwise epilogue.
+#pragma once
+
+#include "psc_fftreg.cuh"
+#include "psc_launch.h"
+
+namespace psc {
+
+// ------------------------------------------------------------------ X inverse (+ drift, + x-derivative)
+template <typename T, int L, bool GW, bool DRIFT>
+__global__ void __launch_bounds__(256) kr_ifft_x(Geo g, cplx<T> *__restrict__ fk, const cplx<T> *__restrict__ pk,
+                                                 cplx<T> *__restrict__ TA, cplx<T> *__restrict__ TB,
+                                                 const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw) {
+    using C = cplx<T>;
+    using RP = RegPlan<L>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *sm = reinterpret_cast<C *>(smem_raw);
+    const int sh = g.tlx_shift, TL = 1 << sh;
+    const int t = threadIdx.x & (TL - 1), j = threadIdx.x >> sh;
+    const int line = blockIdx.x * TL + t;
+    const bool valid = line < g.lines_x;
+    const long long stride = g.lines_x;
+    const long long base = (long long)blockIdx.y * g.modes + line;
+    auto ix = [&](int n) { return n * TL + t; };
+    const T c = DRIFT ? (T)bg->c_drift : T(0);
+    C v[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+        const long long a = base + (long long)(j + r * RP::P) * stride;
+        C x = mk<T>(0, 0);
+        if (valid) {
+            x = fk[a];
+            if (DRIFT) {
+                const C p = pk[a];
+                x.x += c * p.x;
+                x.y += c * p.y;
+                fk[a] = x;
+            }
+        }
+        v[r] = x;
+    }
+    fft_reg<C, L, +1>(v, sm, ix, j, tw, g.N / L);
+    if (valid) {
+#pragma unroll
+        for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+            for (int r = 0; r < RP::RL; ++r) TA[base + (long long)RP::out(j, q, r) * stride] = v[q * RP::RL + r];
+    }
+    if (GW) {
+        __syncthreads();
+        const T kIR = (T)bg->kIR;
+#pragma unroll
+        for (int r = 0; r < 16; ++r) {
+            const int n = j + r * RP::P;
+            C x = mk<T>(0, 0);
+            if (valid) {
+                const C f = fk[base + (long long)n * stride];
+                const T kx = (n == (g.N >> 1)) ? T(0) : kIR * (T)pcoord(n, g.N);
+                x = mk<T>(-kx * f.y, kx * f.x);
+            }
+            v[r] = x;
+        }
+        fft_reg<C, L, +1>(v, sm, ix, j, tw, g.N / L);
+        if (valid) {
+#pragma unroll
+            for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+                for (int r = 0; r < RP::RL; ++r) TB[base + (long long)RP::out(j, q, r) * stride] = v[q * RP::RL + r];
+        }
+    }
+}
+
+// ------------------------------------------------------------------ Y passes
+// One transform of a tile of Y lines (l = x H + kz, element y at (x N + y) H + kz):
+// src -> dst (may alias), optional i k_y multiplier. Ends with a barrier.
+template <typename T, int L, int DIR>
+__device__ __forceinline__ void ry_tile(const Geo &g, const cplx<T> *src, cplx<T> *dst, bool deriv, T kIR, cplx<T> *sm,
+                                        const cplx<T> *__restrict__ tw) {
+    using C = cplx<T>;
+    using RP = RegPlan<L>;
+    const int sh = g.tlx_shift, TL = 1 << sh;
+    const int t = threadIdx.x & (TL - 1), j = threadIdx.x >> sh;
+    const int line = blockIdx.x * TL + t;
+    const bool valid = line < g.lines_x;
+    const int x = line / g.H, kz = line - x * g.H;
+    const long long base = (long long)x * g.N * g.H + kz;
+    const long long stride = g.H;
+    auto ix = [&](int n) { return n * TL + t; };
+    C v[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+        const int n = j + r * RP::P;
+        C a = mk<T>(0, 0);
+        if (valid) {
+            a = src[base + (long long)n * stride];
+            if (deriv) {
+                const T ky = (n == (g.N >> 1)) ? T(0) : kIR * (T)pcoord(n, g.N);
+                a = mk<T>(-ky * a.y, ky * a.x);
+            }
+        }
+        v[r] = a;
+    }
+    fft_reg<C, L, DIR>(v, sm, ix, j, tw, g.N / L);
+    if (valid) {
+#pragma unroll
+        for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+            for (int r = 0; r < RP::RL; ++r) dst[base + (long long)RP::out(j, q, r) * stride] = v[q * RP::RL + r];
+    }
+    __syncthreads();
+}
+
+template <typename T, int L, bool GW>
+__global__ void __launch_bounds__(256) kr_ifft_y(Geo g, cplx<T> *__restrict__ TA, cplx<T> *__restrict__ TB,
+                                                 cplx<T> *__restrict__ TC, const DevBG *__restrict__ bg,
+                                                 const cplx<T> *__restrict__ tw) {
+    using C = cplx<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *sm = reinterpret_cast<C *>(smem_raw);
+    const long long off = (long long)blockIdx.y * g.modes;
+    const T kIR = (T)bg->kIR;
+    if (GW) {
+        // the y-derivative reads TA before TA is transformed in place
+        ry_tile<T, L, +1>(g, TA + off, TC + off, true, kIR, sm, tw);
+        ry_tile<T, L, +1>(g, TA + off, TA + off, false, kIR, sm, tw);
+        ry_tile<T, L, +1>(g, TB + off, TB + off, false, kIR, sm, tw);
+    } else {
+        ry_tile<T, L, +1>(g, TA + off, TA + off, false, kIR, sm, tw);
+    }
+}
+
+struct ArrList8 {
+    void *p[8];
+};
+
+template <typename T, int L>
+__global__ void __launch_bounds__(256) kr_fft_y(Geo g, ArrList8 arrs, const cplx<T> *__restrict__ tw) {
+    using C = cplx<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *sm = reinterpret_cast<C *>(smem_raw);
+    C *a = reinterpret_cast<C *>(arrs.p[blockIdx.y]);
+    ry_tile<T, L, -1>(g, a, a, false, T(0), sm, tw);
+}
+
+// ------------------------------------------------------------------ X forward + kick epilogue
+template <typename T, int L, bool GW>
+__global__ void __launch_bounds__(256) kr_fft_x_final(Geo g, const cplx<T> *__restrict__ QV,
+                                                      const cplx<T> *__restrict__ QS, const cplx<T> *__restrict__ fk,
+                                                      cplx<T> *__restrict__ pk, cplx<T> *__restrict__ uk,
+                                                      cplx<T> *__restrict__ puk, double *__restrict__ partKG,
+                                                      const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw) {
+    using C = cplx<T>;
+    using RP = RegPlan<L>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *sm = reinterpret_cast<C *>(smem_raw);
+    const int sh = g.tlx_shift, TL = 1 << sh, N = g.N, H = g.H, M = g.M;
+    const int t = threadIdx.x & (TL - 1), j = threadIdx.x >> sh;
+    const int line = blockIdx.x * TL + t;
+    const bool valid = line < g.lines_x;
+    const int job = blockIdx.y;
+    const bool field = job < g.nf;
+    const long long off = (long long)(field ? job : job - g.nf) * g.modes;
+    const C *src = (field ? QV : QS) + off;
+    const long long stride = g.lines_x;
+    const long long base = off + line;
+    auto ix = [&](int n) { return n * TL + t; };
+    C v[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r)
+        v[r] = valid ? src[(long long)(j + r * RP::P) * stride + line] : mk<T>(0, 0);
+    fft_reg<C, L, -1>(v, sm, ix, j, tw, N / L);
+
+    const T norm1 = (T)bg->norm1, norm2 = (T)bg->norm2, kIR2 = (T)bg->kIR2;
+    const T c_close = (T)bg->c_close, c_open = (T)bg->c_open;
+    const int y = line / H, kz = line - y * H;
+    const int py = pcoord(y, N);
+    if (field) {
+        double accK = 0.0, accG = 0.0;
+        if (valid) {
+            const bool mask = g.mask != 0;
+            const T hub = (T)bg->hub, apow = (T)bg->apow, a3 = (T)bg->a3;
+            const T dfdp = (T)bg->DFDP, eps = (T)bg->eps;
+            const double wgt = (kz == 0 || kz == M) ? 1.0 : 2.0;
+#pragma unroll
+            for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+                for (int r = 0; r < RP::RL; ++r) {
+                    const int n = RP::out(j, q, r);
+                    const int px = pcoord(n, N);
+                    const T k2 = (T)(px * px + py * py + kz * kz);
+                    const long long a = base + (long long)n * stride;
+                    const C f = fk[a], p = pk[a], qv = v[q * RP::RL + r];
+                    // force (evolution.cpp:1124-1125)
+                    const T fl = -norm1 * kIR2 * k2;
+                    const C F = mk<T>(fl * f.x - norm2 * qv.x, fl * f.y - norm2 * qv.y);
+                    const C pf = mk<T>(p.x + c_close * F.x, p.y + c_close * F.y);
+                    bool inc = true;
+                    if (mask && (n | line) != 0) {
+                        // R_Q2C (evolution.cpp:1038-1056) with the stale a' of the step
+                        const T fm = sqrt(f.x * f.x + f.y * f.y);
+                        const T gx = hub * f.x + apow * pf.x, gy = hub * f.y + apow * pf.y;
+                        const T R = dfdp / (fm * a3 * sqrt(gx * gx + gy * gy));
+                        inc = R < eps;
+                    }
+                    if (inc) {
+                        accK += wgt * ((double)pf.x * pf.x + (double)pf.y * pf.y);
+                        accG += wgt * (double)k2 * ((double)f.x * f.x + (double)f.y * f.y);
+                    }
+                    pk[a] = mk<T>(pf.x + c_open * F.x, pf.y + c_open * F.y);
+                }
+        }
+        double vals[2] = {accK, accG};
+        block_reduce_store<2>(vals, partKG + (size_t)(2 * job) * gridDim.x, gridDim.x, blockIdx.x);
+    } else if (GW && valid) {
+        const T c_drift = (T)bg->c_drift;
+#pragma unroll
+        for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+            for (int r = 0; r < RP::RL; ++r) {
+                const int n = RP::out(j, q, r);
+                const int px = pcoord(n, N);
+                const T k2 = (T)(px * px + py * py + kz * kz);
+                const long long a = base + (long long)n * stride;
+                C u = uk[a];
+                const C w = puk[a], qv = v[q * RP::RL + r];
+                // drift of u_ij deferred from the stage prologue (evolution.cpp:655-662)
+                u.x += c_drift * w.x;
+                u.y += c_drift * w.y;
+                // a^(1+alpha) (lapl u + 2 sum d_i f d_j f)  (evolution.cpp:586-598)
+                const T l = -kIR2 * k2;
+                const C F = mk<T>(norm1 * (l * u.x + qv.x), norm1 * (l * u.y + qv.y));
+                const C wf = mk<T>(w.x + c_close * F.x, w.y + c_close * F.y);
+                uk[a] = u;
+                puk[a] = mk<T>(wf.x + c_open * F.x, wf.y + c_open * F.y);
+            }
+    }
+}
+
+// ------------------------------------------------------------------ fused Z pass
+// Shared memory: nslot real-line slots of TL lines x LS complex (a complex
+// element holds the real sites 2m, 2m+1), index t*LS + m + m/16 (the pad keeps
+// the radix-16 exchange free of bank conflicts).
+template <int L>
+struct ZIdx {
+    static constexpr int LS = L + L / 16;
+    int base;
+    __device__ __forceinline__ int operator()(int n) const { return base + n + (n >> 4); }
+};
+
+template <typename T, int L, bool GW>
+__global__ void __launch_bounds__(256) kr_zpass(Geo g, const cplx<T> *__restrict__ TA, const cplx<T> *__restrict__ TB,
+                                                const cplx<T> *__restrict__ TC, cplx<T> *__restrict__ QV,
+                                                cplx<T> *__restrict__ QS, double *__restrict__ partV,
+                                                const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw) {
+    using C = cplx<T>;
+    using RP = RegPlan<L>;
+    constexpr int M = L, P = RP::P, LS = ZIdx<L>::LS;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *slots = reinterpret_cast<C *>(smem_raw);
+    const int sh = g.tlz_shift, TL = 1 << sh, H = g.H, N = g.N;
+    const int nf = g.nf;
+    const int nin = nf * (GW ? 4 : 1);
+    const int nout = nf + (GW ? 6 : 0);
+    const int j = threadIdx.x % P;
+    const int t = (threadIdx.x / P) & (TL - 1);
+    const int grp = threadIdx.x / (P * TL);   // input handled by this thread in phase 1
+    const int line = blockIdx.x * TL + t;
+    const bool valid = line < g.lines_z;
+    const size_t slot_elems = (size_t)TL * LS;
+    const T inv_n3 = (T)bg->inv_n3;
+    const T kIR = (T)bg->kIR;
+
+    // 1. complex-to-real along z of input grp: pack X[k], X[M-k] into the
+    //    M-point transform Z[k] = (X[k] + conj X[M-k]) + i w^k (X[k] - conj X[M-k]),
+    //    w = e^{+2 pi i/N}; Im X[0] and Im X[M] are ignored, as a c2r does.
+    {
+        const int fld = GW ? (grp >> 2) : grp;
+        const int kind = GW ? (grp & 3) : 0;   // 0: f, 1: d/dx f, 2: d/dy f, 3: d/dz f
+        const C *src = (kind == 1 ? TB : (kind == 2 ? TC : TA)) + (long long)fld * g.modes + (long long)line * H;
+        C v[16];
+#pragma unroll
+        for (int r = 0; r < 16; ++r) {
+            const int k = j + r * P;
+            C x = mk<T>(0, 0), y = mk<T>(0, 0);
+            if (valid) {
+                x = src[k];
+                y = src[M - k];
+                if (kind == 3) {
+                    const T kx = kIR * (T)k;                           // k < M
+                    const T ky = (k == 0) ? T(0) : kIR * (T)(M - k);   // Nyquist zeroed
+                    x = mk<T>(-kx * x.y, kx * x.x);
+                    y = mk<T>(-ky * y.y, ky * y.x);
+                }
+            }
+            y.y = -y.y;
+            if (k == 0) { x.y = T(0); y.y = T(0); }
+            const C s = cadd(x, y), d = csub(x, y);
+            C w = __ldg(&tw[k]);
+            w.y = -w.y;
+            const C td = cmul(w, d);
+            v[r] = mk<T>(s.x - td.y, s.y + td.x);
+        }
+        const ZIdx<L> ix{(int)(grp * slot_elems + t * LS)};
+        fft_reg<C, L, +1>(v, slots, ix, j, tw, N / L);
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+            for (int r = 0; r < RP::RL; ++r) slots[ix(RP::out(j, q, r))] = cscale(v[q * RP::RL + r], inv_n3);
+    }
+    __syncthreads();
+
+    // 2. pointwise epilogue: V'(f), <V>, anisotropic stress
+    Model mdl;
+    mdl.kind = g.model;
+    mdl.gsq = g.gsq;
+    double pot[kMaxTerms] = {0.0, 0.0};
+    for (int idx = threadIdx.x; idx < TL * M; idx += blockDim.x) {
+        const int tt = idx / M, m = idx - tt * M;
+        if (blockIdx.x * TL + tt >= g.lines_z) continue;
+        const int e = tt * LS + m + (m >> 4);
+        C in[8];
+#pragma unroll
+        for (int o = 0; o < 8; ++o)
+            if (o < nin) in[o] = slots[o * slot_elems + e];
+        C out[8];
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            T f[2], vp[2];
+#pragma unroll
+            for (int fl = 0; fl < 2; ++fl) {
+                if (fl < nf) {
+                    const C c = in[GW ? fl * 4 : fl];
+                    f[fl] = half ? c.y : c.x;
+                } else {
+                    f[fl] = T(0);
+                }
+            }
+            model_dvdf<T>(mdl, f, vp, nf);
+            model_potential<T>(mdl, f, pot);
+#pragma unroll
+            for (int fl = 0; fl < 2; ++fl)
+                if (fl < nf) { if (half) out[fl].y = vp[fl]; else out[fl].x = vp[fl]; }
+            if (GW) {
+                T d[2][3];
+#pragma unroll
+                for (int fl = 0; fl < 2; ++fl)
+#pragma unroll
+                    for (int ax = 0; ax < 3; ++ax)
+                        d[fl][ax] = (fl < nf) ? (half ? in[fl * 4 + 1 + ax].y : in[fl * 4 + 1 + ax].x) : T(0);
+                const int si[6] = {0, 0, 0, 1, 1, 2}, sj[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+                for (int c = 0; c < 6; ++c) {
+                    T sum = T(0);
+#pragma unroll
+                    for (int fl = 0; fl < 2; ++fl)
+                        if (fl < nf) sum += T(2) * d[fl][si[c]] * d[fl][sj[c]];
+                    if (half) out[nf + c].y = sum; else out[nf + c].x = sum;
+                }
+            }
+        }
+#pragma unroll
+        for (int o = 0; o < 8; ++o)
+            if (o < nout) slots[o * slot_elems + e] = out[o];
+    }
+    block_reduce_store<kMaxTerms>(pot, partV, gridDim.x, blockIdx.x);
+    __syncthreads();
+
+    // 3. real-to-complex along z of every product; X[k] = (Z[k] + conj Z[M-k])/2
+    //    + e^{-2 pi i k/N} (Z[k] - conj Z[M-k])/(2i), k = 0..M (Z[M] = Z[0])
+    const int rounds = (nout + nin - 1) / nin;
+    for (int it = 0; it < rounds; ++it) {
+        const int o = grp + it * nin;
+        const bool act = o < nout;
+        const ZIdx<L> ix{(int)((act ? o : 0) * slot_elems + t * LS)};
+        C v[16];
+#pragma unroll
+        for (int r = 0; r < 16; ++r) v[r] = act ? slots[ix(j + r * P)] : mk<T>(0, 0);
+        __syncthreads();   // all loads of this round precede the first exchange write
+        fft_reg<C, L, -1>(v, slots, ix, j, tw, N / L, act);
+        __syncthreads();
+        if (act) {
+#pragma unroll
+            for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+                for (int r = 0; r < RP::RL; ++r) slots[ix(RP::out(j, q, r))] = v[q * RP::RL + r];
+        }
+        __syncthreads();
+        if (act && valid) {
+            C *dst = ((o < nf) ? QV + (long long)o * g.modes : QS + (long long)(o - nf) * g.modes) + (long long)line * H;
+#pragma unroll
+            for (int r = 0; r <= 16; ++r) {
+                const int k = (r < 16) ? j + r * P : M;
+                if (r == 16 && j != 0) break;
+                const C zk = slots[ix(k == M ? 0 : k)];
+                const C zc = cconj(slots[ix(k == 0 ? 0 : M - k)]);
+                const C ev = cscale(cadd(zk, zc), T(0.5));
+                const C dd = cscale(csub(zk, zc), T(0.5));
+                const C od = mk<T>(dd.y, -dd.x);
+                C w;
+                if (k < M) w = __ldg(&tw[k]); else w = mk<T>(T(-1), T(0));
+                dst[k] = cadd(ev, cmul(w, od));
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------ real-space view (c2r along z)
+template <typename T, int L>
+__global__ void __launch_bounds__(256) kr_z_c2r_real(Geo g, const cplx<T> *__restrict__ TA, T *__restrict__ out,
+                                                     const cplx<T> *__restrict__ tw, T inv_n3, int tl_shift) {
+    using C = cplx<T>;
+    using RP = RegPlan<L>;
+    constexpr int M = L, P = RP::P, LS = ZIdx<L>::LS;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *sm = reinterpret_cast<C *>(smem_raw);
+    const int TL = 1 << tl_shift, H = g.H, N = g.N;
+    const int j = threadIdx.x % P, t = threadIdx.x / P;
+    const int line = blockIdx.x * TL + t;
+    const bool valid = line < g.lines_z;
+    const C *src = TA + (long long)blockIdx.y * g.modes + (long long)line * H;
+    C v[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+        const int k = j + r * P;
+        C x = mk<T>(0, 0), y = mk<T>(0, 0);
+        if (valid) {
+            x = src[k];
+            y = src[M - k];
+        }
+        y.y = -y.y;
+        if (k == 0) { x.y = T(0); y.y = T(0); }
+        const C s = cadd(x, y), d = csub(x, y);
+        C w = __ldg(&tw[k]);
+        w.y = -w.y;
+        const C td = cmul(w, d);
+        v[r] = mk<T>(s.x - td.y, s.y + td.x);
+    }
+    const ZIdx<L> ix{t * LS};
+    fft_reg<C, L, +1>(v, sm, ix, j, tw, N / L);
+    if (valid) {
+        T *o = out + (long long)blockIdx.y * g.sites + (long long)line * N;
+#pragma unroll
+        for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+            for (int r = 0; r < RP::RL; ++r) {
+                const int m = RP::out(j, q, r);
+                const C c = cscale(v[q * RP::RL + r], inv_n3);
+                o[2 * m] = c.x;
+                o[2 * m + 1] = c.y;
+            }
+    }
+}
+
+}  // namespace psc

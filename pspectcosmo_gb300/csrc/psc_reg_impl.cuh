@@ -1,0 +1,143 @@
+// psc_reg_impl.cuh — launchers of the register-engine passes for one precision
+// (included by psc_reg_f32.cu / psc_reg_f64.cu so the two precisions compile in
+// parallel). Dispatches the run-time lattice size to the compile-time line
+// lengths L = N (X, Y passes) and L = N/2 (Z pass).
+#pragma once
+
+#include "psc_passes.cuh"
+
+namespace psc {
+
+template <typename T, int N>
+struct RegLaunch {
+    using C = cplx<T>;
+    static constexpr int M = N / 2;
+
+    static cudaError_t configure(const LaunchCfg &cfg) {
+        const int sxy = (int)cfg.smem_xy, sz = (int)cfg.smem_z;
+        cudaError_t e;
+#define SETA(kern, bytes)                                                                                   \
+    e = cudaFuncSetAttribute((const void *)(kern), cudaFuncAttributeMaxDynamicSharedMemorySize, (bytes));   \
+    if (e != cudaSuccess) return e;
+        SETA((kr_ifft_x<T, N, false, true>), sxy);
+        SETA((kr_ifft_x<T, N, true, true>), sxy);
+        SETA((kr_ifft_x<T, N, false, false>), sxy);
+        SETA((kr_ifft_x<T, N, true, false>), sxy);
+        SETA((kr_ifft_y<T, N, false>), sxy);
+        SETA((kr_ifft_y<T, N, true>), sxy);
+        SETA((kr_fft_y<T, N>), sxy);
+        SETA((kr_fft_x_final<T, N, false>), sxy);
+        SETA((kr_fft_x_final<T, N, true>), sxy);
+        SETA((kr_zpass<T, M, false>), sz);
+        SETA((kr_zpass<T, M, true>), sz);
+        SETA((kr_z_c2r_real<T, M>), (int)((256 / (M / 16)) * (M + M / 16) * sizeof(C)));
+#undef SETA
+        return cudaSuccess;
+    }
+
+    static cudaError_t stage(const LaunchCfg &cfg, const Buffers &b, int drift, cudaStream_t st, cudaEvent_t *ev,
+                             int scalar_mode) {
+        const Geo &g = cfg.g;
+        const C *tw = reinterpret_cast<const C *>(b.tw);
+        C *fk = (C *)b.fk, *pk = (C *)b.pk, *uk = (C *)b.uk, *puk = (C *)b.puk;
+        C *TA = (C *)b.TA, *TB = (C *)b.TB, *TC = (C *)b.TC, *QV = (C *)b.QV, *QS = (C *)b.QS;
+        const dim3 gx(cfg.nbx, g.nf);
+        const int txy = cfg.thr_xy, tz = cfg.thr_z;
+        auto mark = [&](int i) {
+            if (ev) cudaEventRecord(ev[i], st);
+        };
+        mark(0);
+        if (g.gw) {
+            if (drift) kr_ifft_x<T, N, true, true><<<gx, txy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
+            else kr_ifft_x<T, N, true, false><<<gx, txy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
+            mark(1);
+            kr_ifft_y<T, N, true><<<gx, txy, cfg.smem_xy, st>>>(g, TA, TB, TC, b.bg, tw);
+            mark(2);
+            kr_zpass<T, M, true><<<cfg.nbz, tz, cfg.smem_z, st>>>(g, TA, TB, TC, QV, QS, b.partV, b.bg, tw);
+        } else {
+            if (drift) kr_ifft_x<T, N, false, true><<<gx, txy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
+            else kr_ifft_x<T, N, false, false><<<gx, txy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
+            mark(1);
+            kr_ifft_y<T, N, false><<<gx, txy, cfg.smem_xy, st>>>(g, TA, TB, TC, b.bg, tw);
+            mark(2);
+            kr_zpass<T, M, false><<<cfg.nbz, tz, cfg.smem_z, st>>>(g, TA, TB, TC, QV, QS, b.partV, b.bg, tw);
+        }
+        mark(3);
+        ArrList8 al{};
+        int nj = 0;
+        for (int f = 0; f < g.nf; ++f) al.p[nj++] = QV + (long long)f * g.modes;
+        if (g.gw)
+            for (int c = 0; c < 6; ++c) al.p[nj++] = QS + (long long)c * g.modes;
+        kr_fft_y<T, N><<<dim3(cfg.nbx, nj), txy, cfg.smem_xy, st>>>(g, al, tw);
+        mark(4);
+        const dim3 gf(cfg.nbx, nj);
+        if (g.gw)
+            kr_fft_x_final<T, N, true><<<gf, txy, cfg.smem_xy, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw);
+        else
+            kr_fft_x_final<T, N, false><<<gf, txy, cfg.smem_xy, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw);
+        mark(5);
+        if (scalar_mode >= 0) {
+            cudaError_t e = launch_scalar(cfg, b, scalar_mode, 1, st);
+            if (e != cudaSuccess) return e;
+            mark(6);
+        }
+        return cudaGetLastError();
+    }
+
+    static cudaError_t c2r_real(const LaunchCfg &cfg, const Buffers &b, const void *src, int nsrc, cudaStream_t st) {
+        const Geo &g = cfg.g;
+        const C *tw = reinterpret_cast<const C *>(b.tw);
+        C *TA = (C *)b.TA;
+        constexpr int P = M / 16;
+        int tl = 256 / P;
+        int sh = 0;
+        while ((1 << sh) < tl) ++sh;
+        const size_t smem = (size_t)tl * (M + M / 16) * sizeof(C);
+        const int nbz = (g.lines_z + tl - 1) / tl;
+        for (int s0 = 0; s0 < nsrc; s0 += g.nf) {
+            const int cnt = (nsrc - s0) < g.nf ? (nsrc - s0) : g.nf;
+            const C *s = (const C *)src + (long long)s0 * g.modes;
+            kr_ifft_x<T, N, false, false><<<dim3(cfg.nbx, cnt), cfg.thr_xy, cfg.smem_xy, st>>>(
+                g, (C *)s, nullptr, TA, nullptr, b.bg, tw);
+            kr_ifft_y<T, N, false><<<dim3(cfg.nbx, cnt), cfg.thr_xy, cfg.smem_xy, st>>>(g, TA, nullptr, nullptr, b.bg,
+                                                                                      tw);
+            kr_z_c2r_real<T, M><<<dim3(nbz, cnt), tl * P, smem, st>>>(g, TA, (T *)b.real + (long long)s0 * g.sites,
+                                                                     tw, (T)(1.0 / (double)g.sites), sh);
+        }
+        return cudaGetLastError();
+    }
+};
+
+template <typename T>
+struct RegDispatch {
+    template <typename F>
+    static cudaError_t on(int N, F &&f) {
+        switch (N) {
+        case 32: return f(RegLaunch<T, 32>());
+        case 64: return f(RegLaunch<T, 64>());
+        case 128: return f(RegLaunch<T, 128>());
+        case 256: return f(RegLaunch<T, 256>());
+        case 512: return f(RegLaunch<T, 512>());
+        case 1024: return f(RegLaunch<T, 1024>());
+        default: return cudaErrorInvalidValue;
+        }
+    }
+};
+
+}  // namespace psc
+
+#define PSC_DEFINE_REG_ENTRY(T, SUFFIX)                                                                          \
+    namespace psc {                                                                                              \
+    cudaError_t reg_configure_##SUFFIX(const LaunchCfg &cfg) {                                                   \
+        return RegDispatch<T>::on(cfg.g.N, [&](auto L) { return decltype(L)::configure(cfg); });                 \
+    }                                                                                                            \
+    cudaError_t reg_stage_##SUFFIX(const LaunchCfg &cfg, const Buffers &b, int drift, cudaStream_t st,           \
+                                   cudaEvent_t *ev, int scalar_mode) {                                           \
+        return RegDispatch<T>::on(cfg.g.N,                                                                       \
+                                  [&](auto L) { return decltype(L)::stage(cfg, b, drift, st, ev, scalar_mode); }); \
+    }                                                                                                            \
+    cudaError_t reg_c2r_real_##SUFFIX(const LaunchCfg &cfg, const Buffers &b, const void *src, int nsrc,         \
+                                      cudaStream_t st) {                                                         \
+        return RegDispatch<T>::on(cfg.g.N, [&](auto L) { return decltype(L)::c2r_real(cfg, b, src, nsrc, st); }); \
+    }                                                                                                            \
+    }
