@@ -191,6 +191,20 @@ __device__ C *fft_tile(C *a, C *b, int L, int tl_shift, int LD, const C *__restr
     return src;
 }
 
+// ------------------------------------------------------------------ asynchronous copies
+// One complex element global -> shared with cp.async (sm_80+ LDGSTS); 8-byte
+// elements use the .ca form, 16-byte elements the .cg form.
+__device__ __forceinline__ void cp_async_elem(float2 *dst, const float2 *src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_elem(double2 *dst, const double2 *src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
 // ------------------------------------------------------------------ reductions
 // Block reduction of NV doubles; thread 0 stores out[i * stride + blockIdx.x].
 // Deterministic for a fixed block size.

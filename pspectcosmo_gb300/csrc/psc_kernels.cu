@@ -701,6 +701,7 @@ void plan(const psc_params &p, LaunchCfg *cfg) {
         g.tlx_shift = ilog2i(tl);
         cfg->thr_xy = tl * P;
         cfg->smem_xy = (size_t)tl * g.N * csize;
+        cfg->smem_xf = 3 * cfg->smem_xy;
         cfg->nbx = (g.lines_x + tl - 1) / tl;
         const int Pz = g.M / 16;
         int tlz = 256 / (nin * Pz);
@@ -708,7 +709,7 @@ void plan(const psc_params &p, LaunchCfg *cfg) {
         g.tlz_shift = ilog2i(tlz);
         g.ldz = 0;
         cfg->thr_z = nin * tlz * Pz;
-        cfg->smem_z = (size_t)nslot * tlz * (g.M + g.M / 16) * csize;
+        cfg->smem_z = (size_t)nslot * tlz * (g.M + g.M / 16 + 1) * csize;
         cfg->nbz = (g.lines_z + tlz - 1) / tlz;
         return;
     }
@@ -721,6 +722,7 @@ void plan(const psc_params &p, LaunchCfg *cfg) {
     g.tlx_shift = ilog2i(tl);
     cfg->thr_xy = 256;
     cfg->smem_xy = (size_t)2 * tl * g.N * csize;
+    cfg->smem_xf = cfg->smem_xy;
     cfg->nbx = (g.lines_x + tl - 1) / tl;
     // Z pass: TLz lines, two H-row buffers + nslot M-row real-line slots.
     int tlz = 32;

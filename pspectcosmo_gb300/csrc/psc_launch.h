@@ -29,6 +29,7 @@ struct LaunchCfg {
     Geo g;
     int thr_xy, thr_z;           // threads per block
     size_t smem_xy, smem_z;      // dynamic shared memory bytes
+    size_t smem_xf;              // X forward + kick pass (exchange tile + two prefetched operand tiles)
     int nbx;                     // blocks of the X / Y passes (per array)
     int nbz;                     // blocks of the Z pass
 };

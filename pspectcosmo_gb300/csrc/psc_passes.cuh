@@ -17,7 +17,7 @@ namespace psc {
 
 // ------------------------------------------------------------------ X inverse (+ drift, + x-derivative)
 template <typename T, int L, bool GW, bool DRIFT>
-__global__ void __launch_bounds__(256) kr_ifft_x(Geo g, cplx<T> *__restrict__ fk, const cplx<T> *__restrict__ pk,
+__global__ void __launch_bounds__(256, 2) kr_ifft_x(Geo g, cplx<T> *__restrict__ fk, const cplx<T> *__restrict__ pk,
                                                  cplx<T> *__restrict__ TA, cplx<T> *__restrict__ TB,
                                                  const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw) {
     using C = cplx<T>;
@@ -120,7 +120,7 @@ __device__ __forceinline__ void ry_tile(const Geo &g, const cplx<T> *src, cplx<T
 }
 
 template <typename T, int L, bool GW>
-__global__ void __launch_bounds__(256) kr_ifft_y(Geo g, cplx<T> *__restrict__ TA, cplx<T> *__restrict__ TB,
+__global__ void __launch_bounds__(256, 2) kr_ifft_y(Geo g, cplx<T> *__restrict__ TA, cplx<T> *__restrict__ TB,
                                                  cplx<T> *__restrict__ TC, const DevBG *__restrict__ bg,
                                                  const cplx<T> *__restrict__ tw) {
     using C = cplx<T>;
@@ -143,7 +143,7 @@ struct ArrList8 {
 };
 
 template <typename T, int L>
-__global__ void __launch_bounds__(256) kr_fft_y(Geo g, ArrList8 arrs, const cplx<T> *__restrict__ tw) {
+__global__ void __launch_bounds__(256, 3) kr_fft_y(Geo g, ArrList8 arrs, const cplx<T> *__restrict__ tw) {
     using C = cplx<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *sm = reinterpret_cast<C *>(smem_raw);
@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(256) kr_fft_y(Geo g, ArrList8 arrs, const cplx
 
 // ------------------------------------------------------------------ X forward + kick epilogue
 template <typename T, int L, bool GW>
-__global__ void __launch_bounds__(256) kr_fft_x_final(Geo g, const cplx<T> *__restrict__ QV,
+__global__ void __launch_bounds__(256, 2) kr_fft_x_final(Geo g, const cplx<T> *__restrict__ QV,
                                                       const cplx<T> *__restrict__ QS, const cplx<T> *__restrict__ fk,
                                                       cplx<T> *__restrict__ pk, cplx<T> *__restrict__ uk,
                                                       cplx<T> *__restrict__ puk, double *__restrict__ partKG,
@@ -173,11 +173,26 @@ __global__ void __launch_bounds__(256) kr_fft_x_final(Geo g, const cplx<T> *__re
     const long long stride = g.lines_x;
     const long long base = off + line;
     auto ix = [&](int n) { return n * TL + t; };
+    // Prefetch the kick operands (f_k, pi_half or u_k, pi_u_half) of this tile
+    // into shared memory with cp.async, overlapping their latency with the FFT.
+    C *opA = sm + TL * L, *opB = opA + TL * L;
+    const C *gA = field ? fk : uk, *gB = field ? pk : puk;
+    if (valid) {
+#pragma unroll
+        for (int r = 0; r < 16; ++r) {
+            const int n = RP::out(j, r / RP::RL, r % RP::RL);
+            const long long a = base + (long long)n * stride;
+            cp_async_elem(opA + ix(n), gA + a);
+            cp_async_elem(opB + ix(n), gB + a);
+        }
+    }
+    cp_async_commit();
     C v[16];
 #pragma unroll
     for (int r = 0; r < 16; ++r)
         v[r] = valid ? src[(long long)(j + r * RP::P) * stride + line] : mk<T>(0, 0);
     fft_reg<C, L, -1>(v, sm, ix, j, tw, N / L);
+    cp_async_wait_all();
 
     const T norm1 = (T)bg->norm1, norm2 = (T)bg->norm2, kIR2 = (T)bg->kIR2;
     const T c_close = (T)bg->c_close, c_open = (T)bg->c_open;
@@ -198,7 +213,7 @@ __global__ void __launch_bounds__(256) kr_fft_x_final(Geo g, const cplx<T> *__re
                     const int px = pcoord(n, N);
                     const T k2 = (T)(px * px + py * py + kz * kz);
                     const long long a = base + (long long)n * stride;
-                    const C f = fk[a], p = pk[a], qv = v[q * RP::RL + r];
+                    const C f = opA[ix(n)], p = opB[ix(n)], qv = v[q * RP::RL + r];
                     // force (evolution.cpp:1124-1125)
                     const T fl = -norm1 * kIR2 * k2;
                     const C F = mk<T>(fl * f.x - norm2 * qv.x, fl * f.y - norm2 * qv.y);
@@ -230,8 +245,8 @@ __global__ void __launch_bounds__(256) kr_fft_x_final(Geo g, const cplx<T> *__re
                 const int px = pcoord(n, N);
                 const T k2 = (T)(px * px + py * py + kz * kz);
                 const long long a = base + (long long)n * stride;
-                C u = uk[a];
-                const C w = puk[a], qv = v[q * RP::RL + r];
+                C u = opA[ix(n)];
+                const C w = opB[ix(n)], qv = v[q * RP::RL + r];
                 // drift of u_ij deferred from the stage prologue (evolution.cpp:655-662)
                 u.x += c_drift * w.x;
                 u.y += c_drift * w.y;
@@ -251,13 +266,13 @@ __global__ void __launch_bounds__(256) kr_fft_x_final(Geo g, const cplx<T> *__re
 // the radix-16 exchange free of bank conflicts).
 template <int L>
 struct ZIdx {
-    static constexpr int LS = L + L / 16;
+    static constexpr int LS = L + L / 16 + 1;   // one spare entry holds X[M] while staging
     int base;
     __device__ __forceinline__ int operator()(int n) const { return base + n + (n >> 4); }
 };
 
 template <typename T, int L, bool GW>
-__global__ void __launch_bounds__(256) kr_zpass(Geo g, const cplx<T> *__restrict__ TA, const cplx<T> *__restrict__ TB,
+__global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restrict__ TA, const cplx<T> *__restrict__ TB,
                                                 const cplx<T> *__restrict__ TC, cplx<T> *__restrict__ QV,
                                                 cplx<T> *__restrict__ QS, double *__restrict__ partV,
                                                 const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw) {
@@ -286,14 +301,22 @@ __global__ void __launch_bounds__(256) kr_zpass(Geo g, const cplx<T> *__restrict
         const int fld = GW ? (grp >> 2) : grp;
         const int kind = GW ? (grp & 3) : 0;   // 0: f, 1: d/dx f, 2: d/dy f, 3: d/dz f
         const C *src = (kind == 1 ? TB : (kind == 2 ? TC : TA)) + (long long)fld * g.modes + (long long)line * H;
+        const ZIdx<L> ix{(int)(grp * slot_elems + t * LS)};
+        // stage X[0..M] of the line in its slot (M+1 entries fit: the pad leaves room)
+        if (valid) {
+#pragma unroll
+            for (int r = 0; r < 16; ++r) slots[ix(j + r * P)] = src[j + r * P];
+            if (j == 0) slots[ix(M)] = src[M];
+        }
+        __syncthreads();
         C v[16];
 #pragma unroll
         for (int r = 0; r < 16; ++r) {
             const int k = j + r * P;
             C x = mk<T>(0, 0), y = mk<T>(0, 0);
             if (valid) {
-                x = src[k];
-                y = src[M - k];
+                x = slots[ix(k)];
+                y = slots[ix(M - k)];
                 if (kind == 3) {
                     const T kx = kIR * (T)k;                           // k < M
                     const T ky = (k == 0) ? T(0) : kIR * (T)(M - k);   // Nyquist zeroed
@@ -309,7 +332,7 @@ __global__ void __launch_bounds__(256) kr_zpass(Geo g, const cplx<T> *__restrict
             const C td = cmul(w, d);
             v[r] = mk<T>(s.x - td.y, s.y + td.x);
         }
-        const ZIdx<L> ix{(int)(grp * slot_elems + t * LS)};
+        __syncthreads();   // the slot is reused as the exchange buffer
         fft_reg<C, L, +1>(v, slots, ix, j, tw, N / L);
         __syncthreads();
 #pragma unroll

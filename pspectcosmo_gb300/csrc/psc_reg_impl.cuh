@@ -18,6 +18,9 @@ struct RegLaunch {
         cudaError_t e;
 #define SETA(kern, bytes)                                                                                   \
     e = cudaFuncSetAttribute((const void *)(kern), cudaFuncAttributeMaxDynamicSharedMemorySize, (bytes));   \
+    if (e != cudaSuccess) return e;                                                                         \
+    e = cudaFuncSetAttribute((const void *)(kern), cudaFuncAttributePreferredSharedMemoryCarveout,         \
+                             cudaSharedmemCarveoutMaxShared);                                               \
     if (e != cudaSuccess) return e;
         SETA((kr_ifft_x<T, N, false, true>), sxy);
         SETA((kr_ifft_x<T, N, true, true>), sxy);
@@ -26,11 +29,11 @@ struct RegLaunch {
         SETA((kr_ifft_y<T, N, false>), sxy);
         SETA((kr_ifft_y<T, N, true>), sxy);
         SETA((kr_fft_y<T, N>), sxy);
-        SETA((kr_fft_x_final<T, N, false>), sxy);
-        SETA((kr_fft_x_final<T, N, true>), sxy);
+        SETA((kr_fft_x_final<T, N, false>), (int)cfg.smem_xf);
+        SETA((kr_fft_x_final<T, N, true>), (int)cfg.smem_xf);
         SETA((kr_zpass<T, M, false>), sz);
         SETA((kr_zpass<T, M, true>), sz);
-        SETA((kr_z_c2r_real<T, M>), (int)((256 / (M / 16)) * (M + M / 16) * sizeof(C)));
+        SETA((kr_z_c2r_real<T, M>), (int)((256 / (M / 16)) * ZIdx<M>::LS * sizeof(C)));
 #undef SETA
         return cudaSuccess;
     }
@@ -72,9 +75,9 @@ struct RegLaunch {
         mark(4);
         const dim3 gf(cfg.nbx, nj);
         if (g.gw)
-            kr_fft_x_final<T, N, true><<<gf, txy, cfg.smem_xy, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw);
+            kr_fft_x_final<T, N, true><<<gf, txy, cfg.smem_xf, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw);
         else
-            kr_fft_x_final<T, N, false><<<gf, txy, cfg.smem_xy, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw);
+            kr_fft_x_final<T, N, false><<<gf, txy, cfg.smem_xf, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw);
         mark(5);
         if (scalar_mode >= 0) {
             cudaError_t e = launch_scalar(cfg, b, scalar_mode, 1, st);
@@ -92,7 +95,7 @@ struct RegLaunch {
         int tl = 256 / P;
         int sh = 0;
         while ((1 << sh) < tl) ++sh;
-        const size_t smem = (size_t)tl * (M + M / 16) * sizeof(C);
+        const size_t smem = (size_t)tl * ZIdx<M>::LS * sizeof(C);
         const int nbz = (g.lines_z + tl - 1) / tl;
         for (int s0 = 0; s0 < nsrc; s0 += g.nf) {
             const int cnt = (nsrc - s0) < g.nf ? (nsrc - s0) : g.nf;
