@@ -155,6 +155,28 @@ int psc_time_passes(psc_handle *h, int reps, float *ms);
  * of the arrays it must read and write once), for roofline accounting. */
 int psc_pass_bytes(psc_handle *h, double *bytes);
 
+/* Scalar power spectrum without any device allocation. It has no counterpart in
+ * the reference; it is the bin-summing step of spectra() (output.cpp:626-690) for
+ * callers that cannot call cudaMalloc: applications whose own memory pool owns all
+ * device memory, or code that must not allocate once it is running (an allocation
+ * synchronises the device and can fail late). Instead of a handle it takes the
+ * caller's device arrays: f_k, pi_k ([nflds][N][N][N/2+1] complex of p->precision,
+ * as psc_get_state lays them out) and the outputs numpoints, f2, pi2, n2
+ * ([nflds][maxnumbins], any may be NULL), filled as psc_spectra fills them; a and
+ * ad are the background. Only p->N, p->nflds, p->precision and p->alpha are read.
+ * Limit: N <= PSC_NOALLOC_MAX_N and nflds <= 2, otherwise PSC_ERR_CONFIG. The bin
+ * accumulators live in one fixed array of device memory inside the library (about
+ * 50 KB, held by every GPU that loads the library until the process exits),
+ * shared by all calls on a device: each call clears it first, so calls whose work
+ * overlaps on the GPU (different streams or threads) race and must be serialised
+ * by the caller. The first call on a device looks up that array's device address
+ * (cudaGetSymbolAddress), so make it before any stream capture. Work is queued on
+ * `stream` (a cudaStream_t; NULL = default stream) and is complete when the stream
+ * is. Calls no cudaMalloc or cudaFree. */
+#define PSC_NOALLOC_MAX_N 1024
+int psc_spectra_noalloc(const psc_params *p, double a, double ad, const void *f_k, const void *pi_k,
+                        int32_t *numpoints, double *f2, double *pi2, double *n2, void *stream);
+
 const char *psc_strerror(int code);
 const char *psc_last_error(void);
 

@@ -55,6 +55,8 @@ bool pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
 
 }  // namespace
 
+void psc::set_last_error(const char *msg) { g_last_error = msg ? msg : ""; }
+
 struct psc_handle {
     psc_params p{};
     psc::LaunchCfg cfg{};

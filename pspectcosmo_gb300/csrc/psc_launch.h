@@ -81,6 +81,9 @@ cudaError_t launch_c2r_real(const LaunchCfg &cfg, const Buffers &b, int precisio
 // b.spec_cnt: [nf][nb] then GW [nb]. Zeroes the accumulators first.
 cudaError_t launch_spectra(const LaunchCfg &cfg, const Buffers &b, int precision, int nb, cudaStream_t st);
 
+// Record the message psc_last_error() returns on this thread.
+void set_last_error(const char *msg);
+
 // Register-engine passes (psc_reg_f32.cu, psc_reg_f64.cu), N = 32..1024.
 cudaError_t reg_configure_f32(const LaunchCfg &cfg);
 cudaError_t reg_configure_f64(const LaunchCfg &cfg);
