@@ -39,7 +39,24 @@ CONFIGS = {
     "preheat_256": (dict(kind="preheating", N=256, spectral=1, with_gw=0, vv=4), 0.005,
                     "256^3 two-field preheating (spectral path, no GW), Yoshida-4"),
     "inflation_64": (dict(kind="default", N=64, vv=2), 0.002, "64^3 single-field inflation, velocity Verlet"),
+    # 256 x 32^3 + 64 x 64^3 + 8 x 128^3 single-field realizations, per-realization seed and
+    # phi0 ~ U[10, 12] (host RNG seed 12345), Yoshida-4, one graph per step for all of them
+    "ensemble_mixed": (dict(kind="ensemble"), 1e-4,
+                       "ensemble: 256 x 32^3 + 64 x 64^3 + 8 x 128^3 single-field inflation, Yoshida-4"),
 }
+
+
+def ensemble_params(precision: int):
+    import numpy as np
+    from pspectcosmo_gb300.params import Params
+
+    rng = np.random.default_rng(12345)
+    ps = []
+    for N, count in ((32, 256), (64, 64), (128, 8)):
+        for _ in range(count):
+            ps.append(Params.reference_default(N=N, vv=4, seed=1 + len(ps), precision=precision,
+                                               initfield=[float(rng.uniform(10.0, 12.0)), 0.0]))
+    return ps
 
 # algorithmic HBM bytes per site-step of the fused dataflow: per stage and field 9C + 2R,
 # GW 36C + 12R (C = P (1 + 2/N) per site for a half-spectrum complex array, R = P)
@@ -199,7 +216,43 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_ensemble(args):
+    world, rank, local, dist = dist_setup()
+    from pspectcosmo_gb300 import Ensemble, build
+
+    build.build()
+    _, dt, desc = CONFIGS[args.config]
+    ps = ensemble_params(args.precision)
+    sites = sum(p.sites for p in ps)
+    ens = Ensemble(ps)
+    ens.initialize()
+    ens.evolve(dt, args.warmup)
+    clocks = ClockSampler(local)
+    barrier(dist)
+    clocks.start()
+    barrier(dist)
+    ens.evolve(dt, args.steps)
+    barrier(dist)
+    ms = max_over_ranks(dist, ens.last_step_ms())
+    clk = clocks.stop()
+    value = world * sites * args.steps / (ms / 1e3)
+    if rank == 0:
+        line = {"metric": "site-steps/s", "value": value, "unit": "site-steps/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == 32 else "f64",
+                "data": "synthetic (reference seeded initial conditions per realization)",
+                "config": {"workload": desc, "realizations": len(ps), "groups": ens.groups, "sites": sites,
+                           "dt": dt, "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+                "clocks": clk, "gpu_launches": 3 * 6 * 4 * args.steps}
+        print(json.dumps(line), flush=True)
+    ens.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
 def run_ours(args):
+    if args.config == "ensemble_mixed":
+        return run_ensemble(args)
     world, rank, local, dist = dist_setup()
     from pspectcosmo_gb300 import Lattice, build
     from pspectcosmo_gb300.params import Params  # noqa: F401

@@ -155,6 +155,33 @@ int psc_time_passes(psc_handle *h, int reps, float *ms);
  * of the arrays it must read and write once), for roofline accounting. */
 int psc_pass_bytes(psc_handle *h, double *bytes);
 
+/* ---------------------------------------------------------------- batches
+ * Ensembles of independent realizations (BASELINE's batched configuration). The
+ * reference runs one lattice per process; these entry points have no single
+ * counterpart and compose the ones above. psc_batch_create groups the n
+ * realizations by configuration (all psc_params fields except seed, initfield,
+ * initderivs, a0 and kcutoff must agree within a group; sizes may differ between
+ * groups). Each group is advanced by one launch per pass for all its members, and
+ * one CUDA graph holds a whole step of every group. Realizations are addressed by
+ * their index in the array given to psc_batch_create. */
+typedef struct psc_batch psc_batch;
+int psc_batch_create(const psc_params *per_realization, int n, psc_batch **out);
+void psc_batch_destroy(psc_batch *b);
+int psc_batch_size(psc_batch *b);
+int psc_batch_groups(psc_batch *b);
+int psc_batch_init_ic(psc_batch *b);                      /* initialize() for every realization */
+int psc_batch_step(psc_batch *b, double dt, int nsteps);  /* nsteps steps of every realization */
+int psc_batch_last_step_ms(psc_batch *b, float *ms);
+int psc_batch_set_state(psc_batch *b, int idx, const double *f_k, const double *pi_k, double a, double ad, double add,
+                        const double *u_k, const double *pi_u_k);
+int psc_batch_get_state(psc_batch *b, int idx, double *f_k, double *pi_k, double *a, double *ad, double *add,
+                        double *u_k, double *pi_u_k);
+int psc_batch_spectra(psc_batch *b, int idx, int32_t *numpoints, double *f2, double *pi2, double *n2,
+                      int32_t *gw_numpoints, double *h2, double *hdot2, double *hdot2_zero);
+int psc_batch_energies(psc_batch *b, int idx, double *K, double *G, double *V, double *total,
+                       double *friedmann_violation, double *rho_gw);
+int psc_batch_means(psc_batch *b, int idx, double *out);
+
 /* Scalar power spectrum without any device allocation. It has no counterpart in
  * the reference; it is the bin-summing step of spectra() (output.cpp:626-690) for
  * callers that cannot call cudaMalloc: applications whose own memory pool owns all

@@ -4,6 +4,7 @@ The compute path is libpsc.so (hand-written sm_103a CUDA behind the C ABI declar
 include/psc.h); this package is its Python mirror of the reference's interface.
 """
 from .params import MODEL_PHI2, MODEL_PHI2CHI2, Params
-from .lattice import Lattice, PscError, generate_ic, load_library
+from .lattice import Ensemble, Lattice, PscError, generate_ic, load_library
 
-__all__ = ["Params", "Lattice", "PscError", "generate_ic", "load_library", "MODEL_PHI2", "MODEL_PHI2CHI2"]
+__all__ = ["Params", "Lattice", "Ensemble", "PscError", "generate_ic", "load_library", "MODEL_PHI2",
+           "MODEL_PHI2CHI2"]

@@ -1,11 +1,19 @@
-// psc_api.cu — the C ABI (include/psc.h): one handle per lattice, device
-// buffers, the captured step graph, host<->device state transfer and outputs.
-// Host code only; the kernels live in psc_kernels.cu.
+// psc_api.cu — the C ABI (include/psc.h): handles, device buffers, the captured
+// step graph, host<->device state transfer, outputs, and batches of lattices.
+// Host code only; the kernels live in psc_kernels.cu and psc_reg_*.cu.
+//
+// A handle holds R >= 1 lattices of one configuration ("realizations") laid
+// out back to back in every device array; the pass kernels advance all R with
+// one launch each (realization = blockIdx.z). psc_create makes R = 1; a batch
+// groups its realizations by configuration into such handles and captures all
+// of them in one CUDA graph per step.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <new>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/psc.h"
@@ -53,27 +61,31 @@ const double kW10[31] = {
 
 bool pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
 
+constexpr double kPi = 3.14159265358979323846;
+
 }  // namespace
 
 void psc::set_last_error(const char *msg) { g_last_error = msg ? msg : ""; }
 
 struct psc_handle {
-    psc_params p{};
+    std::vector<psc_params> p;   // per realization (identical except seed / initial values)
+    int R = 1;
     psc::LaunchCfg cfg{};
     psc::Buffers b{};
-    size_t csize = 0;   // bytes of one complex element on the device
+    size_t csize = 0;            // bytes of one complex element on the device
     int s = 1;
     const double *w = kW2;
-    int nb = 0;         // maxnumbins
+    int nb = 0;                  // maxnumbins
     cudaStream_t st = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaGraphExec_t gexec = nullptr;
     bool have_state = false;
     bool diag_valid = false;
     float last_ms = 0.f;
-    void *stage_buf = nullptr;    // pinned staging for precision conversion
+    void *stage_buf = nullptr;   // pinned staging for precision conversion
     size_t stage_bytes = 0;
     std::vector<void *> allocs;
+    const psc_params &p0() const { return p[0]; }
 };
 
 namespace {
@@ -114,6 +126,14 @@ int validate(const psc_params *p) {
     return PSC_OK;
 }
 
+// the fields two realizations must share to be advanced by the same launches
+std::tuple<int, int, int, int, int, int, int, int, int, int, double, double, double, double, double, double>
+config_key(const psc_params &p) {
+    return std::make_tuple(p.N, p.nflds, p.vv, p.alpha, p.expansion, p.simulate_inflation, p.spectral, p.with_gw,
+                           p.precision, p.model, p.gsq, p.kIR, p.MPl, p.m_in_MPl, p.fStar > 0 ? p.fStar : p.MPl,
+                           p.epsilon);
+}
+
 int ensure_staging(psc_handle *h, size_t bytes) {
     if (h->stage_bytes >= bytes) return PSC_OK;
     if (h->stage_buf) cudaFreeHost(h->stage_buf);
@@ -126,7 +146,7 @@ int ensure_staging(psc_handle *h, size_t bytes) {
 
 // host FP64 complex -> device array of the handle's precision
 int upload(psc_handle *h, void *dst, const double *src, size_t ncplx) {
-    if (h->p.precision == 64) {
+    if (h->p0().precision == 64) {
         CU(cudaMemcpyAsync(dst, src, ncplx * 16, cudaMemcpyHostToDevice, h->st));
         CU(cudaStreamSynchronize(h->st));
         return PSC_OK;
@@ -142,7 +162,7 @@ int upload(psc_handle *h, void *dst, const double *src, size_t ncplx) {
 
 // device array of the handle's precision -> host FP64 (count scalars)
 int download_real(psc_handle *h, double *dst, const void *src, size_t count) {
-    if (h->p.precision == 64) {
+    if (h->p0().precision == 64) {
         CU(cudaMemcpyAsync(dst, src, count * 8, cudaMemcpyDeviceToHost, h->st));
         CU(cudaStreamSynchronize(h->st));
         return PSC_OK;
@@ -156,53 +176,481 @@ int download_real(psc_handle *h, double *dst, const void *src, size_t count) {
     return PSC_OK;
 }
 
-int read_bg(psc_handle *h, psc::DevBG *out) {
-    CU(cudaMemcpyAsync(out, h->b.bg, sizeof(psc::DevBG), cudaMemcpyDeviceToHost, h->st));
+int read_bg(psc_handle *h, int r, psc::DevBG *out) {
+    CU(cudaMemcpyAsync(out, h->b.bg + r, sizeof(psc::DevBG), cudaMemcpyDeviceToHost, h->st));
     CU(cudaStreamSynchronize(h->st));
     return PSC_OK;
 }
 
-int write_bg(psc_handle *h, const psc::DevBG &in) {
-    CU(cudaMemcpyAsync(h->b.bg, &in, sizeof(psc::DevBG), cudaMemcpyHostToDevice, h->st));
+int write_bg(psc_handle *h, int r, const psc::DevBG &in) {
+    CU(cudaMemcpyAsync(h->b.bg + r, &in, sizeof(psc::DevBG), cudaMemcpyHostToDevice, h->st));
     CU(cudaStreamSynchronize(h->st));
     return PSC_OK;
 }
 
-// pure evaluation of the force pipeline: K, G, V and (keep_add = 0) a''
+// element offsets of realization r
+void *foff(psc_handle *h, void *base, int r) {
+    return static_cast<char *>(base) + (size_t)r * h->cfg.g.fstride * h->csize;
+}
+void *goff(psc_handle *h, void *base, int r) {
+    return static_cast<char *>(base) + (size_t)r * h->cfg.g.gstride * h->csize;
+}
+
+// the buffers of realization r seen as a single lattice
+psc::Buffers buffers_of(psc_handle *h, int r) {
+    psc::Buffers b = h->b;
+    b.fk = foff(h, h->b.fk, r);
+    b.pk = foff(h, h->b.pk, r);
+    b.TA = foff(h, h->b.TA, r);
+    b.QV = foff(h, h->b.QV, r);
+    if (h->cfg.g.gw) {
+        b.uk = goff(h, h->b.uk, r);
+        b.puk = goff(h, h->b.puk, r);
+        b.TB = foff(h, h->b.TB, r);
+        b.TC = foff(h, h->b.TC, r);
+        b.QS = goff(h, h->b.QS, r);
+    }
+    b.bg = h->b.bg + r;
+    return b;
+}
+
+psc::LaunchCfg single_cfg(psc_handle *h) {
+    psc::LaunchCfg c = h->cfg;
+    c.R = 1;
+    return c;
+}
+
+// pure evaluation of the force pipeline for all realizations: K, G, V and
+// (keep_add = 0) a''
 int evaluate(psc_handle *h, int keep_add) {
     CU(psc::launch_scalar(h->cfg, h->b, psc::SCALAR_EVAL, 0, h->st));
-    CU(psc::launch_stage(h->cfg, h->b, h->p.precision, 0, h->st));
+    CU(psc::launch_stage(h->cfg, h->b, h->p0().precision, 0, h->st));
     CU(psc::launch_scalar(h->cfg, h->b, psc::SCALAR_EVAL_END, keep_add, h->st));
     CU(cudaStreamSynchronize(h->st));
     h->diag_valid = true;
     return PSC_OK;
 }
 
-int build_graph(psc_handle *h) {
-    if (h->gexec) return PSC_OK;
-    cudaGraph_t graph = nullptr;
-    CU(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+// the kernels of one step (all stages) on stream st
+cudaError_t enqueue_step(psc_handle *h, cudaStream_t st) {
     cudaError_t err = cudaSuccess;
     for (int p = 0; p < h->s && err == cudaSuccess; ++p) {
-        err = psc::launch_stage(h->cfg, h->b, h->p.precision, 1, h->st);
-        if (err == cudaSuccess) err = psc::launch_scalar(h->cfg, h->b, psc::SCALAR_END, p, h->st);
+        err = psc::launch_stage(h->cfg, h->b, h->p0().precision, 1, st);
+        if (err == cudaSuccess) err = psc::launch_scalar(h->cfg, h->b, psc::SCALAR_END, p, st);
     }
-    cudaError_t e2 = cudaStreamEndCapture(h->st, &graph);
+    return err;
+}
+
+// the opening half kick of a call and the start of its first step
+cudaError_t enqueue_prologue(psc_handle *h, double dt, int nsteps, cudaStream_t st) {
+    cudaError_t e = psc::launch_set_run(h->b.bg, h->R, dt, nsteps, st);
+    if (e == cudaSuccess) e = psc::launch_scalar(h->cfg, h->b, psc::SCALAR_PRIME, 0, st);
+    if (e == cudaSuccess) e = psc::launch_stage(h->cfg, h->b, h->p0().precision, 0, st);
+    if (e == cudaSuccess) e = psc::launch_scalar(h->cfg, h->b, psc::SCALAR_BEGIN, 0, st);
+    return e;
+}
+
+int instantiate(cudaStream_t st, cudaError_t err, cudaGraphExec_t *out) {
+    cudaGraph_t graph = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(st, &graph);
     if (err != cudaSuccess) {
         if (graph) cudaGraphDestroy(graph);
         return fail(PSC_ERR_CUDA, std::string("step capture: ") + cudaGetErrorString(err));
     }
     if (e2 != cudaSuccess) return fail(PSC_ERR_CUDA, std::string("step capture: ") + cudaGetErrorString(e2));
-    cudaError_t e3 = cudaGraphInstantiate(&h->gexec, graph, 0);
+    cudaError_t e3 = cudaGraphInstantiate(out, graph, 0);
     cudaGraphDestroy(graph);
     if (e3 != cudaSuccess) {
-        h->gexec = nullptr;
+        *out = nullptr;
         return fail(PSC_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e3));
     }
     return PSC_OK;
 }
 
+int build_graph(psc_handle *h) {
+    if (h->gexec) return PSC_OK;
+    CU(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+    return instantiate(h->st, enqueue_step(h, h->st), &h->gexec);
+}
+
+int read_err(psc_handle *h) {
+    std::vector<psc::DevBG> bgs(h->R);
+    CU(cudaMemcpyAsync(bgs.data(), h->b.bg, sizeof(psc::DevBG) * h->R, cudaMemcpyDeviceToHost, h->st));
+    CU(cudaStreamSynchronize(h->st));
+    for (int r = 0; r < h->R; ++r)
+        if (bgs[r].err) return bgs[r].err;
+    return 0;
+}
+
+int create_handle(const psc_params *ps, int R, psc_handle **out) {
+    *out = nullptr;
+    int rc;
+    for (int r = 0; r < R; ++r)
+        if ((rc = validate(ps + r))) return rc;
+    psc_handle *h = new (std::nothrow) psc_handle();
+    if (!h) return fail(PSC_ERR_NOMEM, "host allocation failed");
+    h->p.assign(ps, ps + R);
+    for (auto &q : h->p)
+        if (q.fStar <= 0) q.fStar = q.MPl;
+    h->R = R;
+    const psc_params &p = h->p0();
+    switch (p.vv) {
+    case 4: h->s = 3; h->w = kW4; break;
+    case 6: h->s = 7; h->w = kW6; break;
+    case 8: h->s = 15; h->w = kW8; break;
+    case 10: h->s = 31; h->w = kW10; break;
+    default: h->s = 1; h->w = kW2;
+    }
+    h->csize = p.precision == 32 ? 8 : 16;
+    h->nb = psc_maxnumbins(p.N);
+    psc::plan(p, R, &h->cfg);
+    const psc::Geo &g = h->cfg.g;
+    auto bail = [&](int code) {
+        free_all(h);
+        delete h;
+        return code;
+    };
+#define CUB(call)                                                                                      \
+    do {                                                                                               \
+        cudaError_t e_ = (call);                                                                       \
+        if (e_ != cudaSuccess)                                                                         \
+            return bail(fail(e_ == cudaErrorMemoryAllocation ? PSC_ERR_NOMEM : PSC_ERR_CUDA,           \
+                             std::string(#call) + ": " + cudaGetErrorString(e_)));                     \
+    } while (0)
+    CUB(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+    CUB(cudaEventCreate(&h->ev0));
+    CUB(cudaEventCreate(&h->ev1));
+    CUB(psc::configure(h->cfg, p.precision));
+    const size_t farr = (size_t)R * g.fstride * h->csize;   // nf arrays per realization
+    const size_t garr = (size_t)R * g.gstride * h->csize;   // 6 arrays per realization (GW)
+    psc::Buffers &b = h->b;
+    if ((rc = dalloc(h, &b.fk, farr)) || (rc = dalloc(h, &b.pk, farr)) || (rc = dalloc(h, &b.TA, farr)) ||
+        (rc = dalloc(h, &b.QV, farr)))
+        return bail(rc);
+    if (g.gw) {
+        if ((rc = dalloc(h, &b.uk, garr)) || (rc = dalloc(h, &b.puk, garr)) || (rc = dalloc(h, &b.TB, farr)) ||
+            (rc = dalloc(h, &b.TC, farr)) || (rc = dalloc(h, &b.QS, garr)))
+            return bail(rc);
+    }
+    void *tmp = nullptr;
+    if ((rc = dalloc(h, &b.tw, (size_t)g.N * h->csize))) return bail(rc);
+    if ((rc = dalloc(h, &tmp, sizeof(double) * (size_t)R * g.pkg_stride))) return bail(rc);
+    b.partKG = static_cast<double *>(tmp);
+    if ((rc = dalloc(h, &tmp, sizeof(double) * (size_t)R * g.pv_stride))) return bail(rc);
+    b.partV = static_cast<double *>(tmp);
+    if ((rc = dalloc(h, &tmp, sizeof(double) * (g.nf * 3 + 2) * h->nb))) return bail(rc);
+    b.spec = static_cast<double *>(tmp);
+    if ((rc = dalloc(h, &tmp, sizeof(int) * (g.nf + 1) * h->nb))) return bail(rc);
+    b.spec_cnt = static_cast<int *>(tmp);
+    if ((rc = dalloc(h, &tmp, sizeof(psc::DevBG) * R))) return bail(rc);
+    b.bg = static_cast<psc::DevBG *>(tmp);
+    CUB(cudaMemsetAsync(b.fk, 0, farr, h->st));
+    CUB(cudaMemsetAsync(b.pk, 0, farr, h->st));
+    if (g.gw) {
+        CUB(cudaMemsetAsync(b.uk, 0, garr, h->st));
+        CUB(cudaMemsetAsync(b.puk, 0, garr, h->st));
+    }
+    // twiddles e^{-2 pi i q/N} from FP64 sin/cos
+    {
+        std::vector<double> tw(2 * g.N);
+        for (int q = 0; q < g.N; ++q) {
+            const double ang = 2.0 * kPi * (double)q / (double)g.N;
+            tw[2 * q] = std::cos(ang);
+            tw[2 * q + 1] = -std::sin(ang);
+        }
+        if ((rc = upload(h, b.tw, tw.data(), g.N))) return bail(rc);
+    }
+    for (int r = 0; r < R; ++r) {
+        const psc_params &q = h->p[r];
+        psc::DevBG bg{};
+        bg.a = q.a0;
+        bg.s = h->s;
+        for (int i = 0; i < h->s; ++i) bg.w[i] = h->w[i];
+        bg.alpha = q.alpha;
+        bg.nf = g.nf;
+        bg.nterms = g.nterms;
+        bg.mask = g.mask;
+        bg.model = q.model;
+        bg.nbx = h->cfg.nbx;
+        bg.nbz = h->cfg.nbz;
+        bg.kIR = q.kIR;
+        bg.kIR2 = q.kIR * q.kIR;
+        const double fStar = q.fStar, omegaStar = q.m_in_MPl * fStar;
+        const double L = 2 * kPi / q.kIR, dx = L / (double)q.N;
+        bg.DFDP = std::pow(omegaStar / fStar, 2) * (q.N / dx) / 2.;   // parameters.h:132
+        bg.fs_over_mpl2 = (fStar / q.MPl) * (fStar / q.MPl);
+        bg.eps = q.epsilon;
+        bg.gsq = q.gsq;
+        bg.inv_n3 = 1.0 / (double)g.sites;
+        bg.inv_n3sq = bg.inv_n3 * bg.inv_n3;
+        if ((rc = write_bg(h, r, bg))) return bail(rc);
+    }
+#undef CUB
+    *out = h;
+    return PSC_OK;
+}
+
+int init_ic(psc_handle *h) {
+    const psc::Geo &g = h->cfg.g;
+    const size_t n = (size_t)g.modes;
+    std::vector<double> fk(2 * n * g.nf), pk(2 * n * g.nf), uk, puk;
+    if (g.gw) {
+        uk.resize(2 * n * 6);
+        puk.resize(2 * n * 6);
+    }
+    int rc;
+    for (int r = 0; r < h->R; ++r) {
+        std::fill(fk.begin(), fk.end(), 0.0);
+        std::fill(pk.begin(), pk.end(), 0.0);
+        if (g.gw) {
+            std::fill(uk.begin(), uk.end(), 0.0);
+            std::fill(puk.begin(), puk.end(), 0.0);
+        }
+        psc::ICInfo info = psc::generate_ic(h->p[r], fk.data(), pk.data(), g.gw ? uk.data() : nullptr,
+                                            g.gw ? puk.data() : nullptr);
+        if ((rc = upload(h, foff(h, h->b.fk, r), fk.data(), n * g.nf)) ||
+            (rc = upload(h, foff(h, h->b.pk, r), pk.data(), n * g.nf)))
+            return rc;
+        if (g.gw && ((rc = upload(h, goff(h, h->b.uk, r), uk.data(), n * 6)) ||
+                     (rc = upload(h, goff(h, h->b.puk, r), puk.data(), n * 6))))
+            return rc;
+        psc::DevBG bg;
+        if ((rc = read_bg(h, r, &bg))) return rc;
+        bg.a = info.a;
+        bg.ad = info.ad;
+        bg.add = info.add_printed;
+        bg.t = 0.0;
+        bg.err = 0;
+        if ((rc = write_bg(h, r, bg))) return rc;
+    }
+    h->have_state = true;
+    // initialize() ends with add = kernel_a_k_nopad() / kernel_a() (initialize.cpp:786-797)
+    return evaluate(h, 0);
+}
+
+int set_state(psc_handle *h, int r, const double *f_k, const double *pi_k, double a, double ad, double add,
+              const double *u_k, const double *pi_u_k) {
+    if (!f_k || !pi_k) return fail(PSC_ERR_ARG, "null argument");
+    const psc::Geo &g = h->cfg.g;
+    if (g.gw && (!u_k || !pi_u_k)) return fail(PSC_ERR_ARG, "GW run needs u_k and pi_u_k");
+    const size_t n = (size_t)g.modes;
+    int rc;
+    if ((rc = upload(h, foff(h, h->b.fk, r), f_k, n * g.nf)) || (rc = upload(h, foff(h, h->b.pk, r), pi_k, n * g.nf)))
+        return rc;
+    if (g.gw && ((rc = upload(h, goff(h, h->b.uk, r), u_k, n * 6)) ||
+                 (rc = upload(h, goff(h, h->b.puk, r), pi_u_k, n * 6))))
+        return rc;
+    psc::DevBG bg;
+    if ((rc = read_bg(h, r, &bg))) return rc;
+    bg.a = a;
+    bg.ad = ad;
+    bg.add = add;
+    bg.err = 0;
+    if ((rc = write_bg(h, r, bg))) return rc;
+    h->have_state = true;
+    h->diag_valid = false;
+    return PSC_OK;
+}
+
+int get_state(psc_handle *h, int r, double *f_k, double *pi_k, double *a, double *ad, double *add, double *u_k,
+              double *pi_u_k) {
+    const psc::Geo &g = h->cfg.g;
+    const size_t n = (size_t)g.modes;
+    int rc;
+    if (f_k && (rc = download_real(h, f_k, foff(h, h->b.fk, r), 2 * n * g.nf))) return rc;
+    if (pi_k && (rc = download_real(h, pi_k, foff(h, h->b.pk, r), 2 * n * g.nf))) return rc;
+    if (g.gw) {
+        if (u_k && (rc = download_real(h, u_k, goff(h, h->b.uk, r), 2 * n * 6))) return rc;
+        if (pi_u_k && (rc = download_real(h, pi_u_k, goff(h, h->b.puk, r), 2 * n * 6))) return rc;
+    }
+    psc::DevBG bg;
+    if ((rc = read_bg(h, r, &bg))) return rc;
+    if (a) *a = bg.a;
+    if (ad) *ad = bg.ad;
+    if (add) *add = bg.add;
+    return PSC_OK;
+}
+
+int step(psc_handle *h, double dt, int nsteps) {
+    if (!h->have_state) return fail(PSC_ERR_STATE, "no state: call psc_init_ic or psc_set_state first");
+    if (nsteps < 0 || !(dt > 0) || !std::isfinite(dt)) return fail(PSC_ERR_ARG, "need dt > 0 and nsteps >= 0");
+    if (nsteps == 0) return PSC_OK;
+    int rc = build_graph(h);
+    if (rc) return rc;
+    CU(cudaEventRecord(h->ev0, h->st));
+    // opening half kick: pi_half = pi + w0 dt/2 F(f, a)  (evolution.cpp:1144-1158, stage 0)
+    CU(enqueue_prologue(h, dt, nsteps, h->st));
+    for (int i = 0; i < nsteps; ++i) CU(cudaGraphLaunch(h->gexec, h->st));
+    CU(cudaEventRecord(h->ev1, h->st));
+    const int err = read_err(h);
+    CU(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
+    h->diag_valid = true;
+    if (err) return fail(err, "non-finite background (NaN/Inf in a, a' or a'') during the step");
+    return PSC_OK;
+}
+
+int fields_real(psc_handle *h, int r, double *f, double *pi_f) {
+    const psc::Geo &g = h->cfg.g;
+    const size_t rsize = h->csize / 2;
+    int rc;
+    if (!h->b.real && (rc = dalloc(h, &h->b.real, (size_t)g.sites * g.nf * rsize))) return rc;
+    const psc::LaunchCfg c1 = single_cfg(h);
+    const psc::Buffers b1 = buffers_of(h, r);
+    if (f) {
+        CU(psc::launch_c2r_real(c1, b1, h->p0().precision, b1.fk, g.nf, h->st));
+        if ((rc = download_real(h, f, h->b.real, (size_t)g.sites * g.nf))) return rc;
+    }
+    if (pi_f) {
+        CU(psc::launch_c2r_real(c1, b1, h->p0().precision, b1.pk, g.nf, h->st));
+        if ((rc = download_real(h, pi_f, h->b.real, (size_t)g.sites * g.nf))) return rc;
+    }
+    return PSC_OK;
+}
+
+int spectra(psc_handle *h, int r, int32_t *numpoints, double *f2, double *pi2, double *n2, int32_t *gw_numpoints,
+            double *h2, double *hdot2, double *hdot2_zero) {
+    const psc::Geo &g = h->cfg.g;
+    const int nb = h->nb, nf = g.nf;
+    const psc::Buffers b1 = buffers_of(h, r);
+    CU(psc::launch_spectra(single_cfg(h), b1, h->p0().precision, nb, h->st));
+    std::vector<double> acc((size_t)(nf * 3 + 2) * nb);
+    std::vector<int> cnt((size_t)(nf + 1) * nb);
+    CU(cudaMemcpyAsync(acc.data(), h->b.spec, acc.size() * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CU(cudaMemcpyAsync(cnt.data(), h->b.spec_cnt, cnt.size() * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CU(cudaStreamSynchronize(h->st));
+    for (int f = 0; f < nf; ++f)
+        for (int l = 0; l < nb; ++l) {
+            const int c = cnt[(size_t)f * nb + l];
+            const double d = c > 0 ? (double)c : 1.0;
+            if (numpoints) numpoints[(size_t)f * nb + l] = c;
+            if (f2) f2[(size_t)f * nb + l] = acc[(size_t)f * 3 * nb + l] / d;
+            if (pi2) pi2[(size_t)f * nb + l] = acc[(size_t)f * 3 * nb + nb + l] / d;
+            if (n2) n2[(size_t)f * nb + l] = acc[(size_t)f * 3 * nb + 2 * nb + l] / d;
+        }
+    if (hdot2_zero) *hdot2_zero = 0.0;
+    if (g.gw) {
+        const double *H = acc.data() + (size_t)nf * 3 * nb, *D = H + nb;
+        const int *C = cnt.data() + (size_t)nf * nb;
+        for (int l = 0; l < nb; ++l) {
+            const double d = (C[l] > 0 && l >= 1) ? (double)C[l] : 1.0;
+            if (gw_numpoints) gw_numpoints[l] = C[l];
+            if (h2) h2[l] = H[l] / d;
+            if (hdot2) hdot2[l] = D[l] / d;
+        }
+        if (hdot2_zero) {
+            // |pi_u_k(0)|^2 over the nine components (output.cpp:1033-1039)
+            double z = 0.0;
+            for (int c = 0; c < 6; ++c) {
+                double v[2];
+                const char *base = static_cast<const char *>(b1.puk) + (size_t)c * g.modes * h->csize;
+                if (h->p0().precision == 64) {
+                    CU(cudaMemcpy(v, base, 16, cudaMemcpyDeviceToHost));
+                } else {
+                    float fv[2];
+                    CU(cudaMemcpy(fv, base, 8, cudaMemcpyDeviceToHost));
+                    v[0] = fv[0];
+                    v[1] = fv[1];
+                }
+                const double mult = (c == 0 || c == 3 || c == 5) ? 1.0 : 2.0;
+                z += mult * (v[0] * v[0] + v[1] * v[1]);
+            }
+            *hdot2_zero = z;
+        }
+    }
+    return PSC_OK;
+}
+
+int energies(psc_handle *h, int r, double *K, double *G, double *V, double *total, double *friedmann_violation,
+             double *rho_gw) {
+    int rc;
+    if (!h->diag_valid && (rc = evaluate(h, 1))) return rc;
+    psc::DevBG bg;
+    if ((rc = read_bg(h, r, &bg))) return rc;
+    const psc::Geo &g = h->cfg.g;
+    const psc_params &q = h->p[r];
+    double tot = 0.0;
+    for (int f = 0; f < g.nf; ++f) {
+        if (K) K[f] = bg.K[f];
+        if (G) G[f] = bg.G[f];
+        tot += bg.K[f];
+        tot += bg.G[f];
+    }
+    for (int t = 0; t < g.nterms; ++t) {
+        if (V) V[t] = bg.V[t];
+        tot += bg.V[t];
+    }
+    if (total) *total = tot;
+    // energy(), output.cpp:1178-1185
+    const double LHS = bg.ad * bg.ad;
+    const double RHS = bg.fs_over_mpl2 * std::pow(bg.a, 2 * (q.alpha + 1)) * tot / 3.;
+    if (friedmann_violation) *friedmann_violation = std::fabs(LHS - RHS) / std::fabs(LHS + RHS);
+    if (rho_gw) {
+        *rho_gw = 0.0;
+        if (g.gw) {
+            // output.cpp:1030-1060: zero mode plus the un-normalised bins
+            const int nb = h->nb;
+            std::vector<int> cnt(nb);
+            std::vector<double> hd(nb);
+            double hz = 0.0;
+            if ((rc = spectra(h, r, nullptr, nullptr, nullptr, nullptr, cnt.data(), nullptr, hd.data(), &hz)))
+                return rc;
+            double s = hz;
+            for (int l = 1; l < nb; ++l) s += hd[l] * (cnt[l] > 0 ? cnt[l] : 1);
+            const double fStar = q.fStar, omegaStar = q.m_in_MPl * fStar, MPl = q.MPl;
+            s *= omegaStar * omegaStar * std::pow(fStar, 4) / (MPl * MPl) / 4. * bg.inv_n3sq / std::pow(bg.a, 6);
+            s /= (fStar * omegaStar) * (fStar * omegaStar);
+            *rho_gw = s;
+        }
+    }
+    return PSC_OK;
+}
+
+int means(psc_handle *h, int r, double *out) {
+    const psc::Geo &g = h->cfg.g;
+    std::vector<double> f((size_t)g.sites * g.nf), pf((size_t)g.sites * g.nf);
+    int rc = fields_real(h, r, f.data(), pf.data());
+    if (rc) return rc;
+    psc::DevBG bg;
+    if ((rc = read_bg(h, r, &bg))) return rc;
+    const double aop = std::pow(bg.a, h->p[r].alpha - 3);
+    const double n = (double)g.sites;
+    for (int fl = 0; fl < g.nf; ++fl) {
+        double fa = 0, f2 = 0, pa = 0, p2 = 0;
+        const double *x = f.data() + (size_t)fl * g.sites, *y = pf.data() + (size_t)fl * g.sites;
+        for (long long i = 0; i < g.sites; ++i) {
+            fa += x[i];
+            f2 += x[i] * x[i];
+            pa += y[i];
+            p2 += y[i] * y[i];
+        }
+        fa /= n;
+        f2 /= n;
+        pa /= n;
+        p2 /= n;
+        double *o = out + 6 * fl;
+        o[0] = fa;
+        o[1] = aop * pa;
+        o[2] = f2;
+        o[3] = aop * aop * p2;
+        o[4] = (f2 - fa * fa > 0) ? std::sqrt(f2 - fa * fa) : 0;
+        o[5] = (p2 - pa * pa > 0) ? aop * std::sqrt(p2 - pa * pa) : 0;
+    }
+    return PSC_OK;
+}
+
 }  // namespace
+
+// ------------------------------------------------------------------ batches
+struct psc_batch {
+    std::vector<psc_handle *> groups;
+    std::vector<std::pair<int, int>> where;   // realization index -> (group, slot)
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<cudaEvent_t> join;
+    cudaEvent_t fork = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    float last_ms = 0.f;
+};
 
 extern "C" {
 
@@ -237,105 +685,8 @@ int psc_maxnumbins(int N) { return (int)(std::sqrt(3.0) * (N / 2)) + 2; }
 int psc_create(const psc_params *p, psc_handle **out) {
     if (!out) return fail(PSC_ERR_ARG, "null output handle");
     *out = nullptr;
-    int rc = validate(p);
-    if (rc) return rc;
-    psc_handle *h = new (std::nothrow) psc_handle();
-    if (!h) return fail(PSC_ERR_NOMEM, "host allocation failed");
-    h->p = *p;
-    if (h->p.fStar <= 0) h->p.fStar = h->p.MPl;
-    switch (p->vv) {
-    case 4: h->s = 3; h->w = kW4; break;
-    case 6: h->s = 7; h->w = kW6; break;
-    case 8: h->s = 15; h->w = kW8; break;
-    case 10: h->s = 31; h->w = kW10; break;
-    default: h->s = 1; h->w = kW2;
-    }
-    h->csize = p->precision == 32 ? 8 : 16;
-    h->nb = psc_maxnumbins(p->N);
-    psc::plan(h->p, &h->cfg);
-    const psc::Geo &g = h->cfg.g;
-    auto bail = [&](int code) {
-        free_all(h);
-        delete h;
-        return code;
-    };
-#define CUB(call)                                                                                      \
-    do {                                                                                               \
-        cudaError_t e_ = (call);                                                                       \
-        if (e_ != cudaSuccess)                                                                         \
-            return bail(fail(e_ == cudaErrorMemoryAllocation ? PSC_ERR_NOMEM : PSC_ERR_CUDA,           \
-                             std::string(#call) + ": " + cudaGetErrorString(e_)));                     \
-    } while (0)
-    CUB(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
-    CUB(cudaEventCreate(&h->ev0));
-    CUB(cudaEventCreate(&h->ev1));
-    CUB(psc::configure(h->cfg, p->precision));
-    const size_t arr = (size_t)g.modes * h->csize;
-    const int nf = g.nf;
-    psc::Buffers &b = h->b;
-    if ((rc = dalloc(h, &b.fk, nf * arr)) || (rc = dalloc(h, &b.pk, nf * arr)) || (rc = dalloc(h, &b.TA, nf * arr)) ||
-        (rc = dalloc(h, &b.QV, nf * arr)))
-        return bail(rc);
-    if (g.gw) {
-        if ((rc = dalloc(h, &b.uk, 6 * arr)) || (rc = dalloc(h, &b.puk, 6 * arr)) || (rc = dalloc(h, &b.TB, nf * arr)) ||
-            (rc = dalloc(h, &b.TC, nf * arr)) || (rc = dalloc(h, &b.QS, 6 * arr)))
-            return bail(rc);
-    }
-    void *tmp = nullptr;
-    if ((rc = dalloc(h, &b.tw, (size_t)g.N * h->csize))) return bail(rc);
-    if ((rc = dalloc(h, &tmp, sizeof(double) * 2 * psc::kMaxFields * h->cfg.nbx))) return bail(rc);
-    b.partKG = static_cast<double *>(tmp);
-    if ((rc = dalloc(h, &tmp, sizeof(double) * psc::kMaxTerms * h->cfg.nbz))) return bail(rc);
-    b.partV = static_cast<double *>(tmp);
-    if ((rc = dalloc(h, &tmp, sizeof(double) * (nf * 3 + 2) * h->nb))) return bail(rc);
-    b.spec = static_cast<double *>(tmp);
-    if ((rc = dalloc(h, &tmp, sizeof(int) * (nf + 1) * h->nb))) return bail(rc);
-    b.spec_cnt = static_cast<int *>(tmp);
-    if ((rc = dalloc(h, &tmp, sizeof(psc::DevBG)))) return bail(rc);
-    b.bg = static_cast<psc::DevBG *>(tmp);
-    CUB(cudaMemsetAsync(b.fk, 0, nf * arr, h->st));
-    CUB(cudaMemsetAsync(b.pk, 0, nf * arr, h->st));
-    if (g.gw) {
-        CUB(cudaMemsetAsync(b.uk, 0, 6 * arr, h->st));
-        CUB(cudaMemsetAsync(b.puk, 0, 6 * arr, h->st));
-    }
-    // twiddles e^{-2 pi i q/N} from FP64 sin/cos
-    {
-        std::vector<double> tw(2 * g.N);
-        for (int q = 0; q < g.N; ++q) {
-            const double ang = 2.0 * 3.14159265358979323846 * (double)q / (double)g.N;
-            tw[2 * q] = std::cos(ang);
-            tw[2 * q + 1] = -std::sin(ang);
-        }
-        if ((rc = upload(h, b.tw, tw.data(), g.N))) return bail(rc);
-    }
-    psc::DevBG bg{};
-    bg.a = h->p.a0;
-    bg.s = h->s;
-    for (int i = 0; i < h->s; ++i) bg.w[i] = h->w[i];
-    bg.alpha = p->alpha;
-    bg.nf = nf;
-    bg.nterms = g.nterms;
-    bg.mask = g.mask;
-    bg.model = p->model;
-    bg.nbx = h->cfg.nbx;
-    bg.nbz = h->cfg.nbz;
-    bg.kIR = p->kIR;
-    bg.kIR2 = p->kIR * p->kIR;
-    {
-        const double fStar = h->p.fStar, omegaStar = p->m_in_MPl * fStar;
-        const double L = 2 * 3.14159265358979323846 / p->kIR, dx = L / (double)p->N;
-        bg.DFDP = std::pow(omegaStar / fStar, 2) * (p->N / dx) / 2.;   // parameters.h:132
-        bg.fs_over_mpl2 = (fStar / p->MPl) * (fStar / p->MPl);
-    }
-    bg.eps = p->epsilon;
-    bg.gsq = p->gsq;
-    bg.inv_n3 = 1.0 / (double)g.sites;
-    bg.inv_n3sq = bg.inv_n3 * bg.inv_n3;
-    if ((rc = write_bg(h, bg))) return bail(rc);
-#undef CUB
-    *out = h;
-    return PSC_OK;
+    if (!p) return fail(PSC_ERR_ARG, "null parameters");
+    return create_handle(p, 1, out);
 }
 
 void psc_destroy(psc_handle *h) {
@@ -347,30 +698,7 @@ void psc_destroy(psc_handle *h) {
 
 int psc_init_ic(psc_handle *h) {
     if (!h) return fail(PSC_ERR_ARG, "null handle");
-    const psc::Geo &g = h->cfg.g;
-    const size_t n = (size_t)g.modes;
-    std::vector<double> fk(2 * n * g.nf, 0.0), pk(2 * n * g.nf, 0.0), uk, puk;
-    if (g.gw) {
-        uk.assign(2 * n * 6, 0.0);
-        puk.assign(2 * n * 6, 0.0);
-    }
-    psc::ICInfo info = psc::generate_ic(h->p, fk.data(), pk.data(), g.gw ? uk.data() : nullptr,
-                                        g.gw ? puk.data() : nullptr);
-    int rc;
-    if ((rc = upload(h, h->b.fk, fk.data(), n * g.nf)) || (rc = upload(h, h->b.pk, pk.data(), n * g.nf))) return rc;
-    if (g.gw && ((rc = upload(h, h->b.uk, uk.data(), n * 6)) || (rc = upload(h, h->b.puk, puk.data(), n * 6))))
-        return rc;
-    psc::DevBG bg;
-    if ((rc = read_bg(h, &bg))) return rc;
-    bg.a = info.a;
-    bg.ad = info.ad;
-    bg.add = info.add_printed;
-    bg.t = 0.0;
-    bg.err = 0;
-    if ((rc = write_bg(h, bg))) return rc;
-    h->have_state = true;
-    // initialize() ends with add = kernel_a_k_nopad() / kernel_a() (initialize.cpp:786-797)
-    return evaluate(h, 0);
+    return init_ic(h);
 }
 
 int psc_generate_ic(const psc_params *p, double *f_k, double *pi_k, double *u_k, double *pi_u_k, double *info) {
@@ -400,49 +728,20 @@ int psc_generate_ic(const psc_params *p, double *f_k, double *pi_k, double *u_k,
 
 int psc_set_state(psc_handle *h, const double *f_k, const double *pi_k, double a, double ad, double add,
                   const double *u_k, const double *pi_u_k) {
-    if (!h || !f_k || !pi_k) return fail(PSC_ERR_ARG, "null argument");
-    const psc::Geo &g = h->cfg.g;
-    if (g.gw && (!u_k || !pi_u_k)) return fail(PSC_ERR_ARG, "GW run needs u_k and pi_u_k");
-    const size_t n = (size_t)g.modes;
-    int rc;
-    if ((rc = upload(h, h->b.fk, f_k, n * g.nf)) || (rc = upload(h, h->b.pk, pi_k, n * g.nf))) return rc;
-    if (g.gw && ((rc = upload(h, h->b.uk, u_k, n * 6)) || (rc = upload(h, h->b.puk, pi_u_k, n * 6)))) return rc;
-    psc::DevBG bg;
-    if ((rc = read_bg(h, &bg))) return rc;
-    bg.a = a;
-    bg.ad = ad;
-    bg.add = add;
-    bg.err = 0;
-    if ((rc = write_bg(h, bg))) return rc;
-    h->have_state = true;
-    h->diag_valid = false;
-    return PSC_OK;
+    if (!h) return fail(PSC_ERR_ARG, "null handle");
+    return set_state(h, 0, f_k, pi_k, a, ad, add, u_k, pi_u_k);
 }
 
 int psc_get_state(psc_handle *h, double *f_k, double *pi_k, double *a, double *ad, double *add, double *u_k,
                   double *pi_u_k) {
     if (!h) return fail(PSC_ERR_ARG, "null handle");
-    const psc::Geo &g = h->cfg.g;
-    const size_t n = (size_t)g.modes;
-    int rc;
-    if (f_k && (rc = download_real(h, f_k, h->b.fk, 2 * n * g.nf))) return rc;
-    if (pi_k && (rc = download_real(h, pi_k, h->b.pk, 2 * n * g.nf))) return rc;
-    if (g.gw) {
-        if (u_k && (rc = download_real(h, u_k, h->b.uk, 2 * n * 6))) return rc;
-        if (pi_u_k && (rc = download_real(h, pi_u_k, h->b.puk, 2 * n * 6))) return rc;
-    }
-    psc::DevBG bg;
-    if ((rc = read_bg(h, &bg))) return rc;
-    if (a) *a = bg.a;
-    if (ad) *ad = bg.ad;
-    if (add) *add = bg.add;
-    return PSC_OK;
+    return get_state(h, 0, f_k, pi_k, a, ad, add, u_k, pi_u_k);
 }
 
 int psc_get_time(psc_handle *h, double *t) {
     if (!h || !t) return fail(PSC_ERR_ARG, "null argument");
     psc::DevBG bg;
-    int rc = read_bg(h, &bg);
+    int rc = read_bg(h, 0, &bg);
     if (rc) return rc;
     *t = bg.t;
     return PSC_OK;
@@ -451,34 +750,15 @@ int psc_get_time(psc_handle *h, double *t) {
 int psc_set_time(psc_handle *h, double t) {
     if (!h) return fail(PSC_ERR_ARG, "null handle");
     psc::DevBG bg;
-    int rc = read_bg(h, &bg);
+    int rc = read_bg(h, 0, &bg);
     if (rc) return rc;
     bg.t = t;
-    return write_bg(h, bg);
+    return write_bg(h, 0, bg);
 }
 
 int psc_step(psc_handle *h, double dt, int nsteps) {
     if (!h) return fail(PSC_ERR_ARG, "null handle");
-    if (!h->have_state) return fail(PSC_ERR_STATE, "no state: call psc_init_ic or psc_set_state first");
-    if (nsteps < 0 || !(dt > 0) || !std::isfinite(dt)) return fail(PSC_ERR_ARG, "need dt > 0 and nsteps >= 0");
-    if (nsteps == 0) return PSC_OK;
-    int rc = build_graph(h);
-    if (rc) return rc;
-    CU(cudaEventRecord(h->ev0, h->st));
-    CU(psc::launch_set_run(h->b.bg, dt, nsteps, h->st));
-    // opening half kick: pi_half = pi + w0 dt/2 F(f, a)  (evolution.cpp:1144-1158, stage 0)
-    CU(psc::launch_scalar(h->cfg, h->b, psc::SCALAR_PRIME, 0, h->st));
-    CU(psc::launch_stage(h->cfg, h->b, h->p.precision, 0, h->st));
-    CU(psc::launch_scalar(h->cfg, h->b, psc::SCALAR_BEGIN, 0, h->st));
-    for (int i = 0; i < nsteps; ++i) CU(cudaGraphLaunch(h->gexec, h->st));
-    CU(cudaEventRecord(h->ev1, h->st));
-    int err = 0;
-    CU(cudaMemcpyAsync(&err, &h->b.bg->err, sizeof(int), cudaMemcpyDeviceToHost, h->st));
-    CU(cudaStreamSynchronize(h->st));
-    CU(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
-    h->diag_valid = true;
-    if (err) return fail(err, "non-finite background (NaN/Inf in a, a' or a'') during the step");
-    return PSC_OK;
+    return step(h, dt, nsteps);
 }
 
 int psc_last_step_ms(psc_handle *h, float *ms) {
@@ -496,7 +776,7 @@ int psc_time_passes(psc_handle *h, int reps, float *ms) {
     // zero-length kicks: the state is unchanged; a'' is kept (diagnostics mode)
     for (int r = 0; r < reps; ++r) {
         CU(psc::launch_scalar(h->cfg, h->b, psc::SCALAR_EVAL, 0, h->st));
-        CU(psc::launch_stage_timed(h->cfg, h->b, h->p.precision, 0, psc::SCALAR_EVAL_END, ev, h->st));
+        CU(psc::launch_stage_timed(h->cfg, h->b, h->p0().precision, 0, psc::SCALAR_EVAL_END, ev, h->st));
         CU(cudaEventSynchronize(ev[6]));
         for (int i = 0; i < PSC_NPASS; ++i) {
             float t = 0.f;
@@ -513,9 +793,8 @@ int psc_time_passes(psc_handle *h, int reps, float *ms) {
 int psc_pass_bytes(psc_handle *h, double *bytes) {
     if (!h || !bytes) return fail(PSC_ERR_ARG, "bad argument");
     const psc::Geo &g = h->cfg.g;
-    const double C = (double)g.modes * h->csize, R = (double)g.sites * (h->csize / 2);
+    const double C = (double)g.modes * h->csize * h->R;
     const int nf = g.nf, gw = g.gw;
-    (void)R;
     // X inverse: read f_k, pi_half; write f_k, TA [, TB]
     bytes[0] = nf * (4 + gw) * C;
     // Y inverse: read TA [, TB]; write TA [, TB, TC]
@@ -532,150 +811,183 @@ int psc_pass_bytes(psc_handle *h, double *bytes) {
 
 int psc_get_fields_real(psc_handle *h, double *f, double *pi_f) {
     if (!h) return fail(PSC_ERR_ARG, "null handle");
-    const psc::Geo &g = h->cfg.g;
-    const size_t rsize = h->csize / 2;
-    int rc;
-    if (!h->b.real && (rc = dalloc(h, &h->b.real, (size_t)g.sites * g.nf * rsize))) return rc;
-    if (f) {
-        CU(psc::launch_c2r_real(h->cfg, h->b, h->p.precision, h->b.fk, g.nf, h->st));
-        if ((rc = download_real(h, f, h->b.real, (size_t)g.sites * g.nf))) return rc;
-    }
-    if (pi_f) {
-        CU(psc::launch_c2r_real(h->cfg, h->b, h->p.precision, h->b.pk, g.nf, h->st));
-        if ((rc = download_real(h, pi_f, h->b.real, (size_t)g.sites * g.nf))) return rc;
-    }
-    return PSC_OK;
+    return fields_real(h, 0, f, pi_f);
 }
 
 int psc_spectra(psc_handle *h, int32_t *numpoints, double *f2, double *pi2, double *n2, int32_t *gw_numpoints,
                 double *h2, double *hdot2, double *hdot2_zero) {
     if (!h) return fail(PSC_ERR_ARG, "null handle");
-    const psc::Geo &g = h->cfg.g;
-    const int nb = h->nb, nf = g.nf;
-    CU(psc::launch_spectra(h->cfg, h->b, h->p.precision, nb, h->st));
-    std::vector<double> acc((size_t)(nf * 3 + 2) * nb);
-    std::vector<int> cnt((size_t)(nf + 1) * nb);
-    CU(cudaMemcpyAsync(acc.data(), h->b.spec, acc.size() * sizeof(double), cudaMemcpyDeviceToHost, h->st));
-    CU(cudaMemcpyAsync(cnt.data(), h->b.spec_cnt, cnt.size() * sizeof(int), cudaMemcpyDeviceToHost, h->st));
-    CU(cudaStreamSynchronize(h->st));
-    for (int f = 0; f < nf; ++f)
-        for (int l = 0; l < nb; ++l) {
-            const int c = cnt[(size_t)f * nb + l];
-            const double d = c > 0 ? (double)c : 1.0;
-            if (numpoints) numpoints[(size_t)f * nb + l] = c;
-            if (f2) f2[(size_t)f * nb + l] = acc[(size_t)f * 3 * nb + l] / d;
-            if (pi2) pi2[(size_t)f * nb + l] = acc[(size_t)f * 3 * nb + nb + l] / d;
-            if (n2) n2[(size_t)f * nb + l] = acc[(size_t)f * 3 * nb + 2 * nb + l] / d;
-        }
-    if (g.gw) {
-        const double *H = acc.data() + (size_t)nf * 3 * nb, *D = H + nb;
-        const int *C = cnt.data() + (size_t)nf * nb;
-        for (int l = 0; l < nb; ++l) {
-            const double d = (C[l] > 0 && l >= 1) ? (double)C[l] : 1.0;
-            if (gw_numpoints) gw_numpoints[l] = C[l];
-            if (h2) h2[l] = H[l] / d;
-            if (hdot2) hdot2[l] = D[l] / d;
-        }
-        if (hdot2_zero) {
-            // |pi_u_k(0)|^2 over the nine components (output.cpp:1033-1039)
-            double z = 0.0;
-            for (int c = 0; c < 6; ++c) {
-                double v[2];
-                const char *base = static_cast<const char *>(h->b.puk) + (size_t)c * g.modes * h->csize;
-                if (h->p.precision == 64) {
-                    CU(cudaMemcpy(v, base, 16, cudaMemcpyDeviceToHost));
-                } else {
-                    float fv[2];
-                    CU(cudaMemcpy(fv, base, 8, cudaMemcpyDeviceToHost));
-                    v[0] = fv[0];
-                    v[1] = fv[1];
-                }
-                const double mult = (c == 0 || c == 3 || c == 5) ? 1.0 : 2.0;
-                z += mult * (v[0] * v[0] + v[1] * v[1]);
-            }
-            *hdot2_zero = z;
-        }
-    } else {
-        if (hdot2_zero) *hdot2_zero = 0.0;
-    }
-    return PSC_OK;
+    return spectra(h, 0, numpoints, f2, pi2, n2, gw_numpoints, h2, hdot2, hdot2_zero);
 }
 
 int psc_energies(psc_handle *h, double *K, double *G, double *V, double *total, double *friedmann_violation,
                  double *rho_gw) {
     if (!h) return fail(PSC_ERR_ARG, "null handle");
-    int rc;
-    if (!h->diag_valid && (rc = evaluate(h, 1))) return rc;
-    psc::DevBG bg;
-    if ((rc = read_bg(h, &bg))) return rc;
-    const psc::Geo &g = h->cfg.g;
-    double tot = 0.0;
-    for (int f = 0; f < g.nf; ++f) {
-        if (K) K[f] = bg.K[f];
-        if (G) G[f] = bg.G[f];
-        tot += bg.K[f];
-        tot += bg.G[f];
-    }
-    for (int t = 0; t < g.nterms; ++t) {
-        if (V) V[t] = bg.V[t];
-        tot += bg.V[t];
-    }
-    if (total) *total = tot;
-    // energy(), output.cpp:1178-1185
-    const double LHS = bg.ad * bg.ad;
-    const double RHS = bg.fs_over_mpl2 * std::pow(bg.a, 2 * (h->p.alpha + 1)) * tot / 3.;
-    if (friedmann_violation) *friedmann_violation = std::fabs(LHS - RHS) / std::fabs(LHS + RHS);
-    if (rho_gw) {
-        *rho_gw = 0.0;
-        if (g.gw) {
-            // output.cpp:1030-1060: zero mode plus the un-normalised bins
-            const int nb = h->nb;
-            std::vector<int> cnt(nb);
-            std::vector<double> hd(nb);
-            double hz = 0.0;
-            if ((rc = psc_spectra(h, nullptr, nullptr, nullptr, nullptr, cnt.data(), nullptr, hd.data(), &hz)))
-                return rc;
-            double r = hz;
-            for (int l = 1; l < nb; ++l) r += hd[l] * (cnt[l] > 0 ? cnt[l] : 1);
-            const double fStar = h->p.fStar, omegaStar = h->p.m_in_MPl * fStar, MPl = h->p.MPl;
-            r *= omegaStar * omegaStar * std::pow(fStar, 4) / (MPl * MPl) / 4. * bg.inv_n3sq / std::pow(bg.a, 6);
-            r /= (fStar * omegaStar) * (fStar * omegaStar);
-            *rho_gw = r;
-        }
-    }
-    return PSC_OK;
+    return energies(h, 0, K, G, V, total, friedmann_violation, rho_gw);
 }
 
 int psc_means(psc_handle *h, double *out) {
     if (!h || !out) return fail(PSC_ERR_ARG, "null argument");
-    const psc::Geo &g = h->cfg.g;
-    std::vector<double> f((size_t)g.sites * g.nf), pf((size_t)g.sites * g.nf);
-    int rc = psc_get_fields_real(h, f.data(), pf.data());
-    if (rc) return rc;
-    psc::DevBG bg;
-    if ((rc = read_bg(h, &bg))) return rc;
-    const double aop = std::pow(bg.a, h->p.alpha - 3);
-    const double n = (double)g.sites;
-    for (int fl = 0; fl < g.nf; ++fl) {
-        double fa = 0, f2 = 0, pa = 0, p2 = 0;
-        const double *x = f.data() + (size_t)fl * g.sites, *y = pf.data() + (size_t)fl * g.sites;
-        for (long long i = 0; i < g.sites; ++i) {
-            fa += x[i];
-            f2 += x[i] * x[i];
-            pa += y[i];
-            p2 += y[i] * y[i];
+    return means(h, 0, out);
+}
+
+// ------------------------------------------------------------------ batches
+int psc_batch_create(const psc_params *per_realization, int n, psc_batch **out) {
+    if (!out || !per_realization || n < 1) return fail(PSC_ERR_ARG, "bad argument");
+    *out = nullptr;
+    for (int i = 0; i < n; ++i) {
+        int rc = validate(per_realization + i);
+        if (rc) return rc;
+    }
+    // group realizations that can share launches, in order of first appearance
+    std::map<decltype(config_key(per_realization[0])), int> gid;
+    std::vector<std::vector<int>> members;
+    for (int i = 0; i < n; ++i) {
+        auto key = config_key(per_realization[i]);
+        auto it = gid.find(key);
+        if (it == gid.end()) {
+            it = gid.emplace(key, (int)members.size()).first;
+            members.emplace_back();
         }
-        fa /= n; f2 /= n; pa /= n; p2 /= n;
-        double *o = out + 6 * fl;
-        o[0] = fa;
-        o[1] = aop * pa;
-        o[2] = f2;
-        o[3] = aop * aop * p2;
-        o[4] = (f2 - fa * fa > 0) ? std::sqrt(f2 - fa * fa) : 0;
-        o[5] = (p2 - pa * pa > 0) ? aop * std::sqrt(p2 - pa * pa) : 0;
+        members[it->second].push_back(i);
+    }
+    psc_batch *b = new (std::nothrow) psc_batch();
+    if (!b) return fail(PSC_ERR_NOMEM, "host allocation failed");
+    b->where.resize(n);
+    auto bail = [&](int code) {
+        psc_batch_destroy(b);
+        return code;
+    };
+    for (size_t g = 0; g < members.size(); ++g) {
+        std::vector<psc_params> ps;
+        for (size_t k = 0; k < members[g].size(); ++k) {
+            ps.push_back(per_realization[members[g][k]]);
+            b->where[members[g][k]] = {(int)g, (int)k};
+        }
+        psc_handle *h = nullptr;
+        int rc = create_handle(ps.data(), (int)ps.size(), &h);
+        if (rc) return bail(rc);
+        b->groups.push_back(h);
+    }
+    if (cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess)
+        return bail(fail(PSC_ERR_CUDA, "batch stream/event creation failed"));
+    b->join.resize(b->groups.size());
+    for (auto &e : b->join)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+            return bail(fail(PSC_ERR_CUDA, "batch event creation failed"));
+    *out = b;
+    return PSC_OK;
+}
+
+void psc_batch_destroy(psc_batch *b) {
+    if (!b) return;
+    if (b->st) cudaStreamSynchronize(b->st);
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    for (psc_handle *h : b->groups) psc_destroy(h);
+    for (cudaEvent_t e : b->join)
+        if (e) cudaEventDestroy(e);
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->st) cudaStreamDestroy(b->st);
+    delete b;
+}
+
+int psc_batch_size(psc_batch *b) { return b ? (int)b->where.size() : 0; }
+
+int psc_batch_groups(psc_batch *b) { return b ? (int)b->groups.size() : 0; }
+
+int psc_batch_init_ic(psc_batch *b) {
+    if (!b) return fail(PSC_ERR_ARG, "null batch");
+    for (psc_handle *h : b->groups) {
+        int rc = init_ic(h);
+        if (rc) return rc;
     }
     return PSC_OK;
 }
+
+int psc_batch_step(psc_batch *b, double dt, int nsteps) {
+    if (!b) return fail(PSC_ERR_ARG, "null batch");
+    for (psc_handle *h : b->groups)
+        if (!h->have_state) return fail(PSC_ERR_STATE, "no state: call psc_batch_init_ic first");
+    if (nsteps < 0 || !(dt > 0) || !std::isfinite(dt)) return fail(PSC_ERR_ARG, "need dt > 0 and nsteps >= 0");
+    if (nsteps == 0) return PSC_OK;
+    // one graph per step for every group: fork to the groups' streams, join back
+    auto fork_join = [&](auto &&body) -> cudaError_t {
+        cudaError_t e = cudaEventRecord(b->fork, b->st);
+        for (size_t g = 0; g < b->groups.size() && e == cudaSuccess; ++g) {
+            psc_handle *h = b->groups[g];
+            e = cudaStreamWaitEvent(h->st, b->fork, 0);
+            if (e == cudaSuccess) e = body(h);
+            if (e == cudaSuccess) e = cudaEventRecord(b->join[g], h->st);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(b->st, b->join[g], 0);
+        }
+        return e;
+    };
+    if (!b->gexec) {
+        CU(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+        const cudaError_t err = fork_join([&](psc_handle *h) { return enqueue_step(h, h->st); });
+        int rc = instantiate(b->st, err, &b->gexec);
+        if (rc) return rc;
+    }
+    CU(cudaEventRecord(b->ev0, b->st));
+    CU(fork_join([&](psc_handle *h) { return enqueue_prologue(h, dt, nsteps, h->st); }));
+    for (int i = 0; i < nsteps; ++i) CU(cudaGraphLaunch(b->gexec, b->st));
+    CU(cudaEventRecord(b->ev1, b->st));
+    CU(cudaStreamSynchronize(b->st));
+    CU(cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1));
+    for (psc_handle *h : b->groups) {
+        h->diag_valid = true;
+        const int err = read_err(h);
+        if (err) return fail(err, "non-finite background in a realization of the batch");
+    }
+    return PSC_OK;
+}
+
+int psc_batch_last_step_ms(psc_batch *b, float *ms) {
+    if (!b || !ms) return fail(PSC_ERR_ARG, "null argument");
+    *ms = b->last_ms;
+    return PSC_OK;
+}
+
+#define PSC_BATCH_AT(b, idx, h, r)                                                                              \
+    if (!(b) || (idx) < 0 || (idx) >= (int)(b)->where.size()) return fail(PSC_ERR_ARG, "bad realization index"); \
+    psc_handle *h = (b)->groups[(b)->where[idx].first];                                                         \
+    const int r = (b)->where[idx].second
+
+int psc_batch_set_state(psc_batch *b, int idx, const double *f_k, const double *pi_k, double a, double ad, double add,
+                        const double *u_k, const double *pi_u_k) {
+    PSC_BATCH_AT(b, idx, h, r);
+    return set_state(h, r, f_k, pi_k, a, ad, add, u_k, pi_u_k);
+}
+
+int psc_batch_get_state(psc_batch *b, int idx, double *f_k, double *pi_k, double *a, double *ad, double *add,
+                        double *u_k, double *pi_u_k) {
+    PSC_BATCH_AT(b, idx, h, r);
+    return get_state(h, r, f_k, pi_k, a, ad, add, u_k, pi_u_k);
+}
+
+int psc_batch_spectra(psc_batch *b, int idx, int32_t *numpoints, double *f2, double *pi2, double *n2,
+                      int32_t *gw_numpoints, double *h2, double *hdot2, double *hdot2_zero) {
+    PSC_BATCH_AT(b, idx, h, r);
+    return spectra(h, r, numpoints, f2, pi2, n2, gw_numpoints, h2, hdot2, hdot2_zero);
+}
+
+int psc_batch_energies(psc_batch *b, int idx, double *K, double *G, double *V, double *total,
+                       double *friedmann_violation, double *rho_gw) {
+    PSC_BATCH_AT(b, idx, h, r);
+    return energies(h, r, K, G, V, total, friedmann_violation, rho_gw);
+}
+
+int psc_batch_means(psc_batch *b, int idx, double *out) {
+    PSC_BATCH_AT(b, idx, h, r);
+    if (!out) return fail(PSC_ERR_ARG, "null argument");
+    return means(h, r, out);
+}
+
+#undef PSC_BATCH_AT
 
 const char *psc_strerror(int code) {
     switch (code) {

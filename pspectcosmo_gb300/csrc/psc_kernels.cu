@@ -41,6 +41,14 @@ __global__ void __launch_bounds__(256) k_ifft_x(Geo g, cplx<T> *__restrict__ fk,
     const int sh = g.tlx_shift, TL = 1 << sh, N = g.N;
     C *b0 = reinterpret_cast<C *>(smem_raw);
     C *b1 = b0 + TL * N;
+    {
+        const long long rf = (long long)blockIdx.z * g.fstride;
+        fk += rf;
+        if (DRIFT) pk += rf;
+        TA += rf;
+        if (GW) TB += rf;
+        bg += blockIdx.z;
+    }
     const long long off = (long long)blockIdx.y * g.modes;
     const int line0 = blockIdx.x * TL;
     const long long stride = g.lines_x;
@@ -130,7 +138,8 @@ __global__ void __launch_bounds__(256) k_ifft_y(Geo g, cplx<T> *__restrict__ TA,
     const int TL = 1 << g.tlx_shift;
     C *b0 = reinterpret_cast<C *>(smem_raw);
     C *b1 = b0 + TL * g.N;
-    const long long off = (long long)blockIdx.y * g.modes;
+    const long long off = (long long)blockIdx.y * g.modes + (long long)blockIdx.z * g.fstride;
+    bg += blockIdx.z;
     const T kIR = (T)bg->kIR;
     if (GW) {
         // the y-derivative reads TA before TA is transformed in place
@@ -145,6 +154,7 @@ __global__ void __launch_bounds__(256) k_ifft_y(Geo g, cplx<T> *__restrict__ TA,
 // Forward Y pass in place over a list of arrays (blockIdx.y selects the array).
 struct ArrList {
     void *p[8];
+    long long rs[8];
 };
 
 template <typename T>
@@ -154,7 +164,7 @@ __global__ void __launch_bounds__(256) k_fft_y(Geo g, ArrList arrs, const cplx<T
     const int TL = 1 << g.tlx_shift;
     C *b0 = reinterpret_cast<C *>(smem_raw);
     C *b1 = b0 + TL * g.N;
-    C *a = reinterpret_cast<C *>(arrs.p[blockIdx.y]);
+    C *a = reinterpret_cast<C *>(arrs.p[blockIdx.y]) + (long long)blockIdx.z * arrs.rs[blockIdx.y];
     ypass_tile<T, -1>(g, a, a, false, T(0), b0, b1, tw);
 }
 
@@ -172,6 +182,18 @@ __global__ void __launch_bounds__(256) k_zpass(Geo g, const cplx<T> *__restrict_
     C *b0 = reinterpret_cast<C *>(smem_raw);
     C *b1 = b0 + H * LD;
     C *slots = b1 + H * LD;
+    {
+        const long long rf = (long long)blockIdx.z * g.fstride, rg = (long long)blockIdx.z * g.gstride;
+        TA += rf;
+        QV += rf;
+        if (GW) {
+            TB += rf;
+            TC += rf;
+            QS += rg;
+        }
+        partV += (size_t)blockIdx.z * g.pv_stride;
+        bg += blockIdx.z;
+    }
     const int line0 = blockIdx.x * TL;
     const int nf = g.nf;
     const int nin = nf * (GW ? 4 : 1);
@@ -308,6 +330,19 @@ __global__ void __launch_bounds__(256) k_fft_x_final(Geo g, const cplx<T> *__res
     const int sh = g.tlx_shift, TL = 1 << sh, N = g.N, H = g.H, M = g.M;
     C *b0 = reinterpret_cast<C *>(smem_raw);
     C *b1 = b0 + TL * N;
+    {
+        const long long rf = (long long)blockIdx.z * g.fstride, rg = (long long)blockIdx.z * g.gstride;
+        QV += rf;
+        fk += rf;
+        pk += rf;
+        if (GW) {
+            QS += rg;
+            uk += rg;
+            puk += rg;
+        }
+        partKG += (size_t)blockIdx.z * g.pkg_stride;
+        bg += blockIdx.z;
+    }
     const int job = blockIdx.y;
     const bool field = job < g.nf;
     const long long off = (long long)(field ? job : job - g.nf) * g.modes;
@@ -420,8 +455,12 @@ __device__ double friedmann_add(const DevBG *bg, double K, double G, double V) {
 }
 
 __global__ void __launch_bounds__(512) k_scalar(DevBG *bg, const double *__restrict__ partKG,
-                                                const double *__restrict__ partV, int mode, int p) {
+                                                const double *__restrict__ partV, int mode, int p, int pkg_stride,
+                                                int pv_stride) {
     __shared__ double red[512];
+    bg += blockIdx.x;
+    partKG += (size_t)blockIdx.x * pkg_stride;
+    partV += (size_t)blockIdx.x * pv_stride;
     __shared__ double sums[2 * kMaxFields + kMaxTerms];
     const bool reduce = (mode == SCALAR_END || mode == SCALAR_EVAL_END);
     if (reduce) {
@@ -505,9 +544,11 @@ __global__ void __launch_bounds__(512) k_scalar(DevBG *bg, const double *__restr
     }
 }
 
-__global__ void k_set_run(DevBG *bg, double dt, int nsteps) {
-    bg->dt = dt;
-    bg->steps_left = nsteps;
+__global__ void k_set_run(DevBG *bg, int R, double dt, int nsteps) {
+    for (int r = threadIdx.x; r < R; r += blockDim.x) {
+        bg[r].dt = dt;
+        bg[r].steps_left = nsteps;
+    }
 }
 
 // ------------------------------------------------------------------ real-space view
@@ -674,8 +715,9 @@ static int ilog2i(int v) {
     return l;
 }
 
-void plan(const psc_params &p, LaunchCfg *cfg) {
+void plan(const psc_params &p, int R, LaunchCfg *cfg) {
     Geo &g = cfg->g;
+    cfg->R = R;
     g.N = p.N;
     g.H = p.N / 2 + 1;
     g.M = p.N / 2;
@@ -690,6 +732,8 @@ void plan(const psc_params &p, LaunchCfg *cfg) {
     g.modes = (long long)g.N * g.N * g.H;
     g.sites = (long long)g.N * g.N * g.N;
     g.reg = g.N >= 32 ? 1 : 0;
+    g.fstride = (long long)g.nf * g.modes;
+    g.gstride = g.gw ? 6LL * g.modes : 0;
     const int csize = p.precision == 32 ? 8 : 16;
     const int nin = g.nf * (g.gw ? 4 : 1), nout = g.nf + (g.gw ? 6 : 0);
     const int nslot = nin > nout ? nin : nout;
@@ -711,6 +755,8 @@ void plan(const psc_params &p, LaunchCfg *cfg) {
         cfg->thr_z = nin * tlz * Pz;
         cfg->smem_z = (size_t)nslot * tlz * (g.M + g.M / 16 + 1) * csize;
         cfg->nbz = (g.lines_z + tlz - 1) / tlz;
+        g.pkg_stride = 2 * kMaxFields * cfg->nbx;
+        g.pv_stride = kMaxTerms * cfg->nbz;
         return;
     }
     // generic engine: a tile of TL lines x N elements, two ping-pong buffers of
@@ -734,6 +780,8 @@ void plan(const psc_params &p, LaunchCfg *cfg) {
     cfg->thr_z = 256;
     cfg->smem_z = zbytes(tlz);
     cfg->nbz = (g.lines_z + tlz - 1) / tlz;
+    g.pkg_stride = 2 * kMaxFields * cfg->nbx;
+    g.pv_stride = kMaxTerms * cfg->nbz;
 }
 
 template <typename T>
@@ -772,7 +820,8 @@ static cudaError_t launch_stage_t(const LaunchCfg &cfg, const Buffers &b, int dr
     const C *tw = reinterpret_cast<const C *>(b.tw);
     C *fk = (C *)b.fk, *pk = (C *)b.pk, *uk = (C *)b.uk, *puk = (C *)b.puk;
     C *TA = (C *)b.TA, *TB = (C *)b.TB, *TC = (C *)b.TC, *QV = (C *)b.QV, *QS = (C *)b.QS;
-    const dim3 gx(cfg.nbx, g.nf);
+    const int R = cfg.R;
+    const dim3 gx(cfg.nbx, g.nf, R);
     auto mark = [&](int i) {
         if (ev) cudaEventRecord(ev[i], st);
     };
@@ -783,29 +832,35 @@ static cudaError_t launch_stage_t(const LaunchCfg &cfg, const Buffers &b, int dr
         mark(1);
         k_ifft_y<T, true><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, TA, TB, TC, b.bg, tw);
         mark(2);
-        k_zpass<T, true><<<cfg.nbz, cfg.thr_z, cfg.smem_z, st>>>(g, TA, TB, TC, QV, QS, b.partV, b.bg, tw);
+        k_zpass<T, true><<<dim3(cfg.nbz, 1, R), cfg.thr_z, cfg.smem_z, st>>>(g, TA, TB, TC, QV, QS, b.partV, b.bg, tw);
     } else {
         if (drift) k_ifft_x<T, false, true><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
         else k_ifft_x<T, false, false><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
         mark(1);
         k_ifft_y<T, false><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, TA, TB, TC, b.bg, tw);
         mark(2);
-        k_zpass<T, false><<<cfg.nbz, cfg.thr_z, cfg.smem_z, st>>>(g, TA, TB, TC, QV, QS, b.partV, b.bg, tw);
+        k_zpass<T, false><<<dim3(cfg.nbz, 1, R), cfg.thr_z, cfg.smem_z, st>>>(g, TA, TB, TC, QV, QS, b.partV, b.bg, tw);
     }
     mark(3);
     ArrList al{};
     int nj = 0;
-    for (int f = 0; f < g.nf; ++f) al.p[nj++] = QV + (long long)f * g.modes;
+    for (int f = 0; f < g.nf; ++f) {
+        al.rs[nj] = g.fstride;
+        al.p[nj++] = QV + (long long)f * g.modes;
+    }
     if (g.gw)
-        for (int c = 0; c < 6; ++c) al.p[nj++] = QS + (long long)c * g.modes;
-    k_fft_y<T><<<dim3(cfg.nbx, nj), cfg.thr_xy, cfg.smem_xy, st>>>(g, al, tw);
+        for (int c = 0; c < 6; ++c) {
+            al.rs[nj] = g.gstride;
+            al.p[nj++] = QS + (long long)c * g.modes;
+        }
+    k_fft_y<T><<<dim3(cfg.nbx, nj, R), cfg.thr_xy, cfg.smem_xy, st>>>(g, al, tw);
     mark(4);
-    const dim3 gf(cfg.nbx, nj);
+    const dim3 gf(cfg.nbx, nj, R);
     if (g.gw) k_fft_x_final<T, true><<<gf, cfg.thr_xy, cfg.smem_xy, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw);
     else k_fft_x_final<T, false><<<gf, cfg.thr_xy, cfg.smem_xy, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw);
     mark(5);
     if (scalar_mode >= 0) {
-        k_scalar<<<1, 512, 0, st>>>(b.bg, b.partKG, b.partV, scalar_mode, 1);
+        k_scalar<<<cfg.R, 512, 0, st>>>(b.bg, b.partKG, b.partV, scalar_mode, 1, cfg.g.pkg_stride, cfg.g.pv_stride);
         mark(6);
     }
     return cudaGetLastError();
@@ -828,13 +883,12 @@ cudaError_t launch_stage(const LaunchCfg &cfg, const Buffers &b, int precision, 
 }
 
 cudaError_t launch_scalar(const LaunchCfg &cfg, const Buffers &b, int mode, int p, cudaStream_t st) {
-    (void)cfg;
-    k_scalar<<<1, 512, 0, st>>>(b.bg, b.partKG, b.partV, mode, p);
+    k_scalar<<<cfg.R, 512, 0, st>>>(b.bg, b.partKG, b.partV, mode, p, cfg.g.pkg_stride, cfg.g.pv_stride);
     return cudaGetLastError();
 }
 
-cudaError_t launch_set_run(DevBG *bg, double dt, int nsteps, cudaStream_t st) {
-    k_set_run<<<1, 1, 0, st>>>(bg, dt, nsteps);
+cudaError_t launch_set_run(DevBG *bg, int R, double dt, int nsteps, cudaStream_t st) {
+    k_set_run<<<1, 128, 0, st>>>(bg, R, dt, nsteps);
     return cudaGetLastError();
 }
 

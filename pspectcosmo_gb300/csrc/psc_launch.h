@@ -23,10 +23,16 @@ struct Geo {
     int lines_z;                 // N * N  (Z-pass line count)
     long long modes, sites;
     double gsq;
+    // batches of R same-configuration lattices: realization r = blockIdx.z owns
+    // the arrays at r * fstride (field-sized) / r * gstride (GW-sized), the
+    // background record bg[r] and the partial sums at r * pkg_stride / r * pv_stride.
+    long long fstride, gstride;
+    int pkg_stride, pv_stride;
 };
 
 struct LaunchCfg {
     Geo g;
+    int R;                       // realizations advanced together (1 for a single lattice)
     int thr_xy, thr_z;           // threads per block
     size_t smem_xy, smem_z;      // dynamic shared memory bytes
     size_t smem_xf;              // X forward + kick pass (exchange tile + two prefetched operand tiles)
@@ -58,8 +64,8 @@ enum ScalarMode {
     SCALAR_EVAL_END = 4 // reductions of an evaluation -> K, G, V, a''
 };
 
-// Tile sizes, block sizes and shared memory for one configuration.
-void plan(const psc_params &p, LaunchCfg *cfg);
+// Tile sizes, block sizes and shared memory for R lattices of one configuration.
+void plan(const psc_params &p, int R, LaunchCfg *cfg);
 // Set the dynamic shared-memory limits of the kernels a configuration uses.
 cudaError_t configure(const LaunchCfg &cfg, int precision);
 
@@ -72,7 +78,7 @@ cudaError_t launch_stage(const LaunchCfg &cfg, const Buffers &b, int precision, 
 cudaError_t launch_stage_timed(const LaunchCfg &cfg, const Buffers &b, int precision, int drift, int scalar_mode,
                                cudaEvent_t *ev, cudaStream_t st);
 cudaError_t launch_scalar(const LaunchCfg &cfg, const Buffers &b, int mode, int p, cudaStream_t st);
-cudaError_t launch_set_run(DevBG *bg, double dt, int nsteps, cudaStream_t st);
+cudaError_t launch_set_run(DevBG *bg, int R, double dt, int nsteps, cudaStream_t st);
 // Real-space view of nsrc complex arrays (c2r / N^3) into b.real (precision T).
 cudaError_t launch_c2r_real(const LaunchCfg &cfg, const Buffers &b, int precision, const void *src, int nsrc,
                             cudaStream_t st);

@@ -24,6 +24,14 @@ __global__ void __launch_bounds__(256, 2) kr_ifft_x(Geo g, cplx<T> *__restrict__
     using RP = RegPlan<L>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *sm = reinterpret_cast<C *>(smem_raw);
+    {
+        const long long rf = (long long)blockIdx.z * g.fstride;
+        fk += rf;
+        if (DRIFT) pk += rf;
+        TA += rf;
+        if (GW) TB += rf;
+        bg += blockIdx.z;
+    }
     const int sh = g.tlx_shift, TL = 1 << sh;
     const int t = threadIdx.x & (TL - 1), j = threadIdx.x >> sh;
     const int line = blockIdx.x * TL + t;
@@ -126,7 +134,8 @@ __global__ void __launch_bounds__(256, 2) kr_ifft_y(Geo g, cplx<T> *__restrict__
     using C = cplx<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *sm = reinterpret_cast<C *>(smem_raw);
-    const long long off = (long long)blockIdx.y * g.modes;
+    const long long off = (long long)blockIdx.y * g.modes + (long long)blockIdx.z * g.fstride;
+    bg += blockIdx.z;
     const T kIR = (T)bg->kIR;
     if (GW) {
         // the y-derivative reads TA before TA is transformed in place
@@ -140,6 +149,7 @@ __global__ void __launch_bounds__(256, 2) kr_ifft_y(Geo g, cplx<T> *__restrict__
 
 struct ArrList8 {
     void *p[8];
+    long long rs[8];   // realization stride of each array (elements)
 };
 
 template <typename T, int L>
@@ -147,7 +157,7 @@ __global__ void __launch_bounds__(256, 3) kr_fft_y(Geo g, ArrList8 arrs, const c
     using C = cplx<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *sm = reinterpret_cast<C *>(smem_raw);
-    C *a = reinterpret_cast<C *>(arrs.p[blockIdx.y]);
+    C *a = reinterpret_cast<C *>(arrs.p[blockIdx.y]) + (long long)blockIdx.z * arrs.rs[blockIdx.y];
     ry_tile<T, L, -1>(g, a, a, false, T(0), sm, tw);
 }
 
@@ -162,6 +172,19 @@ __global__ void __launch_bounds__(256, 2) kr_fft_x_final(Geo g, const cplx<T> *_
     using RP = RegPlan<L>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *sm = reinterpret_cast<C *>(smem_raw);
+    {
+        const long long rf = (long long)blockIdx.z * g.fstride, rg = (long long)blockIdx.z * g.gstride;
+        QV += rf;
+        fk += rf;
+        pk += rf;
+        if (GW) {
+            QS += rg;
+            uk += rg;
+            puk += rg;
+        }
+        partKG += (size_t)blockIdx.z * g.pkg_stride;
+        bg += blockIdx.z;
+    }
     const int sh = g.tlx_shift, TL = 1 << sh, N = g.N, H = g.H, M = g.M;
     const int t = threadIdx.x & (TL - 1), j = threadIdx.x >> sh;
     const int line = blockIdx.x * TL + t;
@@ -281,6 +304,18 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
     constexpr int M = L, P = RP::P, LS = ZIdx<L>::LS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *slots = reinterpret_cast<C *>(smem_raw);
+    {
+        const long long rf = (long long)blockIdx.z * g.fstride, rg = (long long)blockIdx.z * g.gstride;
+        TA += rf;
+        QV += rf;
+        if (GW) {
+            TB += rf;
+            TC += rf;
+            QS += rg;
+        }
+        partV += (size_t)blockIdx.z * g.pv_stride;
+        bg += blockIdx.z;
+    }
     const int sh = g.tlz_shift, TL = 1 << sh, H = g.H, N = g.N;
     const int nf = g.nf;
     const int nin = nf * (GW ? 4 : 1);

@@ -44,7 +44,8 @@ struct RegLaunch {
         const C *tw = reinterpret_cast<const C *>(b.tw);
         C *fk = (C *)b.fk, *pk = (C *)b.pk, *uk = (C *)b.uk, *puk = (C *)b.puk;
         C *TA = (C *)b.TA, *TB = (C *)b.TB, *TC = (C *)b.TC, *QV = (C *)b.QV, *QS = (C *)b.QS;
-        const dim3 gx(cfg.nbx, g.nf);
+        const int R = cfg.R;
+        const dim3 gx(cfg.nbx, g.nf, R);
         const int txy = cfg.thr_xy, tz = cfg.thr_z;
         auto mark = [&](int i) {
             if (ev) cudaEventRecord(ev[i], st);
@@ -56,24 +57,30 @@ struct RegLaunch {
             mark(1);
             kr_ifft_y<T, N, true><<<gx, txy, cfg.smem_xy, st>>>(g, TA, TB, TC, b.bg, tw);
             mark(2);
-            kr_zpass<T, M, true><<<cfg.nbz, tz, cfg.smem_z, st>>>(g, TA, TB, TC, QV, QS, b.partV, b.bg, tw);
+            kr_zpass<T, M, true><<<dim3(cfg.nbz, 1, R), tz, cfg.smem_z, st>>>(g, TA, TB, TC, QV, QS, b.partV, b.bg, tw);
         } else {
             if (drift) kr_ifft_x<T, N, false, true><<<gx, txy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
             else kr_ifft_x<T, N, false, false><<<gx, txy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
             mark(1);
             kr_ifft_y<T, N, false><<<gx, txy, cfg.smem_xy, st>>>(g, TA, TB, TC, b.bg, tw);
             mark(2);
-            kr_zpass<T, M, false><<<cfg.nbz, tz, cfg.smem_z, st>>>(g, TA, TB, TC, QV, QS, b.partV, b.bg, tw);
+            kr_zpass<T, M, false><<<dim3(cfg.nbz, 1, R), tz, cfg.smem_z, st>>>(g, TA, TB, TC, QV, QS, b.partV, b.bg, tw);
         }
         mark(3);
         ArrList8 al{};
         int nj = 0;
-        for (int f = 0; f < g.nf; ++f) al.p[nj++] = QV + (long long)f * g.modes;
+        for (int f = 0; f < g.nf; ++f) {
+            al.rs[nj] = g.fstride;
+            al.p[nj++] = QV + (long long)f * g.modes;
+        }
         if (g.gw)
-            for (int c = 0; c < 6; ++c) al.p[nj++] = QS + (long long)c * g.modes;
-        kr_fft_y<T, N><<<dim3(cfg.nbx, nj), txy, cfg.smem_xy, st>>>(g, al, tw);
+            for (int c = 0; c < 6; ++c) {
+                al.rs[nj] = g.gstride;
+                al.p[nj++] = QS + (long long)c * g.modes;
+            }
+        kr_fft_y<T, N><<<dim3(cfg.nbx, nj, R), txy, cfg.smem_xy, st>>>(g, al, tw);
         mark(4);
-        const dim3 gf(cfg.nbx, nj);
+        const dim3 gf(cfg.nbx, nj, R);
         if (g.gw)
             kr_fft_x_final<T, N, true><<<gf, txy, cfg.smem_xf, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw);
         else

@@ -79,13 +79,29 @@ def load_library(path: str | None = None):
     L.psc_last_step_ms.argtypes = [P, ctypes.POINTER(ctypes.c_float)]
     L.psc_time_passes.argtypes = [P, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
     L.psc_pass_bytes.argtypes = [P, D]
+    L.psc_batch_create.argtypes = [PP, ctypes.c_int, ctypes.POINTER(P)]
+    L.psc_batch_destroy.argtypes = [P]
+    L.psc_batch_destroy.restype = None
+    L.psc_batch_size.argtypes = [P]
+    L.psc_batch_groups.argtypes = [P]
+    L.psc_batch_init_ic.argtypes = [P]
+    L.psc_batch_step.argtypes = [P, ctypes.c_double, ctypes.c_int]
+    L.psc_batch_last_step_ms.argtypes = [P, ctypes.POINTER(ctypes.c_float)]
+    L.psc_batch_set_state.argtypes = [P, ctypes.c_int, D, D, ctypes.c_double, ctypes.c_double, ctypes.c_double, D, D]
+    L.psc_batch_get_state.argtypes = [P, ctypes.c_int, D, D, D, D, D, D, D]
+    L.psc_batch_spectra.argtypes = [P, ctypes.c_int, I32, D, D, D, I32, D, D, D]
+    L.psc_batch_energies.argtypes = [P, ctypes.c_int, D, D, D, D, D, D]
+    L.psc_batch_means.argtypes = [P, ctypes.c_int, D]
     L.psc_strerror.argtypes = [ctypes.c_int]
     L.psc_strerror.restype = ctypes.c_char_p
     L.psc_last_error.argtypes = []
     L.psc_last_error.restype = ctypes.c_char_p
     for name in ("psc_create", "psc_init_ic", "psc_generate_ic", "psc_set_state", "psc_get_state", "psc_get_time",
                  "psc_set_time", "psc_step", "psc_get_fields_real", "psc_maxnumbins", "psc_spectra", "psc_energies",
-                 "psc_means", "psc_last_step_ms", "psc_time_passes", "psc_pass_bytes"):
+                 "psc_means", "psc_last_step_ms", "psc_time_passes", "psc_pass_bytes", "psc_batch_create",
+                 "psc_batch_size", "psc_batch_groups", "psc_batch_init_ic", "psc_batch_step", "psc_batch_last_step_ms",
+                 "psc_batch_set_state", "psc_batch_get_state", "psc_batch_spectra", "psc_batch_energies",
+                 "psc_batch_means"):
         getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L
@@ -259,3 +275,74 @@ class Lattice:
         from .outputs import scale_row
 
         return scale_row(self.p, self.background())
+
+
+class Ensemble:
+    """Independent realizations (possibly of different lattice sizes) advanced together:
+    one launch per pass per same-configuration group, one CUDA graph per step."""
+
+    def __init__(self, params_list):
+        self.params = [q.copy() for q in params_list]
+        self._L = load_library()
+        arr = (Params * len(self.params))(*self.params)
+        h = ctypes.c_void_p()
+        _check(self._L.psc_batch_create(arr, len(self.params), ctypes.byref(h)), "psc_batch_create")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.psc_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __len__(self):
+        return self._L.psc_batch_size(self._h)
+
+    @property
+    def groups(self) -> int:
+        return self._L.psc_batch_groups(self._h)
+
+    def initialize(self):
+        _check(self._L.psc_batch_init_ic(self._h), "psc_batch_init_ic")
+
+    def evolve(self, dt: float, nsteps: int = 1):
+        _check(self._L.psc_batch_step(self._h, float(dt), int(nsteps)), "psc_batch_step")
+
+    def last_step_ms(self) -> float:
+        v = ctypes.c_float()
+        _check(self._L.psc_batch_last_step_ms(self._h, ctypes.byref(v)), "psc_batch_last_step_ms")
+        return v.value
+
+    def get_state(self, idx: int):
+        p = self.params[idx]
+        f = np.zeros((p.nflds, p.modes), np.complex128)
+        pi = np.zeros((p.nflds, p.modes), np.complex128)
+        u = np.zeros((6, p.modes), np.complex128) if p.with_gw else None
+        pu = np.zeros((6, p.modes), np.complex128) if p.with_gw else None
+        a, ad, add = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        _check(self._L.psc_batch_get_state(self._h, idx, _dp(f), _dp(pi), ctypes.byref(a), ctypes.byref(ad),
+                                           ctypes.byref(add), _dp(u), _dp(pu)), "psc_batch_get_state")
+        return dict(f_k=f, pi_k=pi, u_k=u, pi_u_k=pu, a=a.value, ad=ad.value, add=add.value)
+
+    def spectra_raw(self, idx: int) -> dict:
+        p = self.params[idx]
+        nb = p.maxnumbins
+        out = dict(numpoints=np.zeros((p.nflds, nb), np.int32), f2=np.zeros((p.nflds, nb)),
+                   pi2=np.zeros((p.nflds, nb)), n2=np.zeros((p.nflds, nb)))
+        hz = ctypes.c_double(0.0)
+        _check(self._L.psc_batch_spectra(self._h, idx, _ip(out["numpoints"]), _dp(out["f2"]), _dp(out["pi2"]),
+                                         _dp(out["n2"]), None, None, None, ctypes.byref(hz)), "psc_batch_spectra")
+        return out
+
+    def energies(self, idx: int) -> dict:
+        p = self.params[idx]
+        K, G, V = np.zeros(p.nflds), np.zeros(p.nflds), np.zeros(p.num_potential_terms)
+        tot, fv, rho = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        _check(self._L.psc_batch_energies(self._h, idx, _dp(K), _dp(G), _dp(V), ctypes.byref(tot), ctypes.byref(fv),
+                                          ctypes.byref(rho)), "psc_batch_energies")
+        return dict(K=K, G=G, V=V, total=tot.value, friedmann_violation=fv.value, rho_gw=rho.value)
