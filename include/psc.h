@@ -204,6 +204,25 @@ int psc_batch_means(psc_batch *b, int idx, double *out);
 int psc_spectra_noalloc(const psc_params *p, double a, double ad, const void *f_k, const void *pi_k,
                         int32_t *numpoints, double *f2, double *pi2, double *n2, void *stream);
 
+/* ---- discrete adjoint (no reference counterpart: the reference has no adjoint).
+ * Differentiates the step of evolve_VV (evolution.cpp:607-694) for the scalar fields and
+ * the self-consistent background (a'' through K, G, V: evolution.cpp:421-439), for the
+ * observable O = <chi^2> (the last field's lattice mean of its square) after `nsteps`
+ * steps of `dt` from the handle's current state, with a''(0) recomputed from that state.
+ * Needs a single-lattice handle, N >= 32, expansion = 2 and the unmasked step
+ * (spectral = 0, or simulate_inflation = 0). Checkpoints are taken every `every` steps
+ * (every <= 0: one segment); each segment is recomputed once in the reverse sweep.
+ * Outputs (any pointer but O may be NULL):
+ *   grad_f_k, grad_pi_k  [nflds][N][N][N/2+1] complex as interleaved doubles:
+ *                        dO/dRe + i dO/dIm of each stored half-spectrum mode;
+ *   grad_ad0             dO/da'(0) at fixed a(0);
+ *   grad_theta[2]        dO/d(gsq) and dO/d(mu), mu the coefficient of phi^2/2 in V (mu = 1).
+ * On return the handle holds the final state, as after psc_step(h, dt, nsteps). */
+int psc_adjoint_chi2(psc_handle *h, double dt, int nsteps, int every, double *O, double *grad_f_k,
+                     double *grad_pi_k, double *grad_ad0, double *grad_theta);
+/* The adjoint's own forward map alone (same stage arithmetic, unfused): O after nsteps. */
+int psc_adjoint_forward_chi2(psc_handle *h, double dt, int nsteps, double *O);
+
 const char *psc_strerror(int code);
 const char *psc_last_error(void);
 

@@ -22,13 +22,20 @@
 #include "psc_launch.h"
 
 namespace {
-
 thread_local std::string g_last_error;
+}  // namespace
 
+namespace psc {
+namespace hapi {
 int fail(int code, const std::string &msg) {
     g_last_error = msg;
     return code;
 }
+}  // namespace hapi
+}  // namespace psc
+using psc::hapi::fail;
+
+namespace {
 
 #define CU(call)                                                                                         \
     do {                                                                                                 \
@@ -67,30 +74,14 @@ constexpr double kPi = 3.14159265358979323846;
 
 void psc::set_last_error(const char *msg) { g_last_error = msg ? msg : ""; }
 
-struct psc_handle {
-    std::vector<psc_params> p;   // per realization (identical except seed / initial values)
-    int R = 1;
-    psc::LaunchCfg cfg{};
-    psc::Buffers b{};
-    size_t csize = 0;            // bytes of one complex element on the device
-    int s = 1;
-    const double *w = kW2;
-    int nb = 0;                  // maxnumbins
-    cudaStream_t st = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    cudaGraphExec_t gexec = nullptr;
-    bool have_state = false;
-    bool diag_valid = false;
-    float last_ms = 0.f;
-    void *stage_buf = nullptr;   // pinned staging for precision conversion
-    size_t stage_bytes = 0;
-    std::vector<void *> allocs;
-    const psc_params &p0() const { return p[0]; }
-};
+#include "psc_handle.h"
 
-namespace {
+namespace psc {
+namespace hapi {
 
 void free_all(psc_handle *h) {
+    if (h->adj && h->adj_free) h->adj_free(h->adj);
+    h->adj = nullptr;
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
     for (void *q : h->allocs) cudaFree(q);
     h->allocs.clear();
@@ -293,6 +284,7 @@ int create_handle(const psc_params *ps, int R, psc_handle **out) {
     for (auto &q : h->p)
         if (q.fStar <= 0) q.fStar = q.MPl;
     h->R = R;
+    h->w = kW2;
     const psc_params &p = h->p0();
     switch (p.vv) {
     case 4: h->s = 3; h->w = kW4; break;
@@ -638,7 +630,9 @@ int means(psc_handle *h, int r, double *out) {
     return PSC_OK;
 }
 
-}  // namespace
+}  // namespace hapi
+}  // namespace psc
+using namespace psc::hapi;
 
 // ------------------------------------------------------------------ batches
 struct psc_batch {

@@ -1,0 +1,46 @@
+// psc_handle.h — the lattice handle shared by the C-ABI layer (psc_api.cu) and
+// the adjoint (psc_adjoint.cu). Private to the library.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "../../include/psc.h"
+#include "psc_bg.h"
+#include "psc_launch.h"
+
+struct psc_handle {
+    std::vector<psc_params> p;   // per realization (identical except seed / initial values)
+    int R = 1;
+    psc::LaunchCfg cfg{};
+    psc::Buffers b{};
+    size_t csize = 0;            // bytes of one complex element on the device
+    int s = 1;
+    const double *w = nullptr;   // Yoshida weights
+    int nb = 0;                  // maxnumbins
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    bool have_state = false;
+    bool diag_valid = false;
+    float last_ms = 0.f;
+    void *stage_buf = nullptr;   // pinned staging for precision conversion
+    size_t stage_bytes = 0;
+    std::vector<void *> allocs;
+    void *adj = nullptr;         // adjoint workspace (psc_adjoint.cu), owned by the handle
+    void (*adj_free)(void *) = nullptr;
+    const psc_params &p0() const { return p[0]; }
+};
+
+namespace psc {
+namespace hapi {
+int fail(int code, const std::string &msg);
+int dalloc(psc_handle *h, void **out, size_t bytes);
+int upload(psc_handle *h, void *dst, const double *src, size_t ncplx);
+int download_real(psc_handle *h, double *dst, const void *src, size_t count);
+int read_bg(psc_handle *h, int r, DevBG *out);
+int write_bg(psc_handle *h, int r, const DevBG &in);
+int step(psc_handle *h, double dt, int nsteps);
+int evaluate(psc_handle *h, int keep_add);
+}  // namespace hapi
+}  // namespace psc

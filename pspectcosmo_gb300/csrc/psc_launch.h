@@ -99,5 +99,11 @@ cudaError_t reg_stage_f64(const LaunchCfg &cfg, const Buffers &b, int drift, cud
                           int scalar_mode);
 cudaError_t reg_c2r_real_f32(const LaunchCfg &cfg, const Buffers &b, const void *src, int nsrc, cudaStream_t st);
 cudaError_t reg_c2r_real_f64(const LaunchCfg &cfg, const Buffers &b, const void *src, int nsrc, cudaStream_t st);
+// General 3-D transforms of n arrays (N >= 32): complex [n][modes] -> real [n][sites]
+// (c2r / N^3, uses TA as scratch) and real -> complex (unnormalised r2c, n <= 8).
+cudaError_t reg_c2r_f32(const LaunchCfg &cfg, const Buffers &b, const void *src, int n, void *dst, cudaStream_t st);
+cudaError_t reg_c2r_f64(const LaunchCfg &cfg, const Buffers &b, const void *src, int n, void *dst, cudaStream_t st);
+cudaError_t reg_r2c_f32(const LaunchCfg &cfg, const Buffers &b, const void *src, int n, void *dst, cudaStream_t st);
+cudaError_t reg_r2c_f64(const LaunchCfg &cfg, const Buffers &b, const void *src, int n, void *dst, cudaStream_t st);
 
 }  // namespace psc

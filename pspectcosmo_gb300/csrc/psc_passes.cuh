@@ -520,4 +520,79 @@ __global__ void __launch_bounds__(256) kr_z_c2r_real(Geo g, const cplx<T> *__res
     }
 }
 
+// ------------------------------------------------------------------ plain forward transforms
+// Real-to-complex along z: real lines [lines_z][N] (blockIdx.y selects the array) ->
+// half-spectrum lines [lines_z][H]; X[k] = (Z[k] + conj Z[M-k])/2 + e^{-2 pi i k/N}
+// (Z[k] - conj Z[M-k])/(2i), Z the M-point transform of x[2m] + i x[2m+1].
+template <typename T, int L>
+__global__ void __launch_bounds__(256) kr_z_r2c_real(Geo g, const T *__restrict__ in, cplx<T> *__restrict__ out,
+                                                     const cplx<T> *__restrict__ tw, int tl_shift) {
+    using C = cplx<T>;
+    using RP = RegPlan<L>;
+    constexpr int M = L, P = RP::P, LS = ZIdx<L>::LS;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *sm = reinterpret_cast<C *>(smem_raw);
+    const int TL = 1 << tl_shift, H = g.H, N = g.N;
+    const int j = threadIdx.x % P, t = threadIdx.x / P;
+    const int line = blockIdx.x * TL + t;
+    const bool valid = line < g.lines_z;
+    const T *src = in + (long long)blockIdx.y * g.sites + (long long)line * N;
+    C v[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+        const int m = j + r * P;
+        v[r] = valid ? mk<T>(src[2 * m], src[2 * m + 1]) : mk<T>(0, 0);
+    }
+    const ZIdx<L> ix{t * LS};
+    fft_reg<C, L, -1>(v, sm, ix, j, tw, N / L);
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+        for (int r = 0; r < RP::RL; ++r) sm[ix(RP::out(j, q, r))] = v[q * RP::RL + r];
+    __syncthreads();
+    if (valid) {
+        C *dst = out + (long long)blockIdx.y * g.modes + (long long)line * H;
+#pragma unroll
+        for (int r = 0; r <= 16; ++r) {
+            const int k = (r < 16) ? j + r * P : M;
+            if (r == 16 && j != 0) break;
+            const C zk = sm[ix(k == M ? 0 : k)];
+            const C zc = cconj(sm[ix(k == 0 ? 0 : M - k)]);
+            const C ev = cscale(cadd(zk, zc), T(0.5));
+            const C dd = cscale(csub(zk, zc), T(0.5));
+            const C od = mk<T>(dd.y, -dd.x);
+            C w;
+            if (k < M) w = __ldg(&tw[k]); else w = mk<T>(T(-1), T(0));
+            dst[k] = cadd(ev, cmul(w, od));
+        }
+    }
+}
+
+// Forward transform along x in place (blockIdx.y selects the array of the list).
+template <typename T, int L>
+__global__ void __launch_bounds__(256, 2) kr_fft_x_plain(Geo g, ArrList8 arrs, const cplx<T> *__restrict__ tw) {
+    using C = cplx<T>;
+    using RP = RegPlan<L>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *sm = reinterpret_cast<C *>(smem_raw);
+    C *a = reinterpret_cast<C *>(arrs.p[blockIdx.y]);
+    const int sh = g.tlx_shift, TL = 1 << sh;
+    const int t = threadIdx.x & (TL - 1), j = threadIdx.x >> sh;
+    const int line = blockIdx.x * TL + t;
+    const bool valid = line < g.lines_x;
+    const long long stride = g.lines_x;
+    auto ix = [&](int n) { return n * TL + t; };
+    C v[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) v[r] = valid ? a[(long long)(j + r * RP::P) * stride + line] : mk<T>(0, 0);
+    fft_reg<C, L, -1>(v, sm, ix, j, tw, g.N / L);
+    if (valid) {
+#pragma unroll
+        for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+            for (int r = 0; r < RP::RL; ++r) a[(long long)RP::out(j, q, r) * stride + line] = v[q * RP::RL + r];
+    }
+}
+
 }  // namespace psc

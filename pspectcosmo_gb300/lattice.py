@@ -92,6 +92,8 @@ def load_library(path: str | None = None):
     L.psc_batch_spectra.argtypes = [P, ctypes.c_int, I32, D, D, D, I32, D, D, D]
     L.psc_batch_energies.argtypes = [P, ctypes.c_int, D, D, D, D, D, D]
     L.psc_batch_means.argtypes = [P, ctypes.c_int, D]
+    L.psc_adjoint_chi2.argtypes = [P, ctypes.c_double, ctypes.c_int, ctypes.c_int, D, D, D, D, D]
+    L.psc_adjoint_forward_chi2.argtypes = [P, ctypes.c_double, ctypes.c_int, D]
     L.psc_strerror.argtypes = [ctypes.c_int]
     L.psc_strerror.restype = ctypes.c_char_p
     L.psc_last_error.argtypes = []
@@ -101,7 +103,7 @@ def load_library(path: str | None = None):
                  "psc_means", "psc_last_step_ms", "psc_time_passes", "psc_pass_bytes", "psc_batch_create",
                  "psc_batch_size", "psc_batch_groups", "psc_batch_init_ic", "psc_batch_step", "psc_batch_last_step_ms",
                  "psc_batch_set_state", "psc_batch_get_state", "psc_batch_spectra", "psc_batch_energies",
-                 "psc_batch_means"):
+                 "psc_batch_means", "psc_adjoint_chi2", "psc_adjoint_forward_chi2"):
         getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L
@@ -207,6 +209,30 @@ class Lattice:
         v = ctypes.c_float()
         _check(self._L.psc_last_step_ms(self._h, ctypes.byref(v)), "psc_last_step_ms")
         return v.value
+
+    # -- adjoint --------------------------------------------------------------
+    def adjoint_chi2(self, dt: float, nsteps: int, every: int = 0) -> dict:
+        """O = <chi^2> after nsteps and its gradient with respect to the current state.
+
+        Returns O, grad_f_k / grad_pi_k (dO/dRe + i dO/dIm per stored mode, shaped like the
+        state), grad_ad0 (dO/da' at fixed a) and grad_theta = (dO/dgsq, dO/dmu). The lattice
+        is left at the final state.
+        """
+        p = self.p
+        O, gad = ctypes.c_double(), ctypes.c_double()
+        gf = np.zeros((p.nflds, p.modes), np.complex128)
+        gp = np.zeros((p.nflds, p.modes), np.complex128)
+        gth = np.zeros(2)
+        _check(self._L.psc_adjoint_chi2(self._h, float(dt), int(nsteps), int(every), ctypes.byref(O), _dp(gf), _dp(gp),
+                                        ctypes.byref(gad), _dp(gth)), "psc_adjoint_chi2")
+        return dict(O=O.value, grad_f_k=gf, grad_pi_k=gp, grad_ad0=gad.value, grad_theta=gth)
+
+    def adjoint_forward_chi2(self, dt: float, nsteps: int) -> float:
+        """O = <chi^2> after nsteps of the adjoint's own (unfused) forward map."""
+        O = ctypes.c_double()
+        _check(self._L.psc_adjoint_forward_chi2(self._h, float(dt), int(nsteps), ctypes.byref(O)),
+               "psc_adjoint_forward_chi2")
+        return O.value
 
     PASS_NAMES = ("ifft_x", "ifft_y", "zpass", "fft_y", "fft_x_kick", "background")
 
