@@ -12,19 +12,28 @@
 // Gradients: with respect to the initial half-spectrum state f_k(0), pi_k(0)
 // (as dO/dRe + i dO/dIm per stored mode), a'(0), and the model couplings
 // (gsq and the phi mass coefficient mu, V = mu phi^2/2 + gsq phi^2 chi^2/2 at
-// mu = 1), at a''(0) consistent with the initial state.
+// mu = 1), at a''(0) = A(state(0)).
 //
-// Per stage, forward (stage inputs f, pi, a, b = a', add = a''; c1 = w dt/2):
-//   bh = b + c1 add;  ph = pi + c1 F(f, a);  ah = a + c1 bh;  f1 = f + w dt ah^(al-3) ph
-//   a1 = ah + c1 bh;  p1 = ph + c1 F(f1, a1);  add1 = A(f1, p1, a1);  b1 = bh + c1 add1
-// with F(f, a) = -a^(1+al) kIR^2 k^2 f_k - a^(3+al) r2c(V'(f(x))) and
-// A = (fStar/MPl)^2/3 a^(1+2al) ((al-2) K + al G + (al+1) V). The reverse sweep
-// transposes these lines in opposite order; (dF/df)^T = F's Laplacian part plus
-// -a^(3+al) r2c(V''(f(x)) lambda(x)) (the Hessian is symmetric). Adjoint arrays
-// are kept as Lambda = r2c(lambda(x)); <lambda, y> = (1/N^3) sum' w Re(conj Lambda Y).
+// Forward map, stage j from point P_j (f, p, a, b = a', add = a'') to P_{j+1},
+// c = w_j dt/2 and F(f, a) = -a^(1+al) kIR^2 k^2 f - a^(3+al) r2c(V'(f(x))):
+//   bh = b + c add;  ph = p + c F_j;  ah = a + c bh;  f' = f + w dt ah^(al-3) ph
+//   a' = ah + c bh;  p' = ph + c F_{j+1};  add' = A(f', p', a');  b' = bh + c add'
+// A = (fStar/MPl)^2/3 a^(1+2al) ((al-2) K + al G + (al+1) V). It is run by the
+// product's own stage kernels, which write a tape of every stage point (f, p, V'_k
+// and the real fields f(x)) and of the background record.
 //
-// Memory: checkpoints of the state every `every` steps; each segment is
-// recomputed from its checkpoint with every stage input kept, then reversed.
+// Reverse sweep. Adjoint arrays are carried as Lambda = r2c(lambda(x)), so
+// <lambda, y> = (1/N^3) sum' w Re(conj Lambda Y) and the gradient with respect to
+// a stored mode is (w_k/N^3) Lambda_k. The two transposed force Jacobians that meet
+// at a stage point P_j (the closing kick of stage j-1 and the opening kick of stage
+// j use the same F at the same f and a) are applied together, once, to
+//   M = (c_{j-1} + c_j) Lp + c_{j-1} beta p_j,
+// linear in the adjoint: J^T M = -a^(1+al) kIR^2 k^2 M - a^(3+al) r2c(V''(f) m),
+// together with the a''-adjoint terms of point j (dA/df, dA/dp, dA/da). All scalar
+// adjoint arithmetic runs in one-thread device kernels on a device record, so the
+// sweep has no host round trip. Memory: checkpoints of the state every `every`
+// steps; each segment is re-run once with the tape on, then reversed.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -45,11 +54,12 @@ namespace {
                         std::string(#call) + ": " + cudaGetErrorString(e_));                             \
     } while (0)
 
+constexpr int kEW = 4 * 152;   // blocks of the elementwise kernels (grid-stride)
 constexpr int kThreads = 256;
 
-__device__ __forceinline__ double wk_of(long long m, int H, int M) {
+__device__ __forceinline__ double wk_of(long long m, int H) {
     const int kz = (int)(m % H);
-    return (kz == 0 || kz == M) ? 1.0 : 2.0;
+    return (kz == 0 || kz == H - 1) ? 1.0 : 2.0;
 }
 
 __device__ __forceinline__ double k2_of(long long m, int N, int H) {
@@ -60,125 +70,199 @@ __device__ __forceinline__ double k2_of(long long m, int N, int H) {
     return (double)(px * px + py * py + kz * kz);
 }
 
-template <int NV>
-__device__ __forceinline__ void block_atomic_add(double (&v)[NV], double *acc) {
-    __shared__ double red[32][NV];
-#pragma unroll
-    for (int i = 0; i < NV; ++i)
-        for (int off = 16; off > 0; off >>= 1) v[i] += __shfl_down_sync(0xffffffffu, v[i], off);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-    __syncthreads();
-    if (lane == 0)
-#pragma unroll
-        for (int i = 0; i < NV; ++i) red[warp][i] = v[i];
-    __syncthreads();
-    if (warp == 0) {
-#pragma unroll
-        for (int i = 0; i < NV; ++i) {
-            double x = lane < nw ? red[lane][i] : 0.0;
-            for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
-            if (lane == 0) atomicAdd(&acc[i], x);
-        }
-    }
-}
-
-// y += (c0 + ck2 k^2) x over n complex elements (n = arrays * modes)
+// point: M = alpha1 Lp + alpha2 p;  Lp += beta p;  part += sum' w k^2 Re(conj M f)
 template <typename T>
-__global__ void ka_lin(long long n, long long modes, int N, int H, psc::cplx<T> *y, const psc::cplx<T> *x, double c0,
-                       double ck2) {
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const double c = c0 + ck2 * k2_of(i % modes, N, H);
-        psc::cplx<T> a = y[i];
-        const psc::cplx<T> b = x[i];
-        a.x += (T)(c * (double)b.x);
-        a.y += (T)(c * (double)b.y);
-        y[i] = a;
-    }
-}
-
-// acc[0] += sum' w Re(conj X Y1) k^2 ; acc[1] += sum' w Re(conj X Y2)  (Y1 or Y2 may be null)
-template <typename T>
-__global__ void ka_dot2(long long n, long long modes, int N, int H, const psc::cplx<T> *X, const psc::cplx<T> *Y1,
-                        const psc::cplx<T> *Y2, double *acc) {
-    double v[2] = {0.0, 0.0};
+__global__ void __launch_bounds__(kThreads) ka_point(long long n, long long modes, int N, int H,
+                                                     psc::cplx<T> *__restrict__ Lp, const psc::cplx<T> *__restrict__ p,
+                                                     const psc::cplx<T> *__restrict__ f, psc::cplx<T> *__restrict__ Mk,
+                                                     const psc::DevAdj *__restrict__ ad, double *__restrict__ part) {
+    const T a1 = (T)ad->alpha1, a2 = (T)ad->alpha2, be = (T)ad->beta;
+    double acc[1] = {0.0};
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const long long m = i % modes;
-        const double w = wk_of(m, H, N / 2);
-        const psc::cplx<T> a = X[i];
-        if (Y1) {
-            const psc::cplx<T> b = Y1[i];
-            v[0] += w * k2_of(m, N, H) * ((double)a.x * b.x + (double)a.y * b.y);
-        }
-        if (Y2) {
-            const psc::cplx<T> b = Y2[i];
-            v[1] += w * ((double)a.x * b.x + (double)a.y * b.y);
-        }
+        const psc::cplx<T> l = Lp[i], q = p[i], fv = f[i];
+        const psc::cplx<T> mv = psc::mk<T>(a1 * l.x + a2 * q.x, a1 * l.y + a2 * q.y);
+        Mk[i] = mv;
+        Lp[i] = psc::mk<T>(l.x + be * q.x, l.y + be * q.y);
+        acc[0] += wk_of(m, H) * k2_of(m, N, H) * ((double)mv.x * fv.x + (double)mv.y * fv.y);
     }
-    block_atomic_add<2>(v, acc);
+    psc::block_reduce_store<1>(acc, part, gridDim.x, blockIdx.x);
 }
 
-// acc[0] += sum' w |p|^2 ; acc[1] += sum' w k^2 |f|^2
+// stage: ph = p + kc (-kn1 k^2 f - kn2 Vp);  part += sum' w Re(conj Lf ph);  Lp += c2 Lf
 template <typename T>
-__global__ void ka_kg(long long n, long long modes, int N, int H, const psc::cplx<T> *f, const psc::cplx<T> *p,
-                      double *acc) {
-    double v[2] = {0.0, 0.0};
+__global__ void __launch_bounds__(kThreads) ka_stage(long long n, long long modes, int N, int H,
+                                                     const psc::cplx<T> *__restrict__ Lf, psc::cplx<T> *__restrict__ Lp,
+                                                     const psc::cplx<T> *__restrict__ p,
+                                                     const psc::cplx<T> *__restrict__ f,
+                                                     const psc::cplx<T> *__restrict__ vp,
+                                                     const psc::DevAdj *__restrict__ ad, double *__restrict__ part) {
+    const T kc = (T)ad->kc, kn1 = (T)ad->kn1, kn2 = (T)ad->kn2, c2 = (T)ad->c2;
+    double acc[1] = {0.0};
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const long long m = i % modes;
-        const double w = wk_of(m, H, N / 2);
-        const psc::cplx<T> a = p[i], b = f[i];
-        v[0] += w * ((double)a.x * a.x + (double)a.y * a.y);
-        v[1] += w * k2_of(m, N, H) * ((double)b.x * b.x + (double)b.y * b.y);
+        const T k2 = (T)k2_of(m, N, H);
+        const psc::cplx<T> l = Lf[i], q = p[i], fv = f[i], v = vp[i];
+        const T fl = -kn1 * k2;
+        const psc::cplx<T> ph = psc::mk<T>(q.x + kc * (fl * fv.x - kn2 * v.x), q.y + kc * (fl * fv.y - kn2 * v.y));
+        acc[0] += wk_of(m, H) * ((double)l.x * ph.x + (double)l.y * ph.y);
+        psc::cplx<T> lp = Lp[i];
+        lp.x += c2 * l.x;
+        lp.y += c2 * l.y;
+        Lp[i] = lp;
     }
-    block_atomic_add<2>(v, acc);
+    psc::block_reduce_store<1>(acc, part, gridDim.x, blockIdx.x);
 }
 
-// Real-space pointwise model work. mode 0: out = V'(f), acc += {V, dV/dgsq, dV/dmu};
-// mode 1: out = V''(f) lambda, acc += {lambda . dV'/dgsq, lambda . dV'/dmu}.
+// observable: part += sum' w |chi_k|^2 and, when Lf is given, Lf = 2 chi_k / N^3
 template <typename T>
-__global__ void kr_model(int mode, long long sites, int nf, int model, double gsq, const T *fx, const T *lam, T *out,
-                         double *acc) {
-    double v[3] = {0.0, 0.0, 0.0};
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < sites;
+__global__ void __launch_bounds__(kThreads) ka_observable(long long modes, int H, const psc::cplx<T> *__restrict__ chi,
+                                                          psc::cplx<T> *__restrict__ Lf, double scale,
+                                                          double *__restrict__ part) {
+    double acc[1] = {0.0};
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < modes;
          i += (long long)gridDim.x * blockDim.x) {
-        const double p = fx[i], c = (nf > 1) ? (double)fx[sites + i] : 0.0;
-        const bool two = (model == PSC_MODEL_PHI2CHI2);
-        if (mode == 0) {
-            out[i] = (T)(two ? p + gsq * p * c * c : p);
-            if (two) out[sites + i] = (T)(gsq * p * p * c);
-            v[0] += 0.5 * p * p + (two ? 0.5 * gsq * p * p * c * c : 0.0);
-            v[1] += two ? 0.5 * p * p * c * c : 0.0;
-            v[2] += 0.5 * p * p;
-        } else {
-            const double l0 = lam[i], l1 = (nf > 1) ? (double)lam[sites + i] : 0.0;
-            if (two) {
-                const double h00 = 1.0 + gsq * c * c, h01 = 2.0 * gsq * p * c, h11 = gsq * p * p;
-                out[i] = (T)(h00 * l0 + h01 * l1);
-                out[sites + i] = (T)(h01 * l0 + h11 * l1);
-                v[0] += l0 * p * c * c + l1 * p * p * c;
-                v[1] += l0 * p;
-            } else {
-                out[i] = (T)l0;
-                v[1] += l0 * p;
-            }
-        }
+        const psc::cplx<T> c = chi[i];
+        acc[0] += wk_of(i, H) * ((double)c.x * c.x + (double)c.y * c.y);
+        if (Lf) Lf[i] = psc::mk<T>((T)(scale * c.x), (T)(scale * c.y));
     }
-    block_atomic_add<3>(v, acc);
+    psc::block_reduce_store<1>(acc, part, gridDim.x, blockIdx.x);
 }
 
-struct BG3 {
-    double a, b, add;
+enum AdjMode { ADJ_INIT = 0, ADJ_PRE = 1, ADJ_POST = 2, ADJ_STAGE_PRE = 3, ADJ_STAGE_POST = 4 };
+
+struct AdjArgs {
+    int mode;
+    int i;           // local point / stage index within the segment
+    long long j;     // global point / stage index
+    double n3;       // N^3
+    // partial-sum regions: [offset, count]
+    int d1_off, d1_n, z_off, z_n, d3_off, d3_n, o_off, o_n;
 };
+
+__device__ double block_sum(const double *__restrict__ v, int n, double *red) {
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) acc += v[i];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = blockDim.x >> 1; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+    }
+    const double r = red[0];
+    __syncthreads();
+    return r;
+}
+
+struct PointBG {
+    double a, b, add, K, G, V, dVg, dVm;
+};
+
+// snapshots of the segment: snap[0] at its first point, snap[1] after the opening
+// of stage 0, snap[i + 2] after the end of local stage i (evolution.cpp:1141-1197)
+__device__ PointBG point_bg(const psc::DevBG *snap, int i) {
+    const psc::DevBG &r = i == 0 ? snap[0] : snap[i + 1];
+    PointBG o;
+    o.a = i == 0 ? snap[0].a : snap[i].a;
+    o.b = i == 0 ? snap[0].ad : r.b;
+    o.add = r.add;
+    o.K = 0;
+    o.G = 0;
+    for (int f = 0; f < r.nf; ++f) {
+        o.K += r.K[f];
+        o.G += r.G[f];
+    }
+    o.V = 0;
+    for (int t = 0; t < r.nterms; ++t) o.V += r.V[t];
+    o.dVm = r.V[0];
+    o.dVg = (r.model == PSC_MODEL_PHI2CHI2) ? r.V[1] / r.gsq : 0.0;
+    return o;
+}
+
+__global__ void __launch_bounds__(256) k_adj(AdjArgs A, psc::DevAdj *__restrict__ ad, const psc::DevBG *__restrict__ snap,
+                                             const double *__restrict__ part) {
+    __shared__ double red[256];
+    double s[4] = {0.0, 0.0, 0.0, 0.0};
+    if (A.mode == ADJ_INIT) s[0] = block_sum(part + A.o_off, A.o_n, red);
+    if (A.mode == ADJ_POST) {
+        s[0] = block_sum(part + A.d1_off, A.d1_n, red);
+        for (int q = 0; q < 3; ++q) s[1 + q] = block_sum(part + A.z_off + q * A.z_n, A.z_n, red);
+    }
+    if (A.mode == ADJ_STAGE_POST) s[0] = block_sum(part + A.d3_off, A.d3_n, red);
+    if (threadIdx.x != 0) return;
+    const psc::DevBG &g0 = snap[0];
+    const int al = g0.alpha, ns = g0.s;
+    const double dt = g0.dt, kIR2 = g0.kIR2, C = g0.fs_over_mpl2 / 3.0, n3 = A.n3;
+    if (A.mode == ADJ_INIT) {
+        ad->la = ad->lb = ad->ladd = ad->lbh = ad->lat = 0.0;
+        ad->gth[0] = ad->gth[1] = 0.0;
+        ad->O = s[0] / (n3 * n3);
+        return;
+    }
+    const int q = (int)(A.j % ns);
+    const double c = g0.w[q] * dt / 2;
+    const PointBG P = point_bg(snap, A.i);
+    const double a = P.a;
+    if (A.mode == ADJ_PRE) {
+        const double cb = A.j > 0 ? g0.w[(q + ns - 1) % ns] * dt / 2 : 0.0;
+        const double lat = ad->ladd + cb * ad->lb;
+        ad->lat = lat;
+        ad->lbh = ad->lb;
+        const double Cc = C * pow(a, (double)(1 + 2 * al));
+        const double beta = lat * Cc * (al - 2) / (pow(a, 6.0) * n3);
+        ad->beta = beta;
+        ad->alpha1 = c + cb;
+        ad->alpha2 = cb * beta;
+        ad->gamma = lat * Cc * (al + 1) / n3;
+        ad->delta = lat * Cc * al * kIR2 / (a * a * n3);
+        ad->eta1 = -pow(a, (double)(1 + al)) * kIR2;
+        ad->eta2 = -pow(a, (double)(3 + al));
+        ad->la += lat * (C * (1 + 2 * al) * pow(a, (double)(2 * al)) * ((al - 2) * P.K + al * P.G + (al + 1) * P.V) +
+                         Cc * ((al - 2) * (-6 * P.K / a) + al * (-2 * P.G / a)));
+        ad->gth[0] += lat * Cc * (al + 1) * P.dVg;
+        ad->gth[1] += lat * Cc * (al + 1) * P.dVm;
+        return;
+    }
+    if (A.mode == ADJ_POST) {
+        const double d1 = s[0] / n3, d2 = s[1];
+        ad->la += (1 + al) * pow(a, (double)al) * (-kIR2) * d1 - (3 + al) * pow(a, (double)(2 + al)) * d2;
+        const double e2 = -pow(a, (double)(3 + al));
+        ad->gth[0] += e2 * s[2];
+        ad->gth[1] += e2 * s[3];
+        return;
+    }
+    if (A.mode == ADJ_STAGE_PRE) {
+        ad->lbh += c * ad->la;
+        ad->c2 = snap[A.i + 1].c_drift;
+        ad->kc = c;
+        ad->kn1 = pow(a, (double)(1 + al)) * kIR2;
+        ad->kn2 = pow(a, (double)(3 + al));
+        return;
+    }
+    // ADJ_STAGE_POST
+    const double d3 = s[0] / n3;
+    const double bh = snap[A.i + 1].b_half;
+    const double ah = a + bh * g0.w[q] * dt / 2.;
+    ad->la += d3 * g0.w[q] * dt * (al - 3) * pow(ah, (double)(al - 4));
+    ad->lbh += c * ad->la;
+    ad->lb = ad->lbh;
+    ad->ladd = c * ad->lbh;
+}
 
 struct AdjWS {
     size_t carr = 0, rarr = 0;   // bytes of nf complex / real arrays
-    void *ph = nullptr, *f1 = nullptr, *p1 = nullptr, *F0 = nullptr, *Vp0 = nullptr, *F1 = nullptr, *Vp1 = nullptr,
-         *Lf = nullptr, *Lp = nullptr, *tmp = nullptr;
-    void *fx0 = nullptr, *fx1 = nullptr, *lam = nullptr, *hout = nullptr;
-    double *acc = nullptr;
-    std::vector<void *> ckpt_f, ckpt_p;   // checkpoints (device)
-    std::vector<BG3> ckpt_bg;
-    std::vector<void *> tape_f, tape_p;   // stage inputs of one segment (device)
-    std::vector<BG3> tape_bg;
+    void *M = nullptr, *Lf = nullptr, *Lp = nullptr;
+    double *part = nullptr;
+    psc::DevAdj *rec = nullptr;
+    psc::DevBG *snap = nullptr;
+    int snap_n = 0;
+    char *tape = nullptr;   // points x (f, p, vp, fx)
+    int tape_n = 0;
+    size_t tape_stride = 0;
+    char *ckpt = nullptr;   // checkpoints x (f, p, bg)
+    int ckpt_n = 0;
+    size_t ckpt_stride = 0;
+    int z_n = 0, part_n = 0;
     std::vector<void *> owned;
 };
 
@@ -194,478 +278,304 @@ int ws_alloc(AdjWS *ws, void **out, size_t bytes) {
     return PSC_OK;
 }
 
-struct Ctx {
-    psc_handle *h;
-    AdjWS *ws;
-    int N, H, nf, prec, alpha, model;
-    long long modes, sites;
-    double kIR2, gsq, C, N3;
-    cudaStream_t st;
-    int grid;
-};
-
-template <typename T>
-int run_lin(const Ctx &c, void *y, const void *x, double c0, double ck2) {
-    ka_lin<T><<<c.grid, kThreads, 0, c.st>>>((long long)c.nf * c.modes, c.modes, c.N, c.H, (psc::cplx<T> *)y,
-                                              (const psc::cplx<T> *)x, c0, ck2);
-    CU(cudaGetLastError());
-    return PSC_OK;
-}
-
-int lin(const Ctx &c, void *y, const void *x, double c0, double ck2) {
-    return c.prec == 32 ? run_lin<float>(c, y, x, c0, ck2) : run_lin<double>(c, y, x, c0, ck2);
-}
-
-int read_acc(const Ctx &c, double *out, int n) {
-    CU(cudaMemcpyAsync(out, c.ws->acc, sizeof(double) * n, cudaMemcpyDeviceToHost, c.st));
-    CU(cudaStreamSynchronize(c.st));
-    return PSC_OK;
-}
-
-int zero_acc(const Ctx &c) {
-    CU(cudaMemsetAsync(c.ws->acc, 0, sizeof(double) * 8, c.st));
-    return PSC_OK;
-}
-
-// sum' w k^2 Re(conj X Y1) and sum' w Re(conj X Y2), divided by N^3
-int dots(const Ctx &c, const void *X, const void *Y1, const void *Y2, double *d1, double *d2) {
-    int rc;
-    if ((rc = zero_acc(c))) return rc;
-    const long long n = (long long)c.nf * c.modes;
-    if (c.prec == 32)
-        ka_dot2<float><<<c.grid, kThreads, 0, c.st>>>(n, c.modes, c.N, c.H, (const float2 *)X, (const float2 *)Y1,
-                                                      (const float2 *)Y2, c.ws->acc);
-    else
-        ka_dot2<double><<<c.grid, kThreads, 0, c.st>>>(n, c.modes, c.N, c.H, (const double2 *)X, (const double2 *)Y1,
-                                                       (const double2 *)Y2, c.ws->acc);
-    CU(cudaGetLastError());
-    double v[2];
-    if ((rc = read_acc(c, v, 2))) return rc;
-    if (d1) *d1 = v[0] / c.N3;
-    if (d2) *d2 = v[1] / c.N3;
-    return PSC_OK;
-}
-
-int c2r(const Ctx &c, const void *src, void *dst) {
-    CU(c.prec == 32 ? psc::reg_c2r_f32(c.h->cfg, c.h->b, src, c.nf, dst, c.st)
-                    : psc::reg_c2r_f64(c.h->cfg, c.h->b, src, c.nf, dst, c.st));
-    return PSC_OK;
-}
-
-int r2c(const Ctx &c, const void *src, void *dst) {
-    CU(c.prec == 32 ? psc::reg_r2c_f32(c.h->cfg, c.h->b, src, c.nf, dst, c.st)
-                    : psc::reg_r2c_f64(c.h->cfg, c.h->b, src, c.nf, dst, c.st));
-    return PSC_OK;
-}
-
-int model(const Ctx &c, int mode, const void *fx, const void *lam, void *out, double *acc3) {
-    int rc;
-    if ((rc = zero_acc(c))) return rc;
-    if (c.prec == 32)
-        kr_model<float><<<c.grid, kThreads, 0, c.st>>>(mode, c.sites, c.nf, c.model, c.gsq, (const float *)fx,
-                                                       (const float *)lam, (float *)out, c.ws->acc);
-    else
-        kr_model<double><<<c.grid, kThreads, 0, c.st>>>(mode, c.sites, c.nf, c.model, c.gsq, (const double *)fx,
-                                                        (const double *)lam, (double *)out, c.ws->acc);
-    CU(cudaGetLastError());
-    return read_acc(c, acc3, 3);
-}
-
-// F = -a^(1+al) kIR^2 k^2 f - a^(3+al) Vp, with fx = f(x) and Vp = r2c(V'(f(x)));
-// vsum3 = {sum V, sum dV/dgsq, sum dV/dmu} over the sites
-int force(const Ctx &c, const void *f, double a, void *fx, void *Vp, void *F, double *vsum3) {
-    int rc;
-    if ((rc = c2r(c, f, fx))) return rc;
-    if ((rc = model(c, 0, fx, nullptr, c.ws->hout, vsum3))) return rc;
-    if ((rc = r2c(c, c.ws->hout, Vp))) return rc;
-    CU(cudaMemsetAsync(F, 0, c.ws->carr, c.st));
-    if ((rc = lin(c, F, f, 0.0, -std::pow(a, 1 + c.alpha) * c.kIR2))) return rc;
-    return lin(c, F, Vp, -std::pow(a, 3 + c.alpha), 0.0);
-}
-
-double A_of(const Ctx &c, double a, double K, double G, double V) {
-    const int al = c.alpha;
-    return c.C * std::pow(a, 1 + 2 * al) * ((al - 2) * K + al * G + (al + 1) * V);
-}
-
-int energies(const Ctx &c, const void *f, const void *p, double a, double vsum, double *K, double *G, double *V) {
-    int rc;
-    if ((rc = zero_acc(c))) return rc;
-    const long long n = (long long)c.nf * c.modes;
-    if (c.prec == 32)
-        ka_kg<float><<<c.grid, kThreads, 0, c.st>>>(n, c.modes, c.N, c.H, (const float2 *)f, (const float2 *)p,
-                                                    c.ws->acc);
-    else
-        ka_kg<double><<<c.grid, kThreads, 0, c.st>>>(n, c.modes, c.N, c.H, (const double2 *)f, (const double2 *)p,
-                                                     c.ws->acc);
-    CU(cudaGetLastError());
-    double v[2];
-    if ((rc = read_acc(c, v, 2))) return rc;
-    *K = .5 * v[0] / std::pow(a, 6) / (c.N3 * c.N3);
-    double grad = c.kIR2 * v[1];
-    grad /= c.N3;
-    grad /= 2.;
-    *G = grad / (a * a) / c.N3;
-    *V = vsum / c.N3;
-    return PSC_OK;
-}
-
-// one stage forward: (f, p, bg) -> (fo, po, bgo); the intermediates stay in the workspace
-int stage_fwd(const Ctx &c, const void *f, const void *p, BG3 bg, double w, double dt, void *fo, void *po, BG3 *bgo,
-              double *vsum1_3 = nullptr, double *KGV = nullptr) {
-    AdjWS *ws = c.ws;
-    const double c1 = w * dt / 2;
-    const double bh = bg.b + c1 * bg.add;
-    double v0[3];
-    int rc;
-    if ((rc = force(c, f, bg.a, ws->fx0, ws->Vp0, ws->F0, v0))) return rc;
-    CU(cudaMemcpyAsync(ws->ph, p, ws->carr, cudaMemcpyDeviceToDevice, c.st));
-    if ((rc = lin(c, ws->ph, ws->F0, c1, 0.0))) return rc;
-    const double ah = bg.a + bh * w * dt / 2.;
-    const double c2 = w * dt * std::pow(ah, c.alpha - 3);
-    CU(cudaMemcpyAsync(fo, f, ws->carr, cudaMemcpyDeviceToDevice, c.st));
-    if ((rc = lin(c, fo, ws->ph, c2, 0.0))) return rc;
-    const double a1 = ah + bh * w * dt / 2.;
-    double v1[3];
-    if ((rc = force(c, fo, a1, ws->fx1, ws->Vp1, ws->F1, v1))) return rc;
-    CU(cudaMemcpyAsync(po, ws->ph, ws->carr, cudaMemcpyDeviceToDevice, c.st));
-    if ((rc = lin(c, po, ws->F1, c1, 0.0))) return rc;
-    double K, G, V;
-    if ((rc = energies(c, fo, po, a1, v1[0], &K, &G, &V))) return rc;
-    bgo->a = a1;
-    bgo->add = A_of(c, a1, K, G, V);
-    bgo->b = bh + c1 * bgo->add;
-    if (vsum1_3)
-        for (int i = 0; i < 3; ++i) vsum1_3[i] = v1[i];
-    if (KGV) {
-        KGV[0] = K;
-        KGV[1] = G;
-        KGV[2] = V;
+int ws_grow(AdjWS *ws, char **ptr, int *have, int want, size_t stride) {
+    if (*have >= want) return PSC_OK;
+    if (*ptr) {
+        auto it = std::find(ws->owned.begin(), ws->owned.end(), (void *)*ptr);
+        if (it != ws->owned.end()) ws->owned.erase(it);
+        cudaFree(*ptr);
+        *ptr = nullptr;
+        *have = 0;
     }
-    return PSC_OK;
-}
-
-struct Adj {
-    double la, lb, ladd;
-    double gth[2];
-};
-
-// (dF/df)^T applied to the adjoint array L at (fx, a), added with factor s into Lf;
-// returns <lambda, dV'/dtheta> sums in th[2]
-int jt_add(const Ctx &c, const void *fx, double a, const void *L, void *Lf, double s, double *th) {
-    AdjWS *ws = c.ws;
-    int rc;
-    if ((rc = c2r(c, L, ws->lam))) return rc;
-    double acc[3];
-    if ((rc = model(c, 1, fx, ws->lam, ws->hout, acc))) return rc;
-    if ((rc = r2c(c, ws->hout, ws->tmp))) return rc;
-    if ((rc = lin(c, Lf, L, 0.0, -s * std::pow(a, 1 + c.alpha) * c.kIR2))) return rc;
-    if ((rc = lin(c, Lf, ws->tmp, -s * std::pow(a, 3 + c.alpha), 0.0))) return rc;
-    th[0] = acc[0];
-    th[1] = acc[1];
-    return PSC_OK;
-}
-
-// reverse one stage given its inputs (f, p, bg); ws->Lf, ws->Lp and adj hold the
-// adjoint of the stage outputs on entry and of its inputs on return
-int stage_adj(const Ctx &c, const void *f, const void *p, BG3 bg, double w, double dt, Adj *adj) {
-    AdjWS *ws = c.ws;
-    const int al = c.alpha;
-    const double c1 = w * dt / 2;
-    int rc;
-    double vs1[3], kgv[3];
-    BG3 o;
-    if ((rc = stage_fwd(c, f, p, bg, w, dt, ws->f1, ws->p1, &o, vs1, kgv))) return rc;
-    const double bh = bg.b + c1 * bg.add;
-    const double ah = bg.a + bh * w * dt / 2.;
-    const double c2 = w * dt * std::pow(ah, al - 3);
-    const double a1 = o.a;
-    const double K1 = kgv[0], G1 = kgv[1], V1 = kgv[2];
-    // b1 = bh + c1 add1
-    const double lat = adj->ladd + c1 * adj->lb;
-    double lbh = adj->lb;
-    double la1 = adj->la;
-    // add1 = A(f1, p1, a1)
-    const double Cc = c.C * std::pow(a1, 1 + 2 * al);
-    if ((rc = lin(c, ws->Lf, ws->f1, 0.0, lat * Cc * al / (a1 * a1 * c.N3) * c.kIR2))) return rc;
-    if ((rc = lin(c, ws->Lf, ws->Vp1, lat * Cc * (al + 1) / c.N3, 0.0))) return rc;
-    if ((rc = lin(c, ws->Lp, ws->p1, lat * Cc * (al - 2) / (std::pow(a1, 6) * c.N3), 0.0))) return rc;
-    la1 += lat * (c.C * (1 + 2 * al) * std::pow(a1, 2 * al) * ((al - 2) * K1 + al * G1 + (al + 1) * V1) +
-                  Cc * ((al - 2) * (-6 * K1 / a1) + al * (-2 * G1 / a1)));
-    adj->gth[0] += lat * Cc * (al + 1) * vs1[1] / c.N3;
-    adj->gth[1] += lat * Cc * (al + 1) * vs1[2] / c.N3;
-    // p1 = ph + c1 F1(f1, a1): dots with Lp1 first, then Lf += c1 J^T Lp1
-    double d1, d2, th[2];
-    if ((rc = dots(c, ws->Lp, ws->f1, ws->Vp1, &d1, &d2))) return rc;
-    la1 += c1 * ((1 + al) * std::pow(a1, al) * (-c.kIR2) * d1 - (3 + al) * std::pow(a1, 2 + al) * d2);
-    if ((rc = jt_add(c, ws->fx1, a1, ws->Lp, ws->Lf, c1, th))) return rc;
-    adj->gth[0] += c1 * (-std::pow(a1, 3 + al)) * th[0];
-    adj->gth[1] += c1 * (-std::pow(a1, 3 + al)) * th[1];
-    // a1 = ah + bh w dt/2
-    double lah = la1;
-    lbh += la1 * w * dt / 2.;
-    // f1 = f + c2(ah) ph: Lph (= Lp buffer) += c2 Lf; lah += <lambda_f1, ph> dc2/dah
-    double d3;
-    if ((rc = dots(c, ws->Lf, nullptr, ws->ph, nullptr, &d3))) return rc;
-    lah += d3 * w * dt * (al - 3) * std::pow(ah, al - 4);
-    if ((rc = lin(c, ws->Lp, ws->Lf, c2, 0.0))) return rc;
-    // ah = a + bh w dt/2
-    double la = lah;
-    lbh += lah * w * dt / 2.;
-    // ph = pi + c1 F0(f, a)
-    if ((rc = dots(c, ws->Lp, f, ws->Vp0, &d1, &d2))) return rc;
-    la += c1 * ((1 + al) * std::pow(bg.a, al) * (-c.kIR2) * d1 - (3 + al) * std::pow(bg.a, 2 + al) * d2);
-    if ((rc = jt_add(c, ws->fx0, bg.a, ws->Lp, ws->Lf, c1, th))) return rc;
-    adj->gth[0] += c1 * (-std::pow(bg.a, 3 + al)) * th[0];
-    adj->gth[1] += c1 * (-std::pow(bg.a, 3 + al)) * th[1];
-    // bh = b + c1 add
-    adj->la = la;
-    adj->lb = lbh;
-    adj->ladd = c1 * lbh;
-    return PSC_OK;
-}
-
-int setup(psc_handle *h, Ctx *c) {
-    if (!h->adj) {
-        AdjWS *ws = new AdjWS();
-        h->adj = ws;
-        h->adj_free = ws_free;
-        const psc::Geo &g = h->cfg.g;
-        ws->carr = (size_t)g.nf * g.modes * h->csize;
-        ws->rarr = (size_t)g.nf * g.sites * (h->csize / 2);
-        void **cs[] = {&ws->ph, &ws->f1, &ws->p1, &ws->F0, &ws->Vp0, &ws->F1, &ws->Vp1, &ws->Lf, &ws->Lp, &ws->tmp};
-        for (void **q : cs)
-            if (int rc = ws_alloc(ws, q, ws->carr)) return rc;
-        void **rs[] = {&ws->fx0, &ws->fx1, &ws->lam, &ws->hout};
-        for (void **q : rs)
-            if (int rc = ws_alloc(ws, q, ws->rarr)) return rc;
-        void *acc;
-        if (int rc = ws_alloc(ws, &acc, sizeof(double) * 8)) return rc;
-        ws->acc = static_cast<double *>(acc);
-    }
-    const psc::Geo &g = h->cfg.g;
-    const psc_params &p = h->p0();
-    c->h = h;
-    c->ws = static_cast<AdjWS *>(h->adj);
-    c->N = g.N;
-    c->H = g.H;
-    c->nf = g.nf;
-    c->prec = p.precision;
-    c->alpha = p.alpha;
-    c->model = p.model;
-    c->modes = g.modes;
-    c->sites = g.sites;
-    c->kIR2 = p.kIR * p.kIR;
-    c->gsq = p.gsq;
-    psc::DevBG bg;
-    if (int rc = psc::hapi::read_bg(h, 0, &bg)) return rc;
-    c->C = bg.fs_over_mpl2 / 3.0;
-    c->N3 = (double)g.sites;
-    c->st = h->st;
-    c->grid = 4 * 152;
+    void *p = nullptr;
+    if (int rc = ws_alloc(ws, &p, stride * (size_t)want)) return rc;
+    *ptr = static_cast<char *>(p);
+    *have = want;
     return PSC_OK;
 }
 
 int check(psc_handle *h) {
+    const psc_params &p = h->p0();
     if (h->R != 1) return fail(PSC_ERR_CONFIG, "the adjoint works on single-lattice handles");
     if (h->cfg.g.N < 32) return fail(PSC_ERR_CONFIG, "the adjoint needs N >= 32");
     if (h->cfg.g.mask)
         return fail(PSC_ERR_CONFIG, "the adjoint differentiates the unmasked step (spectral = 0 or simulate_inflation = 0)");
-    if (h->p0().expansion != 2) return fail(PSC_ERR_CONFIG, "the adjoint needs self-consistent expansion (expansion = 2)");
+    if (p.expansion != 2) return fail(PSC_ERR_CONFIG, "the adjoint needs self-consistent expansion (expansion = 2)");
+    if (p.with_gw) return fail(PSC_ERR_CONFIG, "the adjoint needs with_gw = 0 (GWs do not act on a scalar observable)");
+    if (p.model == PSC_MODEL_PHI2CHI2 && !(p.gsq > 0)) return fail(PSC_ERR_CONFIG, "the adjoint needs gsq > 0");
     if (!h->have_state) return fail(PSC_ERR_STATE, "no state: call psc_init_ic or psc_set_state first");
     return PSC_OK;
+}
+
+struct Run {
+    psc_handle *h;
+    AdjWS *ws;
+    cudaStream_t st;
+    int prec, nf, N, H;
+    long long modes, n;   // n = nf * modes
+    double n3;
+    int z_n;
+};
+
+int setup(psc_handle *h, Run *r) {
+    if (!h->adj) {
+        h->adj = new AdjWS();
+        h->adj_free = ws_free;
+    }
+    AdjWS *ws = static_cast<AdjWS *>(h->adj);
+    const psc::Geo &g = h->cfg.g;
+    if (!ws->M) {
+        ws->carr = (size_t)g.nf * g.modes * h->csize;
+        ws->rarr = (size_t)g.nf * g.sites * (h->csize / 2);
+        void **cs[] = {&ws->M, &ws->Lf, &ws->Lp};
+        for (void **q : cs)
+            if (int rc = ws_alloc(ws, q, ws->carr)) return rc;
+        ws->z_n = h->cfg.nbz;
+        ws->part_n = 3 * kEW + 3 * ws->z_n;
+        void *p;
+        if (int rc = ws_alloc(ws, &p, sizeof(double) * ws->part_n)) return rc;
+        ws->part = static_cast<double *>(p);
+        if (int rc = ws_alloc(ws, &p, sizeof(psc::DevAdj))) return rc;
+        ws->rec = static_cast<psc::DevAdj *>(p);
+        ws->tape_stride = 3 * ws->carr + ws->rarr;
+        ws->ckpt_stride = 2 * ws->carr + ((sizeof(psc::DevBG) + 255) / 256) * 256;
+    }
+    r->h = h;
+    r->ws = ws;
+    r->st = h->st;
+    r->prec = h->p0().precision;
+    r->nf = g.nf;
+    r->N = g.N;
+    r->H = g.H;
+    r->modes = g.modes;
+    r->n = (long long)g.nf * g.modes;
+    r->n3 = (double)g.sites;
+    r->z_n = ws->z_n;
+    return PSC_OK;
+}
+
+AdjArgs args(const Run &r, int mode, int i, long long j) {
+    AdjArgs A;
+    A.mode = mode;
+    A.i = i;
+    A.j = j;
+    A.n3 = r.n3;
+    A.d1_off = 0;
+    A.d1_n = kEW;
+    A.z_off = kEW;
+    A.z_n = r.z_n;
+    A.d3_off = kEW + 3 * r.z_n;
+    A.d3_n = kEW;
+    A.o_off = 2 * kEW + 3 * r.z_n;
+    A.o_n = kEW;
+    return A;
+}
+
+int scalar(const Run &r, int mode, int i, long long j) {
+    k_adj<<<1, 256, 0, r.st>>>(args(r, mode, i, j), r.ws->rec, r.ws->snap, r.ws->part);
+    CU(cudaGetLastError());
+    return PSC_OK;
+}
+
+char *tape_pt(const Run &r, int i) { return r.ws->tape + (size_t)i * r.ws->tape_stride; }
+void *tp_f(const Run &r, int i) { return tape_pt(r, i); }
+void *tp_p(const Run &r, int i) { return tape_pt(r, i) + r.ws->carr; }
+void *tp_vp(const Run &r, int i) { return tape_pt(r, i) + 2 * r.ws->carr; }
+void *tp_fx(const Run &r, int i) { return tape_pt(r, i) + 3 * r.ws->carr; }
+
+// O from the handle's current state (Parseval: <chi^2> = sum' w |chi_k|^2 / N^6)
+// and, with Lf_last, the adjoint seed Lambda_chi = r2c(2 chi / N^3) = 2 chi_k / N^3
+int observable(const Run &r, void *Lf_last) {
+    const size_t one = (size_t)r.modes * r.h->csize;
+    const void *chi = static_cast<const char *>(r.h->b.fk) + (size_t)(r.nf - 1) * one;
+    double *part = r.ws->part + 2 * kEW + 3 * r.z_n;
+    if (r.prec == 32)
+        ka_observable<float><<<kEW, kThreads, 0, r.st>>>(r.modes, r.H, (const float2 *)chi, (float2 *)Lf_last,
+                                                         2.0 / r.n3, part);
+    else
+        ka_observable<double><<<kEW, kThreads, 0, r.st>>>(r.modes, r.H, (const double2 *)chi, (double2 *)Lf_last,
+                                                          2.0 / r.n3, part);
+    CU(cudaGetLastError());
+    return scalar(r, ADJ_INIT, 0, 0);
+}
+
+// the product's step sequence for n steps from the handle's state, writing the tape
+// of points 0 .. n s - 1 and the background snapshots
+int forward_taped(const Run &r, double dt, int n) {
+    psc_handle *h = r.h;
+    AdjWS *ws = r.ws;
+    const int s = h->s, npts = n * s;
+    psc::Buffers bt = h->b;
+    auto tape_at = [&](int i) {
+        if (i < npts) {
+            bt.tape_f = tp_f(r, i);
+            bt.tape_p = tp_p(r, i);
+            bt.tape_vp = tp_vp(r, i);
+            bt.tape_fx = tp_fx(r, i);
+        } else {
+            bt.tape_f = bt.tape_p = bt.tape_vp = bt.tape_fx = nullptr;
+        }
+    };
+    CU(psc::launch_set_run(h->b.bg, 1, dt, n, r.st));
+    CU(cudaMemcpyAsync(ws->snap + 0, h->b.bg, sizeof(psc::DevBG), cudaMemcpyDeviceToDevice, r.st));
+    CU(psc::launch_scalar(h->cfg, h->b, psc::SCALAR_PRIME, 0, r.st));
+    tape_at(0);
+    CU(psc::launch_stage(h->cfg, bt, r.prec, 0, r.st));
+    CU(psc::launch_scalar(h->cfg, h->b, psc::SCALAR_BEGIN, 0, r.st));
+    CU(cudaMemcpyAsync(ws->snap + 1, h->b.bg, sizeof(psc::DevBG), cudaMemcpyDeviceToDevice, r.st));
+    for (int i = 0; i < npts; ++i) {
+        tape_at(i + 1);
+        CU(psc::launch_stage(h->cfg, bt, r.prec, 1, r.st));
+        CU(psc::launch_scalar(h->cfg, h->b, psc::SCALAR_END, i % s, r.st));
+        CU(cudaMemcpyAsync(ws->snap + i + 2, h->b.bg, sizeof(psc::DevBG), cudaMemcpyDeviceToDevice, r.st));
+    }
+    return PSC_OK;
+}
+
+template <typename T>
+int reverse_segment_t(const Run &r, long long jbase, int npts) {
+    using C = psc::cplx<T>;
+    AdjWS *ws = r.ws;
+    psc_handle *h = r.h;
+    double *p_d1 = ws->part, *p_z = ws->part + kEW, *p_d3 = ws->part + kEW + 3 * r.z_n;
+    int rc;
+    for (int i = npts - 1; i >= 0; --i) {
+        const long long j = jbase + i;
+        // the internals of stage j (its drift and a-updates)
+        if ((rc = scalar(r, ADJ_STAGE_PRE, i, j))) return rc;
+        ka_stage<T><<<kEW, kThreads, 0, r.st>>>(r.n, r.modes, r.N, r.H, (const C *)ws->Lf, (C *)ws->Lp,
+                                                (const C *)tp_p(r, i), (const C *)tp_f(r, i), (const C *)tp_vp(r, i),
+                                                ws->rec, p_d3);
+        CU(cudaGetLastError());
+        if ((rc = scalar(r, ADJ_STAGE_POST, i, j))) return rc;
+        // point j: merged J^T of the kicks at P_j and the a''(P_j) terms
+        if ((rc = scalar(r, ADJ_PRE, i, j))) return rc;
+        ka_point<T><<<kEW, kThreads, 0, r.st>>>(r.n, r.modes, r.N, r.H, (C *)ws->Lp, (const C *)tp_p(r, i),
+                                                (const C *)tp_f(r, i), (C *)ws->M, ws->rec, p_d1);
+        CU(cudaGetLastError());
+        CU(r.prec == 32 ? psc::reg_adj_point_f32(h->cfg, h->b, ws->M, tp_f(r, i), tp_fx(r, i), ws->Lf, p_z, ws->rec,
+                                                 r.st)
+                        : psc::reg_adj_point_f64(h->cfg, h->b, ws->M, tp_f(r, i), tp_fx(r, i), ws->Lf, p_z, ws->rec,
+                                                 r.st));
+        if ((rc = scalar(r, ADJ_POST, i, j))) return rc;
+    }
+    return PSC_OK;
+}
+
+int reverse_segment(const Run &r, long long jbase, int npts) {
+    return r.prec == 32 ? reverse_segment_t<float>(r, jbase, npts) : reverse_segment_t<double>(r, jbase, npts);
+}
+
+int save_state(const Run &r, char *dst) {
+    CU(cudaMemcpyAsync(dst, r.h->b.fk, r.ws->carr, cudaMemcpyDeviceToDevice, r.st));
+    CU(cudaMemcpyAsync(dst + r.ws->carr, r.h->b.pk, r.ws->carr, cudaMemcpyDeviceToDevice, r.st));
+    CU(cudaMemcpyAsync(dst + 2 * r.ws->carr, r.h->b.bg, sizeof(psc::DevBG), cudaMemcpyDeviceToDevice, r.st));
+    return PSC_OK;
+}
+
+int restore_state(const Run &r, const char *src) {
+    CU(cudaMemcpyAsync(r.h->b.fk, src, r.ws->carr, cudaMemcpyDeviceToDevice, r.st));
+    CU(cudaMemcpyAsync(r.h->b.pk, src + r.ws->carr, r.ws->carr, cudaMemcpyDeviceToDevice, r.st));
+    CU(cudaMemcpyAsync(r.h->b.bg, src + 2 * r.ws->carr, sizeof(psc::DevBG), cudaMemcpyDeviceToDevice, r.st));
+    return PSC_OK;
+}
+
+int grow_snap(AdjWS *ws, int want) {
+    char *sp = reinterpret_cast<char *>(ws->snap);
+    int rc = ws_grow(ws, &sp, &ws->snap_n, want, sizeof(psc::DevBG));
+    ws->snap = reinterpret_cast<psc::DevBG *>(sp);
+    return rc;
 }
 
 }  // namespace
 
 extern "C" int psc_adjoint_chi2(psc_handle *h, double dt, int nsteps, int every, double *O, double *grad_fk,
                                 double *grad_pik, double *grad_ad0, double *grad_theta) {
-    if (!h || !O || nsteps < 1 || !(dt > 0)) return fail(PSC_ERR_ARG, "bad argument");
-    if (int rc = check(h)) return rc;
-    if (every < 1) every = nsteps;
-    Ctx c;
+    if (!h || !O || nsteps < 1 || !(dt > 0) || !std::isfinite(dt)) return fail(PSC_ERR_ARG, "bad argument");
     int rc;
-    if ((rc = setup(h, &c))) return rc;
-    AdjWS *ws = c.ws;
+    if ((rc = check(h))) return rc;
+    if (every < 1 || every > nsteps) every = nsteps;
+    Run r;
+    if ((rc = setup(h, &r))) return rc;
+    AdjWS *ws = r.ws;
     const int s = h->s;
-    const double *w = h->w;
     const int nseg = (nsteps + every - 1) / every;
-    // storage: checkpoints and one segment's stage inputs
-    while ((int)ws->ckpt_f.size() < nseg) {
-        void *a, *b;
-        if ((rc = ws_alloc(ws, &a, ws->carr)) || (rc = ws_alloc(ws, &b, ws->carr))) return rc;
-        ws->ckpt_f.push_back(a);
-        ws->ckpt_p.push_back(b);
+    const int npts_max = every * s;
+    // storage: tape of one segment, snapshots, checkpoints (+ the final state)
+    if ((rc = ws_grow(ws, &ws->tape, &ws->tape_n, npts_max, ws->tape_stride))) return rc;
+    if ((rc = grow_snap(ws, npts_max + 2))) return rc;
+    if (nseg > 1 && (rc = ws_grow(ws, &ws->ckpt, &ws->ckpt_n, nseg + 1, ws->ckpt_stride))) return rc;
+    // a''(0) = A(state(0)) and the reductions at the first point
+    if ((rc = psc::hapi::evaluate(h, 0))) return rc;
+    CU(cudaMemsetAsync(ws->Lf, 0, ws->carr, r.st));
+    CU(cudaMemsetAsync(ws->Lp, 0, ws->carr, r.st));
+    void *Lf_last = static_cast<char *>(ws->Lf) + (size_t)(r.nf - 1) * r.modes * h->csize;
+    if (nseg > 1) {
+        // checkpoint pass on the product's captured step
+        for (int seg = 0; seg < nseg; ++seg) {
+            if ((rc = save_state(r, ws->ckpt + (size_t)seg * ws->ckpt_stride))) return rc;
+            if ((rc = psc::hapi::step(h, dt, std::min(every, nsteps - seg * every)))) return rc;
+        }
+        if ((rc = save_state(r, ws->ckpt + (size_t)nseg * ws->ckpt_stride))) return rc;
+        CU(cudaMemcpyAsync(ws->snap, h->b.bg, sizeof(psc::DevBG), cudaMemcpyDeviceToDevice, r.st));
+        if ((rc = observable(r, Lf_last))) return rc;
     }
-    ws->ckpt_bg.assign(nseg, BG3{});
-    const int tape_len = every * s;
-    while ((int)ws->tape_f.size() < tape_len) {
-        void *a, *b;
-        if ((rc = ws_alloc(ws, &a, ws->carr)) || (rc = ws_alloc(ws, &b, ws->carr))) return rc;
-        ws->tape_f.push_back(a);
-        ws->tape_p.push_back(b);
-    }
-    ws->tape_bg.assign(tape_len, BG3{});
-    // initial state; a''(0) consistent with it
-    psc::DevBG dbg;
-    if ((rc = psc::hapi::read_bg(h, 0, &dbg))) return rc;
-    BG3 bg0{dbg.a, dbg.ad, 0.0};
-    {
-        double v[3], K, G, V;
-        if ((rc = c2r(c, h->b.fk, ws->fx0))) return rc;
-        if ((rc = model(c, 0, ws->fx0, nullptr, ws->hout, v))) return rc;
-        if ((rc = energies(c, h->b.fk, h->b.pk, bg0.a, v[0], &K, &G, &V))) return rc;
-        bg0.add = A_of(c, bg0.a, K, G, V);
-    }
-    // forward with checkpoints (the handle's arrays carry the state)
-    void *curf = h->b.fk, *curp = h->b.pk;
-    BG3 bg = bg0;
-    for (int seg = 0, done = 0; seg < nseg; ++seg) {
-        CU(cudaMemcpyAsync(ws->ckpt_f[seg], curf, ws->carr, cudaMemcpyDeviceToDevice, c.st));
-        CU(cudaMemcpyAsync(ws->ckpt_p[seg], curp, ws->carr, cudaMemcpyDeviceToDevice, c.st));
-        ws->ckpt_bg[seg] = bg;
-        const int n = std::min(every, nsteps - done);
-        for (int k = 0; k < n; ++k)
-            for (int q = 0; q < s; ++q) {
-                BG3 o;
-                if ((rc = stage_fwd(c, curf, curp, bg, w[q], dt, ws->f1, ws->p1, &o, nullptr))) return rc;
-                CU(cudaMemcpyAsync(curf, ws->f1, ws->carr, cudaMemcpyDeviceToDevice, c.st));
-                CU(cudaMemcpyAsync(curp, ws->p1, ws->carr, cudaMemcpyDeviceToDevice, c.st));
-                bg = o;
-            }
-        done += n;
-    }
-    // observable O = <chi^2> and its adjoint: Lambda_chi = r2c(2 chi / N^3) = 2 chi_k / N^3
-    {
-        if ((rc = c2r(c, curf, ws->fx1))) return rc;
-        std::vector<double> chi;
-        const size_t rbytes = (size_t)c.sites * (h->csize / 2);
-        const char *last = static_cast<const char *>(ws->fx1) + (size_t)(c.nf - 1) * rbytes;
-        chi.resize(c.sites);
-        if ((rc = psc::hapi::download_real(h, chi.data(), last, (size_t)c.sites))) return rc;
-        double acc = 0.0;
-        for (double x : chi) acc += x * x;
-        *O = acc / c.N3;
-    }
-    CU(cudaMemsetAsync(ws->Lf, 0, ws->carr, c.st));
-    CU(cudaMemsetAsync(ws->Lp, 0, ws->carr, c.st));
-    {
-        const size_t one = (size_t)c.modes * h->csize;
-        char *Lf_last = static_cast<char *>(ws->Lf) + (size_t)(c.nf - 1) * one;
-        const char *f_last = static_cast<const char *>(curf) + (size_t)(c.nf - 1) * one;
-        Ctx c1 = c;
-        c1.nf = 1;
-        if ((rc = lin(c1, Lf_last, f_last, 2.0 / c.N3, 0.0))) return rc;
-    }
-    Adj adj{0.0, 0.0, 0.0, {0.0, 0.0}};
-    // reverse sweep over segments
     for (int seg = nseg - 1; seg >= 0; --seg) {
         const int n = std::min(every, nsteps - seg * every);
-        // recompute the segment keeping every stage input
-        CU(cudaMemcpyAsync(curf, ws->ckpt_f[seg], ws->carr, cudaMemcpyDeviceToDevice, c.st));
-        CU(cudaMemcpyAsync(curp, ws->ckpt_p[seg], ws->carr, cudaMemcpyDeviceToDevice, c.st));
-        bg = ws->ckpt_bg[seg];
-        int t = 0;
-        for (int k = 0; k < n; ++k)
-            for (int q = 0; q < s; ++q, ++t) {
-                CU(cudaMemcpyAsync(ws->tape_f[t], curf, ws->carr, cudaMemcpyDeviceToDevice, c.st));
-                CU(cudaMemcpyAsync(ws->tape_p[t], curp, ws->carr, cudaMemcpyDeviceToDevice, c.st));
-                ws->tape_bg[t] = bg;
-                BG3 o;
-                if ((rc = stage_fwd(c, curf, curp, bg, w[q], dt, ws->f1, ws->p1, &o, nullptr))) return rc;
-                CU(cudaMemcpyAsync(curf, ws->f1, ws->carr, cudaMemcpyDeviceToDevice, c.st));
-                CU(cudaMemcpyAsync(curp, ws->p1, ws->carr, cudaMemcpyDeviceToDevice, c.st));
-                bg = o;
-            }
-        for (int k = n - 1; k >= 0; --k)
-            for (int q = s - 1; q >= 0; --q) {
-                const int ti = k * s + q;
-                if ((rc = stage_adj(c, ws->tape_f[ti], ws->tape_p[ti], ws->tape_bg[ti], w[q], dt, &adj))) return rc;
-            }
+        if (nseg > 1 && (rc = restore_state(r, ws->ckpt + (size_t)seg * ws->ckpt_stride))) return rc;
+        if ((rc = forward_taped(r, dt, n))) return rc;
+        if (nseg == 1 && (rc = observable(r, Lf_last))) return rc;
+        if ((rc = reverse_segment(r, (long long)seg * every * s, n * s))) return rc;
     }
-    // a''(0) = A(f0, pi0, a0): fold its adjoint into the initial state
-    {
-        const void *f0 = ws->ckpt_f[0], *p0 = ws->ckpt_p[0];
-        const int al = c.alpha;
-        const double a0 = bg0.a;
-        double v[3], K, G, V;
-        if ((rc = c2r(c, f0, ws->fx0))) return rc;
-        if ((rc = model(c, 0, ws->fx0, nullptr, ws->hout, v))) return rc;
-        if ((rc = r2c(c, ws->hout, ws->Vp0))) return rc;
-        if ((rc = energies(c, f0, p0, a0, v[0], &K, &G, &V))) return rc;
-        const double Cc = c.C * std::pow(a0, 1 + 2 * al);
-        const double l = adj.ladd;
-        if ((rc = lin(c, ws->Lf, f0, 0.0, l * Cc * al / (a0 * a0 * c.N3) * c.kIR2))) return rc;
-        if ((rc = lin(c, ws->Lf, ws->Vp0, l * Cc * (al + 1) / c.N3, 0.0))) return rc;
-        if ((rc = lin(c, ws->Lp, p0, l * Cc * (al - 2) / (std::pow(a0, 6) * c.N3), 0.0))) return rc;
-        adj.gth[0] += l * Cc * (al + 1) * v[1] / c.N3;
-        adj.gth[1] += l * Cc * (al + 1) * v[2] / c.N3;
+    psc::DevAdj rec;
+    CU(cudaMemcpyAsync(&rec, ws->rec, sizeof(rec), cudaMemcpyDeviceToHost, r.st));
+    CU(cudaStreamSynchronize(r.st));
+    if (!std::isfinite(rec.O) || !std::isfinite(rec.lb) || !std::isfinite(rec.gth[0]) || !std::isfinite(rec.gth[1]))
+        return fail(PSC_ERR_NONFINITE, "non-finite observable or gradient");
+    *O = rec.O;
+    if (grad_ad0) *grad_ad0 = rec.lb;
+    if (grad_theta) {
+        grad_theta[0] = rec.gth[0];
+        grad_theta[1] = rec.gth[1];
     }
     // gradients with respect to the stored half spectrum: (w_k / N^3) Lambda_k
-    const size_t ncplx = (size_t)c.nf * c.modes;
+    const size_t ncplx = (size_t)r.n;
     auto to_grad = [&](const void *L, double *out) -> int {
         if (!out) return PSC_OK;
-        int r = psc::hapi::download_real(h, out, L, 2 * ncplx);
-        if (r) return r;
+        int e = psc::hapi::download_real(h, out, L, 2 * ncplx);
+        if (e) return e;
         for (size_t i = 0; i < ncplx; ++i) {
-            const int kz = (int)((i % c.modes) % c.H);
-            const double wk = (kz == 0 || kz == c.H - 1) ? 1.0 : 2.0;
-            out[2 * i] *= wk / c.N3;
-            out[2 * i + 1] *= wk / c.N3;
+            const int kz = (int)((i % r.modes) % r.H);
+            const double wk = (kz == 0 || kz == r.H - 1) ? 1.0 : 2.0;
+            out[2 * i] *= wk / r.n3;
+            out[2 * i + 1] *= wk / r.n3;
         }
         return PSC_OK;
     };
     if ((rc = to_grad(ws->Lf, grad_fk)) || (rc = to_grad(ws->Lp, grad_pik))) return rc;
-    if (grad_ad0) *grad_ad0 = adj.lb;
-    if (grad_theta) {
-        grad_theta[0] = adj.gth[0];
-        grad_theta[1] = adj.gth[1];
+    // leave the handle at the final state, as psc_step(h, dt, nsteps) would
+    if (nseg > 1) {
+        if ((rc = restore_state(r, ws->ckpt + (size_t)nseg * ws->ckpt_stride))) return rc;
+        CU(cudaStreamSynchronize(r.st));
     }
-    // leave the handle at the final state, as psc_step would
-    dbg.a = bg.a;
-    dbg.ad = bg.b;
-    dbg.add = bg.add;
-    dbg.t += dt * nsteps;
-    if ((rc = psc::hapi::write_bg(h, 0, dbg))) return rc;
-    return psc::hapi::evaluate(h, 0);
+    h->diag_valid = true;
+    return PSC_OK;
 }
 
-// Forward only with the same stage sequence (for finite differences of the
-// adjoint's own discrete map): O = <chi^2> after nsteps, a''(0) from the state.
 extern "C" int psc_adjoint_forward_chi2(psc_handle *h, double dt, int nsteps, double *O) {
-    if (!h || !O || nsteps < 1 || !(dt > 0)) return fail(PSC_ERR_ARG, "bad argument");
-    if (int rc = check(h)) return rc;
-    Ctx c;
+    if (!h || !O || nsteps < 1 || !(dt > 0) || !std::isfinite(dt)) return fail(PSC_ERR_ARG, "bad argument");
     int rc;
-    if ((rc = setup(h, &c))) return rc;
-    AdjWS *ws = c.ws;
-    psc::DevBG dbg;
-    if ((rc = psc::hapi::read_bg(h, 0, &dbg))) return rc;
-    BG3 bg{dbg.a, dbg.ad, 0.0};
-    double v[3], K, G, V;
-    if ((rc = c2r(c, h->b.fk, ws->fx0))) return rc;
-    if ((rc = model(c, 0, ws->fx0, nullptr, ws->hout, v))) return rc;
-    if ((rc = energies(c, h->b.fk, h->b.pk, bg.a, v[0], &K, &G, &V))) return rc;
-    bg.add = A_of(c, bg.a, K, G, V);
-    for (int k = 0; k < nsteps; ++k)
-        for (int q = 0; q < h->s; ++q) {
-            BG3 o;
-            if ((rc = stage_fwd(c, h->b.fk, h->b.pk, bg, h->w[q], dt, ws->f1, ws->p1, &o, nullptr))) return rc;
-            CU(cudaMemcpyAsync(h->b.fk, ws->f1, ws->carr, cudaMemcpyDeviceToDevice, c.st));
-            CU(cudaMemcpyAsync(h->b.pk, ws->p1, ws->carr, cudaMemcpyDeviceToDevice, c.st));
-            bg = o;
-        }
-    if ((rc = c2r(c, h->b.fk, ws->fx1))) return rc;
-    std::vector<double> chi(c.sites);
-    const char *last = static_cast<const char *>(ws->fx1) + (size_t)(c.nf - 1) * c.sites * (h->csize / 2);
-    if ((rc = psc::hapi::download_real(h, chi.data(), last, (size_t)c.sites))) return rc;
-    double acc = 0.0;
-    for (double x : chi) acc += x * x;
-    *O = acc / c.N3;
-    dbg.a = bg.a;
-    dbg.ad = bg.b;
-    dbg.add = bg.add;
-    dbg.t += dt * nsteps;
-    if ((rc = psc::hapi::write_bg(h, 0, dbg))) return rc;
-    return psc::hapi::evaluate(h, 0);
+    if ((rc = check(h))) return rc;
+    Run r;
+    if ((rc = setup(h, &r))) return rc;
+    if ((rc = grow_snap(r.ws, 2))) return rc;
+    if ((rc = psc::hapi::evaluate(h, 0))) return rc;
+    if ((rc = psc::hapi::step(h, dt, nsteps))) return rc;
+    CU(cudaMemcpyAsync(r.ws->snap, h->b.bg, sizeof(psc::DevBG), cudaMemcpyDeviceToDevice, r.st));
+    if ((rc = observable(r, nullptr))) return rc;
+    psc::DevAdj rec;
+    CU(cudaMemcpyAsync(&rec, r.ws->rec, sizeof(rec), cudaMemcpyDeviceToHost, r.st));
+    CU(cudaStreamSynchronize(r.st));
+    *O = rec.O;
+    return PSC_OK;
 }

@@ -28,4 +28,19 @@ struct DevBG {
     int stage, steps_left, err, pad;
 };
 
+// Scalar state of the discrete adjoint (psc_adjoint.cu), resident in device memory
+// so the reverse sweep needs no host round trip: the adjoints of a, b = a', a''
+// and of the couplings, and the coefficients the array kernels of the current
+// lattice point (point) or stage (stage) read.
+struct DevAdj {
+    double la, lb, ladd, lbh, lat;
+    double gth[2];
+    // point: M = alpha1 Lp + alpha2 p; Lp += beta p;
+    //        Lf += J^T-part (eta1 k^2 M, eta2 V''(f) m) + gamma V'(f) + delta k^2 f
+    double alpha1, alpha2, beta, gamma, delta, eta1, eta2;
+    // stage: ph = p + kc (-kn1 k^2 f - kn2 Vp); Lp += c2 Lf
+    double c2, kc, kn1, kn2;
+    double O;
+};
+
 }  // namespace psc

@@ -10,6 +10,7 @@
 namespace psc {
 
 struct DevBG;
+struct DevAdj;
 
 // Lattice geometry and tiling, passed by value to every pass kernel.
 struct Geo {
@@ -54,6 +55,9 @@ struct Buffers {
     double *spec;                // spectra accumulators
     int *spec_cnt;
     DevBG *bg;
+    // forward tape of the adjoint (single lattice, no GW; null otherwise): the
+    // stage-point state f, pi (synchronised), V'_k and the real fields f(x)
+    void *tape_f, *tape_p, *tape_vp, *tape_fx;
 };
 
 enum ScalarMode {
@@ -99,11 +103,13 @@ cudaError_t reg_stage_f64(const LaunchCfg &cfg, const Buffers &b, int drift, cud
                           int scalar_mode);
 cudaError_t reg_c2r_real_f32(const LaunchCfg &cfg, const Buffers &b, const void *src, int nsrc, cudaStream_t st);
 cudaError_t reg_c2r_real_f64(const LaunchCfg &cfg, const Buffers &b, const void *src, int nsrc, cudaStream_t st);
-// General 3-D transforms of n arrays (N >= 32): complex [n][modes] -> real [n][sites]
-// (c2r / N^3, uses TA as scratch) and real -> complex (unnormalised r2c, n <= 8).
-cudaError_t reg_c2r_f32(const LaunchCfg &cfg, const Buffers &b, const void *src, int n, void *dst, cudaStream_t st);
-cudaError_t reg_c2r_f64(const LaunchCfg &cfg, const Buffers &b, const void *src, int n, void *dst, cudaStream_t st);
-cudaError_t reg_r2c_f32(const LaunchCfg &cfg, const Buffers &b, const void *src, int n, void *dst, cudaStream_t st);
-cudaError_t reg_r2c_f64(const LaunchCfg &cfg, const Buffers &b, const void *src, int n, void *dst, cudaStream_t st);
+// The adjoint's J^T application at a stage point (register engine, one lattice, no GW):
+// Lf += eta1 k^2 Mk + delta k^2 f_tape + r2c(eta2 V''(f(x)) m + gamma V'(f(x))), m = c2r(Mk) / N^3,
+// coefficients from the device record ad; block partial sums of m.V', m.dV'/dgsq, m.dV'/dmu
+// into part[i * nbz + block]. Uses TA and QV as scratch.
+cudaError_t reg_adj_point_f32(const LaunchCfg &cfg, const Buffers &b, const void *Mk, const void *f_tape,
+                              const void *fx_tape, void *Lf, double *part, const DevAdj *ad, cudaStream_t st);
+cudaError_t reg_adj_point_f64(const LaunchCfg &cfg, const Buffers &b, const void *Mk, const void *f_tape,
+                              const void *fx_tape, void *Lf, double *part, const DevAdj *ad, cudaStream_t st);
 
 }  // namespace psc

@@ -167,7 +167,10 @@ __global__ void __launch_bounds__(256, 2) kr_fft_x_final(Geo g, const cplx<T> *_
                                                       const cplx<T> *__restrict__ QS, const cplx<T> *__restrict__ fk,
                                                       cplx<T> *__restrict__ pk, cplx<T> *__restrict__ uk,
                                                       cplx<T> *__restrict__ puk, double *__restrict__ partKG,
-                                                      const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw) {
+                                                      const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw,
+                                                      cplx<T> *__restrict__ tape_f = nullptr,
+                                                      cplx<T> *__restrict__ tape_p = nullptr,
+                                                      cplx<T> *__restrict__ tape_vp = nullptr) {
     using C = cplx<T>;
     using RP = RegPlan<L>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -254,6 +257,11 @@ __global__ void __launch_bounds__(256, 2) kr_fft_x_final(Geo g, const cplx<T> *_
                         accG += wgt * (double)k2 * ((double)f.x * f.x + (double)f.y * f.y);
                     }
                     pk[a] = mk<T>(pf.x + c_open * F.x, pf.y + c_open * F.y);
+                    if (!GW && tape_p) {   // adjoint tape: the synchronised stage-point state
+                        tape_f[a] = f;
+                        tape_p[a] = pf;
+                        tape_vp[a] = qv;
+                    }
                 }
         }
         double vals[2] = {accK, accG};
@@ -298,7 +306,8 @@ template <typename T, int L, bool GW>
 __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restrict__ TA, const cplx<T> *__restrict__ TB,
                                                 const cplx<T> *__restrict__ TC, cplx<T> *__restrict__ QV,
                                                 cplx<T> *__restrict__ QS, double *__restrict__ partV,
-                                                const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw) {
+                                                const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw,
+                                                T *__restrict__ tape_fx = nullptr) {
     using C = cplx<T>;
     using RP = RegPlan<L>;
     constexpr int M = L, P = RP::P, LS = ZIdx<L>::LS;
@@ -390,6 +399,12 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
 #pragma unroll
         for (int o = 0; o < 8; ++o)
             if (o < nin) in[o] = slots[o * slot_elems + e];
+        if (!GW && tape_fx) {   // adjoint tape: the real fields (sites 2m, 2m+1 of the line)
+            const long long ln = (long long)blockIdx.x * TL + tt;
+#pragma unroll
+            for (int fl = 0; fl < 2; ++fl)
+                if (fl < nf) reinterpret_cast<C *>(tape_fx + fl * g.sites + ln * N)[m] = in[fl];
+        }
         C out[8];
 #pragma unroll
         for (int half = 0; half < 2; ++half) {
@@ -520,79 +535,181 @@ __global__ void __launch_bounds__(256) kr_z_c2r_real(Geo g, const cplx<T> *__res
     }
 }
 
-// ------------------------------------------------------------------ plain forward transforms
-// Real-to-complex along z: real lines [lines_z][N] (blockIdx.y selects the array) ->
-// half-spectrum lines [lines_z][H]; X[k] = (Z[k] + conj Z[M-k])/2 + e^{-2 pi i k/N}
-// (Z[k] - conj Z[M-k])/(2i), Z the M-point transform of x[2m] + i x[2m+1].
+// ------------------------------------------------------------------ adjoint passes
+// Z pass of the adjoint's J^T application at a stage point (no GW): per z line,
+// m = c2r(M) / N^3 of every field, the taped real fields f(x) of the point,
+// out = eta2 V''(f) m + gamma V'(f) and r2c(out) -> QV; block partial sums of
+// sum m.V'(f), sum m.dV'/dgsq, sum m.dV'/dmu (V = mu phi^2/2 + gsq phi^2 chi^2/2, mu = 1).
+// Same thread layout, slots and phases as the product's Z pass.
 template <typename T, int L>
-__global__ void __launch_bounds__(256) kr_z_r2c_real(Geo g, const T *__restrict__ in, cplx<T> *__restrict__ out,
-                                                     const cplx<T> *__restrict__ tw, int tl_shift) {
+__global__ void __launch_bounds__(256, 2) kr_zpass_adj(Geo g, const cplx<T> *__restrict__ TA, const T *__restrict__ fx,
+                                                    cplx<T> *__restrict__ QV, double *__restrict__ part,
+                                                    const DevAdj *__restrict__ ad, const cplx<T> *__restrict__ tw) {
     using C = cplx<T>;
     using RP = RegPlan<L>;
     constexpr int M = L, P = RP::P, LS = ZIdx<L>::LS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    C *sm = reinterpret_cast<C *>(smem_raw);
-    const int TL = 1 << tl_shift, H = g.H, N = g.N;
-    const int j = threadIdx.x % P, t = threadIdx.x / P;
+    C *slots = reinterpret_cast<C *>(smem_raw);
+    const int sh = g.tlz_shift, TL = 1 << sh, H = g.H, N = g.N;
+    const int nf = g.nf;
+    const int j = threadIdx.x % P;
+    const int t = (threadIdx.x / P) & (TL - 1);
+    const int grp = threadIdx.x / (P * TL);
     const int line = blockIdx.x * TL + t;
     const bool valid = line < g.lines_z;
-    const T *src = in + (long long)blockIdx.y * g.sites + (long long)line * N;
-    C v[16];
+    const size_t slot_elems = (size_t)TL * LS;
+    const T inv_n3 = (T)(1.0 / (double)g.sites);
+    // 1. c2r along z of field grp
+    {
+        const C *src = TA + (long long)grp * g.modes + (long long)line * H;
+        const ZIdx<L> ix{(int)(grp * slot_elems + t * LS)};
+        if (valid) {
 #pragma unroll
-    for (int r = 0; r < 16; ++r) {
-        const int m = j + r * P;
-        v[r] = valid ? mk<T>(src[2 * m], src[2 * m + 1]) : mk<T>(0, 0);
+            for (int r = 0; r < 16; ++r) slots[ix(j + r * P)] = src[j + r * P];
+            if (j == 0) slots[ix(M)] = src[M];
+        }
+        __syncthreads();
+        C v[16];
+#pragma unroll
+        for (int r = 0; r < 16; ++r) {
+            const int k = j + r * P;
+            C x = mk<T>(0, 0), y = mk<T>(0, 0);
+            if (valid) {
+                x = slots[ix(k)];
+                y = slots[ix(M - k)];
+            }
+            y.y = -y.y;
+            if (k == 0) { x.y = T(0); y.y = T(0); }
+            const C s = cadd(x, y), d = csub(x, y);
+            C w = __ldg(&tw[k]);
+            w.y = -w.y;
+            const C td = cmul(w, d);
+            v[r] = mk<T>(s.x - td.y, s.y + td.x);
+        }
+        __syncthreads();
+        fft_reg<C, L, +1>(v, slots, ix, j, tw, N / L);
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+            for (int r = 0; r < RP::RL; ++r) slots[ix(RP::out(j, q, r))] = cscale(v[q * RP::RL + r], inv_n3);
     }
-    const ZIdx<L> ix{t * LS};
-    fft_reg<C, L, -1>(v, sm, ix, j, tw, N / L);
     __syncthreads();
+    // 2. pointwise: Hessian and V' of the taped fields
+    const T eta2 = (T)ad->eta2, gam = (T)ad->gamma, gsq = (T)g.gsq;
+    const bool two = g.model == PSC_MODEL_PHI2CHI2;
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (int idx = threadIdx.x; idx < TL * M; idx += blockDim.x) {
+        const int tt = idx / M, m = idx - tt * M;
+        const long long ln = (long long)blockIdx.x * TL + tt;
+        if (ln >= g.lines_z) continue;
+        const int e = tt * LS + m + (m >> 4);
+        const C l0 = slots[e];
+        const C f0 = reinterpret_cast<const C *>(fx + ln * N)[m];
+        if (two) {
+            const C l1 = slots[slot_elems + e];
+            const C f1 = reinterpret_cast<const C *>(fx + g.sites + ln * N)[m];
+            C o0, o1;
 #pragma unroll
-    for (int q = 0; q < RP::NBL; ++q)
-#pragma unroll
-        for (int r = 0; r < RP::RL; ++r) sm[ix(RP::out(j, q, r))] = v[q * RP::RL + r];
+            for (int half = 0; half < 2; ++half) {
+                const T p = half ? f0.y : f0.x, c = half ? f1.y : f1.x;
+                const T a0 = half ? l0.y : l0.x, a1 = half ? l1.y : l1.x;
+                const T vp0 = p + gsq * p * (c * c), vp1 = gsq * (p * p) * c;
+                const T h00 = T(1) + gsq * (c * c), h01 = T(2) * gsq * p * c, h11 = gsq * (p * p);
+                const T r0 = eta2 * (h00 * a0 + h01 * a1) + gam * vp0;
+                const T r1 = eta2 * (h01 * a0 + h11 * a1) + gam * vp1;
+                if (half) { o0.y = r0; o1.y = r1; } else { o0.x = r0; o1.x = r1; }
+                acc[0] += (double)a0 * vp0 + (double)a1 * vp1;
+                acc[1] += (double)a0 * p * ((double)c * c) + (double)a1 * ((double)p * p) * c;
+                acc[2] += (double)a0 * p;
+            }
+            slots[e] = o0;
+            slots[slot_elems + e] = o1;
+        } else {
+            C o0;
+            o0.x = eta2 * l0.x + gam * f0.x;
+            o0.y = eta2 * l0.y + gam * f0.y;
+            const double d = (double)l0.x * f0.x + (double)l0.y * f0.y;
+            acc[0] += d;
+            acc[2] += d;
+            slots[e] = o0;
+        }
+    }
+    block_reduce_store<3>(acc, part, gridDim.x, blockIdx.x);
     __syncthreads();
-    if (valid) {
-        C *dst = out + (long long)blockIdx.y * g.modes + (long long)line * H;
+    // 3. r2c along z of field grp
+    {
+        const ZIdx<L> ix{(int)(grp * slot_elems + t * LS)};
+        C v[16];
 #pragma unroll
-        for (int r = 0; r <= 16; ++r) {
-            const int k = (r < 16) ? j + r * P : M;
-            if (r == 16 && j != 0) break;
-            const C zk = sm[ix(k == M ? 0 : k)];
-            const C zc = cconj(sm[ix(k == 0 ? 0 : M - k)]);
-            const C ev = cscale(cadd(zk, zc), T(0.5));
-            const C dd = cscale(csub(zk, zc), T(0.5));
-            const C od = mk<T>(dd.y, -dd.x);
-            C w;
-            if (k < M) w = __ldg(&tw[k]); else w = mk<T>(T(-1), T(0));
-            dst[k] = cadd(ev, cmul(w, od));
+        for (int r = 0; r < 16; ++r) v[r] = slots[ix(j + r * P)];
+        __syncthreads();
+        fft_reg<C, L, -1>(v, slots, ix, j, tw, N / L);
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+            for (int r = 0; r < RP::RL; ++r) slots[ix(RP::out(j, q, r))] = v[q * RP::RL + r];
+        __syncthreads();
+        if (valid) {
+            C *dst = QV + (long long)grp * g.modes + (long long)line * H;
+#pragma unroll
+            for (int r = 0; r <= 16; ++r) {
+                const int k = (r < 16) ? j + r * P : M;
+                if (r == 16 && j != 0) break;
+                const C zk = slots[ix(k == M ? 0 : k)];
+                const C zc = cconj(slots[ix(k == 0 ? 0 : M - k)]);
+                const C ev = cscale(cadd(zk, zc), T(0.5));
+                const C dd = cscale(csub(zk, zc), T(0.5));
+                const C od = mk<T>(dd.y, -dd.x);
+                C w;
+                if (k < M) w = __ldg(&tw[k]); else w = mk<T>(T(-1), T(0));
+                dst[k] = cadd(ev, cmul(w, od));
+            }
         }
     }
 }
 
-// Forward transform along x in place (blockIdx.y selects the array of the list).
+// X forward transform of the adjoint's J^T application with its epilogue:
+// Lf += fft_x(QV) + eta1 k^2 M + delta k^2 f  (blockIdx.y = field).
 template <typename T, int L>
-__global__ void __launch_bounds__(256, 2) kr_fft_x_plain(Geo g, ArrList8 arrs, const cplx<T> *__restrict__ tw) {
+__global__ void __launch_bounds__(256, 2) kr_fft_x_adj(Geo g, const cplx<T> *__restrict__ QV,
+                                                    const cplx<T> *__restrict__ Mk, const cplx<T> *__restrict__ fk,
+                                                    cplx<T> *__restrict__ Lf, const DevAdj *__restrict__ ad,
+                                                    const cplx<T> *__restrict__ tw) {
     using C = cplx<T>;
     using RP = RegPlan<L>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *sm = reinterpret_cast<C *>(smem_raw);
-    C *a = reinterpret_cast<C *>(arrs.p[blockIdx.y]);
-    const int sh = g.tlx_shift, TL = 1 << sh;
+    const int sh = g.tlx_shift, TL = 1 << sh, N = g.N, H = g.H;
     const int t = threadIdx.x & (TL - 1), j = threadIdx.x >> sh;
     const int line = blockIdx.x * TL + t;
     const bool valid = line < g.lines_x;
     const long long stride = g.lines_x;
+    const long long base = (long long)blockIdx.y * g.modes + line;
     auto ix = [&](int n) { return n * TL + t; };
     C v[16];
 #pragma unroll
-    for (int r = 0; r < 16; ++r) v[r] = valid ? a[(long long)(j + r * RP::P) * stride + line] : mk<T>(0, 0);
-    fft_reg<C, L, -1>(v, sm, ix, j, tw, g.N / L);
-    if (valid) {
+    for (int r = 0; r < 16; ++r) v[r] = valid ? QV[base + (long long)(j + r * RP::P) * stride] : mk<T>(0, 0);
+    fft_reg<C, L, -1>(v, sm, ix, j, tw, N / L);
+    if (!valid) return;
+    const T eta1 = (T)ad->eta1, delta = (T)ad->delta;
+    const int y = line / H, kz = line - y * H;
+    const int py = pcoord(y, N);
 #pragma unroll
-        for (int q = 0; q < RP::NBL; ++q)
+    for (int q = 0; q < RP::NBL; ++q)
 #pragma unroll
-            for (int r = 0; r < RP::RL; ++r) a[(long long)RP::out(j, q, r) * stride + line] = v[q * RP::RL + r];
-    }
+        for (int r = 0; r < RP::RL; ++r) {
+            const int n = RP::out(j, q, r);
+            const int px = pcoord(n, N);
+            const T k2 = (T)(px * px + py * py + kz * kz);
+            const long long a = base + (long long)n * stride;
+            const C mv = Mk[a], fv = fk[a], y0 = v[q * RP::RL + r];
+            C l = Lf[a];
+            l.x += y0.x + k2 * (eta1 * mv.x + delta * fv.x);
+            l.y += y0.y + k2 * (eta1 * mv.y + delta * fv.y);
+            Lf[a] = l;
+        }
 }
 
 }  // namespace psc

@@ -34,8 +34,8 @@ struct RegLaunch {
         SETA((kr_zpass<T, M, false>), sz);
         SETA((kr_zpass<T, M, true>), sz);
         SETA((kr_z_c2r_real<T, M>), (int)((256 / (M / 16)) * ZIdx<M>::LS * sizeof(C)));
-        SETA((kr_z_r2c_real<T, M>), (int)((256 / (M / 16)) * ZIdx<M>::LS * sizeof(C)));
-        SETA((kr_fft_x_plain<T, N>), sxy);
+        SETA((kr_zpass_adj<T, M>), sz);
+        SETA((kr_fft_x_adj<T, N>), sxy);
 #undef SETA
         return cudaSuccess;
     }
@@ -66,7 +66,8 @@ struct RegLaunch {
             mark(1);
             kr_ifft_y<T, N, false><<<gx, txy, cfg.smem_xy, st>>>(g, TA, TB, TC, b.bg, tw);
             mark(2);
-            kr_zpass<T, M, false><<<dim3(cfg.nbz, 1, R), tz, cfg.smem_z, st>>>(g, TA, TB, TC, QV, QS, b.partV, b.bg, tw);
+            kr_zpass<T, M, false><<<dim3(cfg.nbz, 1, R), tz, cfg.smem_z, st>>>(g, TA, TB, TC, QV, QS, b.partV, b.bg, tw,
+                                                                             (T *)b.tape_fx);
         }
         mark(3);
         ArrList8 al{};
@@ -86,7 +87,8 @@ struct RegLaunch {
         if (g.gw)
             kr_fft_x_final<T, N, true><<<gf, txy, cfg.smem_xf, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw);
         else
-            kr_fft_x_final<T, N, false><<<gf, txy, cfg.smem_xf, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw);
+            kr_fft_x_final<T, N, false><<<gf, txy, cfg.smem_xf, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw,
+                                                                       (C *)b.tape_f, (C *)b.tape_p, (C *)b.tape_vp);
         mark(5);
         if (scalar_mode >= 0) {
             cudaError_t e = launch_scalar(cfg, b, scalar_mode, 1, st);
@@ -118,55 +120,24 @@ struct RegLaunch {
         }
         return cudaGetLastError();
     }
-};
 
-template <typename T, int N>
-struct RegTransforms {
-    using C = cplx<T>;
-    static constexpr int M = N / 2;
-    // complex [n][modes] -> real [n][sites] (c2r with 1/N^3); TA (nf arrays) is scratch
-    static cudaError_t c2r(const LaunchCfg &cfg, const Buffers &b, const void *src, int n, void *dst,
-                           cudaStream_t st_) {
+    // J^T application of the adjoint at a stage point (no GW, one lattice): c2r of
+    // Mk (X, Y inverse passes into TA), the fused Z pass with the taped real fields,
+    // the Y forward pass and the X forward pass adding into Lf.
+    static cudaError_t adj_point(const LaunchCfg &cfg, const Buffers &b, const void *Mk, const void *f_tape,
+                                 const void *fx_tape, void *Lf, double *part, const DevAdj *ad, cudaStream_t st) {
         const Geo &g = cfg.g;
         const C *tw = reinterpret_cast<const C *>(b.tw);
-        C *TA = (C *)b.TA;
-        constexpr int P = M / 16;
-        const int tl = 256 / P;
-        int sh = 0;
-        while ((1 << sh) < tl) ++sh;
-        const size_t smem = (size_t)tl * ZIdx<M>::LS * sizeof(C);
-        const int nbz = (g.lines_z + tl - 1) / tl;
-        for (int s0 = 0; s0 < n; s0 += g.nf) {
-            const int cnt = (n - s0) < g.nf ? (n - s0) : g.nf;
-            const C *s = (const C *)src + (long long)s0 * g.modes;
-            kr_ifft_x<T, N, false, false><<<dim3(cfg.nbx, cnt), cfg.thr_xy, cfg.smem_xy, st_>>>(
-                g, (C *)s, nullptr, TA, nullptr, b.bg, tw);
-            kr_ifft_y<T, N, false><<<dim3(cfg.nbx, cnt), cfg.thr_xy, cfg.smem_xy, st_>>>(g, TA, nullptr, nullptr, b.bg,
-                                                                                       tw);
-            kr_z_c2r_real<T, M><<<dim3(nbz, cnt), tl * P, smem, st_>>>(g, TA, (T *)dst + (long long)s0 * g.sites, tw,
-                                                                      (T)(1.0 / (double)g.sites), sh);
-        }
-        return cudaGetLastError();
-    }
-    // real [n][sites] -> complex [n][modes] (unnormalised r2c), n <= 8
-    static cudaError_t r2c(const LaunchCfg &cfg, const Buffers &b, const void *src, int n, void *dst,
-                           cudaStream_t st_) {
-        const Geo &g = cfg.g;
-        const C *tw = reinterpret_cast<const C *>(b.tw);
-        constexpr int P = M / 16;
-        const int tl = 256 / P;
-        int sh = 0;
-        while ((1 << sh) < tl) ++sh;
-        const size_t smem = (size_t)tl * ZIdx<M>::LS * sizeof(C);
-        const int nbz = (g.lines_z + tl - 1) / tl;
-        kr_z_r2c_real<T, M><<<dim3(nbz, n), tl * P, smem, st_>>>(g, (const T *)src, (C *)dst, tw, sh);
+        C *TA = (C *)b.TA, *QV = (C *)b.QV;
+        const dim3 gx(cfg.nbx, g.nf);
+        kr_ifft_x<T, N, false, false><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, (C *)Mk, nullptr, TA, nullptr, b.bg, tw);
+        kr_ifft_y<T, N, false><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, TA, nullptr, nullptr, b.bg, tw);
+        kr_zpass_adj<T, M><<<cfg.nbz, cfg.thr_z, cfg.smem_z, st>>>(g, TA, (const T *)fx_tape, QV, part, ad, tw);
         ArrList8 al{};
-        for (int i = 0; i < n; ++i) {
-            al.p[i] = (C *)dst + (long long)i * g.modes;
-            al.rs[i] = 0;
-        }
-        kr_fft_y<T, N><<<dim3(cfg.nbx, n), cfg.thr_xy, cfg.smem_xy, st_>>>(g, al, tw);
-        kr_fft_x_plain<T, N><<<dim3(cfg.nbx, n), cfg.thr_xy, cfg.smem_xy, st_>>>(g, al, tw);
+        for (int f = 0; f < g.nf; ++f) al.p[f] = QV + (long long)f * g.modes;
+        kr_fft_y<T, N><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, al, tw);
+        kr_fft_x_adj<T, N><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, QV, (const C *)Mk, (const C *)f_tape, (C *)Lf, ad,
+                                                                 tw);
         return cudaGetLastError();
     }
 };
@@ -189,35 +160,14 @@ struct RegDispatch {
 
 }  // namespace psc
 
-#define PSC_REG_TRANSFORM_CASE(T, NN, WHAT, ...)                                                                \
-    case NN:                                                                                                     \
-        return RegTransforms<T, NN>::WHAT(__VA_ARGS__);
-
 #define PSC_DEFINE_REG_ENTRY(T, SUFFIX)                                                                          \
     namespace psc {                                                                                              \
-    cudaError_t reg_c2r_##SUFFIX(const LaunchCfg &cfg, const Buffers &b, const void *src, int n, void *dst,      \
-                                 cudaStream_t st) {                                                              \
-        switch (cfg.g.N) {                                                                                       \
-            PSC_REG_TRANSFORM_CASE(T, 32, c2r, cfg, b, src, n, dst, st)                                              \
-            PSC_REG_TRANSFORM_CASE(T, 64, c2r, cfg, b, src, n, dst, st)                                              \
-            PSC_REG_TRANSFORM_CASE(T, 128, c2r, cfg, b, src, n, dst, st)                                             \
-            PSC_REG_TRANSFORM_CASE(T, 256, c2r, cfg, b, src, n, dst, st)                                             \
-            PSC_REG_TRANSFORM_CASE(T, 512, c2r, cfg, b, src, n, dst, st)                                             \
-            PSC_REG_TRANSFORM_CASE(T, 1024, c2r, cfg, b, src, n, dst, st)                                            \
-        default: return cudaErrorInvalidValue;                                                                   \
-        }                                                                                                        \
-    }                                                                                                            \
-    cudaError_t reg_r2c_##SUFFIX(const LaunchCfg &cfg, const Buffers &b, const void *src, int n, void *dst,      \
-                                 cudaStream_t st) {                                                              \
-        switch (cfg.g.N) {                                                                                       \
-            PSC_REG_TRANSFORM_CASE(T, 32, r2c, cfg, b, src, n, dst, st)                                              \
-            PSC_REG_TRANSFORM_CASE(T, 64, r2c, cfg, b, src, n, dst, st)                                              \
-            PSC_REG_TRANSFORM_CASE(T, 128, r2c, cfg, b, src, n, dst, st)                                             \
-            PSC_REG_TRANSFORM_CASE(T, 256, r2c, cfg, b, src, n, dst, st)                                             \
-            PSC_REG_TRANSFORM_CASE(T, 512, r2c, cfg, b, src, n, dst, st)                                             \
-            PSC_REG_TRANSFORM_CASE(T, 1024, r2c, cfg, b, src, n, dst, st)                                            \
-        default: return cudaErrorInvalidValue;                                                                   \
-        }                                                                                                        \
+    cudaError_t reg_adj_point_##SUFFIX(const LaunchCfg &cfg, const Buffers &b, const void *Mk, const void *f_tape, \
+                                       const void *fx_tape, void *Lf, double *part, const DevAdj *ad,             \
+                                       cudaStream_t st) {                                                         \
+        return RegDispatch<T>::on(cfg.g.N, [&](auto L) {                                                         \
+            return decltype(L)::adj_point(cfg, b, Mk, f_tape, fx_tape, Lf, part, ad, st);                        \
+        });                                                                                                      \
     }                                                                                                            \
     cudaError_t reg_configure_##SUFFIX(const LaunchCfg &cfg) {                                                   \
         return RegDispatch<T>::on(cfg.g.N, [&](auto L) { return decltype(L)::configure(cfg); });                 \
