@@ -217,7 +217,9 @@ int psc_spectra_noalloc(const psc_params *p, double a, double ad, const void *f_
  *                        dO/dRe + i dO/dIm of each stored half-spectrum mode;
  *   grad_ad0             dO/da'(0) at fixed a(0);
  *   grad_theta[2]        dO/d(gsq) and dO/d(mu), mu the coefficient of phi^2/2 in V (mu = 1).
- * On return the handle holds the final state, as after psc_step(h, dt, nsteps). */
+ * On return the handle holds the final state, as after psc_step(h, dt, nsteps), and
+ * psc_last_step_ms reports the device time of the whole computation (evaluation,
+ * forward passes and reverse sweep; not the download of the gradients). */
 int psc_adjoint_chi2(psc_handle *h, double dt, int nsteps, int every, double *O, double *grad_f_k,
                      double *grad_pi_k, double *grad_ad0, double *grad_theta);
 /* The adjoint's own forward map alone (same stage arithmetic, unfused): O after nsteps. */

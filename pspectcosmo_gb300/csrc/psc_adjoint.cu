@@ -57,74 +57,102 @@ namespace {
 constexpr int kEW = 4 * 152;   // blocks of the elementwise kernels (grid-stride)
 constexpr int kThreads = 256;
 
-__device__ __forceinline__ double wk_of(long long m, int H) {
-    const int kz = (int)(m % H);
-    return (kz == 0 || kz == H - 1) ? 1.0 : 2.0;
-}
+// The elementwise kernels walk the half spectrum one row (fixed field, x, y; kz
+// fastest, H entries) per warp: no integer division per element, coalesced rows.
+// Per-lane partial sums of a row are in the field precision, FP64 across rows.
+struct RowIdx {
+    int N, H, lg;   // lg = log2(N)
+    __device__ __forceinline__ int kxy2(int r) const {
+        const int xy = r & ((N * N) - 1);
+        const int x = xy >> lg, y = xy & (N - 1);
+        const int px = psc::pcoord(x, N), py = psc::pcoord(y, N);
+        return px * px + py * py;
+    }
+};
 
-__device__ __forceinline__ double k2_of(long long m, int N, int H) {
-    const int kz = (int)(m % H);
-    const long long xy = m / H;
-    const int y = (int)(xy % N), x = (int)(xy / N);
-    const int px = psc::pcoord(x, N), py = psc::pcoord(y, N);
-    return (double)(px * px + py * py + kz * kz);
+__device__ __forceinline__ void warp_rows(int *r0, int *rstep, int *lane) {
+    *lane = threadIdx.x & 31;
+    *r0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    *rstep = (gridDim.x * blockDim.x) >> 5;
 }
 
 // point: M = alpha1 Lp + alpha2 p;  Lp += beta p;  part += sum' w k^2 Re(conj M f)
 template <typename T>
-__global__ void __launch_bounds__(kThreads) ka_point(long long n, long long modes, int N, int H,
-                                                     psc::cplx<T> *__restrict__ Lp, const psc::cplx<T> *__restrict__ p,
+__global__ void __launch_bounds__(kThreads) ka_point(int rows, RowIdx ri, psc::cplx<T> *__restrict__ Lp,
+                                                     const psc::cplx<T> *__restrict__ p,
                                                      const psc::cplx<T> *__restrict__ f, psc::cplx<T> *__restrict__ Mk,
                                                      const psc::DevAdj *__restrict__ ad, double *__restrict__ part) {
     const T a1 = (T)ad->alpha1, a2 = (T)ad->alpha2, be = (T)ad->beta;
+    int r, rs, lane;
+    warp_rows(&r, &rs, &lane);
     double acc[1] = {0.0};
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const long long m = i % modes;
-        const psc::cplx<T> l = Lp[i], q = p[i], fv = f[i];
-        const psc::cplx<T> mv = psc::mk<T>(a1 * l.x + a2 * q.x, a1 * l.y + a2 * q.y);
-        Mk[i] = mv;
-        Lp[i] = psc::mk<T>(l.x + be * q.x, l.y + be * q.y);
-        acc[0] += wk_of(m, H) * k2_of(m, N, H) * ((double)mv.x * fv.x + (double)mv.y * fv.y);
+    for (; r < rows; r += rs) {
+        const int kxy = ri.kxy2(r);
+        T racc = T(0);
+        for (int kz = lane; kz < ri.H; kz += 32) {
+            const long long i = (long long)r * ri.H + kz;
+            const psc::cplx<T> l = Lp[i], q = p[i], fv = f[i];
+            const psc::cplx<T> mv = psc::mk<T>(a1 * l.x + a2 * q.x, a1 * l.y + a2 * q.y);
+            Mk[i] = mv;
+            Lp[i] = psc::mk<T>(l.x + be * q.x, l.y + be * q.y);
+            const T w = (kz == 0 || kz == ri.H - 1) ? T(1) : T(2);
+            racc += w * (T)(kxy + kz * kz) * (mv.x * fv.x + mv.y * fv.y);
+        }
+        acc[0] += (double)racc;
     }
     psc::block_reduce_store<1>(acc, part, gridDim.x, blockIdx.x);
 }
 
 // stage: ph = p + kc (-kn1 k^2 f - kn2 Vp);  part += sum' w Re(conj Lf ph);  Lp += c2 Lf
 template <typename T>
-__global__ void __launch_bounds__(kThreads) ka_stage(long long n, long long modes, int N, int H,
-                                                     const psc::cplx<T> *__restrict__ Lf, psc::cplx<T> *__restrict__ Lp,
-                                                     const psc::cplx<T> *__restrict__ p,
+__global__ void __launch_bounds__(kThreads) ka_stage(int rows, RowIdx ri, const psc::cplx<T> *__restrict__ Lf,
+                                                     psc::cplx<T> *__restrict__ Lp, const psc::cplx<T> *__restrict__ p,
                                                      const psc::cplx<T> *__restrict__ f,
                                                      const psc::cplx<T> *__restrict__ vp,
                                                      const psc::DevAdj *__restrict__ ad, double *__restrict__ part) {
     const T kc = (T)ad->kc, kn1 = (T)ad->kn1, kn2 = (T)ad->kn2, c2 = (T)ad->c2;
+    int r, rs, lane;
+    warp_rows(&r, &rs, &lane);
     double acc[1] = {0.0};
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const long long m = i % modes;
-        const T k2 = (T)k2_of(m, N, H);
-        const psc::cplx<T> l = Lf[i], q = p[i], fv = f[i], v = vp[i];
-        const T fl = -kn1 * k2;
-        const psc::cplx<T> ph = psc::mk<T>(q.x + kc * (fl * fv.x - kn2 * v.x), q.y + kc * (fl * fv.y - kn2 * v.y));
-        acc[0] += wk_of(m, H) * ((double)l.x * ph.x + (double)l.y * ph.y);
-        psc::cplx<T> lp = Lp[i];
-        lp.x += c2 * l.x;
-        lp.y += c2 * l.y;
-        Lp[i] = lp;
+    for (; r < rows; r += rs) {
+        const int kxy = ri.kxy2(r);
+        T racc = T(0);
+        for (int kz = lane; kz < ri.H; kz += 32) {
+            const long long i = (long long)r * ri.H + kz;
+            const psc::cplx<T> l = Lf[i], q = p[i], fv = f[i], v = vp[i];
+            const T fl = -kn1 * (T)(kxy + kz * kz);
+            const psc::cplx<T> ph =
+                psc::mk<T>(q.x + kc * (fl * fv.x - kn2 * v.x), q.y + kc * (fl * fv.y - kn2 * v.y));
+            const T w = (kz == 0 || kz == ri.H - 1) ? T(1) : T(2);
+            racc += w * (l.x * ph.x + l.y * ph.y);
+            psc::cplx<T> lp = Lp[i];
+            lp.x += c2 * l.x;
+            lp.y += c2 * l.y;
+            Lp[i] = lp;
+        }
+        acc[0] += (double)racc;
     }
     psc::block_reduce_store<1>(acc, part, gridDim.x, blockIdx.x);
 }
 
 // observable: part += sum' w |chi_k|^2 and, when Lf is given, Lf = 2 chi_k / N^3
 template <typename T>
-__global__ void __launch_bounds__(kThreads) ka_observable(long long modes, int H, const psc::cplx<T> *__restrict__ chi,
+__global__ void __launch_bounds__(kThreads) ka_observable(int rows, RowIdx ri, const psc::cplx<T> *__restrict__ chi,
                                                           psc::cplx<T> *__restrict__ Lf, double scale,
                                                           double *__restrict__ part) {
+    int r, rs, lane;
+    warp_rows(&r, &rs, &lane);
     double acc[1] = {0.0};
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < modes;
-         i += (long long)gridDim.x * blockDim.x) {
-        const psc::cplx<T> c = chi[i];
-        acc[0] += wk_of(i, H) * ((double)c.x * c.x + (double)c.y * c.y);
-        if (Lf) Lf[i] = psc::mk<T>((T)(scale * c.x), (T)(scale * c.y));
+    for (; r < rows; r += rs) {
+        double racc = 0.0;
+        for (int kz = lane; kz < ri.H; kz += 32) {
+            const long long i = (long long)r * ri.H + kz;
+            const psc::cplx<T> c = chi[i];
+            const double w = (kz == 0 || kz == ri.H - 1) ? 1.0 : 2.0;
+            racc += w * ((double)c.x * c.x + (double)c.y * c.y);
+            if (Lf) Lf[i] = psc::mk<T>((T)(scale * c.x), (T)(scale * c.y));
+        }
+        acc[0] += racc;
     }
     psc::block_reduce_store<1>(acc, part, gridDim.x, blockIdx.x);
 }
@@ -315,6 +343,7 @@ struct Run {
     long long modes, n;   // n = nf * modes
     double n3;
     int z_n;
+    RowIdx ri;
 };
 
 int setup(psc_handle *h, Run *r) {
@@ -351,6 +380,9 @@ int setup(psc_handle *h, Run *r) {
     r->n = (long long)g.nf * g.modes;
     r->n3 = (double)g.sites;
     r->z_n = ws->z_n;
+    int lg = 0;
+    while ((1 << lg) < g.N) ++lg;
+    r->ri = RowIdx{g.N, g.H, lg};
     return PSC_OK;
 }
 
@@ -389,11 +421,12 @@ int observable(const Run &r, void *Lf_last) {
     const size_t one = (size_t)r.modes * r.h->csize;
     const void *chi = static_cast<const char *>(r.h->b.fk) + (size_t)(r.nf - 1) * one;
     double *part = r.ws->part + 2 * kEW + 3 * r.z_n;
+    const int rows = r.N * r.N;
     if (r.prec == 32)
-        ka_observable<float><<<kEW, kThreads, 0, r.st>>>(r.modes, r.H, (const float2 *)chi, (float2 *)Lf_last,
-                                                         2.0 / r.n3, part);
+        ka_observable<float><<<kEW, kThreads, 0, r.st>>>(rows, r.ri, (const float2 *)chi, (float2 *)Lf_last, 2.0 / r.n3,
+                                                         part);
     else
-        ka_observable<double><<<kEW, kThreads, 0, r.st>>>(r.modes, r.H, (const double2 *)chi, (double2 *)Lf_last,
+        ka_observable<double><<<kEW, kThreads, 0, r.st>>>(rows, r.ri, (const double2 *)chi, (double2 *)Lf_last,
                                                           2.0 / r.n3, part);
     CU(cudaGetLastError());
     return scalar(r, ADJ_INIT, 0, 0);
@@ -438,19 +471,20 @@ int reverse_segment_t(const Run &r, long long jbase, int npts) {
     AdjWS *ws = r.ws;
     psc_handle *h = r.h;
     double *p_d1 = ws->part, *p_z = ws->part + kEW, *p_d3 = ws->part + kEW + 3 * r.z_n;
+    const int rows = r.nf * r.N * r.N;
     int rc;
     for (int i = npts - 1; i >= 0; --i) {
         const long long j = jbase + i;
         // the internals of stage j (its drift and a-updates)
         if ((rc = scalar(r, ADJ_STAGE_PRE, i, j))) return rc;
-        ka_stage<T><<<kEW, kThreads, 0, r.st>>>(r.n, r.modes, r.N, r.H, (const C *)ws->Lf, (C *)ws->Lp,
+        ka_stage<T><<<kEW, kThreads, 0, r.st>>>(rows, r.ri, (const C *)ws->Lf, (C *)ws->Lp,
                                                 (const C *)tp_p(r, i), (const C *)tp_f(r, i), (const C *)tp_vp(r, i),
                                                 ws->rec, p_d3);
         CU(cudaGetLastError());
         if ((rc = scalar(r, ADJ_STAGE_POST, i, j))) return rc;
         // point j: merged J^T of the kicks at P_j and the a''(P_j) terms
         if ((rc = scalar(r, ADJ_PRE, i, j))) return rc;
-        ka_point<T><<<kEW, kThreads, 0, r.st>>>(r.n, r.modes, r.N, r.H, (C *)ws->Lp, (const C *)tp_p(r, i),
+        ka_point<T><<<kEW, kThreads, 0, r.st>>>(rows, r.ri, (C *)ws->Lp, (const C *)tp_p(r, i),
                                                 (const C *)tp_f(r, i), (C *)ws->M, ws->rec, p_d1);
         CU(cudaGetLastError());
         CU(r.prec == 32 ? psc::reg_adj_point_f32(h->cfg, h->b, ws->M, tp_f(r, i), tp_fx(r, i), ws->Lf, p_z, ws->rec,
@@ -505,6 +539,7 @@ extern "C" int psc_adjoint_chi2(psc_handle *h, double dt, int nsteps, int every,
     if ((rc = ws_grow(ws, &ws->tape, &ws->tape_n, npts_max, ws->tape_stride))) return rc;
     if ((rc = grow_snap(ws, npts_max + 2))) return rc;
     if (nseg > 1 && (rc = ws_grow(ws, &ws->ckpt, &ws->ckpt_n, nseg + 1, ws->ckpt_stride))) return rc;
+    CU(cudaEventRecord(h->ev0, r.st));
     // a''(0) = A(state(0)) and the reductions at the first point
     if ((rc = psc::hapi::evaluate(h, 0))) return rc;
     CU(cudaMemsetAsync(ws->Lf, 0, ws->carr, r.st));
@@ -527,9 +562,11 @@ extern "C" int psc_adjoint_chi2(psc_handle *h, double dt, int nsteps, int every,
         if (nseg == 1 && (rc = observable(r, Lf_last))) return rc;
         if ((rc = reverse_segment(r, (long long)seg * every * s, n * s))) return rc;
     }
+    CU(cudaEventRecord(h->ev1, r.st));
     psc::DevAdj rec;
     CU(cudaMemcpyAsync(&rec, ws->rec, sizeof(rec), cudaMemcpyDeviceToHost, r.st));
     CU(cudaStreamSynchronize(r.st));
+    CU(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
     if (!std::isfinite(rec.O) || !std::isfinite(rec.lb) || !std::isfinite(rec.gth[0]) || !std::isfinite(rec.gth[1]))
         return fail(PSC_ERR_NONFINITE, "non-finite observable or gradient");
     *O = rec.O;

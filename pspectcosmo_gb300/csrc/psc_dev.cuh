@@ -54,13 +54,16 @@ __device__ __forceinline__ void model_dvdf(const Model &m, const T *v, T *out, i
     }
 }
 
-template <typename T>
-__device__ __forceinline__ void model_potential(const Model &m, const T *v, double *terms) {
-    const double p = (double)v[0];
-    terms[0] += 0.5 * p * p;
+// Accumulates in A: the field precision for the per-thread partial sums of the
+// register engine (a thread adds a handful of sites before the FP64 block sum),
+// double in the generic engine.
+template <typename T, typename A = double>
+__device__ __forceinline__ void model_potential(const Model &m, const T *v, A *terms) {
+    const A p = (A)v[0];
+    terms[0] += A(0.5) * p * p;
     if (m.kind == 1) {
-        const double c = (double)v[1];
-        terms[1] += 0.5 * m.gsq * p * p * c * c;
+        const A c = (A)v[1];
+        terms[1] += A(0.5) * (A)m.gsq * p * p * c * c;
     }
 }
 

@@ -225,12 +225,12 @@ __global__ void __launch_bounds__(256, 2) kr_fft_x_final(Geo g, const cplx<T> *_
     const int y = line / H, kz = line - y * H;
     const int py = pcoord(y, N);
     if (field) {
-        double accK = 0.0, accG = 0.0;
+        T accK = T(0), accG = T(0);   // per-thread partials (16 modes), FP64 across threads
         if (valid) {
             const bool mask = g.mask != 0;
             const T hub = (T)bg->hub, apow = (T)bg->apow, a3 = (T)bg->a3;
             const T dfdp = (T)bg->DFDP, eps = (T)bg->eps;
-            const double wgt = (kz == 0 || kz == M) ? 1.0 : 2.0;
+            const T wgt = (kz == 0 || kz == M) ? T(1) : T(2);
 #pragma unroll
             for (int q = 0; q < RP::NBL; ++q)
 #pragma unroll
@@ -253,8 +253,8 @@ __global__ void __launch_bounds__(256, 2) kr_fft_x_final(Geo g, const cplx<T> *_
                         inc = R < eps;
                     }
                     if (inc) {
-                        accK += wgt * ((double)pf.x * pf.x + (double)pf.y * pf.y);
-                        accG += wgt * (double)k2 * ((double)f.x * f.x + (double)f.y * f.y);
+                        accK += wgt * (pf.x * pf.x + pf.y * pf.y);
+                        accG += wgt * k2 * (f.x * f.x + f.y * f.y);
                     }
                     pk[a] = mk<T>(pf.x + c_open * F.x, pf.y + c_open * F.y);
                     if (!GW && tape_p) {   // adjoint tape: the synchronised stage-point state
@@ -264,7 +264,7 @@ __global__ void __launch_bounds__(256, 2) kr_fft_x_final(Geo g, const cplx<T> *_
                     }
                 }
         }
-        double vals[2] = {accK, accG};
+        double vals[2] = {(double)accK, (double)accG};
         block_reduce_store<2>(vals, partKG + (size_t)(2 * job) * gridDim.x, gridDim.x, blockIdx.x);
     } else if (GW && valid) {
         const T c_drift = (T)bg->c_drift;
@@ -390,7 +390,7 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
     Model mdl;
     mdl.kind = g.model;
     mdl.gsq = g.gsq;
-    double pot[kMaxTerms] = {0.0, 0.0};
+    T pot_t[kMaxTerms] = {T(0), T(0)};
     for (int idx = threadIdx.x; idx < TL * M; idx += blockDim.x) {
         const int tt = idx / M, m = idx - tt * M;
         if (blockIdx.x * TL + tt >= g.lines_z) continue;
@@ -419,7 +419,7 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
                 }
             }
             model_dvdf<T>(mdl, f, vp, nf);
-            model_potential<T>(mdl, f, pot);
+            model_potential<T, T>(mdl, f, pot_t);
 #pragma unroll
             for (int fl = 0; fl < 2; ++fl)
                 if (fl < nf) { if (half) out[fl].y = vp[fl]; else out[fl].x = vp[fl]; }
@@ -445,6 +445,7 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
         for (int o = 0; o < 8; ++o)
             if (o < nout) slots[o * slot_elems + e] = out[o];
     }
+    double pot[kMaxTerms] = {(double)pot_t[0], (double)pot_t[1]};
     block_reduce_store<kMaxTerms>(pot, partV, gridDim.x, blockIdx.x);
     __syncthreads();
 
@@ -598,7 +599,7 @@ __global__ void __launch_bounds__(256, 2) kr_zpass_adj(Geo g, const cplx<T> *__r
     // 2. pointwise: Hessian and V' of the taped fields
     const T eta2 = (T)ad->eta2, gam = (T)ad->gamma, gsq = (T)g.gsq;
     const bool two = g.model == PSC_MODEL_PHI2CHI2;
-    double acc[3] = {0.0, 0.0, 0.0};
+    T acc_t[3] = {T(0), T(0), T(0)};   // per-thread partials, FP64 across threads
     for (int idx = threadIdx.x; idx < TL * M; idx += blockDim.x) {
         const int tt = idx / M, m = idx - tt * M;
         const long long ln = (long long)blockIdx.x * TL + tt;
@@ -619,9 +620,9 @@ __global__ void __launch_bounds__(256, 2) kr_zpass_adj(Geo g, const cplx<T> *__r
                 const T r0 = eta2 * (h00 * a0 + h01 * a1) + gam * vp0;
                 const T r1 = eta2 * (h01 * a0 + h11 * a1) + gam * vp1;
                 if (half) { o0.y = r0; o1.y = r1; } else { o0.x = r0; o1.x = r1; }
-                acc[0] += (double)a0 * vp0 + (double)a1 * vp1;
-                acc[1] += (double)a0 * p * ((double)c * c) + (double)a1 * ((double)p * p) * c;
-                acc[2] += (double)a0 * p;
+                acc_t[0] += a0 * vp0 + a1 * vp1;
+                acc_t[1] += a0 * p * (c * c) + a1 * (p * p) * c;
+                acc_t[2] += a0 * p;
             }
             slots[e] = o0;
             slots[slot_elems + e] = o1;
@@ -629,12 +630,13 @@ __global__ void __launch_bounds__(256, 2) kr_zpass_adj(Geo g, const cplx<T> *__r
             C o0;
             o0.x = eta2 * l0.x + gam * f0.x;
             o0.y = eta2 * l0.y + gam * f0.y;
-            const double d = (double)l0.x * f0.x + (double)l0.y * f0.y;
-            acc[0] += d;
-            acc[2] += d;
+            const T d = l0.x * f0.x + l0.y * f0.y;
+            acc_t[0] += d;
+            acc_t[2] += d;
             slots[e] = o0;
         }
     }
+    double acc[3] = {(double)acc_t[0], (double)acc_t[1], (double)acc_t[2]};
     block_reduce_store<3>(acc, part, gridDim.x, blockIdx.x);
     __syncthreads();
     // 3. r2c along z of field grp

@@ -211,17 +211,18 @@ class Lattice:
         return v.value
 
     # -- adjoint --------------------------------------------------------------
-    def adjoint_chi2(self, dt: float, nsteps: int, every: int = 0) -> dict:
+    def adjoint_chi2(self, dt: float, nsteps: int, every: int = 0, fields: bool = True) -> dict:
         """O = <chi^2> after nsteps and its gradient with respect to the current state.
 
         Returns O, grad_f_k / grad_pi_k (dO/dRe + i dO/dIm per stored mode, shaped like the
-        state), grad_ad0 (dO/da' at fixed a) and grad_theta = (dO/dgsq, dO/dmu). The lattice
-        is left at the final state.
+        state; None when fields is False), grad_ad0 (dO/da' at fixed a) and grad_theta =
+        (dO/dgsq, dO/dmu). The lattice is left at the final state; last_step_ms() gives the
+        device time of the computation.
         """
         p = self.p
         O, gad = ctypes.c_double(), ctypes.c_double()
-        gf = np.zeros((p.nflds, p.modes), np.complex128)
-        gp = np.zeros((p.nflds, p.modes), np.complex128)
+        gf = np.zeros((p.nflds, p.modes), np.complex128) if fields else None
+        gp = np.zeros((p.nflds, p.modes), np.complex128) if fields else None
         gth = np.zeros(2)
         _check(self._L.psc_adjoint_chi2(self._h, float(dt), int(nsteps), int(every), ctypes.byref(O), _dp(gf), _dp(gp),
                                         ctypes.byref(gad), _dp(gth)), "psc_adjoint_chi2")
