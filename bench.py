@@ -8,7 +8,8 @@ conditions (seed 1), generated on the host. Every array is larger than the 129 M
 (2 GB resident), so no flush is needed between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--config preheat_gw_256|preheat_256|inflation_64] [--precision 32|64]
+                  [--config preheat_gw_256|preheat_256|inflation_64|ensemble_mixed|adjoint_128]
+                  [--precision 32|64]
 
 One JSON line (rank 0). `value` is device-timed whole-job site-steps/s (inputs resident
 in HBM); `e2e` is the same metric through the C ABI with host buffers, the state copied
@@ -43,7 +44,13 @@ CONFIGS = {
     # phi0 ~ U[10, 12] (host RNG seed 12345), Yoshida-4, one graph per step for all of them
     "ensemble_mixed": (dict(kind="ensemble"), 1e-4,
                        "ensemble: 256 x 32^3 + 64 x 64^3 + 8 x 128^3 single-field inflation, Yoshida-4"),
+    # one timed step = one gradient of <chi^2> after ADJ_STEPS model steps (checkpoints every
+    # ADJ_EVERY steps, each segment recomputed once), FP32 fields / FP64 background
+    "adjoint_128": (dict(kind="preheating", N=128, spectral=0, with_gw=0, vv=2), 0.005,
+                    "adjoint of <chi^2> after 2000 steps: 128^3 two-field preheating, velocity Verlet, "
+                    "checkpoints every 100 steps"),
 }
+ADJ_STEPS, ADJ_EVERY = 2000, 100
 
 
 def ensemble_params(precision: int):
@@ -250,9 +257,80 @@ def run_ensemble(args):
         dist.destroy_process_group()
 
 
+def run_adjoint(args):
+    world, rank, local, dist = dist_setup()
+    from pspectcosmo_gb300 import Lattice, build
+
+    build.build()
+    p, dt, desc = make_params(args.config, args.precision)
+    lat = Lattice(p)
+    lat.initialize()
+    st0 = lat.get_state()
+
+    def reset():
+        lat.set_state(st0["f_k"], st0["pi_k"], st0["a"], st0["ad"], st0["add"])
+
+    # forward alone on the product's captured step, the same ADJ_STEPS steps
+    reset()
+    lat.evolve(dt, ADJ_STEPS)
+    reset()
+    lat.evolve(dt, ADJ_STEPS)
+    fwd_ms = lat.last_step_ms()
+    for _ in range(args.warmup):
+        reset()
+        lat.adjoint_chi2(dt, ADJ_STEPS, ADJ_EVERY, fields=False)
+    clocks = ClockSampler(local)
+    barrier(dist)
+    clocks.start()
+    barrier(dist)
+    dev_ms = 0.0
+    for _ in range(args.steps):
+        reset()
+        g = lat.adjoint_chi2(dt, ADJ_STEPS, ADJ_EVERY, fields=False)
+        dev_ms += lat.last_step_ms()
+    barrier(dist)
+    ms = max_over_ranks(dist, dev_ms)
+    clk = clocks.stop()
+    value = world * p.sites * ADJ_STEPS * args.steps / (ms / 1e3)
+    # end to end: host state in, every gradient array out
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        reset()
+        g = lat.adjoint_chi2(dt, ADJ_STEPS, ADJ_EVERY)
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+    state_bytes = 2 * p.nflds * p.modes * 16
+    if rank == 0:
+        line = {"metric": "site-steps/s", "value": value, "unit": "site-steps/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32" if p.precision == 32 else "f64",
+                "data": "synthetic (reference seeded initial conditions, seed 1)",
+                "config": {"workload": desc, "N": p.N, "nflds": p.nflds, "vv": p.vv, "dt": dt,
+                           "model_steps_per_gradient": ADJ_STEPS, "checkpoint_every": ADJ_EVERY,
+                           "precision": f"fp{p.precision} fields, fp64 background/reductions/adjoint scalars",
+                           "parallelism": f"replicas x{world}" if world > 1 else "single lattice",
+                           "l2": "arrays > 129 MB L2 (no flush needed)"},
+                "adjoint_over_forward": (ms / args.steps) / fwd_ms,
+                "forward_ms": fwd_ms,
+                "observable": g["O"], "grad_theta": list(map(float, g["grad_theta"])),
+                "e2e": {"value": world * p.sites * ADJ_STEPS * args.steps / e2e_s, "unit": "site-steps/s",
+                        "h2d_bytes_per_step": state_bytes + 24, "d2h_bytes_per_step": state_bytes + 32},
+                "roofline": None,
+                "cpu_baseline": None,
+                "clocks": clk,
+                "gpu_launches": int(ADJ_STEPS * p.stages * (2 * 6 + 11) + 16)}
+        print(json.dumps(line), flush=True)
+    lat.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
 def run_ours(args):
     if args.config == "ensemble_mixed":
         return run_ensemble(args)
+    if args.config == "adjoint_128":
+        return run_adjoint(args)
     world, rank, local, dist = dist_setup()
     from pspectcosmo_gb300 import Lattice, build
     from pspectcosmo_gb300.params import Params  # noqa: F401
