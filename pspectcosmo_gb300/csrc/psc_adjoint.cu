@@ -236,16 +236,16 @@ __global__ void __launch_bounds__(256) k_adj(AdjArgs A, psc::DevAdj *__restrict_
         const double lat = ad->ladd + cb * ad->lb;
         ad->lat = lat;
         ad->lbh = ad->lb;
-        const double Cc = C * pow(a, (double)(1 + 2 * al));
-        const double beta = lat * Cc * (al - 2) / (pow(a, 6.0) * n3);
+        const double Cc = C * psc::ipow(a, 1 + 2 * al);
+        const double beta = lat * Cc * (al - 2) / (psc::ipow(a, 6) * n3);
         ad->beta = beta;
         ad->alpha1 = c + cb;
         ad->alpha2 = cb * beta;
         ad->gamma = lat * Cc * (al + 1) / n3;
         ad->delta = lat * Cc * al * kIR2 / (a * a * n3);
-        ad->eta1 = -pow(a, (double)(1 + al)) * kIR2;
-        ad->eta2 = -pow(a, (double)(3 + al));
-        ad->la += lat * (C * (1 + 2 * al) * pow(a, (double)(2 * al)) * ((al - 2) * P.K + al * P.G + (al + 1) * P.V) +
+        ad->eta1 = -psc::ipow(a, 1 + al) * kIR2;
+        ad->eta2 = -psc::ipow(a, 3 + al);
+        ad->la += lat * (C * (1 + 2 * al) * psc::ipow(a, 2 * al) * ((al - 2) * P.K + al * P.G + (al + 1) * P.V) +
                          Cc * ((al - 2) * (-6 * P.K / a) + al * (-2 * P.G / a)));
         ad->gth[0] += lat * Cc * (al + 1) * P.dVg;
         ad->gth[1] += lat * Cc * (al + 1) * P.dVm;
@@ -253,8 +253,8 @@ __global__ void __launch_bounds__(256) k_adj(AdjArgs A, psc::DevAdj *__restrict_
     }
     if (A.mode == ADJ_POST) {
         const double d1 = s[0] / n3, d2 = s[1];
-        ad->la += (1 + al) * pow(a, (double)al) * (-kIR2) * d1 - (3 + al) * pow(a, (double)(2 + al)) * d2;
-        const double e2 = -pow(a, (double)(3 + al));
+        ad->la += (1 + al) * psc::ipow(a, al) * (-kIR2) * d1 - (3 + al) * psc::ipow(a, 2 + al) * d2;
+        const double e2 = -psc::ipow(a, 3 + al);
         ad->gth[0] += e2 * s[2];
         ad->gth[1] += e2 * s[3];
         return;
@@ -263,15 +263,15 @@ __global__ void __launch_bounds__(256) k_adj(AdjArgs A, psc::DevAdj *__restrict_
         ad->lbh += c * ad->la;
         ad->c2 = snap[A.i + 1].c_drift;
         ad->kc = c;
-        ad->kn1 = pow(a, (double)(1 + al)) * kIR2;
-        ad->kn2 = pow(a, (double)(3 + al));
+        ad->kn1 = psc::ipow(a, 1 + al) * kIR2;
+        ad->kn2 = psc::ipow(a, 3 + al);
         return;
     }
     // ADJ_STAGE_POST
     const double d3 = s[0] / n3;
     const double bh = snap[A.i + 1].b_half;
     const double ah = a + bh * g0.w[q] * dt / 2.;
-    ad->la += d3 * g0.w[q] * dt * (al - 3) * pow(ah, (double)(al - 4));
+    ad->la += d3 * g0.w[q] * dt * (al - 3) * psc::ipow(ah, al - 4);
     ad->lbh += c * ad->la;
     ad->lb = ad->lbh;
     ad->ladd = c * ad->lbh;

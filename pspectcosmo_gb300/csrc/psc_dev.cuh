@@ -235,4 +235,18 @@ __device__ __forceinline__ void block_reduce_store(double (&v)[NV], double *out,
 
 __device__ __forceinline__ int pcoord(int i, int N) { return i <= (N >> 1) ? i : i - N; }
 
+// x^n for a small integer n by repeated squaring: the scale-factor powers a^(1+alpha),
+// a^(3+alpha), a^(alpha-3), ... of the background update. A one-thread kernel runs
+// these on the FP64 pipe, where a general pow() costs microseconds.
+__device__ __forceinline__ double ipow(double x, int n) {
+    unsigned m = n < 0 ? (unsigned)(-n) : (unsigned)n;
+    double r = 1.0, b = x;
+    while (m) {
+        if (m & 1u) r *= b;
+        b *= b;
+        m >>= 1;
+    }
+    return n < 0 ? 1.0 / r : r;
+}
+
 }  // namespace psc

@@ -423,16 +423,16 @@ __device__ void begin_stage(DevBG *bg, int p) {
     // evolution.cpp:1141, 1161, 1165, 1180
     bg->b_half = bg->b + w * dt / 2. * bg->add;
     const double a_half = bg->a + bg->b_half * w * dt / 2.;
-    bg->c_drift = w * dt * pow(a_half, (double)(al - 3));
+    bg->c_drift = w * dt * ipow(a_half, al - 3);
     bg->a = a_half + bg->b_half * w * dt / 2.;
-    bg->norm1 = pow(bg->a, (double)(1 + al));
-    bg->norm2 = pow(bg->a, (double)(3 + al));
+    bg->norm1 = ipow(bg->a, 1 + al);
+    bg->norm2 = ipow(bg->a, 3 + al);
     bg->c_close = w * dt / 2;
     if (p + 1 < bg->s) bg->c_open = bg->w[p + 1] * dt / 2;
     else bg->c_open = (bg->steps_left > 1) ? bg->w[0] * dt / 2 : 0.0;
     bg->hub = bg->ad_stale / bg->a;
-    bg->apow = pow(bg->a, (double)(al - 3));
-    bg->a3 = pow(bg->a, (double)(3 - al));
+    bg->apow = ipow(bg->a, al - 3);
+    bg->a3 = ipow(bg->a, 3 - al);
     bg->stage = p;
 }
 
@@ -440,18 +440,18 @@ __device__ void eval_coeffs(DevBG *bg) {
     const int al = bg->alpha;
     bg->c_drift = 0.0;
     bg->c_close = 0.0;
-    bg->norm1 = pow(bg->a, (double)(1 + al));
-    bg->norm2 = pow(bg->a, (double)(3 + al));
+    bg->norm1 = ipow(bg->a, 1 + al);
+    bg->norm2 = ipow(bg->a, 3 + al);
     bg->ad_stale = bg->ad;
     bg->hub = bg->ad / bg->a;
-    bg->apow = pow(bg->a, (double)(al - 3));
-    bg->a3 = pow(bg->a, (double)(3 - al));
+    bg->apow = ipow(bg->a, al - 3);
+    bg->a3 = ipow(bg->a, 3 - al);
 }
 
 // a'' = (1/3)(fStar/MPl)^2 a^(1+2 alpha) ((alpha-2) K + alpha G + (alpha+1) V)  (evolution.cpp:1087)
 __device__ double friedmann_add(const DevBG *bg, double K, double G, double V) {
     const int al = bg->alpha;
-    return 1. / 3. * bg->fs_over_mpl2 * pow(bg->a, (double)(1 + 2 * al)) * ((al - 2) * K + al * G + (al + 1) * V);
+    return 1. / 3. * bg->fs_over_mpl2 * ipow(bg->a, 1 + 2 * al) * ((al - 2) * K + al * G + (al + 1) * V);
 }
 
 __global__ void __launch_bounds__(512) k_scalar(DevBG *bg, const double *__restrict__ partKG,
@@ -505,7 +505,7 @@ __global__ void __launch_bounds__(512) k_scalar(DevBG *bg, const double *__restr
     double K = 0, G = 0, V = 0;
     const double a = bg->a;
     for (int f = 0; f < bg->nf; ++f) {
-        const double k = .5 * sums[2 * f] / pow(a, 6.0) * bg->inv_n3sq;
+        const double k = .5 * sums[2 * f] / ipow(a, 6) * bg->inv_n3sq;
         double grad = bg->kIR2 * sums[2 * f + 1];
         grad *= bg->inv_n3;
         grad /= 2.;
@@ -602,7 +602,7 @@ __global__ void k_spectra_scalar(Geo g, const cplx<T> *__restrict__ fk, const cp
     for (int i = threadIdx.x; i < nb; i += blockDim.x) { sF[i] = sP[i] = sN[i] = 0.0; sC[i] = 0; }
     __syncthreads();
     const int fld = blockIdx.y, N = g.N, H = g.H, M = g.M;
-    const double a = bg->a, hub = bg->ad / a, aop = pow(a, (double)(bg->alpha - 3));
+    const double a = bg->a, hub = bg->ad / a, aop = ipow(a, bg->alpha - 3);
     const cplx<T> *f = fk + (long long)fld * g.modes, *p = pk + (long long)fld * g.modes;
     for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < g.modes;
          m += (long long)gridDim.x * blockDim.x) {
@@ -753,8 +753,21 @@ void plan(const psc_params &p, int R, LaunchCfg *cfg) {
         g.tlz_shift = ilog2i(tlz);
         g.ldz = 0;
         cfg->thr_z = nin * tlz * Pz;
-        cfg->smem_z = (size_t)nslot * tlz * (g.M + g.M / 16 + 1) * csize;
-        cfg->nbz = (g.lines_z + tlz - 1) / tlz;
+        // work slots + staging slots of the Z pass. Without GWs (one or two inputs per
+        // line) the pass is persistent, one wave of blocks prefetching their next tile;
+        // the eight-input GW pass is bound by its instruction stream and runs one tile
+        // per block (measured faster on GB300).
+        cfg->smem_z = (size_t)(nslot + (g.gw ? 0 : nin)) * tlz * (g.M + g.M / 16 + 1) * csize;
+        const int ntiles = (g.lines_z + tlz - 1) / tlz;
+        int sms = 0, dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                      cudaSuccess || sms <= 0)
+            sms = 152;
+        const size_t smem_sm = 227 * 1024;
+        int per_sm = (int)(smem_sm / cfg->smem_z);
+        if (per_sm > 2) per_sm = 2;
+        if (per_sm < 1) per_sm = 1;
+        cfg->nbz = (g.gw || ntiles < per_sm * sms) ? ntiles : per_sm * sms;
         g.pkg_stride = 2 * kMaxFields * cfg->nbx;
         g.pv_stride = kMaxTerms * cfg->nbz;
         return;

@@ -302,6 +302,12 @@ struct ZIdx {
     __device__ __forceinline__ int operator()(int n) const { return base + n + (n >> 4); }
 };
 
+// Without GWs (one or two inputs per line) the pass is persistent: a block walks the
+// tiles blockIdx.x, blockIdx.x + gridDim.x, ...; while one tile is transformed, the
+// input lines of the next are copied into a staging area by cp.async (no register
+// round trip), so the HBM reads overlap the FFT work. Shared memory: nslot work slots,
+// then nin staging slots. The eight-input GW pass, bound by its instruction stream,
+// runs one tile per block and loads its lines straight into the work slots.
 template <typename T, int L, bool GW>
 __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restrict__ TA, const cplx<T> *__restrict__ TB,
                                                 const cplx<T> *__restrict__ TC, cplx<T> *__restrict__ QV,
@@ -311,6 +317,7 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
     using C = cplx<T>;
     using RP = RegPlan<L>;
     constexpr int M = L, P = RP::P, LS = ZIdx<L>::LS;
+    constexpr bool STAGED = !GW;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *slots = reinterpret_cast<C *>(smem_raw);
     {
@@ -329,164 +336,187 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
     const int nf = g.nf;
     const int nin = nf * (GW ? 4 : 1);
     const int nout = nf + (GW ? 6 : 0);
+    const int nslot = nin > nout ? nin : nout;
     const int j = threadIdx.x % P;
     const int t = (threadIdx.x / P) & (TL - 1);
     const int grp = threadIdx.x / (P * TL);   // input handled by this thread in phase 1
-    const int line = blockIdx.x * TL + t;
-    const bool valid = line < g.lines_z;
     const size_t slot_elems = (size_t)TL * LS;
+    C *stage = slots + (size_t)nslot * slot_elems;
     const T inv_n3 = (T)bg->inv_n3;
     const T kIR = (T)bg->kIR;
-
-    // 1. complex-to-real along z of input grp: pack X[k], X[M-k] into the
-    //    M-point transform Z[k] = (X[k] + conj X[M-k]) + i w^k (X[k] - conj X[M-k]),
-    //    w = e^{+2 pi i/N}; Im X[0] and Im X[M] are ignored, as a c2r does.
-    {
-        const int fld = GW ? (grp >> 2) : grp;
-        const int kind = GW ? (grp & 3) : 0;   // 0: f, 1: d/dx f, 2: d/dy f, 3: d/dz f
-        const C *src = (kind == 1 ? TB : (kind == 2 ? TC : TA)) + (long long)fld * g.modes + (long long)line * H;
+    const int fld = GW ? (grp >> 2) : grp;
+    const int kind = GW ? (grp & 3) : 0;   // 0: f, 1: d/dx f, 2: d/dy f, 3: d/dz f
+    const C *src0 = (kind == 1 ? TB : (kind == 2 ? TC : TA)) + (long long)fld * g.modes;
+    const ZIdx<L> ixs{(int)(grp * slot_elems + t * LS)};
+    const int ntiles = (g.lines_z + TL - 1) >> sh;
+    // stage X[0..M] of this thread's line of tile `tile` (M+1 entries fit: the pad leaves room)
+    auto prefetch = [&](int tile) {
+        const int ln = tile * TL + t;
+        if (tile < ntiles && ln < g.lines_z) {
+            const C *src = src0 + (long long)ln * H;
+#pragma unroll
+            for (int r = 0; r < 16; ++r) cp_async_elem(stage + ixs(j + r * P), src + j + r * P);
+            if (j == 0) cp_async_elem(stage + ixs(M), src + M);
+        }
+        cp_async_commit();
+    };
+    Model mdl;
+    mdl.kind = g.model;
+    mdl.gsq = g.gsq;
+    T pot_t[kMaxTerms] = {T(0), T(0)};
+    if (STAGED) prefetch(blockIdx.x);
+    for (int tile = blockIdx.x; tile < ntiles; tile = STAGED ? tile + gridDim.x : ntiles) {
+        const int line = tile * TL + t;
+        const bool valid = line < g.lines_z;
         const ZIdx<L> ix{(int)(grp * slot_elems + t * LS)};
-        // stage X[0..M] of the line in its slot (M+1 entries fit: the pad leaves room)
-        if (valid) {
+        const C *in_buf = STAGED ? stage : slots;
+        if (STAGED) {
+            cp_async_wait_all();
+        } else if (valid) {
+            const C *src = src0 + (long long)line * H;
 #pragma unroll
             for (int r = 0; r < 16; ++r) slots[ix(j + r * P)] = src[j + r * P];
             if (j == 0) slots[ix(M)] = src[M];
         }
         __syncthreads();
-        C v[16];
+        // 1. complex-to-real along z of input grp: pack X[k], X[M-k] into the
+        //    M-point transform Z[k] = (X[k] + conj X[M-k]) + i w^k (X[k] - conj X[M-k]),
+        //    w = e^{+2 pi i/N}; Im X[0] and Im X[M] are ignored, as a c2r does.
+        {
+            C v[16];
 #pragma unroll
-        for (int r = 0; r < 16; ++r) {
-            const int k = j + r * P;
-            C x = mk<T>(0, 0), y = mk<T>(0, 0);
-            if (valid) {
-                x = slots[ix(k)];
-                y = slots[ix(M - k)];
-                if (kind == 3) {
-                    const T kx = kIR * (T)k;                           // k < M
-                    const T ky = (k == 0) ? T(0) : kIR * (T)(M - k);   // Nyquist zeroed
-                    x = mk<T>(-kx * x.y, kx * x.x);
-                    y = mk<T>(-ky * y.y, ky * y.x);
+            for (int r = 0; r < 16; ++r) {
+                const int k = j + r * P;
+                C x = mk<T>(0, 0), y = mk<T>(0, 0);
+                if (valid) {
+                    x = in_buf[ixs(k)];
+                    y = in_buf[ixs(M - k)];
+                    if (kind == 3) {
+                        const T kx = kIR * (T)k;                           // k < M
+                        const T ky = (k == 0) ? T(0) : kIR * (T)(M - k);   // Nyquist zeroed
+                        x = mk<T>(-kx * x.y, kx * x.x);
+                        y = mk<T>(-ky * y.y, ky * y.x);
+                    }
                 }
+                y.y = -y.y;
+                if (k == 0) { x.y = T(0); y.y = T(0); }
+                const C s = cadd(x, y), d = csub(x, y);
+                C w = __ldg(&tw[k]);
+                w.y = -w.y;
+                const C td = cmul(w, d);
+                v[r] = mk<T>(s.x - td.y, s.y + td.x);
             }
-            y.y = -y.y;
-            if (k == 0) { x.y = T(0); y.y = T(0); }
-            const C s = cadd(x, y), d = csub(x, y);
-            C w = __ldg(&tw[k]);
-            w.y = -w.y;
-            const C td = cmul(w, d);
-            v[r] = mk<T>(s.x - td.y, s.y + td.x);
-        }
-        __syncthreads();   // the slot is reused as the exchange buffer
-        fft_reg<C, L, +1>(v, slots, ix, j, tw, N / L);
-        __syncthreads();
-#pragma unroll
-        for (int q = 0; q < RP::NBL; ++q)
-#pragma unroll
-            for (int r = 0; r < RP::RL; ++r) slots[ix(RP::out(j, q, r))] = cscale(v[q * RP::RL + r], inv_n3);
-    }
-    __syncthreads();
-
-    // 2. pointwise epilogue: V'(f), <V>, anisotropic stress
-    Model mdl;
-    mdl.kind = g.model;
-    mdl.gsq = g.gsq;
-    T pot_t[kMaxTerms] = {T(0), T(0)};
-    for (int idx = threadIdx.x; idx < TL * M; idx += blockDim.x) {
-        const int tt = idx / M, m = idx - tt * M;
-        if (blockIdx.x * TL + tt >= g.lines_z) continue;
-        const int e = tt * LS + m + (m >> 4);
-        C in[8];
-#pragma unroll
-        for (int o = 0; o < 8; ++o)
-            if (o < nin) in[o] = slots[o * slot_elems + e];
-        if (!GW && tape_fx) {   // adjoint tape: the real fields (sites 2m, 2m+1 of the line)
-            const long long ln = (long long)blockIdx.x * TL + tt;
-#pragma unroll
-            for (int fl = 0; fl < 2; ++fl)
-                if (fl < nf) reinterpret_cast<C *>(tape_fx + fl * g.sites + ln * N)[m] = in[fl];
-        }
-        C out[8];
-#pragma unroll
-        for (int half = 0; half < 2; ++half) {
-            T f[2], vp[2];
-#pragma unroll
-            for (int fl = 0; fl < 2; ++fl) {
-                if (fl < nf) {
-                    const C c = in[GW ? fl * 4 : fl];
-                    f[fl] = half ? c.y : c.x;
-                } else {
-                    f[fl] = T(0);
-                }
-            }
-            model_dvdf<T>(mdl, f, vp, nf);
-            model_potential<T, T>(mdl, f, pot_t);
-#pragma unroll
-            for (int fl = 0; fl < 2; ++fl)
-                if (fl < nf) { if (half) out[fl].y = vp[fl]; else out[fl].x = vp[fl]; }
-            if (GW) {
-                T d[2][3];
-#pragma unroll
-                for (int fl = 0; fl < 2; ++fl)
-#pragma unroll
-                    for (int ax = 0; ax < 3; ++ax)
-                        d[fl][ax] = (fl < nf) ? (half ? in[fl * 4 + 1 + ax].y : in[fl * 4 + 1 + ax].x) : T(0);
-                const int si[6] = {0, 0, 0, 1, 1, 2}, sj[6] = {0, 1, 2, 1, 2, 2};
-#pragma unroll
-                for (int c = 0; c < 6; ++c) {
-                    T sum = T(0);
-#pragma unroll
-                    for (int fl = 0; fl < 2; ++fl)
-                        if (fl < nf) sum += T(2) * d[fl][si[c]] * d[fl][sj[c]];
-                    if (half) out[nf + c].y = sum; else out[nf + c].x = sum;
-                }
-            }
-        }
-#pragma unroll
-        for (int o = 0; o < 8; ++o)
-            if (o < nout) slots[o * slot_elems + e] = out[o];
-    }
-    double pot[kMaxTerms] = {(double)pot_t[0], (double)pot_t[1]};
-    block_reduce_store<kMaxTerms>(pot, partV, gridDim.x, blockIdx.x);
-    __syncthreads();
-
-    // 3. real-to-complex along z of every product; X[k] = (Z[k] + conj Z[M-k])/2
-    //    + e^{-2 pi i k/N} (Z[k] - conj Z[M-k])/(2i), k = 0..M (Z[M] = Z[0])
-    const int rounds = (nout + nin - 1) / nin;
-    for (int it = 0; it < rounds; ++it) {
-        const int o = grp + it * nin;
-        const bool act = o < nout;
-        const ZIdx<L> ix{(int)((act ? o : 0) * slot_elems + t * LS)};
-        C v[16];
-#pragma unroll
-        for (int r = 0; r < 16; ++r) v[r] = act ? slots[ix(j + r * P)] : mk<T>(0, 0);
-        __syncthreads();   // all loads of this round precede the first exchange write
-        fft_reg<C, L, -1>(v, slots, ix, j, tw, N / L, act);
-        __syncthreads();
-        if (act) {
+            __syncthreads();   // every thread has read the input lines
+            if (STAGED) prefetch(tile + gridDim.x);
+            fft_reg<C, L, +1>(v, slots, ix, j, tw, N / L);
+            __syncthreads();
 #pragma unroll
             for (int q = 0; q < RP::NBL; ++q)
 #pragma unroll
-                for (int r = 0; r < RP::RL; ++r) slots[ix(RP::out(j, q, r))] = v[q * RP::RL + r];
+                for (int r = 0; r < RP::RL; ++r) slots[ix(RP::out(j, q, r))] = cscale(v[q * RP::RL + r], inv_n3);
         }
         __syncthreads();
-        if (act && valid) {
-            C *dst = ((o < nf) ? QV + (long long)o * g.modes : QS + (long long)(o - nf) * g.modes) + (long long)line * H;
+
+        // 2. pointwise epilogue: V'(f), <V>, anisotropic stress
+        for (int idx = threadIdx.x; idx < TL * M; idx += blockDim.x) {
+            const int tt = idx / M, m = idx - tt * M;
+            const long long ln = (long long)tile * TL + tt;
+            if (ln >= g.lines_z) continue;
+            const int e = tt * LS + m + (m >> 4);
+            C in[8];
 #pragma unroll
-            for (int r = 0; r <= 16; ++r) {
-                const int k = (r < 16) ? j + r * P : M;
-                if (r == 16 && j != 0) break;
-                const C zk = slots[ix(k == M ? 0 : k)];
-                const C zc = cconj(slots[ix(k == 0 ? 0 : M - k)]);
-                const C ev = cscale(cadd(zk, zc), T(0.5));
-                const C dd = cscale(csub(zk, zc), T(0.5));
-                const C od = mk<T>(dd.y, -dd.x);
-                C w;
-                if (k < M) w = __ldg(&tw[k]); else w = mk<T>(T(-1), T(0));
-                dst[k] = cadd(ev, cmul(w, od));
+            for (int o = 0; o < 8; ++o)
+                if (o < nin) in[o] = slots[o * slot_elems + e];
+            if (!GW && tape_fx) {   // adjoint tape: the real fields (sites 2m, 2m+1 of the line)
+#pragma unroll
+                for (int fl = 0; fl < 2; ++fl)
+                    if (fl < nf) reinterpret_cast<C *>(tape_fx + fl * g.sites + ln * N)[m] = in[fl];
             }
+            C out[8];
+#pragma unroll
+            for (int half = 0; half < 2; ++half) {
+                T f[2], vp[2];
+#pragma unroll
+                for (int fl = 0; fl < 2; ++fl) {
+                    if (fl < nf) {
+                        const C c = in[GW ? fl * 4 : fl];
+                        f[fl] = half ? c.y : c.x;
+                    } else {
+                        f[fl] = T(0);
+                    }
+                }
+                model_dvdf<T>(mdl, f, vp, nf);
+                model_potential<T, T>(mdl, f, pot_t);
+#pragma unroll
+                for (int fl = 0; fl < 2; ++fl)
+                    if (fl < nf) { if (half) out[fl].y = vp[fl]; else out[fl].x = vp[fl]; }
+                if (GW) {
+                    T d[2][3];
+#pragma unroll
+                    for (int fl = 0; fl < 2; ++fl)
+#pragma unroll
+                        for (int ax = 0; ax < 3; ++ax)
+                            d[fl][ax] = (fl < nf) ? (half ? in[fl * 4 + 1 + ax].y : in[fl * 4 + 1 + ax].x) : T(0);
+                    const int si[6] = {0, 0, 0, 1, 1, 2}, sj[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) {
+                        T sum = T(0);
+#pragma unroll
+                        for (int fl = 0; fl < 2; ++fl)
+                            if (fl < nf) sum += T(2) * d[fl][si[c]] * d[fl][sj[c]];
+                        if (half) out[nf + c].y = sum; else out[nf + c].x = sum;
+                    }
+                }
+            }
+#pragma unroll
+            for (int o = 0; o < 8; ++o)
+                if (o < nout) slots[o * slot_elems + e] = out[o];
         }
         __syncthreads();
+
+        // 3. real-to-complex along z of every product; X[k] = (Z[k] + conj Z[M-k])/2
+        //    + e^{-2 pi i k/N} (Z[k] - conj Z[M-k])/(2i), k = 0..M (Z[M] = Z[0])
+        const int rounds = (nout + nin - 1) / nin;
+        for (int it = 0; it < rounds; ++it) {
+            const int o = grp + it * nin;
+            const bool act = o < nout;
+            const ZIdx<L> ix{(int)((act ? o : 0) * slot_elems + t * LS)};
+            C v[16];
+#pragma unroll
+            for (int r = 0; r < 16; ++r) v[r] = act ? slots[ix(j + r * P)] : mk<T>(0, 0);
+            __syncthreads();   // all loads of this round precede the first exchange write
+            fft_reg<C, L, -1>(v, slots, ix, j, tw, N / L, act);
+            __syncthreads();
+            if (act) {
+#pragma unroll
+                for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+                    for (int r = 0; r < RP::RL; ++r) slots[ix(RP::out(j, q, r))] = v[q * RP::RL + r];
+            }
+            __syncthreads();
+            if (act && valid) {
+                C *dst =
+                    ((o < nf) ? QV + (long long)o * g.modes : QS + (long long)(o - nf) * g.modes) + (long long)line * H;
+#pragma unroll
+                for (int r = 0; r <= 16; ++r) {
+                    const int k = (r < 16) ? j + r * P : M;
+                    if (r == 16 && j != 0) break;
+                    const C zk = slots[ix(k == M ? 0 : k)];
+                    const C zc = cconj(slots[ix(k == 0 ? 0 : M - k)]);
+                    const C ev = cscale(cadd(zk, zc), T(0.5));
+                    const C dd = cscale(csub(zk, zc), T(0.5));
+                    const C od = mk<T>(dd.y, -dd.x);
+                    C w;
+                    if (k < M) w = __ldg(&tw[k]); else w = mk<T>(T(-1), T(0));
+                    dst[k] = cadd(ev, cmul(w, od));
+                }
+            }
+            __syncthreads();
+        }
     }
+    if (STAGED) cp_async_wait_all();
+    double pot[kMaxTerms] = {(double)pot_t[0], (double)pot_t[1]};
+    block_reduce_store<kMaxTerms>(pot, partV, gridDim.x, blockIdx.x);
 }
 
 // ------------------------------------------------------------------ real-space view (c2r along z)
@@ -552,124 +582,127 @@ __global__ void __launch_bounds__(256, 2) kr_zpass_adj(Geo g, const cplx<T> *__r
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *slots = reinterpret_cast<C *>(smem_raw);
     const int sh = g.tlz_shift, TL = 1 << sh, H = g.H, N = g.N;
-    const int nf = g.nf;
     const int j = threadIdx.x % P;
     const int t = (threadIdx.x / P) & (TL - 1);
     const int grp = threadIdx.x / (P * TL);
-    const int line = blockIdx.x * TL + t;
-    const bool valid = line < g.lines_z;
     const size_t slot_elems = (size_t)TL * LS;
     const T inv_n3 = (T)(1.0 / (double)g.sites);
-    // 1. c2r along z of field grp
-    {
-        const C *src = TA + (long long)grp * g.modes + (long long)line * H;
-        const ZIdx<L> ix{(int)(grp * slot_elems + t * LS)};
-        if (valid) {
-#pragma unroll
-            for (int r = 0; r < 16; ++r) slots[ix(j + r * P)] = src[j + r * P];
-            if (j == 0) slots[ix(M)] = src[M];
-        }
-        __syncthreads();
-        C v[16];
-#pragma unroll
-        for (int r = 0; r < 16; ++r) {
-            const int k = j + r * P;
-            C x = mk<T>(0, 0), y = mk<T>(0, 0);
-            if (valid) {
-                x = slots[ix(k)];
-                y = slots[ix(M - k)];
-            }
-            y.y = -y.y;
-            if (k == 0) { x.y = T(0); y.y = T(0); }
-            const C s = cadd(x, y), d = csub(x, y);
-            C w = __ldg(&tw[k]);
-            w.y = -w.y;
-            const C td = cmul(w, d);
-            v[r] = mk<T>(s.x - td.y, s.y + td.x);
-        }
-        __syncthreads();
-        fft_reg<C, L, +1>(v, slots, ix, j, tw, N / L);
-        __syncthreads();
-#pragma unroll
-        for (int q = 0; q < RP::NBL; ++q)
-#pragma unroll
-            for (int r = 0; r < RP::RL; ++r) slots[ix(RP::out(j, q, r))] = cscale(v[q * RP::RL + r], inv_n3);
-    }
-    __syncthreads();
-    // 2. pointwise: Hessian and V' of the taped fields
     const T eta2 = (T)ad->eta2, gam = (T)ad->gamma, gsq = (T)g.gsq;
     const bool two = g.model == PSC_MODEL_PHI2CHI2;
+    const int ntiles = (g.lines_z + TL - 1) >> sh;
     T acc_t[3] = {T(0), T(0), T(0)};   // per-thread partials, FP64 across threads
-    for (int idx = threadIdx.x; idx < TL * M; idx += blockDim.x) {
-        const int tt = idx / M, m = idx - tt * M;
-        const long long ln = (long long)blockIdx.x * TL + tt;
-        if (ln >= g.lines_z) continue;
-        const int e = tt * LS + m + (m >> 4);
-        const C l0 = slots[e];
-        const C f0 = reinterpret_cast<const C *>(fx + ln * N)[m];
-        if (two) {
-            const C l1 = slots[slot_elems + e];
-            const C f1 = reinterpret_cast<const C *>(fx + g.sites + ln * N)[m];
-            C o0, o1;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int line = tile * TL + t;
+        const bool valid = line < g.lines_z;
+        // 1. c2r along z of field grp
+        {
+            const C *src = TA + (long long)grp * g.modes + (long long)line * H;
+            const ZIdx<L> ix{(int)(grp * slot_elems + t * LS)};
+            if (valid) {
 #pragma unroll
-            for (int half = 0; half < 2; ++half) {
-                const T p = half ? f0.y : f0.x, c = half ? f1.y : f1.x;
-                const T a0 = half ? l0.y : l0.x, a1 = half ? l1.y : l1.x;
-                const T vp0 = p + gsq * p * (c * c), vp1 = gsq * (p * p) * c;
-                const T h00 = T(1) + gsq * (c * c), h01 = T(2) * gsq * p * c, h11 = gsq * (p * p);
-                const T r0 = eta2 * (h00 * a0 + h01 * a1) + gam * vp0;
-                const T r1 = eta2 * (h01 * a0 + h11 * a1) + gam * vp1;
-                if (half) { o0.y = r0; o1.y = r1; } else { o0.x = r0; o1.x = r1; }
-                acc_t[0] += a0 * vp0 + a1 * vp1;
-                acc_t[1] += a0 * p * (c * c) + a1 * (p * p) * c;
-                acc_t[2] += a0 * p;
+                for (int r = 0; r < 16; ++r) slots[ix(j + r * P)] = src[j + r * P];
+                if (j == 0) slots[ix(M)] = src[M];
             }
-            slots[e] = o0;
-            slots[slot_elems + e] = o1;
-        } else {
-            C o0;
-            o0.x = eta2 * l0.x + gam * f0.x;
-            o0.y = eta2 * l0.y + gam * f0.y;
-            const T d = l0.x * f0.x + l0.y * f0.y;
-            acc_t[0] += d;
-            acc_t[2] += d;
-            slots[e] = o0;
+            __syncthreads();
+            C v[16];
+#pragma unroll
+            for (int r = 0; r < 16; ++r) {
+                const int k = j + r * P;
+                C x = mk<T>(0, 0), y = mk<T>(0, 0);
+                if (valid) {
+                    x = slots[ix(k)];
+                    y = slots[ix(M - k)];
+                }
+                y.y = -y.y;
+                if (k == 0) { x.y = T(0); y.y = T(0); }
+                const C s = cadd(x, y), d = csub(x, y);
+                C w = __ldg(&tw[k]);
+                w.y = -w.y;
+                const C td = cmul(w, d);
+                v[r] = mk<T>(s.x - td.y, s.y + td.x);
+            }
+            __syncthreads();
+            fft_reg<C, L, +1>(v, slots, ix, j, tw, N / L);
+            __syncthreads();
+#pragma unroll
+            for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+                for (int r = 0; r < RP::RL; ++r) slots[ix(RP::out(j, q, r))] = cscale(v[q * RP::RL + r], inv_n3);
+        }
+        __syncthreads();
+        // 2. pointwise: Hessian and V' of the taped fields
+        for (int idx = threadIdx.x; idx < TL * M; idx += blockDim.x) {
+            const int tt = idx / M, m = idx - tt * M;
+            const long long ln = (long long)tile * TL + tt;
+            if (ln >= g.lines_z) continue;
+            const int e = tt * LS + m + (m >> 4);
+            const C l0 = slots[e];
+            const C f0 = reinterpret_cast<const C *>(fx + ln * N)[m];
+            if (two) {
+                const C l1 = slots[slot_elems + e];
+                const C f1 = reinterpret_cast<const C *>(fx + g.sites + ln * N)[m];
+                C o0, o1;
+#pragma unroll
+                for (int half = 0; half < 2; ++half) {
+                    const T p = half ? f0.y : f0.x, c = half ? f1.y : f1.x;
+                    const T a0 = half ? l0.y : l0.x, a1 = half ? l1.y : l1.x;
+                    const T vp0 = p + gsq * p * (c * c), vp1 = gsq * (p * p) * c;
+                    const T h00 = T(1) + gsq * (c * c), h01 = T(2) * gsq * p * c, h11 = gsq * (p * p);
+                    const T r0 = eta2 * (h00 * a0 + h01 * a1) + gam * vp0;
+                    const T r1 = eta2 * (h01 * a0 + h11 * a1) + gam * vp1;
+                    if (half) { o0.y = r0; o1.y = r1; } else { o0.x = r0; o1.x = r1; }
+                    acc_t[0] += a0 * vp0 + a1 * vp1;
+                    acc_t[1] += a0 * p * (c * c) + a1 * (p * p) * c;
+                    acc_t[2] += a0 * p;
+                }
+                slots[e] = o0;
+                slots[slot_elems + e] = o1;
+            } else {
+                C o0;
+                o0.x = eta2 * l0.x + gam * f0.x;
+                o0.y = eta2 * l0.y + gam * f0.y;
+                const T d = l0.x * f0.x + l0.y * f0.y;
+                acc_t[0] += d;
+                acc_t[2] += d;
+                slots[e] = o0;
+            }
+        }
+        __syncthreads();
+        // 3. r2c along z of field grp
+        {
+            const ZIdx<L> ix{(int)(grp * slot_elems + t * LS)};
+            C v[16];
+#pragma unroll
+            for (int r = 0; r < 16; ++r) v[r] = slots[ix(j + r * P)];
+            __syncthreads();
+            fft_reg<C, L, -1>(v, slots, ix, j, tw, N / L);
+            __syncthreads();
+#pragma unroll
+            for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+                for (int r = 0; r < RP::RL; ++r) slots[ix(RP::out(j, q, r))] = v[q * RP::RL + r];
+            __syncthreads();
+            if (valid) {
+                C *dst = QV + (long long)grp * g.modes + (long long)line * H;
+#pragma unroll
+                for (int r = 0; r <= 16; ++r) {
+                    const int k = (r < 16) ? j + r * P : M;
+                    if (r == 16 && j != 0) break;
+                    const C zk = slots[ix(k == M ? 0 : k)];
+                    const C zc = cconj(slots[ix(k == 0 ? 0 : M - k)]);
+                    const C ev = cscale(cadd(zk, zc), T(0.5));
+                    const C dd = cscale(csub(zk, zc), T(0.5));
+                    const C od = mk<T>(dd.y, -dd.x);
+                    C w;
+                    if (k < M) w = __ldg(&tw[k]); else w = mk<T>(T(-1), T(0));
+                    dst[k] = cadd(ev, cmul(w, od));
+                }
+            }
+            __syncthreads();
         }
     }
     double acc[3] = {(double)acc_t[0], (double)acc_t[1], (double)acc_t[2]};
     block_reduce_store<3>(acc, part, gridDim.x, blockIdx.x);
-    __syncthreads();
-    // 3. r2c along z of field grp
-    {
-        const ZIdx<L> ix{(int)(grp * slot_elems + t * LS)};
-        C v[16];
-#pragma unroll
-        for (int r = 0; r < 16; ++r) v[r] = slots[ix(j + r * P)];
-        __syncthreads();
-        fft_reg<C, L, -1>(v, slots, ix, j, tw, N / L);
-        __syncthreads();
-#pragma unroll
-        for (int q = 0; q < RP::NBL; ++q)
-#pragma unroll
-            for (int r = 0; r < RP::RL; ++r) slots[ix(RP::out(j, q, r))] = v[q * RP::RL + r];
-        __syncthreads();
-        if (valid) {
-            C *dst = QV + (long long)grp * g.modes + (long long)line * H;
-#pragma unroll
-            for (int r = 0; r <= 16; ++r) {
-                const int k = (r < 16) ? j + r * P : M;
-                if (r == 16 && j != 0) break;
-                const C zk = slots[ix(k == M ? 0 : k)];
-                const C zc = cconj(slots[ix(k == 0 ? 0 : M - k)]);
-                const C ev = cscale(cadd(zk, zc), T(0.5));
-                const C dd = cscale(csub(zk, zc), T(0.5));
-                const C od = mk<T>(dd.y, -dd.x);
-                C w;
-                if (k < M) w = __ldg(&tw[k]); else w = mk<T>(T(-1), T(0));
-                dst[k] = cadd(ev, cmul(w, od));
-            }
-        }
-    }
 }
 
 // X forward transform of the adjoint's J^T application with its epilogue:
