@@ -233,6 +233,32 @@ __device__ __forceinline__ void block_reduce_store(double (&v)[NV], double *out,
     }
 }
 
+// The same with the per-thread values in the field precision T: the warp-level
+// shuffle sums run in T, only the per-warp partials are summed in FP64 (GB300's FP64
+// pipe is narrow; a full FP64 tree per block showed up as 10-17 % FP64-pipe time in
+// the passes that reduce).
+template <typename T, int NV>
+__device__ __forceinline__ void block_reduce_store_t(T (&v)[NV], double *out, int stride, int slot) {
+    __shared__ double red[32][NV > 0 ? NV : 1];
+#pragma unroll
+    for (int i = 0; i < NV; ++i)
+        for (int off = 16; off > 0; off >>= 1) v[i] += __shfl_down_sync(0xffffffffu, v[i], off);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int i = 0; i < NV; ++i) red[warp][i] = (double)v[i];
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            double x = lane < nw ? red[lane][i] : 0.0;
+            for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+            if (lane == 0) out[i * stride + slot] = x;
+        }
+    }
+}
+
 __device__ __forceinline__ int pcoord(int i, int N) { return i <= (N >> 1) ? i : i - N; }
 
 // x^n for a small integer n by repeated squaring: the scale-factor powers a^(1+alpha),

@@ -40,49 +40,40 @@ __global__ void __launch_bounds__(256, 2) kr_ifft_x(Geo g, cplx<T> *__restrict__
     const long long base = (long long)blockIdx.y * g.modes + line;
     auto ix = [&](int n) { return n * TL + t; };
     const T c = DRIFT ? (T)bg->c_drift : T(0);
-    C v[16];
-#pragma unroll
-    for (int r = 0; r < 16; ++r) {
-        const long long a = base + (long long)(j + r * RP::P) * stride;
-        C x = mk<T>(0, 0);
-        if (valid) {
-            x = fk[a];
-            if (DRIFT) {
-                const C p = pk[a];
-                x.x += c * p.x;
-                x.y += c * p.y;
-                fk[a] = x;
-            }
-        }
-        v[r] = x;
-    }
-    fft_reg<C, L, +1>(v, sm, ix, j, tw, g.N / L);
-    if (valid) {
-#pragma unroll
-        for (int q = 0; q < RP::NBL; ++q)
-#pragma unroll
-            for (int r = 0; r < RP::RL; ++r) TA[base + (long long)RP::out(j, q, r) * stride] = v[q * RP::RL + r];
-    }
-    if (GW) {
-        __syncthreads();
-        const T kIR = (T)bg->kIR;
+    const T kIR = GW ? (T)bg->kIR : T(0);
+    // pass 0: (drifted) f -> TA; with GWs pass 1: i k_x f -> TB (one copy of the
+    // transform code for both keeps the register allocation spill-free)
+#pragma unroll 1
+    for (int pass = 0; pass < (GW ? 2 : 1); ++pass) {
+        if (pass) __syncthreads();   // the exchange buffer is free again
+        C v[16];
 #pragma unroll
         for (int r = 0; r < 16; ++r) {
             const int n = j + r * RP::P;
+            const long long a = base + (long long)n * stride;
             C x = mk<T>(0, 0);
             if (valid) {
-                const C f = fk[base + (long long)n * stride];
-                const T kx = (n == (g.N >> 1)) ? T(0) : kIR * (T)pcoord(n, g.N);
-                x = mk<T>(-kx * f.y, kx * f.x);
+                x = fk[a];
+                if (pass == 0 && DRIFT) {
+                    const C p = pk[a];
+                    x.x += c * p.x;
+                    x.y += c * p.y;
+                    fk[a] = x;
+                }
+                if (pass == 1) {
+                    const T kx = (n == (g.N >> 1)) ? T(0) : kIR * (T)pcoord(n, g.N);
+                    x = mk<T>(-kx * x.y, kx * x.x);
+                }
             }
             v[r] = x;
         }
         fft_reg<C, L, +1>(v, sm, ix, j, tw, g.N / L);
+        C *dst = pass ? TB : TA;
         if (valid) {
 #pragma unroll
             for (int q = 0; q < RP::NBL; ++q)
 #pragma unroll
-                for (int r = 0; r < RP::RL; ++r) TB[base + (long long)RP::out(j, q, r) * stride] = v[q * RP::RL + r];
+                for (int r = 0; r < RP::RL; ++r) dst[base + (long long)RP::out(j, q, r) * stride] = v[q * RP::RL + r];
         }
     }
 }
@@ -138,10 +129,14 @@ __global__ void __launch_bounds__(256, 2) kr_ifft_y(Geo g, cplx<T> *__restrict__
     bg += blockIdx.z;
     const T kIR = (T)bg->kIR;
     if (GW) {
-        // the y-derivative reads TA before TA is transformed in place
-        ry_tile<T, L, +1>(g, TA + off, TC + off, true, kIR, sm, tw);
-        ry_tile<T, L, +1>(g, TA + off, TA + off, false, kIR, sm, tw);
-        ry_tile<T, L, +1>(g, TB + off, TB + off, false, kIR, sm, tw);
+        // the y-derivative reads TA before TA is transformed in place; one copy of the
+        // transform code for the three arrays keeps the register allocation spill-free
+#pragma unroll 1
+        for (int a = 0; a < 3; ++a) {
+            const cplx<T> *src = (a == 2 ? TB : TA) + off;
+            cplx<T> *dst = (a == 0 ? TC : (a == 1 ? TA : TB)) + off;
+            ry_tile<T, L, +1>(g, src, dst, a == 0, kIR, sm, tw);
+        }
     } else {
         ry_tile<T, L, +1>(g, TA + off, TA + off, false, kIR, sm, tw);
     }
@@ -153,7 +148,8 @@ struct ArrList8 {
 };
 
 template <typename T, int L>
-__global__ void __launch_bounds__(256, 3) kr_fft_y(Geo g, ArrList8 arrs, const cplx<T> *__restrict__ tw) {
+__global__ void __launch_bounds__(256, 3) kr_fft_y(Geo g, const __grid_constant__ ArrList8 arrs,
+                                                 const cplx<T> *__restrict__ tw) {
     using C = cplx<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *sm = reinterpret_cast<C *>(smem_raw);
@@ -264,8 +260,8 @@ __global__ void __launch_bounds__(256, 2) kr_fft_x_final(Geo g, const cplx<T> *_
                     }
                 }
         }
-        double vals[2] = {(double)accK, (double)accG};
-        block_reduce_store<2>(vals, partKG + (size_t)(2 * job) * gridDim.x, gridDim.x, blockIdx.x);
+        T vals[2] = {accK, accG};
+        block_reduce_store_t<T, 2>(vals, partKG + (size_t)(2 * job) * gridDim.x, gridDim.x, blockIdx.x);
     } else if (GW && valid) {
         const T c_drift = (T)bg->c_drift;
 #pragma unroll
@@ -515,8 +511,7 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
         }
     }
     if (STAGED) cp_async_wait_all();
-    double pot[kMaxTerms] = {(double)pot_t[0], (double)pot_t[1]};
-    block_reduce_store<kMaxTerms>(pot, partV, gridDim.x, blockIdx.x);
+    block_reduce_store_t<T, kMaxTerms>(pot_t, partV, gridDim.x, blockIdx.x);
 }
 
 // ------------------------------------------------------------------ real-space view (c2r along z)
@@ -701,8 +696,7 @@ __global__ void __launch_bounds__(256, 2) kr_zpass_adj(Geo g, const cplx<T> *__r
             __syncthreads();
         }
     }
-    double acc[3] = {(double)acc_t[0], (double)acc_t[1], (double)acc_t[2]};
-    block_reduce_store<3>(acc, part, gridDim.x, blockIdx.x);
+    block_reduce_store_t<T, 3>(acc_t, part, gridDim.x, blockIdx.x);
 }
 
 // X forward transform of the adjoint's J^T application with its epilogue:
