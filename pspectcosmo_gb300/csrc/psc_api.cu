@@ -767,10 +767,12 @@ int psc_time_passes(psc_handle *h, int reps, float *ms) {
     cudaEvent_t ev[7];
     for (int i = 0; i < 7; ++i) CU(cudaEventCreate(&ev[i]));
     double acc[PSC_NPASS] = {0, 0, 0, 0, 0, 0};
-    // zero-length kicks: the state is unchanged; a'' is kept (diagnostics mode)
+    // the passes of a stage with the drift on and zero drift and kick coefficients
+    // (SCALAR_EVAL): the full memory traffic of a step's stage, the state unchanged
+    // (f + 0 pi = f exactly); a'' is kept (diagnostics mode)
     for (int r = 0; r < reps; ++r) {
         CU(psc::launch_scalar(h->cfg, h->b, psc::SCALAR_EVAL, 0, h->st));
-        CU(psc::launch_stage_timed(h->cfg, h->b, h->p0().precision, 0, psc::SCALAR_EVAL_END, ev, h->st));
+        CU(psc::launch_stage_timed(h->cfg, h->b, h->p0().precision, 1, psc::SCALAR_EVAL_END, ev, h->st));
         CU(cudaEventSynchronize(ev[6]));
         for (int i = 0; i < PSC_NPASS; ++i) {
             float t = 0.f;
