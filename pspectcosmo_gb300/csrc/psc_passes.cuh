@@ -298,6 +298,43 @@ struct ZIdx {
     __device__ __forceinline__ int operator()(int n) const { return base + n + (n >> 4); }
 };
 
+// Half-length packing partners by warp shuffle. The P = M/16 lanes of a z line are
+// consecutive lanes of one warp. Input order (thread j holds x[j + rP], r < 16): the
+// partner of k = j + rP is M - k = (15 - r) P + (P - j), held by lane P - j in its
+// register 15 - r (lane 0: its own register 16 - r, and x[M] for r = 0).
+template <typename C>
+__device__ __forceinline__ C shfl_c(C a, int src, int width) {
+    C r;
+    r.x = __shfl_sync(0xffffffffu, a.x, src, width);
+    r.y = __shfl_sync(0xffffffffu, a.y, src, width);
+    return r;
+}
+
+template <typename C, int M>
+__device__ __forceinline__ void partners_in(const C (&v)[16], C xM, int j, C (&y)[16]) {
+    constexpr int P = M / 16;
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+        const C s = shfl_c(v[15 - r], (P - j) & (P - 1), P);
+        y[r] = (j == 0) ? (r == 0 ? xM : v[(16 - r) & 15]) : s;
+    }
+}
+
+// Output order of the forward transform (thread j holds Z[out(j, q, r)] in v[q RL + r]):
+// the partner of k = (j NBL + q) + r NSL is M - k, held by lane P - j (q = 0) or
+// P - 1 - j (q > 0) in register ((NBL - q) mod NBL) RL + RL - 1 - r; lane 0 with q = 0
+// holds it itself (register RL - r, and Z[0] for r = 0). Returns conj Z[M - k].
+template <typename C, int M>
+__device__ __forceinline__ C partner_out(const C (&v)[16], int j, int q, int r) {
+    using RP = RegPlan<M>;
+    constexpr int P = RP::P, RL = RP::RL, NBL = RP::NBL;
+    const C a = v[(q == 0 ? 0 : NBL - q) * RL + (RL - 1 - r)];
+    const C s = shfl_c(a, q == 0 ? ((P - j) & (P - 1)) : (P - 1 - j), P);
+    C z = s;
+    if (q == 0 && j == 0) z = (r == 0) ? v[0] : v[(RL - r) % RL];
+    return cconj(z);
+}
+
 // Without GWs (one or two inputs per line) the pass is persistent: a block walks the
 // tiles blockIdx.x, blockIdx.x + gridDim.x, ...; while one tile is transformed, the
 // input lines of the next are copied into a staging area by cp.async (no register
@@ -365,28 +402,41 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
         const int line = tile * TL + t;
         const bool valid = line < g.lines_z;
         const ZIdx<L> ix{(int)(grp * slot_elems + t * LS)};
-        const C *in_buf = STAGED ? stage : slots;
-        if (STAGED) {
-            cp_async_wait_all();
-        } else if (valid) {
-            const C *src = src0 + (long long)line * H;
-#pragma unroll
-            for (int r = 0; r < 16; ++r) slots[ix(j + r * P)] = src[j + r * P];
-            if (j == 0) slots[ix(M)] = src[M];
-        }
-        __syncthreads();
         // 1. complex-to-real along z of input grp: pack X[k], X[M-k] into the
         //    M-point transform Z[k] = (X[k] + conj X[M-k]) + i w^k (X[k] - conj X[M-k]),
         //    w = e^{+2 pi i/N}; Im X[0] and Im X[M] are ignored, as a c2r does.
+        //    Staged form: both from the staging area; one-tile form: own elements from
+        //    global memory into registers, partners by warp shuffle.
+        C v[16], yv[16];
+        if (STAGED) {
+            cp_async_wait_all();
+            __syncthreads();
+        } else {
+            C xM = mk<T>(0, 0);
+            if (valid) {
+                const C *src = src0 + (long long)line * H;
+#pragma unroll
+                for (int r = 0; r < 16; ++r) v[r] = src[j + r * P];
+                if (j == 0) xM = src[M];
+            } else {
+#pragma unroll
+                for (int r = 0; r < 16; ++r) v[r] = mk<T>(0, 0);
+            }
+            partners_in<C, M>(v, xM, j, yv);
+        }
         {
-            C v[16];
 #pragma unroll
             for (int r = 0; r < 16; ++r) {
                 const int k = j + r * P;
                 C x = mk<T>(0, 0), y = mk<T>(0, 0);
                 if (valid) {
-                    x = in_buf[ixs(k)];
-                    y = in_buf[ixs(M - k)];
+                    if (STAGED) {
+                        x = stage[ixs(k)];
+                        y = stage[ixs(M - k)];
+                    } else {
+                        x = v[r];
+                        y = yv[r];
+                    }
                     if (kind == 3) {
                         const T kx = kIR * (T)k;                           // k < M
                         const T ky = (k == 0) ? T(0) : kIR * (T)(M - k);   // Nyquist zeroed
@@ -402,8 +452,10 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
                 const C td = cmul(w, d);
                 v[r] = mk<T>(s.x - td.y, s.y + td.x);
             }
-            __syncthreads();   // every thread has read the input lines
-            if (STAGED) prefetch(tile + gridDim.x);
+            if (STAGED) {
+                __syncthreads();   // every thread has read the staging area
+                prefetch(tile + gridDim.x);
+            }
             fft_reg<C, L, +1>(v, slots, ix, j, tw, N / L);
             __syncthreads();
 #pragma unroll
@@ -477,11 +529,35 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
             const int o = grp + it * nin;
             const bool act = o < nout;
             const ZIdx<L> ix{(int)((act ? o : 0) * slot_elems + t * LS)};
-            C v[16];
 #pragma unroll
             for (int r = 0; r < 16; ++r) v[r] = act ? slots[ix(j + r * P)] : mk<T>(0, 0);
             __syncthreads();   // all loads of this round precede the first exchange write
             fft_reg<C, L, -1>(v, slots, ix, j, tw, N / L, act);
+            if (!STAGED) {
+                // one-tile form: the partners Z[M-k] by warp shuffle, X[k] straight out
+                C *dst =
+                    ((o < nf) ? QV + (long long)o * g.modes : QS + (long long)(o - nf) * g.modes) + (long long)line * H;
+                const bool wr = act && valid;
+#pragma unroll
+                for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+                    for (int r = 0; r < RP::RL; ++r) {
+                        const int k = RP::out(j, q, r);
+                        const C zk = v[q * RP::RL + r];
+                        const C zc = partner_out<C, M>(v, j, q, r);
+                        const C ev = cscale(cadd(zk, zc), T(0.5));
+                        const C dd = cscale(csub(zk, zc), T(0.5));
+                        const C od = mk<T>(dd.y, -dd.x);
+                        const C w = __ldg(&tw[k]);
+                        if (wr) dst[k] = cadd(ev, cmul(w, od));
+                    }
+                if (wr && j == 0) {   // X[M] = Re Z[0] - Im Z[0]
+                    const C z0 = v[0];
+                    dst[M] = mk<T>(z0.x - z0.y, T(0));
+                }
+                __syncthreads();   // the transform's last exchange read precedes the next writes
+                continue;
+            }
             __syncthreads();
             if (act) {
 #pragma unroll

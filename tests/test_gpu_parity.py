@@ -175,6 +175,29 @@ def test_other_lattice_sizes_fp64(oracle_mod, N):
     _compare_state(lat, o, p, 1e-10, 1e-12)
 
 
+@pytest.mark.parametrize("precision", [64, 32])
+@pytest.mark.parametrize("N", [32, 64])
+def test_gw_register_engine(oracle_mod, N, precision):
+    """The register-engine passes with GWs (N >= 32: z lines of 16 and 32 points, two
+    different last-stage radices) against the oracle's real-space GW step."""
+    from pspectcosmo_gb300 import Lattice
+    from pspectcosmo_gb300.params import Params
+
+    p = Params.preheating(N=N, vv=2, spectral=0, with_gw=1, precision=precision)
+    q = p.copy()
+    q.precision = 64
+    o = oracle_mod.Oracle(q)
+    o.init_ic()
+    lat = Lattice(p)
+    lat.initialize()
+    lat.evolve(0.005, 3)
+    o.step(0.005, 3)
+    if precision == 64:
+        _compare_state(lat, o, p, 1e-10, 1e-12)
+    else:
+        _compare_state(lat, o, p, FP32_FIELD_TOL, FP32_BG_TOL, FP32_ADD_TOL)
+
+
 def test_nonfinite_state_is_reported():
     """A NaN planted in host-side initial data is caught by the device finite check."""
     from pspectcosmo_gb300 import Lattice, PscError
