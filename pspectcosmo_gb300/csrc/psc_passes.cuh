@@ -46,26 +46,30 @@ __global__ void __launch_bounds__(256, 2) kr_ifft_x(Geo g, cplx<T> *__restrict__
 #pragma unroll 1
     for (int pass = 0; pass < (GW ? 2 : 1); ++pass) {
         if (pass) __syncthreads();   // the exchange buffer is free again
+        // every load of the line before the first store back to f_k: the drift's
+        // read-modify-write of f_k through one pointer would otherwise keep each load
+        // behind the previous store (no alias proof at run-time strides)
         C v[16];
 #pragma unroll
-        for (int r = 0; r < 16; ++r) {
-            const int n = j + r * RP::P;
-            const long long a = base + (long long)n * stride;
-            C x = mk<T>(0, 0);
-            if (valid) {
-                x = fk[a];
-                if (pass == 0 && DRIFT) {
-                    const C p = pk[a];
-                    x.x += c * p.x;
-                    x.y += c * p.y;
-                    fk[a] = x;
-                }
-                if (pass == 1) {
-                    const T kx = (n == (g.N >> 1)) ? T(0) : kIR * (T)pcoord(n, g.N);
-                    x = mk<T>(-kx * x.y, kx * x.x);
-                }
+        for (int r = 0; r < 16; ++r) v[r] = valid ? fk[base + (long long)(j + r * RP::P) * stride] : mk<T>(0, 0);
+        if (pass == 0 && DRIFT) {
+            C pv[16];
+#pragma unroll
+            for (int r = 0; r < 16; ++r) pv[r] = valid ? pk[base + (long long)(j + r * RP::P) * stride] : mk<T>(0, 0);
+#pragma unroll
+            for (int r = 0; r < 16; ++r) {
+                v[r].x += c * pv[r].x;
+                v[r].y += c * pv[r].y;
+                if (valid) fk[base + (long long)(j + r * RP::P) * stride] = v[r];
             }
-            v[r] = x;
+        }
+        if (pass == 1) {
+#pragma unroll
+            for (int r = 0; r < 16; ++r) {
+                const int n = j + r * RP::P;
+                const T kx = (n == (g.N >> 1)) ? T(0) : kIR * (T)pcoord(n, g.N);
+                v[r] = mk<T>(-kx * v[r].y, kx * v[r].x);
+            }
         }
         fft_reg<C, L, +1>(v, sm, ix, j, tw, g.N / L);
         C *dst = pass ? TB : TA;
@@ -411,6 +415,11 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
         if (STAGED) {
             cp_async_wait_all();
             __syncthreads();
+            C xM = mk<T>(0, 0);
+#pragma unroll
+            for (int r = 0; r < 16; ++r) v[r] = stage[ixs(j + r * P)];
+            if (j == 0) xM = stage[ixs(M)];
+            partners_in<C, M>(v, xM, j, yv);
         } else {
             C xM = mk<T>(0, 0);
             if (valid) {
@@ -430,13 +439,8 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
                 const int k = j + r * P;
                 C x = mk<T>(0, 0), y = mk<T>(0, 0);
                 if (valid) {
-                    if (STAGED) {
-                        x = stage[ixs(k)];
-                        y = stage[ixs(M - k)];
-                    } else {
-                        x = v[r];
-                        y = yv[r];
-                    }
+                    x = v[r];
+                    y = yv[r];
                     if (kind == 3) {
                         const T kx = kIR * (T)k;                           // k < M
                         const T ky = (k == 0) ? T(0) : kIR * (T)(M - k);   // Nyquist zeroed
@@ -533,8 +537,8 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
             for (int r = 0; r < 16; ++r) v[r] = act ? slots[ix(j + r * P)] : mk<T>(0, 0);
             __syncthreads();   // all loads of this round precede the first exchange write
             fft_reg<C, L, -1>(v, slots, ix, j, tw, N / L, act);
-            if (!STAGED) {
-                // one-tile form: the partners Z[M-k] by warp shuffle, X[k] straight out
+            {
+                // the partners Z[M-k] by warp shuffle, X[k] straight out
                 C *dst =
                     ((o < nf) ? QV + (long long)o * g.modes : QS + (long long)(o - nf) * g.modes) + (long long)line * H;
                 const bool wr = act && valid;
@@ -555,35 +559,8 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
                     const C z0 = v[0];
                     dst[M] = mk<T>(z0.x - z0.y, T(0));
                 }
-                __syncthreads();   // the transform's last exchange read precedes the next writes
-                continue;
             }
-            __syncthreads();
-            if (act) {
-#pragma unroll
-                for (int q = 0; q < RP::NBL; ++q)
-#pragma unroll
-                    for (int r = 0; r < RP::RL; ++r) slots[ix(RP::out(j, q, r))] = v[q * RP::RL + r];
-            }
-            __syncthreads();
-            if (act && valid) {
-                C *dst =
-                    ((o < nf) ? QV + (long long)o * g.modes : QS + (long long)(o - nf) * g.modes) + (long long)line * H;
-#pragma unroll
-                for (int r = 0; r <= 16; ++r) {
-                    const int k = (r < 16) ? j + r * P : M;
-                    if (r == 16 && j != 0) break;
-                    const C zk = slots[ix(k == M ? 0 : k)];
-                    const C zc = cconj(slots[ix(k == 0 ? 0 : M - k)]);
-                    const C ev = cscale(cadd(zk, zc), T(0.5));
-                    const C dd = cscale(csub(zk, zc), T(0.5));
-                    const C od = mk<T>(dd.y, -dd.x);
-                    C w;
-                    if (k < M) w = __ldg(&tw[k]); else w = mk<T>(T(-1), T(0));
-                    dst[k] = cadd(ev, cmul(w, od));
-                }
-            }
-            __syncthreads();
+            __syncthreads();   // the transform's last exchange read precedes the next writes
         }
     }
     if (STAGED) cp_async_wait_all();
@@ -665,24 +642,22 @@ __global__ void __launch_bounds__(256, 2) kr_zpass_adj(Geo g, const cplx<T> *__r
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int line = tile * TL + t;
         const bool valid = line < g.lines_z;
-        // 1. c2r along z of field grp
+        // 1. c2r along z of field grp (own elements into registers, partners by shuffle)
         {
             const C *src = TA + (long long)grp * g.modes + (long long)line * H;
             const ZIdx<L> ix{(int)(grp * slot_elems + t * LS)};
-            if (valid) {
+            C v[16], yv[16], xM = mk<T>(0, 0);
 #pragma unroll
-                for (int r = 0; r < 16; ++r) slots[ix(j + r * P)] = src[j + r * P];
-                if (j == 0) slots[ix(M)] = src[M];
-            }
-            __syncthreads();
-            C v[16];
+            for (int r = 0; r < 16; ++r) v[r] = valid ? src[j + r * P] : mk<T>(0, 0);
+            if (valid && j == 0) xM = src[M];
+            partners_in<C, M>(v, xM, j, yv);
 #pragma unroll
             for (int r = 0; r < 16; ++r) {
                 const int k = j + r * P;
                 C x = mk<T>(0, 0), y = mk<T>(0, 0);
                 if (valid) {
-                    x = slots[ix(k)];
-                    y = slots[ix(M - k)];
+                    x = v[r];
+                    y = yv[r];
                 }
                 y.y = -y.y;
                 if (k == 0) { x.y = T(0); y.y = T(0); }
@@ -692,7 +667,6 @@ __global__ void __launch_bounds__(256, 2) kr_zpass_adj(Geo g, const cplx<T> *__r
                 const C td = cmul(w, d);
                 v[r] = mk<T>(s.x - td.y, s.y + td.x);
             }
-            __syncthreads();
             fft_reg<C, L, +1>(v, slots, ix, j, tw, N / L);
             __syncthreads();
 #pragma unroll
@@ -747,28 +721,21 @@ __global__ void __launch_bounds__(256, 2) kr_zpass_adj(Geo g, const cplx<T> *__r
             for (int r = 0; r < 16; ++r) v[r] = slots[ix(j + r * P)];
             __syncthreads();
             fft_reg<C, L, -1>(v, slots, ix, j, tw, N / L);
-            __syncthreads();
+            C *dst = QV + (long long)grp * g.modes + (long long)line * H;
 #pragma unroll
             for (int q = 0; q < RP::NBL; ++q)
 #pragma unroll
-                for (int r = 0; r < RP::RL; ++r) slots[ix(RP::out(j, q, r))] = v[q * RP::RL + r];
-            __syncthreads();
-            if (valid) {
-                C *dst = QV + (long long)grp * g.modes + (long long)line * H;
-#pragma unroll
-                for (int r = 0; r <= 16; ++r) {
-                    const int k = (r < 16) ? j + r * P : M;
-                    if (r == 16 && j != 0) break;
-                    const C zk = slots[ix(k == M ? 0 : k)];
-                    const C zc = cconj(slots[ix(k == 0 ? 0 : M - k)]);
+                for (int r = 0; r < RP::RL; ++r) {
+                    const int k = RP::out(j, q, r);
+                    const C zk = v[q * RP::RL + r];
+                    const C zc = partner_out<C, M>(v, j, q, r);
                     const C ev = cscale(cadd(zk, zc), T(0.5));
                     const C dd = cscale(csub(zk, zc), T(0.5));
                     const C od = mk<T>(dd.y, -dd.x);
-                    C w;
-                    if (k < M) w = __ldg(&tw[k]); else w = mk<T>(T(-1), T(0));
-                    dst[k] = cadd(ev, cmul(w, od));
+                    const C w = __ldg(&tw[k]);
+                    if (valid) dst[k] = cadd(ev, cmul(w, od));
                 }
-            }
+            if (valid && j == 0) dst[M] = mk<T>(v[0].x - v[0].y, T(0));   // X[M] = Re Z[0] - Im Z[0]
             __syncthreads();
         }
     }
@@ -801,6 +768,11 @@ __global__ void __launch_bounds__(256, 2) kr_fft_x_adj(Geo g, const cplx<T> *__r
     const T eta1 = (T)ad->eta1, delta = (T)ad->delta;
     const int y = line / H, kz = line - y * H;
     const int py = pcoord(y, N);
+    C lv[16];   // every Lf load before the first Lf store (no alias proof at run-time strides)
+#pragma unroll
+    for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+        for (int r = 0; r < RP::RL; ++r) lv[q * RP::RL + r] = Lf[base + (long long)RP::out(j, q, r) * stride];
 #pragma unroll
     for (int q = 0; q < RP::NBL; ++q)
 #pragma unroll
@@ -810,7 +782,7 @@ __global__ void __launch_bounds__(256, 2) kr_fft_x_adj(Geo g, const cplx<T> *__r
             const T k2 = (T)(px * px + py * py + kz * kz);
             const long long a = base + (long long)n * stride;
             const C mv = Mk[a], fv = fk[a], y0 = v[q * RP::RL + r];
-            C l = Lf[a];
+            C l = lv[q * RP::RL + r];
             l.x += y0.x + k2 * (eta1 * mv.x + delta * fv.x);
             l.y += y0.y + k2 * (eta1 * mv.y + delta * fv.y);
             Lf[a] = l;
