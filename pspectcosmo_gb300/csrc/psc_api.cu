@@ -382,30 +382,50 @@ int create_handle(const psc_params *ps, int R, psc_handle **out) {
     return PSC_OK;
 }
 
+// the host generator (initialize.cpp:562-810) for realization r, uploaded
+int init_ic_host(psc_handle *h, int r, std::vector<double> &fk, std::vector<double> &pk, std::vector<double> &uk,
+                 std::vector<double> &puk, psc::ICInfo *info) {
+    const psc::Geo &g = h->cfg.g;
+    const size_t n = (size_t)g.modes;
+    int rc;
+    std::fill(fk.begin(), fk.end(), 0.0);
+    std::fill(pk.begin(), pk.end(), 0.0);
+    if (g.gw) {
+        std::fill(uk.begin(), uk.end(), 0.0);
+        std::fill(puk.begin(), puk.end(), 0.0);
+    }
+    *info = psc::generate_ic(h->p[r], fk.data(), pk.data(), g.gw ? uk.data() : nullptr, g.gw ? puk.data() : nullptr);
+    if ((rc = upload(h, foff(h, h->b.fk, r), fk.data(), n * g.nf)) ||
+        (rc = upload(h, foff(h, h->b.pk, r), pk.data(), n * g.nf)))
+        return rc;
+    if (g.gw && ((rc = upload(h, goff(h, h->b.uk, r), uk.data(), n * 6)) ||
+                 (rc = upload(h, goff(h, h->b.puk, r), puk.data(), n * 6))))
+        return rc;
+    return PSC_OK;
+}
+
 int init_ic(psc_handle *h) {
     const psc::Geo &g = h->cfg.g;
     const size_t n = (size_t)g.modes;
-    std::vector<double> fk(2 * n * g.nf), pk(2 * n * g.nf), uk, puk;
-    if (g.gw) {
-        uk.resize(2 * n * 6);
-        puk.resize(2 * n * 6);
-    }
+    std::vector<double> fk, pk, uk, puk;
     int rc;
     for (int r = 0; r < h->R; ++r) {
-        std::fill(fk.begin(), fk.end(), 0.0);
-        std::fill(pk.begin(), pk.end(), 0.0);
-        if (g.gw) {
-            std::fill(uk.begin(), uk.end(), 0.0);
-            std::fill(puk.begin(), puk.end(), 0.0);
+        psc::ICInfo info;
+        if (h->p[r].seed >= 1 && !(psc::ic_setup(h->p[r]).k2c > 0.)) {
+            // on the device: one thread per mode (initialize.cpp:686-749 by skip-ahead)
+            if ((rc = psc::ic_device(h, r, &info))) return rc;
+        } else {
+            // seed < 1 (constant draws) or an initial low-pass cut: the host generator
+            if (fk.empty()) {
+                fk.resize(2 * n * g.nf);
+                pk.resize(2 * n * g.nf);
+                if (g.gw) {
+                    uk.resize(2 * n * 6);
+                    puk.resize(2 * n * 6);
+                }
+            }
+            if ((rc = init_ic_host(h, r, fk, pk, uk, puk, &info))) return rc;
         }
-        psc::ICInfo info = psc::generate_ic(h->p[r], fk.data(), pk.data(), g.gw ? uk.data() : nullptr,
-                                            g.gw ? puk.data() : nullptr);
-        if ((rc = upload(h, foff(h, h->b.fk, r), fk.data(), n * g.nf)) ||
-            (rc = upload(h, foff(h, h->b.pk, r), pk.data(), n * g.nf)))
-            return rc;
-        if (g.gw && ((rc = upload(h, goff(h, h->b.uk, r), uk.data(), n * 6)) ||
-                     (rc = upload(h, goff(h, h->b.puk, r), puk.data(), n * 6))))
-            return rc;
         psc::DevBG bg;
         if ((rc = read_bg(h, r, &bg))) return rc;
         bg.a = info.a;

@@ -220,6 +220,58 @@ void set_mode_gw(Ctx &c, const double kv[3], double k2, long long m, bool isReal
 
 }  // namespace
 
+ICSetup ic_setup(const psc_params &p) {
+    Ctx c(p);
+    ICSetup s{};
+    const int N = c.N, nf = p.nflds;
+    s.N = N;
+    s.H = c.H;
+    s.nf = nf;
+    s.model = p.model;
+    s.alpha = p.alpha;
+    s.simulate_inflation = p.simulate_inflation;
+    s.gw = p.with_gw;
+    s.fStar = c.fStar;
+    s.omegaStar = c.omegaStar;
+    s.dx = c.dx;
+    s.DFDP = c.DFDP;
+    s.kIR = p.kIR;
+    s.gsq = p.gsq;
+    s.dp2 = pw2(p.kIR);
+    s.k2c = c.k2cutoff();
+    for (int fld = 0; fld < nf; fld++) {
+        s.f0[fld] = p.initfield[fld] / c.fStar;
+        s.fd0[fld] = p.initderivs[fld] / c.fStar / c.omegaStar;
+    }
+    effective_mass(p, s.m2, s.f0);
+    s.a = p.a0;
+    s.info.a = s.a;
+    if (p.expansion > 0) {
+        double fdsq = 0., pot = 0.;
+        for (int fld = 0; fld < nf; fld++) fdsq += pw2(s.fd0[fld]);
+        const int nterms = p.model == PSC_MODEL_PHI2 ? 1 : 2;
+        for (int t = 0; t < nterms; t++) pot += potential_term(p, t, s.f0);
+        double h = fdsq / 2.;
+        h += pot;
+        h *= pw2(c.fStar / p.MPl) / 3.;
+        s.hubble = std::sqrt(h);
+        s.info.ad = s.hubble * s.a;
+        s.info.add_printed = pw2(c.fStar / p.MPl) / 3. * ((p.alpha - 2) * fdsq + (p.alpha + 1) * pot) * s.a;
+        s.info.kinetic = fdsq / 2.;
+        s.info.potential = pot;
+    }
+    s.info.hubble_init = s.hubble;
+    s.aop = std::pow(s.a, p.alpha - 3);
+    s.norm_s = std::sqrt(c.DFDP);
+    s.norm_gw = p.MPl * c.omegaStar / pw2(c.fStar) * std::pow(c.N / c.dx, 1.5);
+    s.n3 = (double)N * N * N;
+    s.seed = p.seed;
+    const long long h2 = N / 2 - 1;
+    s.visits = 2 * h2 * (N + 2) + h2 * (long long)N * N + 8;
+    s.dpm = p.simulate_inflation ? 1 : 4;
+    return s;
+}
+
 ICInfo generate_ic(const psc_params &p, double *f_k, double *pi_k, double *u_k, double *pi_u_k) {
     Ctx c(p);
     const int N = c.N, H = c.H, nf = p.nflds;
