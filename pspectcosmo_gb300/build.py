@@ -62,7 +62,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         if verbose and r.stderr:
             sys.stderr.write(r.stderr)
     tmp = LIB + ".tmp"
-    r = subprocess.run([cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"], capture_output=True, text=True)
+    r = subprocess.run([cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lpthread"], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)

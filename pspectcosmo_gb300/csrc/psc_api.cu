@@ -14,6 +14,7 @@
 #include <new>
 #include <string>
 #include <tuple>
+#include <thread>
 #include <vector>
 
 #include "../../include/psc.h"
@@ -135,6 +136,31 @@ int ensure_staging(psc_handle *h, size_t bytes) {
     return PSC_OK;
 }
 
+// out[i] = (To)in[i] for i < n on all host cores (the FP64 <-> FP32 conversion of the
+// state exchange is memory-bound; one thread converts ~1-2 GB/s)
+template <typename To, typename From>
+void convert_parallel(To *out, const From *in, size_t n) {
+    const size_t kMin = 1u << 20;
+    unsigned nt = std::thread::hardware_concurrency();
+    if (nt == 0) nt = 1;
+    if (nt > 32) nt = 32;
+    if (n < kMin * 2 || nt == 1) {
+        for (size_t i = 0; i < n; ++i) out[i] = (To)in[i];
+        return;
+    }
+    if ((size_t)nt > n / kMin) nt = (unsigned)(n / kMin);
+    std::vector<std::thread> th;
+    th.reserve(nt);
+    const size_t chunk = (n + nt - 1) / nt;
+    for (unsigned t = 0; t < nt; ++t) {
+        const size_t b = t * chunk, e = std::min(n, b + chunk);
+        th.emplace_back([=] {
+            for (size_t i = b; i < e; ++i) out[i] = (To)in[i];
+        });
+    }
+    for (auto &x : th) x.join();
+}
+
 // host FP64 complex -> device array of the handle's precision
 int upload(psc_handle *h, void *dst, const double *src, size_t ncplx) {
     if (h->p0().precision == 64) {
@@ -145,7 +171,7 @@ int upload(psc_handle *h, void *dst, const double *src, size_t ncplx) {
     int rc = ensure_staging(h, ncplx * 8);
     if (rc) return rc;
     float *f = static_cast<float *>(h->stage_buf);
-    for (size_t i = 0; i < 2 * ncplx; ++i) f[i] = (float)src[i];
+    convert_parallel(f, src, 2 * ncplx);
     CU(cudaMemcpyAsync(dst, f, ncplx * 8, cudaMemcpyHostToDevice, h->st));
     CU(cudaStreamSynchronize(h->st));
     return PSC_OK;
@@ -162,8 +188,7 @@ int download_real(psc_handle *h, double *dst, const void *src, size_t count) {
     if (rc) return rc;
     CU(cudaMemcpyAsync(h->stage_buf, src, count * 4, cudaMemcpyDeviceToHost, h->st));
     CU(cudaStreamSynchronize(h->st));
-    const float *f = static_cast<const float *>(h->stage_buf);
-    for (size_t i = 0; i < count; ++i) dst[i] = (double)f[i];
+    convert_parallel(dst, static_cast<const float *>(h->stage_buf), count);
     return PSC_OK;
 }
 
