@@ -111,3 +111,92 @@ def test_gradients_against_central_differences(oracle_mod, nf, vv, scale):
     for name, Of, pred in checks:
         fd = (Of(1.0) - Of(-1.0)) / 2
         assert abs(fd - pred) <= 1e-5 * abs(fd), (name, fd, pred)
+
+
+def _gw_state(oracle_mod, N, zero_gw):
+    p = Params.preheating(N=N, vv=2, spectral=0, with_gw=1)
+    o = oracle_mod.Oracle(p)
+    o.init_ic()
+    f, pi, u, pu = o.state_k()
+    bg = o.bg()
+    sh, sg = (2, N, N, N // 2 + 1), (6, N, N, N // 2 + 1)
+    z = 0.0 if zero_gw else 1.0
+    st0 = [f.reshape(sh), pi.reshape(sh), bg["a"], bg["ad"], bg["add"], z * u.reshape(sg), z * pu.reshape(sg)]
+    fs = p.fStar if p.fStar > 0 else p.MPl
+    lat = A.Lattice(N, p.kIR, 2, p.gsq, alpha=p.alpha, fs_over_mpl2=(fs / p.MPl) ** 2, vv=2, gw=True)
+    return p, o, st0, lat
+
+
+def test_gw_forward_map_and_rho_gw_are_the_reference(oracle_mod):
+    """u, pi_u after the real-space GW step and energy()'s rho_GW (output.cpp:1030-1060)."""
+    p, o, st0, lat = _gw_state(oracle_mod, 16, False)
+    st = list(st0)
+    st[4] = lat.A(st[0], st[1], st[2])
+    for _ in range(3):
+        st = lat.step(st, 0.005)
+    o.step(0.005, 3)
+    f, pi, u, pu = o.state_k()
+    assert rel(st[5].reshape(u.shape), u) < 1e-12
+    assert rel(st[6].reshape(pu.shape), pu) < 1e-12
+    assert abs(lat.rho_gw(st[6], st[2]) / o.energies()["rho_gw"] - 1) < 1e-12
+
+
+def test_rho_gw_gradients_against_central_differences(oracle_mod):
+    """rho_GW generated by the scalar source from u = pi_u = 0 (so it depends on the fields at
+    O(1)); FD step 1e-3 of the fluctuation amplitude / 1e-6 of a scalar."""
+    N, dt, nsteps = 8, 0.005, 4
+    p, o, st0, lat = _gw_state(oracle_mod, N, True)
+    O, gf, gp, _, gb, gth, gu, gpu = A.gradient(lat, st0, dt, nsteps, observable="rho_gw")
+    assert O > 0
+    rng = np.random.default_rng(5)
+    checks = []
+    for name, i, g in (("f", 0, gf), ("pi", 1, gp)):
+        d = np.fft.rfftn(rng.standard_normal((2, N, N, N)), axes=(-3, -2, -1))
+        fl = st0[i].copy()
+        fl[:, 0, 0, 0] = 0
+        d *= 1e-3 * np.abs(fl).mean() / np.abs(d).mean()
+
+        def Of(e, d=d, i=i):
+            s = list(st0)
+            s[i] = st0[i] + e * d
+            return A.run_O(lat, s, dt, nsteps, "rho_gw")
+
+        checks.append((name, Of, float(np.sum(np.real(np.conj(g) * d)))))
+    hb = 1e-6 * abs(st0[3])
+
+    def Ob(e):
+        s = list(st0)
+        s[3] = st0[3] + e * hb
+        return A.run_O(lat, s, dt, nsteps, "rho_gw")
+
+    checks.append(("ad", Ob, gb * hb))
+    for k, th in enumerate(("gsq", "mu")):
+        base = getattr(lat.model, th)
+        h = 1e-4 * base
+
+        def Ot(e, th=th, base=base, h=h):
+            m = A.Lattice.__new__(A.Lattice)
+            m.__dict__.update(lat.__dict__)
+            m.model = A.Model(lat.nf, lat.model.gsq, lat.model.mu)
+            setattr(m.model, th, base + e * h)
+            return A.run_O(m, st0, dt, nsteps, "rho_gw")
+
+        checks.append((th, Ot, gth[k] * h))
+    for name, Of, pred in checks:
+        fd = (Of(1.0) - Of(-1.0)) / 2
+        assert abs(fd - pred) <= 1e-5 * abs(fd), (name, fd, pred)
+    # the GW tensors' own gradients: rho_GW is quadratic in pi_u(T), linear response in u(0), pi_u(0)
+    _, _, st0g, _ = _gw_state(oracle_mod, N, False)
+    O, gf, gp, _, gb, gth, gu, gpu = A.gradient(lat, st0g, dt, nsteps, observable="rho_gw")
+    for name, i, g in (("u", 5, gu), ("pu", 6, gpu)):
+        d = np.fft.rfftn(rng.standard_normal((6, N, N, N)), axes=(-3, -2, -1))
+        d *= 1e-3 * np.abs(st0g[i]).mean() / np.abs(d).mean()
+
+        def Og(e, d=d, i=i):
+            s = list(st0g)
+            s[i] = st0g[i] + e * d
+            return A.run_O(lat, s, dt, nsteps, "rho_gw")
+
+        fd = (Og(1.0) - Og(-1.0)) / 2
+        pred = float(np.sum(np.real(np.conj(g) * d)))
+        assert abs(fd - pred) <= 1e-7 * abs(fd), (name, fd, pred)
