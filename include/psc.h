@@ -210,7 +210,7 @@ int psc_spectra_noalloc(const psc_params *p, double a, double ad, const void *f_
  * observable O = <chi^2> (the last field's lattice mean of its square) after `nsteps`
  * steps of `dt` from the handle's current state, with a''(0) recomputed from that state.
  * Needs a single-lattice handle, N >= 32, expansion = 2 and the unmasked step
- * (spectral = 0, or simulate_inflation = 0). Checkpoints are taken every `every` steps
+ * (spectral = 0, or simulate_inflation = 0); with GWs N <= 512. Checkpoints are taken every `every` steps
  * (every <= 0: one segment); each segment is recomputed once in the reverse sweep.
  * Outputs (any pointer but O may be NULL):
  *   grad_f_k, grad_pi_k  [nflds][N][N][N/2+1] complex as interleaved doubles:
@@ -222,8 +222,22 @@ int psc_spectra_noalloc(const psc_params *p, double a, double ad, const void *f_
  * forward passes and reverse sweep; not the download of the gradients). */
 int psc_adjoint_chi2(psc_handle *h, double dt, int nsteps, int every, double *O, double *grad_f_k,
                      double *grad_pi_k, double *grad_ad0, double *grad_theta);
-/* The adjoint's own forward map alone (same stage arithmetic, unfused): O after nsteps. */
+/* The adjoint's forward map alone (the product step from a''(0) = A(state(0))): O after nsteps. */
 int psc_adjoint_forward_chi2(psc_handle *h, double dt, int nsteps, double *O);
+
+/* The same adjoint for a chosen observable (no reference counterpart):
+ *   PSC_OBS_CHI2    O = <chi^2>, as psc_adjoint_chi2;
+ *   PSC_OBS_RHO_GW  O = rho_GW, the GW energy density of energy() (output.cpp:1030-1060):
+ *                   (fStar/MPl)^2 / (4 N^6 a^6) [sum over spectra()'s GW walk of the P-projected
+ *                   |pi_u_k|^2 (output.cpp:18-53, 780-1062) + the k = 0 term]; needs with_gw = 1
+ *                   and N <= 512 (spectral = 0, the GW path).
+ * grad_u_k, grad_pi_u_k ([6][N][N][N/2+1] interleaved, may be NULL) receive dO/d(u_k(0), pi_u_k(0))
+ * on a GW handle (zero for PSC_OBS_CHI2); the other outputs as psc_adjoint_chi2. */
+#define PSC_OBS_CHI2 0
+#define PSC_OBS_RHO_GW 1
+int psc_adjoint(psc_handle *h, int observable, double dt, int nsteps, int every, double *O, double *grad_f_k,
+                double *grad_pi_k, double *grad_u_k, double *grad_pi_u_k, double *grad_ad0, double *grad_theta);
+int psc_adjoint_forward(psc_handle *h, int observable, double dt, int nsteps, double *O);
 
 const char *psc_strerror(int code);
 const char *psc_last_error(void);

@@ -157,7 +157,154 @@ __global__ void __launch_bounds__(kThreads) ka_observable(int rows, RowIdx ri, c
     psc::block_reduce_store<1>(acc, part, gridDim.x, blockIdx.x);
 }
 
-enum AdjMode { ADJ_INIT = 0, ADJ_PRE = 1, ADJ_POST = 2, ADJ_STAGE_PRE = 3, ADJ_STAGE_POST = 4 };
+// GW point: Mu = alpha1 Lpu (the merged kicks' adjoint), Lu += eta1 k^2 Mu,
+// part += sum' w Re(conj Mu Fu), Fu = -kIR^2 k^2 u + S_k from the tape (six components)
+template <typename T>
+__global__ void __launch_bounds__(kThreads) ka_point_gw(int rows, RowIdx ri, const psc::cplx<T> *__restrict__ Lpu,
+                                                        psc::cplx<T> *__restrict__ Lu,
+                                                        const psc::cplx<T> *__restrict__ fu,
+                                                        psc::cplx<T> *__restrict__ Mu,
+                                                        const psc::DevAdj *__restrict__ ad, double *__restrict__ part) {
+    const T a1 = (T)ad->alpha1, e1 = (T)ad->eta1;
+    int r, rs, lane;
+    warp_rows(&r, &rs, &lane);
+    double acc[1] = {0.0};
+    for (; r < rows; r += rs) {
+        const int kxy = ri.kxy2(r);
+        T racc = T(0);
+        for (int kz = lane; kz < ri.H; kz += 32) {
+            const long long i = (long long)r * ri.H + kz;
+            const psc::cplx<T> l = Lpu[i], fv = fu[i];
+            psc::cplx<T> lu = Lu[i];
+            const psc::cplx<T> mv = psc::mk<T>(a1 * l.x, a1 * l.y);
+            const T k2 = (T)(kxy + kz * kz);
+            Mu[i] = mv;
+            lu.x += e1 * k2 * mv.x;
+            lu.y += e1 * k2 * mv.y;
+            Lu[i] = lu;
+            const T w = (kz == 0 || kz == ri.H - 1) ? T(1) : T(2);
+            racc += w * (mv.x * fv.x + mv.y * fv.y);
+        }
+        acc[0] += (double)racc;
+    }
+    psc::block_reduce_store<1>(acc, part, gridDim.x, blockIdx.x);
+}
+
+// GW stage: pu_half = pu + kfu Fu;  part += sum' w Re(conj Lu pu_half);  Lpu += c2 Lu
+template <typename T>
+__global__ void __launch_bounds__(kThreads) ka_stage_gw(int rows, RowIdx ri, const psc::cplx<T> *__restrict__ Lu,
+                                                        psc::cplx<T> *__restrict__ Lpu,
+                                                        const psc::cplx<T> *__restrict__ pu,
+                                                        const psc::cplx<T> *__restrict__ fu,
+                                                        const psc::DevAdj *__restrict__ ad, double *__restrict__ part) {
+    const T kf = (T)ad->kfu, c2 = (T)ad->c2;
+    int r, rs, lane;
+    warp_rows(&r, &rs, &lane);
+    double acc[1] = {0.0};
+    for (; r < rows; r += rs) {
+        T racc = T(0);
+        for (int kz = lane; kz < ri.H; kz += 32) {
+            const long long i = (long long)r * ri.H + kz;
+            const psc::cplx<T> l = Lu[i], q = pu[i], fv = fu[i];
+            psc::cplx<T> lp = Lpu[i];
+            const T w = (kz == 0 || kz == ri.H - 1) ? T(1) : T(2);
+            racc += w * (l.x * (q.x + kf * fv.x) + l.y * (q.y + kf * fv.y));
+            lp.x += c2 * l.x;
+            lp.y += c2 * l.y;
+            Lpu[i] = lp;
+        }
+        acc[0] += (double)racc;
+    }
+    psc::block_reduce_store<1>(acc, part, gridDim.x, blockIdx.x);
+}
+
+// rho_GW of energy() (output.cpp:1030-1060) and its adjoint seed, one row (x, y) per
+// warp: q_k = sum_ij |(P U)_ij|^2 - |tr P U|^2 / 2 with P = 1 - khat khat (spectra()'s
+// projection, output.cpp:18-53), weighted as spectra()'s walk visits the stored modes
+// (interior 2; on the kz = 0, N/2 planes the "+" half 2, the real corners 1, the rest 0),
+// hz = sum |pi_u_ab(0)|^2 at k = 0. part += sum wq q; Lpu = fac 2 N^3 (wq / w) dq/d conj(U),
+// fac = (fStar/MPl)^2 / (4 N^6 a^6).
+template <typename T>
+__global__ void __launch_bounds__(kThreads) ka_seed_gw(RowIdx ri, long long modes, const psc::cplx<T> *__restrict__ puk,
+                                                       psc::cplx<T> *__restrict__ Lpu,
+                                                       const psc::DevBG *__restrict__ fin, double n3,
+                                                       double *__restrict__ part) {
+    const int N = ri.N, h = N / 2, rows = N * N;
+    const double kIR = fin->kIR, a = fin->a;
+    const double fac = fin->fs_over_mpl2 / (4.0 * n3 * n3 * psc::ipow(a, 6));
+    const int si[6] = {0, 0, 0, 1, 1, 2}, sj[6] = {0, 1, 2, 1, 2, 2};
+    const int sy[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+    int r, rs, lane;
+    warp_rows(&r, &rs, &lane);
+    double acc[1] = {0.0};
+    for (; r < rows; r += rs) {
+        const int x = r >> ri.lg, y = r & (N - 1);
+        for (int kz = lane; kz < ri.H; kz += 32) {
+            const long long m = (long long)r * ri.H + kz;
+            double cr[6], ci[6];
+            for (int c = 0; c < 6; ++c) {
+                const psc::cplx<T> v = puk[c * modes + m];
+                cr[c] = (double)v.x;
+                ci[c] = (double)v.y;
+            }
+            const bool plane = (kz == 0 || kz == h);
+            double wq = 2.0;
+            if (plane) {
+                if (x >= 1 && x < h) wq = 2.0;
+                else if (x == 0 || x == h) wq = (y >= 1 && y < h) ? 2.0 : ((y == 0 || y == h) ? 1.0 : 0.0);
+                else wq = 0.0;
+            }
+            const double wk = plane ? 1.0 : 2.0;
+            double gr[6], gi[6], q;
+            if (x == 0 && y == 0 && kz == 0) {
+                q = 0.0;
+                for (int c = 0; c < 6; ++c) {
+                    const double mult = (si[c] == sj[c]) ? 1.0 : 2.0;
+                    q += mult * (cr[c] * cr[c] + ci[c] * ci[c]);
+                    gr[c] = mult * cr[c];
+                    gi[c] = mult * ci[c];
+                }
+            } else {
+                const double kv[3] = {kIR * psc::pcoord(x, N), kIR * psc::pcoord(y, N), kIR * kz};
+                const double kn = sqrt(kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2]);
+                double P[3][3];
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 3; ++j) P[i][j] = (i == j ? 1.0 : 0.0) - (kv[i] / kn) * (kv[j] / kn);
+                double Vr[3][3], Vi[3][3];
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 3; ++j) {
+                        double vr = 0, vi = 0;
+                        for (int k = 0; k < 3; ++k) {
+                            vr += P[i][k] * cr[sy[k][j]];
+                            vi += P[i][k] * ci[sy[k][j]];
+                        }
+                        Vr[i][j] = vr;
+                        Vi[i][j] = vi;
+                    }
+                const double tr = Vr[0][0] + Vr[1][1] + Vr[2][2], ti = Vi[0][0] + Vi[1][1] + Vi[2][2];
+                q = -(tr * tr + ti * ti) / 2;
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 3; ++j) q += Vr[i][j] * Vr[i][j] + Vi[i][j] * Vi[i][j];
+                for (int c = 0; c < 6; ++c) {
+                    const int i = si[c], j = sj[c];
+                    double xr = Vr[i][j] - 0.5 * tr * P[i][j], xi = Vi[i][j] - 0.5 * ti * P[i][j];
+                    if (i != j) {
+                        xr += Vr[j][i] - 0.5 * tr * P[j][i];
+                        xi += Vi[j][i] - 0.5 * ti * P[j][i];
+                    }
+                    gr[c] = xr;
+                    gi[c] = xi;
+                }
+            }
+            acc[0] += wq * q;
+            const double s = fac * 2.0 * n3 * wq / wk;
+            for (int c = 0; c < 6; ++c) Lpu[c * modes + m] = psc::mk<T>((T)(s * gr[c]), (T)(s * gi[c]));
+        }
+    }
+    psc::block_reduce_store<1>(acc, part, gridDim.x, blockIdx.x);
+}
+
+enum AdjMode { ADJ_INIT = 0, ADJ_PRE = 1, ADJ_POST = 2, ADJ_STAGE_PRE = 3, ADJ_STAGE_POST = 4, ADJ_INIT_GW = 5 };
 
 struct AdjArgs {
     int mode;
@@ -165,7 +312,9 @@ struct AdjArgs {
     long long j;     // global point / stage index
     double n3;       // N^3
     // partial-sum regions: [offset, count]
-    int d1_off, d1_n, z_off, z_n, d3_off, d3_n, o_off, o_n;
+    int d1_off, d1_n, z_off, z_n, d3_off, d3_n, o_off, o_n, dg_off, d3g_off;
+    int gw;     // the GW adjoint runs (rho_GW observable)
+    int last;   // the final point: no stage after it, only its GW kick adjoint
 };
 
 __device__ double block_sum(const double *__restrict__ v, int n, double *red) {
@@ -210,25 +359,38 @@ __device__ PointBG point_bg(const psc::DevBG *snap, int i) {
 __global__ void __launch_bounds__(256) k_adj(AdjArgs A, psc::DevAdj *__restrict__ ad, const psc::DevBG *__restrict__ snap,
                                              const double *__restrict__ part) {
     __shared__ double red[256];
-    double s[4] = {0.0, 0.0, 0.0, 0.0};
-    if (A.mode == ADJ_INIT) s[0] = block_sum(part + A.o_off, A.o_n, red);
+    double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    if (A.mode == ADJ_INIT || A.mode == ADJ_INIT_GW) s[0] = block_sum(part + A.o_off, A.o_n, red);
     if (A.mode == ADJ_POST) {
-        s[0] = block_sum(part + A.d1_off, A.d1_n, red);
-        for (int q = 0; q < 3; ++q) s[1 + q] = block_sum(part + A.z_off + q * A.z_n, A.z_n, red);
+        if (!A.last) {
+            s[0] = block_sum(part + A.d1_off, A.d1_n, red);
+            for (int q = 0; q < 3; ++q) s[1 + q] = block_sum(part + A.z_off + q * A.z_n, A.z_n, red);
+        }
+        if (A.gw) s[4] = block_sum(part + A.dg_off, A.d1_n, red);
     }
-    if (A.mode == ADJ_STAGE_POST) s[0] = block_sum(part + A.d3_off, A.d3_n, red);
+    if (A.mode == ADJ_STAGE_POST) {
+        s[0] = block_sum(part + A.d3_off, A.d3_n, red);
+        if (A.gw) s[0] += block_sum(part + A.d3g_off, A.d3_n, red);
+    }
     if (threadIdx.x != 0) return;
     const psc::DevBG &g0 = snap[0];
     const int al = g0.alpha, ns = g0.s;
     const double dt = g0.dt, kIR2 = g0.kIR2, C = g0.fs_over_mpl2 / 3.0, n3 = A.n3;
-    if (A.mode == ADJ_INIT) {
+    if (A.mode == ADJ_INIT || A.mode == ADJ_INIT_GW) {
         ad->la = ad->lb = ad->ladd = ad->lbh = ad->lat = 0.0;
         ad->gth[0] = ad->gth[1] = 0.0;
-        ad->O = s[0] / (n3 * n3);
+        if (A.mode == ADJ_INIT) {
+            ad->O = s[0] / (n3 * n3);   // <chi^2> by Parseval
+        } else {
+            // rho_GW = (fStar/MPl)^2 / (4 N^6 a^6) sum wq q; its a-adjoint -6 rho_GW / a
+            const double a = g0.a;
+            ad->O = g0.fs_over_mpl2 / (4.0 * n3 * n3 * psc::ipow(a, 6)) * s[0];
+            ad->la = -6.0 * ad->O / a;
+        }
         return;
     }
     const int q = (int)(A.j % ns);
-    const double c = g0.w[q] * dt / 2;
+    const double c = A.last ? 0.0 : g0.w[q] * dt / 2;   // the stage after the point (none after the last)
     const PointBG P = point_bg(snap, A.i);
     const double a = P.a;
     if (A.mode == ADJ_PRE) {
@@ -245,6 +407,7 @@ __global__ void __launch_bounds__(256) k_adj(AdjArgs A, psc::DevAdj *__restrict_
         ad->delta = lat * Cc * al * kIR2 / (a * a * n3);
         ad->eta1 = -psc::ipow(a, 1 + al) * kIR2;
         ad->eta2 = -psc::ipow(a, 3 + al);
+        ad->etaS = -psc::ipow(a, 1 + al);
         ad->la += lat * (C * (1 + 2 * al) * psc::ipow(a, 2 * al) * ((al - 2) * P.K + al * P.G + (al + 1) * P.V) +
                          Cc * ((al - 2) * (-6 * P.K / a) + al * (-2 * P.G / a)));
         ad->gth[0] += lat * Cc * (al + 1) * P.dVg;
@@ -252,11 +415,17 @@ __global__ void __launch_bounds__(256) k_adj(AdjArgs A, psc::DevAdj *__restrict_
         return;
     }
     if (A.mode == ADJ_POST) {
+        if (A.last) {   // the final point: only the closing GW kick of the last stage
+            if (A.gw) ad->la += (1 + al) * psc::ipow(a, al) * s[4] / n3;
+            return;
+        }
         const double d1 = s[0] / n3, d2 = s[1];
         ad->la += (1 + al) * psc::ipow(a, al) * (-kIR2) * d1 - (3 + al) * psc::ipow(a, 2 + al) * d2;
         const double e2 = -psc::ipow(a, 3 + al);
         ad->gth[0] += e2 * s[2];
         ad->gth[1] += e2 * s[3];
+        // GW kicks: dF_u/da = (1 + alpha) a^alpha (-kIR^2 k^2 u + S_k)
+        if (A.gw) ad->la += (1 + al) * psc::ipow(a, al) * s[4] / n3;
         return;
     }
     if (A.mode == ADJ_STAGE_PRE) {
@@ -265,6 +434,7 @@ __global__ void __launch_bounds__(256) k_adj(AdjArgs A, psc::DevAdj *__restrict_
         ad->kc = c;
         ad->kn1 = psc::ipow(a, 1 + al) * kIR2;
         ad->kn2 = psc::ipow(a, 3 + al);
+        ad->kfu = c * psc::ipow(a, 1 + al);
         return;
     }
     // ADJ_STAGE_POST
@@ -279,7 +449,10 @@ __global__ void __launch_bounds__(256) k_adj(AdjArgs A, psc::DevAdj *__restrict_
 
 struct AdjWS {
     size_t carr = 0, rarr = 0;   // bytes of nf complex / real arrays
+    size_t garr = 0;             // bytes of the six GW component arrays (0 without GWs)
     void *M = nullptr, *Lf = nullptr, *Lp = nullptr;
+    void *Mu = nullptr, *Lu = nullptr, *Lpu = nullptr, *Tarr = nullptr;   // GW adjoint
+    psc::DevBG *fin = nullptr;   // the background at the final point
     double *part = nullptr;
     psc::DevAdj *rec = nullptr;
     psc::DevBG *snap = nullptr;
@@ -322,14 +495,16 @@ int ws_grow(AdjWS *ws, char **ptr, int *have, int want, size_t stride) {
     return PSC_OK;
 }
 
-int check(psc_handle *h) {
+int check(psc_handle *h, int obs) {
     const psc_params &p = h->p0();
+    if (obs != PSC_OBS_CHI2 && obs != PSC_OBS_RHO_GW) return fail(PSC_ERR_ARG, "unknown observable");
     if (h->R != 1) return fail(PSC_ERR_CONFIG, "the adjoint works on single-lattice handles");
     if (h->cfg.g.N < 32) return fail(PSC_ERR_CONFIG, "the adjoint needs N >= 32");
     if (h->cfg.g.mask)
         return fail(PSC_ERR_CONFIG, "the adjoint differentiates the unmasked step (spectral = 0 or simulate_inflation = 0)");
     if (p.expansion != 2) return fail(PSC_ERR_CONFIG, "the adjoint needs self-consistent expansion (expansion = 2)");
-    if (p.with_gw) return fail(PSC_ERR_CONFIG, "the adjoint needs with_gw = 0 (GWs do not act on a scalar observable)");
+    if (obs == PSC_OBS_RHO_GW && !p.with_gw) return fail(PSC_ERR_CONFIG, "the rho_GW observable needs with_gw = 1");
+    if (p.with_gw && h->cfg.g.N > 512) return fail(PSC_ERR_CONFIG, "the adjoint with GWs needs N <= 512");
     if (p.model == PSC_MODEL_PHI2CHI2 && !(p.gsq > 0)) return fail(PSC_ERR_CONFIG, "the adjoint needs gsq > 0");
     if (!h->have_state) return fail(PSC_ERR_STATE, "no state: call psc_init_ic or psc_set_state first");
     return PSC_OK;
@@ -344,6 +519,8 @@ struct Run {
     double n3;
     int z_n;
     RowIdx ri;
+    bool gw;      // the handle evolves GWs (tape of pi_u and the GW force)
+    bool gwadj;   // the GW adjoint runs (rho_GW observable)
 };
 
 int setup(psc_handle *h, Run *r) {
@@ -356,18 +533,27 @@ int setup(psc_handle *h, Run *r) {
     if (!ws->M) {
         ws->carr = (size_t)g.nf * g.modes * h->csize;
         ws->rarr = (size_t)g.nf * g.sites * (h->csize / 2);
+        ws->garr = g.gw ? (size_t)6 * g.modes * h->csize : 0;
         void **cs[] = {&ws->M, &ws->Lf, &ws->Lp};
         for (void **q : cs)
             if (int rc = ws_alloc(ws, q, ws->carr)) return rc;
-        ws->z_n = h->cfg.nbz;
-        ws->part_n = 3 * kEW + 3 * ws->z_n;
+        if (g.gw) {
+            void **gs[] = {&ws->Mu, &ws->Lu, &ws->Lpu};
+            for (void **q : gs)
+                if (int rc = ws_alloc(ws, q, ws->garr)) return rc;
+            if (int rc = ws_alloc(ws, &ws->Tarr, (size_t)3 * ws->carr)) return rc;
+        }
+        ws->z_n = psc::adj_z_blocks(g.N, g.nf);   // the scalar adjoint Z pass's grid
+        ws->part_n = 5 * kEW + 3 * ws->z_n;
         void *p;
         if (int rc = ws_alloc(ws, &p, sizeof(double) * ws->part_n)) return rc;
         ws->part = static_cast<double *>(p);
         if (int rc = ws_alloc(ws, &p, sizeof(psc::DevAdj))) return rc;
         ws->rec = static_cast<psc::DevAdj *>(p);
-        ws->tape_stride = 3 * ws->carr + ws->rarr;
-        ws->ckpt_stride = 2 * ws->carr + ((sizeof(psc::DevBG) + 255) / 256) * 256;
+        if (int rc = ws_alloc(ws, &p, sizeof(psc::DevBG))) return rc;
+        ws->fin = static_cast<psc::DevBG *>(p);
+        ws->tape_stride = 3 * ws->carr + ws->rarr + 2 * ws->garr;
+        ws->ckpt_stride = 2 * ws->carr + 2 * ws->garr + ((sizeof(psc::DevBG) + 255) / 256) * 256;
     }
     r->h = h;
     r->ws = ws;
@@ -383,6 +569,8 @@ int setup(psc_handle *h, Run *r) {
     int lg = 0;
     while ((1 << lg) < g.N) ++lg;
     r->ri = RowIdx{g.N, g.H, lg};
+    r->gw = g.gw != 0;
+    r->gwadj = false;
     return PSC_OK;
 }
 
@@ -400,11 +588,17 @@ AdjArgs args(const Run &r, int mode, int i, long long j) {
     A.d3_n = kEW;
     A.o_off = 2 * kEW + 3 * r.z_n;
     A.o_n = kEW;
+    A.dg_off = 3 * kEW + 3 * r.z_n;
+    A.d3g_off = 4 * kEW + 3 * r.z_n;
+    A.gw = r.gwadj ? 1 : 0;
+    A.last = 0;
     return A;
 }
 
-int scalar(const Run &r, int mode, int i, long long j) {
-    k_adj<<<1, 256, 0, r.st>>>(args(r, mode, i, j), r.ws->rec, r.ws->snap, r.ws->part);
+int scalar(const Run &r, int mode, int i, long long j, const psc::DevBG *snap = nullptr, bool last = false) {
+    AdjArgs A = args(r, mode, i, j);
+    A.last = last ? 1 : 0;
+    k_adj<<<1, 256, 0, r.st>>>(A, r.ws->rec, snap ? snap : r.ws->snap, r.ws->part);
     CU(cudaGetLastError());
     return PSC_OK;
 }
@@ -414,6 +608,22 @@ void *tp_f(const Run &r, int i) { return tape_pt(r, i); }
 void *tp_p(const Run &r, int i) { return tape_pt(r, i) + r.ws->carr; }
 void *tp_vp(const Run &r, int i) { return tape_pt(r, i) + 2 * r.ws->carr; }
 void *tp_fx(const Run &r, int i) { return tape_pt(r, i) + 3 * r.ws->carr; }
+void *tp_pu(const Run &r, int i) { return tape_pt(r, i) + 3 * r.ws->carr + r.ws->rarr; }
+void *tp_fu(const Run &r, int i) { return tape_pt(r, i) + 3 * r.ws->carr + r.ws->rarr + r.ws->garr; }
+
+// rho_GW from the handle's current pi_u and its adjoint seed into Lpu (and the a seed)
+int observable_gw(const Run &r, void *Lpu) {
+    CU(cudaMemcpyAsync(r.ws->fin, r.h->b.bg, sizeof(psc::DevBG), cudaMemcpyDeviceToDevice, r.st));
+    double *part = r.ws->part + 2 * kEW + 3 * r.z_n;
+    if (r.prec == 32)
+        ka_seed_gw<float><<<kEW, kThreads, 0, r.st>>>(r.ri, r.modes, (const float2 *)r.h->b.puk, (float2 *)Lpu,
+                                                      r.ws->fin, r.n3, part);
+    else
+        ka_seed_gw<double><<<kEW, kThreads, 0, r.st>>>(r.ri, r.modes, (const double2 *)r.h->b.puk, (double2 *)Lpu,
+                                                       r.ws->fin, r.n3, part);
+    CU(cudaGetLastError());
+    return scalar(r, ADJ_INIT_GW, 0, 0, r.ws->fin);
+}
 
 // O from the handle's current state (Parseval: <chi^2> = sum' w |chi_k|^2 / N^6)
 // and, with Lf_last, the adjoint seed Lambda_chi = r2c(2 chi / N^3) = 2 chi_k / N^3
@@ -429,7 +639,8 @@ int observable(const Run &r, void *Lf_last) {
         ka_observable<double><<<kEW, kThreads, 0, r.st>>>(rows, r.ri, (const double2 *)chi, (double2 *)Lf_last,
                                                           2.0 / r.n3, part);
     CU(cudaGetLastError());
-    return scalar(r, ADJ_INIT, 0, 0);
+    CU(cudaMemcpyAsync(r.ws->fin, r.h->b.bg, sizeof(psc::DevBG), cudaMemcpyDeviceToDevice, r.st));
+    return scalar(r, ADJ_INIT, 0, 0, r.ws->fin);
 }
 
 // the product's step sequence for n steps from the handle's state, writing the tape
@@ -440,13 +651,15 @@ int forward_taped(const Run &r, double dt, int n) {
     const int s = h->s, npts = n * s;
     psc::Buffers bt = h->b;
     auto tape_at = [&](int i) {
-        if (i < npts) {
+        if (i <= npts) {
             bt.tape_f = tp_f(r, i);
             bt.tape_p = tp_p(r, i);
             bt.tape_vp = tp_vp(r, i);
             bt.tape_fx = tp_fx(r, i);
+            bt.tape_pu = r.gw ? tp_pu(r, i) : nullptr;
+            bt.tape_fu = r.gw ? tp_fu(r, i) : nullptr;
         } else {
-            bt.tape_f = bt.tape_p = bt.tape_vp = bt.tape_fx = nullptr;
+            bt.tape_f = bt.tape_p = bt.tape_vp = bt.tape_fx = bt.tape_pu = bt.tape_fu = nullptr;
         }
     };
     CU(psc::launch_set_run(h->b.bg, 1, dt, n, r.st));
@@ -466,13 +679,27 @@ int forward_taped(const Run &r, double dt, int n) {
 }
 
 template <typename T>
-int reverse_segment_t(const Run &r, long long jbase, int npts) {
+int reverse_segment_t(const Run &r, long long jbase, int npts, bool final_seg) {
     using C = psc::cplx<T>;
     AdjWS *ws = r.ws;
     psc_handle *h = r.h;
     double *p_d1 = ws->part, *p_z = ws->part + kEW, *p_d3 = ws->part + kEW + 3 * r.z_n;
-    const int rows = r.nf * r.N * r.N;
+    double *p_dg = ws->part + 3 * kEW + 3 * r.z_n, *p_d3g = ws->part + 4 * kEW + 3 * r.z_n;
+    const int rows = r.nf * r.N * r.N, rows_gw = 6 * r.N * r.N;
     int rc;
+    if (final_seg && r.gwadj) {
+        // the final point P_S: the closing GW kick of the last stage (the scalar part is
+        // zero there: nothing depends on pi(S) or on a''(S))
+        const long long j = jbase + npts;
+        if ((rc = scalar(r, ADJ_PRE, npts, j, nullptr, true))) return rc;
+        ka_point_gw<T><<<kEW, kThreads, 0, r.st>>>(rows_gw, r.ri, (const C *)ws->Lpu, (C *)ws->Lu,
+                                                   (const C *)tp_fu(r, npts), (C *)ws->Mu, ws->rec, p_dg);
+        CU(cudaGetLastError());
+        CU(r.prec == 32 ? psc::reg_adj_point_gw_f32(h->cfg, h->b, ws->Mu, tp_f(r, npts), ws->Tarr, ws->Lf, ws->rec, r.st)
+                        : psc::reg_adj_point_gw_f64(h->cfg, h->b, ws->Mu, tp_f(r, npts), ws->Tarr, ws->Lf, ws->rec,
+                                                    r.st));
+        if ((rc = scalar(r, ADJ_POST, npts, j, nullptr, true))) return rc;
+    }
     for (int i = npts - 1; i >= 0; --i) {
         const long long j = jbase + i;
         // the internals of stage j (its drift and a-updates)
@@ -481,6 +708,11 @@ int reverse_segment_t(const Run &r, long long jbase, int npts) {
                                                 (const C *)tp_p(r, i), (const C *)tp_f(r, i), (const C *)tp_vp(r, i),
                                                 ws->rec, p_d3);
         CU(cudaGetLastError());
+        if (r.gwadj) {
+            ka_stage_gw<T><<<kEW, kThreads, 0, r.st>>>(rows_gw, r.ri, (const C *)ws->Lu, (C *)ws->Lpu,
+                                                       (const C *)tp_pu(r, i), (const C *)tp_fu(r, i), ws->rec, p_d3g);
+            CU(cudaGetLastError());
+        }
         if ((rc = scalar(r, ADJ_STAGE_POST, i, j))) return rc;
         // point j: merged J^T of the kicks at P_j and the a''(P_j) terms
         if ((rc = scalar(r, ADJ_PRE, i, j))) return rc;
@@ -491,26 +723,47 @@ int reverse_segment_t(const Run &r, long long jbase, int npts) {
                                                  r.st)
                         : psc::reg_adj_point_f64(h->cfg, h->b, ws->M, tp_f(r, i), tp_fx(r, i), ws->Lf, p_z, ws->rec,
                                                  r.st));
+        if (r.gwadj) {
+            // the merged GW kicks at P_j: Mu, Lu, the a-dot, then the transposed source into Lf
+            ka_point_gw<T><<<kEW, kThreads, 0, r.st>>>(rows_gw, r.ri, (const C *)ws->Lpu, (C *)ws->Lu,
+                                                       (const C *)tp_fu(r, i), (C *)ws->Mu, ws->rec, p_dg);
+            CU(cudaGetLastError());
+            CU(r.prec == 32 ? psc::reg_adj_point_gw_f32(h->cfg, h->b, ws->Mu, tp_f(r, i), ws->Tarr, ws->Lf, ws->rec,
+                                                        r.st)
+                            : psc::reg_adj_point_gw_f64(h->cfg, h->b, ws->Mu, tp_f(r, i), ws->Tarr, ws->Lf, ws->rec,
+                                                        r.st));
+        }
         if ((rc = scalar(r, ADJ_POST, i, j))) return rc;
     }
     return PSC_OK;
 }
 
-int reverse_segment(const Run &r, long long jbase, int npts) {
-    return r.prec == 32 ? reverse_segment_t<float>(r, jbase, npts) : reverse_segment_t<double>(r, jbase, npts);
+int reverse_segment(const Run &r, long long jbase, int npts, bool final_seg) {
+    return r.prec == 32 ? reverse_segment_t<float>(r, jbase, npts, final_seg)
+                        : reverse_segment_t<double>(r, jbase, npts, final_seg);
 }
 
 int save_state(const Run &r, char *dst) {
-    CU(cudaMemcpyAsync(dst, r.h->b.fk, r.ws->carr, cudaMemcpyDeviceToDevice, r.st));
-    CU(cudaMemcpyAsync(dst + r.ws->carr, r.h->b.pk, r.ws->carr, cudaMemcpyDeviceToDevice, r.st));
-    CU(cudaMemcpyAsync(dst + 2 * r.ws->carr, r.h->b.bg, sizeof(psc::DevBG), cudaMemcpyDeviceToDevice, r.st));
+    const size_t c = r.ws->carr, g = r.ws->garr;
+    CU(cudaMemcpyAsync(dst, r.h->b.fk, c, cudaMemcpyDeviceToDevice, r.st));
+    CU(cudaMemcpyAsync(dst + c, r.h->b.pk, c, cudaMemcpyDeviceToDevice, r.st));
+    if (g) {
+        CU(cudaMemcpyAsync(dst + 2 * c, r.h->b.uk, g, cudaMemcpyDeviceToDevice, r.st));
+        CU(cudaMemcpyAsync(dst + 2 * c + g, r.h->b.puk, g, cudaMemcpyDeviceToDevice, r.st));
+    }
+    CU(cudaMemcpyAsync(dst + 2 * c + 2 * g, r.h->b.bg, sizeof(psc::DevBG), cudaMemcpyDeviceToDevice, r.st));
     return PSC_OK;
 }
 
 int restore_state(const Run &r, const char *src) {
-    CU(cudaMemcpyAsync(r.h->b.fk, src, r.ws->carr, cudaMemcpyDeviceToDevice, r.st));
-    CU(cudaMemcpyAsync(r.h->b.pk, src + r.ws->carr, r.ws->carr, cudaMemcpyDeviceToDevice, r.st));
-    CU(cudaMemcpyAsync(r.h->b.bg, src + 2 * r.ws->carr, sizeof(psc::DevBG), cudaMemcpyDeviceToDevice, r.st));
+    const size_t c = r.ws->carr, g = r.ws->garr;
+    CU(cudaMemcpyAsync(r.h->b.fk, src, c, cudaMemcpyDeviceToDevice, r.st));
+    CU(cudaMemcpyAsync(r.h->b.pk, src + c, c, cudaMemcpyDeviceToDevice, r.st));
+    if (g) {
+        CU(cudaMemcpyAsync(r.h->b.uk, src + 2 * c, g, cudaMemcpyDeviceToDevice, r.st));
+        CU(cudaMemcpyAsync(r.h->b.puk, src + 2 * c + g, g, cudaMemcpyDeviceToDevice, r.st));
+    }
+    CU(cudaMemcpyAsync(r.h->b.bg, src + 2 * c + 2 * g, sizeof(psc::DevBG), cudaMemcpyDeviceToDevice, r.st));
     return PSC_OK;
 }
 
@@ -523,20 +776,22 @@ int grow_snap(AdjWS *ws, int want) {
 
 }  // namespace
 
-extern "C" int psc_adjoint_chi2(psc_handle *h, double dt, int nsteps, int every, double *O, double *grad_fk,
-                                double *grad_pik, double *grad_ad0, double *grad_theta) {
+extern "C" int psc_adjoint(psc_handle *h, int observable_id, double dt, int nsteps, int every, double *O,
+                           double *grad_fk, double *grad_pik, double *grad_uk, double *grad_piuk, double *grad_ad0,
+                           double *grad_theta) {
     if (!h || !O || nsteps < 1 || !(dt > 0) || !std::isfinite(dt)) return fail(PSC_ERR_ARG, "bad argument");
     int rc;
-    if ((rc = check(h))) return rc;
+    if ((rc = check(h, observable_id))) return rc;
     if (every < 1 || every > nsteps) every = nsteps;
     Run r;
     if ((rc = setup(h, &r))) return rc;
+    r.gwadj = observable_id == PSC_OBS_RHO_GW;
     AdjWS *ws = r.ws;
     const int s = h->s;
     const int nseg = (nsteps + every - 1) / every;
     const int npts_max = every * s;
     // storage: tape of one segment, snapshots, checkpoints (+ the final state)
-    if ((rc = ws_grow(ws, &ws->tape, &ws->tape_n, npts_max, ws->tape_stride))) return rc;
+    if ((rc = ws_grow(ws, &ws->tape, &ws->tape_n, npts_max + 1, ws->tape_stride))) return rc;
     if ((rc = grow_snap(ws, npts_max + 2))) return rc;
     if (nseg > 1 && (rc = ws_grow(ws, &ws->ckpt, &ws->ckpt_n, nseg + 1, ws->ckpt_stride))) return rc;
     CU(cudaEventRecord(h->ev0, r.st));
@@ -544,7 +799,14 @@ extern "C" int psc_adjoint_chi2(psc_handle *h, double dt, int nsteps, int every,
     if ((rc = psc::hapi::evaluate(h, 0))) return rc;
     CU(cudaMemsetAsync(ws->Lf, 0, ws->carr, r.st));
     CU(cudaMemsetAsync(ws->Lp, 0, ws->carr, r.st));
+    if (r.gw) {
+        CU(cudaMemsetAsync(ws->Lu, 0, ws->garr, r.st));
+        CU(cudaMemsetAsync(ws->Lpu, 0, ws->garr, r.st));
+    }
     void *Lf_last = static_cast<char *>(ws->Lf) + (size_t)(r.nf - 1) * r.modes * h->csize;
+    // the observable and its adjoint seed from the final state (the background record
+    // goes to its own slot: the segment snapshots stay as the reverse sweep reads them)
+    auto seed = [&]() -> int { return r.gwadj ? observable_gw(r, ws->Lpu) : observable(r, Lf_last); };
     if (nseg > 1) {
         // checkpoint pass on the product's captured step
         for (int seg = 0; seg < nseg; ++seg) {
@@ -552,15 +814,14 @@ extern "C" int psc_adjoint_chi2(psc_handle *h, double dt, int nsteps, int every,
             if ((rc = psc::hapi::step(h, dt, std::min(every, nsteps - seg * every)))) return rc;
         }
         if ((rc = save_state(r, ws->ckpt + (size_t)nseg * ws->ckpt_stride))) return rc;
-        CU(cudaMemcpyAsync(ws->snap, h->b.bg, sizeof(psc::DevBG), cudaMemcpyDeviceToDevice, r.st));
-        if ((rc = observable(r, Lf_last))) return rc;
+        if ((rc = seed())) return rc;
     }
     for (int seg = nseg - 1; seg >= 0; --seg) {
         const int n = std::min(every, nsteps - seg * every);
         if (nseg > 1 && (rc = restore_state(r, ws->ckpt + (size_t)seg * ws->ckpt_stride))) return rc;
         if ((rc = forward_taped(r, dt, n))) return rc;
-        if (nseg == 1 && (rc = observable(r, Lf_last))) return rc;
-        if ((rc = reverse_segment(r, (long long)seg * every * s, n * s))) return rc;
+        if (nseg == 1 && (rc = seed())) return rc;
+        if ((rc = reverse_segment(r, (long long)seg * every * s, n * s, seg == nseg - 1))) return rc;
     }
     CU(cudaEventRecord(h->ev1, r.st));
     psc::DevAdj rec;
@@ -576,9 +837,12 @@ extern "C" int psc_adjoint_chi2(psc_handle *h, double dt, int nsteps, int every,
         grad_theta[1] = rec.gth[1];
     }
     // gradients with respect to the stored half spectrum: (w_k / N^3) Lambda_k
-    const size_t ncplx = (size_t)r.n;
-    auto to_grad = [&](const void *L, double *out) -> int {
+    auto to_grad = [&](const void *L, double *out, size_t ncplx) -> int {
         if (!out) return PSC_OK;
+        if (!L) {
+            std::memset(out, 0, sizeof(double) * 2 * ncplx);
+            return PSC_OK;
+        }
         int e = psc::hapi::download_real(h, out, L, 2 * ncplx);
         if (e) return e;
         for (size_t i = 0; i < ncplx; ++i) {
@@ -589,7 +853,11 @@ extern "C" int psc_adjoint_chi2(psc_handle *h, double dt, int nsteps, int every,
         }
         return PSC_OK;
     };
-    if ((rc = to_grad(ws->Lf, grad_fk)) || (rc = to_grad(ws->Lp, grad_pik))) return rc;
+    if ((rc = to_grad(ws->Lf, grad_fk, (size_t)r.n)) || (rc = to_grad(ws->Lp, grad_pik, (size_t)r.n))) return rc;
+    const size_t ng = (size_t)6 * r.modes;
+    if (r.gw && ((rc = to_grad(r.gwadj ? ws->Lu : nullptr, grad_uk, ng)) ||
+                 (rc = to_grad(r.gwadj ? ws->Lpu : nullptr, grad_piuk, ng))))
+        return rc;
     // leave the handle at the final state, as psc_step(h, dt, nsteps) would
     if (nseg > 1) {
         if ((rc = restore_state(r, ws->ckpt + (size_t)nseg * ws->ckpt_stride))) return rc;
@@ -599,20 +867,33 @@ extern "C" int psc_adjoint_chi2(psc_handle *h, double dt, int nsteps, int every,
     return PSC_OK;
 }
 
-extern "C" int psc_adjoint_forward_chi2(psc_handle *h, double dt, int nsteps, double *O) {
+extern "C" int psc_adjoint_chi2(psc_handle *h, double dt, int nsteps, int every, double *O, double *grad_fk,
+                                double *grad_pik, double *grad_ad0, double *grad_theta) {
+    return psc_adjoint(h, PSC_OBS_CHI2, dt, nsteps, every, O, grad_fk, grad_pik, nullptr, nullptr, grad_ad0,
+                       grad_theta);
+}
+
+extern "C" int psc_adjoint_forward(psc_handle *h, int observable_id, double dt, int nsteps, double *O) {
     if (!h || !O || nsteps < 1 || !(dt > 0) || !std::isfinite(dt)) return fail(PSC_ERR_ARG, "bad argument");
     int rc;
-    if ((rc = check(h))) return rc;
+    if ((rc = check(h, observable_id))) return rc;
     Run r;
     if ((rc = setup(h, &r))) return rc;
     if ((rc = grow_snap(r.ws, 2))) return rc;
     if ((rc = psc::hapi::evaluate(h, 0))) return rc;
     if ((rc = psc::hapi::step(h, dt, nsteps))) return rc;
-    CU(cudaMemcpyAsync(r.ws->snap, h->b.bg, sizeof(psc::DevBG), cudaMemcpyDeviceToDevice, r.st));
-    if ((rc = observable(r, nullptr))) return rc;
+    if (observable_id == PSC_OBS_RHO_GW) {
+        if ((rc = observable_gw(r, r.ws->Mu))) return rc;   // Mu: scratch for the seed
+    } else {
+        if ((rc = observable(r, nullptr))) return rc;
+    }
     psc::DevAdj rec;
     CU(cudaMemcpyAsync(&rec, r.ws->rec, sizeof(rec), cudaMemcpyDeviceToHost, r.st));
     CU(cudaStreamSynchronize(r.st));
     *O = rec.O;
     return PSC_OK;
+}
+
+extern "C" int psc_adjoint_forward_chi2(psc_handle *h, double dt, int nsteps, double *O) {
+    return psc_adjoint_forward(h, PSC_OBS_CHI2, dt, nsteps, O);
 }

@@ -40,6 +40,8 @@ struct DevAdj {
     double alpha1, alpha2, beta, gamma, delta, eta1, eta2;
     // stage: ph = p + kc (-kn1 k^2 f - kn2 Vp); Lp += c2 Lf
     double c2, kc, kn1, kn2;
+    // GW: transposed source factor -a^(1+alpha) (point), pi_u_half = pi_u + kfu Fu (stage)
+    double etaS, kfu;
     double O;
 };
 

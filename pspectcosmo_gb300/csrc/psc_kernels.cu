@@ -727,6 +727,7 @@ void plan(const psc_params &p, int R, LaunchCfg *cfg) {
     g.nterms = p.model == PSC_MODEL_PHI2 ? 1 : 2;
     g.mask = (p.spectral && p.simulate_inflation) ? 1 : 0;
     g.gsq = p.gsq;
+    g.kIR = p.kIR;
     g.lines_x = g.N * g.H;
     g.lines_z = g.N * g.N;
     g.modes = (long long)g.N * g.N * g.H;

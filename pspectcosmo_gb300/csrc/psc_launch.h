@@ -23,7 +23,7 @@ struct Geo {
     int lines_x;                 // N * H  (X-pass and Y-pass line count per array)
     int lines_z;                 // N * N  (Z-pass line count)
     long long modes, sites;
-    double gsq;
+    double gsq, kIR;
     // batches of R same-configuration lattices: realization r = blockIdx.z owns
     // the arrays at r * fstride (field-sized) / r * gstride (GW-sized), the
     // background record bg[r] and the partial sums at r * pkg_stride / r * pv_stride.
@@ -55,9 +55,10 @@ struct Buffers {
     double *spec;                // spectra accumulators
     int *spec_cnt;
     DevBG *bg;
-    // forward tape of the adjoint (single lattice, no GW; null otherwise): the
-    // stage-point state f, pi (synchronised), V'_k and the real fields f(x)
-    void *tape_f, *tape_p, *tape_vp, *tape_fx;
+    // forward tape of the adjoint (single lattice; null otherwise): the stage-point
+    // state f, pi (synchronised), V'_k and the real fields f(x); with GWs also pi_u
+    // (synchronised) and -kIR^2 k^2 u + S_k (the GW force without its a^(1+alpha))
+    void *tape_f, *tape_p, *tape_vp, *tape_fx, *tape_pu, *tape_fu;
 };
 
 enum ScalarMode {
@@ -103,13 +104,37 @@ cudaError_t reg_stage_f64(const LaunchCfg &cfg, const Buffers &b, int drift, cud
                           int scalar_mode);
 cudaError_t reg_c2r_real_f32(const LaunchCfg &cfg, const Buffers &b, const void *src, int nsrc, cudaStream_t st);
 cudaError_t reg_c2r_real_f64(const LaunchCfg &cfg, const Buffers &b, const void *src, int nsrc, cudaStream_t st);
+// Tiling of the adjoint's scalar Z pass (nf inputs of P = N/32 threads per z line, TL
+// lines per block, at most kAdjZBlocks blocks walking the tiles); its block partial sums
+// have adj_z_blocks() slots per quantity.
+constexpr int kAdjZBlocks = 2 * 152;
+inline int adj_z_tile(int N, int nf) {
+    const int P = N / 32;
+    int t = 1;
+    while (nf * P * t * 2 <= 256) t *= 2;
+    return t;
+}
+inline int adj_z_blocks(int N, int nf) {
+    const int tl = adj_z_tile(N, nf);
+    const int ntiles = (N * N + tl - 1) / tl;
+    return ntiles < kAdjZBlocks ? ntiles : kAdjZBlocks;
+}
+
 // The adjoint's J^T application at a stage point (register engine, one lattice, no GW):
 // Lf += eta1 k^2 Mk + delta k^2 f_tape + r2c(eta2 V''(f(x)) m + gamma V'(f(x))), m = c2r(Mk) / N^3,
 // coefficients from the device record ad; block partial sums of m.V', m.dV'/dgsq, m.dV'/dmu
-// into part[i * nbz + block]. Uses TA and QV as scratch.
+// into part[i * kAdjZBlocks + block]. Uses TA and QV as scratch.
 cudaError_t reg_adj_point_f32(const LaunchCfg &cfg, const Buffers &b, const void *Mk, const void *f_tape,
                               const void *fx_tape, void *Lf, double *part, const DevAdj *ad, cudaStream_t st);
 cudaError_t reg_adj_point_f64(const LaunchCfg &cfg, const Buffers &b, const void *Mk, const void *f_tape,
                               const void *fx_tape, void *Lf, double *part, const DevAdj *ad, cudaStream_t st);
+// The transposed GW source at a stage point (N <= 512, one lattice with GWs):
+// Lf += -a^(1+alpha) sum_a i k_a r2c(T_a), T_a = 2 sum_b (1 + delta_ab) lambda_ab d_b f,
+// lambda = c2r(Mu) / N^3 (six components), f the taped stage-point fields; etaS from ad.
+// Uses TA, TB, TC, QS and Tarr ([3 nf][modes]) as scratch.
+cudaError_t reg_adj_point_gw_f32(const LaunchCfg &cfg, const Buffers &b, const void *Mu, const void *f_tape,
+                                 void *Tarr, void *Lf, const DevAdj *ad, cudaStream_t st);
+cudaError_t reg_adj_point_gw_f64(const LaunchCfg &cfg, const Buffers &b, const void *Mu, const void *f_tape,
+                                 void *Tarr, void *Lf, const DevAdj *ad, cudaStream_t st);
 
 }  // namespace psc

@@ -170,7 +170,9 @@ __global__ void __launch_bounds__(256, 2) kr_fft_x_final(Geo g, const cplx<T> *_
                                                       const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw,
                                                       cplx<T> *__restrict__ tape_f = nullptr,
                                                       cplx<T> *__restrict__ tape_p = nullptr,
-                                                      cplx<T> *__restrict__ tape_vp = nullptr) {
+                                                      cplx<T> *__restrict__ tape_vp = nullptr,
+                                                      cplx<T> *__restrict__ tape_pu = nullptr,
+                                                      cplx<T> *__restrict__ tape_fu = nullptr) {
     using C = cplx<T>;
     using RP = RegPlan<L>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -257,7 +259,7 @@ __global__ void __launch_bounds__(256, 2) kr_fft_x_final(Geo g, const cplx<T> *_
                         accG += wgt * k2 * (f.x * f.x + f.y * f.y);
                     }
                     pk[a] = mk<T>(pf.x + c_open * F.x, pf.y + c_open * F.y);
-                    if (!GW && tape_p) {   // adjoint tape: the synchronised stage-point state
+                    if (tape_p) {   // adjoint tape: the synchronised stage-point state
                         tape_f[a] = f;
                         tape_p[a] = pf;
                         tape_vp[a] = qv;
@@ -283,10 +285,15 @@ __global__ void __launch_bounds__(256, 2) kr_fft_x_final(Geo g, const cplx<T> *_
                 u.y += c_drift * w.y;
                 // a^(1+alpha) (lapl u + 2 sum d_i f d_j f)  (evolution.cpp:586-598)
                 const T l = -kIR2 * k2;
-                const C F = mk<T>(norm1 * (l * u.x + qv.x), norm1 * (l * u.y + qv.y));
+                const C fu = mk<T>(l * u.x + qv.x, l * u.y + qv.y);
+                const C F = mk<T>(norm1 * fu.x, norm1 * fu.y);
                 const C wf = mk<T>(w.x + c_close * F.x, w.y + c_close * F.y);
                 uk[a] = u;
                 puk[a] = mk<T>(wf.x + c_open * F.x, wf.y + c_open * F.y);
+                if (tape_pu) {   // adjoint tape: synchronised pi_u and the force without a^(1+alpha)
+                    tape_pu[a] = wf;
+                    tape_fu[a] = fu;
+                }
             }
     }
 }
@@ -479,10 +486,10 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
 #pragma unroll
             for (int o = 0; o < 8; ++o)
                 if (o < nin) in[o] = slots[o * slot_elems + e];
-            if (!GW && tape_fx) {   // adjoint tape: the real fields (sites 2m, 2m+1 of the line)
+            if (tape_fx) {   // adjoint tape: the real fields (sites 2m, 2m+1 of the line)
 #pragma unroll
                 for (int fl = 0; fl < 2; ++fl)
-                    if (fl < nf) reinterpret_cast<C *>(tape_fx + fl * g.sites + ln * N)[m] = in[fl];
+                    if (fl < nf) reinterpret_cast<C *>(tape_fx + fl * g.sites + ln * N)[m] = in[GW ? fl * 4 : fl];
             }
             C out[8];
 #pragma unroll
@@ -623,13 +630,15 @@ __global__ void __launch_bounds__(256) kr_z_c2r_real(Geo g, const cplx<T> *__res
 template <typename T, int L>
 __global__ void __launch_bounds__(256, 2) kr_zpass_adj(Geo g, const cplx<T> *__restrict__ TA, const T *__restrict__ fx,
                                                     cplx<T> *__restrict__ QV, double *__restrict__ part,
-                                                    const DevAdj *__restrict__ ad, const cplx<T> *__restrict__ tw) {
+                                                    const DevAdj *__restrict__ ad, const cplx<T> *__restrict__ tw,
+                                                    int tl_shift) {
     using C = cplx<T>;
     using RP = RegPlan<L>;
     constexpr int M = L, P = RP::P, LS = ZIdx<L>::LS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *slots = reinterpret_cast<C *>(smem_raw);
-    const int sh = g.tlz_shift, TL = 1 << sh, H = g.H, N = g.N;
+    // tile of TL lines x nf inputs (its own geometry: a GW handle's Z pass has 4 nf inputs)
+    const int sh = tl_shift, TL = 1 << sh, H = g.H, N = g.N;
     const int j = threadIdx.x % P;
     const int t = (threadIdx.x / P) & (TL - 1);
     const int grp = threadIdx.x / (P * TL);
@@ -786,6 +795,200 @@ __global__ void __launch_bounds__(256, 2) kr_fft_x_adj(Geo g, const cplx<T> *__r
             l.x += y0.x + k2 * (eta1 * mv.x + delta * fv.x);
             l.y += y0.y + k2 * (eta1 * mv.y + delta * fv.y);
             Lf[a] = l;
+        }
+}
+
+// ------------------------------------------------------------------ GW adjoint passes
+// Z pass of the transposed GW source at a stage point: per z line, the c2r / N^3 of the
+// field gradients d_x f (TB), d_y f (TC), d_z f (i k_z TA) of every field and of the six
+// adjoint tensor components lambda_ab (LAM), then per site and field
+// T_a = 2 sum_b (1 + delta_ab) lambda_ab d_b f (the transpose of S_ab = 2 sum_f d_a f d_b f,
+// kernel_GW evolution.cpp:581-601) and the r2c of the 3 nf T_a into Tout.
+// nin = 3 nf + 6 inputs; one tile of TL lines per block.
+template <typename T, int L>
+__global__ void __launch_bounds__(256) kr_zpass_adj_gw(Geo g, const cplx<T> *__restrict__ TA,
+                                                     const cplx<T> *__restrict__ TB, const cplx<T> *__restrict__ TC,
+                                                     const cplx<T> *__restrict__ LAM, cplx<T> *__restrict__ Tout,
+                                                     const cplx<T> *__restrict__ tw, int tl_shift) {
+    using C = cplx<T>;
+    using RP = RegPlan<L>;
+    constexpr int M = L, P = RP::P, LS = ZIdx<L>::LS;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *slots = reinterpret_cast<C *>(smem_raw);
+    const int TL = 1 << tl_shift, H = g.H, N = g.N;
+    const int nf = g.nf;
+    const int nin = 3 * nf + 6, nout = 3 * nf;
+    const int j = threadIdx.x % P;
+    const int t = (threadIdx.x / P) & (TL - 1);
+    const int grp = threadIdx.x / (P * TL);
+    const int line = blockIdx.x * TL + t;
+    const bool valid = line < g.lines_z;
+    const size_t slot_elems = (size_t)TL * LS;
+    const T inv_n3 = (T)(1.0 / (double)g.sites);
+    // input grp: fields' gradients first (fld = grp / 3, axis = grp % 3), then lambda_c
+    const bool isgrad = grp < 3 * nf;
+    const int fld = isgrad ? grp / 3 : 0, axis = isgrad ? grp % 3 : 0;
+    const C *src0 = isgrad ? ((axis == 0 ? TB : (axis == 1 ? TC : TA)) + (long long)fld * g.modes)
+                           : (LAM + (long long)(grp - 3 * nf) * g.modes);
+    const ZIdx<L> ix{(int)(grp * slot_elems + t * LS)};
+    // 1. c2r along z (own elements from global memory, partners by shuffle)
+    {
+        C v[16], yv[16], xM = mk<T>(0, 0);
+        const C *src = src0 + (long long)line * H;
+#pragma unroll
+        for (int r = 0; r < 16; ++r) v[r] = valid ? src[j + r * P] : mk<T>(0, 0);
+        if (valid && j == 0) xM = src[M];
+        partners_in<C, M>(v, xM, j, yv);
+        const T kz_ir = (T)g.kIR;
+#pragma unroll
+        for (int r = 0; r < 16; ++r) {
+            const int k = j + r * P;
+            C x = v[r], y = yv[r];
+            if (isgrad && axis == 2) {   // d/dz: i k_z, Nyquist zeroed
+                const T kx = kz_ir * (T)k;
+                const T ky = (k == 0) ? T(0) : kz_ir * (T)(M - k);
+                x = mk<T>(-kx * x.y, kx * x.x);
+                y = mk<T>(-ky * y.y, ky * y.x);
+            }
+            y.y = -y.y;
+            if (k == 0) { x.y = T(0); y.y = T(0); }
+            const C s = cadd(x, y), d = csub(x, y);
+            C w = __ldg(&tw[k]);
+            w.y = -w.y;
+            const C td = cmul(w, d);
+            v[r] = mk<T>(s.x - td.y, s.y + td.x);
+        }
+        fft_reg<C, L, +1>(v, slots, ix, j, tw, N / L);
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+            for (int r = 0; r < RP::RL; ++r) slots[ix(RP::out(j, q, r))] = cscale(v[q * RP::RL + r], inv_n3);
+    }
+    __syncthreads();
+    // 2. T_a = 2 sum_b (1 + delta_ab) lambda_ab d_b f per field and site
+    for (int idx = threadIdx.x; idx < TL * M; idx += blockDim.x) {
+        const int tt = idx / M, m = idx - tt * M;
+        if (blockIdx.x * TL + tt >= g.lines_z) continue;
+        const int e = tt * LS + m + (m >> 4);
+        C lam[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) lam[c] = slots[(3 * nf + c) * slot_elems + e];
+        C dd[2][3];
+#pragma unroll
+        for (int fl = 0; fl < 2; ++fl)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) dd[fl][b] = (fl < nf) ? slots[(fl * 3 + b) * slot_elems + e] : mk<T>(0, 0);
+        // symmetric index of (a, b): 00 0, 01 1, 02 2, 11 3, 12 4, 22 5
+        const int sy[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+#pragma unroll
+        for (int fl = 0; fl < 2; ++fl) {
+            if (fl >= nf) break;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                C o = mk<T>(0, 0);
+#pragma unroll
+                for (int b = 0; b < 3; ++b) {
+                    const T c2 = (a == b) ? T(4) : T(2);
+                    const C l = lam[sy[a][b]], d = dd[fl][b];
+                    o.x += c2 * l.x * d.x;   // sites 2m (x) and 2m+1 (y) separately
+                    o.y += c2 * l.y * d.y;
+                }
+                slots[(fl * 3 + a) * slot_elems + e] = o;
+            }
+        }
+    }
+    __syncthreads();
+    // 3. r2c along z of the 3 nf T_a (groups >= nout only keep the barriers)
+    {
+        const bool act = grp < nout;
+        const ZIdx<L> ixo{(int)((act ? grp : 0) * slot_elems + t * LS)};
+        C v[16];
+#pragma unroll
+        for (int r = 0; r < 16; ++r) v[r] = act ? slots[ixo(j + r * P)] : mk<T>(0, 0);
+        __syncthreads();
+        fft_reg<C, L, -1>(v, slots, ixo, j, tw, N / L, act);
+        C *dst = Tout + (long long)(act ? grp : 0) * g.modes + (long long)line * H;
+        const bool wr = act && valid;
+#pragma unroll
+        for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+            for (int r = 0; r < RP::RL; ++r) {
+                const int k = RP::out(j, q, r);
+                const C zk = v[q * RP::RL + r];
+                const C zc = partner_out<C, M>(v, j, q, r);
+                const C ev = cscale(cadd(zk, zc), T(0.5));
+                const C dq = cscale(csub(zk, zc), T(0.5));
+                const C od = mk<T>(dq.y, -dq.x);
+                const C w = __ldg(&tw[k]);
+                if (wr) dst[k] = cadd(ev, cmul(w, od));
+            }
+        if (wr && j == 0) dst[M] = mk<T>(v[0].x - v[0].y, T(0));
+    }
+}
+
+// X forward transform of the three T_a of field blockIdx.y and the transposed source
+// gradient: Lf += etaS sum_a i k_a fft_x(T_a), k_a with the Nyquist bin zeroed
+// (field_1st_derivative evolution.cpp:466-578), etaS = -a^(1+alpha).
+template <typename T, int L>
+__global__ void __launch_bounds__(256, 2) kr_fft_x_gwadj(Geo g, const cplx<T> *__restrict__ Tin,
+                                                      cplx<T> *__restrict__ Lf, const DevAdj *__restrict__ ad,
+                                                      const cplx<T> *__restrict__ tw) {
+    using C = cplx<T>;
+    using RP = RegPlan<L>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *sm = reinterpret_cast<C *>(smem_raw);
+    const int sh = g.tlx_shift, TL = 1 << sh, N = g.N, H = g.H;
+    const int t = threadIdx.x & (TL - 1), j = threadIdx.x >> sh;
+    const int line = blockIdx.x * TL + t;
+    const bool valid = line < g.lines_x;
+    const long long stride = g.lines_x;
+    const int fl = blockIdx.y;
+    auto ix = [&](int n) { return n * TL + t; };
+    const T kIR = (T)g.kIR;
+    const int y = line / H, kz = line - y * H;
+    const T ky = (y == (N >> 1)) ? T(0) : kIR * (T)pcoord(y, N);
+    const T kzv = (kz == (N >> 1)) ? T(0) : kIR * (T)kz;
+    C acc[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) acc[r] = mk<T>(0, 0);
+#pragma unroll 1
+    for (int a = 0; a < 3; ++a) {
+        if (a) __syncthreads();   // the exchange buffer is free again
+        const long long base = (long long)(fl * 3 + a) * g.modes + line;
+        C v[16];
+#pragma unroll
+        for (int r = 0; r < 16; ++r) v[r] = valid ? Tin[base + (long long)(j + r * RP::P) * stride] : mk<T>(0, 0);
+        fft_reg<C, L, -1>(v, sm, ix, j, tw, N / L);
+#pragma unroll
+        for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+            for (int r = 0; r < RP::RL; ++r) {
+                const int n = RP::out(j, q, r);
+                const T kk = (a == 0) ? ((n == (N >> 1)) ? T(0) : kIR * (T)pcoord(n, N)) : (a == 1 ? ky : kzv);
+                const C z = v[q * RP::RL + r];
+                C &o = acc[q * RP::RL + r];
+                o.x -= kk * z.y;
+                o.y += kk * z.x;
+            }
+    }
+    if (!valid) return;
+    const T etaS = (T)ad->etaS;
+    const long long base = (long long)fl * g.modes + line;
+    C lv[16];
+#pragma unroll
+    for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+        for (int r = 0; r < RP::RL; ++r) lv[q * RP::RL + r] = Lf[base + (long long)RP::out(j, q, r) * stride];
+#pragma unroll
+    for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+        for (int r = 0; r < RP::RL; ++r) {
+            C l = lv[q * RP::RL + r];
+            const C o = acc[q * RP::RL + r];
+            l.x += etaS * o.x;
+            l.y += etaS * o.y;
+            Lf[base + (long long)RP::out(j, q, r) * stride] = l;
         }
 }
 

@@ -13,6 +13,16 @@ struct RegLaunch {
     using C = cplx<T>;
     static constexpr int M = N / 2;
 
+    static void gw_adj_tile(int nf, int *tl, int *sh);
+    // the scalar adjoint Z pass (adj_z_tile / adj_z_blocks, psc_launch.h)
+    static void zadj_tile(int nf, int *tl, int *sh) {
+        const int t = adj_z_tile(N, nf);
+        int s = 0;
+        while ((1 << s) < t) ++s;
+        *tl = t;
+        *sh = s;
+    }
+
     static cudaError_t configure(const LaunchCfg &cfg) {
         const int sxy = (int)cfg.smem_xy, sz = (int)cfg.smem_z;
         cudaError_t e;
@@ -34,8 +44,18 @@ struct RegLaunch {
         SETA((kr_zpass<T, M, false>), sz);
         SETA((kr_zpass<T, M, true>), sz);
         SETA((kr_z_c2r_real<T, M>), (int)((256 / (M / 16)) * ZIdx<M>::LS * sizeof(C)));
-        SETA((kr_zpass_adj<T, M>), sz);
+        {
+            int tl = 1, sh = 0;
+            zadj_tile(cfg.g.nf, &tl, &sh);
+            SETA((kr_zpass_adj<T, M>), (int)(cfg.g.nf * tl * ZIdx<M>::LS * sizeof(C)));
+        }
         SETA((kr_fft_x_adj<T, N>), sxy);
+        SETA((kr_fft_x_gwadj<T, N>), sxy);
+        {
+            int tl = 1, sh = 0;
+            gw_adj_tile(cfg.g.nf, &tl, &sh);
+            SETA((kr_zpass_adj_gw<T, M>), (int)((3 * cfg.g.nf + 6) * tl * ZIdx<M>::LS * sizeof(C)));
+        }
 #undef SETA
         return cudaSuccess;
     }
@@ -59,7 +79,8 @@ struct RegLaunch {
             mark(1);
             kr_ifft_y<T, N, true><<<gx, txy, cfg.smem_xy, st>>>(g, TA, TB, TC, b.bg, tw);
             mark(2);
-            kr_zpass<T, M, true><<<dim3(cfg.nbz, 1, R), tz, cfg.smem_z, st>>>(g, TA, TB, TC, QV, QS, b.partV, b.bg, tw);
+            kr_zpass<T, M, true><<<dim3(cfg.nbz, 1, R), tz, cfg.smem_z, st>>>(g, TA, TB, TC, QV, QS, b.partV, b.bg, tw,
+                                                                            (T *)b.tape_fx);
         } else {
             if (drift) kr_ifft_x<T, N, false, true><<<gx, txy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
             else kr_ifft_x<T, N, false, false><<<gx, txy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
@@ -85,7 +106,9 @@ struct RegLaunch {
         mark(4);
         const dim3 gf(cfg.nbx, nj, R);
         if (g.gw)
-            kr_fft_x_final<T, N, true><<<gf, txy, cfg.smem_xf, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw);
+            kr_fft_x_final<T, N, true><<<gf, txy, cfg.smem_xf, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw,
+                                                                      (C *)b.tape_f, (C *)b.tape_p, (C *)b.tape_vp,
+                                                                      (C *)b.tape_pu, (C *)b.tape_fu);
         else
             kr_fft_x_final<T, N, false><<<gf, txy, cfg.smem_xf, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw,
                                                                        (C *)b.tape_f, (C *)b.tape_p, (C *)b.tape_vp);
@@ -132,7 +155,11 @@ struct RegLaunch {
         const dim3 gx(cfg.nbx, g.nf);
         kr_ifft_x<T, N, false, false><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, (C *)Mk, nullptr, TA, nullptr, b.bg, tw);
         kr_ifft_y<T, N, false><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, TA, nullptr, nullptr, b.bg, tw);
-        kr_zpass_adj<T, M><<<cfg.nbz, cfg.thr_z, cfg.smem_z, st>>>(g, TA, (const T *)fx_tape, QV, part, ad, tw);
+        int tl = 1, sh = 0;
+        zadj_tile(g.nf, &tl, &sh);
+        const int nbz = adj_z_blocks(N, g.nf);
+        kr_zpass_adj<T, M><<<nbz, g.nf * (M / 16) * tl, (size_t)g.nf * tl * ZIdx<M>::LS * sizeof(C), st>>>(
+            g, TA, (const T *)fx_tape, QV, part, ad, tw, sh);
         ArrList8 al{};
         for (int f = 0; f < g.nf; ++f) al.p[f] = QV + (long long)f * g.modes;
         kr_fft_y<T, N><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, al, tw);
@@ -140,7 +167,46 @@ struct RegLaunch {
                                                                  tw);
         return cudaGetLastError();
     }
+
+    // transposed GW source at a stage point (one lattice with GWs): the field gradients of
+    // the taped f (X, Y inverse GW passes into TA, TB, TC), the six adjoint components Mu
+    // (X, Y inverse into QS), the GW adjoint Z pass into Tarr (3 nf arrays), the Y forward
+    // pass and the X forward pass adding etaS sum_a i k_a T_a into Lf.
+    static cudaError_t adj_point_gw(const LaunchCfg &cfg, const Buffers &b, const void *Mu, const void *f_tape,
+                                    void *Tarr, void *Lf, const DevAdj *ad, cudaStream_t st) {
+        const Geo &g = cfg.g;
+        const C *tw = reinterpret_cast<const C *>(b.tw);
+        C *TA = (C *)b.TA, *TB = (C *)b.TB, *TC = (C *)b.TC, *QS = (C *)b.QS;
+        const dim3 gx(cfg.nbx, g.nf), g6(cfg.nbx, 6);
+        kr_ifft_x<T, N, true, false><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, (C *)f_tape, nullptr, TA, TB, b.bg, tw);
+        kr_ifft_y<T, N, true><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, TA, TB, TC, b.bg, tw);
+        kr_ifft_x<T, N, false, false><<<g6, cfg.thr_xy, cfg.smem_xy, st>>>(g, (C *)Mu, nullptr, QS, nullptr, b.bg, tw);
+        kr_ifft_y<T, N, false><<<g6, cfg.thr_xy, cfg.smem_xy, st>>>(g, QS, nullptr, nullptr, b.bg, tw);
+        int tl = 1, sh = 0;
+        gw_adj_tile(g.nf, &tl, &sh);
+        const int nin = 3 * g.nf + 6, P = M / 16;
+        const size_t smem = (size_t)nin * tl * ZIdx<M>::LS * sizeof(C);
+        kr_zpass_adj_gw<T, M><<<(g.lines_z + tl - 1) / tl, nin * P * tl, smem, st>>>(g, TA, TB, TC, QS, (C *)Tarr, tw,
+                                                                                    sh);
+        ArrList8 al{};
+        for (int i = 0; i < 3 * g.nf; ++i) al.p[i] = (C *)Tarr + (long long)i * g.modes;
+        kr_fft_y<T, N><<<dim3(cfg.nbx, 3 * g.nf), cfg.thr_xy, cfg.smem_xy, st>>>(g, al, tw);
+        kr_fft_x_gwadj<T, N><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, (const C *)Tarr, (C *)Lf, ad, tw);
+        return cudaGetLastError();
+    }
 };
+
+// the GW adjoint Z pass: 3 nf + 6 inputs of P = N/32 threads each per line
+template <typename T, int N>
+void RegLaunch<T, N>::gw_adj_tile(int nf, int *tl, int *sh) {
+    const int nin = 3 * nf + 6, P = (N / 2) / 16;
+    int t = 1;
+    while (nin * P * t * 2 <= 256) t *= 2;
+    int s = 0;
+    while ((1 << s) < t) ++s;
+    *tl = t;
+    *sh = s;
+}
 
 template <typename T>
 struct RegDispatch {
@@ -167,6 +233,13 @@ struct RegDispatch {
                                        cudaStream_t st) {                                                         \
         return RegDispatch<T>::on(cfg.g.N, [&](auto L) {                                                         \
             return decltype(L)::adj_point(cfg, b, Mk, f_tape, fx_tape, Lf, part, ad, st);                        \
+        });                                                                                                      \
+    }                                                                                                            \
+    cudaError_t reg_adj_point_gw_##SUFFIX(const LaunchCfg &cfg, const Buffers &b, const void *Mu,               \
+                                          const void *f_tape, void *Tarr, void *Lf, const DevAdj *ad,             \
+                                          cudaStream_t st) {                                                      \
+        return RegDispatch<T>::on(cfg.g.N, [&](auto L) {                                                         \
+            return decltype(L)::adj_point_gw(cfg, b, Mu, f_tape, Tarr, Lf, ad, st);                              \
         });                                                                                                      \
     }                                                                                                            \
     cudaError_t reg_configure_##SUFFIX(const LaunchCfg &cfg) {                                                   \

@@ -94,6 +94,8 @@ def load_library(path: str | None = None):
     L.psc_batch_means.argtypes = [P, ctypes.c_int, D]
     L.psc_adjoint_chi2.argtypes = [P, ctypes.c_double, ctypes.c_int, ctypes.c_int, D, D, D, D, D]
     L.psc_adjoint_forward_chi2.argtypes = [P, ctypes.c_double, ctypes.c_int, D]
+    L.psc_adjoint.argtypes = [P, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, D, D, D, D, D, D, D]
+    L.psc_adjoint_forward.argtypes = [P, ctypes.c_int, ctypes.c_double, ctypes.c_int, D]
     L.psc_strerror.argtypes = [ctypes.c_int]
     L.psc_strerror.restype = ctypes.c_char_p
     L.psc_last_error.argtypes = []
@@ -103,7 +105,7 @@ def load_library(path: str | None = None):
                  "psc_means", "psc_last_step_ms", "psc_time_passes", "psc_pass_bytes", "psc_batch_create",
                  "psc_batch_size", "psc_batch_groups", "psc_batch_init_ic", "psc_batch_step", "psc_batch_last_step_ms",
                  "psc_batch_set_state", "psc_batch_get_state", "psc_batch_spectra", "psc_batch_energies",
-                 "psc_batch_means", "psc_adjoint_chi2", "psc_adjoint_forward_chi2"):
+                 "psc_batch_means", "psc_adjoint_chi2", "psc_adjoint_forward_chi2", "psc_adjoint", "psc_adjoint_forward"):
         getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L
@@ -227,6 +229,33 @@ class Lattice:
         _check(self._L.psc_adjoint_chi2(self._h, float(dt), int(nsteps), int(every), ctypes.byref(O), _dp(gf), _dp(gp),
                                         ctypes.byref(gad), _dp(gth)), "psc_adjoint_chi2")
         return dict(O=O.value, grad_f_k=gf, grad_pi_k=gp, grad_ad0=gad.value, grad_theta=gth)
+
+    OBSERVABLES = {"chi2": 0, "rho_gw": 1}
+
+    def adjoint(self, observable: str, dt: float, nsteps: int, every: int = 0, fields: bool = True) -> dict:
+        """O (observable "chi2" = <chi^2> or "rho_gw" = the GW energy density) after nsteps and
+        its gradient with respect to the current state: grad_f_k, grad_pi_k and, on a GW lattice,
+        grad_u_k, grad_pi_u_k (dO/dRe + i dO/dIm per stored mode), grad_ad0, grad_theta =
+        (dO/dgsq, dO/dmu). The lattice is left at the final state."""
+        p = self.p
+        O, gad = ctypes.c_double(), ctypes.c_double()
+        gf = np.zeros((p.nflds, p.modes), np.complex128) if fields else None
+        gp = np.zeros((p.nflds, p.modes), np.complex128) if fields else None
+        gu = np.zeros((6, p.modes), np.complex128) if (fields and p.with_gw) else None
+        gpu = np.zeros((6, p.modes), np.complex128) if (fields and p.with_gw) else None
+        gth = np.zeros(2)
+        _check(self._L.psc_adjoint(self._h, self.OBSERVABLES[observable], float(dt), int(nsteps), int(every),
+                                   ctypes.byref(O), _dp(gf), _dp(gp), _dp(gu), _dp(gpu), ctypes.byref(gad), _dp(gth)),
+               "psc_adjoint")
+        return dict(O=O.value, grad_f_k=gf, grad_pi_k=gp, grad_u_k=gu, grad_pi_u_k=gpu, grad_ad0=gad.value,
+                    grad_theta=gth)
+
+    def adjoint_forward(self, observable: str, dt: float, nsteps: int) -> float:
+        """O after nsteps of the product step from a''(0) = A(state(0)) (no gradient)."""
+        O = ctypes.c_double()
+        _check(self._L.psc_adjoint_forward(self._h, self.OBSERVABLES[observable], float(dt), int(nsteps),
+                                           ctypes.byref(O)), "psc_adjoint_forward")
+        return O.value
 
     def adjoint_forward_chi2(self, dt: float, nsteps: int) -> float:
         """O = <chi^2> after nsteps of the adjoint's own (unfused) forward map."""

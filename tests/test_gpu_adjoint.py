@@ -190,3 +190,121 @@ def test_unsupported_configurations_are_rejected(psc_lib):
         with pytest.raises(PscError) as e:
             lat.adjoint_chi2(0.005, 2)
         assert e.value.code == -1
+
+
+# ---------------------------------------------------------------- rho_GW (GW energy density)
+def _gw_params(N=32, precision=64):
+    from pspectcosmo_gb300.params import Params
+
+    p = Params.preheating(N=N, vv=2, spectral=0, with_gw=1)
+    p.precision = precision
+    return p
+
+
+def _gw_setup(p, zero_gw):
+    from pspectcosmo_gb300 import generate_ic
+
+    f, pi, u, pu, info = generate_ic(p)
+    z = 0.0 if zero_gw else 1.0
+    return f, pi, z * u, z * pu, info
+
+
+def _gw_lattice(p, f, pi, u, pu, info, ad=None, add=None):
+    from pspectcosmo_gb300 import Lattice
+
+    lat = Lattice(p)
+    lat.set_state(f, pi, info["a"], info["ad"] if ad is None else ad, info["add_printed"] if add is None else add,
+                  u, pu)
+    return lat
+
+
+def _gw_ref(p, f, pi, u, pu, info, dt, nsteps):
+    fs = p.fStar if p.fStar > 0 else p.MPl
+    lat = A.Lattice(p.N, p.kIR, p.nflds, p.gsq, alpha=p.alpha, fs_over_mpl2=(fs / p.MPl) ** 2, vv=p.vv, gw=True)
+    sh, sg = (p.nflds, p.N, p.N, p.N // 2 + 1), (6, p.N, p.N, p.N // 2 + 1)
+    st0 = [f.reshape(sh), pi.reshape(sh), info["a"], info["ad"], 0.0, u.reshape(sg), pu.reshape(sg)]
+    O, gf, gp, _, gb, gth, gu, gpu = A.gradient(lat, st0, dt, nsteps, observable="rho_gw")
+    return O, gf.reshape(f.shape), gp.reshape(pi.shape), gu.reshape(u.shape), gpu.reshape(pu.shape), gb, gth, lat
+
+
+@pytest.mark.parametrize("zero_gw", [True, False])
+def test_rho_gw_gradients_match_fp64_adjoint(psc_lib, zero_gw):
+    """rho_GW generated from u = pi_u = 0 by the scalar source, and from the GW vacuum."""
+    p = _gw_params()
+    f, pi, u, pu, info = _gw_setup(p, zero_gw)
+    dt, nsteps = 0.005, 6
+    with _gw_lattice(p, f, pi, u, pu, info) as lat:
+        g = lat.adjoint("rho_gw", dt, nsteps, 4)
+    O, gf, gp, gu, gpu, gb, gth, _ = _gw_ref(p, f, pi, u, pu, info, dt, nsteps)
+    assert abs(g["O"] / O - 1) < FP64_TOL
+    assert rel(g["grad_f_k"], gf) < FP64_TOL
+    assert rel(g["grad_pi_k"], gp) < FP64_TOL
+    assert rel(g["grad_u_k"], gu) < FP64_TOL
+    assert rel(g["grad_pi_u_k"], gpu) < FP64_TOL
+    assert abs(g["grad_ad0"] / gb - 1) < FP64_TOL
+    for k in range(2):
+        assert abs(g["grad_theta"][k] - gth[k]) <= FP64_TOL * abs(gth[k]) + 1e-300, k
+
+
+def test_rho_gw_is_the_product_energy(psc_lib):
+    """The adjoint's rho_GW is psc_energies' rho_GW of the same final state (energy(), the GW walk)."""
+    p = _gw_params()
+    f, pi, u, pu, info = _gw_setup(p, False)
+    with _gw_lattice(p, f, pi, u, pu, info) as lat:
+        O = lat.adjoint_forward("rho_gw", 0.005, 5)
+        rho = lat.energies()["rho_gw"]
+    assert abs(O / rho - 1) < 1e-12
+
+
+def test_rho_gw_gradients_against_device_central_differences(psc_lib):
+    p = _gw_params()
+    f, pi, u, pu, info = _gw_setup(p, True)
+    dt, nsteps = 0.005, 6
+    with _gw_lattice(p, f, pi, u, pu, info) as lat:
+        g = lat.adjoint("rho_gw", dt, nsteps)
+    N = p.N
+    rng = np.random.default_rng(13)
+
+    def run(ff, pp, ad=None, gsq=None):
+        q = _gw_params()
+        if gsq is not None:
+            q.gsq = gsq
+        with _gw_lattice(q, ff, pp, u, pu, info, ad) as lat:
+            return lat.adjoint_forward("rho_gw", dt, nsteps)
+
+    for name in ("f", "pi"):
+        d = np.fft.rfftn(rng.standard_normal((2, N, N, N)), axes=(-3, -2, -1)).reshape(f.shape)
+        base = (f if name == "f" else pi).copy()
+        base[:, 0] = 0
+        d *= 1e-3 * np.abs(base).mean() / np.abs(d).mean()
+        if name == "f":
+            fd = (run(f + d, pi) - run(f - d, pi)) / 2
+        else:
+            fd = (run(f, pi + d) - run(f, pi - d)) / 2
+        pred = float(np.sum(np.real(np.conj(g["grad_f_k" if name == "f" else "grad_pi_k"]) * d)))
+        assert abs(fd - pred) <= FD_TOL * abs(fd), (name, fd, pred)
+    hb = 1e-6 * abs(info["ad"])
+    fd = (run(f, pi, ad=info["ad"] + hb) - run(f, pi, ad=info["ad"] - hb)) / 2
+    assert abs(fd - g["grad_ad0"] * hb) <= FD_TOL * abs(fd), ("ad", fd, g["grad_ad0"] * hb)
+    h = 1e-4 * p.gsq
+    fd = (run(f, pi, gsq=p.gsq + h) - run(f, pi, gsq=p.gsq - h)) / 2
+    assert abs(fd - g["grad_theta"][0] * h) <= FD_TOL * abs(fd), ("gsq", fd, g["grad_theta"][0] * h)
+
+
+def test_rho_gw_checkpoint_spacing_and_fp32(psc_lib):
+    p = _gw_params()
+    f, pi, u, pu, info = _gw_setup(p, True)
+    dt, nsteps = 0.005, 6
+    out = []
+    for every in (1, 0):
+        with _gw_lattice(p, f, pi, u, pu, info) as lat:
+            out.append(lat.adjoint("rho_gw", dt, nsteps, every))
+    assert abs(out[1]["O"] / out[0]["O"] - 1) < 1e-13
+    for k in ("grad_f_k", "grad_pi_k", "grad_pi_u_k"):
+        assert rel(out[1][k], out[0][k]) < 1e-12, k
+    q = _gw_params(precision=32)
+    with _gw_lattice(q, f, pi, u, pu, info) as lat:
+        g32 = lat.adjoint("rho_gw", dt, nsteps)
+    assert abs(g32["O"] / out[1]["O"] - 1) < 5e-3
+    assert rel(g32["grad_f_k"], out[1]["grad_f_k"]) < 5e-3
+    assert rel(g32["grad_pi_u_k"], out[1]["grad_pi_u_k"]) < 5e-3
