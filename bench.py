@@ -44,11 +44,12 @@ CONFIGS = {
     # phi0 ~ U[10, 12] (host RNG seed 12345), Yoshida-4, one graph per step for all of them
     "ensemble_mixed": (dict(kind="ensemble"), 1e-4,
                        "ensemble: 256 x 32^3 + 64 x 64^3 + 8 x 128^3 single-field inflation, Yoshida-4"),
-    # one timed step = one gradient of <chi^2> after ADJ_STEPS model steps (checkpoints every
-    # ADJ_EVERY steps, each segment recomputed once), FP32 fields / FP64 background
-    "adjoint_128": (dict(kind="preheating", N=128, spectral=0, with_gw=0, vv=2), 0.005,
-                    "adjoint of <chi^2> after 2000 steps: 128^3 two-field preheating, velocity Verlet, "
-                    "checkpoints every 100 steps"),
+    # one timed step = the gradients of <chi^2> and of rho_GW after ADJ_STEPS model steps of the
+    # two-field + GW lattice (checkpoints every ADJ_EVERY steps, each segment recomputed once),
+    # FP32 fields / FP64 background
+    "adjoint_128": (dict(kind="preheating", N=128, spectral=0, with_gw=1, vv=2), 0.005,
+                    "adjoint of <chi^2> and rho_GW after 2000 steps: 128^3 two-field preheating + GW, "
+                    "velocity Verlet, checkpoints every 100 steps"),
 }
 ADJ_STEPS, ADJ_EVERY = 2000, 100
 
@@ -268,7 +269,7 @@ def run_adjoint(args):
     st0 = lat.get_state()
 
     def reset():
-        lat.set_state(st0["f_k"], st0["pi_k"], st0["a"], st0["ad"], st0["add"])
+        lat.set_state(st0["f_k"], st0["pi_k"], st0["a"], st0["ad"], st0["add"], st0["u_k"], st0["pi_u_k"])
 
     # forward alone on the product's captured step, the same ADJ_STEPS steps
     reset()
@@ -278,16 +279,21 @@ def run_adjoint(args):
     fwd_ms = lat.last_step_ms()
     for _ in range(args.warmup):
         reset()
-        lat.adjoint_chi2(dt, ADJ_STEPS, ADJ_EVERY, fields=False)
+        lat.adjoint("rho_gw", dt, ADJ_STEPS, ADJ_EVERY, fields=False)
     clocks = ClockSampler(local)
     barrier(dist)
     clocks.start()
     barrier(dist)
-    dev_ms = 0.0
+    # one step: both gradients (<chi^2> and rho_GW) from the same initial state
+    dev_ms, ms_obs = 0.0, {"chi2": 0.0, "rho_gw": 0.0}
+    obs = {}
     for _ in range(args.steps):
-        reset()
-        g = lat.adjoint_chi2(dt, ADJ_STEPS, ADJ_EVERY, fields=False)
-        dev_ms += lat.last_step_ms()
+        for name in ("chi2", "rho_gw"):
+            reset()
+            g = lat.adjoint(name, dt, ADJ_STEPS, ADJ_EVERY, fields=False)
+            dev_ms += lat.last_step_ms()
+            ms_obs[name] += lat.last_step_ms()
+            obs[name] = g
     barrier(dist)
     ms = max_over_ranks(dist, dev_ms)
     clk = clocks.stop()
@@ -296,10 +302,11 @@ def run_adjoint(args):
     barrier(dist)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        reset()
-        g = lat.adjoint_chi2(dt, ADJ_STEPS, ADJ_EVERY)
+        for name in ("chi2", "rho_gw"):
+            reset()
+            lat.adjoint(name, dt, ADJ_STEPS, ADJ_EVERY)
     e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
-    state_bytes = 2 * p.nflds * p.modes * 16
+    state_bytes = (2 * p.nflds + 12) * p.modes * 16
     if rank == 0:
         line = {"metric": "site-steps/s", "value": value, "unit": "site-steps/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -311,15 +318,18 @@ def run_adjoint(args):
                            "precision": f"fp{p.precision} fields, fp64 background/reductions/adjoint scalars",
                            "parallelism": f"replicas x{world}" if world > 1 else "single lattice",
                            "l2": "arrays > 129 MB L2 (no flush needed)"},
-                "adjoint_over_forward": (ms / args.steps) / fwd_ms,
+                "adjoint_over_forward": {k: (v / args.steps) / fwd_ms for k, v in ms_obs.items()},
                 "forward_ms": fwd_ms,
-                "observable": g["O"], "grad_theta": list(map(float, g["grad_theta"])),
+                "adjoint_ms": {k: v / args.steps for k, v in ms_obs.items()},
+                "observables": {k: {"O": v["O"], "grad_theta": list(map(float, v["grad_theta"])),
+                                    "grad_ad0": v["grad_ad0"]} for k, v in obs.items()},
                 "e2e": {"value": world * p.sites * ADJ_STEPS * args.steps / e2e_s, "unit": "site-steps/s",
-                        "h2d_bytes_per_step": state_bytes + 24, "d2h_bytes_per_step": state_bytes + 32},
+                        "h2d_bytes_per_step": 2 * (state_bytes + 24),
+                        "d2h_bytes_per_step": 2 * (state_bytes + 32)},
                 "roofline": None,
                 "cpu_baseline": None,
                 "clocks": clk,
-                "gpu_launches": int(ADJ_STEPS * p.stages * (2 * 6 + 11) + 16)}
+                "gpu_launches": int(ADJ_STEPS * p.stages * (2 * (2 * 6 + 11) + 13) + 32)}
         print(json.dumps(line), flush=True)
     lat.close()
     if dist is not None:
