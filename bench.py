@@ -402,6 +402,30 @@ def run_ours(args):
     launches_per_stage = 6
     gpu_launches = 1 + 7 + p.stages * launches_per_stage * args.steps
 
+    # the same K steps in FP64 (the plain method): its rate and the FP32 spectrum error
+    # against it (spectra() bins, max-norm relative over bins; GW h^2, hdot^2 when on)
+    fp_cmp = None
+    if p.precision == 32 and rank == 0 and not args.no_fp64:
+        q = p.copy()
+        q.precision = 64
+        lat64 = Lattice(q)
+        lat64.initialize()
+        lat64.evolve(dt, args.steps)
+        ms64 = lat64.last_step_ms()
+        s32, s64 = lat.spectra_raw(), lat64.spectra_raw()
+        lat64.close()
+
+        def relmax(a, b):
+            d = float(np.abs(b).max())
+            return float(np.abs(a - b).max() / d) if d > 0 else 0.0
+
+        err = {k: relmax(s32[k], s64[k]) for k in ("f2", "pi2", "n2") + (("h2", "hdot2") if p.with_gw else ())}
+        fp_cmp = {"fp64_value": p.sites * args.steps / (ms64 / 1e3), "fp64_ms_per_step": ms64 / args.steps,
+                  "fp32_over_fp64": (ms64 / args.steps) / (ms / args.steps),
+                  "spectrum_rel_err": err, "stated_tolerance": {"f2": 1e-3, "pi2": 1e-3, "n2": 1e-2, "h2": 1e-3,
+                                                                  "hdot2": 1e-3},
+                  "after_steps": args.steps}
+
     if rank == 0:
         cpu = cpu_sample(p, dt, budget_s=20.0) if (world == 1 and not args.no_cpu) else None
         line = {
@@ -422,6 +446,7 @@ def run_ours(args):
                          "step": {"algorithmic_bytes_per_site_step": algorithmic_bytes_per_site_step(p),
                                   "achieved": step_achieved, "frac": step_achieved / peak}},
             "passes_ms": passes,
+            "fp32_vs_fp64": fp_cmp,
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": gpu_launches,
@@ -441,6 +466,7 @@ def main():
     ap.add_argument("--config", default="preheat_gw_256", choices=sorted(CONFIGS))
     ap.add_argument("--precision", type=int, default=32, choices=[32, 64])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

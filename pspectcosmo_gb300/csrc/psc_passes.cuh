@@ -133,13 +133,54 @@ __global__ void __launch_bounds__(256, 2) kr_ifft_y(Geo g, cplx<T> *__restrict__
     bg += blockIdx.z;
     const T kIR = (T)bg->kIR;
     if (GW) {
-        // the y-derivative reads TA before TA is transformed in place; one copy of the
-        // transform code for the three arrays keeps the register allocation spill-free
+        // This thread's TA and TB elements are copied into two shared staging tiles by
+        // cp.async at once (every load in flight together, TA read from HBM once); then
+        // three transforms from the tiles: d/dy TA -> TC, TA -> TA, TB -> TB (one copy of
+        // the transform code keeps the register allocation spill-free).
+        using RP = RegPlan<L>;
+        const int sh = g.tlx_shift, TL = 1 << sh;
+        const int t = threadIdx.x & (TL - 1), j = threadIdx.x >> sh;
+        const int line = blockIdx.x * TL + t;
+        const bool valid = line < g.lines_x;
+        const int x = line / g.H, kz = line - x * g.H;
+        const long long base = off + (long long)x * g.N * g.H + kz;
+        const long long stride = g.H;
+        auto ix = [&](int n) { return n * TL + t; };
+        C *stA = sm + TL * L, *stB = stA + TL * L;
+        if (valid) {
+#pragma unroll
+            for (int r = 0; r < 16; ++r) {
+                const int n = j + r * RP::P;
+                cp_async_elem(stA + ix(n), TA + base + (long long)n * stride);
+                cp_async_elem(stB + ix(n), TB + base + (long long)n * stride);
+            }
+        }
+        cp_async_commit();
+        cp_async_wait_all();   // own elements only: no barrier needed to read them
 #pragma unroll 1
         for (int a = 0; a < 3; ++a) {
-            const cplx<T> *src = (a == 2 ? TB : TA) + off;
-            cplx<T> *dst = (a == 0 ? TC : (a == 1 ? TA : TB)) + off;
-            ry_tile<T, L, +1>(g, src, dst, a == 0, kIR, sm, tw);
+            if (a) __syncthreads();   // the exchange buffer is free again
+            const C *st = (a == 2) ? stB : stA;
+            C v[16];
+#pragma unroll
+            for (int r = 0; r < 16; ++r) {
+                const int n = j + r * RP::P;
+                C e = valid ? st[ix(n)] : mk<T>(0, 0);
+                if (a == 0) {
+                    const T ky = (n == (g.N >> 1)) ? T(0) : kIR * (T)pcoord(n, g.N);
+                    e = mk<T>(-ky * e.y, ky * e.x);
+                }
+                v[r] = e;
+            }
+            fft_reg<C, L, +1>(v, sm, ix, j, tw, g.N / L);
+            C *dst = (a == 0 ? TC : (a == 1 ? TA : TB));
+            if (valid) {
+#pragma unroll
+                for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+                    for (int r = 0; r < RP::RL; ++r)
+                        dst[base + (long long)RP::out(j, q, r) * stride] = v[q * RP::RL + r];
+            }
         }
     } else {
         ry_tile<T, L, +1>(g, TA + off, TA + off, false, kIR, sm, tw);
