@@ -394,7 +394,7 @@ __device__ __forceinline__ C partner_out(const C (&v)[16], int j, int q, int r) 
 // then nin staging slots. The eight-input GW pass, bound by its instruction stream,
 // runs one tile per block and loads its lines straight into the work slots.
 template <typename T, int L, bool GW>
-__global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restrict__ TA, const cplx<T> *__restrict__ TB,
+__global__ void __launch_bounds__(256, GW ? 3 : 2) kr_zpass(Geo g, const cplx<T> *__restrict__ TA, const cplx<T> *__restrict__ TB,
                                                 const cplx<T> *__restrict__ TC, cplx<T> *__restrict__ QV,
                                                 cplx<T> *__restrict__ QS, double *__restrict__ partV,
                                                 const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw,
