@@ -37,7 +37,7 @@ struct RegLaunch {
         SETA((kr_ifft_x<T, N, false, false>), sxy);
         SETA((kr_ifft_x<T, N, true, false>), sxy);
         SETA((kr_ifft_y<T, N, false>), sxy);
-        SETA((kr_ifft_y<T, N, true>), (int)cfg.smem_xf);
+        SETA((kr_ifft_y<T, N, true>), 3 * sxy);   // exchange tile + TA and TB staging tiles
         SETA((kr_fft_y<T, N>), sxy);
         SETA((kr_fft_x_final<T, N, false>), (int)cfg.smem_xf);
         SETA((kr_fft_x_final<T, N, true>), (int)cfg.smem_xf);
@@ -77,7 +77,7 @@ struct RegLaunch {
             if (drift) kr_ifft_x<T, N, true, true><<<gx, txy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
             else kr_ifft_x<T, N, true, false><<<gx, txy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
             mark(1);
-            kr_ifft_y<T, N, true><<<gx, txy, cfg.smem_xf, st>>>(g, TA, TB, TC, b.bg, tw);
+            kr_ifft_y<T, N, true><<<gx, txy, 3 * cfg.smem_xy, st>>>(g, TA, TB, TC, b.bg, tw);
             mark(2);
             kr_zpass<T, M, true><<<dim3(cfg.nbz, 1, R), tz, cfg.smem_z, st>>>(g, TA, TB, TC, QV, QS, b.partV, b.bg, tw,
                                                                             (T *)b.tape_fx);
@@ -179,7 +179,7 @@ struct RegLaunch {
         C *TA = (C *)b.TA, *TB = (C *)b.TB, *TC = (C *)b.TC, *QS = (C *)b.QS;
         const dim3 gx(cfg.nbx, g.nf), g6(cfg.nbx, 6);
         kr_ifft_x<T, N, true, false><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, (C *)f_tape, nullptr, TA, TB, b.bg, tw);
-        kr_ifft_y<T, N, true><<<gx, cfg.thr_xy, cfg.smem_xf, st>>>(g, TA, TB, TC, b.bg, tw);
+        kr_ifft_y<T, N, true><<<gx, cfg.thr_xy, 3 * cfg.smem_xy, st>>>(g, TA, TB, TC, b.bg, tw);
         kr_ifft_x<T, N, false, false><<<g6, cfg.thr_xy, cfg.smem_xy, st>>>(g, (C *)Mu, nullptr, QS, nullptr, b.bg, tw);
         kr_ifft_y<T, N, false><<<g6, cfg.thr_xy, cfg.smem_xy, st>>>(g, QS, nullptr, nullptr, b.bg, tw);
         int tl = 1, sh = 0;
