@@ -38,13 +38,17 @@ template <typename C> __device__ __forceinline__ C cconj(C a) { a.y = -a.y; retu
 // ------------------------------------------------------------------ model (model.h)
 // Device mirror of model.h: V, dV/dphi for the shipped phi^2 model
 // (model.h:35-82) and the two-field phi^2 chi^2 model written in the same API.
-struct Model {
+// The coupling is held in the precision G of the arithmetic that uses it (the field
+// precision in the register engine: no per-site FP64 -> FP32 conversion).
+template <typename G = double>
+struct ModelG {
     int kind;   // 0 = phi^2, 1 = phi^2 chi^2
-    double gsq;
+    G gsq;
 };
+using Model = ModelG<double>;
 
-template <typename T>
-__device__ __forceinline__ void model_dvdf(const Model &m, const T *v, T *out, int nf) {
+template <typename T, typename G>
+__device__ __forceinline__ void model_dvdf(const ModelG<G> &m, const T *v, T *out, int nf) {
     if (m.kind == 0) {
         out[0] = v[0];
     } else {
@@ -57,8 +61,8 @@ __device__ __forceinline__ void model_dvdf(const Model &m, const T *v, T *out, i
 // Accumulates in A: the field precision for the per-thread partial sums of the
 // register engine (a thread adds a handful of sites before the FP64 block sum),
 // double in the generic engine.
-template <typename T, typename A = double>
-__device__ __forceinline__ void model_potential(const Model &m, const T *v, A *terms) {
+template <typename T, typename A = double, typename G = double>
+__device__ __forceinline__ void model_potential(const ModelG<G> &m, const T *v, A *terms) {
     const A p = (A)v[0];
     terms[0] += A(0.5) * p * p;
     if (m.kind == 1) {

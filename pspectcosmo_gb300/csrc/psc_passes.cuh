@@ -445,9 +445,9 @@ __global__ void __launch_bounds__(256, GW ? 3 : 2) kr_zpass(Geo g, const cplx<T>
         }
         cp_async_commit();
     };
-    Model mdl;
+    ModelG<T> mdl;
     mdl.kind = g.model;
-    mdl.gsq = g.gsq;
+    mdl.gsq = (T)g.gsq;
     T pot_t[kMaxTerms] = {T(0), T(0)};
     if (STAGED) prefetch(blockIdx.x);
     for (int tile = blockIdx.x; tile < ntiles; tile = STAGED ? tile + gridDim.x : ntiles) {
@@ -546,7 +546,7 @@ __global__ void __launch_bounds__(256, GW ? 3 : 2) kr_zpass(Geo g, const cplx<T>
                     }
                 }
                 model_dvdf<T>(mdl, f, vp, nf);
-                model_potential<T, T>(mdl, f, pot_t);
+                model_potential<T, T, T>(mdl, f, pot_t);
 #pragma unroll
                 for (int fl = 0; fl < 2; ++fl)
                     if (fl < nf) { if (half) out[fl].y = vp[fl]; else out[fl].x = vp[fl]; }
