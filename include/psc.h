@@ -39,6 +39,7 @@ extern "C" {
 #define PSC_ERR_TIMEOUT (-5)    /* a bounded device-side wait gave up */
 #define PSC_ERR_STATE (-6)      /* call out of order (e.g. step before state is set) */
 #define PSC_ERR_NOMEM (-7)      /* device allocation failed */
+#define PSC_ERR_IO (-8)         /* a file could not be written */
 
 #define PSC_MODEL_PHI2 0      /* V = phi^2/2 (reference model.h:35-99) */
 #define PSC_MODEL_PHI2CHI2 1  /* V = phi^2/2 + gsq phi^2 chi^2 / 2 (two-field preheating) */
@@ -139,6 +140,34 @@ int psc_energies(psc_handle *h, double *K, double *G, double *V, double *total, 
  * a^(2(alpha-3))<pi^2>, rms(f), a^(alpha-3) rms(pi); out has 6*nflds doubles. */
 int psc_means(psc_handle *h, double *out);
 
+/* histograms() (output.cpp:1193-1297): for each field, the nbins frequencies of its
+ * real-space values ([nflds][nbins], each count divided by the number of points
+ * binned), the lower edge of the first bin and the bin width ([nflds] each). With
+ * hmin == hmax (the reference's histogram_min == histogram_max) the bins span the
+ * field's current minimum and maximum; otherwise [hmin, hmax]. Bin index
+ * (int)((f - bmin) / df) in FP64, the maximum in the last bin, as the reference. */
+int psc_histograms(psc_handle *h, int nbins, double hmin, double hmax, double *binfreq, double *bmin, double *df);
+
+/* The datasets of snapshots() (output.cpp:1541-1648), N^3 doubles each, [x][y][z];
+ * any pointer may be NULL: f = the real-space fields [nflds][N^3]; pot, kin, grad,
+ * tot = the lattice energy densities of SNAPSHOTS_ENERGY at the current scale factor
+ * (kinetic_energy_lattice and gradient_energy_lattice, evolution.cpp:7-138; the
+ * potential and their sum, output.cpp:1614-1627). */
+int psc_snapshot_arrays(psc_handle *h, double *f, double *pot, double *kin, double *grad, double *tot);
+
+/* Writes the reference's snapshot file (output.cpp:1541-1648; the reference names it
+ * <dir>/Snapshots/data_<step>_snapshot.h5) at `path`: HDF5 with the N x N x N
+ * IEEE F64LE datasets /ScalarField_<fld> and, when with_energy (SNAPSHOTS_ENERGY),
+ * /PotentialEnergy, /KineticEnergy, /GradientEnergy and /TotalEnergy. The file is
+ * written by the library's own HDF5 writer (no libhdf5 needed). PSC_ERR_IO when
+ * the file cannot be written. */
+int psc_write_snapshot(psc_handle *h, const char *path, int with_energy);
+
+/* The HDF5 writer alone (host only): n datasets names[i] of shape dims[0..rank) from
+ * the host FP64 arrays data[i], in the layout psc_write_snapshot uses. */
+int psc_h5_write_f64(const char *path, int n, const char *const *names, const double *const *data, int rank,
+                     const uint64_t *dims);
+
 /* Device-time of the last psc_step call (CUDA events on the handle's stream), ms. */
 int psc_last_step_ms(psc_handle *h, float *ms);
 
@@ -181,6 +210,9 @@ int psc_batch_spectra(psc_batch *b, int idx, int32_t *numpoints, double *f2, dou
 int psc_batch_energies(psc_batch *b, int idx, double *K, double *G, double *V, double *total,
                        double *friedmann_violation, double *rho_gw);
 int psc_batch_means(psc_batch *b, int idx, double *out);
+int psc_batch_histograms(psc_batch *b, int idx, int nbins, double hmin, double hmax, double *binfreq, double *bmin,
+                         double *df);
+int psc_batch_write_snapshot(psc_batch *b, int idx, const char *path, int with_energy);
 
 /* Scalar power spectrum without any device allocation. It has no counterpart in
  * the reference; it is the bin-summing step of spectra() (output.cpp:626-690) for

@@ -48,6 +48,12 @@ CONFIGS: dict[str, tuple[str, dict[str, str]]] = {
         "initfield[]": "{0.193 * MPl, 0.}",
         "initderivs[]": "{-0.142e-6 * MPl * MPl, 0.}",
     }),
+    # the same with snapshots on (HDF5 datasets through the shim: fields + lattice energies)
+    "snap2_n16_vv4": ("phi2chi2", {
+        "N": "16", "VV": "4", "nflds": "2", "kIR": "1", "ssnapshot": "true",
+        "initfield[]": "{0.193 * MPl, 0.}",
+        "initderivs[]": "{-0.142e-6 * MPl * MPl, 0.}",
+    }),
     # real-space pseudo-spectral path with gravitational waves (evolve_VV)
     "gw2_n16_vv4": ("phi2chi2", {
         "N": "16", "VV": "4", "nflds": "2", "kIR": "1",

@@ -12,14 +12,15 @@
  *   - steps evolve_VV_k_nopad(dt) (evolution.cpp:1131) or evolve_VV(dt)
  *     (evolution.cpp:607) with the FIXED dt given on the command line instead of
  *     the adaptive calculate_dt (pspectcosmo.cpp:213-233);
- *   - every `every` steps calls save_Freq() and save_Infreq() (output.cpp:1831,
- *     1842) and dumps the raw state.
+ *   - every `every` steps calls save_Freq(), save_Infreq() and save_Snap(step)
+ *     (output.cpp:1831, 1842, 1850) and dumps the raw state.
  * Everything runs on a thread with a 2 GiB stack, because the real-space path
  * keeps N^3 arrays on the stack (evolution.cpp:612, 441, 581).
  *
  * usage: harness NSTEPS DT EVERY      (run inside the output directory)
  * writes: output/*.txt (reference writers, 17 digits), state_<step>.bin, bg.txt,
- *         ic_info.txt
+ *         ic_info.txt, and with ssnapshot output/Snapshots/data_<step>_snapshot.h5.*.bin
+ *         (the raw datasets, through the HDF5 shim)
  */
 #include "pspectcosmo.h"
 
@@ -113,6 +114,7 @@ static void *run(void *) {
         if (s % g_every == 0) {
             save_Freq();
             save_Infreq();
+            save_Snap((double)s);   // snapshots() when ssnapshot is on (output.cpp:1850-1853)
             dump_state(s);
         }
     }

@@ -1028,6 +1028,17 @@ int psc_batch_means(psc_batch *b, int idx, double *out) {
     return means(h, r, out);
 }
 
+int psc_batch_histograms(psc_batch *b, int idx, int nbins, double hmin, double hmax, double *binfreq, double *bmin,
+                         double *df) {
+    PSC_BATCH_AT(b, idx, h, r);
+    return histograms(h, r, nbins, hmin, hmax, binfreq, bmin, df);
+}
+
+int psc_batch_write_snapshot(psc_batch *b, int idx, const char *path, int with_energy) {
+    PSC_BATCH_AT(b, idx, h, r);
+    return write_snapshot(h, r, path, with_energy);
+}
+
 #undef PSC_BATCH_AT
 
 const char *psc_strerror(int code) {
@@ -1040,6 +1051,7 @@ const char *psc_strerror(int code) {
     case PSC_ERR_TIMEOUT: return "device-side wait timed out";
     case PSC_ERR_STATE: return "call out of order";
     case PSC_ERR_NOMEM: return "out of device memory";
+    case PSC_ERR_IO: return "file could not be written";
     default: return "unknown error";
     }
 }

@@ -1,5 +1,6 @@
 // psc_handle.h — the lattice handle shared by the C-ABI layer (psc_api.cu) and
-// the adjoint (psc_adjoint.cu). Private to the library.
+// the adjoint (psc_adjoint.cu) and the output quantities (psc_outputs.cu).
+// Private to the library.
 #pragma once
 
 #include <string>
@@ -42,5 +43,11 @@ int read_bg(psc_handle *h, int r, DevBG *out);
 int write_bg(psc_handle *h, int r, const DevBG &in);
 int step(psc_handle *h, double dt, int nsteps);
 int evaluate(psc_handle *h, int keep_add);
+Buffers buffers_of(psc_handle *h, int r);
+LaunchCfg single_cfg(psc_handle *h);
+// psc_outputs.cu: histograms and snapshot datasets of realization r
+int histograms(psc_handle *h, int r, int nbins, double hmin, double hmax, double *binfreq, double *bmin, double *df);
+int snapshot_arrays(psc_handle *h, int r, double *f, double *pot, double *kin, double *grad, double *tot);
+int write_snapshot(psc_handle *h, int r, const char *path, int with_energy);
 }  // namespace hapi
 }  // namespace psc

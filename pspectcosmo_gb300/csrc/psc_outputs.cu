@@ -1,0 +1,449 @@
+// psc_outputs.cu — output-step quantities of the real-space fields, on the device:
+//   * histograms()      output.cpp:1193-1297 (bin frequencies, lower edge, bin width);
+//   * snapshots()       output.cpp:1541-1648 (the fields and, with SNAPSHOTS_ENERGY,
+//     the lattice energy densities: kinetic_energy_lattice / gradient_energy_lattice
+//     evolution.cpp:7-138, potential and total output.cpp:1614-1627), written as the
+//     reference's HDF5 file by the host writer in psc_h5.cpp.
+// The real-space fields come from the c2r of the state (the reference's isChanged
+// block, output.cpp:1219-1240 / 1555-1578); the gradients are c2r's of i kIR k_a f_k
+// with that axis' Nyquist bin zeroed, which is what the reference's 1-D r2c, multiply
+// and c2r along each axis compute (evolution.cpp:34-127).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "psc_dev.cuh"
+#include "psc_h5.h"
+#include "psc_handle.h"
+
+namespace psc {
+namespace {
+
+constexpr int kOutBlocks = 4 * 152;
+constexpr int kOutThreads = 256;
+
+// out = i kIR k_axis f_k, k_axis the signed wavenumber along axis (0 = x, 1 = y,
+// 2 = z), zero on that axis' Nyquist bin (evolution.cpp:47-56, 79-88, 107-116)
+template <typename T>
+__global__ void __launch_bounds__(kOutThreads) k_deriv_axis(const cplx<T> *__restrict__ fk, cplx<T> *__restrict__ out,
+                                                            int N, int H, long long modes, int axis, double kIR) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < modes; m += stride) {
+        int n;
+        if (axis == 2) {
+            n = (int)(m % H);
+        } else if (axis == 1) {
+            n = (int)((m / H) % N);
+        } else {
+            n = (int)(m / ((long long)N * H));
+        }
+        const int kap = (n == N / 2) ? 0 : (n < N / 2 ? n : n - N);
+        const T s = (T)(kIR * kap);
+        const cplx<T> v = fk[m];
+        out[m] = mk<T>(-s * v.y, s * v.x);
+    }
+}
+
+// potential energy density per site (output.cpp:1618-1625): the sum over the model's
+// terms of potential_energy(term, f(x)); tot = pot
+template <typename T>
+__global__ void __launch_bounds__(kOutThreads) k_snap_pot(const T *__restrict__ real, double *__restrict__ pot,
+                                                          double *__restrict__ tot, long long sites, int model,
+                                                          double gsq) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < sites; s += stride) {
+        const double phi = (double)real[s];
+        double v = 0.0 + 0.5 * (phi * phi);
+        if (model == 1) {
+            const double chi = (double)real[sites + s];
+            v += 0.5 * gsq * (phi * phi) * (chi * chi);
+        }
+        pot[s] = v;
+        tot[s] = v;
+    }
+}
+
+// kinetic energy density (evolution.cpp:7-19): norm * sum_f pi_f(x)^2; tot += it
+template <typename T>
+__global__ void __launch_bounds__(kOutThreads) k_snap_kin(const T *__restrict__ real, double *__restrict__ kin,
+                                                          double *__restrict__ tot, long long sites, int nf,
+                                                          double norm) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < sites; s += stride) {
+        double k = 0.0;
+        for (int f = 0; f < nf; ++f) {
+            const double p = (double)real[(long long)f * sites + s];
+            k += p * p;
+        }
+        k *= norm;
+        kin[s] = k;
+        tot[s] += k;
+    }
+}
+
+// gradient energy density (evolution.cpp:23-138): grad += (d_a f)^2 for one field and
+// axis (first: grad = ...); the final call scales by norm and adds to tot
+template <typename T>
+__global__ void __launch_bounds__(kOutThreads) k_snap_grad(const T *__restrict__ d, double *__restrict__ grad,
+                                                           double *__restrict__ tot, long long sites, int first,
+                                                           int last, double norm) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < sites; s += stride) {
+        const double x = (double)d[s];
+        double g = first ? 0.0 : grad[s];
+        g += x * x;
+        if (last) {
+            g *= norm;
+            tot[s] += g;
+        }
+        grad[s] = g;
+    }
+}
+
+// block partial minimum and maximum of x[0..n) (output.cpp:1250-1256)
+template <typename T>
+__global__ void __launch_bounds__(kOutThreads) k_minmax(const T *__restrict__ x, long long n, double *__restrict__ part) {
+    __shared__ double smin[kOutThreads / 32], smax[kOutThreads / 32];
+    double lo = (double)x[0], hi = lo;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const double v = (double)x[i];
+        lo = v < lo ? v : lo;
+        hi = v > hi ? v : hi;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const double a = __shfl_xor_sync(0xffffffffu, lo, o), b = __shfl_xor_sync(0xffffffffu, hi, o);
+        lo = a < lo ? a : lo;
+        hi = b > hi ? b : hi;
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        smin[w] = lo;
+        smax[w] = hi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int i = 1; i < (int)(blockDim.x >> 5); ++i) {
+            lo = smin[i] < lo ? smin[i] : lo;
+            hi = smax[i] > hi ? smax[i] : hi;
+        }
+        part[2 * blockIdx.x] = lo;
+        part[2 * blockIdx.x + 1] = hi;
+    }
+}
+
+// bin counts of x[0..n) over [bmin, bmax] in nbins bins (output.cpp:1244-1279):
+// binnum = (int)((x - bmin) / df), x == bmax in the last bin, values whose bin falls
+// outside [0, nbins) not counted. With auto_range the limits are the minimum and
+// maximum of the block partials. edges = {bmin, df}.
+template <typename T>
+__global__ void __launch_bounds__(kOutThreads) k_hist(const T *__restrict__ x, long long n,
+                                                      const double *__restrict__ part, int nparts, int auto_range,
+                                                      double hmin, double hmax, int nbins,
+                                                      unsigned *__restrict__ counts, double *__restrict__ edges) {
+    extern __shared__ unsigned sc[];
+    __shared__ double lim[2];
+    if (threadIdx.x == 0) {
+        double lo = hmin, hi = hmax;
+        if (auto_range) {
+            lo = part[0];
+            hi = part[1];
+            for (int i = 1; i < nparts; ++i) {
+                lo = part[2 * i] < lo ? part[2 * i] : lo;
+                hi = part[2 * i + 1] > hi ? part[2 * i + 1] : hi;
+            }
+        }
+        lim[0] = lo;
+        lim[1] = hi;
+        if (blockIdx.x == 0) {
+            edges[0] = lo;
+            edges[1] = (hi - lo) / (double)nbins;
+        }
+    }
+    for (int i = threadIdx.x; i < nbins; i += blockDim.x) sc[i] = 0u;
+    __syncthreads();
+    const double bmin = lim[0], bmax = lim[1];
+    const double df = (bmax - bmin) / (double)nbins;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const double v = (double)x[i];
+        int bin;
+        if (v == bmax) {
+            bin = nbins - 1;
+        } else {
+            const double q = (v - bmin) / df;
+            if (q != q) continue;           // NaN: no bin
+            bin = __double2int_rz(q);       // truncation toward zero; saturates out of range
+        }
+        if (bin >= 0 && bin < nbins) atomicAdd(&sc[bin], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nbins; i += blockDim.x)
+        if (sc[i]) atomicAdd(&counts[i], sc[i]);
+}
+
+template <typename T>
+cudaError_t launch_deriv(const Geo &g, const void *fk, void *out, int axis, cudaStream_t st) {
+    k_deriv_axis<T><<<kOutBlocks, kOutThreads, 0, st>>>((const cplx<T> *)fk, (cplx<T> *)out, g.N, g.H, g.modes, axis,
+                                                         g.kIR);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+namespace hapi {
+
+#define CU(call)                                                                                         \
+    do {                                                                                                 \
+        cudaError_t e_ = (call);                                                                         \
+        if (e_ != cudaSuccess)                                                                           \
+            return fail(e_ == cudaErrorMemoryAllocation ? PSC_ERR_NOMEM : PSC_ERR_CUDA,                  \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                             \
+    } while (0)
+
+namespace {
+
+int ensure_real(psc_handle *h) {
+    const Geo &g = h->cfg.g;
+    if (h->b.real) return PSC_OK;
+    return dalloc(h, &h->b.real, (size_t)g.sites * g.nf * (h->csize / 2));
+}
+
+// c2r of nsrc arrays of realization r into h->b.real
+int to_real(psc_handle *h, int r, const void *src, int nsrc) {
+    int rc = ensure_real(h);
+    if (rc) return rc;
+    const Buffers b1 = buffers_of(h, r);
+    CU(launch_c2r_real(single_cfg(h), b1, h->p0().precision, src, nsrc, h->st));
+    return PSC_OK;
+}
+
+template <typename T>
+int histograms_t(psc_handle *h, int r, int nbins, double hmin, double hmax, double *binfreq, double *bmin,
+                 double *df) {
+    const Geo &g = h->cfg.g;
+    const Buffers b1 = buffers_of(h, r);
+    int rc = to_real(h, r, b1.fk, g.nf);
+    if (rc) return rc;
+    // device scratch: block partials, counters, edges
+    const size_t part_b = 2 * kOutBlocks * sizeof(double), cnt_b = (size_t)nbins * sizeof(unsigned);
+    void *scratch = nullptr;
+    CU(cudaMallocAsync(&scratch, part_b + cnt_b + 2 * sizeof(double), h->st));
+    double *part = static_cast<double *>(scratch);
+    unsigned *cnt = reinterpret_cast<unsigned *>(static_cast<char *>(scratch) + part_b);
+    double *edges = reinterpret_cast<double *>(static_cast<char *>(scratch) + part_b + cnt_b);
+    std::vector<unsigned> hc((size_t)nbins);
+    double he[2];
+    const int auto_range = (hmin == hmax);
+    cudaError_t e = cudaSuccess;
+    if (cnt_b > 48 * 1024)
+        e = cudaFuncSetAttribute(k_hist<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cnt_b);
+    for (int f = 0; f < g.nf && e == cudaSuccess; ++f) {
+        const T *x = static_cast<const T *>(h->b.real) + (long long)f * g.sites;
+        if (auto_range) k_minmax<T><<<kOutBlocks, kOutThreads, 0, h->st>>>(x, g.sites, part);
+        if ((e = cudaMemsetAsync(cnt, 0, cnt_b, h->st)) != cudaSuccess) break;
+        k_hist<T><<<kOutBlocks, kOutThreads, cnt_b, h->st>>>(x, g.sites, part, kOutBlocks, auto_range, hmin, hmax,
+                                                            nbins, cnt, edges);
+        if ((e = cudaGetLastError()) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(hc.data(), cnt, cnt_b, cudaMemcpyDeviceToHost, h->st)) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(he, edges, sizeof he, cudaMemcpyDeviceToHost, h->st)) != cudaSuccess) break;
+        if ((e = cudaStreamSynchronize(h->st)) != cudaSuccess) break;
+        unsigned long long numpts = 0;
+        for (unsigned c : hc) numpts += c;
+        if (binfreq)
+            for (int i = 0; i < nbins; ++i) binfreq[(size_t)f * nbins + i] = (double)hc[i] / (double)numpts;
+        if (bmin) bmin[f] = he[0];
+        if (df) df[f] = he[1];
+    }
+    cudaFreeAsync(scratch, h->st);
+    CU(e);
+    CU(cudaStreamSynchronize(h->st));
+    return PSC_OK;
+}
+
+// Runs the snapshot datasets through `sink(name, device_or_host_data)`: the fields
+// (host arrays, converted to FP64) and, with energy, the four densities (device FP64).
+struct Sink {
+    virtual int fields(const double *host_f) = 0;            // [nf][sites]
+    virtual int energy(int which, const double *dev) = 0;    // 0 pot, 1 kin, 2 grad, 3 tot
+    virtual ~Sink() {}
+};
+
+template <typename T>
+int snapshot_t(psc_handle *h, int r, int want_fields, int with_energy, Sink &sink) {
+    const Geo &g = h->cfg.g;
+    const Buffers b1 = buffers_of(h, r);
+    int rc;
+    DevBG bg;
+    if ((rc = read_bg(h, r, &bg))) return rc;
+    if ((rc = to_real(h, r, b1.fk, g.nf))) return rc;
+    if (want_fields) {
+        std::vector<double> hf((size_t)g.sites * g.nf);
+        if ((rc = download_real(h, hf.data(), h->b.real, hf.size()))) return rc;
+        if ((rc = sink.fields(hf.data()))) return rc;
+    }
+    if (!with_energy) return PSC_OK;
+    double *work = nullptr, *tot = nullptr;
+    const size_t bytes = (size_t)g.sites * sizeof(double);
+    CU(cudaMallocAsync(reinterpret_cast<void **>(&work), 2 * bytes, h->st));
+    tot = work + g.sites;
+    auto run = [&]() -> int {
+        const T *real = static_cast<const T *>(h->b.real);
+        k_snap_pot<T><<<kOutBlocks, kOutThreads, 0, h->st>>>(real, work, tot, g.sites, g.model, g.gsq);
+        CU(cudaGetLastError());
+        int rc2 = sink.energy(0, work);
+        if (rc2) return rc2;
+        if ((rc2 = to_real(h, r, b1.pk, g.nf))) return rc2;
+        // kinetic_energy_lattice: pow(a, 6) / 2 (evolution.cpp:9)
+        k_snap_kin<T><<<kOutBlocks, kOutThreads, 0, h->st>>>(real, work, tot, g.sites, g.nf, std::pow(bg.a, 6) / 2.);
+        CU(cudaGetLastError());
+        if ((rc2 = sink.energy(1, work))) return rc2;
+        // gradient_energy_lattice: field by field, axes x, y, z; pw2(a) / 2 (evolution.cpp:133)
+        const double gnorm = bg.a * bg.a / 2.;
+        for (int f = 0; f < g.nf; ++f)
+            for (int ax = 0; ax < 3; ++ax) {
+                const void *src = static_cast<const char *>(b1.fk) + (size_t)f * g.modes * h->csize;
+                CU(launch_deriv<T>(g, src, b1.QV, ax, h->st));
+                if ((rc2 = to_real(h, r, b1.QV, 1))) return rc2;
+                const int first = (f == 0 && ax == 0), last = (f == g.nf - 1 && ax == 2);
+                k_snap_grad<T><<<kOutBlocks, kOutThreads, 0, h->st>>>(real, work, tot, g.sites, first, last, gnorm);
+                CU(cudaGetLastError());
+            }
+        if ((rc2 = sink.energy(2, work))) return rc2;
+        return sink.energy(3, tot);
+    };
+    rc = run();
+    cudaFreeAsync(work, h->st);
+    if (rc) return rc;
+    CU(cudaStreamSynchronize(h->st));
+    return PSC_OK;
+}
+
+struct ArraySink : Sink {
+    psc_handle *h;
+    size_t n, nf;
+    double *f, *out[4];
+    int fields(const double *hf) override {
+        if (f) std::copy(hf, hf + n * nf, f);
+        return PSC_OK;
+    }
+    int energy(int which, const double *dev) override {
+        if (!out[which]) return PSC_OK;
+        CU(cudaMemcpyAsync(out[which], dev, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        CU(cudaStreamSynchronize(h->st));
+        return PSC_OK;
+    }
+};
+
+struct FileSink : Sink {
+    psc_handle *h;
+    size_t n, nf;
+    h5::Writer *w;
+    std::vector<double> host;
+    int fields(const double *hf) override {
+        for (size_t f = 0; f < nf; ++f)
+            if (w->write((int)f, hf + f * n)) return fail(PSC_ERR_IO, w->error());
+        return PSC_OK;
+    }
+    int energy(int which, const double *dev) override {
+        host.resize(n);
+        CU(cudaMemcpyAsync(host.data(), dev, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        CU(cudaStreamSynchronize(h->st));
+        if (w->write((int)(nf + which), host.data())) return fail(PSC_ERR_IO, w->error());
+        return PSC_OK;
+    }
+};
+
+}  // namespace
+
+int histograms(psc_handle *h, int r, int nbins, double hmin, double hmax, double *binfreq, double *bmin,
+               double *df) {
+    if (nbins < 1 || nbins > 16384) return fail(PSC_ERR_ARG, "nbins must be in [1, 16384]");
+    if (!h->have_state) return fail(PSC_ERR_STATE, "no state");
+    return h->p0().precision == 32 ? histograms_t<float>(h, r, nbins, hmin, hmax, binfreq, bmin, df)
+                                   : histograms_t<double>(h, r, nbins, hmin, hmax, binfreq, bmin, df);
+}
+
+int snapshot_arrays(psc_handle *h, int r, double *f, double *pot, double *kin, double *grad, double *tot) {
+    if (!h->have_state) return fail(PSC_ERR_STATE, "no state");
+    const Geo &g = h->cfg.g;
+    ArraySink s;
+    s.h = h;
+    s.n = (size_t)g.sites;
+    s.nf = (size_t)g.nf;
+    s.f = f;
+    s.out[0] = pot;
+    s.out[1] = kin;
+    s.out[2] = grad;
+    s.out[3] = tot;
+    const int energy = pot || kin || grad || tot;
+    return h->p0().precision == 32 ? snapshot_t<float>(h, r, f != nullptr, energy, s)
+                                   : snapshot_t<double>(h, r, f != nullptr, energy, s);
+}
+
+int write_snapshot(psc_handle *h, int r, const char *path, int with_energy) {
+    if (!path) return fail(PSC_ERR_ARG, "null path");
+    if (!h->have_state) return fail(PSC_ERR_STATE, "no state");
+    const Geo &g = h->cfg.g;
+    // dataset names of snapshots() (output.cpp:1581-1593)
+    std::vector<std::string> names;
+    for (int f = 0; f < g.nf; ++f) names.push_back("/ScalarField_" + std::to_string(f));
+    if (with_energy)
+        for (const char *e : {"/PotentialEnergy", "/KineticEnergy", "/GradientEnergy", "/TotalEnergy"})
+            names.push_back(e);
+    h5::Writer w;
+    const uint64_t N = (uint64_t)g.N;
+    if (w.open(path, names, {N, N, N})) return fail(PSC_ERR_IO, w.error());
+    FileSink s;
+    s.h = h;
+    s.n = (size_t)g.sites;
+    s.nf = (size_t)g.nf;
+    s.w = &w;
+    const int rc = h->p0().precision == 32 ? snapshot_t<float>(h, r, 1, with_energy, s)
+                                           : snapshot_t<double>(h, r, 1, with_energy, s);
+    if (rc) return rc;
+    if (w.close()) return fail(PSC_ERR_IO, w.error());
+    return PSC_OK;
+}
+
+}  // namespace hapi
+}  // namespace psc
+
+using namespace psc::hapi;
+
+extern "C" {
+
+int psc_histograms(psc_handle *h, int nbins, double hmin, double hmax, double *binfreq, double *bmin, double *df) {
+    if (!h) return fail(PSC_ERR_ARG, "null handle");
+    return histograms(h, 0, nbins, hmin, hmax, binfreq, bmin, df);
+}
+
+int psc_snapshot_arrays(psc_handle *h, double *f, double *pot, double *kin, double *grad, double *tot) {
+    if (!h) return fail(PSC_ERR_ARG, "null handle");
+    return snapshot_arrays(h, 0, f, pot, kin, grad, tot);
+}
+
+int psc_write_snapshot(psc_handle *h, const char *path, int with_energy) {
+    if (!h) return fail(PSC_ERR_ARG, "null handle");
+    return write_snapshot(h, 0, path, with_energy);
+}
+
+int psc_h5_write_f64(const char *path, int n, const char *const *names, const double *const *data, int rank,
+                     const uint64_t *dims) {
+    if (!path || n < 1 || !names || !data || rank < 1 || !dims) return fail(PSC_ERR_ARG, "bad arguments");
+    std::vector<std::string> nm;
+    for (int i = 0; i < n; ++i) {
+        if (!names[i] || !data[i]) return fail(PSC_ERR_ARG, "null dataset name or data");
+        nm.push_back(names[i]);
+    }
+    psc::h5::Writer w;
+    if (w.open(path, nm, std::vector<uint64_t>(dims, dims + rank))) return fail(PSC_ERR_IO, w.error());
+    for (int i = 0; i < n; ++i)
+        if (w.write(i, data[i])) return fail(PSC_ERR_IO, w.error());
+    if (w.close()) return fail(PSC_ERR_IO, w.error());
+    return PSC_OK;
+}
+
+}  // extern "C"

@@ -33,6 +33,7 @@ PSC_ERR_NONFINITE = -4
 PSC_ERR_TIMEOUT = -5
 PSC_ERR_STATE = -6
 PSC_ERR_NOMEM = -7
+PSC_ERR_IO = -8
 
 _lib = None
 
@@ -96,6 +97,13 @@ def load_library(path: str | None = None):
     L.psc_adjoint_forward_chi2.argtypes = [P, ctypes.c_double, ctypes.c_int, D]
     L.psc_adjoint.argtypes = [P, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, D, D, D, D, D, D, D]
     L.psc_adjoint_forward.argtypes = [P, ctypes.c_int, ctypes.c_double, ctypes.c_int, D]
+    L.psc_histograms.argtypes = [P, ctypes.c_int, ctypes.c_double, ctypes.c_double, D, D, D]
+    L.psc_snapshot_arrays.argtypes = [P, D, D, D, D, D]
+    L.psc_write_snapshot.argtypes = [P, ctypes.c_char_p, ctypes.c_int]
+    L.psc_h5_write_f64.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_char_p),
+                                   ctypes.POINTER(D), ctypes.c_int, ctypes.POINTER(ctypes.c_uint64)]
+    L.psc_batch_histograms.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, D, D, D]
+    L.psc_batch_write_snapshot.argtypes = [P, ctypes.c_int, ctypes.c_char_p, ctypes.c_int]
     L.psc_strerror.argtypes = [ctypes.c_int]
     L.psc_strerror.restype = ctypes.c_char_p
     L.psc_last_error.argtypes = []
@@ -105,7 +113,9 @@ def load_library(path: str | None = None):
                  "psc_means", "psc_last_step_ms", "psc_time_passes", "psc_pass_bytes", "psc_batch_create",
                  "psc_batch_size", "psc_batch_groups", "psc_batch_init_ic", "psc_batch_step", "psc_batch_last_step_ms",
                  "psc_batch_set_state", "psc_batch_get_state", "psc_batch_spectra", "psc_batch_energies",
-                 "psc_batch_means", "psc_adjoint_chi2", "psc_adjoint_forward_chi2", "psc_adjoint", "psc_adjoint_forward"):
+                 "psc_batch_means", "psc_adjoint_chi2", "psc_adjoint_forward_chi2", "psc_adjoint", "psc_adjoint_forward",
+                 "psc_histograms", "psc_snapshot_arrays", "psc_write_snapshot", "psc_h5_write_f64",
+                 "psc_batch_histograms", "psc_batch_write_snapshot"):
         getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L
@@ -122,6 +132,20 @@ def _ip(a):
 def _check(rc: int, where: str):
     if rc != PSC_OK:
         raise PscError(rc, where)
+
+
+def h5_write(path: str, datasets: dict) -> None:
+    """Write FP64 arrays of one shape as root-group datasets of an HDF5 file with the
+    library's own writer (the layout of psc_write_snapshot)."""
+    L = load_library()
+    arrs = [np.ascontiguousarray(v, dtype=np.float64) for v in datasets.values()]
+    shape = arrs[0].shape
+    if any(x.shape != shape for x in arrs):
+        raise ValueError("all datasets must have the same shape")
+    names = (ctypes.c_char_p * len(arrs))(*[k.encode() for k in datasets])
+    ptrs = (ctypes.POINTER(ctypes.c_double) * len(arrs))(*[_dp(x) for x in arrs])
+    dims = (ctypes.c_uint64 * len(shape))(*shape)
+    _check(L.psc_h5_write_f64(os.fsencode(path), len(arrs), names, ptrs, len(shape), dims), "psc_h5_write_f64")
 
 
 def generate_ic(params: Params):
@@ -313,6 +337,32 @@ class Lattice:
         _check(self._L.psc_means(self._h, _dp(out)), "psc_means")
         return out
 
+    def histograms(self, nbins: int = 256, hmin: float = 0.0, hmax: float = 0.0) -> dict:
+        """histograms() (output.cpp:1193-1297): binfreq [nflds][nbins], bmin, df [nflds]."""
+        p = self.p
+        freq, bmin, df = np.zeros((p.nflds, nbins)), np.zeros(p.nflds), np.zeros(p.nflds)
+        _check(self._L.psc_histograms(self._h, int(nbins), float(hmin), float(hmax), _dp(freq), _dp(bmin), _dp(df)),
+               "psc_histograms")
+        return dict(binfreq=freq, bmin=bmin, df=df)
+
+    def snapshot_arrays(self, fields: bool = True, energy: bool = True) -> dict:
+        """The datasets of snapshots() (output.cpp:1541-1648) as [N][N][N] arrays."""
+        p = self.p
+        sh = (p.N, p.N, p.N)
+        out = {}
+        if fields:
+            out["f"] = np.zeros((p.nflds,) + sh)
+        if energy:
+            for k in ("pot", "kin", "grad", "tot"):
+                out[k] = np.zeros(sh)
+        _check(self._L.psc_snapshot_arrays(self._h, _dp(out.get("f")), _dp(out.get("pot")), _dp(out.get("kin")),
+                                           _dp(out.get("grad")), _dp(out.get("tot"))), "psc_snapshot_arrays")
+        return out
+
+    def write_snapshot(self, path: str, with_energy: bool = True) -> None:
+        """The reference's data_<step>_snapshot.h5 (output.cpp:1541-1648) at `path`."""
+        _check(self._L.psc_write_snapshot(self._h, os.fsencode(path), int(bool(with_energy))), "psc_write_snapshot")
+
     # reference-named output rows (the columns the reference writes)
     def spectra(self) -> dict:
         from .outputs import spectra_rows
@@ -394,6 +444,17 @@ class Ensemble:
         _check(self._L.psc_batch_spectra(self._h, idx, _ip(out["numpoints"]), _dp(out["f2"]), _dp(out["pi2"]),
                                          _dp(out["n2"]), None, None, None, ctypes.byref(hz)), "psc_batch_spectra")
         return out
+
+    def histograms(self, idx: int, nbins: int = 256, hmin: float = 0.0, hmax: float = 0.0) -> dict:
+        p = self.params[idx]
+        freq, bmin, df = np.zeros((p.nflds, nbins)), np.zeros(p.nflds), np.zeros(p.nflds)
+        _check(self._L.psc_batch_histograms(self._h, idx, int(nbins), float(hmin), float(hmax), _dp(freq), _dp(bmin),
+                                            _dp(df)), "psc_batch_histograms")
+        return dict(binfreq=freq, bmin=bmin, df=df)
+
+    def write_snapshot(self, idx: int, path: str, with_energy: bool = True) -> None:
+        _check(self._L.psc_batch_write_snapshot(self._h, idx, os.fsencode(path), int(bool(with_energy))),
+               "psc_batch_write_snapshot")
 
     def energies(self, idx: int) -> dict:
         p = self.params[idx]

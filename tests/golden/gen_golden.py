@@ -31,6 +31,7 @@ RUNS = {
     "spec1_n64_dt1e-4": ("spec1_n64", 200, 0.0001, 50, False),
     "spec2_n16_vv4": ("spec2_n16_vv4", 20, 0.005, 10, True),
     "spec2_n32_vv2": ("spec2_n32_vv2", 40, 0.005, 20, False),
+    "snap2_n16_vv4": ("snap2_n16_vv4", 20, 0.005, 10, True),
     "gw2_n16_vv4": ("gw2_n16_vv4", 10, 0.005, 5, True),
     "gw1_n16_vv2": ("gw1_n16_vv2", 10, 0.002, 5, True),
 }
@@ -146,6 +147,20 @@ def generate(run: str) -> str:
         if ic["gw"]:
             out["spectra_gws"] = read_blocks(os.path.join(o, "spectra_gws.txt"))
             out["energy_gws"] = read_rows(os.path.join(o, "energy_gws.txt"))
+        # with snapshots on: the histograms (histograms(), output.cpp:1193-1297, one block
+        # per output call) and the raw snapshot datasets of the last step
+        # (output.cpp:1541-1648, written through the HDF5 shim)
+        snap = os.path.join(o, "Snapshots")
+        if os.path.isdir(snap) and os.listdir(snap):
+            for fld in range(ic["nflds"]):
+                out[f"histogram_{fld}"] = read_blocks(os.path.join(o, f"histogram{fld}.txt"))[..., 0]
+            out["histogramtimes"] = read_rows(os.path.join(o, "histogramtimes.txt"))
+            N = ic["N"]
+            names = [f"ScalarField_{fld}" for fld in range(ic["nflds"])]
+            names += ["PotentialEnergy", "KineticEnergy", "GradientEnergy", "TotalEnergy"]
+            for name in names:
+                raw = np.fromfile(os.path.join(snap, f"data_{nsteps}_snapshot.h5._{name}.bin"), dtype=np.float64)
+                out[f"snap_{name}"] = raw.reshape(N, N, N)
         # initial state in k-space (what both paths start from)
         out["ic_f_k"] = ic["f_k"]
         out["ic_pi_k"] = ic["pi_k"]

@@ -1,0 +1,149 @@
+"""Device histograms and snapshot datasets (psc_histograms, psc_snapshot_arrays,
+psc_write_snapshot) against the reference's own outputs and the oracle.
+
+Tolerances: FP64 snapshot datasets within 1e-11 of the reference's (its real-space
+fields come from its own c2r; the difference is FFT rounding). Histograms: bit-exact
+with the oracle on the same real-space field (the device bins in FP64 with the
+reference's arithmetic); against the reference's files, whose field differs from the
+device one by FFT rounding, the edges agree to 1e-13 and at most two points per field
+may fall in a neighbouring bin. FP32 datasets within 1e-5 of the FP64 oracle."""
+import os
+
+import numpy as np
+import pytest
+
+import h5read
+from golden_util import load, params_for, rel
+
+pytestmark = pytest.mark.gpu
+
+
+def _oref():
+    import importlib
+    import sys
+
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle"))
+    return importlib.import_module("outputs_ref")
+
+
+def _final_state_lattice(precision=64):
+    from pspectcosmo_gb300 import Lattice
+
+    g, meta = load("snap2_n16_vv4")
+    p = params_for(meta, precision)
+    lat = Lattice(p)
+    row = g["bg"][-1]
+    lat.set_state(g["fin_f_k"], g["fin_pi_k"], row[2], row[3], row[4])
+    return g, meta, p, lat
+
+
+def test_snapshot_arrays_match_reference():
+    g, meta, p, lat = _final_state_lattice()
+    s = lat.snapshot_arrays()
+    assert rel(s["f"][0], g["snap_ScalarField_0"]) < 1e-12
+    assert rel(s["f"][1], g["snap_ScalarField_1"]) < 1e-12
+    assert rel(s["pot"], g["snap_PotentialEnergy"]) < 1e-11
+    assert rel(s["kin"], g["snap_KineticEnergy"]) < 1e-11
+    assert rel(s["grad"], g["snap_GradientEnergy"]) < 1e-11
+    assert rel(s["tot"], g["snap_TotalEnergy"]) < 1e-11
+
+
+def test_histograms_match_reference_and_oracle():
+    g, meta, p, lat = _final_state_lattice()
+    h = lat.histograms(256)
+    f, _ = lat.fields_real()
+    freq, bmin, df = _oref().histograms(f, 256)
+    assert np.array_equal(h["binfreq"], freq) and np.array_equal(h["bmin"], bmin) and np.array_equal(h["df"], df)
+    times = g["histogramtimes"][-1]
+    npts = p.N ** 3
+    for fld in range(p.nflds):
+        assert abs(h["bmin"][fld] - times[1 + 2 * fld]) <= 1e-13 * abs(times[1 + 2 * fld])
+        assert abs(h["df"][fld] - times[2 + 2 * fld]) <= 1e-13 * abs(times[2 + 2 * fld])
+        moved = np.abs(np.rint(h["binfreq"][fld] * npts) - np.rint(g[f"histogram_{fld}"][-1] * npts)).sum()
+        assert moved <= 4
+
+
+def test_histograms_explicit_limits_and_bins():
+    g, meta, p, lat = _final_state_lattice()
+    f, _ = lat.fields_real()
+    o = _oref()
+    for nbins, lo, hi in ((256, 0.18, 0.2), (7, -1e-3, 1e-3), (1000, 0.0, 0.0)):
+        h = lat.histograms(nbins, lo, hi)
+        freq, bmin, df = o.histograms(f, nbins, lo, hi)
+        assert np.array_equal(h["binfreq"], freq) and np.array_equal(h["df"], df), (nbins, lo, hi)
+
+
+def test_write_snapshot_file(tmp_path):
+    g, meta, p, lat = _final_state_lattice()
+    s = lat.snapshot_arrays()
+    path = str(tmp_path / "data_20_snapshot.h5")
+    lat.write_snapshot(path)
+    f = h5read.File(path)
+    assert f.keys() == sorted(["ScalarField_0", "ScalarField_1", "PotentialEnergy", "KineticEnergy",
+                               "GradientEnergy", "TotalEnergy"])
+    assert np.array_equal(f.read("/ScalarField_0"), s["f"][0])
+    assert np.array_equal(f.read("/ScalarField_1"), s["f"][1])
+    for name, k in (("PotentialEnergy", "pot"), ("KineticEnergy", "kin"), ("GradientEnergy", "grad"),
+                    ("TotalEnergy", "tot")):
+        assert np.array_equal(f.read(name), s[k]), name
+    path2 = str(tmp_path / "fields_only.h5")
+    lat.write_snapshot(path2, with_energy=False)
+    assert h5read.File(path2).keys() == ["ScalarField_0", "ScalarField_1"]
+
+
+@pytest.mark.parametrize("precision,tol", [(64, 1e-11), (32, 1e-5)])
+def test_snapshot_register_engine_vs_oracle(precision, tol):
+    """64^3 (register-engine passes), two fields, a few steps from the device ICs."""
+    from pspectcosmo_gb300 import Lattice, Params
+
+    p = Params.preheating(N=64, precision=precision, vv=4)
+    lat = Lattice(p)
+    lat.initialize()
+    lat.evolve(0.005, 4)
+    st = lat.get_state()
+    N, H = p.N, p.N // 2 + 1
+    c2r = lambda x: np.fft.irfftn(x.reshape(N, N, H), s=(N, N, N), axes=(0, 1, 2))
+    f = np.stack([c2r(x) for x in st["f_k"]])
+    pi = np.stack([c2r(x) for x in st["pi_k"]])
+    e = _oref().lattice_energies(f, pi, st["a"], p.kIR, p.model, p.gsq)
+    s = lat.snapshot_arrays()
+    assert rel(s["f"], f) < tol
+    for k in ("pot", "kin", "grad", "tot"):
+        assert rel(s[k], e[k]) < tol, k
+    fr, _ = lat.fields_real()
+    h = lat.histograms(256)
+    freq, bmin, df = _oref().histograms(fr, 256)
+    assert np.array_equal(h["binfreq"], freq) and np.array_equal(h["bmin"], bmin)
+
+
+def test_batch_outputs_equal_single(tmp_path):
+    from pspectcosmo_gb300 import Ensemble, Lattice, Params
+
+    ps = [Params.preheating(N=32, seed=s) for s in (3, 5)]
+    ens = Ensemble(ps)
+    ens.initialize()
+    ens.evolve(0.005, 2)
+    lat = Lattice(ps[1])
+    lat.initialize()
+    lat.evolve(0.005, 2)
+    hb, hs = ens.histograms(1), lat.histograms()
+    assert np.array_equal(hb["binfreq"], hs["binfreq"]) and np.array_equal(hb["bmin"], hs["bmin"])
+    ens.write_snapshot(1, str(tmp_path / "b.h5"))
+    lat.write_snapshot(str(tmp_path / "s.h5"))
+    fb, fs = h5read.File(str(tmp_path / "b.h5")), h5read.File(str(tmp_path / "s.h5"))
+    for k in fs.keys():
+        assert np.array_equal(fb.read(k), fs.read(k)), k
+
+
+def test_errors():
+    from pspectcosmo_gb300 import Lattice, Params
+    from pspectcosmo_gb300.lattice import PscError
+
+    lat = Lattice(Params.preheating(N=16))
+    with pytest.raises(PscError):
+        lat.histograms()          # no state yet
+    lat.initialize()
+    with pytest.raises(PscError):
+        lat.histograms(0)
+    with pytest.raises(PscError):
+        lat.write_snapshot("/nonexistent_dir/x.h5")

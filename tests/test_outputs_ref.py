@@ -1,0 +1,125 @@
+"""Output-step oracle (histograms, lattice energy densities) pinned to the reference's own
+outputs, and the HDF5 snapshot writer checked structurally (CPU only).
+
+The golden run snap2_n16_vv4 is the reference's code (two-field preheating, 16^3,
+Yoshida-4, spectral step) with snapshots on: its histogram files and the raw datasets
+its snapshots() wrote at step 20."""
+import os
+
+import numpy as np
+import pytest
+
+import h5read
+from golden_util import load, rel
+
+SCIPY_H5 = None
+try:
+    import scipy
+
+    _p = os.path.join(os.path.dirname(scipy.__file__), "io", "matlab", "tests", "data", "testhdf5_7.4_GLNX86.mat")
+    SCIPY_H5 = _p if os.path.exists(_p) else None
+except ImportError:
+    pass
+
+
+@pytest.fixture(scope="module")
+def snap():
+    g, meta = load("snap2_n16_vv4")
+    return g, meta
+
+
+def _outputs_ref():
+    import importlib
+    import sys
+
+    here = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, os.path.join(here, "oracle"))
+    return importlib.import_module("outputs_ref")
+
+
+def test_histograms_bit_exact_with_reference(snap):
+    g, meta = snap
+    o = _outputs_ref()
+    f = np.stack([g["snap_ScalarField_0"], g["snap_ScalarField_1"]])
+    freq, bmin, df = o.histograms(f, 256)
+    times = g["histogramtimes"][-1]
+    for fld in range(2):
+        assert np.array_equal(freq[fld], g[f"histogram_{fld}"][-1])
+        assert bmin[fld] == times[1 + 2 * fld] and df[fld] == times[2 + 2 * fld]
+
+
+def test_histogram_edge_cases():
+    o = _outputs_ref()
+    x = np.array([0.0, 0.25, 0.5, 0.75, 1.0, 1.0])
+    freq, bmin, df = o.histogram(x, 4)
+    assert (bmin, df) == (0.0, 0.25)
+    assert np.array_equal(freq * 6, [1, 1, 1, 3])   # the maximum goes to the top bin
+    # explicit limits: (int) truncates toward zero, so values less than one bin below
+    # hmin land in bin 0; values at or beyond hmax + df are dropped
+    freq, _, _ = o.histogram(np.array([-0.1, 0.0, 0.5, 2.0, 5.0]), 2, hmin=0.0, hmax=1.0)
+    assert np.array_equal(freq * 3, [2, 1])
+    # constant field: (x - bmin) / 0 is NaN, every point equals bmax -> top bin
+    freq, _, df = o.histogram(np.full(8, 3.0), 4)
+    assert df == 0.0 and np.array_equal(freq, [0, 0, 0, 1])
+
+
+def test_lattice_energies_match_reference(snap):
+    g, meta = snap
+    o = _outputs_ref()
+    N = meta["N"]
+    H = N // 2 + 1
+    f = np.stack([g["snap_ScalarField_0"], g["snap_ScalarField_1"]])
+    # pi(x) = c2r(pi_k) / N^3 of the final state (the reference's isChanged block)
+    pi = np.stack([np.fft.irfftn(g["fin_pi_k"][i].reshape(N, N, H), s=(N, N, N), axes=(0, 1, 2)) for i in range(2)])
+    a = g["bg"][-1][2]
+    from pspectcosmo_gb300.params import Params
+
+    p = Params.preheating(N=N)
+    e = o.lattice_energies(f, pi, a, p.kIR, 1, p.gsq)
+    assert rel(e["pot"], g["snap_PotentialEnergy"]) < 1e-15
+    assert rel(e["kin"], g["snap_KineticEnergy"]) < 1e-12
+    assert rel(e["grad"], g["snap_GradientEnergy"]) < 1e-12
+    assert rel(e["tot"], g["snap_TotalEnergy"]) < 1e-12
+
+
+@pytest.mark.skipif(SCIPY_H5 is None, reason="SciPy's HDF5 test file is not installed")
+def test_reader_reads_a_libhdf5_file():
+    # a file written by libhdf5 (MATLAB 7.3 format, 512-byte user block)
+    f = h5read.File(SCIPY_H5)
+    assert f.keys() == ["testdouble"]
+    x = f.read("testdouble").ravel()
+    assert np.allclose(x, np.arange(9) * np.pi / 4, rtol=0, atol=1e-15)
+
+
+def test_writer_round_trip(tmp_path, psc_lib):
+    from pspectcosmo_gb300.lattice import h5_write
+
+    rng = np.random.default_rng(7)
+    # more names than one symbol table node holds, unsorted, with leading '/'
+    names = [f"/ScalarField_{i}" for i in (3, 0, 10, 1, 2, 9, 4, 5, 6, 7, 8)] + ["/TotalEnergy", "/PotentialEnergy"]
+    data = {n: rng.standard_normal((4, 8, 16)) for n in names}
+    path = str(tmp_path / "data_7_snapshot.h5")
+    h5_write(path, data)
+    f = h5read.File(path)
+    assert f.keys() == sorted(n[1:] for n in names)
+    assert f.eof == os.path.getsize(path)
+    for n, v in data.items():
+        info = f.dataset_info(n)
+        assert info["shape"] == (4, 8, 16) and info["dtype"] == np.dtype("<f8")
+        assert np.array_equal(f.read(n), v)
+    if SCIPY_H5:
+        # datatype bit field and fill value message as libhdf5 writes them
+        ref = h5read.File(SCIPY_H5).dataset_info("testdouble")
+        assert info["type_bits"] == ref["type_bits"]
+        assert info["fill"] == ref["fill"]
+
+
+def test_writer_rejects_bad_input(tmp_path, psc_lib):
+    from pspectcosmo_gb300.lattice import PscError, h5_write
+
+    with pytest.raises(PscError):
+        h5_write(str(tmp_path / "x.h5"), {"/a": np.zeros(4), "a": np.zeros(4)})   # duplicate
+    with pytest.raises(PscError):
+        h5_write(str(tmp_path / "x.h5"), {"/g/a": np.zeros(4)})                    # not in the root group
+    with pytest.raises(PscError):
+        h5_write(str(tmp_path / "no_such_dir" / "x.h5"), {"a": np.zeros(4)})
