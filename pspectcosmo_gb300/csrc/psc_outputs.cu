@@ -227,13 +227,15 @@ int histograms_t(psc_handle *h, int r, int nbins, double hmin, double hmax, doub
     const Buffers b1 = buffers_of(h, r);
     int rc = to_real(h, r, b1.fk, g.nf);
     if (rc) return rc;
-    // device scratch: block partials, counters, edges
-    const size_t part_b = 2 * kOutBlocks * sizeof(double), cnt_b = (size_t)nbins * sizeof(unsigned);
+    // device scratch: block partials and the two edges (doubles, 8-byte aligned) first,
+    // then the nbins 4-byte counters
+    const size_t part_b = 2 * kOutBlocks * sizeof(double), edge_b = 2 * sizeof(double);
+    const size_t cnt_b = (size_t)nbins * sizeof(unsigned);
     void *scratch = nullptr;
-    CU(cudaMallocAsync(&scratch, part_b + cnt_b + 2 * sizeof(double), h->st));
+    CU(cudaMallocAsync(&scratch, part_b + edge_b + cnt_b, h->st));
     double *part = static_cast<double *>(scratch);
-    unsigned *cnt = reinterpret_cast<unsigned *>(static_cast<char *>(scratch) + part_b);
-    double *edges = reinterpret_cast<double *>(static_cast<char *>(scratch) + part_b + cnt_b);
+    double *edges = part + 2 * kOutBlocks;
+    unsigned *cnt = reinterpret_cast<unsigned *>(static_cast<char *>(scratch) + part_b + edge_b);
     std::vector<unsigned> hc((size_t)nbins);
     double he[2];
     const int auto_range = (hmin == hmax);

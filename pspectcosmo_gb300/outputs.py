@@ -83,10 +83,16 @@ def scale_row(p: Params, bg: dict) -> list:
 class TextWriter:
     """Appends the reference's text outputs (output.cpp) in directory `dir_`."""
 
-    def __init__(self, p: Params, dir_: str = "output", ext: str = ".txt"):
+    def __init__(self, p: Params, dir_: str = "output", ext: str = ".txt", shistograms: bool = True,
+                 nbins: int = 256, histogram_min: float = 0.0, histogram_max: float = 0.0,
+                 snapshots_energy: bool = True):
         self.p, self.dir, self.ext = p, dir_, ext
         os.makedirs(os.path.join(dir_, "Snapshots"), exist_ok=True)
         self._first_spectra = True
+        # parameters.h:90-93 (histograms) and :14 (SNAPSHOTS_ENERGY)
+        self.shistograms, self.nbins = shistograms, nbins
+        self.histogram_min, self.histogram_max = histogram_min, histogram_max
+        self.snapshots_energy = snapshots_energy
 
     def _open(self, name):
         return open(os.path.join(self.dir, name + self.ext), "a")
@@ -118,8 +124,31 @@ class TextWriter:
             with self._open("average_energy_conservation") as fh:
                 fh.write(f"{bg['t']:.3f} {en['friedmann_violation']:.8e} {lhs:.6f} {rhs:.6f}\n")
 
+    def histograms(self, lat):
+        """histograms() (output.cpp:1193-1297): histogram<f>.txt, one frequency per line and
+        a blank line per call; histogramtimes.txt: t, then bmin and df of each field."""
+        p = self.p
+        h = lat.histograms(self.nbins, self.histogram_min, self.histogram_max)
+        for f in range(p.nflds):
+            with self._open(f"histogram{f}") as fh:
+                fh.write("".join(f"{v:.6e}\n" for v in h["binfreq"][f]) + "\n")
+        with self._open("histogramtimes") as fh:
+            t = lat.background()["t"]
+            fh.write(f"{t:.6f}" + "".join(f" {h['bmin'][f]:.6e} {h['df'][f]:.6e}" for f in range(p.nflds)) + "\n")
+
+    def snapshot(self, lat, step: int) -> str:
+        """save_Snap(step) -> snapshots() (output.cpp:1541-1648): <dir>/Snapshots/
+        data_<step>_snapshot.h5 with the fields and, with SNAPSHOTS_ENERGY, the lattice
+        energy densities. Returns the path."""
+        path = os.path.join(self.dir, "Snapshots", f"data_{int(step)}_snapshot.h5")
+        lat.write_snapshot(path, self.snapshots_energy)
+        return path
+
     def save_infreq(self, lat):
-        """spectra() (output.cpp:490-1062)."""
+        """save_Infreq() (output.cpp:1842-1848): histograms() when shistograms, then
+        spectra() (output.cpp:490-1062)."""
+        if self.shistograms:
+            self.histograms(lat)
         p = self.p
         bg = lat.background()
         en = lat.energies()

@@ -2,7 +2,10 @@
 psc_write_snapshot) against the reference's own outputs and the oracle.
 
 Tolerances: FP64 snapshot datasets within 1e-11 of the reference's (its real-space
-fields come from its own c2r; the difference is FFT rounding). Histograms: bit-exact
+fields come from its own c2r; the difference is FFT rounding), except the gradient
+energy density at 1e-8: the reference differentiates the real field phi0 + dphi(x)
+(evolution.cpp:34-127), whose rounding eps * phi0 is ~1e-9 of the fluctuation dphi,
+while the device differentiates the k-space state (no such floor). Histograms: bit-exact
 with the oracle on the same real-space field (the device bins in FP64 with the
 reference's arithmetic); against the reference's files, whose field differs from the
 device one by FFT rounding, the edges agree to 1e-13 and at most two points per field
@@ -16,6 +19,8 @@ import h5read
 from golden_util import load, params_for, rel
 
 pytestmark = pytest.mark.gpu
+
+GRAD_FLOOR = 1e-8   # eps * phi0 / dphi of a real-space derivative (module docstring)
 
 
 def _oref():
@@ -44,7 +49,7 @@ def test_snapshot_arrays_match_reference():
     assert rel(s["f"][1], g["snap_ScalarField_1"]) < 1e-12
     assert rel(s["pot"], g["snap_PotentialEnergy"]) < 1e-11
     assert rel(s["kin"], g["snap_KineticEnergy"]) < 1e-11
-    assert rel(s["grad"], g["snap_GradientEnergy"]) < 1e-11
+    assert rel(s["grad"], g["snap_GradientEnergy"]) < GRAD_FLOOR
     assert rel(s["tot"], g["snap_TotalEnergy"]) < 1e-11
 
 
@@ -67,10 +72,14 @@ def test_histograms_explicit_limits_and_bins():
     g, meta, p, lat = _final_state_lattice()
     f, _ = lat.fields_real()
     o = _oref()
-    for nbins, lo, hi in ((256, 0.18, 0.2), (7, -1e-3, 1e-3), (1000, 0.0, 0.0)):
+    # part of field 0's range; part of field 1's; a range holding no point of either
+    # (0/0 frequencies, NaN as in the reference); the automatic range with 1000 bins
+    q25, q75 = np.quantile(f[0], [0.25, 0.75])
+    for nbins, lo, hi in ((256, q25, q75), (7, -1e-8, 1e-8), (16, 5.0, 6.0), (1000, 0.0, 0.0)):
         h = lat.histograms(nbins, lo, hi)
         freq, bmin, df = o.histograms(f, nbins, lo, hi)
-        assert np.array_equal(h["binfreq"], freq) and np.array_equal(h["df"], df), (nbins, lo, hi)
+        assert np.array_equal(h["binfreq"], freq, equal_nan=True), (nbins, lo, hi)
+        assert np.array_equal(h["bmin"], bmin) and np.array_equal(h["df"], df), (nbins, lo, hi)
 
 
 def test_write_snapshot_file(tmp_path):
@@ -109,7 +118,7 @@ def test_snapshot_register_engine_vs_oracle(precision, tol):
     s = lat.snapshot_arrays()
     assert rel(s["f"], f) < tol
     for k in ("pot", "kin", "grad", "tot"):
-        assert rel(s[k], e[k]) < tol, k
+        assert rel(s[k], e[k]) < (max(tol, GRAD_FLOOR) if k == "grad" else tol), k
     fr, _ = lat.fields_real()
     h = lat.histograms(256)
     freq, bmin, df = _oref().histograms(fr, 256)
@@ -147,3 +156,28 @@ def test_errors():
         lat.histograms(0)
     with pytest.raises(PscError):
         lat.write_snapshot("/nonexistent_dir/x.h5")
+
+
+def test_text_writer_histograms_and_snapshot(tmp_path):
+    """TextWriter: histogram<f>.txt / histogramtimes.txt with the reference's 6-digit
+    formatting, and Snapshots/data_<step>_snapshot.h5."""
+    from pspectcosmo_gb300.outputs import TextWriter
+
+    g, meta, p, lat = _final_state_lattice()
+    lat.t = g["bg"][-1][1]
+    w = TextWriter(p, str(tmp_path))
+    w.save_infreq(lat)
+    path = w.snapshot(lat, 20)
+    assert os.path.basename(path) == "data_20_snapshot.h5"
+    assert h5read.File(path).keys()[0] == "GradientEnergy"
+    npts = p.N ** 3
+    for fld in range(p.nflds):
+        lines = open(tmp_path / f"histogram{fld}.txt").read().split("\n")
+        assert lines[256:] == ["", ""] and all("e" in x for x in lines[:256])
+        vals = np.array([float(x) for x in lines[:256]])
+        ref = g[f"histogram_{fld}"][-1]
+        assert np.abs(np.rint(vals * npts) - np.rint(ref * npts)).sum() <= 4
+    row = open(tmp_path / "histogramtimes.txt").read().split()
+    ref = g["histogramtimes"][-1]
+    assert row[0] == f"{ref[0]:.6f}"
+    assert np.allclose([float(x) for x in row[1:]], ref[1:], rtol=1e-6, atol=0)
