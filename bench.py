@@ -8,7 +8,8 @@ conditions (seed 1), generated on the host. Every array is larger than the 129 M
 (2 GB resident), so no flush is needed between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--config preheat_gw_256|preheat_256|inflation_64|ensemble_mixed|adjoint_128]
+                  [--config preheat_gw_256|preheat_gw_1024|preheat_256|inflation_64|ensemble_mixed|
+                            adjoint_128]
                   [--precision 32|64]
 
 One JSON line (rank 0). `value` is device-timed whole-job site-steps/s (inputs resident
@@ -37,6 +38,11 @@ CONFIGS = {
     # name: (Params factory kwargs, dt, description)
     "preheat_gw_256": (dict(kind="preheating", N=256, spectral=0, with_gw=1, vv=4), 0.005,
                        "256^3 two-field preheating + GW, Yoshida-4"),
+    # the 1024^3 configuration (~90 GB resident): the stated dt = 0.01 breaks the Yoshida-4
+    # stability bound (omega_max dt ~ 8.9 with omega_max = kIR N sqrt(3)/2 ~ 887), so it runs
+    # at the reference's own adaptive rule dt = 0.2 a / (kIR N sqrt(3)/2) at a = 1
+    "preheat_gw_1024": (dict(kind="preheating", N=1024, spectral=0, with_gw=1, vv=4), 0.2 / (1024 * 3 ** 0.5 / 2),
+                        "1024^3 two-field preheating + GW, Yoshida-4"),
     "preheat_256": (dict(kind="preheating", N=256, spectral=1, with_gw=0, vv=4), 0.005,
                     "256^3 two-field preheating (spectral path, no GW), Yoshida-4"),
     "inflation_64": (dict(kind="default", N=64, vv=2), 0.002, "64^3 single-field inflation, velocity Verlet"),
@@ -337,6 +343,47 @@ def run_adjoint(args):
         dist.destroy_process_group()
 
 
+def fft_yardstick(lat, p, reps: int = 10):
+    """The library's 3-D c2r (X, Y inverse passes and the Z c2r pass) of the field arrays
+    beside cuFFT's (torch.fft.irfftn, complex64 -> float32) on the same half spectra: device
+    ms per field, the achieved GB/s against the compulsory bytes of a c2r (read the half
+    spectrum, write the real array) and the max-norm relative difference of the outputs."""
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    if p.precision != 32 or not torch.cuda.is_available():
+        return None
+    N, H = p.N, p.N // 2 + 1
+    ours_ms = lat.time_c2r(reps) / p.nflds
+    f0 = np.zeros((p.nflds, N, N, N))
+    rc = lat._L.psc_get_fields_real(lat._h, f0.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), None)
+    if rc != 0:
+        return None
+    fk = lat.get_state()["f_k"][0].reshape(N, N, H).astype(np.complex64)
+    x = torch.from_numpy(fk).cuda()
+    for _ in range(3):
+        y = torch.fft.irfftn(x, s=(N, N, N))
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record()
+    for _ in range(reps):
+        y = torch.fft.irfftn(x, s=(N, N, N))
+    ev1.record()
+    torch.cuda.synchronize()
+    cufft_ms = ev0.elapsed_time(ev1) / reps
+    yc = y.cpu().numpy().astype(np.float64)
+    diff = float(np.abs(f0[0] - yc).max() / max(np.abs(yc).max(), 1e-300))
+    nbytes = 8 * N * N * H + 4 * N ** 3
+    del x, y
+    torch.cuda.empty_cache()
+    return {"transform": f"3-D c2r {N}^3 fp32 (one field)", "ours_ms": ours_ms, "cufft_ms": cufft_ms,
+            "ours_over_cufft_time": ours_ms / cufft_ms, "compulsory_bytes": nbytes,
+            "ours_gbs": nbytes / (ours_ms / 1e3) / 1e9, "cufft_gbs": nbytes / (cufft_ms / 1e3) / 1e9,
+            "max_rel_diff": diff, "library": "cuFFT via torch.fft (yardstick only, not on the product path)"}
+
+
 def run_ours(args):
     if args.config == "ensemble_mixed":
         return run_ensemble(args)
@@ -350,10 +397,16 @@ def run_ours(args):
     p, dt, desc = make_params(args.config, args.precision)
     lat = Lattice(p)
     lat.initialize()
-    st0 = lat.get_state()   # host copy of the initial state (e2e input)
+    # host copy of the initial state (the e2e input); at 1024^3 the FP64 host state would be
+    # ~140 GB, so that size has no e2e leg and restarts from the device generator instead
+    big = p.N >= 1024
+    st0 = None if big else lat.get_state()
     # warm-up (graph build, first launches)
     lat.evolve(dt, args.warmup)
-    lat.set_state(st0["f_k"], st0["pi_k"], st0["a"], st0["ad"], st0["add"], st0["u_k"], st0["pi_u_k"])
+    if big:
+        lat.initialize()
+    else:
+        lat.set_state(st0["f_k"], st0["pi_k"], st0["a"], st0["ad"], st0["add"], st0["u_k"], st0["pi_u_k"])
 
     clocks = ClockSampler(local)
     barrier(dist)
@@ -368,20 +421,21 @@ def run_ours(args):
     # end to end through the C ABI with host buffers
     import numpy as np  # noqa: F401
 
-    barrier(dist)
-    t0 = time.perf_counter()
-    lat.set_state(st0["f_k"], st0["pi_k"], st0["a"], st0["ad"], st0["add"], st0["u_k"], st0["pi_u_k"])
-    for _ in range(args.steps):
-        lat.evolve(dt, 1)
-        lat.background()
-    out = lat.get_state()
-    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
-    e2e_value = world * p.sites * args.steps / e2e_s
-    csize = 8 if p.precision == 32 else 16
-    state_arrays = 2 * p.nflds + (12 if p.with_gw else 0)
-    state_bytes_host = state_arrays * p.modes * 16   # host buffers are FP64 complex
-    h2d = state_bytes_host / args.steps + 8
-    d2h = state_bytes_host / args.steps + 3 * 8 + 4 + 8
+    e2e = None
+    if not big:
+        barrier(dist)
+        t0 = time.perf_counter()
+        lat.set_state(st0["f_k"], st0["pi_k"], st0["a"], st0["ad"], st0["add"], st0["u_k"], st0["pi_u_k"])
+        for _ in range(args.steps):
+            lat.evolve(dt, 1)
+            lat.background()
+        lat.get_state()
+        e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+        state_arrays = 2 * p.nflds + (12 if p.with_gw else 0)
+        state_bytes_host = state_arrays * p.modes * 16   # host buffers are FP64 complex
+        e2e = {"value": world * p.sites * args.steps / e2e_s, "unit": "site-steps/s",
+               "h2d_bytes_per_step": state_bytes_host / args.steps + 8,
+               "d2h_bytes_per_step": state_bytes_host / args.steps + 3 * 8 + 4 + 8}
 
     # per-pass device times and roofline of the dominant pass
     passes = lat.time_passes(reps=3)
@@ -406,7 +460,7 @@ def run_ours(args):
     # the same K steps in FP64 (the plain method): its rate and the FP32 spectrum error
     # against it (spectra() bins, max-norm relative over bins; GW h^2, hdot^2 when on)
     fp_cmp = None
-    if p.precision == 32 and rank == 0 and not args.no_fp64:
+    if p.precision == 32 and rank == 0 and not args.no_fp64 and not big:
         q = p.copy()
         q.precision = 64
         lat64 = Lattice(q)
@@ -428,7 +482,8 @@ def run_ours(args):
                   "after_steps": args.steps}
 
     if rank == 0:
-        cpu = cpu_sample(p, dt, budget_s=20.0) if (world == 1 and not args.no_cpu) else None
+        yard = None if big else fft_yardstick(lat, p)
+        cpu = cpu_sample(p, dt, budget_s=20.0) if (world == 1 and not args.no_cpu and not big) else None
         line = {
             "metric": "site-steps/s", "value": value, "unit": "site-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -439,8 +494,7 @@ def run_ours(args):
                        "precision": f"fp{p.precision} fields, fp64 background/reductions",
                        "parallelism": f"replicas x{world}" if world > 1 else "single lattice",
                        "l2": "arrays > 129 MB L2 (no flush needed)"},
-            "e2e": {"value": e2e_value, "unit": "site-steps/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
+            "e2e": e2e,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                          "bytes_per_launch": pbytes[dom], "ms_per_launch": passes[dom],
@@ -448,6 +502,7 @@ def run_ours(args):
                                   "achieved": step_achieved, "frac": step_achieved / peak}},
             "passes_ms": passes,
             "fp32_vs_fp64": fp_cmp,
+            "fft_yardstick": yard,
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": gpu_launches,

@@ -60,7 +60,9 @@ typedef struct psc_params {
     int precision;          /* 64: FP64 state (the plain method) or 32: FP32 state, FP64 background */
     int model;              /* PSC_MODEL_* (model.h) */
     int seed;               /* parameters.h:65   Park-Miller seed (rand_uniform, initialize.cpp:13) */
-    int reserved0;
+    int N_pad;              /* parameters.h:13,23 PAD_FLAG / N_pad: 0 = off, else the padded grid of the
+                               dealiased spectral step evolve_VV_k_pad (power of two, N < N_pad <= 1024,
+                               spectral = 1, no GWs) */
     double kIR;             /* parameters.h:27   smallest lattice wavenumber (program units) */
     double a0;              /* parameters.h:29   initial scale factor */
     double MPl;             /* parameters.h:121  Planck mass */
@@ -179,6 +181,22 @@ int psc_last_step_ms(psc_handle *h, float *ms);
  * it was (the evaluations apply zero-length kicks). */
 #define PSC_NPASS 6
 int psc_time_passes(psc_handle *h, int reps, float *ms);
+
+/* Sets the state from a coarser Nsrc lattice (Nsrc < N, power of two; arrays in the
+ * layout of psc_set_state at Nsrc): every mode is placed at its image in this N lattice
+ * by the zero-padding of padding() (evolution.cpp:1271-1443: zero outside the Nsrc band,
+ * each Nyquist index split over its +-Nsrc/2 images with 1/2 per Nyquist axis) with the
+ * amplitudes times (N/Nsrc)^3 for the unnormalised transforms, so the real-space fields
+ * are the spectral interpolation of the coarse ones. u_k, pi_u_k as in psc_set_state. */
+int psc_set_state_padded(psc_handle *h, int Nsrc, const double *f_k, const double *pi_k, double a, double ad,
+                         double add, const double *u_k, const double *pi_u_k);
+
+/* Device time of one c2r of the nflds field arrays f_k to real space (X, Y inverse
+ * passes and the Z c2r pass, the transform of the reference's isChanged block,
+ * output.cpp:1555-1578), averaged over `reps` launches on the handle's stream, ms.
+ * The yardstick against a library 3-D c2r of the same size; the result is left in
+ * the real-space buffer that psc_get_fields_real reads. */
+int psc_time_c2r(psc_handle *h, int reps, float *ms);
 
 /* Compulsory HBM bytes each of the PSC_NPASS passes moves per launch (the bytes
  * of the arrays it must read and write once), for roofline accounting. */

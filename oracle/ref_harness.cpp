@@ -9,8 +9,8 @@
  *   - calls initialize() (initialize.cpp:562) and, with GWs, initialize_GW()
  *     (initialize.cpp:341), then save() (output.cpp:1796) as main does
  *     (pspectcosmo.cpp:489-545);
- *   - steps evolve_VV_k_nopad(dt) (evolution.cpp:1131) or evolve_VV(dt)
- *     (evolution.cpp:607) with the FIXED dt given on the command line instead of
+ *   - steps evolve_VV_k_nopad(dt) (evolution.cpp:1131), evolve_VV_k_pad(dt) with
+ *     PAD_FLAG (evolution.cpp:1688) or evolve_VV(dt) (evolution.cpp:607) with the FIXED dt given on the command line instead of
  *     the adaptive calculate_dt (pspectcosmo.cpp:213-233);
  *   - every `every` steps calls save_Freq(), save_Infreq() and save_Snap(step)
  *     (output.cpp:1831, 1842, 1850) and dumps the raw state.
@@ -58,7 +58,9 @@ static void dump_state(long step) {
 }
 
 static void step_once(double dt_) {
-#if SPECTRAL_FLAG
+#if SPECTRAL_FLAG && PAD_FLAG
+    evolve_VV_k_pad(dt_);
+#elif SPECTRAL_FLAG
     evolve_VV_k_nopad(dt_);
 #else
     evolve_VV(dt_);
@@ -82,6 +84,17 @@ static void *run(void *) {
         kernel_f_k[fld] = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes);
 #endif
     }
+#if SPECTRAL_FLAG && PAD_FLAG
+    // the padded step's buffers (pspectcosmo.cpp:254-271)
+    {
+        const size_t modes_pad = (size_t)N_pad * N_pad * (N_pad / 2 + 1);
+        Cache_Data_k_pad = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes_pad);
+        for (int fld = 0; fld < nflds; fld++) {
+            f_k_pad[fld] = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes_pad);
+            V_prime_k_pad[fld] = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes_pad);
+        }
+    }
+#endif
 #if WITH_GW
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++) {

@@ -499,6 +499,7 @@ int check(psc_handle *h, int obs) {
     const psc_params &p = h->p0();
     if (obs != PSC_OBS_CHI2 && obs != PSC_OBS_RHO_GW) return fail(PSC_ERR_ARG, "unknown observable");
     if (h->R != 1) return fail(PSC_ERR_CONFIG, "the adjoint works on single-lattice handles");
+    if (h->padded) return fail(PSC_ERR_CONFIG, "the adjoint differentiates the unpadded step (N_pad = 0)");
     if (h->cfg.g.N < 32) return fail(PSC_ERR_CONFIG, "the adjoint needs N >= 32");
     if (h->cfg.g.mask)
         return fail(PSC_ERR_CONFIG, "the adjoint differentiates the unmasked step (spectral = 0 or simulate_inflation = 0)");

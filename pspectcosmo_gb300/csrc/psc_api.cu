@@ -7,6 +7,7 @@
 // one launch each (realization = blockIdx.z). psc_create makes R = 1; a batch
 // groups its realizations by configuration into such handles and captures all
 // of them in one CUDA graph per step.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -112,6 +113,12 @@ int validate(const psc_params *p) {
     if (p->precision != 32 && p->precision != 64) return fail(PSC_ERR_CONFIG, "precision must be 32 or 64");
     if (p->with_gw && p->spectral)
         return fail(PSC_ERR_CONFIG, "GWs are evolved on the real-space path only (spectral = 0), as in the reference");
+    if (p->N_pad != 0) {
+        if (!p->spectral || p->with_gw)
+            return fail(PSC_ERR_CONFIG, "the padded step (N_pad) is the spectral step without GWs, as in the reference");
+        if (!pow2(p->N_pad) || p->N_pad <= p->N || p->N_pad > 1024 || p->N_pad < 32)
+            return fail(PSC_ERR_CONFIG, "N_pad must be a power of two with N < N_pad <= 1024 and N_pad >= 32");
+    }
     if (p->expansion < 0 || p->expansion > 2) return fail(PSC_ERR_CONFIG, "expansion must be 0, 1 or 2");
     if (!(p->kIR > 0) || !(p->MPl > 0) || !(p->m_in_MPl > 0) || !(p->a0 > 0))
         return fail(PSC_ERR_CONFIG, "kIR, MPl, m_in_MPl and a0 must be positive");
@@ -236,11 +243,18 @@ psc::LaunchCfg single_cfg(psc_handle *h) {
     return c;
 }
 
+// one force evaluation (with the drift when drift != 0): the padded step's on a padded
+// handle (psc_pad.cu), the fused passes otherwise
+cudaError_t stage_of(psc_handle *h, int drift, cudaStream_t st) {
+    if (h->padded) return psc::launch_pad_stage(h->cfg, h->cfgp, h->b, h->bp, h->p0().precision, drift, st);
+    return psc::launch_stage(h->cfg, h->b, h->p0().precision, drift, st);
+}
+
 // pure evaluation of the force pipeline for all realizations: K, G, V and
 // (keep_add = 0) a''
 int evaluate(psc_handle *h, int keep_add) {
     CU(psc::launch_scalar(h->cfg, h->b, psc::SCALAR_EVAL, 0, h->st));
-    CU(psc::launch_stage(h->cfg, h->b, h->p0().precision, 0, h->st));
+    CU(stage_of(h, 0, h->st));
     CU(psc::launch_scalar(h->cfg, h->b, psc::SCALAR_EVAL_END, keep_add, h->st));
     CU(cudaStreamSynchronize(h->st));
     h->diag_valid = true;
@@ -251,7 +265,7 @@ int evaluate(psc_handle *h, int keep_add) {
 cudaError_t enqueue_step(psc_handle *h, cudaStream_t st) {
     cudaError_t err = cudaSuccess;
     for (int p = 0; p < h->s && err == cudaSuccess; ++p) {
-        err = psc::launch_stage(h->cfg, h->b, h->p0().precision, 1, st);
+        err = stage_of(h, 1, st);
         if (err == cudaSuccess) err = psc::launch_scalar(h->cfg, h->b, psc::SCALAR_END, p, st);
     }
     return err;
@@ -261,7 +275,7 @@ cudaError_t enqueue_step(psc_handle *h, cudaStream_t st) {
 cudaError_t enqueue_prologue(psc_handle *h, double dt, int nsteps, cudaStream_t st) {
     cudaError_t e = psc::launch_set_run(h->b.bg, h->R, dt, nsteps, st);
     if (e == cudaSuccess) e = psc::launch_scalar(h->cfg, h->b, psc::SCALAR_PRIME, 0, st);
-    if (e == cudaSuccess) e = psc::launch_stage(h->cfg, h->b, h->p0().precision, 0, st);
+    if (e == cudaSuccess) e = stage_of(h, 0, st);
     if (e == cudaSuccess) e = psc::launch_scalar(h->cfg, h->b, psc::SCALAR_BEGIN, 0, st);
     return e;
 }
@@ -321,6 +335,18 @@ int create_handle(const psc_params *ps, int R, psc_handle **out) {
     h->csize = p.precision == 32 ? 8 : 16;
     h->nb = psc_maxnumbins(p.N);
     psc::plan(p, R, &h->cfg);
+    h->padded = p.N_pad > 0;
+    if (h->padded) {
+        if (R != 1) {
+            delete h;
+            return fail(PSC_ERR_CONFIG, "padded lattices run one per handle (no batches)");
+        }
+        // the padded step never fills the R_Q2C mask (evolution.cpp:1611-1637): K, G over all modes
+        h->cfg.g.mask = 0;
+        psc_params q = p;
+        q.N = p.N_pad;
+        psc::plan(q, 1, &h->cfgp);
+    }
     const psc::Geo &g = h->cfg.g;
     auto bail = [&](int code) {
         free_all(h);
@@ -338,6 +364,7 @@ int create_handle(const psc_params *ps, int R, psc_handle **out) {
     CUB(cudaEventCreate(&h->ev0));
     CUB(cudaEventCreate(&h->ev1));
     CUB(psc::configure(h->cfg, p.precision));
+    if (h->padded) CUB(psc::configure(h->cfgp, p.precision));
     const size_t farr = (size_t)R * g.fstride * h->csize;   // nf arrays per realization
     const size_t garr = (size_t)R * g.gstride * h->csize;   // 6 arrays per realization (GW)
     psc::Buffers &b = h->b;
@@ -353,7 +380,8 @@ int create_handle(const psc_params *ps, int R, psc_handle **out) {
     if ((rc = dalloc(h, &b.tw, (size_t)g.N * h->csize))) return bail(rc);
     if ((rc = dalloc(h, &tmp, sizeof(double) * (size_t)R * g.pkg_stride))) return bail(rc);
     b.partKG = static_cast<double *>(tmp);
-    if ((rc = dalloc(h, &tmp, sizeof(double) * (size_t)R * g.pv_stride))) return bail(rc);
+    const size_t pv = h->padded ? std::max(g.pv_stride, h->cfgp.g.pv_stride) : g.pv_stride;
+    if ((rc = dalloc(h, &tmp, sizeof(double) * (size_t)R * pv))) return bail(rc);
     b.partV = static_cast<double *>(tmp);
     if ((rc = dalloc(h, &tmp, sizeof(double) * (g.nf * 3 + 2) * h->nb))) return bail(rc);
     b.spec = static_cast<double *>(tmp);
@@ -361,6 +389,19 @@ int create_handle(const psc_params *ps, int R, psc_handle **out) {
     b.spec_cnt = static_cast<int *>(tmp);
     if ((rc = dalloc(h, &tmp, sizeof(psc::DevBG) * R))) return bail(rc);
     b.bg = static_cast<psc::DevBG *>(tmp);
+    if (h->padded) {
+        // N_pad-grid arrays: padded spectra (zero outside the band, written in-band each
+        // stage), the transform intermediates and the N_pad twiddles
+        const psc::Geo &gp = h->cfgp.g;
+        const size_t parr = (size_t)gp.fstride * h->csize;
+        psc::Buffers &bp = h->bp;
+        bp = b;   // partKG, partV, bg shared with the lattice grid
+        if ((rc = dalloc(h, &bp.fk, parr)) || (rc = dalloc(h, &bp.TA, parr)) || (rc = dalloc(h, &bp.QV, parr)) ||
+            (rc = dalloc(h, &bp.tw, (size_t)gp.N * h->csize)))
+            return bail(rc);
+        bp.pk = bp.uk = bp.puk = bp.TB = bp.TC = bp.QS = nullptr;
+        CUB(cudaMemsetAsync(bp.fk, 0, parr, h->st));
+    }
     CUB(cudaMemsetAsync(b.fk, 0, farr, h->st));
     CUB(cudaMemsetAsync(b.pk, 0, farr, h->st));
     if (g.gw) {
@@ -376,6 +417,16 @@ int create_handle(const psc_params *ps, int R, psc_handle **out) {
             tw[2 * q + 1] = -std::sin(ang);
         }
         if ((rc = upload(h, b.tw, tw.data(), g.N))) return bail(rc);
+        if (h->padded) {
+            const int Np = h->cfgp.g.N;
+            tw.assign(2 * Np, 0.0);
+            for (int q = 0; q < Np; ++q) {
+                const double ang = 2.0 * kPi * (double)q / (double)Np;
+                tw[2 * q] = std::cos(ang);
+                tw[2 * q + 1] = -std::sin(ang);
+            }
+            if ((rc = upload(h, h->bp.tw, tw.data(), Np))) return bail(rc);
+        }
     }
     for (int r = 0; r < R; ++r) {
         const psc_params &q = h->p[r];
@@ -400,6 +451,12 @@ int create_handle(const psc_params *ps, int R, psc_handle **out) {
         bg.gsq = q.gsq;
         bg.inv_n3 = 1.0 / (double)g.sites;
         bg.inv_n3sq = bg.inv_n3 * bg.inv_n3;
+        bg.inv_nv = bg.inv_n3;
+        if (h->padded) {
+            // <V> over the padded sites (kernel_a_k_pad, evolution.cpp:1624-1631)
+            bg.nbz = h->cfgp.nbz;
+            bg.inv_nv = 1.0 / (double)h->cfgp.g.sites;
+        }
         if ((rc = write_bg(h, r, bg))) return bail(rc);
     }
 #undef CUB
@@ -771,6 +828,47 @@ int psc_set_state(psc_handle *h, const double *f_k, const double *pi_k, double a
     return set_state(h, 0, f_k, pi_k, a, ad, add, u_k, pi_u_k);
 }
 
+int psc_set_state_padded(psc_handle *h, int Nsrc, const double *f_k, const double *pi_k, double a, double ad,
+                         double add, const double *u_k, const double *pi_u_k) {
+    if (!h || !f_k || !pi_k) return fail(PSC_ERR_ARG, "null argument");
+    if (h->R != 1) return fail(PSC_ERR_CONFIG, "single-lattice handles only");
+    const psc::Geo &g = h->cfg.g;
+    if (!pow2(Nsrc) || Nsrc < 2 || Nsrc >= g.N) return fail(PSC_ERR_ARG, "Nsrc must be a power of two below N");
+    if (g.gw && (!u_k || !pi_u_k)) return fail(PSC_ERR_ARG, "GW run needs u_k and pi_u_k");
+    const size_t ms = (size_t)Nsrc * Nsrc * (Nsrc / 2 + 1);
+    const int prec = h->p0().precision;
+    void *src = nullptr;
+    CU(cudaMallocAsync(&src, ms * 6 * h->csize, h->st));
+    struct Arr { const double *host; void *dev; int count; };
+    std::vector<Arr> arrs = {{f_k, h->b.fk, g.nf}, {pi_k, h->b.pk, g.nf}};
+    if (g.gw) {
+        arrs.push_back({u_k, h->b.uk, 6});
+        arrs.push_back({pi_u_k, h->b.puk, 6});
+    }
+    int rc = PSC_OK;
+    for (const Arr &x : arrs) {
+        if ((rc = upload(h, src, x.host, ms * x.count))) break;
+        const cudaError_t e = psc::launch_prolong(src, x.dev, x.count, Nsrc, g.N, prec, h->st);
+        if (e != cudaSuccess) {
+            rc = fail(PSC_ERR_CUDA, std::string("prolongation: ") + cudaGetErrorString(e));
+            break;
+        }
+    }
+    cudaFreeAsync(src, h->st);
+    if (rc) return rc;
+    CU(cudaStreamSynchronize(h->st));
+    psc::DevBG bg;
+    if ((rc = read_bg(h, 0, &bg))) return rc;
+    bg.a = a;
+    bg.ad = ad;
+    bg.add = add;
+    bg.err = 0;
+    if ((rc = write_bg(h, 0, bg))) return rc;
+    h->have_state = true;
+    h->diag_valid = false;
+    return PSC_OK;
+}
+
 int psc_get_state(psc_handle *h, double *f_k, double *pi_k, double *a, double *ad, double *add, double *u_k,
                   double *pi_u_k) {
     if (!h) return fail(PSC_ERR_ARG, "null handle");
@@ -809,6 +907,7 @@ int psc_last_step_ms(psc_handle *h, float *ms) {
 int psc_time_passes(psc_handle *h, int reps, float *ms) {
     if (!h || !ms || reps < 1) return fail(PSC_ERR_ARG, "bad argument");
     if (!h->have_state) return fail(PSC_ERR_STATE, "no state");
+    if (h->padded) return fail(PSC_ERR_CONFIG, "per-pass times are those of the unpadded step (N_pad = 0)");
     cudaEvent_t ev[7];
     for (int i = 0; i < 7; ++i) CU(cudaEventCreate(&ev[i]));
     double acc[PSC_NPASS] = {0, 0, 0, 0, 0, 0};
@@ -879,6 +978,7 @@ int psc_batch_create(const psc_params *per_realization, int n, psc_batch **out) 
     for (int i = 0; i < n; ++i) {
         int rc = validate(per_realization + i);
         if (rc) return rc;
+        if (per_realization[i].N_pad) return fail(PSC_ERR_CONFIG, "padded lattices run one per handle (no batches)");
     }
     // group realizations that can share launches, in order of first appearance
     std::map<decltype(config_key(per_realization[0])), int> gid;

@@ -24,7 +24,8 @@ struct DevBG {
     double w[kMaxStages];
     // run constants
     double kIR, kIR2, DFDP, eps, fs_over_mpl2, gsq, inv_n3, inv_n3sq;
-    int s, alpha, nf, nterms, mask, model, nbx, nbz;
+    double inv_nv;                  // 1 / (sites the <V> partials sum over): N^3, or N_pad^3 when padded
+    int s, alpha, nf, nterms, mask, model, nbx, nbz;   // nbz: blocks of the <V> partials
     int stage, steps_left, err, pad;
 };
 

@@ -30,6 +30,11 @@ struct psc_handle {
     std::vector<void *> allocs;
     void *adj = nullptr;         // adjoint workspace (psc_adjoint.cu), owned by the handle
     void (*adj_free)(void *) = nullptr;
+    // padded step (N_pad > 0): the launch configuration and buffers of the N_pad grid
+    // (fk = padded spectra, TA, QV = transform intermediates, tw = N_pad twiddles)
+    bool padded = false;
+    psc::LaunchCfg cfgp{};
+    psc::Buffers bp{};
     const psc_params &p0() const { return p[0]; }
 };
 

@@ -516,7 +516,7 @@ __global__ void __launch_bounds__(512) k_scalar(DevBG *bg, const double *__restr
         G += gq;
     }
     for (int tt = 0; tt < bg->nterms; ++tt) {
-        const double v = sums[2 * bg->nf + tt] * bg->inv_n3;
+        const double v = sums[2 * bg->nf + tt] * bg->inv_nv;   // V_E /= N3 (or N3_pad, evolution.cpp:1631)
         bg->V[tt] = v;
         V += v;
     }

@@ -102,6 +102,16 @@ cudaError_t reg_stage_f32(const LaunchCfg &cfg, const Buffers &b, int drift, cud
                           int scalar_mode);
 cudaError_t reg_stage_f64(const LaunchCfg &cfg, const Buffers &b, int drift, cudaStream_t st, cudaEvent_t *ev,
                           int scalar_mode);
+cudaError_t reg_pad_passes_f32(const LaunchCfg &cfg, const Buffers &b, cudaStream_t st);
+cudaError_t reg_pad_passes_f64(const LaunchCfg &cfg, const Buffers &b, cudaStream_t st);
+// The padded step's force evaluation (psc_pad.cu): drift (drift != 0) and padding of f_k
+// into bp.fk, the passes at N_pad (cfgp, bp), extraction, force and kicks at N.
+cudaError_t launch_pad_stage(const LaunchCfg &cfg, const LaunchCfg &cfgp, const Buffers &b, const Buffers &bp,
+                             int precision, int drift, cudaStream_t st);
+// nsrc_arrays half spectra of an Ns lattice -> the Nd lattice (Nd > Ns): zero-padding as
+// padding() does, amplitudes times (Nd/Ns)^3 (dst is zeroed first).
+cudaError_t launch_prolong(const void *src, void *dst, int nsrc_arrays, int Ns, int Nd, int precision,
+                           cudaStream_t st);
 cudaError_t reg_c2r_real_f32(const LaunchCfg &cfg, const Buffers &b, const void *src, int nsrc, cudaStream_t st);
 cudaError_t reg_c2r_real_f64(const LaunchCfg &cfg, const Buffers &b, const void *src, int nsrc, cudaStream_t st);
 // Tiling of the adjoint's scalar Z pass (nf inputs of P = N/32 threads per z line, TL

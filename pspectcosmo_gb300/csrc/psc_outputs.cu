@@ -432,6 +432,23 @@ int psc_write_snapshot(psc_handle *h, const char *path, int with_energy) {
     return write_snapshot(h, 0, path, with_energy);
 }
 
+int psc_time_c2r(psc_handle *h, int reps, float *ms) {
+    if (!h || !ms || reps < 1) return fail(PSC_ERR_ARG, "bad arguments");
+    if (!h->have_state) return fail(PSC_ERR_STATE, "no state");
+    const psc::Buffers b1 = buffers_of(h, 0);
+    int rc = to_real(h, 0, b1.fk, h->cfg.g.nf);   // warm-up (and allocation of the real buffer)
+    if (rc) return rc;
+    CU(cudaEventRecord(h->ev0, h->st));
+    for (int i = 0; i < reps; ++i)
+        if ((rc = to_real(h, 0, b1.fk, h->cfg.g.nf))) return rc;
+    CU(cudaEventRecord(h->ev1, h->st));
+    CU(cudaEventSynchronize(h->ev1));
+    float t = 0.f;
+    CU(cudaEventElapsedTime(&t, h->ev0, h->ev1));
+    *ms = t / (float)reps;
+    return PSC_OK;
+}
+
 int psc_h5_write_f64(const char *path, int n, const char *const *names, const double *const *data, int rank,
                      const uint64_t *dims) {
     if (!path || n < 1 || !names || !data || rank < 1 || !dims) return fail(PSC_ERR_ARG, "bad arguments");

@@ -1033,4 +1033,33 @@ __global__ void __launch_bounds__(256, 2) kr_fft_x_gwadj(Geo g, const cplx<T> *_
         }
 }
 
+// Forward transform along x in place (blockIdx.y selects the array of the list): the
+// last pass of the padded step's r2c on the padded grid, whose kick runs on the
+// lattice grid afterwards.
+template <typename T, int L>
+__global__ void __launch_bounds__(256, 3) kr_fft_x_plain(Geo g, const __grid_constant__ ArrList8 arrs,
+                                                       const cplx<T> *__restrict__ tw) {
+    using C = cplx<T>;
+    using RP = RegPlan<L>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *sm = reinterpret_cast<C *>(smem_raw);
+    C *a = reinterpret_cast<C *>(arrs.p[blockIdx.y]);
+    const int sh = g.tlx_shift, TL = 1 << sh;
+    const int t = threadIdx.x & (TL - 1), j = threadIdx.x >> sh;
+    const int line = blockIdx.x * TL + t;
+    const bool valid = line < g.lines_x;
+    const long long stride = g.lines_x;
+    auto ix = [&](int n) { return n * TL + t; };
+    C v[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) v[r] = valid ? a[(long long)(j + r * RP::P) * stride + line] : mk<T>(0, 0);
+    fft_reg<C, L, -1>(v, sm, ix, j, tw, g.N / L);
+    if (valid) {
+#pragma unroll
+        for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+            for (int r = 0; r < RP::RL; ++r) a[(long long)RP::out(j, q, r) * stride + line] = v[q * RP::RL + r];
+    }
+}
+
 }  // namespace psc

@@ -49,6 +49,7 @@ struct RegLaunch {
             zadj_tile(cfg.g.nf, &tl, &sh);
             SETA((kr_zpass_adj<T, M>), (int)(cfg.g.nf * tl * ZIdx<M>::LS * sizeof(C)));
         }
+        SETA((kr_fft_x_plain<T, N>), sxy);
         SETA((kr_fft_x_adj<T, N>), sxy);
         SETA((kr_fft_x_gwadj<T, N>), sxy);
         {
@@ -118,6 +119,28 @@ struct RegLaunch {
             if (e != cudaSuccess) return e;
             mark(6);
         }
+        return cudaGetLastError();
+    }
+
+    // The transforms of the padded step (evolution.cpp:1639-1661) on the padded grid, this
+    // N being N_pad: c2r of the padded spectra b.fk with the lattice's 1/N^3, V'(f_pad)
+    // and the <V> partials over the padded sites, r2c, ending in k-space in b.QV.
+    static cudaError_t pad_passes(const LaunchCfg &cfg, const Buffers &b, cudaStream_t st) {
+        const Geo &g = cfg.g;
+        const C *tw = reinterpret_cast<const C *>(b.tw);
+        C *fk = (C *)b.fk, *TA = (C *)b.TA, *QV = (C *)b.QV;
+        const dim3 gx(cfg.nbx, g.nf);
+        kr_ifft_x<T, N, false, false><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, fk, nullptr, TA, nullptr, b.bg, tw);
+        kr_ifft_y<T, N, false><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, TA, nullptr, nullptr, b.bg, tw);
+        kr_zpass<T, M, false><<<dim3(cfg.nbz, 1, 1), cfg.thr_z, cfg.smem_z, st>>>(g, TA, nullptr, nullptr, QV, nullptr,
+                                                                                b.partV, b.bg, tw, (T *)nullptr);
+        ArrList8 al{};
+        for (int f = 0; f < g.nf; ++f) {
+            al.rs[f] = g.fstride;
+            al.p[f] = QV + (long long)f * g.modes;
+        }
+        kr_fft_y<T, N><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, al, tw);
+        kr_fft_x_plain<T, N><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, al, tw);
         return cudaGetLastError();
     }
 
@@ -249,6 +272,9 @@ struct RegDispatch {
                                    cudaEvent_t *ev, int scalar_mode) {                                           \
         return RegDispatch<T>::on(cfg.g.N,                                                                       \
                                   [&](auto L) { return decltype(L)::stage(cfg, b, drift, st, ev, scalar_mode); }); \
+    }                                                                                                            \
+    cudaError_t reg_pad_passes_##SUFFIX(const LaunchCfg &cfg, const Buffers &b, cudaStream_t st) {               \
+        return RegDispatch<T>::on(cfg.g.N, [&](auto L) { return decltype(L)::pad_passes(cfg, b, st); });          \
     }                                                                                                            \
     cudaError_t reg_c2r_real_##SUFFIX(const LaunchCfg &cfg, const Buffers &b, const void *src, int nsrc,         \
                                       cudaStream_t st) {                                                         \

@@ -104,6 +104,9 @@ def load_library(path: str | None = None):
                                    ctypes.POINTER(D), ctypes.c_int, ctypes.POINTER(ctypes.c_uint64)]
     L.psc_batch_histograms.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, D, D, D]
     L.psc_batch_write_snapshot.argtypes = [P, ctypes.c_int, ctypes.c_char_p, ctypes.c_int]
+    L.psc_time_c2r.argtypes = [P, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
+    L.psc_set_state_padded.argtypes = [P, ctypes.c_int, D, D, ctypes.c_double, ctypes.c_double, ctypes.c_double, D,
+                                       D]
     L.psc_strerror.argtypes = [ctypes.c_int]
     L.psc_strerror.restype = ctypes.c_char_p
     L.psc_last_error.argtypes = []
@@ -115,7 +118,8 @@ def load_library(path: str | None = None):
                  "psc_batch_set_state", "psc_batch_get_state", "psc_batch_spectra", "psc_batch_energies",
                  "psc_batch_means", "psc_adjoint_chi2", "psc_adjoint_forward_chi2", "psc_adjoint", "psc_adjoint_forward",
                  "psc_histograms", "psc_snapshot_arrays", "psc_write_snapshot", "psc_h5_write_f64",
-                 "psc_batch_histograms", "psc_batch_write_snapshot"):
+                 "psc_batch_histograms", "psc_batch_write_snapshot", "psc_time_c2r",
+                 "psc_set_state_padded"):
         getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L
@@ -199,6 +203,14 @@ class Lattice:
         f_k, pi_k, u_k, pi_u_k = c(f_k), c(pi_k), c(u_k), c(pi_u_k)
         _check(self._L.psc_set_state(self._h, _dp(f_k), _dp(pi_k), a, ad, add, _dp(u_k), _dp(pi_u_k)),
                "psc_set_state")
+
+    def set_state_padded(self, Nsrc: int, f_k, pi_k, a, ad, add, u_k=None, pi_u_k=None):
+        """State of a coarser Nsrc lattice, spectrally interpolated to this N (padding(),
+        evolution.cpp:1271-1443, amplitudes x (N/Nsrc)^3)."""
+        c = lambda x: None if x is None else np.ascontiguousarray(x, np.complex128)
+        f_k, pi_k, u_k, pi_u_k = c(f_k), c(pi_k), c(u_k), c(pi_u_k)
+        _check(self._L.psc_set_state_padded(self._h, int(Nsrc), _dp(f_k), _dp(pi_k), a, ad, add, _dp(u_k),
+                                            _dp(pi_u_k)), "psc_set_state_padded")
 
     def get_state(self):
         p = self.p
@@ -295,6 +307,12 @@ class Lattice:
         ms = (ctypes.c_float * 6)()
         _check(self._L.psc_time_passes(self._h, int(reps), ms), "psc_time_passes")
         return dict(zip(self.PASS_NAMES, [float(x) for x in ms]))
+
+    def time_c2r(self, reps: int = 10) -> float:
+        """Device ms of one c2r of the field arrays to real space (the library's 3-D c2r)."""
+        v = ctypes.c_float()
+        _check(self._L.psc_time_c2r(self._h, int(reps), ctypes.byref(v)), "psc_time_c2r")
+        return v.value
 
     def pass_bytes(self) -> dict:
         """Compulsory HBM bytes per launch of each pass."""

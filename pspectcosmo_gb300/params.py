@@ -29,7 +29,7 @@ class Params(ctypes.Structure):
         ("precision", ctypes.c_int),
         ("model", ctypes.c_int),
         ("seed", ctypes.c_int),
-        ("reserved0", ctypes.c_int),
+        ("N_pad", ctypes.c_int),       # PAD_FLAG / N_pad: 0 = off
         ("kIR", ctypes.c_double),
         ("a0", ctypes.c_double),
         ("MPl", ctypes.c_double),

@@ -32,6 +32,8 @@ RUNS = {
     "spec2_n16_vv4": ("spec2_n16_vv4", 20, 0.005, 10, True),
     "spec2_n32_vv2": ("spec2_n32_vv2", 40, 0.005, 20, False),
     "snap2_n16_vv4": ("snap2_n16_vv4", 20, 0.005, 10, True),
+    "pad1_n16": ("pad1_n16", 20, 0.002, 10, True),
+    "pad2_n16_vv4": ("pad2_n16_vv4", 20, 0.005, 10, True),
     "gw2_n16_vv4": ("gw2_n16_vv4", 10, 0.005, 5, True),
     "gw1_n16_vv2": ("gw1_n16_vv2", 10, 0.002, 5, True),
 }
