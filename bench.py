@@ -361,7 +361,10 @@ def fft_yardstick(lat, p, reps: int = 10):
     rc = lat._L.psc_get_fields_real(lat._h, f0.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), None)
     if rc != 0:
         return None
-    fk = lat.get_state()["f_k"][0].reshape(N, N, H).astype(np.complex64)
+    # the last field: with two fields chi has zero mean, so the comparison sees its
+    # fluctuations (phi's sit below FP32 resolution next to phi0 ~ 0.19)
+    last = p.nflds - 1
+    fk = lat.get_state()["f_k"][last].reshape(N, N, H).astype(np.complex64)
     x = torch.from_numpy(fk).cuda()
     for _ in range(3):
         y = torch.fft.irfftn(x, s=(N, N, N))
@@ -374,14 +377,14 @@ def fft_yardstick(lat, p, reps: int = 10):
     torch.cuda.synchronize()
     cufft_ms = ev0.elapsed_time(ev1) / reps
     yc = y.cpu().numpy().astype(np.float64)
-    diff = float(np.abs(f0[0] - yc).max() / max(np.abs(yc).max(), 1e-300))
+    diff = float(np.abs(f0[last] - yc).max() / max(np.abs(yc).max(), 1e-300))
     nbytes = 8 * N * N * H + 4 * N ** 3
     del x, y
     torch.cuda.empty_cache()
     return {"transform": f"3-D c2r {N}^3 fp32 (one field)", "ours_ms": ours_ms, "cufft_ms": cufft_ms,
             "ours_over_cufft_time": ours_ms / cufft_ms, "compulsory_bytes": nbytes,
             "ours_gbs": nbytes / (ours_ms / 1e3) / 1e9, "cufft_gbs": nbytes / (cufft_ms / 1e3) / 1e9,
-            "max_rel_diff": diff, "library": "cuFFT via torch.fft (yardstick only, not on the product path)"}
+            "max_rel_diff": diff, "compared_field": last, "library": "cuFFT via torch.fft (yardstick only, not on the product path)"}
 
 
 def run_ours(args):

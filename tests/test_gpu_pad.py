@@ -12,7 +12,10 @@
   no product reaches the 32^3 Nyquist and every volume average (K, G, V, rho_GW) and the
   background a, a', a'' evolve identically on every N: equal to 1e-11 (FP64) / 2e-5 (FP32)
   after 3 Yoshida-4 steps of the GW path; in FP32 a'' to 1e-4, the parity tests' FP32
-  bound for it (a'' ~ (V - 2K)/3 cancels: 5e-5 measured at 1024^3).
+  bound for it (a'' ~ (V - 2K)/3 cancels). The step is the reference's adaptive
+  dt = 0.2 a / (kIR N sqrt(3)/2) of the large lattice (pspectcosmo.cpp:213-233): at a fixed
+  dt = 0.005 the modes of a 1024^3 lattice have omega dt up to 4.4, beyond the Yoshida-4
+  bound (~1.57), and the FP32 rounding noise there grows by orders of magnitude per step.
 """
 import os
 import sys
@@ -146,7 +149,7 @@ def test_large_lattices_band_limited(N, precision):
             lat.set_state(f, pi, a0, ad0, add0, u, pu)
         else:
             lat.set_state_padded(32, f, pi, a0, ad0, add0, u, pu)
-        lat.evolve(0.005, 3)
+        lat.evolve(0.2 / (N * 3 ** 0.5 / 2), 3)
         e = lat.energies()
         out[n] = (lat.background(), e)
         lat.close()
