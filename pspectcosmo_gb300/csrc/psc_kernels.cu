@@ -739,9 +739,12 @@ void plan(const psc_params &p, int R, LaunchCfg *cfg) {
     const int nin = g.nf * (g.gw ? 4 : 1), nout = g.nf + (g.gw ? 6 : 0);
     const int nslot = nin > nout ? nin : nout;
     if (g.reg) {
-        // register engine: P = L/16 threads per line, 256 threads per block
+        // register engine: P = L/16 threads per line, 256 threads per block (512 for FP32
+        // 1024-point lines: 8 lines per block, 64 contiguous bytes per row; in FP64 the X
+        // forward pass's three tiles would not fit in shared memory at that width)
         const int P = g.N / 16;
-        int tl = 256 / P;
+        const int xy_thr = (g.N >= 1024 && p.precision == 32) ? 512 : 256;
+        int tl = xy_thr / P;
         while (tl > 1 && tl / 2 >= g.lines_x) tl /= 2;
         g.tlx_shift = ilog2i(tl);
         cfg->thr_xy = tl * P;

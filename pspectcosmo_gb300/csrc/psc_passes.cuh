@@ -15,9 +15,16 @@
 
 namespace psc {
 
+// X/Y pass block sizes: 256 threads, except 512 for 1024-point lines, so that a block
+// still holds 8 lines (64 contiguous bytes of every FP32 row it streams instead of 32).
+// Both give the kernels the same 128-register budget.
+template <int L> constexpr int xy_threads() { return L >= 1024 ? 512 : 256; }
+template <int L> constexpr int xy_blocks(int k) { return L >= 1024 ? 1 : k; }
+
+
 // ------------------------------------------------------------------ X inverse (+ drift, + x-derivative)
 template <typename T, int L, bool GW, bool DRIFT>
-__global__ void __launch_bounds__(256, 2) kr_ifft_x(Geo g, cplx<T> *__restrict__ fk, const cplx<T> *__restrict__ pk,
+__global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_ifft_x(Geo g, cplx<T> *__restrict__ fk, const cplx<T> *__restrict__ pk,
                                                  cplx<T> *__restrict__ TA, cplx<T> *__restrict__ TB,
                                                  const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw) {
     using C = cplx<T>;
@@ -123,7 +130,7 @@ __device__ __forceinline__ void ry_tile(const Geo &g, const cplx<T> *src, cplx<T
 }
 
 template <typename T, int L, bool GW>
-__global__ void __launch_bounds__(256, 2) kr_ifft_y(Geo g, cplx<T> *__restrict__ TA, cplx<T> *__restrict__ TB,
+__global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_ifft_y(Geo g, cplx<T> *__restrict__ TA, cplx<T> *__restrict__ TB,
                                                  cplx<T> *__restrict__ TC, const DevBG *__restrict__ bg,
                                                  const cplx<T> *__restrict__ tw) {
     using C = cplx<T>;
@@ -193,7 +200,7 @@ struct ArrList8 {
 };
 
 template <typename T, int L>
-__global__ void __launch_bounds__(256, 3) kr_fft_y(Geo g, const __grid_constant__ ArrList8 arrs,
+__global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(3)) kr_fft_y(Geo g, const __grid_constant__ ArrList8 arrs,
                                                  const cplx<T> *__restrict__ tw) {
     using C = cplx<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -204,7 +211,7 @@ __global__ void __launch_bounds__(256, 3) kr_fft_y(Geo g, const __grid_constant_
 
 // ------------------------------------------------------------------ X forward + kick epilogue
 template <typename T, int L, bool GW>
-__global__ void __launch_bounds__(256, 2) kr_fft_x_final(Geo g, const cplx<T> *__restrict__ QV,
+__global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_fft_x_final(Geo g, const cplx<T> *__restrict__ QV,
                                                       const cplx<T> *__restrict__ QS, const cplx<T> *__restrict__ fk,
                                                       cplx<T> *__restrict__ pk, cplx<T> *__restrict__ uk,
                                                       cplx<T> *__restrict__ puk, double *__restrict__ partKG,
@@ -795,7 +802,7 @@ __global__ void __launch_bounds__(256, 2) kr_zpass_adj(Geo g, const cplx<T> *__r
 // X forward transform of the adjoint's J^T application with its epilogue:
 // Lf += fft_x(QV) + eta1 k^2 M + delta k^2 f  (blockIdx.y = field).
 template <typename T, int L>
-__global__ void __launch_bounds__(256, 2) kr_fft_x_adj(Geo g, const cplx<T> *__restrict__ QV,
+__global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_fft_x_adj(Geo g, const cplx<T> *__restrict__ QV,
                                                     const cplx<T> *__restrict__ Mk, const cplx<T> *__restrict__ fk,
                                                     cplx<T> *__restrict__ Lf, const DevAdj *__restrict__ ad,
                                                     const cplx<T> *__restrict__ tw) {
@@ -972,7 +979,7 @@ __global__ void __launch_bounds__(256) kr_zpass_adj_gw(Geo g, const cplx<T> *__r
 // gradient: Lf += etaS sum_a i k_a fft_x(T_a), k_a with the Nyquist bin zeroed
 // (field_1st_derivative evolution.cpp:466-578), etaS = -a^(1+alpha).
 template <typename T, int L>
-__global__ void __launch_bounds__(256, 2) kr_fft_x_gwadj(Geo g, const cplx<T> *__restrict__ Tin,
+__global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_fft_x_gwadj(Geo g, const cplx<T> *__restrict__ Tin,
                                                       cplx<T> *__restrict__ Lf, const DevAdj *__restrict__ ad,
                                                       const cplx<T> *__restrict__ tw) {
     using C = cplx<T>;
@@ -1037,7 +1044,7 @@ __global__ void __launch_bounds__(256, 2) kr_fft_x_gwadj(Geo g, const cplx<T> *_
 // last pass of the padded step's r2c on the padded grid, whose kick runs on the
 // lattice grid afterwards.
 template <typename T, int L>
-__global__ void __launch_bounds__(256, 3) kr_fft_x_plain(Geo g, const __grid_constant__ ArrList8 arrs,
+__global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(3)) kr_fft_x_plain(Geo g, const __grid_constant__ ArrList8 arrs,
                                                        const cplx<T> *__restrict__ tw) {
     using C = cplx<T>;
     using RP = RegPlan<L>;
