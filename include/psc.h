@@ -165,10 +165,26 @@ int psc_snapshot_arrays(psc_handle *h, double *f, double *pot, double *kin, doub
  * the file cannot be written. */
 int psc_write_snapshot(psc_handle *h, const char *path, int with_energy);
 
+/* Checkpoint / resume in a fixed format (the reference's own checkpoint, output.cpp:1652-1705,
+ * stores only real-space fields and cannot resume a k-space run, initialize.cpp:590-620).
+ * An HDF5 file (the library's writer) with the full state in the layout of psc_get_state:
+ * /f_k, /pi_k [nflds][N*N*(N/2+1)][2] and with GWs /u_k, /pi_u_k [6][...][2], FP64;
+ * /background = {t, a, a', a''}; /lattice = {N, nflds, with_gw, spectral, N_pad, vv,
+ * model, precision}. psc_checkpoint_read restores state, background and t into a handle
+ * of the same N, nflds and with_gw (PSC_ERR_CONFIG otherwise); a run continued from it
+ * repeats the uninterrupted run bit for bit. */
+int psc_checkpoint_write(psc_handle *h, const char *path);
+int psc_checkpoint_read(psc_handle *h, const char *path);
+
 /* The HDF5 writer alone (host only): n datasets names[i] of shape dims[0..rank) from
  * the host FP64 arrays data[i], in the layout psc_write_snapshot uses. */
 int psc_h5_write_f64(const char *path, int n, const char *const *names, const double *const *data, int rank,
                      const uint64_t *dims);
+/* Reading back a file in that layout (host only; other HDF5 layouts are refused with
+ * PSC_ERR_IO): the shape of dataset `name` (rank, dims[0..min(rank, maxrank))) and its
+ * count FP64 values. */
+int psc_h5_dataset_shape(const char *path, const char *name, uint64_t *dims, int maxrank, int *rank);
+int psc_h5_read_f64(const char *path, const char *name, double *out, uint64_t count);
 
 /* Device-time of the last psc_step call (CUDA events on the handle's stream), ms. */
 int psc_last_step_ms(psc_handle *h, float *ms);

@@ -64,10 +64,17 @@ int Writer::fail(const std::string &m) {
 
 int Writer::open(const std::string &path, const std::vector<std::string> &names_in,
                  const std::vector<uint64_t> &dims) {
+    return open(path, names_in, std::vector<std::vector<uint64_t>>(names_in.size(), dims));
+}
+
+int Writer::open(const std::string &path, const std::vector<std::string> &names_in,
+                 const std::vector<std::vector<uint64_t>> &shapes) {
     if (!host_little_endian()) return fail("the HDF5 writer stores little-endian doubles from host memory");
     const size_t n = names_in.size();
     if (n == 0) return fail("no datasets");
-    if (dims.empty() || dims.size() > 32) return fail("dataset rank must be 1..32");
+    if (shapes.size() != n) return fail("one shape per dataset");
+    for (const auto &dims : shapes)
+        if (dims.empty() || dims.size() > 32) return fail("dataset rank must be 1..32");
     std::vector<std::string> names(n);
     for (size_t i = 0; i < n; ++i) {
         names[i] = (!names_in[i].empty() && names_in[i][0] == '/') ? names_in[i].substr(1) : names_in[i];
@@ -95,15 +102,19 @@ int Writer::open(const std::string &path, const std::vector<std::string> &names_
     const uint64_t free_off = heap_size;
     heap_size += 16;
 
-    uint64_t elems = 1;
-    for (uint64_t d : dims) {
-        if (d == 0) return fail("zero-sized dimension");
-        elems *= d;
+    data_bytes_.assign(n, 0);
+    std::vector<uint64_t> oh_size(n), oh_addr(n);
+    const size_t type_sz = 24, fill_sz = 8, layout_sz = 24;
+    for (size_t i = 0; i < n; ++i) {
+        uint64_t elems = 1;
+        for (uint64_t d : shapes[i]) {
+            if (d == 0) return fail("zero-sized dimension");
+            elems *= d;
+        }
+        data_bytes_[i] = elems * 8;
+        const size_t space_sz = 8 + 8 * shapes[i].size();
+        oh_size[i] = 16 + (8 + space_sz) + (8 + type_sz) + (8 + fill_sz) + (8 + layout_sz);
     }
-    data_bytes_ = elems * 8;
-    const size_t rank = dims.size();
-    const size_t space_sz = 8 + 8 * rank, type_sz = 24, fill_sz = 8, layout_sz = 24;
-    const size_t dset_oh = 16 + (8 + space_sz) + (8 + type_sz) + (8 + fill_sz) + (8 + layout_sz);
 
     const uint64_t root_oh = kSuperblock;
     const uint64_t heap_hdr = root_oh + 16 + 8 + 16;
@@ -111,10 +122,18 @@ int Writer::open(const std::string &path, const std::vector<std::string> &names_
     const uint64_t btree = heap_data + heap_size;
     const uint64_t snod0 = btree + kBtree;
     const uint64_t oh0 = snod0 + nsnod * kSnod;
-    const uint64_t meta_end = oh0 + n * dset_oh;
+    uint64_t meta_end = oh0;
+    for (size_t i = 0; i < n; ++i) {
+        oh_addr[i] = meta_end;
+        meta_end += oh_size[i];
+    }
     data_addr_.assign(n, 0);
-    for (size_t i = 0; i < n; ++i) data_addr_[i] = align8(meta_end) + i * data_bytes_;
-    const uint64_t eof = data_addr_[n - 1] + data_bytes_;
+    uint64_t at_data = align8(meta_end);
+    for (size_t i = 0; i < n; ++i) {
+        data_addr_[i] = at_data;
+        at_data += data_bytes_[i];
+    }
+    const uint64_t eof = at_data;
 
     Buf o((size_t)meta_end);
     // superblock version 0
@@ -177,17 +196,19 @@ int Writer::open(const std::string &path, const std::vector<std::string> &names_
         for (size_t e = 0; e < cnt; ++e) {
             const size_t i = order[first + e], ep = at + 8 + e * kEntry;
             o.le(ep, name_off[i], 8);
-            o.le(ep + 8, oh0 + i * dset_oh, 8);   // cache type 0, empty scratch pad
+            o.le(ep + 8, oh_addr[i], 8);   // cache type 0, empty scratch pad
         }
     }
 
     // dataset object headers (version 1)
     for (size_t i = 0; i < n; ++i) {
-        const size_t at = oh0 + i * dset_oh;
+        const size_t at = oh_addr[i];
+        const std::vector<uint64_t> &dims = shapes[i];
+        const size_t rank = dims.size(), space_sz = 8 + 8 * rank;
         o.u8(at, 1);
         o.le(at + 2, 4, 2);
         o.le(at + 4, 1, 4);
-        o.le(at + 8, dset_oh - 16, 4);
+        o.le(at + 8, oh_size[i] - 16, 4);
         // dataspace, version 1: rank, no maximum dimensions
         d = msg(o, at + 16, 0x0001, (unsigned)space_sz, 0);
         o.u8(d, 1);
@@ -219,7 +240,7 @@ int Writer::open(const std::string &path, const std::vector<std::string> &names_
         o.u8(d, 3);
         o.u8(d + 1, 1);
         o.le(d + 2, data_addr_[i], 8);
-        o.le(d + 10, data_bytes_, 8);
+        o.le(d + 10, data_bytes_[i], 8);
     }
 
     fp_ = std::fopen(path.c_str(), "wb");
@@ -236,7 +257,7 @@ int Writer::write(int i, const double *data) {
     if (!fp_) return fail("file not open");
     if (i < 0 || (size_t)i >= data_addr_.size()) return fail("no such dataset");
     if (fseeko(fp_, (off_t)data_addr_[i], SEEK_SET) != 0) return fail("seek failed");
-    const size_t cnt = (size_t)(data_bytes_ / 8);
+    const size_t cnt = (size_t)(data_bytes_[i] / 8);
     if (std::fwrite(data, 8, cnt, fp_) != cnt) return fail("write failed");
     return 0;
 }
@@ -247,6 +268,134 @@ int Writer::close() {
     fp_ = nullptr;
     if (rc != 0) return fail("close failed");
     return 0;
+}
+
+Reader::~Reader() {
+    if (fp_) std::fclose(fp_);
+}
+
+int Reader::fail(const std::string &m) {
+    err_ = m;
+    return -1;
+}
+
+int Reader::get(uint64_t addr, void *dst, size_t n) {
+    if (addr > eof_ || n > eof_ - addr) return fail("structure outside the file");
+    if (fseeko(fp_, (off_t)addr, SEEK_SET) != 0 || std::fread(dst, 1, n, fp_) != n) return fail("read failed");
+    return 0;
+}
+
+namespace {
+uint64_t rd(const unsigned char *p, int nbytes) {
+    uint64_t v = 0;
+    for (int i = nbytes - 1; i >= 0; --i) v = (v << 8) | p[i];
+    return v;
+}
+}  // namespace
+
+int Reader::open(const std::string &path) {
+    if (!host_little_endian()) return fail("the HDF5 reader fills little-endian doubles into host memory");
+    fp_ = std::fopen(path.c_str(), "rb");
+    if (!fp_) return fail("cannot open " + path);
+    if (fseeko(fp_, 0, SEEK_END) != 0) return fail("seek failed");
+    eof_ = (uint64_t)ftello(fp_);
+    unsigned char sb[kSuperblock];
+    if (get(0, sb, sizeof sb)) return -1;
+    const unsigned char sig[8] = {0x89, 'H', 'D', 'F', '\r', '\n', 0x1a, '\n'};
+    if (std::memcmp(sb, sig, 8) != 0) return fail("not an HDF5 file (at offset 0)");
+    if (sb[8] != 0 || sb[13] != 8 || sb[14] != 8) return fail("unsupported HDF5 superblock");
+    if (rd(sb + 24, 8) != 0) return fail("unsupported base address");
+    const uint64_t btree = rd(sb + 80, 8), heap = rd(sb + 88, 8);
+    if (rd(sb + 72, 4) != 1) return fail("root group without a cached symbol table");
+    unsigned char hh[kHeapHeader];
+    if (get(heap, hh, sizeof hh)) return -1;
+    if (std::memcmp(hh, "HEAP", 4) != 0) return fail("bad local heap");
+    const uint64_t heap_size = rd(hh + 8, 8), heap_data = rd(hh + 24, 8);
+    if (heap_size > (1u << 24)) return fail("local heap too large");
+    std::vector<unsigned char> names(heap_size + 1, 0);
+    if (get(heap_data, names.data(), heap_size)) return -1;
+    std::vector<unsigned char> bt(kBtree);
+    if (get(btree, bt.data(), bt.size())) return -1;
+    if (std::memcmp(bt.data(), "TREE", 4) != 0 || bt[4] != 0 || bt[5] != 0)
+        return fail("unsupported group B-tree (only one leaf node)");
+    const unsigned used = (unsigned)rd(bt.data() + 6, 2);
+    if (used > 2u * kInternalK) return fail("bad B-tree node");
+    for (unsigned c = 0; c < used; ++c) {
+        const uint64_t snod = rd(bt.data() + 24 + 8 + 16 * c, 8);
+        std::vector<unsigned char> sn(kSnod);
+        if (get(snod, sn.data(), sn.size())) return -1;
+        if (std::memcmp(sn.data(), "SNOD", 4) != 0) return fail("bad symbol table node");
+        const unsigned nsym = (unsigned)rd(sn.data() + 6, 2);
+        if (nsym > 2u * kLeafK) return fail("bad symbol table node");
+        for (unsigned e = 0; e < nsym; ++e) {
+            const unsigned char *ep = sn.data() + 8 + e * kEntry;
+            const uint64_t off = rd(ep, 8);
+            if (off >= heap_size) return fail("bad link name");
+            links_.emplace_back(std::string(reinterpret_cast<const char *>(names.data() + off)), rd(ep + 8, 8));
+        }
+    }
+    return 0;
+}
+
+int Reader::dataset(const std::string &name_in, Dset *d) {
+    const std::string name = (!name_in.empty() && name_in[0] == '/') ? name_in.substr(1) : name_in;
+    uint64_t oh = 0;
+    bool found = false;
+    for (const auto &l : links_)
+        if (l.first == name) {
+            oh = l.second;
+            found = true;
+        }
+    if (!found) return fail("no dataset " + name);
+    unsigned char pre[16];
+    if (get(oh, pre, sizeof pre)) return -1;
+    if (pre[0] != 1) return fail("unsupported object header");
+    const unsigned nmsg = (unsigned)rd(pre + 2, 2);
+    const uint64_t size = rd(pre + 8, 4);
+    if (size > 4096) return fail("object header too large");
+    std::vector<unsigned char> m(size);
+    if (get(oh + 16, m.data(), m.size())) return -1;
+    bool space = false, type = false, layout = false;
+    size_t q = 0;
+    for (unsigned i = 0; i < nmsg && q + 8 <= m.size(); ++i) {
+        const unsigned mt = (unsigned)rd(&m[q], 2), ms = (unsigned)rd(&m[q + 2], 2);
+        if (q + 8 + ms > m.size()) return fail("bad object header message");
+        const unsigned char *b = &m[q + 8];
+        if (mt == 0x0001) {
+            if (b[0] != 1 || ms < 8u + 8u * b[1]) return fail("unsupported dataspace");
+            d->dims.clear();
+            for (int r = 0; r < b[1]; ++r) d->dims.push_back(rd(b + 8 + 8 * r, 8));
+            space = true;
+        } else if (mt == 0x0003) {
+            if ((b[0] & 0x0f) != 1 || (b[1] & 1) != 0 || rd(b + 4, 4) != 8) return fail("dataset is not F64LE");
+            type = true;
+        } else if (mt == 0x0008) {
+            if (b[0] != 3 || b[1] != 1) return fail("dataset is not contiguous");
+            d->addr = rd(b + 2, 8);
+            d->bytes = rd(b + 10, 8);
+            layout = true;
+        }
+        q += 8 + ms;
+    }
+    if (!space || !type || !layout) return fail("incomplete dataset header: " + name);
+    uint64_t count = 1;
+    for (uint64_t x : d->dims) count *= x;
+    if (count * 8 != d->bytes) return fail("dataset size disagrees with its shape: " + name);
+    return 0;
+}
+
+int Reader::shape(const std::string &name, std::vector<uint64_t> *dims) {
+    Dset d;
+    if (dataset(name, &d)) return -1;
+    *dims = d.dims;
+    return 0;
+}
+
+int Reader::read(const std::string &name, double *out, size_t count) {
+    Dset d;
+    if (dataset(name, &d)) return -1;
+    if (d.bytes != (uint64_t)count * 8) return fail("dataset " + name + " has another size");
+    return get(d.addr, out, (size_t)d.bytes);
 }
 
 }  // namespace h5

@@ -31,6 +31,9 @@ class Writer {
     // each of shape `dims` (row-major, last dimension fastest), and writes all
     // metadata. Returns 0 or -1 (see error()).
     int open(const std::string &path, const std::vector<std::string> &names, const std::vector<uint64_t> &dims);
+    // The same with a shape per dataset.
+    int open(const std::string &path, const std::vector<std::string> &names,
+             const std::vector<std::vector<uint64_t>> &shapes);
     // Writes the whole of dataset i (in the order given to open) from `data`.
     int write(int i, const double *data);
     int close();
@@ -39,8 +42,33 @@ class Writer {
   private:
     int fail(const std::string &msg);
     std::FILE *fp_ = nullptr;
-    std::vector<uint64_t> data_addr_;
-    uint64_t data_bytes_ = 0;
+    std::vector<uint64_t> data_addr_, data_bytes_;
+    std::string err_;
+};
+
+// Reads the files Writer writes (superblock 0, symbol-table root group, version-1
+// object headers, contiguous IEEE F64LE datasets); anything else is refused.
+class Reader {
+  public:
+    ~Reader();
+    int open(const std::string &path);
+    // shape of dataset `name` (a leading '/' is dropped); -1 if absent
+    int shape(const std::string &name, std::vector<uint64_t> *dims);
+    // reads the whole dataset (count = product of its dims) into out
+    int read(const std::string &name, double *out, size_t count);
+    const std::string &error() const { return err_; }
+
+  private:
+    struct Dset {
+        std::vector<uint64_t> dims;
+        uint64_t addr = 0, bytes = 0;
+    };
+    int fail(const std::string &msg);
+    int get(uint64_t addr, void *dst, size_t n);
+    int dataset(const std::string &name, Dset *d);
+    std::FILE *fp_ = nullptr;
+    uint64_t eof_ = 0;
+    std::vector<std::pair<std::string, uint64_t>> links_;   // name -> object header address
     std::string err_;
 };
 

@@ -49,6 +49,10 @@ int write_bg(psc_handle *h, int r, const DevBG &in);
 int step(psc_handle *h, double dt, int nsteps);
 int evaluate(psc_handle *h, int keep_add);
 Buffers buffers_of(psc_handle *h, int r);
+int set_state(psc_handle *h, int r, const double *f_k, const double *pi_k, double a, double ad, double add,
+              const double *u_k, const double *pi_u_k);
+int get_state(psc_handle *h, int r, double *f_k, double *pi_k, double *a, double *ad, double *add, double *u_k,
+              double *pi_u_k);
 LaunchCfg single_cfg(psc_handle *h);
 // psc_outputs.cu: histograms and snapshot datasets of realization r
 int histograms(psc_handle *h, int r, int nbins, double hmin, double hmax, double *binfreq, double *bmin, double *df);

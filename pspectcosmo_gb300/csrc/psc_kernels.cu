@@ -454,34 +454,58 @@ __device__ double friedmann_add(const DevBG *bg, double K, double G, double V) {
     return 1. / 3. * bg->fs_over_mpl2 * ipow(bg->a, 1 + 2 * al) * ((al - 2) * K + al * G + (al + 1) * V);
 }
 
-__global__ void __launch_bounds__(512) k_scalar(DevBG *bg, const double *__restrict__ partKG,
+__global__ void __launch_bounds__(1024) k_scalar(DevBG *bg, const double *__restrict__ partKG,
                                                 const double *__restrict__ partV, int mode, int p, int pkg_stride,
                                                 int pv_stride) {
-    __shared__ double red[512];
+    constexpr int NQ = 2 * kMaxFields + kMaxTerms;
+    __shared__ double red[32][NQ];
     bg += blockIdx.x;
     partKG += (size_t)blockIdx.x * pkg_stride;
     partV += (size_t)blockIdx.x * pv_stride;
-    __shared__ double sums[2 * kMaxFields + kMaxTerms];
+    __shared__ double sums[NQ];
     const bool reduce = (mode == SCALAR_END || mode == SCALAR_EVAL_END);
     if (reduce) {
+        // every quantity in one sweep (all loads of a thread in flight together), then
+        // one warp-shuffle + shared-memory tree for all of them
         const int nbx = bg->nbx, nbz = bg->nbz, nf = bg->nf, nt = bg->nterms;
-        const int nq = 2 * nf + nt;
-        for (int q = 0; q < nq; ++q) {
-            double acc = 0.0;
-            if (q < 2 * nf) {
-                for (int i = threadIdx.x; i < nbx; i += blockDim.x) acc += partKG[(size_t)q * nbx + i];
-            } else {
-                for (int i = threadIdx.x; i < nbz; i += blockDim.x) acc += partV[(size_t)(q - 2 * nf) * nbz + i];
+        double acc[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) acc[q] = 0.0;
+#pragma unroll 4
+        for (int i = threadIdx.x; i < nbx; i += blockDim.x)
+#pragma unroll
+            for (int q = 0; q < 2 * kMaxFields; ++q)
+                if (q < 2 * nf) acc[q] += partKG[(size_t)q * nbx + i];
+        // fixed slots (K, G of field f at 2f, 2f+1; term t at 2 kMaxFields + t): no
+        // run-time register index
+#pragma unroll 8
+        for (int i = threadIdx.x; i < nbz; i += blockDim.x)
+#pragma unroll
+            for (int q = 0; q < kMaxTerms; ++q)
+                if (q < nt) acc[2 * kMaxFields + q] += partV[(size_t)q * nbz + i];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q)
+            for (int o = 16; o > 0; o >>= 1) acc[q] += __shfl_down_sync(0xffffffffu, acc[q], o);
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        if (lane == 0)
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) red[warp][q] = acc[q];
+        __syncthreads();
+        if (warp == 0) {
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) {
+                double x = lane < nw ? red[lane][q] : 0.0;
+                for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+                if (lane == 0) {
+                    if (q < 2 * kMaxFields) {
+                        if (q < 2 * nf) sums[q] = x;
+                    } else if (q - 2 * kMaxFields < nt) {
+                        sums[2 * nf + (q - 2 * kMaxFields)] = x;
+                    }
+                }
             }
-            red[threadIdx.x] = acc;
-            __syncthreads();
-            for (int s = blockDim.x >> 1; s > 0; s >>= 1) {
-                if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
-                __syncthreads();
-            }
-            if (threadIdx.x == 0) sums[q] = red[0];
-            __syncthreads();
         }
+        __syncthreads();
     }
     if (threadIdx.x != 0) return;
     if (mode == SCALAR_PRIME) {
@@ -877,7 +901,7 @@ static cudaError_t launch_stage_t(const LaunchCfg &cfg, const Buffers &b, int dr
     else k_fft_x_final<T, false><<<gf, cfg.thr_xy, cfg.smem_xy, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw);
     mark(5);
     if (scalar_mode >= 0) {
-        k_scalar<<<cfg.R, 512, 0, st>>>(b.bg, b.partKG, b.partV, scalar_mode, 1, cfg.g.pkg_stride, cfg.g.pv_stride);
+        k_scalar<<<cfg.R, 1024, 0, st>>>(b.bg, b.partKG, b.partV, scalar_mode, 1, cfg.g.pkg_stride, cfg.g.pv_stride);
         mark(6);
     }
     return cudaGetLastError();
@@ -900,7 +924,7 @@ cudaError_t launch_stage(const LaunchCfg &cfg, const Buffers &b, int precision, 
 }
 
 cudaError_t launch_scalar(const LaunchCfg &cfg, const Buffers &b, int mode, int p, cudaStream_t st) {
-    k_scalar<<<cfg.R, 512, 0, st>>>(b.bg, b.partKG, b.partV, mode, p, cfg.g.pkg_stride, cfg.g.pv_stride);
+    k_scalar<<<cfg.R, 1024, 0, st>>>(b.bg, b.partKG, b.partV, mode, p, cfg.g.pkg_stride, cfg.g.pv_stride);
     return cudaGetLastError();
 }
 

@@ -1,4 +1,5 @@
-// psc_outputs.cu — output-step quantities of the real-space fields, on the device:
+// psc_outputs.cu — output-step quantities of the real-space fields, on the device, and
+// the checkpoint files:
 //   * histograms()      output.cpp:1193-1297 (bin frequencies, lower edge, bin width);
 //   * snapshots()       output.cpp:1541-1648 (the fields and, with SNAPSHOTS_ENERGY,
 //     the lattice energy densities: kinetic_energy_lattice / gradient_energy_lattice
@@ -410,6 +411,77 @@ int write_snapshot(psc_handle *h, int r, const char *path, int with_energy) {
     return PSC_OK;
 }
 
+// Checkpoint file (HDF5, the library's writer): f_k, pi_k [nflds][modes][2] and with GWs
+// u_k, pi_u_k [6][modes][2] in the layout of psc_get_state, background = {t, a, a', a''},
+// lattice = {N, nflds, with_gw, spectral, N_pad, vv, model, precision}.
+int checkpoint_write(psc_handle *h, int r, const char *path) {
+    if (!path) return fail(PSC_ERR_ARG, "null path");
+    if (!h->have_state) return fail(PSC_ERR_STATE, "no state");
+    const Geo &g = h->cfg.g;
+    const psc_params &q = h->p[r];
+    const uint64_t n = (uint64_t)g.modes, nf = (uint64_t)g.nf;
+    std::vector<double> fk(2 * n * nf), pk(2 * n * nf), uk, puk;
+    if (g.gw) {
+        uk.resize(2 * n * 6);
+        puk.resize(2 * n * 6);
+    }
+    double bgv[4];
+    int rc = get_state(h, r, fk.data(), pk.data(), bgv + 1, bgv + 2, bgv + 3, g.gw ? uk.data() : nullptr,
+                       g.gw ? puk.data() : nullptr);
+    if (rc) return rc;
+    DevBG bg;
+    if ((rc = read_bg(h, r, &bg))) return rc;
+    bgv[0] = bg.t;
+    const double lat[8] = {(double)q.N, (double)q.nflds, (double)q.with_gw, (double)q.spectral, (double)q.N_pad,
+                           (double)q.vv, (double)q.model, (double)q.precision};
+    std::vector<std::string> names = {"/f_k", "/pi_k", "/background", "/lattice"};
+    std::vector<std::vector<uint64_t>> shapes = {{nf, n, 2}, {nf, n, 2}, {4}, {8}};
+    std::vector<const double *> data = {fk.data(), pk.data(), bgv, lat};
+    if (g.gw) {
+        names.push_back("/u_k");
+        names.push_back("/pi_u_k");
+        shapes.push_back({6, n, 2});
+        shapes.push_back({6, n, 2});
+        data.push_back(uk.data());
+        data.push_back(puk.data());
+    }
+    h5::Writer w;
+    if (w.open(path, names, shapes)) return fail(PSC_ERR_IO, w.error());
+    for (size_t i = 0; i < data.size(); ++i)
+        if (w.write((int)i, data[i])) return fail(PSC_ERR_IO, w.error());
+    if (w.close()) return fail(PSC_ERR_IO, w.error());
+    return PSC_OK;
+}
+
+int checkpoint_read(psc_handle *h, int r, const char *path) {
+    if (!path) return fail(PSC_ERR_ARG, "null path");
+    const Geo &g = h->cfg.g;
+    const psc_params &q = h->p[r];
+    h5::Reader rd;
+    if (rd.open(path)) return fail(PSC_ERR_IO, rd.error());
+    double lat[8], bgv[4];
+    if (rd.read("/lattice", lat, 8) || rd.read("/background", bgv, 4)) return fail(PSC_ERR_IO, rd.error());
+    if ((int)lat[0] != q.N || (int)lat[1] != q.nflds || (int)lat[2] != q.with_gw)
+        return fail(PSC_ERR_CONFIG, "checkpoint of another lattice (N, nflds or with_gw differ)");
+    const size_t n = (size_t)g.modes;
+    std::vector<double> fk(2 * n * g.nf), pk(2 * n * g.nf), uk, puk;
+    if (rd.read("/f_k", fk.data(), fk.size()) || rd.read("/pi_k", pk.data(), pk.size()))
+        return fail(PSC_ERR_IO, rd.error());
+    if (g.gw) {
+        uk.resize(2 * n * 6);
+        puk.resize(2 * n * 6);
+        if (rd.read("/u_k", uk.data(), uk.size()) || rd.read("/pi_u_k", puk.data(), puk.size()))
+            return fail(PSC_ERR_IO, rd.error());
+    }
+    int rc = set_state(h, r, fk.data(), pk.data(), bgv[1], bgv[2], bgv[3], g.gw ? uk.data() : nullptr,
+                       g.gw ? puk.data() : nullptr);
+    if (rc) return rc;
+    DevBG bg;
+    if ((rc = read_bg(h, r, &bg))) return rc;
+    bg.t = bgv[0];
+    return write_bg(h, r, bg);
+}
+
 }  // namespace hapi
 }  // namespace psc
 
@@ -449,6 +521,16 @@ int psc_time_c2r(psc_handle *h, int reps, float *ms) {
     return PSC_OK;
 }
 
+int psc_checkpoint_write(psc_handle *h, const char *path) {
+    if (!h) return fail(PSC_ERR_ARG, "null handle");
+    return checkpoint_write(h, 0, path);
+}
+
+int psc_checkpoint_read(psc_handle *h, const char *path) {
+    if (!h) return fail(PSC_ERR_ARG, "null handle");
+    return checkpoint_read(h, 0, path);
+}
+
 int psc_h5_write_f64(const char *path, int n, const char *const *names, const double *const *data, int rank,
                      const uint64_t *dims) {
     if (!path || n < 1 || !names || !data || rank < 1 || !dims) return fail(PSC_ERR_ARG, "bad arguments");
@@ -462,6 +544,23 @@ int psc_h5_write_f64(const char *path, int n, const char *const *names, const do
     for (int i = 0; i < n; ++i)
         if (w.write(i, data[i])) return fail(PSC_ERR_IO, w.error());
     if (w.close()) return fail(PSC_ERR_IO, w.error());
+    return PSC_OK;
+}
+
+int psc_h5_dataset_shape(const char *path, const char *name, uint64_t *dims, int maxrank, int *rank) {
+    if (!path || !name || !rank || (maxrank > 0 && !dims)) return fail(PSC_ERR_ARG, "bad arguments");
+    psc::h5::Reader rd;
+    std::vector<uint64_t> d;
+    if (rd.open(path) || rd.shape(name, &d)) return fail(PSC_ERR_IO, rd.error());
+    *rank = (int)d.size();
+    for (int i = 0; i < maxrank && i < (int)d.size(); ++i) dims[i] = d[i];
+    return PSC_OK;
+}
+
+int psc_h5_read_f64(const char *path, const char *name, double *out, uint64_t count) {
+    if (!path || !name || !out) return fail(PSC_ERR_ARG, "bad arguments");
+    psc::h5::Reader rd;
+    if (rd.open(path) || rd.read(name, out, (size_t)count)) return fail(PSC_ERR_IO, rd.error());
     return PSC_OK;
 }
 

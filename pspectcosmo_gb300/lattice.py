@@ -107,6 +107,11 @@ def load_library(path: str | None = None):
     L.psc_time_c2r.argtypes = [P, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
     L.psc_set_state_padded.argtypes = [P, ctypes.c_int, D, D, ctypes.c_double, ctypes.c_double, ctypes.c_double, D,
                                        D]
+    L.psc_checkpoint_write.argtypes = [P, ctypes.c_char_p]
+    L.psc_checkpoint_read.argtypes = [P, ctypes.c_char_p]
+    L.psc_h5_dataset_shape.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint64),
+                                       ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+    L.psc_h5_read_f64.argtypes = [ctypes.c_char_p, ctypes.c_char_p, D, ctypes.c_uint64]
     L.psc_strerror.argtypes = [ctypes.c_int]
     L.psc_strerror.restype = ctypes.c_char_p
     L.psc_last_error.argtypes = []
@@ -119,7 +124,8 @@ def load_library(path: str | None = None):
                  "psc_batch_means", "psc_adjoint_chi2", "psc_adjoint_forward_chi2", "psc_adjoint", "psc_adjoint_forward",
                  "psc_histograms", "psc_snapshot_arrays", "psc_write_snapshot", "psc_h5_write_f64",
                  "psc_batch_histograms", "psc_batch_write_snapshot", "psc_time_c2r",
-                 "psc_set_state_padded"):
+                 "psc_set_state_padded", "psc_checkpoint_write", "psc_checkpoint_read",
+                 "psc_h5_dataset_shape", "psc_h5_read_f64"):
         getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L
@@ -150,6 +156,19 @@ def h5_write(path: str, datasets: dict) -> None:
     ptrs = (ctypes.POINTER(ctypes.c_double) * len(arrs))(*[_dp(x) for x in arrs])
     dims = (ctypes.c_uint64 * len(shape))(*shape)
     _check(L.psc_h5_write_f64(os.fsencode(path), len(arrs), names, ptrs, len(shape), dims), "psc_h5_write_f64")
+
+
+def h5_read(path: str, name: str) -> np.ndarray:
+    """One FP64 dataset of a file in the library's HDF5 layout (snapshots, checkpoints)."""
+    L = load_library()
+    dims = (ctypes.c_uint64 * 32)()
+    rank = ctypes.c_int()
+    _check(L.psc_h5_dataset_shape(os.fsencode(path), name.encode(), dims, 32, ctypes.byref(rank)),
+           "psc_h5_dataset_shape")
+    shape = tuple(int(dims[i]) for i in range(rank.value))
+    out = np.empty(shape, dtype=np.float64)
+    _check(L.psc_h5_read_f64(os.fsencode(path), name.encode(), _dp(out), out.size), "psc_h5_read_f64")
+    return out
 
 
 def generate_ic(params: Params):
@@ -376,6 +395,14 @@ class Lattice:
         _check(self._L.psc_snapshot_arrays(self._h, _dp(out.get("f")), _dp(out.get("pot")), _dp(out.get("kin")),
                                            _dp(out.get("grad")), _dp(out.get("tot"))), "psc_snapshot_arrays")
         return out
+
+    def checkpoint(self, path: str) -> None:
+        """Full state, background and time to an HDF5 checkpoint file."""
+        _check(self._L.psc_checkpoint_write(self._h, os.fsencode(path)), "psc_checkpoint_write")
+
+    def restore(self, path: str) -> None:
+        """Resume from a checkpoint file of a lattice with the same N, nflds, with_gw."""
+        _check(self._L.psc_checkpoint_read(self._h, os.fsencode(path)), "psc_checkpoint_read")
 
     def write_snapshot(self, path: str, with_energy: bool = True) -> None:
         """The reference's data_<step>_snapshot.h5 (output.cpp:1541-1648) at `path`."""

@@ -123,3 +123,25 @@ def test_writer_rejects_bad_input(tmp_path, psc_lib):
         h5_write(str(tmp_path / "x.h5"), {"/g/a": np.zeros(4)})                    # not in the root group
     with pytest.raises(PscError):
         h5_write(str(tmp_path / "no_such_dir" / "x.h5"), {"a": np.zeros(4)})
+
+
+def test_reader_round_trip(tmp_path, psc_lib):
+    """The library's reader on the library's files (host only)."""
+    from pspectcosmo_gb300.lattice import h5_read, h5_write
+
+    rng = np.random.default_rng(9)
+    data = {"/a": rng.standard_normal((3, 5)), "/b": rng.standard_normal((3, 5))}
+    path = str(tmp_path / "x.h5")
+    h5_write(path, data)
+    for k, v in data.items():
+        assert np.array_equal(h5_read(path, k), v)
+        assert np.array_equal(h5_read(path, k.lstrip("/")), v)
+
+
+def test_reader_refuses_other_layouts(psc_lib):
+    from pspectcosmo_gb300.lattice import PscError, h5_read
+
+    if SCIPY_H5 is None:
+        pytest.skip("SciPy's HDF5 test file is not installed")
+    with pytest.raises(PscError):
+        h5_read(SCIPY_H5, "testdouble")   # user block + layout version 2: not this library's layout
