@@ -500,6 +500,7 @@ int check(psc_handle *h, int obs) {
     if (obs != PSC_OBS_CHI2 && obs != PSC_OBS_RHO_GW) return fail(PSC_ERR_ARG, "unknown observable");
     if (h->R != 1) return fail(PSC_ERR_CONFIG, "the adjoint works on single-lattice handles");
     if (h->padded) return fail(PSC_ERR_CONFIG, "the adjoint differentiates the unpadded step (N_pad = 0)");
+    h->force_valid = false;   // the reverse sweep rewrites the stage buffers
     if (h->cfg.g.N < 32) return fail(PSC_ERR_CONFIG, "the adjoint needs N >= 32");
     if (h->cfg.g.mask)
         return fail(PSC_ERR_CONFIG, "the adjoint differentiates the unmasked step (spectral = 0 or simulate_inflation = 0)");
@@ -817,6 +818,8 @@ extern "C" int psc_adjoint(psc_handle *h, int observable_id, double dt, int nste
         if ((rc = save_state(r, ws->ckpt + (size_t)nseg * ws->ckpt_stride))) return rc;
         if ((rc = seed())) return rc;
     }
+    // the segment replays below rewrite the state and the kept force
+    h->force_valid = false;
     for (int seg = nseg - 1; seg >= 0; --seg) {
         const int n = std::min(every, nsteps - seg * every);
         if (nseg > 1 && (rc = restore_state(r, ws->ckpt + (size_t)seg * ws->ckpt_stride))) return rc;

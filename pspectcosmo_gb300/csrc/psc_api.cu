@@ -226,6 +226,8 @@ psc::Buffers buffers_of(psc_handle *h, int r) {
     b.pk = foff(h, h->b.pk, r);
     b.TA = foff(h, h->b.TA, r);
     b.QV = foff(h, h->b.QV, r);
+    if (h->b.Fk) b.Fk = foff(h, h->b.Fk, r);
+    if (h->b.Fu) b.Fu = goff(h, h->b.Fu, r);
     if (h->cfg.g.gw) {
         b.uk = goff(h, h->b.uk, r);
         b.puk = goff(h, h->b.puk, r);
@@ -275,7 +277,10 @@ cudaError_t enqueue_step(psc_handle *h, cudaStream_t st) {
 cudaError_t enqueue_prologue(psc_handle *h, double dt, int nsteps, cudaStream_t st) {
     cudaError_t e = psc::launch_set_run(h->b.bg, h->R, dt, nsteps, st);
     if (e == cudaSuccess) e = psc::launch_scalar(h->cfg, h->b, psc::SCALAR_PRIME, 0, st);
-    if (e == cudaSuccess) e = stage_of(h, 0, st);
+    // the force at the current (f, a) is the one the previous call's last kick kept: the
+    // opening half kick needs no force evaluation then (same arithmetic, same bits)
+    if (e == cudaSuccess)
+        e = h->force_valid ? psc::launch_open_kick(h->cfg, h->b, h->p0().precision, st) : stage_of(h, 0, st);
     if (e == cudaSuccess) e = psc::launch_scalar(h->cfg, h->b, psc::SCALAR_BEGIN, 0, st);
     return e;
 }
@@ -389,6 +394,12 @@ int create_handle(const psc_params *ps, int R, psc_handle **out) {
     b.spec_cnt = static_cast<int *>(tmp);
     if ((rc = dalloc(h, &tmp, sizeof(psc::DevBG) * R))) return bail(rc);
     b.bg = static_cast<psc::DevBG *>(tmp);
+    // the kept force (register-engine and padded steps; the small-N generic engine
+    // evaluates the opening force every call)
+    if (g.reg || h->padded) {
+        if ((rc = dalloc(h, &b.Fk, farr))) return bail(rc);
+        if (g.gw && (rc = dalloc(h, &b.Fu, garr))) return bail(rc);
+    }
     if (h->padded) {
         // N_pad-grid arrays: padded spectra (zero outside the band, written in-band each
         // stage), the transform intermediates and the N_pad twiddles
@@ -400,6 +411,7 @@ int create_handle(const psc_params *ps, int R, psc_handle **out) {
             (rc = dalloc(h, &bp.tw, (size_t)gp.N * h->csize)))
             return bail(rc);
         bp.pk = bp.uk = bp.puk = bp.TB = bp.TC = bp.QS = nullptr;
+        bp.Fk = bp.Fu = nullptr;
         CUB(cudaMemsetAsync(bp.fk, 0, parr, h->st));
     }
     CUB(cudaMemsetAsync(b.fk, 0, farr, h->st));
@@ -518,6 +530,7 @@ int init_ic(psc_handle *h) {
         if ((rc = write_bg(h, r, bg))) return rc;
     }
     h->have_state = true;
+    h->force_valid = false;
     // initialize() ends with add = kernel_a_k_nopad() / kernel_a() (initialize.cpp:786-797)
     return evaluate(h, 0);
 }
@@ -543,6 +556,7 @@ int set_state(psc_handle *h, int r, const double *f_k, const double *pi_k, doubl
     if ((rc = write_bg(h, r, bg))) return rc;
     h->have_state = true;
     h->diag_valid = false;
+    h->force_valid = false;
     return PSC_OK;
 }
 
@@ -571,15 +585,22 @@ int step(psc_handle *h, double dt, int nsteps) {
     if (nsteps == 0) return PSC_OK;
     int rc = build_graph(h);
     if (rc) return rc;
+    const bool kept = h->force_valid;
+    h->force_valid = false;
     CU(cudaEventRecord(h->ev0, h->st));
     // opening half kick: pi_half = pi + w0 dt/2 F(f, a)  (evolution.cpp:1144-1158, stage 0)
-    CU(enqueue_prologue(h, dt, nsteps, h->st));
+    h->force_valid = kept;
+    const cudaError_t pe = enqueue_prologue(h, dt, nsteps, h->st);
+    h->force_valid = false;
+    CU(pe);
     for (int i = 0; i < nsteps; ++i) CU(cudaGraphLaunch(h->gexec, h->st));
     CU(cudaEventRecord(h->ev1, h->st));
     const int err = read_err(h);
     CU(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
     h->diag_valid = true;
+    h->force_valid = false;
     if (err) return fail(err, "non-finite background (NaN/Inf in a, a' or a'') during the step");
+    h->force_valid = h->b.Fk != nullptr;
     return PSC_OK;
 }
 
@@ -866,6 +887,7 @@ int psc_set_state_padded(psc_handle *h, int Nsrc, const double *f_k, const doubl
     if ((rc = write_bg(h, 0, bg))) return rc;
     h->have_state = true;
     h->diag_valid = false;
+    h->force_valid = false;
     return PSC_OK;
 }
 

@@ -23,6 +23,9 @@ struct psc_handle {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaGraphExec_t gexec = nullptr;
     bool have_state = false;
+    // the kept force (b.Fk, b.Fu) is that of the current state: the last call was a step
+    // call that ended with a synchronising kick and nothing has changed the state since
+    bool force_valid = false;
     bool diag_valid = false;
     float last_ms = 0.f;
     void *stage_buf = nullptr;   // pinned staging for precision conversion

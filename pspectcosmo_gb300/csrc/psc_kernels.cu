@@ -928,6 +928,47 @@ cudaError_t launch_scalar(const LaunchCfg &cfg, const Buffers &b, int mode, int 
     return cudaGetLastError();
 }
 
+// pi += c_open F (pi_u += c_open F_u) for every realization: the opening half kick of a step
+// call (evolution.cpp:1144-1158) from the force the previous call's last kick kept, with the
+// epilogue's own arithmetic (pf = p + c_close F, then pf + c_open F).
+template <typename T>
+__global__ void __launch_bounds__(256) k_open_kick(Geo g, cplx<T> *__restrict__ pk, const cplx<T> *__restrict__ Fk,
+                                                   cplx<T> *__restrict__ puk, const cplx<T> *__restrict__ Fu,
+                                                   const DevBG *__restrict__ bg) {
+    const int arr = blockIdx.y, r = blockIdx.z;
+    bg += r;
+    cplx<T> *p;
+    const cplx<T> *F;
+    if (arr < g.nf) {
+        const long long off = (long long)r * g.fstride + (long long)arr * g.modes;
+        p = pk + off;
+        F = Fk + off;
+    } else {
+        const long long off = (long long)r * g.gstride + (long long)(arr - g.nf) * g.modes;
+        p = puk + off;
+        F = Fu + off;
+    }
+    const T c_close = (T)bg->c_close, c_open = (T)bg->c_open;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < g.modes; m += stride) {
+        const cplx<T> f = F[m], q = p[m];
+        const cplx<T> pf = mk<T>(q.x + c_close * f.x, q.y + c_close * f.y);
+        p[m] = mk<T>(pf.x + c_open * f.x, pf.y + c_open * f.y);
+    }
+}
+
+cudaError_t launch_open_kick(const LaunchCfg &cfg, const Buffers &b, int precision, cudaStream_t st) {
+    const Geo &g = cfg.g;
+    const dim3 grid(2 * 152, g.nf + (g.gw ? 6 : 0), cfg.R);
+    if (precision == 32)
+        k_open_kick<float><<<grid, 256, 0, st>>>(g, (float2 *)b.pk, (const float2 *)b.Fk, (float2 *)b.puk,
+                                                 (const float2 *)b.Fu, b.bg);
+    else
+        k_open_kick<double><<<grid, 256, 0, st>>>(g, (double2 *)b.pk, (const double2 *)b.Fk, (double2 *)b.puk,
+                                                  (const double2 *)b.Fu, b.bg);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_set_run(DevBG *bg, int R, double dt, int nsteps, cudaStream_t st) {
     k_set_run<<<1, 128, 0, st>>>(bg, R, dt, nsteps);
     return cudaGetLastError();

@@ -59,6 +59,10 @@ struct Buffers {
     // state f, pi (synchronised), V'_k and the real fields f(x); with GWs also pi_u
     // (synchronised) and -kIR^2 k^2 u + S_k (the GW force without its a^(1+alpha))
     void *tape_f, *tape_p, *tape_vp, *tape_fx, *tape_pu, *tape_fu;
+    // the force of the last synchronising kick (c_open = 0), per mode: F of the fields
+    // [nf][modes] and a^(1+alpha)(-k^2 u + S) of the GW [6][modes]. The opening half kick of
+    // the next step call uses it instead of a force evaluation (null: not kept)
+    void *Fk, *Fu;
 };
 
 enum ScalarMode {
@@ -84,6 +88,8 @@ cudaError_t launch_stage_timed(const LaunchCfg &cfg, const Buffers &b, int preci
                                cudaEvent_t *ev, cudaStream_t st);
 cudaError_t launch_scalar(const LaunchCfg &cfg, const Buffers &b, int mode, int p, cudaStream_t st);
 cudaError_t launch_set_run(DevBG *bg, int R, double dt, int nsteps, cudaStream_t st);
+// The opening half kick of a step call from the kept force: pi += c_open F (and pi_u).
+cudaError_t launch_open_kick(const LaunchCfg &cfg, const Buffers &b, int precision, cudaStream_t st);
 // Real-space view of nsrc complex arrays (c2r / N^3) into b.real (precision T).
 cudaError_t launch_c2r_real(const LaunchCfg &cfg, const Buffers &b, int precision, const void *src, int nsrc,
                             cudaStream_t st);

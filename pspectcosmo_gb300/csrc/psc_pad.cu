@@ -71,19 +71,22 @@ __global__ void __launch_bounds__(kPadThreads) k_pad_scatter(cplx<T> *__restrict
 // stage (as the unpadded kick epilogue: closing half kick -> synchronised pi for the
 // K, G partials, then the opening half kick of the next stage). One field per blockIdx.y;
 // gridDim.x = the lattice's nbx (the K, G partial layout the background kernel reads).
-template <typename T>
+template <typename T, typename C_ = cplx<T>>
 __global__ void __launch_bounds__(kPadThreads) k_pad_kick(const cplx<T> *__restrict__ qvp, const cplx<T> *__restrict__ fk,
                                                           cplx<T> *__restrict__ pk, double *__restrict__ partKG,
                                                           int N, int Np, long long modes, long long modes_p,
-                                                          T inv_ratio3, const DevBG *__restrict__ bg) {
+                                                          T inv_ratio3, const DevBG *__restrict__ bg,
+                                                          C_ *__restrict__ fcache) {
     using C = cplx<T>;
     const int H = N / 2 + 1, Hp = Np / 2 + 1, h = N / 2;
     const int fld = blockIdx.y;
     qvp += (long long)fld * modes_p;
     fk += (long long)fld * modes;
     pk += (long long)fld * modes;
+    if (fcache) fcache += (long long)fld * modes;
     const T norm1 = (T)bg->norm1, norm2 = (T)bg->norm2, kIR2 = (T)bg->kIR2;
     const T c_close = (T)bg->c_close, c_open = (T)bg->c_open;
+    const bool keep = bg->c_open == 0.0 && fcache != nullptr;   // the force of a synchronising kick
     T accK = T(0), accG = T(0);
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < modes; m += stride) {
@@ -109,6 +112,7 @@ __global__ void __launch_bounds__(kPadThreads) k_pad_kick(const cplx<T> *__restr
         accK += wgt * (pf.x * pf.x + pf.y * pf.y);
         accG += wgt * k2 * (f.x * f.x + f.y * f.y);
         pk[m] = mk<T>(pf.x + c_open * F.x, pf.y + c_open * F.y);
+        if (keep) fcache[m] = F;
     }
     T vals[2] = {accK, accG};
     block_reduce_store_t<T, 2>(vals, partKG + (size_t)(2 * fld) * gridDim.x, gridDim.x, blockIdx.x);
@@ -133,7 +137,7 @@ cudaError_t pad_stage_t(const LaunchCfg &cfg, const LaunchCfg &cfgp, const Buffe
     // extract_padding divides by pow(N_pad / N, 3): an exact power of two here
     const double r = (double)gp.N / (double)g.N;
     k_pad_kick<T><<<grid, kPadThreads, 0, st>>>((const C *)bp.QV, (const C *)b.fk, (C *)b.pk, b.partKG, g.N, gp.N,
-                                                g.modes, gp.modes, (T)(1.0 / (r * r * r)), b.bg);
+                                                g.modes, gp.modes, (T)(1.0 / (r * r * r)), b.bg, (C *)b.Fk);
     return cudaGetLastError();
 }
 

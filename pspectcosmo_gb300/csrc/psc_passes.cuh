@@ -220,7 +220,9 @@ __global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_fft_x_fin
                                                       cplx<T> *__restrict__ tape_p = nullptr,
                                                       cplx<T> *__restrict__ tape_vp = nullptr,
                                                       cplx<T> *__restrict__ tape_pu = nullptr,
-                                                      cplx<T> *__restrict__ tape_fu = nullptr) {
+                                                      cplx<T> *__restrict__ tape_fu = nullptr,
+                                                      cplx<T> *__restrict__ fcache = nullptr,
+                                                      cplx<T> *__restrict__ ucache = nullptr) {
     using C = cplx<T>;
     using RP = RegPlan<L>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -230,7 +232,9 @@ __global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_fft_x_fin
         QV += rf;
         fk += rf;
         pk += rf;
+        if (fcache) fcache += rf;
         if (GW) {
+            if (ucache) ucache += rg;
             QS += rg;
             uk += rg;
             puk += rg;
@@ -272,6 +276,8 @@ __global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_fft_x_fin
 
     const T norm1 = (T)bg->norm1, norm2 = (T)bg->norm2, kIR2 = (T)bg->kIR2;
     const T c_close = (T)bg->c_close, c_open = (T)bg->c_open;
+    // a synchronising kick (the last of a step call, or an evaluation) keeps its force
+    const bool keep = bg->c_open == 0.0;
     const int y = line / H, kz = line - y * H;
     const int py = pcoord(y, N);
     if (field) {
@@ -307,6 +313,7 @@ __global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_fft_x_fin
                         accG += wgt * k2 * (f.x * f.x + f.y * f.y);
                     }
                     pk[a] = mk<T>(pf.x + c_open * F.x, pf.y + c_open * F.y);
+                    if (keep && fcache) fcache[a] = F;
                     if (tape_p) {   // adjoint tape: the synchronised stage-point state
                         tape_f[a] = f;
                         tape_p[a] = pf;
@@ -338,6 +345,7 @@ __global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_fft_x_fin
                 const C wf = mk<T>(w.x + c_close * F.x, w.y + c_close * F.y);
                 uk[a] = u;
                 puk[a] = mk<T>(wf.x + c_open * F.x, wf.y + c_open * F.y);
+                if (keep && ucache) ucache[a] = F;
                 if (tape_pu) {   // adjoint tape: synchronised pi_u and the force without a^(1+alpha)
                     tape_pu[a] = wf;
                     tape_fu[a] = fu;

@@ -109,10 +109,12 @@ struct RegLaunch {
         if (g.gw)
             kr_fft_x_final<T, N, true><<<gf, txy, cfg.smem_xf, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw,
                                                                       (C *)b.tape_f, (C *)b.tape_p, (C *)b.tape_vp,
-                                                                      (C *)b.tape_pu, (C *)b.tape_fu);
+                                                                      (C *)b.tape_pu, (C *)b.tape_fu, (C *)b.Fk,
+                                                                      (C *)b.Fu);
         else
             kr_fft_x_final<T, N, false><<<gf, txy, cfg.smem_xf, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw,
-                                                                       (C *)b.tape_f, (C *)b.tape_p, (C *)b.tape_vp);
+                                                                       (C *)b.tape_f, (C *)b.tape_p, (C *)b.tape_vp,
+                                                                       nullptr, nullptr, (C *)b.Fk, nullptr);
         mark(5);
         if (scalar_mode >= 0) {
             cudaError_t e = launch_scalar(cfg, b, scalar_mode, 1, st);
