@@ -54,6 +54,8 @@ CONFIGS: dict[str, tuple[str, dict[str, str]]] = {
         "initfield[]": "{0.193 * MPl, 0.}",
         "initderivs[]": "{-0.142e-6 * MPl * MPl, 0.}",
     }),
+    # the reference's own main() (adaptive dt, output cadence) on the shipped model, to t = 0.02
+    "drive1_n16": ("phi2", {"N": "16", "tf": "0.02", "tOutputInfreq": "0.005"}),
     # the dealiased spectral step evolve_VV_k_pad (PAD_FLAG, V' on an N_pad = 2N grid)
     "pad1_n16": ("phi2", {"N": "16", "PAD_FLAG": "true", "N_pad": "32"}),
     "pad2_n16_vv4": ("phi2chi2", {

@@ -18,6 +18,7 @@
  * keeps N^3 arrays on the stack (evolution.cpp:612, 441, 581).
  *
  * usage: harness NSTEPS DT EVERY      (run inside the output directory)
+ *        harness main                 (the reference's own main(): its adaptive-dt driver loop)
  * writes: output/*.txt (reference writers, 17 digits), state_<step>.bin, bg.txt,
  *         ic_info.txt, and with ssnapshot output/Snapshots/data_<step>_snapshot.h5.*.bin
  *         (the raw datasets, through the HDF5 shim)
@@ -27,6 +28,7 @@
 #include <pthread.h>
 #include <cstdio>
 #include <cstdlib>
+#include <string>
 
 static long g_nsteps = 0, g_every = 1;
 static double g_dt = 0.0;
@@ -135,9 +137,26 @@ static void *run(void *) {
     return nullptr;
 }
 
+int reference_main();   // the reference's own main() (pspectcosmo.cpp:236), renamed at compile time
+
+static void *run_reference_main(void *) {
+    reference_main();
+    return nullptr;
+}
+
 int main(int argc, char **argv) {
+    if (argc == 2 && std::string(argv[1]) == "main") {
+        // the reference's own driver: adaptive dt, output cadence (pspectcosmo.cpp:600-697)
+        pthread_attr_t attr;
+        pthread_attr_init(&attr);
+        pthread_attr_setstacksize(&attr, (size_t)2 << 30);
+        pthread_t th;
+        if (pthread_create(&th, &attr, run_reference_main, nullptr) != 0) return 3;
+        pthread_join(th, nullptr);
+        return 0;
+    }
     if (argc < 4) {
-        std::fprintf(stderr, "usage: %s NSTEPS DT EVERY\n", argv[0]);
+        std::fprintf(stderr, "usage: %s NSTEPS DT EVERY | %s main\n", argv[0], argv[0]);
         return 2;
     }
     g_nsteps = std::atol(argv[1]);

@@ -101,6 +101,14 @@ class TextWriter:
     def _e(x):
         return f"{x:15.6e}"
 
+    def save(self, lat, numsteps: int = 0, ssnapshot: bool = False):
+        """save() (output.cpp:1796-1829): meansvars, scale, energy, histograms, the snapshot
+        when ssnapshot, spectra."""
+        self.save_freq(lat)
+        if ssnapshot:
+            self.snapshot(lat, numsteps)
+        self.save_infreq(lat)
+
     def save_freq(self, lat):
         """save_Freq(): meansvars, scale, energy (output.cpp:1831-1840)."""
         p = self.p

@@ -189,9 +189,37 @@ def generate(run: str) -> str:
     return path
 
 
+# runs of the reference's own main() (its adaptive-dt driver loop and output cadence)
+MAIN_RUNS = {"drive1_n16": "drive1_n16"}
+
+
+def generate_main(run: str) -> str:
+    cfg = MAIN_RUNS[run]
+    exe = os.path.join(ROOT, "oracle", "_ref", cfg, "harness")
+    if not os.path.exists(exe):
+        import build_ref  # noqa: E402
+
+        exe = build_ref.build(cfg)
+    with tempfile.TemporaryDirectory() as tmp:
+        res = subprocess.run([exe, "main"], cwd=tmp, stdin=subprocess.DEVNULL, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise SystemExit(f"{run}: reference main failed\n{res.stderr}")
+        o = os.path.join(tmp, "output")
+        out = {}
+        for name in ("average_scalar_0", "average_scale_factor", "average_energies", "average_energy_conservation",
+                     "average_spectra_times", "histogramtimes"):
+            out[name] = read_rows(os.path.join(o, name + ".txt"))
+        out["spectra_scalar_0"] = read_blocks(os.path.join(o, "spectra_scalar_0.txt"))
+        out["histogram0"] = read_blocks(os.path.join(o, "histogram0.txt"))[..., 0]
+        out["meta"] = np.array(json.dumps({"run": run, "config": cfg, "mode": "reference main()"}))
+    path = os.path.join(HERE, f"{run}.npz")
+    np.savez_compressed(path, **out)
+    return path
+
+
 def main(argv):
-    for run in (argv or list(RUNS)):
-        p = generate(run)
+    for run in (argv or list(RUNS) + list(MAIN_RUNS)):
+        p = generate_main(run) if run in MAIN_RUNS else generate(run)
         print(f"{p}  {os.path.getsize(p) / 1024:.0f} KiB")
 
 

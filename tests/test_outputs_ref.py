@@ -145,3 +145,12 @@ def test_reader_refuses_other_layouts(psc_lib):
         pytest.skip("SciPy's HDF5 test file is not installed")
     with pytest.raises(PscError):
         h5_read(SCIPY_H5, "testdouble")   # user block + layout version 2: not this library's layout
+
+
+def test_calculate_dt():
+    """calculate_dt (pspectcosmo.cpp:213-233): 2 / (k / a) / 10, host arithmetic."""
+    from pspectcosmo_gb300.driver import calculate_dt
+
+    k = 25 * 16 * 3 ** 0.5 / 2
+    assert calculate_dt(k, 1.0) == 2.0 / (k / 1.0) / 10
+    assert calculate_dt(k, 2.0) == 2 * calculate_dt(k, 1.0)
