@@ -35,6 +35,8 @@ def run(p: Params, tf: float, tOutputFreq: float, tOutputInfreq: float, tSnapFre
     lat = lattice if lattice is not None else Lattice(p)
     lat.initialize()
     w = writer if writer is not None else TextWriter(p, dir_)
+    t0 = lat.t
+    w.info_begin(0.0)   # initialize() ends with output_parameters() (initialize.cpp:803); dt is not set yet
     numsteps = 0
     w.save(lat, numsteps, ssnapshot)
     t = lat.t
@@ -58,4 +60,5 @@ def run(p: Params, tf: float, tOutputFreq: float, tOutputInfreq: float, tSnapFre
             numsteps += 1
             if ssnapshot:
                 w.snapshot(lat, numsteps)
+    w.info_end(t0, t)   # output_parameters() after the loop (pspectcosmo.cpp:699)
     return lat

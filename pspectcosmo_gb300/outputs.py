@@ -101,6 +101,59 @@ class TextWriter:
     def _e(x):
         return f"{x:15.6e}"
 
+    @staticmethod
+    def _g(x) -> str:
+        """A double as an ostream prints it by default (6 significant digits, %g)."""
+        return f"{x:g}"
+
+    @staticmethod
+    def readable_time(t: int) -> str:
+        """readable_time (output.cpp:1708-1744)."""
+        if t == 0:
+            return "less than 1 second\n"
+        parts = []
+        for unit, name in ((86400, "days"), (3600, "hours"), (60, "minutes")):
+            if t > unit:
+                parts.append(f"{t // unit} {name}")
+                t %= unit
+        if t > 0:
+            parts.append(f"{t} seconds")
+        return ", ".join(parts) + "\n"
+
+    def info_begin(self, dt: float = 0.0):
+        """output_parameters() at the start of a run (output.cpp:1750-1786): info.txt with the
+        model and program information and the start time."""
+        import time
+
+        p, g = self.p, self._g
+        omega = p.m_in_MPl * p.f_star
+        lines = ["--------------------------\n", "Model Specific Information\n", "--------------------------\n"]
+        if p.model == 1:
+            lines += ["two-field phi^2 + g^2 phi^2 chi^2 Model\n", "V = 1/2 m^2 PHI^2 + 1/2 g^2 PHI^2 CHI^2\n\n",
+                      f"m_in_MPl = {g(p.m_in_MPl)}\n", f"g^2 (program units) = {g(p.gsq)}\n"]
+        else:
+            lines += ["single phi^2 Model\n", "V = 1/2 * m_in_MPl^2 * PHI^2 \n\n", f"m_in_MPl = {g(p.m_in_MPl)}\n"]
+        lines += [f"fStar = {g(p.f_star)}\n", f"omegaStar = {g(omega)}\n"]
+        lines += ["\n--------------------------\n", "General Program Information\n", "-----------------------------\n",
+                  f"Grid size={p.N}^3\n", f"Number of fields={p.nflds}\n", f"L={g(p.L)}\n", f"kIR={g(p.kIR)}\n",
+                  f"dt={g(dt)}, dt/dx={g(dt / (p.L / p.N))}\n",
+                  {0: "No expansion\n", 1: "Fixed background expansion\n",
+                   2: "Expansion calculated self-consistently\n"}.get(p.expansion, "")]
+        self._t_start = time.time()
+        lines.append("\nRun began at " + time.ctime(self._t_start) + "\n")
+        with open(os.path.join(self.dir, "info" + self.ext), "w") as fh:
+            fh.write("".join(lines))
+
+    def info_end(self, t0: float, t: float):
+        """output_parameters() at the end of a run: end time and elapsed wall time."""
+        import time
+
+        now = time.time()
+        took = int(now - getattr(self, "_t_start", now))
+        with open(os.path.join(self.dir, "info" + self.ext), "a") as fh:
+            fh.write("Run ended at " + time.ctime(now) + "\n")
+            fh.write(f"\nRun from t={self._g(t0)} to t={self._g(t)} took " + self.readable_time(took) + "\n")
+
     def save(self, lat, numsteps: int = 0, ssnapshot: bool = False):
         """save() (output.cpp:1796-1829): meansvars, scale, energy, histograms, the snapshot
         when ssnapshot, spectra."""

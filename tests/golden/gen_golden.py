@@ -211,7 +211,10 @@ def generate_main(run: str) -> str:
             out[name] = read_rows(os.path.join(o, name + ".txt"))
         out["spectra_scalar_0"] = read_blocks(os.path.join(o, "spectra_scalar_0.txt"))
         out["histogram0"] = read_blocks(os.path.join(o, "histogram0.txt"))[..., 0]
-        out["meta"] = np.array(json.dumps({"run": run, "config": cfg, "mode": "reference main()"}))
+        # info.txt up to its clock lines (output_parameters, output.cpp:1750-1786)
+        with open(os.path.join(o, "info.txt")) as fh:
+            info = fh.read().split("\nRun began at")[0]
+        out["meta"] = np.array(json.dumps({"run": run, "config": cfg, "mode": "reference main()", "info": info}))
     path = os.path.join(HERE, f"{run}.npz")
     np.savez_compressed(path, **out)
     return path

@@ -80,4 +80,9 @@ def test_run_loop_matches_reference_main(tmp_path):
     npts = 16 ** 3
     moved = np.abs(np.rint(hb * npts) - np.rint(g["histogram0"] * npts)).sum(axis=1)
     assert np.all(moved <= 4)
+    # info.txt (output_parameters) up to its clock lines, character for character
+    with open(o("info")) as fh:
+        info = fh.read()
+    assert info.split("\nRun began at")[0] == meta["info"]
+    assert "Run ended at" in info and " took " in info
 

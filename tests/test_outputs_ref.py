@@ -154,3 +154,21 @@ def test_calculate_dt():
     k = 25 * 16 * 3 ** 0.5 / 2
     assert calculate_dt(k, 1.0) == 2.0 / (k / 1.0) / 10
     assert calculate_dt(k, 2.0) == 2 * calculate_dt(k, 1.0)
+
+
+def test_info_file_matches_reference(tmp_path):
+    """info.txt (output_parameters, output.cpp:1750-1794) up to its clock lines, against the
+    reference's own file from its main() run (golden drive1_n16)."""
+    import json
+
+    from pspectcosmo_gb300 import Params
+    from pspectcosmo_gb300.outputs import TextWriter
+
+    g, meta = load("drive1_n16")
+    w = TextWriter(Params.reference_default(N=16), str(tmp_path))
+    w.info_begin(0.0)
+    w.info_end(0.0, 0.02)
+    text = (tmp_path / "info.txt").read_text()
+    assert text.split("\nRun began at")[0] == meta["info"]
+    assert text.rstrip().endswith("took less than 1 second")
+    assert TextWriter.readable_time(90061) == "1 days, 1 hours, 1 minutes, 1 seconds\n"
