@@ -207,6 +207,28 @@ int psc_time_passes(psc_handle *h, int reps, float *ms);
 int psc_set_state_padded(psc_handle *h, int Nsrc, const double *f_k, const double *pi_k, double a, double ad,
                          double add, const double *u_k, const double *pi_u_k);
 
+/* ANALYTIC_EVOLUTION, the analytic pre-lattice phase (single-lattice handles):
+ *   psc_analytic_begin      k_square_initialize + initialize_analytic_perturbation
+ *                           (initialize.cpp:815-958, 1124-1138): the background and, for every
+ *                           distinct k^2 of the lattice, the left and right Bunch-Davies mode
+ *                           functions of every field, at t = 0;
+ *   psc_analytic_step       evolve_VV_analytic_perturbation(dt) (evolution.cpp:167-336): the
+ *                           background on the host, every mode on the device;
+ *   psc_analytic_background t, a, a', a'' and the homogeneous fields / momenta ([nflds]);
+ *   psc_analytic_modes      the number of distinct k^2, their values (sorted) and the modes
+ *                           [4][nflds][nk] complex (f_left, pi_left, f_right, pi_right; index 0
+ *                           holds the background as the reference stores it: (f, 0) and
+ *                           (pi, pi at the last half step)), any pointer may be NULL;
+ *   psc_analytic_to_lattice initialize_lattice() (initialize.cpp:961-1097): the lattice state
+ *                           from the modes with the reference's random phases and amplitudes,
+ *                           a, a', a'' and t of the phase (no GW modes). */
+int psc_analytic_begin(psc_handle *h);
+int psc_analytic_step(psc_handle *h, double dt);
+int psc_analytic_background(psc_handle *h, double *t, double *a, double *ad, double *add, double *f_bg,
+                            double *pi_bg);
+int psc_analytic_modes(psc_handle *h, int *nk, int32_t *k2, double *modes);
+int psc_analytic_to_lattice(psc_handle *h);
+
 /* Device time of one c2r of the nflds field arrays f_k to real space (X, Y inverse
  * passes and the Z c2r pass, the transform of the reference's isChanged block,
  * output.cpp:1555-1578), averaged over `reps` launches on the handle's stream, ms.

@@ -56,6 +56,14 @@ CONFIGS: dict[str, tuple[str, dict[str, str]]] = {
     }),
     # the reference's own main() (adaptive dt, output cadence) on the shipped model, to t = 0.02
     "drive1_n16": ("phi2", {"N": "16", "tf": "0.02", "tOutputInfreq": "0.005"}),
+    # the analytic pre-lattice phase (ANALYTIC_EVOLUTION): linear modes on the distinct |k|^2,
+    # then initialize_lattice(); shipped model and the two-field preheating model
+    "anal1_n16": ("phi2", {"N": "16", "ANALYTIC_EVOLUTION": "true", "t_analytic": "0.01"}),
+    "anal2_n16_vv4": ("phi2chi2", {
+        "N": "16", "VV": "4", "nflds": "2", "kIR": "1", "ANALYTIC_EVOLUTION": "true", "t_analytic": "0.1",
+        "initfield[]": "{0.193 * MPl, 0.}",
+        "initderivs[]": "{-0.142e-6 * MPl * MPl, 0.}",
+    }),
     # the dealiased spectral step evolve_VV_k_pad (PAD_FLAG, V' on an N_pad = 2N grid)
     "pad1_n16": ("phi2", {"N": "16", "PAD_FLAG": "true", "N_pad": "32"}),
     "pad2_n16_vv4": ("phi2chi2", {

@@ -19,6 +19,8 @@
  *
  * usage: harness NSTEPS DT EVERY      (run inside the output directory)
  *        harness main                 (the reference's own main(): its adaptive-dt driver loop)
+ *        harness analytic NA DTA EVERYA NSTEPS DT EVERY   (ANALYTIC_EVOLUTION builds: NA analytic
+ *                                     steps of DTA, initialize_lattice(), NSTEPS lattice steps)
  * writes: output/*.txt (reference writers, 17 digits), state_<step>.bin, bg.txt,
  *         ic_info.txt, and with ssnapshot output/Snapshots/data_<step>_snapshot.h5.*.bin
  *         (the raw datasets, through the HDF5 shim)
@@ -26,6 +28,9 @@
 #include "pspectcosmo.h"
 
 #include <pthread.h>
+#include <algorithm>
+#include <complex>
+#include <vector>
 #include <cstdio>
 #include <cstdlib>
 #include <string>
@@ -58,6 +63,25 @@ static void dump_state(long step) {
 #endif
     std::fclose(fp);
 }
+
+#if ANALYTIC_EVOLUTION
+// the analytic perturbation state (initialize.cpp:814-958, evolution.cpp:174-336)
+static void dump_analytic(long step) {
+    char name[64];
+    std::snprintf(name, sizeof name, "analytic_%06ld.bin", step);
+    std::FILE *fp = std::fopen(name, "wb");
+    if (!fp) { std::perror(name); std::exit(3); }
+    int hdr[4] = {0x41435350 /* 'PSCA' */, (int)num_k_values, nflds, 0};
+    std::fwrite(hdr, sizeof(int), 4, fp);
+    double bg[4] = {t, a_k, ad_k, add_k};
+    std::fwrite(bg, sizeof(double), 4, fp);
+    std::vector<int> k2(k_square_vec.begin(), k_square_vec.end());
+    std::fwrite(k2.data(), sizeof(int), k2.size(), fp);
+    for (const auto *v : {&fk_left, &pi_k_left, &fk_right, &pi_k_right})
+        for (int fld = 0; fld < nflds; fld++) std::fwrite((*v)[fld].data(), sizeof(std::complex<double>), num_k_values, fp);
+    std::fclose(fp);
+}
+#endif
 
 static void step_once(double dt_) {
 #if SPECTRAL_FLAG && PAD_FLAG
@@ -144,7 +168,70 @@ static void *run_reference_main(void *) {
     return nullptr;
 }
 
+#if ANALYTIC_EVOLUTION
+static long g_na = 0, g_everya = 1;
+static double g_dta = 0.0;
+
+// the reference's analytic phase with a fixed step (pspectcosmo.cpp:370-447 with its
+// adaptive dt replaced), initialize_lattice(), then fixed-dt lattice steps
+static void *run_analytic(void *) {
+    checkdirectory();
+    fftw_init_threads();
+    fftw_plan_with_nthreads(n_threads);
+    const size_t modes = (size_t)N * N * (N / 2 + 1);
+    Cache_Data_k = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes);
+    R_k = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes);
+    for (int fld = 0; fld < nflds; fld++) {
+        f_k[fld] = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes);
+        pi_k[fld] = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes);
+#if SPECTRAL_FLAG
+        pi_k_half[fld] = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes);
+        V_prime_k[fld] = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes);
+        kernel_f_k[fld] = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes);
+#endif
+    }
+    t0 = 0.;
+    t = t0;
+    a = a0;
+    k_square_initialize();
+    initialize_analytic_perturbation();
+    dump_analytic(0);
+    for (long s = 1; s <= g_na; s++) {
+        evolve_VV_analytic_perturbation(g_dta);
+        if (s % g_everya == 0) {
+            save_Freq_analytic();
+            save_Infreq_analytic();
+            dump_analytic(s);
+        }
+    }
+    initialize_lattice();
+    dump_state(0);
+    for (long s = 1; s <= g_nsteps; s++) {
+        step_once(g_dt);
+        if (s % g_every == 0) dump_state(s);
+    }
+    return nullptr;
+}
+#endif
+
 int main(int argc, char **argv) {
+#if ANALYTIC_EVOLUTION
+    if (argc == 8 && std::string(argv[1]) == "analytic") {
+        g_na = std::atol(argv[2]);
+        g_dta = std::atof(argv[3]);
+        g_everya = std::max(1L, std::atol(argv[4]));
+        g_nsteps = std::atol(argv[5]);
+        g_dt = std::atof(argv[6]);
+        g_every = std::max(1L, std::atol(argv[7]));
+        pthread_attr_t attr;
+        pthread_attr_init(&attr);
+        pthread_attr_setstacksize(&attr, (size_t)2 << 30);
+        pthread_t th;
+        if (pthread_create(&th, &attr, run_analytic, nullptr) != 0) return 3;
+        pthread_join(th, nullptr);
+        return 0;
+    }
+#endif
     if (argc == 2 && std::string(argv[1]) == "main") {
         // the reference's own driver: adaptive dt, output cadence (pspectcosmo.cpp:600-697)
         pthread_attr_t attr;

@@ -18,7 +18,8 @@ ROOT = os.path.dirname(HERE)
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpsc.so")
 SOURCES = ["psc_kernels.cu", "psc_reg_f32.cu", "psc_reg_f64.cu", "psc_api.cu", "psc_noalloc.cu", "psc_adjoint.cu",
-           "psc_ic_gpu.cu", "psc_outputs.cu", "psc_pad.cu", "psc_ic.cpp", "psc_h5.cpp"]
+           "psc_ic_gpu.cu", "psc_outputs.cu", "psc_pad.cu", "psc_analytic.cu",
+           "psc_ic.cpp", "psc_h5.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

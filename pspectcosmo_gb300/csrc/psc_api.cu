@@ -84,6 +84,8 @@ namespace hapi {
 void free_all(psc_handle *h) {
     if (h->adj && h->adj_free) h->adj_free(h->adj);
     h->adj = nullptr;
+    if (h->ana && h->ana_free) h->ana_free(h->ana);
+    h->ana = nullptr;
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
     for (void *q : h->allocs) cudaFree(q);
     h->allocs.clear();

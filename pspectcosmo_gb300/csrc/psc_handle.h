@@ -33,6 +33,8 @@ struct psc_handle {
     std::vector<void *> allocs;
     void *adj = nullptr;         // adjoint workspace (psc_adjoint.cu), owned by the handle
     void (*adj_free)(void *) = nullptr;
+    void *ana = nullptr;         // analytic pre-lattice phase (psc_analytic.cu), owned by the handle
+    void (*ana_free)(void *) = nullptr;
     // padded step (N_pad > 0): the launch configuration and buffers of the N_pad grid
     // (fk = padded spectra, TA, QV = transform intermediates, tw = N_pad twiddles)
     bool padded = false;

@@ -29,19 +29,47 @@ def calculate_dt(k: float, a: float) -> float:
 
 def run(p: Params, tf: float, tOutputFreq: float, tOutputInfreq: float, tSnapFreq: float = 0.05,
         ssnapshot: bool = False, dir_: str = "output", writer: TextWriter | None = None,
-        lattice: Lattice | None = None) -> Lattice:
+        lattice: Lattice | None = None, t_analytic: float | None = None) -> Lattice:
     """initialize(), save(), then the main loop to tf (pspectcosmo.cpp:600-697). Returns the
-    lattice at the final time; the reference's text files (and snapshots) are in dir_."""
+    lattice at the final time; the reference's text files (and snapshots) are in dir_.
+
+    With t_analytic (ANALYTIC_EVOLUTION, pspectcosmo.cpp:370-447) the run starts with the
+    analytic phase to t_analytic (the same adaptive dt on a_k and output cadence, its own
+    output functions), then initialize_lattice() and the lattice loop from there."""
     lat = lattice if lattice is not None else Lattice(p)
-    lat.initialize()
     w = writer if writer is not None else TextWriter(p, dir_)
-    t0 = lat.t
-    w.info_begin(0.0)   # initialize() ends with output_parameters() (initialize.cpp:803); dt is not set yet
-    numsteps = 0
-    w.save(lat, numsteps, ssnapshot)
-    t = lat.t
-    next_freq, next_infreq, next_snap = tOutputFreq, tOutputInfreq, t + tSnapFreq
     kmax = p.kIR * p.N * math.sqrt(3) / 2.0
+    next_freq, next_infreq = tOutputFreq, tOutputInfreq
+    numsteps = 0
+    if t_analytic is not None:
+        lat.analytic_begin()
+        t0 = 0.0
+        w.info_begin(0.0)
+        w.save_analytic(lat)   # initialize_analytic_perturbation ends with save_analytic()
+        t = 0.0
+        while t < t_analytic:
+            dt = calculate_dt(kmax, lat.analytic_background()["a"])
+            dt = min(dt, tOutputFreq)
+            if t + dt > next_freq or t + dt > next_infreq:
+                dt = min(next_freq - t, next_infreq - t)
+            lat.analytic_step(dt)
+            t = lat.analytic_background()["t"]
+            if abs(t - next_freq) < 1e-10:
+                next_freq += tOutputFreq
+                w.save_freq_analytic(lat)
+            if abs(t - next_infreq) < 1e-10:
+                next_infreq += tOutputInfreq
+                w.save_infreq_analytic(lat)
+        lat.analytic_to_lattice()
+        t = lat.t
+        next_snap = t_analytic + tSnapFreq
+    else:
+        lat.initialize()
+        t0 = lat.t
+        w.info_begin(0.0)   # initialize() ends with output_parameters() (initialize.cpp:803); dt is not set yet
+        w.save(lat, numsteps, ssnapshot)
+        t = lat.t
+        next_snap = t + tSnapFreq
     while t < tf:
         dt = calculate_dt(kmax, lat.background()["a"])
         dt = min(dt, tOutputFreq)

@@ -112,6 +112,11 @@ def load_library(path: str | None = None):
     L.psc_h5_dataset_shape.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint64),
                                        ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
     L.psc_h5_read_f64.argtypes = [ctypes.c_char_p, ctypes.c_char_p, D, ctypes.c_uint64]
+    L.psc_analytic_begin.argtypes = [P]
+    L.psc_analytic_step.argtypes = [P, ctypes.c_double]
+    L.psc_analytic_background.argtypes = [P, D, D, D, D, D, D]
+    L.psc_analytic_modes.argtypes = [P, ctypes.POINTER(ctypes.c_int), I32, D]
+    L.psc_analytic_to_lattice.argtypes = [P]
     L.psc_strerror.argtypes = [ctypes.c_int]
     L.psc_strerror.restype = ctypes.c_char_p
     L.psc_last_error.argtypes = []
@@ -125,7 +130,8 @@ def load_library(path: str | None = None):
                  "psc_histograms", "psc_snapshot_arrays", "psc_write_snapshot", "psc_h5_write_f64",
                  "psc_batch_histograms", "psc_batch_write_snapshot", "psc_time_c2r",
                  "psc_set_state_padded", "psc_checkpoint_write", "psc_checkpoint_read",
-                 "psc_h5_dataset_shape", "psc_h5_read_f64"):
+                 "psc_h5_dataset_shape", "psc_h5_read_f64", "psc_analytic_begin", "psc_analytic_step",
+                 "psc_analytic_background", "psc_analytic_modes", "psc_analytic_to_lattice"):
         getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L
@@ -395,6 +401,36 @@ class Lattice:
         _check(self._L.psc_snapshot_arrays(self._h, _dp(out.get("f")), _dp(out.get("pot")), _dp(out.get("kin")),
                                            _dp(out.get("grad")), _dp(out.get("tot"))), "psc_snapshot_arrays")
         return out
+
+    # -- analytic pre-lattice phase (ANALYTIC_EVOLUTION) ---------------------------------
+    def analytic_begin(self):
+        """k_square_initialize + initialize_analytic_perturbation (initialize.cpp:815-958)."""
+        _check(self._L.psc_analytic_begin(self._h), "psc_analytic_begin")
+
+    def analytic_step(self, dt: float):
+        """evolve_VV_analytic_perturbation(dt) (evolution.cpp:167-336)."""
+        _check(self._L.psc_analytic_step(self._h, float(dt)), "psc_analytic_step")
+
+    def analytic_background(self) -> dict:
+        nf = self.p.nflds
+        t, a, ad, add = (ctypes.c_double() for _ in range(4))
+        f, pi = np.zeros(nf), np.zeros(nf)
+        _check(self._L.psc_analytic_background(self._h, ctypes.byref(t), ctypes.byref(a), ctypes.byref(ad),
+                                               ctypes.byref(add), _dp(f), _dp(pi)), "psc_analytic_background")
+        return dict(t=t.value, a=a.value, ad=ad.value, add=add.value, f=f, pi=pi)
+
+    def analytic_modes(self):
+        """(k2 [nk], modes [4][nflds][nk] complex: f_left, pi_left, f_right, pi_right)."""
+        nk = ctypes.c_int()
+        _check(self._L.psc_analytic_modes(self._h, ctypes.byref(nk), None, None), "psc_analytic_modes")
+        k2 = np.zeros(nk.value, np.int32)
+        modes = np.zeros((4, self.p.nflds, nk.value), np.complex128)
+        _check(self._L.psc_analytic_modes(self._h, ctypes.byref(nk), _ip(k2), _dp(modes)), "psc_analytic_modes")
+        return k2, modes
+
+    def analytic_to_lattice(self):
+        """initialize_lattice() (initialize.cpp:961-1097)."""
+        _check(self._L.psc_analytic_to_lattice(self._h), "psc_analytic_to_lattice")
 
     def checkpoint(self, path: str) -> None:
         """Full state, background and time to an HDF5 checkpoint file."""

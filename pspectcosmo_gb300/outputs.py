@@ -154,6 +154,68 @@ class TextWriter:
             fh.write("Run ended at " + time.ctime(now) + "\n")
             fh.write(f"\nRun from t={self._g(t0)} to t={self._g(t)} took " + self.readable_time(took) + "\n")
 
+    # analytic pre-lattice phase (output.cpp:117-375): the same files from the background
+    # and the mode functions
+    def save_freq_analytic(self, lat):
+        """save_Freq_analytic(): meansvars_analytic, scale_analytic, energy_analytic."""
+        p = self.p
+        bg = lat.analytic_background()
+        t, a = bg["t"], bg["a"]
+        aop = a ** (p.alpha - 3)
+        for f in range(p.nflds):
+            vals = [bg["f"][f], bg["pi"][f] * aop, bg["f"][f] ** 2, (bg["pi"][f] * aop) ** 2]
+            with self._open(f"average_scalar_{f}") as fh:
+                fh.write(f"{t:.3f}" + "".join(self._e(v) for v in vals) + f"{0:15d}{0:15d}\n")
+        if p.expansion == 2:
+            r = scale_row(p, bg)
+            with self._open("average_scale_factor") as fh:
+                fh.write(f"{r[0]:.6f} {r[1]:.6f} {r[2]:.6f} {r[3]:.6f} {r[4]:.6f} {r[5]:15.6e} {r[6]:.6f}\n")
+        total, cols = 0.0, []
+        for f in range(p.nflds):
+            k = bg["pi"][f] ** 2 / a ** 6 / 2.0
+            total += k
+            cols += [k, 0.0]
+        fv = list(bg["f"]) + [0.0] * (2 - p.nflds)
+        for term in range(p.num_potential_terms):
+            v = 0.5 * fv[0] ** 2 if term == 0 else 0.5 * p.gsq * fv[0] ** 2 * fv[1] ** 2
+            total += v
+            cols.append(v)
+        with self._open("average_energies") as fh:
+            fh.write(f"{t:.3f}" + "".join(f" {v:.6e}" for v in cols) + f" {total:.6e}\n")
+        if p.expansion != 1:
+            lhs = bg["ad"] ** 2
+            rhs = (p.f_star / p.MPl) ** 2 * a ** (2 * (p.alpha + 1)) * total / 3.0
+            with self._open("average_energy_conservation") as fh:
+                fh.write(f"{t:.3f} {abs(lhs - rhs) / abs(lhs + rhs):.8e} {lhs:.6f} {rhs:.6f}\n")
+
+    def save_infreq_analytic(self, lat):
+        """save_Infreq_analytic() -> spectra_analytic_discrete() (output.cpp:164-258): per
+        l = 1 .. maxnumbins-1 the mode of k^2 = l^2: k, k^3/(2 pi^2) |f_k|^2,
+        a^(2(alpha-3)) k^3/(2 pi^2) |pi_k|^2 (left-moving solution), 0, 0."""
+        import math
+
+        p = self.p
+        bg = lat.analytic_background()
+        k2, modes = lat.analytic_modes()
+        aop = bg["a"] ** (p.alpha - 3)
+        pos = {int(v): i for i, v in enumerate(k2)}
+        for f in range(p.nflds):
+            with self._open(f"spectra_scalar_{f}") as fh:
+                for l in range(1, p.maxnumbins):
+                    q = pos[l * l]
+                    km = math.sqrt(k2[q]) * p.kIR
+                    s1 = km ** 3 / (2 * math.pi ** 2) * abs(modes[0, f, q]) ** 2
+                    s2 = aop ** 2 * km ** 3 / (2 * math.pi ** 2) * abs(modes[1, f, q]) ** 2
+                    fh.write(f"{km:.1f} {s1:15.6e} {s2:15.6e} 0 0\n")
+                fh.write("\n")
+        with self._open("average_spectra_times") as fh:
+            fh.write(f"{bg['t']:.2f}\n")
+
+    def save_analytic(self, lat):
+        """save_analytic() (output.cpp:1855-1873): the frequent and infrequent outputs."""
+        self.save_freq_analytic(lat)
+        self.save_infreq_analytic(lat)
+
     def save(self, lat, numsteps: int = 0, ssnapshot: bool = False):
         """save() (output.cpp:1796-1829): meansvars, scale, energy, histograms, the snapshot
         when ssnapshot, spectra."""

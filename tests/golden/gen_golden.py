@@ -189,6 +189,63 @@ def generate(run: str) -> str:
     return path
 
 
+# the analytic pre-lattice phase (ANALYTIC_EVOLUTION builds): NA analytic steps of DTA with a
+# dump every EVERYA, initialize_lattice(), NSTEPS lattice steps of DT with a dump every EVERY
+ANALYTIC_RUNS = {
+    "anal1_n16": ("anal1_n16", 10, 0.001, 5, 4, 0.002, 2),
+    "anal2_n16_vv4": ("anal2_n16_vv4", 10, 0.002, 5, 4, 0.005, 2),
+}
+
+
+def read_analytic(path: str) -> dict:
+    with open(path, "rb") as fh:
+        raw = fh.read()
+    hdr = np.frombuffer(raw, dtype=np.int32, count=4)
+    assert hdr[0] == 0x41435350, "bad analytic dump magic"
+    na, nf = int(hdr[1]), int(hdr[2])
+    bg = np.frombuffer(raw, dtype=np.float64, count=4, offset=16)
+    k2 = np.frombuffer(raw, dtype=np.int32, count=na, offset=48)
+    off = 48 + 4 * na
+    modes = np.frombuffer(raw, dtype=np.complex128, count=4 * nf * na, offset=off).reshape(4, nf, na).copy()
+    assert off + modes.nbytes == len(raw), "trailing bytes in analytic dump"
+    return {"t": bg[0], "a": bg[1], "ad": bg[2], "add": bg[3], "k2": k2.copy(), "modes": modes}
+
+
+def generate_analytic(run: str) -> str:
+    cfg, na, dta, everya, nsteps, dt, every = ANALYTIC_RUNS[run]
+    exe = os.path.join(ROOT, "oracle", "_ref", cfg, "harness")
+    if not os.path.exists(exe):
+        import build_ref  # noqa: E402
+
+        exe = build_ref.build(cfg)
+    with tempfile.TemporaryDirectory() as tmp:
+        args = [exe, "analytic", str(na), repr(dta), str(everya), str(nsteps), repr(dt), str(every)]
+        res = subprocess.run(args, cwd=tmp, stdin=subprocess.DEVNULL, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise SystemExit(f"{run}: harness failed\n{res.stderr}")
+        out = {}
+        for s in range(0, na + 1, everya):
+            d = read_analytic(os.path.join(tmp, f"analytic_{s:06d}.bin"))
+            out[f"ana_{s}_bg"] = np.array([d["t"], d["a"], d["ad"], d["add"]])
+            out[f"ana_{s}_modes"] = d["modes"]
+            out["k2"] = d["k2"]
+        ic = read_state(os.path.join(tmp, "state_000000.bin"))
+        fin = read_state(os.path.join(tmp, f"state_{nsteps:06d}.bin"))
+        out["lat_ic_bg"] = np.array([ic["t"], ic["a"], ic["ad"], ic["add"]])
+        out["lat_ic_f_k"] = ic["f_k"]
+        out["lat_ic_pi_k"] = ic["pi_k"]
+        out["lat_fin_bg"] = np.array([fin["t"], fin["a"], fin["ad"], fin["add"]])
+        out["lat_fin_f_k"] = fin["f_k"]
+        out["lat_fin_pi_k"] = fin["pi_k"]
+        meta = {"run": run, "config": cfg, "N": ic["N"], "nflds": ic["nflds"], "spectral": ic["spectral"],
+                "gw": ic["gw"], "na_steps": na, "dta": dta, "everya": everya, "nsteps": nsteps, "dt": dt,
+                "every": every}
+        out["meta"] = np.array(json.dumps(meta))
+    path = os.path.join(HERE, f"{run}.npz")
+    np.savez_compressed(path, **out)
+    return path
+
+
 # runs of the reference's own main() (its adaptive-dt driver loop and output cadence)
 MAIN_RUNS = {"drive1_n16": "drive1_n16"}
 
@@ -221,8 +278,13 @@ def generate_main(run: str) -> str:
 
 
 def main(argv):
-    for run in (argv or list(RUNS) + list(MAIN_RUNS)):
-        p = generate_main(run) if run in MAIN_RUNS else generate(run)
+    for run in (argv or list(RUNS) + list(MAIN_RUNS) + list(ANALYTIC_RUNS)):
+        if run in MAIN_RUNS:
+            p = generate_main(run)
+        elif run in ANALYTIC_RUNS:
+            p = generate_analytic(run)
+        else:
+            p = generate(run)
         print(f"{p}  {os.path.getsize(p) / 1024:.0f} KiB")
 
 

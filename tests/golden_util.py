@@ -23,7 +23,7 @@ def load(run: str):
 
 def params_for(meta: dict, precision: int = 64) -> Params:
     c = meta["config"]
-    if c.startswith(("spec1", "gw1", "pad1")):
+    if c.startswith(("spec1", "gw1", "pad1", "anal1")):
         p = Params.reference_default(N=meta["N"])
     else:
         p = Params.preheating(N=meta["N"])
