@@ -150,6 +150,20 @@ int psc_means(psc_handle *h, double *out);
  * (int)((f - bmin) / df) in FP64, the maximum in the last bin, as the reference. */
 int psc_histograms(psc_handle *h, int nbins, double hmin, double hmax, double *binfreq, double *bmin, double *df);
 
+/* histograms_2d() (output.cpp:1300-1413) of the field pair (fld1, fld2): binfreq
+ * [nbins0][nbins1] = counts / N^3 (the reference's normalisation), bmin[2], df[2]; limits
+ * as psc_histograms (hmin == hmax: the fields' own minima and maxima). */
+int psc_histograms_2d(psc_handle *h, int fld1, int fld2, int nbins0, int nbins1, double hmin, double hmax,
+                      double *binfreq, double *bmin, double *df);
+
+/* slices() (output.cpp:1415-1539): per field the values of a slicedim-dimensional slice
+ * through the origin (a z line at x = y = 0, the x = 0 plane, or the lattice), every
+ * sliceskip-th site up to slicelength * sliceskip (at most N), each the mean of its
+ * sliceskip block when sliceaverage. out = [nflds][*count] in the reference's output
+ * order (NULL: only *count). */
+int psc_slices(psc_handle *h, int slicedim, int slicelength, int sliceskip, int sliceaverage, double *out,
+               long long *count);
+
 /* The datasets of snapshots() (output.cpp:1541-1648), N^3 doubles each, [x][y][z];
  * any pointer may be NULL: f = the real-space fields [nflds][N^3]; pot, kin, grad,
  * tot = the lattice energy densities of SNAPSHOTS_ENERGY at the current scale factor

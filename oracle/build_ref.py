@@ -56,6 +56,14 @@ CONFIGS: dict[str, tuple[str, dict[str, str]]] = {
     }),
     # the reference's own main() (adaptive dt, output cadence) on the shipped model, to t = 0.02
     "drive1_n16": ("phi2", {"N": "16", "tf": "0.02", "tOutputInfreq": "0.005"}),
+    # the optional outputs of save(): 2-D histograms (field pair 0, 1) and 2-D slices with
+    # averaging over 2 x 2 blocks (output.cpp:1300-1539)
+    "out2_n16_vv4": ("phi2chi2", {
+        "N": "16", "VV": "4", "nflds": "2", "kIR": "1", "shistograms2d": "true", "sslices": "true",
+        "slicedim": "2", "slicelength": "N, sliceskip = 2",
+        "initfield[]": "{0.193 * MPl, 0.}",
+        "initderivs[]": "{-0.142e-6 * MPl * MPl, 0.}",
+    }),
     # the analytic pre-lattice phase (ANALYTIC_EVOLUTION): linear modes on the distinct |k|^2,
     # then initialize_lattice(); shipped model and the two-field preheating model
     "anal1_n16": ("phi2", {"N": "16", "ANALYTIC_EVOLUTION": "true", "t_analytic": "0.01"}),

@@ -5,6 +5,8 @@ Test infrastructure only (the oracle): the product computes these on the device
 (tests/golden/snap2_n16_vv4.npz: its histogram files and the raw snapshot datasets).
 
   histograms()              output.cpp:1193-1297
+  histograms_2d()           output.cpp:1300-1413
+  slices()                  output.cpp:1415-1539
   kinetic_energy_lattice    evolution.cpp:7-19
   gradient_energy_lattice   evolution.cpp:23-138
   snapshot energies         output.cpp:1614-1627
@@ -85,3 +87,75 @@ def lattice_energies(f_all: np.ndarray, pi_all: np.ndarray, a: float, kIR: float
             grad = grad + d * d
     grad = grad * (a * a / 2.0)
     return dict(pot=pot, kin=kin, grad=grad, tot=pot + kin + grad)
+
+
+def histogram_2d(f1: np.ndarray, f2: np.ndarray, nbins0: int = 10, nbins1: int = 10, hmin: float = 0.0,
+                 hmax: float = 0.0):
+    """One field pair (output.cpp:1369-1410): binfreq [nbins0][nbins1] (counts / N^3, not /
+    the points binned), bmin [2], df [2]."""
+    x, y = np.asarray(f1, np.float64).ravel(), np.asarray(f2, np.float64).ravel()
+    if hmax == hmin:
+        bmin = [float(x.min()), float(y.min())]
+        bmax = [float(x.max()), float(y.max())]
+    else:
+        bmin, bmax = [float(hmin)] * 2, [float(hmax)] * 2
+    df = [(bmax[0] - bmin[0]) / float(nbins0), (bmax[1] - bmin[1]) / float(nbins1)]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        b0 = _c_int_cast((x - bmin[0]) / df[0])
+        b1 = _c_int_cast((y - bmin[1]) / df[1])
+    b0[x == bmax[0]] = nbins0 - 1
+    b1[y == bmax[1]] = nbins1 - 1
+    keep = (b0 >= 0) & (b0 < nbins0) & (b1 >= 0) & (b1 < nbins1)
+    counts = np.bincount(b0[keep] * nbins1 + b1[keep], minlength=nbins0 * nbins1).astype(np.float64)
+    return (counts / float(x.size)).reshape(nbins0, nbins1), np.array(bmin), np.array(df)
+
+
+def slices(f: np.ndarray, slicedim: int = 1, slicelength: int | None = None, sliceskip: int = 1,
+           sliceaverage: int = 1) -> np.ndarray:
+    """One field's slice values in output order (output.cpp:1456-1534): the first slicedim
+    axes from the origin (x = y = 0 for a line, x = 0 for a plane), every sliceskip-th point
+    up to slicelength * sliceskip (at most N), each optionally the mean of its skip block
+    (the 3-D case multiplies by 1/numpts, the others divide)."""
+    N = f.shape[0]
+    slicelength = N if slicelength is None else slicelength
+    dim = min(slicedim, 3)
+    final = min(slicelength * sliceskip, N)
+    out = []
+    starts = range(0, final, sliceskip)
+    if dim == 1:
+        for k in starts:
+            if sliceaverage == 1:
+                v, n = 0.0, 0
+                for z in range(k, min(k + sliceskip, N)):
+                    v += f[0, 0, z]
+                    n += 1
+                out.append(v / float(n))
+            else:
+                out.append(f[0, 0, k])
+    elif dim == 2:
+        for j in starts:
+            for k in starts:
+                if sliceaverage == 1:
+                    v, n = 0.0, 0
+                    for y in range(j, min(j + sliceskip, N)):
+                        for z in range(k, min(k + sliceskip, N)):
+                            v += f[0, y, z]
+                            n += 1
+                    out.append(v / float(n))
+                else:
+                    out.append(f[0, j, k])
+    else:
+        for i in starts:
+            for j in starts:
+                for k in starts:
+                    if sliceaverage == 1:
+                        v, n = 0.0, 0
+                        for x in range(i, min(i + sliceskip, N)):
+                            for y in range(j, min(j + sliceskip, N)):
+                                for z in range(k, min(k + sliceskip, N)):
+                                    v += f[x, y, z]
+                                    n += 1
+                        out.append(v * (1 / float(n)))
+                    else:
+                        out.append(f[i, j, k])
+    return np.array(out)

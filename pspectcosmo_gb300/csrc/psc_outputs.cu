@@ -11,6 +11,7 @@
 // and c2r along each axis compute (evolution.cpp:34-127).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <string>
 #include <vector>
@@ -185,6 +186,91 @@ __global__ void __launch_bounds__(kOutThreads) k_hist(const T *__restrict__ x, l
         if (sc[i]) atomicAdd(&counts[i], sc[i]);
 }
 
+// 2-D histogram of a field pair (output.cpp:1369-1410): both bin indices as the 1-D
+// histogram computes them; lim = {bmin0, bmax0, bmin1, bmax1}
+template <typename T>
+__global__ void __launch_bounds__(kOutThreads) k_hist2d(const T *__restrict__ x, const T *__restrict__ y, long long n,
+                                                        const double *__restrict__ lim, int nb0, int nb1,
+                                                        unsigned *__restrict__ counts) {
+    extern __shared__ unsigned sc2[];
+    const int nb = nb0 * nb1;
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) sc2[i] = 0u;
+    __syncthreads();
+    const double b0 = lim[0], e0 = lim[1], b1 = lim[2], e1 = lim[3];
+    const double d0 = (e0 - b0) / (double)nb0, d1 = (e1 - b1) / (double)nb1;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const double u = (double)x[i], v = (double)y[i];
+        int i0, i1;
+        if (u == e0) {
+            i0 = nb0 - 1;
+        } else {
+            const double q = (u - b0) / d0;
+            if (q != q) continue;
+            i0 = __double2int_rz(q);
+        }
+        if (v == e1) {
+            i1 = nb1 - 1;
+        } else {
+            const double q = (v - b1) / d1;
+            if (q != q) continue;
+            i1 = __double2int_rz(q);
+        }
+        if (i0 >= 0 && i0 < nb0 && i1 >= 0 && i1 < nb1) atomicAdd(&sc2[i0 * nb1 + i1], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nb; i += blockDim.x)
+        if (sc2[i]) atomicAdd(&counts[i], sc2[i]);
+}
+
+// the global minimum and maximum of the block partials of k_minmax into lim[0], lim[1]
+__global__ void k_minmax_final(const double *__restrict__ part, int nparts, double *__restrict__ lim) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double lo = part[0], hi = part[1];
+    for (int i = 1; i < nparts; ++i) {
+        lo = part[2 * i] < lo ? part[2 * i] : lo;
+        hi = part[2 * i + 1] > hi ? part[2 * i + 1] : hi;
+    }
+    lim[0] = lo;
+    lim[1] = hi;
+}
+
+// slices() (output.cpp:1456-1534): output value o of a dim-dimensional slice with side
+// `side` points (every skip-th site from the origin), each the mean of its skip block when
+// average != 0 (sequential sum in the reference's loop order; 3-D multiplies by 1/n)
+template <typename T>
+__global__ void __launch_bounds__(kOutThreads) k_slices(const T *__restrict__ f, int N, int dim, int side, int skip,
+                                                        int average, double *__restrict__ out) {
+    long long total = side;
+    for (int d = 1; d < dim; ++d) total *= side;
+    const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= total) return;
+    int c[3] = {0, 0, 0};   // x, y, z start of the block
+    long long r = o;
+    for (int d = 2; d >= 3 - dim; --d) {
+        c[d] = (int)(r % side) * skip;
+        r /= side;
+    }
+    const size_t NN = (size_t)N;
+    double v;
+    if (average) {
+        v = 0.0;
+        int n = 0;
+        const int xe = dim == 3 ? min(c[0] + skip, N) : 1, ye = dim >= 2 ? min(c[1] + skip, N) : 1;
+        const int ze = min(c[2] + skip, N);
+        for (int x = c[0]; x < xe; ++x)
+            for (int y = c[1]; y < ye; ++y)
+                for (int z = c[2]; z < ze; ++z) {
+                    v += (double)f[((size_t)x * NN + y) * NN + z];
+                    ++n;
+                }
+        v = dim == 3 ? v * (1 / (double)n) : v / (double)n;
+    } else {
+        v = (double)f[((size_t)c[0] * NN + c[1]) * NN + c[2]];
+    }
+    out[o] = v;
+}
+
 template <typename T>
 cudaError_t launch_deriv(const Geo &g, const void *fk, void *out, int axis, cudaStream_t st) {
     k_deriv_axis<T><<<kOutBlocks, kOutThreads, 0, st>>>((const cplx<T> *)fk, (cplx<T> *)out, g.N, g.H, g.modes, axis,
@@ -263,6 +349,90 @@ int histograms_t(psc_handle *h, int r, int nbins, double hmin, double hmax, doub
     cudaFreeAsync(scratch, h->st);
     CU(e);
     CU(cudaStreamSynchronize(h->st));
+    return PSC_OK;
+}
+
+template <typename T>
+int histograms2d_t(psc_handle *h, int r, int f1, int f2, int nb0, int nb1, double hmin, double hmax, double *binfreq,
+                   double *bmin, double *df) {
+    const Geo &g = h->cfg.g;
+    const Buffers b1 = buffers_of(h, r);
+    int rc = to_real(h, r, b1.fk, g.nf);
+    if (rc) return rc;
+    const size_t part_b = 2 * kOutBlocks * sizeof(double), lim_b = 4 * sizeof(double);
+    const size_t cnt_b = (size_t)nb0 * nb1 * sizeof(unsigned);
+    void *scratch = nullptr;
+    CU(cudaMallocAsync(&scratch, part_b + lim_b + cnt_b, h->st));
+    double *part = static_cast<double *>(scratch);
+    double *lim = part + 2 * kOutBlocks;
+    unsigned *cnt = reinterpret_cast<unsigned *>(static_cast<char *>(scratch) + part_b + lim_b);
+    const T *x = static_cast<const T *>(h->b.real) + (long long)f1 * g.sites;
+    const T *y = static_cast<const T *>(h->b.real) + (long long)f2 * g.sites;
+    cudaError_t e = cudaSuccess;
+    if (hmin == hmax) {
+        k_minmax<T><<<kOutBlocks, kOutThreads, 0, h->st>>>(x, g.sites, part);
+        k_minmax_final<<<1, 32, 0, h->st>>>(part, kOutBlocks, lim);
+        k_minmax<T><<<kOutBlocks, kOutThreads, 0, h->st>>>(y, g.sites, part);
+        k_minmax_final<<<1, 32, 0, h->st>>>(part, kOutBlocks, lim + 2);
+    } else {
+        const double l[4] = {hmin, hmax, hmin, hmax};
+        e = cudaMemcpyAsync(lim, l, sizeof l, cudaMemcpyHostToDevice, h->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    }
+    if (e == cudaSuccess) e = cudaMemsetAsync(cnt, 0, cnt_b, h->st);
+    if (e == cudaSuccess && cnt_b > 48 * 1024)
+        e = cudaFuncSetAttribute(k_hist2d<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cnt_b);
+    std::vector<unsigned> hc((size_t)nb0 * nb1);
+    double hl[4];
+    if (e == cudaSuccess) {
+        k_hist2d<T><<<kOutBlocks, kOutThreads, cnt_b, h->st>>>(x, y, g.sites, lim, nb0, nb1, cnt);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hc.data(), cnt, cnt_b, cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hl, lim, sizeof hl, cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    cudaFreeAsync(scratch, h->st);
+    CU(e);
+    // binfreq / N^3 (output.cpp:1407), df = (bmax - bmin) / nbins
+    const double n3 = (double)g.sites;
+    if (binfreq)
+        for (size_t i = 0; i < hc.size(); ++i) binfreq[i] = (double)hc[i] / n3;
+    if (bmin) {
+        bmin[0] = hl[0];
+        bmin[1] = hl[2];
+    }
+    if (df) {
+        df[0] = (hl[1] - hl[0]) / (double)nb0;
+        df[1] = (hl[3] - hl[2]) / (double)nb1;
+    }
+    return PSC_OK;
+}
+
+template <typename T>
+int slices_t(psc_handle *h, int r, int dim, int length, int skip, int average, double *out, long long count) {
+    const Geo &g = h->cfg.g;
+    const Buffers b1 = buffers_of(h, r);
+    int rc = to_real(h, r, b1.fk, g.nf);
+    if (rc) return rc;
+    const int N = g.N;
+    const int fin = std::min((long long)length * skip, (long long)N) > 0 ? (int)std::min((long long)length * skip,
+                                                                                         (long long)N)
+                                                                       : 0;
+    const int side = (fin + skip - 1) / skip;
+    double *dout = nullptr;
+    CU(cudaMallocAsync(reinterpret_cast<void **>(&dout), (size_t)count * g.nf * sizeof(double), h->st));
+    cudaError_t e = cudaSuccess;
+    for (int f = 0; f < g.nf && e == cudaSuccess; ++f) {
+        const T *x = static_cast<const T *>(h->b.real) + (long long)f * g.sites;
+        const unsigned blocks = (unsigned)((count + kOutThreads - 1) / kOutThreads);
+        k_slices<T><<<blocks, kOutThreads, 0, h->st>>>(x, N, dim, side, skip, average, dout + (size_t)f * count);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out, dout, (size_t)count * g.nf * sizeof(double), cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    cudaFreeAsync(dout, h->st);
+    CU(e);
     return PSC_OK;
 }
 
@@ -367,6 +537,37 @@ int histograms(psc_handle *h, int r, int nbins, double hmin, double hmax, double
     if (!h->have_state) return fail(PSC_ERR_STATE, "no state");
     return h->p0().precision == 32 ? histograms_t<float>(h, r, nbins, hmin, hmax, binfreq, bmin, df)
                                    : histograms_t<double>(h, r, nbins, hmin, hmax, binfreq, bmin, df);
+}
+
+int histograms2d(psc_handle *h, int r, int f1, int f2, int nb0, int nb1, double hmin, double hmax, double *binfreq,
+                 double *bmin, double *df) {
+    if (!h->have_state) return fail(PSC_ERR_STATE, "no state");
+    const int nf = h->cfg.g.nf;
+    if (f1 < 0 || f1 >= nf || f2 < 0 || f2 >= nf) return fail(PSC_ERR_ARG, "field index out of range");
+    if (nb0 < 1 || nb1 < 1 || (long long)nb0 * nb1 > 16384) return fail(PSC_ERR_ARG, "nbins0 * nbins1 must be in [1, 16384]");
+    return h->p0().precision == 32 ? histograms2d_t<float>(h, r, f1, f2, nb0, nb1, hmin, hmax, binfreq, bmin, df)
+                                   : histograms2d_t<double>(h, r, f1, f2, nb0, nb1, hmin, hmax, binfreq, bmin, df);
+}
+
+long long slice_count(int N, int dim, int length, int skip) {
+    if (dim < 1 || length < 1 || skip < 1) return -1;
+    if (dim > 3) dim = 3;
+    const long long fin = std::min((long long)length * skip, (long long)N);
+    const long long side = (fin + skip - 1) / skip;
+    long long c = side;
+    for (int d = 1; d < dim; ++d) c *= side;
+    return c;
+}
+
+int slices(psc_handle *h, int r, int dim, int length, int skip, int average, double *out, long long *count) {
+    if (!h->have_state) return fail(PSC_ERR_STATE, "no state");
+    const long long c = slice_count(h->cfg.g.N, dim, length, skip);
+    if (c < 0) return fail(PSC_ERR_ARG, "slicedim, slicelength and sliceskip must be positive");
+    if (count) *count = c;
+    if (!out) return PSC_OK;
+    if (dim > 3) dim = 3;
+    return h->p0().precision == 32 ? slices_t<float>(h, r, dim, length, skip, average, out, c)
+                                   : slices_t<double>(h, r, dim, length, skip, average, out, c);
 }
 
 int snapshot_arrays(psc_handle *h, int r, double *f, double *pot, double *kin, double *grad, double *tot) {
@@ -492,6 +693,18 @@ extern "C" {
 int psc_histograms(psc_handle *h, int nbins, double hmin, double hmax, double *binfreq, double *bmin, double *df) {
     if (!h) return fail(PSC_ERR_ARG, "null handle");
     return histograms(h, 0, nbins, hmin, hmax, binfreq, bmin, df);
+}
+
+int psc_histograms_2d(psc_handle *h, int fld1, int fld2, int nbins0, int nbins1, double hmin, double hmax,
+                      double *binfreq, double *bmin, double *df) {
+    if (!h) return fail(PSC_ERR_ARG, "null handle");
+    return histograms2d(h, 0, fld1, fld2, nbins0, nbins1, hmin, hmax, binfreq, bmin, df);
+}
+
+int psc_slices(psc_handle *h, int slicedim, int slicelength, int sliceskip, int sliceaverage, double *out,
+               long long *count) {
+    if (!h) return fail(PSC_ERR_ARG, "null handle");
+    return slices(h, 0, slicedim, slicelength, sliceskip, sliceaverage, out, count);
 }
 
 int psc_snapshot_arrays(psc_handle *h, double *f, double *pot, double *kin, double *grad, double *tot) {

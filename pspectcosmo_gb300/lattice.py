@@ -117,6 +117,10 @@ def load_library(path: str | None = None):
     L.psc_analytic_background.argtypes = [P, D, D, D, D, D, D]
     L.psc_analytic_modes.argtypes = [P, ctypes.POINTER(ctypes.c_int), I32, D]
     L.psc_analytic_to_lattice.argtypes = [P]
+    L.psc_histograms_2d.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                    ctypes.c_double, D, D, D]
+    L.psc_slices.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, D,
+                             ctypes.POINTER(ctypes.c_longlong)]
     L.psc_strerror.argtypes = [ctypes.c_int]
     L.psc_strerror.restype = ctypes.c_char_p
     L.psc_last_error.argtypes = []
@@ -131,7 +135,8 @@ def load_library(path: str | None = None):
                  "psc_batch_histograms", "psc_batch_write_snapshot", "psc_time_c2r",
                  "psc_set_state_padded", "psc_checkpoint_write", "psc_checkpoint_read",
                  "psc_h5_dataset_shape", "psc_h5_read_f64", "psc_analytic_begin", "psc_analytic_step",
-                 "psc_analytic_background", "psc_analytic_modes", "psc_analytic_to_lattice"):
+                 "psc_analytic_background", "psc_analytic_modes", "psc_analytic_to_lattice",
+                 "psc_histograms_2d", "psc_slices"):
         getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L
@@ -387,6 +392,26 @@ class Lattice:
         _check(self._L.psc_histograms(self._h, int(nbins), float(hmin), float(hmax), _dp(freq), _dp(bmin), _dp(df)),
                "psc_histograms")
         return dict(binfreq=freq, bmin=bmin, df=df)
+
+    def histograms_2d(self, fld1: int = 0, fld2: int = 1, nbins0: int = 10, nbins1: int = 10, hmin: float = 0.0,
+                      hmax: float = 0.0) -> dict:
+        """histograms_2d() (output.cpp:1300-1413): binfreq [nbins0][nbins1], bmin [2], df [2]."""
+        freq, bmin, df = np.zeros((nbins0, nbins1)), np.zeros(2), np.zeros(2)
+        _check(self._L.psc_histograms_2d(self._h, fld1, fld2, nbins0, nbins1, float(hmin), float(hmax), _dp(freq),
+                                         _dp(bmin), _dp(df)), "psc_histograms_2d")
+        return dict(binfreq=freq, bmin=bmin, df=df)
+
+    def slices(self, slicedim: int = 1, slicelength: int | None = None, sliceskip: int = 1,
+               sliceaverage: int = 1) -> np.ndarray:
+        """slices() (output.cpp:1415-1539): [nflds][count] values in output order."""
+        length = self.p.N if slicelength is None else slicelength
+        cnt = ctypes.c_longlong()
+        _check(self._L.psc_slices(self._h, slicedim, length, sliceskip, sliceaverage, None, ctypes.byref(cnt)),
+               "psc_slices")
+        out = np.zeros((self.p.nflds, cnt.value))
+        _check(self._L.psc_slices(self._h, slicedim, length, sliceskip, sliceaverage, _dp(out), ctypes.byref(cnt)),
+               "psc_slices")
+        return out
 
     def snapshot_arrays(self, fields: bool = True, energy: bool = True) -> dict:
         """The datasets of snapshots() (output.cpp:1541-1648) as [N][N][N] arrays."""

@@ -85,7 +85,10 @@ class TextWriter:
 
     def __init__(self, p: Params, dir_: str = "output", ext: str = ".txt", shistograms: bool = True,
                  nbins: int = 256, histogram_min: float = 0.0, histogram_max: float = 0.0,
-                 snapshots_energy: bool = True):
+                 snapshots_energy: bool = True, shistograms2d: bool = False, nbins2d: tuple = (10, 10),
+                 histogram2d_min: float = 0.0, histogram2d_max: float = 0.0, hist2dflds: tuple = (0, 1),
+                 sslices: bool = False, slicedim: int = 1, slicelength: int | None = None, sliceskip: int = 1,
+                 sliceaverage: int = 1):
         self.p, self.dir, self.ext = p, dir_, ext
         os.makedirs(os.path.join(dir_, "Snapshots"), exist_ok=True)
         self._first_spectra = True
@@ -93,6 +96,12 @@ class TextWriter:
         self.shistograms, self.nbins = shistograms, nbins
         self.histogram_min, self.histogram_max = histogram_min, histogram_max
         self.snapshots_energy = snapshots_energy
+        # parameters.h:95-105 (2-D histograms, slices)
+        self.shistograms2d, self.nbins2d = shistograms2d, tuple(nbins2d)
+        self.histogram2d_min, self.histogram2d_max = histogram2d_min, histogram2d_max
+        self.hist2dflds = tuple(hist2dflds)
+        self.sslices, self.slicedim, self.sliceskip, self.sliceaverage = sslices, slicedim, sliceskip, sliceaverage
+        self.slicelength = p.N if slicelength is None else slicelength
 
     def _open(self, name):
         return open(os.path.join(self.dir, name + self.ext), "a")
@@ -217,12 +226,18 @@ class TextWriter:
         self.save_infreq_analytic(lat)
 
     def save(self, lat, numsteps: int = 0, ssnapshot: bool = False):
-        """save() (output.cpp:1796-1829): meansvars, scale, energy, histograms, the snapshot
-        when ssnapshot, spectra."""
+        """save() (output.cpp:1796-1829): meansvars, scale, energy, histograms, the 2-D
+        histograms and slices when on, the snapshot when ssnapshot, spectra."""
         self.save_freq(lat)
+        if self.shistograms:
+            self.histograms(lat)
+        if self.shistograms2d:
+            self.histograms_2d(lat)
+        if self.sslices:
+            self.slices(lat)
         if ssnapshot:
             self.snapshot(lat, numsteps)
-        self.save_infreq(lat)
+        self.spectra(lat)
 
     def save_freq(self, lat):
         """save_Freq(): meansvars, scale, energy (output.cpp:1831-1840)."""
@@ -259,6 +274,31 @@ class TextWriter:
             t = lat.background()["t"]
             fh.write(f"{t:.6f}" + "".join(f" {h['bmin'][f]:.6e} {h['df'][f]:.6e}" for f in range(p.nflds)) + "\n")
 
+    def histograms_2d(self, lat):
+        """histograms_2d() (output.cpp:1300-1413): histogram2d<f1>_<f2>.txt per field pair,
+        the nbins0 x nbins1 frequencies one per line and a blank line per call;
+        histogram2dtimes.txt: t, then bmin and df of both fields of each pair."""
+        t = lat.background()["t"]
+        times = f"{t:.6f}"
+        for q in range(len(self.hist2dflds) // 2):
+            f1, f2 = self.hist2dflds[2 * q], self.hist2dflds[2 * q + 1]
+            h = lat.histograms_2d(f1, f2, self.nbins2d[0], self.nbins2d[1], self.histogram2d_min, self.histogram2d_max)
+            with self._open(f"histogram2d{f1}_{f2}") as fh:
+                fh.write("".join(f"{v:.6e}\n" for v in h["binfreq"].ravel()) + "\n")
+            times += f" {h['bmin'][0]:.6e} {h['df'][0]:.6e} {h['bmin'][1]:.6e} {h['df'][1]:.6e}"
+        with self._open("histogram2dtimes") as fh:
+            fh.write(times + "\n")
+
+    def slices(self, lat):
+        """slices() (output.cpp:1415-1539): slices<f>.txt, one value per line and a blank line
+        per call; slicetimes.txt: t."""
+        v = lat.slices(self.slicedim, self.slicelength, self.sliceskip, self.sliceaverage)
+        for f in range(self.p.nflds):
+            with self._open(f"slices{f}") as fh:
+                fh.write("".join(f"{x:.6e}\n" for x in v[f]) + "\n")
+        with self._open("slicetimes") as fh:
+            fh.write(f"{lat.background()['t']:.6f}\n")
+
     def snapshot(self, lat, step: int) -> str:
         """save_Snap(step) -> snapshots() (output.cpp:1541-1648): <dir>/Snapshots/
         data_<step>_snapshot.h5 with the fields and, with SNAPSHOTS_ENERGY, the lattice
@@ -272,6 +312,11 @@ class TextWriter:
         spectra() (output.cpp:490-1062)."""
         if self.shistograms:
             self.histograms(lat)
+        self.spectra(lat)
+
+    def spectra(self, lat):
+        """spectra() (output.cpp:490-1062): spectra_scalar_<f>.txt, average_spectra_times.txt
+        and with GWs spectra_gws.txt, energy_gws.txt."""
         p = self.p
         bg = lat.background()
         en = lat.energies()

@@ -32,6 +32,7 @@ RUNS = {
     "spec2_n16_vv4": ("spec2_n16_vv4", 20, 0.005, 10, True),
     "spec2_n32_vv2": ("spec2_n32_vv2", 40, 0.005, 20, False),
     "snap2_n16_vv4": ("snap2_n16_vv4", 20, 0.005, 10, True),
+    "out2_n16_vv4": ("out2_n16_vv4", 0, 0.005, 1, True),
     "pad1_n16": ("pad1_n16", 20, 0.002, 10, True),
     "pad2_n16_vv4": ("pad2_n16_vv4", 20, 0.005, 10, True),
     "gw2_n16_vv4": ("gw2_n16_vv4", 10, 0.005, 5, True),
@@ -163,6 +164,15 @@ def generate(run: str) -> str:
             for name in names:
                 raw = np.fromfile(os.path.join(snap, f"data_{nsteps}_snapshot.h5._{name}.bin"), dtype=np.float64)
                 out[f"snap_{name}"] = raw.reshape(N, N, N)
+        # with shistograms2d / sslices on: save()'s 2-D histograms and slices at t = 0
+        if os.path.exists(os.path.join(o, "histogram2d0_1.txt")):
+            out["histogram2d0_1"] = read_blocks(os.path.join(o, "histogram2d0_1.txt"))[..., 0]
+            out["histogram2dtimes"] = read_rows(os.path.join(o, "histogram2dtimes.txt"))
+            out["ic_f_real"] = ic["f"]   # the real-space fields save() binned and sliced
+        if os.path.exists(os.path.join(o, "slices0.txt")):
+            for fld in range(ic["nflds"]):
+                out[f"slices_{fld}"] = read_blocks(os.path.join(o, f"slices{fld}.txt"))[..., 0]
+            out["slicetimes"] = read_rows(os.path.join(o, "slicetimes.txt"))
         # initial state in k-space (what both paths start from)
         out["ic_f_k"] = ic["f_k"]
         out["ic_pi_k"] = ic["pi_k"]

@@ -181,3 +181,35 @@ def test_text_writer_histograms_and_snapshot(tmp_path):
     ref = g["histogramtimes"][-1]
     assert row[0] == f"{ref[0]:.6f}"
     assert np.allclose([float(x) for x in row[1:]], ref[1:], rtol=1e-6, atol=0)
+
+
+def test_histograms_2d_and_slices():
+    """Device 2-D histograms and slices: bit-exact with the oracle on the same real field,
+    and against the reference's own save() at t = 0 (golden out2_n16_vv4; the fields differ
+    from the reference's by FFT rounding: slices 1e-12, at most 2 points in another bin)."""
+    from pspectcosmo_gb300 import Lattice
+
+    g, meta = load("out2_n16_vv4")
+    p = params_for(meta, 64)
+    lat = Lattice(p)
+    bg = g["bg"][0]
+    lat.set_state(g["ic_f_k"], g["ic_pi_k"], bg[2], bg[3], bg[4])
+    f, _ = lat.fields_real()
+    o = _oref()
+    h = lat.histograms_2d(0, 1, 10, 10)
+    freq, bmin, df = o.histogram_2d(f[0], f[1], 10, 10)
+    assert np.array_equal(h["binfreq"], freq) and np.array_equal(h["bmin"], bmin) and np.array_equal(h["df"], df)
+    npts = p.N ** 3
+    assert np.abs(np.rint(h["binfreq"].ravel() * npts) - np.rint(g["histogram2d0_1"][0] * npts)).sum() <= 4
+    row = g["histogram2dtimes"][0]
+    assert np.allclose([h["bmin"][0], h["df"][0], h["bmin"][1], h["df"][1]], row[1:], rtol=1e-12, atol=0)
+    for dim, skip, avg in ((2, 2, 1), (1, 3, 1), (3, 4, 1), (2, 1, 0), (3, 5, 0)):
+        s = lat.slices(dim, p.N, skip, avg)
+        for fld in range(2):
+            assert np.array_equal(s[fld], o.slices(f[fld], dim, p.N, skip, avg)), (dim, skip, avg)
+    s = lat.slices(2, p.N, 2, 1)
+    for fld in range(2):
+        assert rel(s[fld], g[f"slices_{fld}"][0]) < 1e-12
+    h2 = lat.histograms_2d(1, 0, 7, 5, -1e-8, 1e-8)
+    freq, _, _ = o.histogram_2d(f[1], f[0], 7, 5, -1e-8, 1e-8)
+    assert np.array_equal(h2["binfreq"], freq)

@@ -172,3 +172,17 @@ def test_info_file_matches_reference(tmp_path):
     assert text.split("\nRun began at")[0] == meta["info"]
     assert text.rstrip().endswith("took less than 1 second")
     assert TextWriter.readable_time(90061) == "1 days, 1 hours, 1 minutes, 1 seconds\n"
+
+
+def test_histogram_2d_and_slices_match_reference():
+    """histograms_2d() and slices() (output.cpp:1300-1539) of the reference's own save() at
+    t = 0 (golden out2_n16_vv4: field pair 0, 1 in 10 x 10 bins; 2-D slices, skip 2, averaged)."""
+    g, meta = load("out2_n16_vv4")
+    o = _outputs_ref()
+    f = g["ic_f_real"]
+    freq, bmin, df = o.histogram_2d(f[0], f[1], 10, 10)
+    assert np.array_equal(freq.ravel(), g["histogram2d0_1"][0])
+    row = g["histogram2dtimes"][0]
+    assert list(row[1:]) == [bmin[0], df[0], bmin[1], df[1]]
+    for fld in range(2):
+        assert np.array_equal(o.slices(f[fld], slicedim=2, sliceskip=2), g[f"slices_{fld}"][0])
