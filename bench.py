@@ -484,6 +484,42 @@ def run_ours(args):
                                                                   "hdot2": 1e-3},
                   "after_steps": args.steps}
 
+    # a long FP32 and FP64 trajectory side by side (--fp64-steps S): the spectrum, a and rho_GW
+    # errors of the FP32 path against the FP64 one and both Friedmann violations along the way
+    traj = None
+    if p.precision == 32 and rank == 0 and args.fp64_steps > 0 and not big:
+        q = p.copy()
+        q.precision = 64
+        lat32, lat64 = Lattice(p), Lattice(q)
+        lat32.initialize()
+        lat64.initialize()
+        points, done = [], 0
+        chunk = max(1, args.fp64_steps // 8)
+        while done < args.fp64_steps:
+            n = min(chunk, args.fp64_steps - done)
+            lat32.evolve(dt, n)
+            lat64.evolve(dt, n)
+            done += n
+            s32, s64 = lat32.spectra_raw(), lat64.spectra_raw()
+            e32, e64 = lat32.energies(), lat64.energies()
+            b32, b64 = lat32.background(), lat64.background()
+
+            def relmax(a, b):
+                d = float(np.abs(b).max())
+                return float(np.abs(a - b).max() / d) if d > 0 else 0.0
+
+            pt = {"step": done, "t": b64["t"], "a": b64["a"], "a_rel_err": abs(b32["a"] - b64["a"]) / abs(b64["a"]),
+                  "friedmann_violation_fp32": e32["friedmann_violation"],
+                  "friedmann_violation_fp64": e64["friedmann_violation"]}
+            pt.update({f"{k}_rel_err": relmax(s32[k], s64[k])
+                       for k in ("f2", "pi2", "n2") + (("h2", "hdot2") if p.with_gw else ())})
+            if p.with_gw:
+                pt["rho_gw_rel_err"] = abs(e32["rho_gw"] - e64["rho_gw"]) / abs(e64["rho_gw"])
+            points.append(pt)
+        lat32.close()
+        lat64.close()
+        traj = {"steps": args.fp64_steps, "dt": dt, "points": points}
+
     if rank == 0:
         yard = None if big else fft_yardstick(lat, p)
         cpu = cpu_sample(p, dt, budget_s=20.0) if (world == 1 and not args.no_cpu and not big) else None
@@ -506,6 +542,7 @@ def run_ours(args):
             "passes_ms": passes,
             "fp32_vs_fp64": fp_cmp,
             "fft_yardstick": yard,
+            "fp32_vs_fp64_trajectory": traj,
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": gpu_launches,
@@ -526,6 +563,8 @@ def main():
     ap.add_argument("--precision", type=int, default=32, choices=[32, 64])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
+    ap.add_argument("--fp64-steps", type=int, default=0,
+                    help="also run FP32 and FP64 lattices this many steps side by side and report the errors")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
