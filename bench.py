@@ -441,7 +441,7 @@ def run_ours(args):
                "d2h_bytes_per_step": state_bytes_host / args.steps + 3 * 8 + 4 + 8}
 
     # per-pass device times and roofline of the dominant pass
-    passes = lat.time_passes(reps=3)
+    passes = lat.time_passes(reps=10)
     pbytes = lat.pass_bytes()
     peak, peak_kind = measured_peaks()
     dom = max((k for k in passes if k != "background"), key=lambda k: passes[k])
