@@ -11,6 +11,12 @@
  *   evolve_VV_k_nopad(dt) / evolve_VV(dt) -> psc_step
  *   spectra(), energy(), meansvars(), scale() -> psc_spectra, psc_energies, psc_means
  *   global arrays f_k, pi_k, u_k, pi_u_k, a, ad, add -> psc_get_state / psc_set_state
+ *   histograms(), histograms_2d(), slices()   -> psc_histograms, psc_histograms_2d, psc_slices
+ *   save_Snap() / the HDF5 snapshot files     -> psc_snapshot_arrays, psc_write_snapshot, psc_h5_*
+ *   evolve_VV_k_pad(dt) (N_PAD != N)          -> psc_step on a handle created with N_pad
+ *   ANALYTIC_EVOLUTION phase                  -> psc_analytic_begin / _step / _to_lattice
+ *   (no reference counterpart) checkpoint/resume, ensembles, adjoint gradients
+ *                                             -> psc_checkpoint_*, psc_batch_*, psc_adjoint*
  *
  * Conventions: every call returns PSC_OK (0) or a negative PSC_ERR_* code and
  * never throws or exits; psc_strerror names the code and psc_last_error gives the
