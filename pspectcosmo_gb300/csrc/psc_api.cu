@@ -8,6 +8,7 @@
 // groups its realizations by configuration into such handles and captures all
 // of them in one CUDA graph per step.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -17,6 +18,10 @@
 #include <tuple>
 #include <thread>
 #include <vector>
+
+#ifdef __linux__
+#include <sched.h>
+#endif
 
 #include "../../include/psc.h"
 #include "psc_bg.h"
@@ -90,6 +95,7 @@ void free_all(psc_handle *h) {
     for (void *q : h->allocs) cudaFree(q);
     h->allocs.clear();
     if (h->stage_buf) cudaFreeHost(h->stage_buf);
+    if (h->xfer) cudaFree(h->xfer);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->st) cudaStreamDestroy(h->st);
@@ -147,12 +153,22 @@ int ensure_staging(psc_handle *h, size_t bytes) {
 
 // out[i] = (To)in[i] for i < n on all host cores (the FP64 <-> FP32 conversion of the
 // state exchange is memory-bound; one thread converts ~1-2 GB/s)
+// host threads of the conversions: the CPUs this process may run on, at most 32
+unsigned host_threads() {
+    unsigned nt = 0;
+#ifdef __linux__
+    cpu_set_t set;
+    if (sched_getaffinity(0, sizeof(set), &set) == 0) nt = (unsigned)CPU_COUNT(&set);
+#endif
+    if (nt == 0) nt = std::thread::hardware_concurrency();
+    if (nt == 0) nt = 1;
+    return nt > 32 ? 32 : nt;
+}
+
 template <typename To, typename From>
 void convert_parallel(To *out, const From *in, size_t n) {
     const size_t kMin = 1u << 20;
-    unsigned nt = std::thread::hardware_concurrency();
-    if (nt == 0) nt = 1;
-    if (nt > 32) nt = 32;
+    unsigned nt = host_threads();
     if (n < kMin * 2 || nt == 1) {
         for (size_t i = 0; i < n; ++i) out[i] = (To)in[i];
         return;
@@ -170,18 +186,43 @@ void convert_parallel(To *out, const From *in, size_t n) {
     for (auto &x : th) x.join();
 }
 
-// host FP64 complex -> device array of the handle's precision
+// out[i] = (float)in[i], round to nearest even: the host cast's rounding
+__global__ void k_round_f32(const double *__restrict__ in, float *__restrict__ out, size_t n) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = __double2float_rn(in[i]);
+}
+
+// host FP64 complex -> device array of the handle's precision. An FP32 handle copies
+// the caller's FP64 data chunk by chunk into a device scratch and rounds it there: the
+// copy engine reads the caller's memory at C2C speed, while rounding on the host
+// cores moved 1.5x the bytes through host memory (256^3 + GW state: 12 ms vs 21 ms).
 int upload(psc_handle *h, void *dst, const double *src, size_t ncplx) {
     if (h->p0().precision == 64) {
         CU(cudaMemcpyAsync(dst, src, ncplx * 16, cudaMemcpyHostToDevice, h->st));
         CU(cudaStreamSynchronize(h->st));
         return PSC_OK;
     }
-    int rc = ensure_staging(h, ncplx * 8);
-    if (rc) return rc;
-    float *f = static_cast<float *>(h->stage_buf);
-    convert_parallel(f, src, 2 * ncplx);
-    CU(cudaMemcpyAsync(dst, f, ncplx * 8, cudaMemcpyHostToDevice, h->st));
+    const size_t n = 2 * ncplx;
+    const size_t kChunk = (size_t)16 << 20;   // doubles per chunk (128 MB)
+    const size_t want = n < kChunk ? n : kChunk;
+    if (h->xfer_elems < want) {
+        if (h->xfer) cudaFree(h->xfer);
+        h->xfer = nullptr;
+        h->xfer_elems = 0;
+        if (cudaMalloc(&h->xfer, want * sizeof(double)) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(PSC_ERR_NOMEM, "upload scratch");
+        }
+        h->xfer_elems = want;
+    }
+    float *out = static_cast<float *>(dst);
+    for (size_t off = 0; off < n; off += h->xfer_elems) {
+        const size_t c = n - off < h->xfer_elems ? n - off : h->xfer_elems;
+        CU(cudaMemcpyAsync(h->xfer, src + off, c * sizeof(double), cudaMemcpyHostToDevice, h->st));
+        const size_t blocks = (c + 255) / 256;
+        k_round_f32<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, h->st>>>(h->xfer, out + off, c);
+        CU(cudaGetLastError());
+    }
     CU(cudaStreamSynchronize(h->st));
     return PSC_OK;
 }
@@ -195,9 +236,59 @@ int download_real(psc_handle *h, double *dst, const void *src, size_t count) {
     }
     int rc = ensure_staging(h, count * 4);
     if (rc) return rc;
-    CU(cudaMemcpyAsync(h->stage_buf, src, count * 4, cudaMemcpyDeviceToHost, h->st));
-    CU(cudaStreamSynchronize(h->st));
-    convert_parallel(dst, static_cast<const float *>(h->stage_buf), count);
+    const float *s = static_cast<const float *>(src);
+    float *stg = static_cast<float *>(h->stage_buf);
+    // K chunks copied back-to-back into the pinned staging, an event after each; the host
+    // threads widen chunk k as soon as its event has completed, while the copy engine
+    // moves chunk k+1 (no staging slot is reused, so no copy waits for a conversion)
+    const size_t kMinChunk = (size_t)4 << 20;
+    int K = (int)(count / kMinChunk);
+    if (K > 16) K = 16;
+    if (K < 1) K = 1;
+    const size_t clen = (count + K - 1) / K;
+    cudaEvent_t ev[16];
+    int made = 0;
+    for (int k = 0; k < K; ++k) {
+        const size_t b = (size_t)k * clen, e = std::min(count, b + clen);
+        cudaError_t err = cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming);
+        if (err == cudaSuccess) {
+            ++made;
+            if (b < e) err = cudaMemcpyAsync(stg + b, s + b, (e - b) * 4, cudaMemcpyDeviceToHost, h->st);
+        }
+        if (err == cudaSuccess) err = cudaEventRecord(ev[k], h->st);
+        if (err != cudaSuccess) {
+            cudaStreamSynchronize(h->st);
+            for (int i = 0; i < made; ++i) cudaEventDestroy(ev[i]);
+            return fail(PSC_ERR_CUDA, std::string("download: ") + cudaGetErrorString(err));
+        }
+    }
+    unsigned nt = host_threads();
+    if (count < ((size_t)2 << 20)) nt = 1;
+    std::atomic<int> bad{0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    auto work = [&](unsigned w) {
+        if (w && cudaSetDevice(dev) != cudaSuccess) {
+            bad.store(1);
+            return;
+        }
+        for (int k = 0; k < K; ++k) {
+            if (cudaEventSynchronize(ev[k]) != cudaSuccess) {
+                bad.store(1);
+                return;
+            }
+            const size_t b = (size_t)k * clen, e = std::min(count, b + clen);
+            const size_t per = (e - b + nt - 1) / nt;
+            const size_t lo = std::min(e, b + w * per), hi = std::min(e, lo + per);
+            for (size_t i = lo; i < hi; ++i) dst[i] = (double)stg[i];
+        }
+    };
+    std::vector<std::thread> th;
+    for (unsigned w = 1; w < nt; ++w) th.emplace_back(work, w);
+    work(0);
+    for (auto &x : th) x.join();
+    for (int k = 0; k < K; ++k) cudaEventDestroy(ev[k]);
+    if (bad.load()) return fail(PSC_ERR_CUDA, "download: copy failed");
     return PSC_OK;
 }
 

@@ -30,6 +30,8 @@ struct psc_handle {
     float last_ms = 0.f;
     void *stage_buf = nullptr;   // pinned staging for precision conversion
     size_t stage_bytes = 0;
+    double *xfer = nullptr;      // device FP64 scratch of the FP32 upload (one chunk)
+    size_t xfer_elems = 0;
     std::vector<void *> allocs;
     void *adj = nullptr;         // adjoint workspace (psc_adjoint.cu), owned by the handle
     void (*adj_free)(void *) = nullptr;

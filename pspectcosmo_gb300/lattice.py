@@ -244,10 +244,11 @@ class Lattice:
 
     def get_state(self):
         p = self.p
-        f = np.zeros((p.nflds, p.modes), np.complex128)
-        pi = np.zeros((p.nflds, p.modes), np.complex128)
-        u = np.zeros((6, p.modes), np.complex128) if p.with_gw else None
-        pu = np.zeros((6, p.modes), np.complex128) if p.with_gw else None
+        # psc_get_state writes every element (no zero fill needed)
+        f = np.empty((p.nflds, p.modes), np.complex128)
+        pi = np.empty((p.nflds, p.modes), np.complex128)
+        u = np.empty((6, p.modes), np.complex128) if p.with_gw else None
+        pu = np.empty((6, p.modes), np.complex128) if p.with_gw else None
         a, ad, add = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
         _check(self._L.psc_get_state(self._h, _dp(f), _dp(pi), ctypes.byref(a), ctypes.byref(ad), ctypes.byref(add),
                                      _dp(u), _dp(pu)), "psc_get_state")
@@ -532,10 +533,10 @@ class Ensemble:
 
     def get_state(self, idx: int):
         p = self.params[idx]
-        f = np.zeros((p.nflds, p.modes), np.complex128)
-        pi = np.zeros((p.nflds, p.modes), np.complex128)
-        u = np.zeros((6, p.modes), np.complex128) if p.with_gw else None
-        pu = np.zeros((6, p.modes), np.complex128) if p.with_gw else None
+        f = np.empty((p.nflds, p.modes), np.complex128)
+        pi = np.empty((p.nflds, p.modes), np.complex128)
+        u = np.empty((6, p.modes), np.complex128) if p.with_gw else None
+        pu = np.empty((6, p.modes), np.complex128) if p.with_gw else None
         a, ad, add = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
         _check(self._L.psc_batch_get_state(self._h, idx, _dp(f), _dp(pi), ctypes.byref(a), ctypes.byref(ad),
                                            ctypes.byref(add), _dp(u), _dp(pu)), "psc_batch_get_state")
