@@ -1028,10 +1028,13 @@ int psc_time_passes(psc_handle *h, int reps, float *ms) {
     double acc[PSC_NPASS] = {0, 0, 0, 0, 0, 0};
     // the passes of a stage with the drift on and zero drift and kick coefficients
     // (SCALAR_EVAL): the full memory traffic of a step's stage, the state unchanged
-    // (f + 0 pi = f exactly); a'' is kept (diagnostics mode)
+    // (f + 0 pi = f exactly); a'' is kept (diagnostics mode). The kick does not keep its
+    // force (no Fk, Fu): like every stage of a step call but the call's last one.
+    psc::Buffers bt = h->b;
+    bt.Fk = bt.Fu = nullptr;
     for (int r = 0; r < reps; ++r) {
-        CU(psc::launch_scalar(h->cfg, h->b, psc::SCALAR_EVAL, 0, h->st));
-        CU(psc::launch_stage_timed(h->cfg, h->b, h->p0().precision, 1, psc::SCALAR_EVAL_END, ev, h->st));
+        CU(psc::launch_scalar(h->cfg, bt, psc::SCALAR_EVAL, 0, h->st));
+        CU(psc::launch_stage_timed(h->cfg, bt, h->p0().precision, 1, psc::SCALAR_EVAL_END, ev, h->st));
         CU(cudaEventSynchronize(ev[6]));
         for (int i = 0; i < PSC_NPASS; ++i) {
             float t = 0.f;
