@@ -786,6 +786,8 @@ void plan(const psc_params &p, int R, LaunchCfg *cfg) {
         // the eight-input GW pass is bound by its instruction stream and runs one tile
         // per block (measured faster on GB300).
         cfg->smem_z = (size_t)(nslot + (g.gw ? 0 : nin)) * tlz * (g.M + g.M / 16 + 1) * csize;
+        // the GW pass on full-length transforms (N <= 512): four slots of N-point lines
+        if (g.gw && g.N <= 512) cfg->smem_z = (size_t)4 * tlz * (g.N + g.N / 16 + 1) * csize;
         const int ntiles = (g.lines_z + tlz - 1) / tlz;
         int sms = 0, dev = 0;
         if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
