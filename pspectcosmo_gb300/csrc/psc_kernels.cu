@@ -786,8 +786,12 @@ void plan(const psc_params &p, int R, LaunchCfg *cfg) {
         // the eight-input GW pass is bound by its instruction stream and runs one tile
         // per block (measured faster on GB300).
         cfg->smem_z = (size_t)(nslot + (g.gw ? 0 : nin)) * tlz * (g.M + g.M / 16 + 1) * csize;
-        // the GW pass on full-length transforms (N <= 512): four slots of N-point lines
-        if (g.gw && g.N <= 512) cfg->smem_z = (size_t)4 * tlz * (g.N + g.N / 16 + 1) * csize;
+        // the GW pass on full-length transforms (N <= 512): four slots of N-point lines and,
+        // in FP32 (persistent, next tile staged), the nf x 3 input lines of a tile
+        const bool gw_full = g.gw && g.N <= 512, gw_staged = gw_full && p.precision == 32;
+        if (gw_full)
+            cfg->smem_z = ((size_t)4 * tlz * (g.N + g.N / 16 + 1) +
+                           (gw_staged ? (size_t)g.nf * 3 * tlz * (g.M + 2) : 0)) * csize;
         const int ntiles = (g.lines_z + tlz - 1) / tlz;
         int sms = 0, dev = 0;
         if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
@@ -795,9 +799,9 @@ void plan(const psc_params &p, int R, LaunchCfg *cfg) {
             sms = 152;
         const size_t smem_sm = 227 * 1024;
         int per_sm = (int)(smem_sm / cfg->smem_z);
-        if (per_sm > 2) per_sm = 2;
+        if (per_sm > (gw_staged ? 3 : 2)) per_sm = gw_staged ? 3 : 2;
         if (per_sm < 1) per_sm = 1;
-        cfg->nbz = (g.gw || ntiles < per_sm * sms) ? ntiles : per_sm * sms;
+        cfg->nbz = ((g.gw && !gw_staged) || ntiles < per_sm * sms) ? ntiles : per_sm * sms;
         g.pkg_stride = 2 * kMaxFields * cfg->nbx;
         g.pv_stride = kMaxTerms * cfg->nbz;
         return;

@@ -641,7 +641,7 @@ __global__ void __launch_bounds__(256, GW ? 3 : 2) kr_zpass(Geo g, const cplx<T>
 // P[k] = (Z[k] + conj Z[N-k]) / 2, Q[k] = (Z[k] - conj Z[N-k]) / 2i, k = 0..N/2.
 // Thread layout as kr_zpass (pair, line, j), one tile of TL lines per block; shared
 // memory: four slots of TL lines x LS complex.
-template <typename T, int L>
+template <typename T, int L, bool STAGED>
 __global__ void __launch_bounds__(256, 3) kr_zpass_gw(Geo g, const cplx<T> *__restrict__ TA,
                                                      const cplx<T> *__restrict__ TB, const cplx<T> *__restrict__ TC,
                                                      cplx<T> *__restrict__ QV, cplx<T> *__restrict__ QS,
@@ -651,6 +651,7 @@ __global__ void __launch_bounds__(256, 3) kr_zpass_gw(Geo g, const cplx<T> *__re
     using C = cplx<T>;
     using RP = RegPlan<L>;
     constexpr int P = RP::P, LS = ZIdx<L>::LS, HL = L / 2;
+    constexpr int HS = HL + 2;   // staging stride of one input line (H = N/2 + 1 entries)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *slots = reinterpret_cast<C *>(smem_raw);
     {
@@ -670,141 +671,176 @@ __global__ void __launch_bounds__(256, 3) kr_zpass_gw(Geo g, const cplx<T> *__re
     const int t = (threadIdx.x / P) & (TL - 1);
     const int grp = threadIdx.x / (P * TL);         // this thread's input pair in phase 1
     const size_t slot_elems = (size_t)TL * LS;
+    // staging (STAGED): the next tile's input lines, [field][TA, TB, TC][line][HS]
+    C *stage = slots + 4 * slot_elems;
     const T inv_n3 = (T)bg->inv_n3;
     const T kIR = (T)bg->kIR;
+    const T fj = (T)j;
     const int fld = grp >> 1, kind = grp & 1;
     const C *srcA = (kind ? TB : TA) + (long long)fld * g.modes;
     const C *srcB = TC + (long long)fld * g.modes;
-    const int tile = blockIdx.x;
-    const int line = tile * TL + t;
-    const bool valid = line < g.lines_z;
+    const C *stA = stage + ((size_t)(fld * 3 + (kind ? 1 : 0)) * TL + t) * HS;
+    const C *stB = stage + ((size_t)(fld * 3 + 2) * TL + t) * HS;
+    const int ntiles = (g.lines_z + TL - 1) / TL;
+    // copy the input lines of tile `tl` into the staging area: warp w takes the lines
+    // w, w + 8, ... of the nf x 3 x TL, its lanes consecutive entries of each
+    auto prefetch = [&](int tl) {
+        if (tl < ntiles) {
+            const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+            const int nl = nf * 3 * TL;
+            for (int li = threadIdx.x >> 5; li < nl; li += nw) {
+                const int a = li >> g.tlz_shift, tt = li & (TL - 1);
+                const long long ln = (long long)tl * TL + tt;
+                if (ln >= g.lines_z) continue;
+                const int fl = a >= 3 ? 1 : 0, w = a - 3 * fl;
+                const C *src = (w == 0 ? TA : (w == 1 ? TB : TC)) + (long long)fl * g.modes + ln * H;
+                C *dst = stage + (size_t)li * HS;
+                for (int m = lane; m < H; m += 32) cp_async_elem(dst + m, src + m);
+            }
+        }
+        cp_async_commit();
+    };
     ModelG<T> mdl;
     mdl.kind = g.model;
     mdl.gsq = (T)g.gsq;
     T pot_t[kMaxTerms] = {T(0), T(0)};
-    C v[16];
-    {
-        // 1. two real c2r in one N-point transform
-        const ZIdx<L> ix{(int)(grp * slot_elems + t * LS)};
-        const long long lo = (long long)line * H;
-#pragma unroll
-        for (int r = 0; r < 16; ++r) {
-            const int n = j + r * P;
-            const int m = n <= HL ? n : L - n;
-            C a = mk<T>(0, 0), b = mk<T>(0, 0);
-            if (valid) {
-                a = srcA[lo + m];
-                if (kind) {
-                    b = srcB[lo + m];
-                } else {
-                    const T kz = (m == HL) ? T(0) : kIR * (T)m;   // d/dz, Nyquist zeroed
-                    b = mk<T>(-kz * a.y, kz * a.x);
-                }
-                if (m == 0 || m == HL) {
-                    a.y = T(0);
-                    b.y = T(0);
-                }
-            }
-            v[r] = (n <= HL) ? mk<T>(a.x - b.y, a.y + b.x) : mk<T>(a.x + b.y, b.x - a.y);
-        }
-        fft_reg<C, L, +1>(v, slots, ix, j, tw, N / L);
-        __syncthreads();
-#pragma unroll
-        for (int q = 0; q < RP::NBL; ++q)
-#pragma unroll
-            for (int r = 0; r < RP::RL; ++r) slots[ix(RP::out(j, q, r))] = cscale(v[q * RP::RL + r], inv_n3);
-    }
-    __syncthreads();
-
-    // 2. pointwise epilogue per site: V'(f), <V>, anisotropic stress
-    for (int idx = threadIdx.x; idx < TL * L; idx += blockDim.x) {
-        const int tt = idx / L, z = idx - tt * L;
-        const long long ln = (long long)tile * TL + tt;
-        if (ln >= g.lines_z) continue;
-        const int e = tt * LS + z + (z >> 4);
-        T f[2], d[2][3];
-#pragma unroll
-        for (int fl = 0; fl < 2; ++fl) {
-            if (fl < nf) {
-                const C p0 = slots[(2 * fl) * slot_elems + e], p1 = slots[(2 * fl + 1) * slot_elems + e];
-                f[fl] = p0.x;
-                d[fl][2] = p0.y;
-                d[fl][0] = p1.x;
-                d[fl][1] = p1.y;
-            } else {
-                f[fl] = T(0);
-                d[fl][0] = d[fl][1] = d[fl][2] = T(0);
-            }
-        }
-        if (tape_fx) {   // adjoint tape: the real fields
-#pragma unroll
-            for (int fl = 0; fl < 2; ++fl)
-                if (fl < nf) tape_fx[fl * g.sites + ln * N + z] = f[fl];
-        }
-        T vp[2] = {T(0), T(0)};
-        model_dvdf<T>(mdl, f, vp, nf);
-        model_potential<T, T, T>(mdl, f, pot_t);
-        T o[8];
-        const int si[6] = {0, 0, 0, 1, 1, 2}, sj[6] = {0, 1, 2, 1, 2, 2};
-        o[0] = vp[0];
-        o[1] = vp[1];
-#pragma unroll
-        for (int c = 0; c < 6; ++c) {
-            T sum = T(0);
-#pragma unroll
-            for (int fl = 0; fl < 2; ++fl)
-                if (fl < nf) sum += T(2) * d[fl][si[c]] * d[fl][sj[c]];
-            o[2 + c] = sum;
-        }
-        if (nf == 1) {   // V', S_00, ..., S_22, 0
-#pragma unroll
-            for (int c = 1; c < 7; ++c) o[c] = o[c + 1];
-            o[7] = T(0);
-        }
-#pragma unroll
-        for (int p = 0; p < 4; ++p) slots[p * slot_elems + e] = mk<T>(o[2 * p], o[2 * p + 1]);
-    }
-    __syncthreads();
-
-    // 3. two real r2c per N-point forward transform of output pair o
-    const int nreal = nf + 6;
-    const int rounds = (4 + pin - 1) / pin;
-    for (int it = 0; it < rounds; ++it) {
-        const int o = grp + it * pin;
-        const bool act = o < 4;
-        const ZIdx<L> ix{(int)((act ? o : 0) * slot_elems + t * LS)};
-#pragma unroll
-        for (int r = 0; r < 16; ++r) v[r] = act ? slots[ix(j + r * P)] : mk<T>(0, 0);
-        __syncthreads();   // all loads of this round precede the first exchange write
-        fft_reg<C, L, -1>(v, slots, ix, j, tw, N / L, act);
+    if (STAGED) prefetch(blockIdx.x);
+    for (int tile = blockIdx.x; tile < ntiles; tile = STAGED ? tile + gridDim.x : ntiles) {
+        const int line = tile * TL + t;
+        const bool valid = line < g.lines_z;
+        C v[16];
         {
-            const int r0 = 2 * o, r1 = 2 * o + 1;
-            auto arr = [&](int ri) -> C * {
-                return ri < nf ? QV + (long long)ri * g.modes : QS + (long long)(ri - nf) * g.modes;
-            };
-            const bool wr = act && valid;
-            C *d0 = wr ? arr(r0) + (long long)line * H : nullptr;
-            C *d1 = (wr && r1 < nreal) ? arr(r1) + (long long)line * H : nullptr;
+            // 1. two real c2r in one N-point transform
+            const ZIdx<L> ix{(int)(grp * slot_elems + t * LS)};
+            const long long lo = (long long)line * H;
+            if (STAGED) {
+                cp_async_wait_all();
+                __syncthreads();   // every thread's copies of this tile have landed
+            }
+#pragma unroll
+            for (int r = 0; r < 16; ++r) {
+                const int n = j + r * P;
+                const int m = n <= HL ? n : L - n;
+                const T fm = n <= HL ? fj + T(r * P) : T(L - r * P) - fj;   // (T)m without a conversion
+                C a = mk<T>(0, 0), b = mk<T>(0, 0);
+                if (valid) {
+                    a = STAGED ? stA[m] : srcA[lo + m];
+                    if (kind) {
+                        b = STAGED ? stB[m] : srcB[lo + m];
+                    } else {
+                        const T kz = (m == HL) ? T(0) : kIR * fm;   // d/dz, Nyquist zeroed
+                        b = mk<T>(-kz * a.y, kz * a.x);
+                    }
+                    if (m == 0 || m == HL) {
+                        a.y = T(0);
+                        b.y = T(0);
+                    }
+                }
+                v[r] = (n <= HL) ? mk<T>(a.x - b.y, a.y + b.x) : mk<T>(a.x + b.y, b.x - a.y);
+            }
+            if (STAGED) {
+                __syncthreads();   // every staging read of this tile is done
+                prefetch(tile + gridDim.x);
+            }
+            fft_reg<C, L, +1>(v, slots, ix, j, tw, N / L);
+            __syncthreads();
 #pragma unroll
             for (int q = 0; q < RP::NBL; ++q)
 #pragma unroll
-                for (int r = 0; r < RP::RL; ++r) {
-                    // out(j, q, r) grows with j: a register whose lane-0 index is above N/2
-                    // holds no written k in any lane (a compile-time skip)
-                    if (RP::out(0, q, r) > HL) continue;
-                    const int k = RP::out(j, q, r);
-                    const C zk = v[q * RP::RL + r];
-                    const C zc = partner_out<C, L>(v, j, q, r);   // conj Z[N - k]
-                    if (wr && k <= HL) {
-                        const C ev = cscale(cadd(zk, zc), T(0.5));
-                        const C dd = cscale(csub(zk, zc), T(0.5));
-                        d0[k] = ev;
-                        if (d1) d1[k] = mk<T>(dd.y, -dd.x);
-                    }
-                }
+                for (int r = 0; r < RP::RL; ++r) slots[ix(RP::out(j, q, r))] = cscale(v[q * RP::RL + r], inv_n3);
         }
-        __syncthreads();   // the transform's last exchange read precedes the next writes
+        __syncthreads();
+        // 2. pointwise epilogue per site: V'(f), <V>, anisotropic stress
+        for (int idx = threadIdx.x; idx < TL * L; idx += blockDim.x) {
+            const int tt = idx / L, z = idx - tt * L;
+            const long long ln = (long long)tile * TL + tt;
+            if (ln >= g.lines_z) continue;
+            const int e = tt * LS + z + (z >> 4);
+            T f[2], d[2][3];
+#pragma unroll
+            for (int fl = 0; fl < 2; ++fl) {
+                if (fl < nf) {
+                    const C p0 = slots[(2 * fl) * slot_elems + e], p1 = slots[(2 * fl + 1) * slot_elems + e];
+                    f[fl] = p0.x;
+                    d[fl][2] = p0.y;
+                    d[fl][0] = p1.x;
+                    d[fl][1] = p1.y;
+                } else {
+                    f[fl] = T(0);
+                    d[fl][0] = d[fl][1] = d[fl][2] = T(0);
+                }
+            }
+            if (tape_fx) {   // adjoint tape: the real fields
+#pragma unroll
+                for (int fl = 0; fl < 2; ++fl)
+                    if (fl < nf) tape_fx[fl * g.sites + ln * N + z] = f[fl];
+            }
+            T vp[2] = {T(0), T(0)};
+            model_dvdf<T>(mdl, f, vp, nf);
+            model_potential<T, T, T>(mdl, f, pot_t);
+            T o[8];
+            const int si[6] = {0, 0, 0, 1, 1, 2}, sj[6] = {0, 1, 2, 1, 2, 2};
+            o[0] = vp[0];
+            o[1] = vp[1];
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                T sum = T(0);
+#pragma unroll
+                for (int fl = 0; fl < 2; ++fl)
+                    if (fl < nf) sum += T(2) * d[fl][si[c]] * d[fl][sj[c]];
+                o[2 + c] = sum;
+            }
+            if (nf == 1) {   // V', S_00, ..., S_22, 0
+#pragma unroll
+                for (int c = 1; c < 7; ++c) o[c] = o[c + 1];
+                o[7] = T(0);
+            }
+#pragma unroll
+            for (int p = 0; p < 4; ++p) slots[p * slot_elems + e] = mk<T>(o[2 * p], o[2 * p + 1]);
+        }
+        __syncthreads();
+
+        // 3. two real r2c per N-point forward transform of output pair o
+        const int nreal = nf + 6;
+        const int rounds = (4 + pin - 1) / pin;
+        for (int it = 0; it < rounds; ++it) {
+            const int o = grp + it * pin;
+            const bool act = o < 4;
+            const ZIdx<L> ix{(int)((act ? o : 0) * slot_elems + t * LS)};
+#pragma unroll
+            for (int r = 0; r < 16; ++r) v[r] = act ? slots[ix(j + r * P)] : mk<T>(0, 0);
+            __syncthreads();   // all loads of this round precede the first exchange write
+            fft_reg<C, L, -1>(v, slots, ix, j, tw, N / L, act);
+            {
+                const int r0 = 2 * o, r1 = 2 * o + 1;
+                auto arr = [&](int ri) -> C * {
+                    return ri < nf ? QV + (long long)ri * g.modes : QS + (long long)(ri - nf) * g.modes;
+                };
+                const bool wr = act && valid;
+                C *d0 = wr ? arr(r0) + (long long)line * H : nullptr;
+                C *d1 = (wr && r1 < nreal) ? arr(r1) + (long long)line * H : nullptr;
+#pragma unroll
+                for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+                    for (int r = 0; r < RP::RL; ++r) {
+                        // out(j, q, r) grows with j: a register whose lane-0 index is above N/2
+                        // holds no written k in any lane (a compile-time skip)
+                        if (RP::out(0, q, r) > HL) continue;
+                        const int k = RP::out(j, q, r);
+                        const C zk = v[q * RP::RL + r];
+                        const C zc = partner_out<C, L>(v, j, q, r);   // conj Z[N - k]
+                        if (wr && k <= HL) {
+                            const C ev = cscale(cadd(zk, zc), T(0.5));
+                            const C dd = cscale(csub(zk, zc), T(0.5));
+                            d0[k] = ev;
+                            if (d1) d1[k] = mk<T>(dd.y, -dd.x);
+                        }
+                    }
+            }
+            __syncthreads();   // the transform's last exchange read precedes the next writes
+        }
     }
+    if (STAGED) cp_async_wait_all();
     block_reduce_store_t<T, kMaxTerms>(pot_t, partV, gridDim.x, blockIdx.x);
 }
 

@@ -44,7 +44,7 @@ struct RegLaunch {
         SETA((kr_zpass<T, M, false>), sz);
         SETA((kr_zpass<T, M, true>), sz);
         if constexpr (N <= 512) {
-            SETA((kr_zpass_gw<T, N>), sz);
+            SETA((kr_zpass_gw<T, N, sizeof(T) == 4>), sz);
         }
         SETA((kr_z_c2r_real<T, M>), (int)((256 / (M / 16)) * ZIdx<M>::LS * sizeof(C)));
         {
@@ -84,8 +84,8 @@ struct RegLaunch {
             kr_ifft_y<T, N, true><<<gx, txy, 3 * cfg.smem_xy, st>>>(g, TA, TB, TC, b.bg, tw);
             mark(2);
             if constexpr (N <= 512)
-                kr_zpass_gw<T, N><<<dim3(cfg.nbz, 1, R), tz, cfg.smem_z, st>>>(g, TA, TB, TC, QV, QS, b.partV, b.bg,
-                                                                             tw, (T *)b.tape_fx);
+                kr_zpass_gw<T, N, sizeof(T) == 4><<<dim3(cfg.nbz, 1, R), tz, cfg.smem_z, st>>>(
+                    g, TA, TB, TC, QV, QS, b.partV, b.bg, tw, (T *)b.tape_fx);
             else
                 kr_zpass<T, M, true><<<dim3(cfg.nbz, 1, R), tz, cfg.smem_z, st>>>(g, TA, TB, TC, QV, QS, b.partV, b.bg,
                                                                                 tw, (T *)b.tape_fx);
