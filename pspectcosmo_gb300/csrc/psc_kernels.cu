@@ -786,9 +786,9 @@ void plan(const psc_params &p, int R, LaunchCfg *cfg) {
         // the eight-input GW pass is bound by its instruction stream and runs one tile
         // per block (measured faster on GB300).
         cfg->smem_z = (size_t)(nslot + (g.gw ? 0 : nin)) * tlz * (g.M + g.M / 16 + 1) * csize;
-        // the GW pass on full-length transforms (N <= 512): four slots of N-point lines and,
-        // in FP32 (persistent, next tile staged), the nf x 3 input lines of a tile
-        const bool gw_full = g.gw && g.N <= 512, gw_staged = gw_full && p.precision == 32;
+        // the GW pass on full-length transforms: four slots of N-point lines and, in FP32
+        // (persistent, next tile staged), the nf x 3 input lines of a tile
+        const bool gw_full = g.gw, gw_staged = gw_full && p.precision == 32;
         if (gw_full)
             cfg->smem_z = ((size_t)4 * tlz * (g.N + g.N / 16 + 1) +
                            (gw_staged ? (size_t)g.nf * 3 * tlz * (g.M + 2) : 0)) * csize;

@@ -463,7 +463,10 @@ __global__ void __launch_bounds__(256, GW ? 3 : 2) kr_zpass(Geo g, const cplx<T>
     ModelG<T> mdl;
     mdl.kind = g.model;
     mdl.gsq = (T)g.gsq;
+    // <V> partial sums: a tile's sites in the field precision, the tiles of a persistent
+    // block in FP64 (thousands of tiles per block at N = 1024)
     T pot_t[kMaxTerms] = {T(0), T(0)};
+    double pot_d[kMaxTerms] = {0.0, 0.0};
     if (STAGED) prefetch(blockIdx.x);
     for (int tile = blockIdx.x; tile < ntiles; tile = STAGED ? tile + gridDim.x : ntiles) {
         const int line = tile * TL + t;
@@ -587,6 +590,11 @@ __global__ void __launch_bounds__(256, GW ? 3 : 2) kr_zpass(Geo g, const cplx<T>
             for (int o = 0; o < 8; ++o)
                 if (o < nout) slots[o * slot_elems + e] = out[o];
         }
+#pragma unroll
+        for (int i = 0; i < kMaxTerms; ++i) {
+            pot_d[i] += (double)pot_t[i];
+            pot_t[i] = T(0);
+        }
         __syncthreads();
 
         // 3. real-to-complex along z of every product; X[k] = (Z[k] + conj Z[M-k])/2
@@ -627,27 +635,29 @@ __global__ void __launch_bounds__(256, GW ? 3 : 2) kr_zpass(Geo g, const cplx<T>
         }
     }
     if (STAGED) cp_async_wait_all();
-    block_reduce_store_t<T, kMaxTerms>(pot_t, partV, gridDim.x, blockIdx.x);
+    block_reduce_store_t<double, kMaxTerms>(pot_d, partV, gridDim.x, blockIdx.x);
 }
 
-// GW form of the Z pass on full-length line transforms (N <= 512, so that the P = N/16
-// lanes of a line sit in one warp). The eight real lines of a z line (f, d/dx f, d/dy f,
-// d/dz f of each field) travel as complex lines a + i b: pair 2 fld = f + i d/dz f (both
-// from TA), pair 2 fld + 1 = d/dx f + i d/dy f (TB, TC). One N-point inverse transform of
-// Z[n] = A[n] + i B[n] (n <= N/2), conj A[N-n] + i conj B[N-n] (n > N/2) gives both real
-// lines, with no packing step: Im of the kz = 0 and N/2 entries is dropped first, as a c2r
-// does. The products (V' of each field, then S_00, S_01, S_02, S_11, S_12, S_22) return
-// as four pairs, each split after one N-point forward transform:
-// P[k] = (Z[k] + conj Z[N-k]) / 2, Q[k] = (Z[k] - conj Z[N-k]) / 2i, k = 0..N/2.
-// Thread layout as kr_zpass (pair, line, j), one tile of TL lines per block; shared
-// memory: four slots of TL lines x LS complex.
+// GW form of the Z pass on full-length line transforms. The eight real lines of a z line
+// (f, d/dx f, d/dy f, d/dz f of each field) travel as complex lines a + i b: pair 2 fld =
+// f + i d/dz f (both from TA), pair 2 fld + 1 = d/dx f + i d/dy f (TB, TC). One N-point
+// inverse transform of Z[n] = A[n] + i B[n] (n <= N/2), conj A[N-n] + i conj B[N-n]
+// (n > N/2) gives both real lines, with no packing step: Im of the kz = 0 and N/2 entries
+// is dropped first, as a c2r does. The products (V' of each field, then S_00, S_01, S_02,
+// S_11, S_12, S_22) return as four pairs, each split after one N-point forward transform:
+// P[k] = (Z[k] + conj Z[N-k]) / 2, Q[k] = (Z[k] - conj Z[N-k]) / 2i, k = 0..N/2, the
+// partner Z[N-k] by warp shuffle (N <= 512) or through shared memory (N = 1024, where the
+// 64 lanes of a line span two warps). Thread layout as kr_zpass (pair, line, j).
+// STAGED (FP32): persistent, one wave of blocks walking the tiles; the input lines of the
+// next tile are copied into a staging area by cp.async while the current one is
+// transformed. Otherwise one tile per block, inputs read straight from global memory.
+// Shared memory: four slots of TL lines x LS complex, then (STAGED) the staging area.
 template <typename T, int L, bool STAGED>
 __global__ void __launch_bounds__(256, 3) kr_zpass_gw(Geo g, const cplx<T> *__restrict__ TA,
                                                      const cplx<T> *__restrict__ TB, const cplx<T> *__restrict__ TC,
                                                      cplx<T> *__restrict__ QV, cplx<T> *__restrict__ QS,
                                                      double *__restrict__ partV, const DevBG *__restrict__ bg,
                                                      const cplx<T> *__restrict__ tw, T *__restrict__ tape_fx) {
-    static_assert(L / 16 <= 32, "the lanes of a line must sit in one warp");
     using C = cplx<T>;
     using RP = RegPlan<L>;
     constexpr int P = RP::P, LS = ZIdx<L>::LS, HL = L / 2;
@@ -703,7 +713,10 @@ __global__ void __launch_bounds__(256, 3) kr_zpass_gw(Geo g, const cplx<T> *__re
     ModelG<T> mdl;
     mdl.kind = g.model;
     mdl.gsq = (T)g.gsq;
+    // <V> partial sums: a tile's sites in the field precision, the tiles of a persistent
+    // block in FP64 (thousands of tiles per block at N = 1024)
     T pot_t[kMaxTerms] = {T(0), T(0)};
+    double pot_d[kMaxTerms] = {0.0, 0.0};
     if (STAGED) prefetch(blockIdx.x);
     for (int tile = blockIdx.x; tile < ntiles; tile = STAGED ? tile + gridDim.x : ntiles) {
         const int line = tile * TL + t;
@@ -798,6 +811,11 @@ __global__ void __launch_bounds__(256, 3) kr_zpass_gw(Geo g, const cplx<T> *__re
 #pragma unroll
             for (int p = 0; p < 4; ++p) slots[p * slot_elems + e] = mk<T>(o[2 * p], o[2 * p + 1]);
         }
+#pragma unroll
+        for (int i = 0; i < kMaxTerms; ++i) {
+            pot_d[i] += (double)pot_t[i];
+            pot_t[i] = T(0);
+        }
         __syncthreads();
 
         // 3. two real r2c per N-point forward transform of output pair o
@@ -819,29 +837,52 @@ __global__ void __launch_bounds__(256, 3) kr_zpass_gw(Geo g, const cplx<T> *__re
                 const bool wr = act && valid;
                 C *d0 = wr ? arr(r0) + (long long)line * H : nullptr;
                 C *d1 = (wr && r1 < nreal) ? arr(r1) + (long long)line * H : nullptr;
+                if constexpr (P <= 32) {
+                    // the partners Z[N-k] by warp shuffle (the P lanes of a line in one warp)
 #pragma unroll
-                for (int q = 0; q < RP::NBL; ++q)
+                    for (int q = 0; q < RP::NBL; ++q)
 #pragma unroll
-                    for (int r = 0; r < RP::RL; ++r) {
-                        // out(j, q, r) grows with j: a register whose lane-0 index is above N/2
-                        // holds no written k in any lane (a compile-time skip)
-                        if (RP::out(0, q, r) > HL) continue;
-                        const int k = RP::out(j, q, r);
-                        const C zk = v[q * RP::RL + r];
-                        const C zc = partner_out<C, L>(v, j, q, r);   // conj Z[N - k]
-                        if (wr && k <= HL) {
+                        for (int r = 0; r < RP::RL; ++r) {
+                            // out(j, q, r) grows with j: a register whose lane-0 index is above
+                            // N/2 holds no written k in any lane (a compile-time skip)
+                            if (RP::out(0, q, r) > HL) continue;
+                            const int k = RP::out(j, q, r);
+                            const C zk = v[q * RP::RL + r];
+                            const C zc = partner_out<C, L>(v, j, q, r);   // conj Z[N - k]
+                            if (wr && k <= HL) {
+                                const C ev = cscale(cadd(zk, zc), T(0.5));
+                                const C dd = cscale(csub(zk, zc), T(0.5));
+                                d0[k] = ev;
+                                if (d1) d1[k] = mk<T>(dd.y, -dd.x);
+                            }
+                        }
+                } else {
+                    // a line's lanes span two warps (N = 1024): Z goes through its slot and
+                    // each lane splits k = j, j + P, ... <= N/2 from there
+                    __syncthreads();   // the transform's last exchange reads are done
+                    if (act) {
+#pragma unroll
+                        for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+                            for (int r = 0; r < RP::RL; ++r) slots[ix(RP::out(j, q, r))] = v[q * RP::RL + r];
+                    }
+                    __syncthreads();
+                    if (wr) {
+                        for (int k = j; k <= HL; k += P) {
+                            const C zk = slots[ix(k)], zc = cconj(slots[ix((L - k) & (L - 1))]);
                             const C ev = cscale(cadd(zk, zc), T(0.5));
                             const C dd = cscale(csub(zk, zc), T(0.5));
                             d0[k] = ev;
                             if (d1) d1[k] = mk<T>(dd.y, -dd.x);
                         }
                     }
+                }
             }
             __syncthreads();   // the transform's last exchange read precedes the next writes
         }
     }
     if (STAGED) cp_async_wait_all();
-    block_reduce_store_t<T, kMaxTerms>(pot_t, partV, gridDim.x, blockIdx.x);
+    block_reduce_store_t<double, kMaxTerms>(pot_d, partV, gridDim.x, blockIdx.x);
 }
 
 // ------------------------------------------------------------------ real-space view (c2r along z)
@@ -917,7 +958,9 @@ __global__ void __launch_bounds__(256, 2) kr_zpass_adj(Geo g, const cplx<T> *__r
     const T eta2 = (T)ad->eta2, gam = (T)ad->gamma, gsq = (T)g.gsq;
     const bool two = g.model == PSC_MODEL_PHI2CHI2;
     const int ntiles = (g.lines_z + TL - 1) >> sh;
-    T acc_t[3] = {T(0), T(0), T(0)};   // per-thread partials, FP64 across threads
+    // per-thread partials: a tile's sites in the field precision, the block's tiles in FP64
+    T acc_t[3] = {T(0), T(0), T(0)};
+    double acc_d[3] = {0.0, 0.0, 0.0};
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int line = tile * TL + t;
         const bool valid = line < g.lines_z;
@@ -991,6 +1034,11 @@ __global__ void __launch_bounds__(256, 2) kr_zpass_adj(Geo g, const cplx<T> *__r
                 slots[e] = o0;
             }
         }
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            acc_d[i] += (double)acc_t[i];
+            acc_t[i] = T(0);
+        }
         __syncthreads();
         // 3. r2c along z of field grp
         {
@@ -1018,7 +1066,7 @@ __global__ void __launch_bounds__(256, 2) kr_zpass_adj(Geo g, const cplx<T> *__r
             __syncthreads();
         }
     }
-    block_reduce_store_t<T, 3>(acc_t, part, gridDim.x, blockIdx.x);
+    block_reduce_store_t<double, 3>(acc_d, part, gridDim.x, blockIdx.x);
 }
 
 // X forward transform of the adjoint's J^T application with its epilogue:

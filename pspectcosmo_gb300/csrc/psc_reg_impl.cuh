@@ -42,10 +42,7 @@ struct RegLaunch {
         SETA((kr_fft_x_final<T, N, false>), (int)cfg.smem_xf);
         SETA((kr_fft_x_final<T, N, true>), (int)cfg.smem_xf);
         SETA((kr_zpass<T, M, false>), sz);
-        SETA((kr_zpass<T, M, true>), sz);
-        if constexpr (N <= 512) {
-            SETA((kr_zpass_gw<T, N, sizeof(T) == 4>), sz);
-        }
+        SETA((kr_zpass_gw<T, N, sizeof(T) == 4>), sz);
         SETA((kr_z_c2r_real<T, M>), (int)((256 / (M / 16)) * ZIdx<M>::LS * sizeof(C)));
         {
             int tl = 1, sh = 0;
@@ -83,12 +80,8 @@ struct RegLaunch {
             mark(1);
             kr_ifft_y<T, N, true><<<gx, txy, 3 * cfg.smem_xy, st>>>(g, TA, TB, TC, b.bg, tw);
             mark(2);
-            if constexpr (N <= 512)
-                kr_zpass_gw<T, N, sizeof(T) == 4><<<dim3(cfg.nbz, 1, R), tz, cfg.smem_z, st>>>(
-                    g, TA, TB, TC, QV, QS, b.partV, b.bg, tw, (T *)b.tape_fx);
-            else
-                kr_zpass<T, M, true><<<dim3(cfg.nbz, 1, R), tz, cfg.smem_z, st>>>(g, TA, TB, TC, QV, QS, b.partV, b.bg,
-                                                                                tw, (T *)b.tape_fx);
+            kr_zpass_gw<T, N, sizeof(T) == 4><<<dim3(cfg.nbz, 1, R), tz, cfg.smem_z, st>>>(
+                g, TA, TB, TC, QV, QS, b.partV, b.bg, tw, (T *)b.tape_fx);
         } else {
             if (drift) kr_ifft_x<T, N, false, true><<<gx, txy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
             else kr_ifft_x<T, N, false, false><<<gx, txy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
