@@ -781,17 +781,16 @@ void plan(const psc_params &p, int R, LaunchCfg *cfg) {
         g.tlz_shift = ilog2i(tlz);
         g.ldz = 0;
         cfg->thr_z = nin * tlz * Pz;
-        // work slots + staging slots of the Z pass. Without GWs (one or two inputs per
-        // line) the pass is persistent, one wave of blocks prefetching their next tile;
-        // the eight-input GW pass is bound by its instruction stream and runs one tile
-        // per block (measured faster on GB300).
-        cfg->smem_z = (size_t)(nslot + (g.gw ? 0 : nin)) * tlz * (g.M + g.M / 16 + 1) * csize;
-        // the GW pass on full-length transforms: four slots of N-point lines and, in FP32
-        // (persistent, next tile staged), the nf x 3 input lines of a tile
-        const bool gw_full = g.gw, gw_staged = gw_full && p.precision == 32;
-        if (gw_full)
+        // Z pass shared memory. Without GWs (kr_zpass): nf work slots + nf staging slots of
+        // half-length lines, persistent (2 blocks per SM). With GWs (kr_zpass_gw): four
+        // slots of N-point lines and, in FP32 (persistent, 3 blocks per SM, next tile
+        // staged), the nf x 3 input lines of a tile; in FP64 one tile per block.
+        const bool gw_staged = g.gw && p.precision == 32;
+        if (g.gw)
             cfg->smem_z = ((size_t)4 * tlz * (g.N + g.N / 16 + 1) +
                            (gw_staged ? (size_t)g.nf * 3 * tlz * (g.M + 2) : 0)) * csize;
+        else
+            cfg->smem_z = (size_t)2 * g.nf * tlz * (g.M + g.M / 16 + 1) * csize;
         const int ntiles = (g.lines_z + tlz - 1) / tlz;
         int sms = 0, dev = 0;
         if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=

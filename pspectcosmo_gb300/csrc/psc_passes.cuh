@@ -402,52 +402,38 @@ __device__ __forceinline__ C partner_out(const C (&v)[16], int j, int q, int r) 
     return cconj(z);
 }
 
-// Without GWs (one or two inputs per line) the pass is persistent: a block walks the
-// tiles blockIdx.x, blockIdx.x + gridDim.x, ...; while one tile is transformed, the
-// input lines of the next are copied into a staging area by cp.async (no register
-// round trip), so the HBM reads overlap the FFT work. Shared memory: nslot work slots,
-// then nin staging slots. The eight-input GW pass, bound by its instruction stream,
-// runs one tile per block and loads its lines straight into the work slots.
-template <typename T, int L, bool GW>
-__global__ void __launch_bounds__(256, GW ? 3 : 2) kr_zpass(Geo g, const cplx<T> *__restrict__ TA, const cplx<T> *__restrict__ TB,
-                                                const cplx<T> *__restrict__ TC, cplx<T> *__restrict__ QV,
-                                                cplx<T> *__restrict__ QS, double *__restrict__ partV,
-                                                const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw,
-                                                T *__restrict__ tape_fx = nullptr) {
+// Z pass without GWs (one or two fields, one input line per field). Persistent: a block
+// walks the tiles blockIdx.x, blockIdx.x + gridDim.x, ...; while one tile is transformed,
+// the input lines of the next are copied into a staging area by cp.async (no register
+// round trip), so the HBM reads overlap the FFT work. Shared memory: nf work slots, then
+// nf staging slots, TL lines x LS complex each (a complex element holds the real sites
+// 2m, 2m+1). The GW form is kr_zpass_gw.
+template <typename T, int L>
+__global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restrict__ TA, cplx<T> *__restrict__ QV,
+                                                double *__restrict__ partV, const DevBG *__restrict__ bg,
+                                                const cplx<T> *__restrict__ tw, T *__restrict__ tape_fx = nullptr) {
     using C = cplx<T>;
     using RP = RegPlan<L>;
     constexpr int M = L, P = RP::P, LS = ZIdx<L>::LS;
-    constexpr bool STAGED = !GW;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *slots = reinterpret_cast<C *>(smem_raw);
     {
-        const long long rf = (long long)blockIdx.z * g.fstride, rg = (long long)blockIdx.z * g.gstride;
+        const long long rf = (long long)blockIdx.z * g.fstride;
         TA += rf;
         QV += rf;
-        if (GW) {
-            TB += rf;
-            TC += rf;
-            QS += rg;
-        }
         partV += (size_t)blockIdx.z * g.pv_stride;
         bg += blockIdx.z;
     }
     const int sh = g.tlz_shift, TL = 1 << sh, H = g.H, N = g.N;
     const int nf = g.nf;
-    const int nin = nf * (GW ? 4 : 1);
-    const int nout = nf + (GW ? 6 : 0);
-    const int nslot = nin > nout ? nin : nout;
     const int j = threadIdx.x % P;
     const int t = (threadIdx.x / P) & (TL - 1);
-    const int grp = threadIdx.x / (P * TL);   // input handled by this thread in phase 1
+    const int grp = threadIdx.x / (P * TL);   // the field this thread transforms
     const size_t slot_elems = (size_t)TL * LS;
-    C *stage = slots + (size_t)nslot * slot_elems;
+    C *stage = slots + (size_t)nf * slot_elems;
     const T inv_n3 = (T)bg->inv_n3;
-    const T kIR = (T)bg->kIR;
-    const int fld = GW ? (grp >> 2) : grp;
-    const int kind = GW ? (grp & 3) : 0;   // 0: f, 1: d/dx f, 2: d/dy f, 3: d/dz f
-    const C *src0 = (kind == 1 ? TB : (kind == 2 ? TC : TA)) + (long long)fld * g.modes;
-    const ZIdx<L> ixs{(int)(grp * slot_elems + t * LS)};
+    const C *src0 = TA + (long long)grp * g.modes;
+    const ZIdx<L> ix{(int)(grp * slot_elems + t * LS)};
     const int ntiles = (g.lines_z + TL - 1) >> sh;
     // stage X[0..M] of this thread's line of tile `tile` (M+1 entries fit: the pad leaves room)
     auto prefetch = [&](int tile) {
@@ -455,51 +441,37 @@ __global__ void __launch_bounds__(256, GW ? 3 : 2) kr_zpass(Geo g, const cplx<T>
         if (tile < ntiles && ln < g.lines_z) {
             const C *src = src0 + (long long)ln * H;
 #pragma unroll
-            for (int r = 0; r < 16; ++r) cp_async_elem(stage + ixs(j + r * P), src + j + r * P);
-            if (j == 0) cp_async_elem(stage + ixs(M), src + M);
+            for (int r = 0; r < 16; ++r) cp_async_elem(stage + ix(j + r * P), src + j + r * P);
+            if (j == 0) cp_async_elem(stage + ix(M), src + M);
         }
         cp_async_commit();
     };
     ModelG<T> mdl;
     mdl.kind = g.model;
     mdl.gsq = (T)g.gsq;
-    // <V> partial sums: a tile's sites in the field precision, the tiles of a persistent
-    // block in FP64 (thousands of tiles per block at N = 1024)
+    // <V> partial sums: up to 16 tiles' sites in the field precision, then folded into
+    // FP64 (a persistent block walks thousands of tiles at N = 1024; a fold per tile
+    // would put a conversion and an add per thread and tile on the narrow FP64 pipe)
     T pot_t[kMaxTerms] = {T(0), T(0)};
     double pot_d[kMaxTerms] = {0.0, 0.0};
-    if (STAGED) prefetch(blockIdx.x);
-    for (int tile = blockIdx.x; tile < ntiles; tile = STAGED ? tile + gridDim.x : ntiles) {
+    int nfold = 0;
+    prefetch(blockIdx.x);
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int line = tile * TL + t;
         const bool valid = line < g.lines_z;
-        const ZIdx<L> ix{(int)(grp * slot_elems + t * LS)};
-        // 1. complex-to-real along z of input grp: pack X[k], X[M-k] into the
-        //    M-point transform Z[k] = (X[k] + conj X[M-k]) + i w^k (X[k] - conj X[M-k]),
-        //    w = e^{+2 pi i/N}; Im X[0] and Im X[M] are ignored, as a c2r does.
-        //    Staged form: both from the staging area; one-tile form: own elements from
-        //    global memory into registers, partners by warp shuffle.
+        // 1. complex-to-real along z of field grp: pack X[k], X[M-k] into the M-point
+        //    transform Z[k] = (X[k] + conj X[M-k]) + i w^k (X[k] - conj X[M-k]),
+        //    w = e^{+2 pi i/N}; Im X[0] and Im X[M] are ignored, as a c2r does. Own
+        //    elements from the staging area, partners by warp shuffle.
         C v[16], yv[16];
-        if (STAGED) {
+        {
             cp_async_wait_all();
             __syncthreads();
             C xM = mk<T>(0, 0);
 #pragma unroll
-            for (int r = 0; r < 16; ++r) v[r] = stage[ixs(j + r * P)];
-            if (j == 0) xM = stage[ixs(M)];
+            for (int r = 0; r < 16; ++r) v[r] = stage[ix(j + r * P)];
+            if (j == 0) xM = stage[ix(M)];
             partners_in<C, M>(v, xM, j, yv);
-        } else {
-            C xM = mk<T>(0, 0);
-            if (valid) {
-                const C *src = src0 + (long long)line * H;
-#pragma unroll
-                for (int r = 0; r < 16; ++r) v[r] = src[j + r * P];
-                if (j == 0) xM = src[M];
-            } else {
-#pragma unroll
-                for (int r = 0; r < 16; ++r) v[r] = mk<T>(0, 0);
-            }
-            partners_in<C, M>(v, xM, j, yv);
-        }
-        {
 #pragma unroll
             for (int r = 0; r < 16; ++r) {
                 const int k = j + r * P;
@@ -507,12 +479,6 @@ __global__ void __launch_bounds__(256, GW ? 3 : 2) kr_zpass(Geo g, const cplx<T>
                 if (valid) {
                     x = v[r];
                     y = yv[r];
-                    if (kind == 3) {
-                        const T kx = kIR * (T)k;                           // k < M
-                        const T ky = (k == 0) ? T(0) : kIR * (T)(M - k);   // Nyquist zeroed
-                        x = mk<T>(-kx * x.y, kx * x.x);
-                        y = mk<T>(-ky * y.y, ky * y.x);
-                    }
                 }
                 y.y = -y.y;
                 if (k == 0) { x.y = T(0); y.y = T(0); }
@@ -522,10 +488,8 @@ __global__ void __launch_bounds__(256, GW ? 3 : 2) kr_zpass(Geo g, const cplx<T>
                 const C td = cmul(w, d);
                 v[r] = mk<T>(s.x - td.y, s.y + td.x);
             }
-            if (STAGED) {
-                __syncthreads();   // every thread has read the staging area
-                prefetch(tile + gridDim.x);
-            }
+            __syncthreads();   // every thread has read the staging area
+            prefetch(tile + gridDim.x);
             fft_reg<C, L, +1>(v, slots, ix, j, tw, N / L);
             __syncthreads();
 #pragma unroll
@@ -535,106 +499,78 @@ __global__ void __launch_bounds__(256, GW ? 3 : 2) kr_zpass(Geo g, const cplx<T>
         }
         __syncthreads();
 
-        // 2. pointwise epilogue: V'(f), <V>, anisotropic stress
+        // 2. pointwise epilogue: V'(f), <V>
         for (int idx = threadIdx.x; idx < TL * M; idx += blockDim.x) {
             const int tt = idx / M, m = idx - tt * M;
             const long long ln = (long long)tile * TL + tt;
             if (ln >= g.lines_z) continue;
             const int e = tt * LS + m + (m >> 4);
-            C in[8];
+            C in[2];
 #pragma unroll
-            for (int o = 0; o < 8; ++o)
-                if (o < nin) in[o] = slots[o * slot_elems + e];
+            for (int o = 0; o < 2; ++o)
+                if (o < nf) in[o] = slots[o * slot_elems + e];
             if (tape_fx) {   // adjoint tape: the real fields (sites 2m, 2m+1 of the line)
 #pragma unroll
                 for (int fl = 0; fl < 2; ++fl)
-                    if (fl < nf) reinterpret_cast<C *>(tape_fx + fl * g.sites + ln * N)[m] = in[GW ? fl * 4 : fl];
+                    if (fl < nf) reinterpret_cast<C *>(tape_fx + fl * g.sites + ln * N)[m] = in[fl];
             }
-            C out[8];
+            C out[2];
 #pragma unroll
             for (int half = 0; half < 2; ++half) {
                 T f[2], vp[2];
 #pragma unroll
-                for (int fl = 0; fl < 2; ++fl) {
-                    if (fl < nf) {
-                        const C c = in[GW ? fl * 4 : fl];
-                        f[fl] = half ? c.y : c.x;
-                    } else {
-                        f[fl] = T(0);
-                    }
-                }
+                for (int fl = 0; fl < 2; ++fl) f[fl] = (fl < nf) ? (half ? in[fl].y : in[fl].x) : T(0);
                 model_dvdf<T>(mdl, f, vp, nf);
                 model_potential<T, T, T>(mdl, f, pot_t);
 #pragma unroll
                 for (int fl = 0; fl < 2; ++fl)
                     if (fl < nf) { if (half) out[fl].y = vp[fl]; else out[fl].x = vp[fl]; }
-                if (GW) {
-                    T d[2][3];
-#pragma unroll
-                    for (int fl = 0; fl < 2; ++fl)
-#pragma unroll
-                        for (int ax = 0; ax < 3; ++ax)
-                            d[fl][ax] = (fl < nf) ? (half ? in[fl * 4 + 1 + ax].y : in[fl * 4 + 1 + ax].x) : T(0);
-                    const int si[6] = {0, 0, 0, 1, 1, 2}, sj[6] = {0, 1, 2, 1, 2, 2};
-#pragma unroll
-                    for (int c = 0; c < 6; ++c) {
-                        T sum = T(0);
-#pragma unroll
-                        for (int fl = 0; fl < 2; ++fl)
-                            if (fl < nf) sum += T(2) * d[fl][si[c]] * d[fl][sj[c]];
-                        if (half) out[nf + c].y = sum; else out[nf + c].x = sum;
-                    }
-                }
             }
 #pragma unroll
-            for (int o = 0; o < 8; ++o)
-                if (o < nout) slots[o * slot_elems + e] = out[o];
+            for (int o = 0; o < 2; ++o)
+                if (o < nf) slots[o * slot_elems + e] = out[o];
         }
+        if ((++nfold & 15) == 0) {
 #pragma unroll
-        for (int i = 0; i < kMaxTerms; ++i) {
-            pot_d[i] += (double)pot_t[i];
-            pot_t[i] = T(0);
+            for (int i = 0; i < kMaxTerms; ++i) {
+                pot_d[i] += (double)pot_t[i];
+                pot_t[i] = T(0);
+            }
         }
         __syncthreads();
 
-        // 3. real-to-complex along z of every product; X[k] = (Z[k] + conj Z[M-k])/2
+        // 3. real-to-complex along z of V'(f) of field grp; X[k] = (Z[k] + conj Z[M-k])/2
         //    + e^{-2 pi i k/N} (Z[k] - conj Z[M-k])/(2i), k = 0..M (Z[M] = Z[0])
-        const int rounds = (nout + nin - 1) / nin;
-        for (int it = 0; it < rounds; ++it) {
-            const int o = grp + it * nin;
-            const bool act = o < nout;
-            const ZIdx<L> ix{(int)((act ? o : 0) * slot_elems + t * LS)};
 #pragma unroll
-            for (int r = 0; r < 16; ++r) v[r] = act ? slots[ix(j + r * P)] : mk<T>(0, 0);
-            __syncthreads();   // all loads of this round precede the first exchange write
-            fft_reg<C, L, -1>(v, slots, ix, j, tw, N / L, act);
-            {
-                // the partners Z[M-k] by warp shuffle, X[k] straight out
-                C *dst =
-                    ((o < nf) ? QV + (long long)o * g.modes : QS + (long long)(o - nf) * g.modes) + (long long)line * H;
-                const bool wr = act && valid;
+        for (int r = 0; r < 16; ++r) v[r] = slots[ix(j + r * P)];
+        __syncthreads();   // all loads precede the first exchange write
+        fft_reg<C, L, -1>(v, slots, ix, j, tw, N / L);
+        {
+            // the partners Z[M-k] by warp shuffle, X[k] straight out
+            C *dst = QV + (long long)grp * g.modes + (long long)line * H;
 #pragma unroll
-                for (int q = 0; q < RP::NBL; ++q)
+            for (int q = 0; q < RP::NBL; ++q)
 #pragma unroll
-                    for (int r = 0; r < RP::RL; ++r) {
-                        const int k = RP::out(j, q, r);
-                        const C zk = v[q * RP::RL + r];
-                        const C zc = partner_out<C, M>(v, j, q, r);
-                        const C ev = cscale(cadd(zk, zc), T(0.5));
-                        const C dd = cscale(csub(zk, zc), T(0.5));
-                        const C od = mk<T>(dd.y, -dd.x);
-                        const C w = __ldg(&tw[k]);
-                        if (wr) dst[k] = cadd(ev, cmul(w, od));
-                    }
-                if (wr && j == 0) {   // X[M] = Re Z[0] - Im Z[0]
-                    const C z0 = v[0];
-                    dst[M] = mk<T>(z0.x - z0.y, T(0));
+                for (int r = 0; r < RP::RL; ++r) {
+                    const int k = RP::out(j, q, r);
+                    const C zk = v[q * RP::RL + r];
+                    const C zc = partner_out<C, M>(v, j, q, r);
+                    const C ev = cscale(cadd(zk, zc), T(0.5));
+                    const C dd = cscale(csub(zk, zc), T(0.5));
+                    const C od = mk<T>(dd.y, -dd.x);
+                    const C w = __ldg(&tw[k]);
+                    if (valid) dst[k] = cadd(ev, cmul(w, od));
                 }
+            if (valid && j == 0) {   // X[M] = Re Z[0] - Im Z[0]
+                const C z0 = v[0];
+                dst[M] = mk<T>(z0.x - z0.y, T(0));
             }
-            __syncthreads();   // the transform's last exchange read precedes the next writes
         }
+        __syncthreads();   // the transform's last exchange read precedes the next writes
     }
-    if (STAGED) cp_async_wait_all();
+    cp_async_wait_all();
+#pragma unroll
+    for (int i = 0; i < kMaxTerms; ++i) pot_d[i] += (double)pot_t[i];
     block_reduce_store_t<double, kMaxTerms>(pot_d, partV, gridDim.x, blockIdx.x);
 }
 
@@ -713,10 +649,12 @@ __global__ void __launch_bounds__(256, 3) kr_zpass_gw(Geo g, const cplx<T> *__re
     ModelG<T> mdl;
     mdl.kind = g.model;
     mdl.gsq = (T)g.gsq;
-    // <V> partial sums: a tile's sites in the field precision, the tiles of a persistent
-    // block in FP64 (thousands of tiles per block at N = 1024)
+    // <V> partial sums: up to 16 tiles' sites in the field precision, then folded into
+    // FP64 (a persistent block walks thousands of tiles at N = 1024; a fold per tile
+    // would put a conversion and an add per thread and tile on the narrow FP64 pipe)
     T pot_t[kMaxTerms] = {T(0), T(0)};
     double pot_d[kMaxTerms] = {0.0, 0.0};
+    int nfold = 0;
     if (STAGED) prefetch(blockIdx.x);
     for (int tile = blockIdx.x; tile < ntiles; tile = STAGED ? tile + gridDim.x : ntiles) {
         const int line = tile * TL + t;
@@ -811,10 +749,12 @@ __global__ void __launch_bounds__(256, 3) kr_zpass_gw(Geo g, const cplx<T> *__re
 #pragma unroll
             for (int p = 0; p < 4; ++p) slots[p * slot_elems + e] = mk<T>(o[2 * p], o[2 * p + 1]);
         }
+        if ((++nfold & 15) == 0) {
 #pragma unroll
-        for (int i = 0; i < kMaxTerms; ++i) {
-            pot_d[i] += (double)pot_t[i];
-            pot_t[i] = T(0);
+            for (int i = 0; i < kMaxTerms; ++i) {
+                pot_d[i] += (double)pot_t[i];
+                pot_t[i] = T(0);
+            }
         }
         __syncthreads();
 
@@ -882,6 +822,8 @@ __global__ void __launch_bounds__(256, 3) kr_zpass_gw(Geo g, const cplx<T> *__re
         }
     }
     if (STAGED) cp_async_wait_all();
+#pragma unroll
+    for (int i = 0; i < kMaxTerms; ++i) pot_d[i] += (double)pot_t[i];
     block_reduce_store_t<double, kMaxTerms>(pot_d, partV, gridDim.x, blockIdx.x);
 }
 

@@ -41,7 +41,7 @@ struct RegLaunch {
         SETA((kr_fft_y<T, N>), sxy);
         SETA((kr_fft_x_final<T, N, false>), (int)cfg.smem_xf);
         SETA((kr_fft_x_final<T, N, true>), (int)cfg.smem_xf);
-        SETA((kr_zpass<T, M, false>), sz);
+        SETA((kr_zpass<T, M>), sz);
         SETA((kr_zpass_gw<T, N, sizeof(T) == 4>), sz);
         SETA((kr_z_c2r_real<T, M>), (int)((256 / (M / 16)) * ZIdx<M>::LS * sizeof(C)));
         {
@@ -88,8 +88,8 @@ struct RegLaunch {
             mark(1);
             kr_ifft_y<T, N, false><<<gx, txy, cfg.smem_xy, st>>>(g, TA, TB, TC, b.bg, tw);
             mark(2);
-            kr_zpass<T, M, false><<<dim3(cfg.nbz, 1, R), tz, cfg.smem_z, st>>>(g, TA, TB, TC, QV, QS, b.partV, b.bg, tw,
-                                                                             (T *)b.tape_fx);
+            kr_zpass<T, M><<<dim3(cfg.nbz, 1, R), tz, cfg.smem_z, st>>>(g, TA, QV, b.partV, b.bg, tw,
+                                                                      (T *)b.tape_fx);
         }
         mark(3);
         ArrList8 al{};
@@ -134,8 +134,8 @@ struct RegLaunch {
         const dim3 gx(cfg.nbx, g.nf);
         kr_ifft_x<T, N, false, false><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, fk, nullptr, TA, nullptr, b.bg, tw);
         kr_ifft_y<T, N, false><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, TA, nullptr, nullptr, b.bg, tw);
-        kr_zpass<T, M, false><<<dim3(cfg.nbz, 1, 1), cfg.thr_z, cfg.smem_z, st>>>(g, TA, nullptr, nullptr, QV, nullptr,
-                                                                                b.partV, b.bg, tw, (T *)nullptr);
+        kr_zpass<T, M><<<dim3(cfg.nbz, 1, 1), cfg.thr_z, cfg.smem_z, st>>>(g, TA, QV, b.partV, b.bg, tw,
+                                                                         (T *)nullptr);
         ArrList8 al{};
         for (int f = 0; f < g.nf; ++f) {
             al.rs[f] = g.fstride;
