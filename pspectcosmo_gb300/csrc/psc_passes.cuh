@@ -589,7 +589,7 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
 // transformed. Otherwise one tile per block, inputs read straight from global memory.
 // Shared memory: four slots of TL lines x LS complex, then (STAGED) the staging area.
 template <typename T, int L, bool STAGED>
-__global__ void __launch_bounds__(256, 3) kr_zpass_gw(Geo g, const cplx<T> *__restrict__ TA,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g, const cplx<T> *__restrict__ TA,
                                                      const cplx<T> *__restrict__ TB, const cplx<T> *__restrict__ TC,
                                                      cplx<T> *__restrict__ QV, cplx<T> *__restrict__ QS,
                                                      double *__restrict__ partV, const DevBG *__restrict__ bg,
