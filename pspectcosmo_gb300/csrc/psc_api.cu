@@ -151,9 +151,8 @@ int ensure_staging(psc_handle *h, size_t bytes) {
     return PSC_OK;
 }
 
-// out[i] = (To)in[i] for i < n on all host cores (the FP64 <-> FP32 conversion of the
-// state exchange is memory-bound; one thread converts ~1-2 GB/s)
-// host threads of the conversions: the CPUs this process may run on, at most 32
+// host threads of the download's FP32 -> FP64 widening (memory-bound; one thread
+// converts ~1-2 GB/s): the CPUs this process may run on, at most 32
 unsigned host_threads() {
     unsigned nt = 0;
 #ifdef __linux__
@@ -163,27 +162,6 @@ unsigned host_threads() {
     if (nt == 0) nt = std::thread::hardware_concurrency();
     if (nt == 0) nt = 1;
     return nt > 32 ? 32 : nt;
-}
-
-template <typename To, typename From>
-void convert_parallel(To *out, const From *in, size_t n) {
-    const size_t kMin = 1u << 20;
-    unsigned nt = host_threads();
-    if (n < kMin * 2 || nt == 1) {
-        for (size_t i = 0; i < n; ++i) out[i] = (To)in[i];
-        return;
-    }
-    if ((size_t)nt > n / kMin) nt = (unsigned)(n / kMin);
-    std::vector<std::thread> th;
-    th.reserve(nt);
-    const size_t chunk = (n + nt - 1) / nt;
-    for (unsigned t = 0; t < nt; ++t) {
-        const size_t b = t * chunk, e = std::min(n, b + chunk);
-        th.emplace_back([=] {
-            for (size_t i = b; i < e; ++i) out[i] = (To)in[i];
-        });
-    }
-    for (auto &x : th) x.join();
 }
 
 // out[i] = (float)in[i], round to nearest even: the host cast's rounding
