@@ -1064,7 +1064,11 @@ __global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_fft_x_adj
 // adjoint tensor components lambda_ab (LAM), then per site and field
 // T_a = 2 sum_b (1 + delta_ab) lambda_ab d_b f (the transpose of S_ab = 2 sum_f d_a f d_b f,
 // kernel_GW evolution.cpp:581-601) and the r2c of the 3 nf T_a into Tout.
-// nin = 3 nf + 6 inputs; one tile of TL lines per block.
+// Full-length transforms of real-line pairs, as in kr_zpass_gw: input pairs
+// (d_x f, d_y f) of each field, (d_z f_0, d_z f_1 or 0), (lambda_0, lambda_1),
+// (lambda_2, lambda_3), (lambda_4, lambda_5): nf + 4 pairs; output pairs: the 3 nf T_a
+// (field-major) two by two. One tile of TL lines per block; shared memory: nf + 4 slots
+// of TL lines x LS complex.
 template <typename T, int L>
 __global__ void __launch_bounds__(256) kr_zpass_adj_gw(Geo g, const cplx<T> *__restrict__ TA,
                                                      const cplx<T> *__restrict__ TB, const cplx<T> *__restrict__ TC,
@@ -1072,12 +1076,14 @@ __global__ void __launch_bounds__(256) kr_zpass_adj_gw(Geo g, const cplx<T> *__r
                                                      const cplx<T> *__restrict__ tw, int tl_shift) {
     using C = cplx<T>;
     using RP = RegPlan<L>;
-    constexpr int M = L, P = RP::P, LS = ZIdx<L>::LS;
+    constexpr int P = RP::P, LS = ZIdx<L>::LS, HL = L / 2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *slots = reinterpret_cast<C *>(smem_raw);
     const int TL = 1 << tl_shift, H = g.H, N = g.N;
     const int nf = g.nf;
-    const int nout = 3 * nf;
+    const int pin = nf + 4;          // input pairs
+    const int nreal = 3 * nf;        // output reals
+    const int pout = (nreal + 1) / 2;
     const int j = threadIdx.x % P;
     const int t = (threadIdx.x / P) & (TL - 1);
     const int grp = threadIdx.x / (P * TL);
@@ -1085,38 +1091,47 @@ __global__ void __launch_bounds__(256) kr_zpass_adj_gw(Geo g, const cplx<T> *__r
     const bool valid = line < g.lines_z;
     const size_t slot_elems = (size_t)TL * LS;
     const T inv_n3 = (T)(1.0 / (double)g.sites);
-    // input grp: fields' gradients first (fld = grp / 3, axis = grp % 3), then lambda_c
-    const bool isgrad = grp < 3 * nf;
-    const int fld = isgrad ? grp / 3 : 0, axis = isgrad ? grp % 3 : 0;
-    const C *src0 = isgrad ? ((axis == 0 ? TB : (axis == 1 ? TC : TA)) + (long long)fld * g.modes)
-                           : (LAM + (long long)(grp - 3 * nf) * g.modes);
+    const T kIR = (T)g.kIR;
+    const T fj = (T)j;
+    // this thread's pair: kind 0 (d_x f, d_y f) of field grp, 1 (d_z f_0, d_z f_1), 2 lambda
+    const int kind = grp < nf ? 0 : (grp == nf ? 1 : 2);
+    const C *srcA, *srcB;
+    if (kind == 0) {
+        srcA = TB + (long long)grp * g.modes;
+        srcB = TC + (long long)grp * g.modes;
+    } else if (kind == 1) {
+        srcA = TA;
+        srcB = nf > 1 ? TA + g.modes : nullptr;
+    } else {
+        const int c = 2 * (grp - nf - 1);
+        srcA = LAM + (long long)c * g.modes;
+        srcB = LAM + (long long)(c + 1) * g.modes;
+    }
     const ZIdx<L> ix{(int)(grp * slot_elems + t * LS)};
-    // 1. c2r along z (own elements from global memory, partners by shuffle)
+    C v[16];
+    // 1. two real c2r in one N-point transform
     {
-        C v[16], yv[16], xM = mk<T>(0, 0);
-        const C *src = src0 + (long long)line * H;
-#pragma unroll
-        for (int r = 0; r < 16; ++r) v[r] = valid ? src[j + r * P] : mk<T>(0, 0);
-        if (valid && j == 0) xM = src[M];
-        partners_in<C, M>(v, xM, j, yv);
-        const T kz_ir = (T)g.kIR;
+        const long long lo = (long long)line * H;
 #pragma unroll
         for (int r = 0; r < 16; ++r) {
-            const int k = j + r * P;
-            C x = v[r], y = yv[r];
-            if (isgrad && axis == 2) {   // d/dz: i k_z, Nyquist zeroed
-                const T kx = kz_ir * (T)k;
-                const T ky = (k == 0) ? T(0) : kz_ir * (T)(M - k);
-                x = mk<T>(-kx * x.y, kx * x.x);
-                y = mk<T>(-ky * y.y, ky * y.x);
+            const int n = j + r * P;
+            const int m = n <= HL ? n : L - n;
+            C a = mk<T>(0, 0), b = mk<T>(0, 0);
+            if (valid) {
+                a = srcA[lo + m];
+                if (srcB) b = srcB[lo + m];
+                if (kind == 1) {   // d/dz of both: i k_z, Nyquist zeroed
+                    const T fm = n <= HL ? fj + T(r * P) : T(L - r * P) - fj;
+                    const T kz = (m == HL) ? T(0) : kIR * fm;
+                    a = mk<T>(-kz * a.y, kz * a.x);
+                    b = mk<T>(-kz * b.y, kz * b.x);
+                }
+                if (m == 0 || m == HL) {
+                    a.y = T(0);
+                    b.y = T(0);
+                }
             }
-            y.y = -y.y;
-            if (k == 0) { x.y = T(0); y.y = T(0); }
-            const C s = cadd(x, y), d = csub(x, y);
-            C w = __ldg(&tw[k]);
-            w.y = -w.y;
-            const C td = cmul(w, d);
-            v[r] = mk<T>(s.x - td.y, s.y + td.x);
+            v[r] = (n <= HL) ? mk<T>(a.x - b.y, a.y + b.x) : mk<T>(a.x + b.y, b.x - a.y);
         }
         fft_reg<C, L, +1>(v, slots, ix, j, tw, N / L);
         __syncthreads();
@@ -1127,63 +1142,97 @@ __global__ void __launch_bounds__(256) kr_zpass_adj_gw(Geo g, const cplx<T> *__r
     }
     __syncthreads();
     // 2. T_a = 2 sum_b (1 + delta_ab) lambda_ab d_b f per field and site
-    for (int idx = threadIdx.x; idx < TL * M; idx += blockDim.x) {
-        const int tt = idx / M, m = idx - tt * M;
+    for (int idx = threadIdx.x; idx < TL * L; idx += blockDim.x) {
+        const int tt = idx / L, z = idx - tt * L;
         if (blockIdx.x * TL + tt >= g.lines_z) continue;
-        const int e = tt * LS + m + (m >> 4);
-        C lam[6];
+        const int e = tt * LS + z + (z >> 4);
+        T lam[6];
 #pragma unroll
-        for (int c = 0; c < 6; ++c) lam[c] = slots[(3 * nf + c) * slot_elems + e];
-        C dd[2][3];
+        for (int c = 0; c < 3; ++c) {
+            const C l = slots[(nf + 1 + c) * slot_elems + e];
+            lam[2 * c] = l.x;
+            lam[2 * c + 1] = l.y;
+        }
+        const C dz = slots[nf * slot_elems + e];
+        T d[2][3];
+#pragma unroll
+        for (int fl = 0; fl < 2; ++fl) {
+            if (fl < nf) {
+                const C dxy = slots[fl * slot_elems + e];
+                d[fl][0] = dxy.x;
+                d[fl][1] = dxy.y;
+                d[fl][2] = fl ? dz.y : dz.x;
+            } else {
+                d[fl][0] = d[fl][1] = d[fl][2] = T(0);
+            }
+        }
+        // symmetric index of (a, b): 00 0, 01 1, 02 2, 11 3, 12 4, 22 5
+        const int sy[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+        T o[6];
 #pragma unroll
         for (int fl = 0; fl < 2; ++fl)
 #pragma unroll
-            for (int b = 0; b < 3; ++b) dd[fl][b] = (fl < nf) ? slots[(fl * 3 + b) * slot_elems + e] : mk<T>(0, 0);
-        // symmetric index of (a, b): 00 0, 01 1, 02 2, 11 3, 12 4, 22 5
-        const int sy[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
-#pragma unroll
-        for (int fl = 0; fl < 2; ++fl) {
-            if (fl >= nf) break;
-#pragma unroll
             for (int a = 0; a < 3; ++a) {
-                C o = mk<T>(0, 0);
+                T acc = T(0);
 #pragma unroll
-                for (int b = 0; b < 3; ++b) {
-                    const T c2 = (a == b) ? T(4) : T(2);
-                    const C l = lam[sy[a][b]], d = dd[fl][b];
-                    o.x += c2 * l.x * d.x;   // sites 2m (x) and 2m+1 (y) separately
-                    o.y += c2 * l.y * d.y;
-                }
-                slots[(fl * 3 + a) * slot_elems + e] = o;
+                for (int b2 = 0; b2 < 3; ++b2) acc += ((a == b2) ? T(4) : T(2)) * lam[sy[a][b2]] * d[fl][b2];
+                o[fl * 3 + a] = acc;
             }
-        }
+        if (nf == 1) o[3] = T(0);
+#pragma unroll
+        for (int p = 0; p < 3; ++p)
+            if (p < pout) slots[p * slot_elems + e] = mk<T>(o[2 * p], o[2 * p + 1]);
     }
     __syncthreads();
-    // 3. r2c along z of the 3 nf T_a (groups >= nout only keep the barriers)
+    // 3. two real r2c per N-point forward transform of output pair grp (groups >= pout
+    //    only keep the barriers)
     {
-        const bool act = grp < nout;
+        const bool act = grp < pout;
         const ZIdx<L> ixo{(int)((act ? grp : 0) * slot_elems + t * LS)};
-        C v[16];
 #pragma unroll
         for (int r = 0; r < 16; ++r) v[r] = act ? slots[ixo(j + r * P)] : mk<T>(0, 0);
         __syncthreads();
         fft_reg<C, L, -1>(v, slots, ixo, j, tw, N / L, act);
-        C *dst = Tout + (long long)(act ? grp : 0) * g.modes + (long long)line * H;
+        const int r0 = 2 * grp, r1 = 2 * grp + 1;
         const bool wr = act && valid;
+        C *d0 = wr ? Tout + (long long)r0 * g.modes + (long long)line * H : nullptr;
+        C *d1 = (wr && r1 < nreal) ? Tout + (long long)r1 * g.modes + (long long)line * H : nullptr;
+        if constexpr (P <= 32) {
 #pragma unroll
-        for (int q = 0; q < RP::NBL; ++q)
+            for (int q = 0; q < RP::NBL; ++q)
 #pragma unroll
-            for (int r = 0; r < RP::RL; ++r) {
-                const int k = RP::out(j, q, r);
-                const C zk = v[q * RP::RL + r];
-                const C zc = partner_out<C, M>(v, j, q, r);
-                const C ev = cscale(cadd(zk, zc), T(0.5));
-                const C dq = cscale(csub(zk, zc), T(0.5));
-                const C od = mk<T>(dq.y, -dq.x);
-                const C w = __ldg(&tw[k]);
-                if (wr) dst[k] = cadd(ev, cmul(w, od));
+                for (int r = 0; r < RP::RL; ++r) {
+                    if (RP::out(0, q, r) > HL) continue;   // no lane holds a written k
+                    const int k = RP::out(j, q, r);
+                    const C zk = v[q * RP::RL + r];
+                    const C zc = partner_out<C, L>(v, j, q, r);   // conj Z[N - k]
+                    if (wr && k <= HL) {
+                        const C ev = cscale(cadd(zk, zc), T(0.5));
+                        const C dd = cscale(csub(zk, zc), T(0.5));
+                        d0[k] = ev;
+                        if (d1) d1[k] = mk<T>(dd.y, -dd.x);
+                    }
+                }
+        } else {
+            // a line's lanes span two warps: Z through its slot, then the split from there
+            __syncthreads();
+            if (act) {
+#pragma unroll
+                for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+                    for (int r = 0; r < RP::RL; ++r) slots[ixo(RP::out(j, q, r))] = v[q * RP::RL + r];
             }
-        if (wr && j == 0) dst[M] = mk<T>(v[0].x - v[0].y, T(0));
+            __syncthreads();
+            if (wr) {
+                for (int k = j; k <= HL; k += P) {
+                    const C zk = slots[ixo(k)], zc = cconj(slots[ixo((L - k) & (L - 1))]);
+                    const C ev = cscale(cadd(zk, zc), T(0.5));
+                    const C dd = cscale(csub(zk, zc), T(0.5));
+                    d0[k] = ev;
+                    if (d1) d1[k] = mk<T>(dd.y, -dd.x);
+                }
+            }
+        }
     }
 }
 

@@ -55,7 +55,7 @@ struct RegLaunch {
         {
             int tl = 1, sh = 0;
             gw_adj_tile(cfg.g.nf, &tl, &sh);
-            SETA((kr_zpass_adj_gw<T, M>), (int)((3 * cfg.g.nf + 6) * tl * ZIdx<M>::LS * sizeof(C)));
+            SETA((kr_zpass_adj_gw<T, N>), (int)((cfg.g.nf + 4) * tl * ZIdx<N>::LS * sizeof(C)));
         }
 #undef SETA
         return cudaSuccess;
@@ -209,9 +209,9 @@ struct RegLaunch {
         kr_ifft_y<T, N, false><<<g6, cfg.thr_xy, cfg.smem_xy, st>>>(g, QS, nullptr, nullptr, b.bg, tw);
         int tl = 1, sh = 0;
         gw_adj_tile(g.nf, &tl, &sh);
-        const int nin = 3 * g.nf + 6, P = M / 16;
-        const size_t smem = (size_t)nin * tl * ZIdx<M>::LS * sizeof(C);
-        kr_zpass_adj_gw<T, M><<<(g.lines_z + tl - 1) / tl, nin * P * tl, smem, st>>>(g, TA, TB, TC, QS, (C *)Tarr, tw,
+        const int pin = g.nf + 4, P = N / 16;
+        const size_t smem = (size_t)pin * tl * ZIdx<N>::LS * sizeof(C);
+        kr_zpass_adj_gw<T, N><<<(g.lines_z + tl - 1) / tl, pin * P * tl, smem, st>>>(g, TA, TB, TC, QS, (C *)Tarr, tw,
                                                                                     sh);
         ArrList8 al{};
         for (int i = 0; i < 3 * g.nf; ++i) al.p[i] = (C *)Tarr + (long long)i * g.modes;
@@ -221,12 +221,12 @@ struct RegLaunch {
     }
 };
 
-// the GW adjoint Z pass: 3 nf + 6 inputs of P = N/32 threads each per line
+// the GW adjoint Z pass: nf + 4 input pairs of P = N/16 threads each per line
 template <typename T, int N>
 void RegLaunch<T, N>::gw_adj_tile(int nf, int *tl, int *sh) {
-    const int nin = 3 * nf + 6, P = (N / 2) / 16;
+    const int pin = nf + 4, P = N / 16;
     int t = 1;
-    while (nin * P * t * 2 <= 256) t *= 2;
+    while (pin * P * t * 2 <= 256) t *= 2;
     int s = 0;
     while ((1 << s) < t) ++s;
     *tl = t;
