@@ -198,6 +198,29 @@ def test_gw_register_engine(oracle_mod, N, precision):
         _compare_state(lat, o, p, FP32_FIELD_TOL, FP32_BG_TOL, FP32_ADD_TOL)
 
 
+@pytest.mark.parametrize("precision", [64, 32])
+def test_gw_single_field(oracle_mod, precision):
+    """One field with GWs (the shipped phi^2 model, real-space step): the GW Z pass's
+    single-field layout (two input pairs, the seven products in four output pairs, the last
+    half empty) against the oracle."""
+    from pspectcosmo_gb300 import Lattice
+    from pspectcosmo_gb300.params import Params
+
+    p = Params.reference_default(N=32, vv=2, spectral=0, with_gw=1, precision=precision)
+    q = p.copy()
+    q.precision = 64
+    o = oracle_mod.Oracle(q)
+    o.init_ic()
+    lat = Lattice(p)
+    lat.initialize()
+    lat.evolve(0.002, 3)
+    o.step(0.002, 3)
+    if precision == 64:
+        _compare_state(lat, o, p, 1e-10, 1e-12)
+    else:
+        _compare_state(lat, o, p, FP32_FIELD_TOL, FP32_BG_TOL, FP32_ADD_TOL)
+
+
 def test_nonfinite_state_is_reported():
     """A NaN planted in host-side initial data is caught by the device finite check."""
     from pspectcosmo_gb300 import Lattice, PscError
