@@ -94,8 +94,11 @@ void psc_destroy(psc_handle *h);
 
 /* Initial conditions with the reference's RNG stream and mode order
  * (initialize.cpp:562-810 and, with GWs, initialize_GW initialize.cpp:341-470).
- * Generates on the host in FP64, uploads, and computes a'' as
- * kernel_a_k_nopad / kernel_a (evolution.cpp:1061, 421). */
+ * Generated on the device, one thread per mode, each thread reaching its draws of the
+ * Park-Miller stream by skip-ahead (the integer draws are the reference's exactly);
+ * seed < 1 (constant draws) and an initial low-pass cut (kcutoff) use the FP64 host
+ * generator of psc_generate_ic and upload. Then a'' as kernel_a_k_nopad / kernel_a
+ * (evolution.cpp:1061, 421). */
 int psc_init_ic(psc_handle *h);
 
 /* Host-only initial conditions: fills f_k, pi_k (nflds blocks) and, with GWs,
