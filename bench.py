@@ -343,6 +343,24 @@ def run_adjoint(args):
         dist.destroy_process_group()
 
 
+def pinned_state(st):
+    """Copies of the host state's arrays in pinned (page-locked) host memory, and pinned
+    output arrays of the same shapes for get_state(out=...); (None, None) without CUDA."""
+    import numpy as np
+    import torch
+
+    if not torch.cuda.is_available():
+        return None, None
+    keys = [k for k in ("f_k", "pi_k", "u_k", "pi_u_k") if st[k] is not None]
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    src = dict(st)
+    out = {}
+    for k in keys:
+        src[k] = pin(st[k])
+        out[k] = pin(np.empty_like(st[k]))
+    return src, out
+
+
 def fft_yardstick(lat, p, reps: int = 10):
     """The library's 3-D c2r (X, Y inverse passes and the Z c2r pass) of the field arrays
     beside cuFFT's (torch.fft.irfftn, complex64 -> float32) on the same half spectra: device
@@ -426,26 +444,34 @@ def run_ours(args):
 
     e2e = None
     if not big:
-        # median of three repetitions: the host side (first touch of the returned arrays,
-        # host memory traffic of the FP64 <-> FP32 conversion) varies by +-20 % run to run
-        reps = []
-        for _ in range(3):
-            barrier(dist)
-            t0 = time.perf_counter()
-            lat.set_state(st0["f_k"], st0["pi_k"], st0["a"], st0["ad"], st0["add"], st0["u_k"], st0["pi_u_k"])
-            for _ in range(args.steps):
-                lat.evolve(dt, 1)
-                lat.background()
-            out = lat.get_state()
-            reps.append(max_over_ranks(dist, time.perf_counter() - t0))
-            del out
-        e2e_s = sorted(reps)[1]
+        # the host state in pinned memory (input and output buffers, allocated once), and
+        # for comparison in ordinary pageable numpy arrays with fresh output arrays per call;
+        # each the median of three repetitions (the host side varies by +-20 % run to run)
+        def e2e_run(src, out=None):
+            reps = []
+            for _ in range(3):
+                barrier(dist)
+                t0 = time.perf_counter()
+                lat.set_state(src["f_k"], src["pi_k"], src["a"], src["ad"], src["add"], src["u_k"], src["pi_u_k"])
+                for _ in range(args.steps):
+                    lat.evolve(dt, 1)
+                    lat.background()
+                res = lat.get_state(out=out)
+                reps.append(max_over_ranks(dist, time.perf_counter() - t0))
+                del res
+            return sorted(reps)[1], reps
+
+        pinned, pinned_out = pinned_state(st0)
+        e2e_s, reps = e2e_run(pinned if pinned is not None else st0, pinned_out)
+        e2e_pg, reps_pg = e2e_run(st0)
         state_arrays = 2 * p.nflds + (12 if p.with_gw else 0)
         state_bytes_host = state_arrays * p.modes * 16   # host buffers are FP64 complex
         e2e = {"value": world * p.sites * args.steps / e2e_s, "unit": "site-steps/s",
                "h2d_bytes_per_step": state_bytes_host / args.steps + 8,
                "d2h_bytes_per_step": state_bytes_host / args.steps + 3 * 8 + 4 + 8,
-               "timing": "median of 3 repetitions", "repetitions_s": reps}
+               "host_buffers": "pinned" if pinned is not None else "pageable (pinning unavailable)",
+               "timing": "median of 3 repetitions", "repetitions_s": reps,
+               "pageable_host_value": world * p.sites * args.steps / e2e_pg, "pageable_repetitions_s": reps_pg}
 
     # per-pass device times and roofline of the dominant pass
     passes = lat.time_passes(reps=10)

@@ -242,13 +242,27 @@ class Lattice:
         _check(self._L.psc_set_state_padded(self._h, int(Nsrc), _dp(f_k), _dp(pi_k), a, ad, add, _dp(u_k),
                                             _dp(pi_u_k)), "psc_set_state_padded")
 
-    def get_state(self):
+    def get_state(self, out: dict | None = None):
+        """The state (psc_get_state). `out` (optional): caller-owned arrays f_k, pi_k and,
+        with GWs, u_k, pi_u_k, C-contiguous complex128 of the returned shapes (e.g. in
+        pinned host memory, reused across calls); they are filled and returned."""
         p = self.p
-        # psc_get_state writes every element (no zero fill needed)
-        f = np.empty((p.nflds, p.modes), np.complex128)
-        pi = np.empty((p.nflds, p.modes), np.complex128)
-        u = np.empty((6, p.modes), np.complex128) if p.with_gw else None
-        pu = np.empty((6, p.modes), np.complex128) if p.with_gw else None
+        shapes = dict(f_k=(p.nflds, p.modes), pi_k=(p.nflds, p.modes), u_k=(6, p.modes), pi_u_k=(6, p.modes))
+        if out is not None:
+            for k in ("f_k", "pi_k") + (("u_k", "pi_u_k") if p.with_gw else ()):
+                x = out[k]
+                if (not isinstance(x, np.ndarray) or x.dtype != np.complex128 or x.shape != shapes[k]
+                        or not x.flags.c_contiguous or not x.flags.writeable):
+                    raise ValueError(f"out[{k!r}] must be a writeable C-contiguous complex128 array of shape "
+                                     f"{shapes[k]}")
+            f, pi = out["f_k"], out["pi_k"]
+            u, pu = (out["u_k"], out["pi_u_k"]) if p.with_gw else (None, None)
+        else:
+            # psc_get_state writes every element (no zero fill needed)
+            f = np.empty(shapes["f_k"], np.complex128)
+            pi = np.empty(shapes["pi_k"], np.complex128)
+            u = np.empty(shapes["u_k"], np.complex128) if p.with_gw else None
+            pu = np.empty(shapes["pi_u_k"], np.complex128) if p.with_gw else None
         a, ad, add = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
         _check(self._L.psc_get_state(self._h, _dp(f), _dp(pi), ctypes.byref(a), ctypes.byref(ad), ctypes.byref(add),
                                      _dp(u), _dp(pu)), "psc_get_state")

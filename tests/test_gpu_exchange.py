@@ -1,7 +1,8 @@
 """State exchange through the C ABI (psc_set_state / psc_get_state) at the benchmark's size.
 
 The FP32 upload copies the caller's FP64 arrays through a 16 Mi-double device scratch and
-rounds on the device; the download copies in up to 16 chunks and widens on the host cores.
+rounds on the device; the download copies in up to 16 chunks and widens on the host cores,
+or, into page-locked buffers, widens on the device and copies the FP64 values straight in.
 At 256^3 with GWs every array group spans several chunks of both. A round trip must give
 exactly the FP32 rounding of the input (round to nearest even, as a host cast), and an FP64
 lattice must return its input unchanged."""
@@ -35,3 +36,25 @@ def test_round_trip_is_the_fp32_rounding(N, precision):
         want = st[k] if precision == 64 else st[k].astype(np.complex64).astype(np.complex128)
         g, w = got[k].view(np.float64), want.view(np.float64)
         assert np.array_equal(g, w, equal_nan=True), k
+    # into caller-owned buffers (get_state(out=...)): the same values, the same arrays back
+    out = {k: np.full_like(got[k], np.nan) for k in ("f_k", "pi_k", "u_k", "pi_u_k")}
+    got2 = lat.get_state(out=out)
+    for k in out:
+        assert got2[k] is out[k]
+        assert np.array_equal(out[k].view(np.float64), got[k].view(np.float64), equal_nan=True), k
+    with pytest.raises(ValueError):
+        lat.get_state(out=dict(out, f_k=np.empty((p.nflds, p.modes), np.complex64)))
+    # page-locked buffers (widened on the device, copied straight in) and a page-locked
+    # source: the same values
+    import torch
+
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    outp = {k: pin(np.full_like(got[k], np.nan)) for k in out}
+    lat.get_state(out=outp)
+    for k in outp:
+        assert np.array_equal(outp[k].view(np.float64), got[k].view(np.float64), equal_nan=True), k
+    src = {k: pin(st[k]) for k in st}
+    lat.set_state(src["f_k"], src["pi_k"], 1.25, 0.5, -0.125, src["u_k"], src["pi_u_k"])
+    lat.get_state(out=outp)
+    for k in outp:
+        assert np.array_equal(outp[k].view(np.float64), got[k].view(np.float64), equal_nan=True), k
