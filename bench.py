@@ -13,9 +13,10 @@ conditions (seed 1), generated on the host. Every array is larger than the 129 M
                   [--precision 32|64]
 
 One JSON line (rank 0). `value` is device-timed whole-job site-steps/s (inputs resident
-in HBM); `e2e` is the same metric through the C ABI with host buffers, the state copied
-host->device before the steps and device->host after them, and the background read
-back after every step. `--impl reference` times the CPU restatement of the reference's
+in HBM); `e2e` is the same metric through the C ABI with host buffers in pinned memory,
+the state copied host->device before the steps and device->host after them, and the
+background read back after every step (`pageable_host_value`: the same from ordinary
+numpy arrays). `--impl reference` times the CPU restatement of the reference's
 FP64 path (oracle/port) on this machine's host cores.
 Multi-GPU: independent replicas, one lattice per rank (the path does not shard); the
 timed region is bracketed by barriers and the max over ranks is reported.
