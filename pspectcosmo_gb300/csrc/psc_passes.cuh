@@ -4,10 +4,13 @@
 //
 // Thread layout of the X/Y passes (strided lines): TL lines x P = L/16 threads,
 // t fastest, so each of a thread's 16 loads is one coalesced TL-wide row.
-// Thread layout of the Z pass (contiguous lines): (input, line, j) with j
+// Thread layout of the Z passes (contiguous lines): (input, line, j) with j
 // fastest, so consecutive threads read consecutive kz of one line; all inputs
 // of a tile are transformed at the same time and meet in shared memory for the
-// pointwise epilogue.
+// pointwise epilogue. Without GWs an input is one field's line, transformed by
+// half-length packing (kr_zpass); with GWs an input is a pair of real lines
+// carried as one complex line through a full-length transform (kr_zpass_gw, and
+// the adjoint's kr_zpass_adj_gw).
 #pragma once
 
 #include "psc_fftreg.cuh"
