@@ -264,7 +264,7 @@ int psc_time_c2r(psc_handle *h, int reps, float *ms);
 int psc_pass_bytes(psc_handle *h, double *bytes);
 
 /* ---------------------------------------------------------------- batches
- * Ensembles of independent realizations (BASELINE's batched configuration). The
+ * Ensembles of independent realizations (the batched-ensemble workload). The
  * reference runs one lattice per process; these entry points have no single
  * counterpart and compose the ones above. psc_batch_create groups the n
  * realizations by configuration (all psc_params fields except seed, initfield,

@@ -1,7 +1,7 @@
 """CUDA path (libpsc.so through its C ABI) against the FP64 oracle.
 
 FP64 device path: the plain method; it must match the oracle to 1e-10 relative in the
-fields after the runs below (the spec bar for FP64) and bit for bit in the
+fields after the runs below (the FP64 parity bar) and bit for bit in the
 spectrum bin counts. Spectra of the real-space (GW) path are compared at 1e-7: the
 reference keeps phi0 + dphi(x) in real space there, so its fluctuation spectra carry a
 rounding floor of ~eps * phi0 / dphi ~ 1e-9 per step that the k-space state does not
@@ -126,7 +126,7 @@ def test_fp64_1000_steps_64cubed(oracle_mod):
 
 
 def test_fp64_shipped_dt_background_track(oracle_mod):
-    """The shipped configuration at the BASELINE dt = 0.002 (unstable at the start):
+    """The shipped configuration at dt = 0.002 (unstable at the start):
     a(t) and a'(t) follow the reference's golden track over 1000 steps."""
     from pspectcosmo_gb300 import Lattice
 
@@ -178,8 +178,8 @@ def test_other_lattice_sizes_fp64(oracle_mod, N):
 @pytest.mark.parametrize("precision", [64, 32])
 @pytest.mark.parametrize("N", [32, 64])
 def test_gw_register_engine(oracle_mod, N, precision):
-    """The register-engine passes with GWs (N >= 32: z lines of 16 and 32 points, two
-    different last-stage radices) against the oracle's real-space GW step."""
+    """The register-engine passes with GWs (N >= 32: full-length z transforms of 32 and 64
+    points, two different last-stage radices) against the oracle's real-space GW step."""
     from pspectcosmo_gb300 import Lattice
     from pspectcosmo_gb300.params import Params
 
