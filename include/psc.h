@@ -263,6 +263,14 @@ int psc_time_c2r(psc_handle *h, int reps, float *ms);
  * of the arrays it must read and write once), for roofline accounting. */
 int psc_pass_bytes(psc_handle *h, double *bytes);
 
+/* Failure detection of the device-side waits (no reference counterpart). The GW Z pass
+ * waits for its bulk copies (TMA) on an mbarrier for at most one second of wall time; a
+ * wait that runs out makes psc_step return PSC_ERR_TIMEOUT and leaves the context usable.
+ * This self-test runs that bounded wait on an mbarrier whose transactions never arrive, for
+ * limit_ms milliseconds (0 < limit_ms <= 10000), and stores the kernel's status in *status:
+ * PSC_ERR_TIMEOUT when the wait ran out as designed. */
+int psc_selftest_bulk_wait(double limit_ms, int *status);
+
 /* ---------------------------------------------------------------- batches
  * Ensembles of independent realizations (the batched-ensemble workload). The
  * reference runs one lattice per process; these entry points have no single

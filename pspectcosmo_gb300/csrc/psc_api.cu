@@ -25,6 +25,7 @@
 
 #include "../../include/psc.h"
 #include "psc_bg.h"
+#include "psc_dev.cuh"
 #include "psc_ic.h"
 #include "psc_launch.h"
 
@@ -707,6 +708,7 @@ int step(psc_handle *h, double dt, int nsteps) {
     CU(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
     h->diag_valid = true;
     h->force_valid = false;
+    if (err == PSC_ERR_TIMEOUT) return fail(err, "a bulk copy's bounded wait ran out during the step");
     if (err) return fail(err, "non-finite background (NaN/Inf in a, a' or a'') during the step");
     h->force_valid = h->b.Fk != nullptr;
     return PSC_OK;
@@ -1063,6 +1065,42 @@ int psc_time_passes(psc_handle *h, int reps, float *ms) {
     return PSC_OK;
 }
 
+// the bounded wait of the bulk-copy staging on an mbarrier whose transactions never
+// arrive: thread 0 expects 16 bytes that no copy delivers
+__global__ void k_bulk_wait_selftest(int *out, unsigned long long limit_ns) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        psc::mbar_init(&bar, 1);
+        psc::mbar_fence_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) psc::mbar_arrive_expect_tx(&bar, 16);
+    const bool ok = psc::mbar_wait_bounded(&bar, 0, limit_ns);
+    if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) out[0] = PSC_ERR_TIMEOUT;
+        return;
+    }
+    if (threadIdx.x == 0) out[0] = PSC_OK;
+}
+
+int psc_selftest_bulk_wait(double limit_ms, int *status) {
+    if (!status || !(limit_ms > 0.0) || limit_ms > 10000.0) return fail(PSC_ERR_ARG, "bad argument");
+    int *d = nullptr;
+    CU(cudaMalloc(&d, sizeof(int)));
+    int v = PSC_ERR_STATE;
+    cudaError_t e = cudaMemcpy(d, &v, sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        k_bulk_wait_selftest<<<1, 64>>>(d, (unsigned long long)(limit_ms * 1e6));
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(&v, d, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(PSC_ERR_CUDA, std::string("wait self-test: ") + cudaGetErrorString(e));
+    *status = v;
+    return PSC_OK;
+}
+
 int psc_pass_bytes(psc_handle *h, double *bytes) {
     if (!h || !bytes) return fail(PSC_ERR_ARG, "bad argument");
     const psc::Geo &g = h->cfg.g;
@@ -1215,6 +1253,7 @@ int psc_batch_step(psc_batch *b, double dt, int nsteps) {
     for (psc_handle *h : b->groups) {
         h->diag_valid = true;
         const int err = read_err(h);
+        if (err == PSC_ERR_TIMEOUT) return fail(err, "a bulk copy's bounded wait ran out in a realization of the batch");
         if (err) return fail(err, "non-finite background in a realization of the batch");
     }
     return PSC_OK;

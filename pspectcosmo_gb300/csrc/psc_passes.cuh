@@ -595,13 +595,13 @@ template <typename T, int L, bool STAGED>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g, const cplx<T> *__restrict__ TA,
                                                      const cplx<T> *__restrict__ TB, const cplx<T> *__restrict__ TC,
                                                      cplx<T> *__restrict__ QV, cplx<T> *__restrict__ QS,
-                                                     double *__restrict__ partV, const DevBG *__restrict__ bg,
+                                                     double *__restrict__ partV, const DevBG *bg,
                                                      const cplx<T> *__restrict__ tw, T *__restrict__ tape_fx) {
     using C = cplx<T>;
     using RP = RegPlan<L>;
     constexpr int P = RP::P, LS = ZIdx<L>::LS, HL = L / 2;
-    constexpr int HS = HL + 2;   // staging stride of one input line (H = N/2 + 1 entries)
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ uint64_t zbar;   // completion of a tile's bulk copies
     C *slots = reinterpret_cast<C *>(smem_raw);
     {
         const long long rf = (long long)blockIdx.z * g.fstride, rg = (long long)blockIdx.z * g.gstride;
@@ -620,20 +620,46 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
     const int t = (threadIdx.x / P) & (TL - 1);
     const int grp = threadIdx.x / (P * TL);         // this thread's input pair in phase 1
     const size_t slot_elems = (size_t)TL * LS;
-    // staging (STAGED): the next tile's input lines, [field][TA, TB, TC][line][HS]
+    // staging (STAGED): the next tile's input lines, [field][TA, TB, TC][line][hs]. The TL
+    // lines of one array in a tile are contiguous in global memory; when that run is a
+    // multiple of 16 bytes (TL even in FP32) it is one bulk copy by the tensor memory
+    // accelerator (line stride hs = H), otherwise warps copy it by cp.async (hs = H + 1).
     C *stage = slots + 4 * slot_elems;
+    const bool bulk = STAGED && ((size_t)TL * H * sizeof(C)) % 16 == 0;
+    const int hs = bulk ? H : H + 1;
     const T inv_n3 = (T)bg->inv_n3;
     const T kIR = (T)bg->kIR;
     const T fj = (T)j;
     const int fld = grp >> 1, kind = grp & 1;
     const C *srcA = (kind ? TB : TA) + (long long)fld * g.modes;
     const C *srcB = TC + (long long)fld * g.modes;
-    const C *stA = stage + ((size_t)(fld * 3 + (kind ? 1 : 0)) * TL + t) * HS;
-    const C *stB = stage + ((size_t)(fld * 3 + 2) * TL + t) * HS;
+    const C *stA = stage + ((size_t)(fld * 3 + (kind ? 1 : 0)) * TL + t) * hs;
+    const C *stB = stage + ((size_t)(fld * 3 + 2) * TL + t) * hs;
     const int ntiles = (g.lines_z + TL - 1) / TL;
-    // copy the input lines of tile `tl` into the staging area: warp w takes the lines
-    // w, w + 8, ... of the nf x 3 x TL, its lanes consecutive entries of each
+    if (bulk && threadIdx.x == 0) {
+        mbar_init(&zbar, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    // copy the input lines of tile `tl` into the staging area. Bulk: thread 0 issues one
+    // copy per array (lines_z is a multiple of TL, so a tile never runs past the array).
+    // Otherwise warp w takes the lines w, w + 8, ... of the nf x 3 x TL, its lanes
+    // consecutive entries of each.
     auto prefetch = [&](int tl) {
+        if (bulk) {
+            if (threadIdx.x == 0 && tl < ntiles) {
+                const unsigned run = (unsigned)((size_t)TL * H * sizeof(C));
+                fence_proxy_async();   // the staging reads of the previous tile come first
+                mbar_arrive_expect_tx(&zbar, (unsigned)(nf * 3) * run);
+                for (int a = 0; a < nf * 3; ++a) {
+                    const int fl = a >= 3 ? 1 : 0, w = a - 3 * fl;
+                    const C *src = (w == 0 ? TA : (w == 1 ? TB : TC)) + (long long)fl * g.modes +
+                                   (long long)tl * TL * H;
+                    bulk_copy_g2s(stage + (size_t)a * TL * H, src, run, &zbar);
+                }
+            }
+            return;
+        }
         if (tl < ntiles) {
             const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
             const int nl = nf * 3 * TL;
@@ -643,7 +669,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
                 if (ln >= g.lines_z) continue;
                 const int fl = a >= 3 ? 1 : 0, w = a - 3 * fl;
                 const C *src = (w == 0 ? TA : (w == 1 ? TB : TC)) + (long long)fl * g.modes + ln * H;
-                C *dst = stage + (size_t)li * HS;
+                C *dst = stage + (size_t)li * hs;
                 for (int m = lane; m < H; m += 32) cp_async_elem(dst + m, src + m);
             }
         }
@@ -659,6 +685,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
     double pot_d[kMaxTerms] = {0.0, 0.0};
     int nfold = 0;
     if (STAGED) prefetch(blockIdx.x);
+    unsigned phase = 0;   // parity of the bulk-copy phase the next tile completes
     for (int tile = blockIdx.x; tile < ntiles; tile = STAGED ? tile + gridDim.x : ntiles) {
         const int line = tile * TL + t;
         const bool valid = line < g.lines_z;
@@ -667,7 +694,17 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
             // 1. two real c2r in one N-point transform
             const ZIdx<L> ix{(int)(grp * slot_elems + t * LS)};
             const long long lo = (long long)line * H;
-            if (STAGED) {
+            if (bulk) {
+                const bool ok = mbar_wait_bounded(&zbar, phase, kBulkWaitNs);
+                if (__syncthreads_or(!ok)) {
+                    // the copies did not complete in time: report it, give the copies in
+                    // flight one more bounded wait, and leave (the whole block together)
+                    if (threadIdx.x == 0) const_cast<DevBG *>(bg)->err = PSC_ERR_TIMEOUT;
+                    mbar_wait_bounded(&zbar, phase, kBulkWaitNs);
+                    return;
+                }
+                phase ^= 1u;
+            } else if (STAGED) {
                 cp_async_wait_all();
                 __syncthreads();   // every thread's copies of this tile have landed
             }
