@@ -46,6 +46,9 @@ extern "C" {
 #define PSC_ERR_STATE (-6)      /* call out of order (e.g. step before state is set) */
 #define PSC_ERR_NOMEM (-7)      /* device allocation failed */
 #define PSC_ERR_IO (-8)         /* a file could not be written */
+#define PSC_ERR_DEVICE (-9)     /* a bounded wait ran out and the copies it waited for never completed:
+                                   the CUDA context can no longer be trusted (destroy the handle and
+                                   do no further GPU work in this process) */
 
 #define PSC_MODEL_PHI2 0      /* V = phi^2/2 (reference model.h:35-99) */
 #define PSC_MODEL_PHI2CHI2 1  /* V = phi^2/2 + gsq phi^2 chi^2 / 2 (two-field preheating) */
@@ -264,12 +267,26 @@ int psc_time_c2r(psc_handle *h, int reps, float *ms);
 int psc_pass_bytes(psc_handle *h, double *bytes);
 
 /* Failure detection of the device-side waits (no reference counterpart). The GW Z pass
- * waits for its bulk copies (TMA) on an mbarrier for at most one second of wall time; a
- * wait that runs out makes psc_step return PSC_ERR_TIMEOUT and leaves the context usable.
+ * waits for its bulk copies (TMA) on an mbarrier for at most one second of wall time. When
+ * a wait runs out, the block records PSC_ERR_TIMEOUT and waits once more (bounded) for the
+ * copies still in flight, so that it never leaves while a copy can write into its shared
+ * memory. If they land, psc_step returns PSC_ERR_TIMEOUT and the context stays usable
+ * (psc_set_state / psc_init_ic / psc_checkpoint_read clear the handle's error). If they
+ * never land, psc_step returns PSC_ERR_DEVICE: the context can no longer be trusted. After
+ * a failure the rest of the step call does no work (no further waits).
  * This self-test runs that bounded wait on an mbarrier whose transactions never arrive, for
  * limit_ms milliseconds (0 < limit_ms <= 10000), and stores the kernel's status in *status:
  * PSC_ERR_TIMEOUT when the wait ran out as designed. */
 int psc_selftest_bulk_wait(double limit_ms, int *status);
+
+/* Test hook of the same waits on the real path. Sets the handle's wait limit to limit_ms
+ * (0 < limit_ms <= 10000; 1000 by default) and, with plant_bytes > 0 (at most 4096), makes
+ * every tile of the GW Z pass expect plant_bytes more than its copies deliver: the copies
+ * land, the wait runs out, the timeout path counts the planted bytes itself and the block
+ * leaves, so psc_step returns PSC_ERR_TIMEOUT. plant_bytes = 0 restores normal waits.
+ * PSC_ERR_CONFIG when plant_bytes > 0 and the handle's GW Z pass does not stage its tiles by
+ * bulk copies (FP32 GW runs with an even number of lines per tile do). */
+int psc_test_wait_hook(psc_handle *h, double limit_ms, int plant_bytes);
 
 /* ---------------------------------------------------------------- batches
  * Ensembles of independent realizations (the batched-ensemble workload). The
@@ -315,10 +332,12 @@ int psc_batch_write_snapshot(psc_batch *b, int idx, const char *path, int with_e
  * 50 KB, held by every GPU that loads the library until the process exits),
  * shared by all calls on a device: each call clears it first, so calls whose work
  * overlaps on the GPU (different streams or threads) race and must be serialised
- * by the caller. The first call on a device looks up that array's device address
- * (cudaGetSymbolAddress), so make it before any stream capture. Work is queued on
- * `stream` (a cudaStream_t; NULL = default stream) and is complete when the stream
- * is. Calls no cudaMalloc or cudaFree. */
+ * by the caller. Every call looks up that array's address on the current device
+ * (cudaGetSymbolAddress, which allocates nothing); the first call in a CUDA context also
+ * loads the library's device code there, so make it before any stream capture. Work is
+ * queued on `stream` (a cudaStream_t; NULL = default stream), which must belong to the
+ * current device (PSC_ERR_ARG otherwise), and is complete when the stream is. Calls no
+ * cudaMalloc or cudaFree. */
 #define PSC_NOALLOC_MAX_N 1024
 int psc_spectra_noalloc(const psc_params *p, double a, double ad, const void *f_k, const void *pi_k,
                         int32_t *numpoints, double *f2, double *pi2, double *n2, void *stream);

@@ -417,13 +417,25 @@ int build_graph(psc_handle *h) {
     return instantiate(h->st, enqueue_step(h, h->st), &h->gexec);
 }
 
+// the error word of the handle's realizations: PSC_ERR_DEVICE before any other code
 int read_err(psc_handle *h) {
     std::vector<psc::DevBG> bgs(h->R);
     CU(cudaMemcpyAsync(bgs.data(), h->b.bg, sizeof(psc::DevBG) * h->R, cudaMemcpyDeviceToHost, h->st));
     CU(cudaStreamSynchronize(h->st));
+    int err = 0;
     for (int r = 0; r < h->R; ++r)
-        if (bgs[r].err) return bgs[r].err;
-    return 0;
+        if (bgs[r].err && (!err || bgs[r].err == PSC_ERR_DEVICE)) err = bgs[r].err;
+    return err;
+}
+
+const char *step_err_msg(int err) {
+    switch (err) {
+    case PSC_ERR_TIMEOUT: return "a bulk copy's bounded wait ran out during the step (the copies then landed)";
+    case PSC_ERR_DEVICE:
+        return "a bulk copy's bounded wait ran out and the copies never completed: the CUDA context can no "
+               "longer be trusted";
+    default: return "non-finite background (NaN/Inf in a, a' or a'') during the step";
+    }
 }
 
 int create_handle(const psc_params *ps, int R, psc_handle **out) {
@@ -573,6 +585,7 @@ int create_handle(const psc_params *ps, int R, psc_handle **out) {
         bg.inv_n3 = 1.0 / (double)g.sites;
         bg.inv_n3sq = bg.inv_n3 * bg.inv_n3;
         bg.inv_nv = bg.inv_n3;
+        bg.wait_ns = psc::kBulkWaitNs;
         if (h->padded) {
             // <V> over the padded sites (kernel_a_k_pad, evolution.cpp:1624-1631)
             bg.nbz = h->cfgp.nbz;
@@ -708,8 +721,7 @@ int step(psc_handle *h, double dt, int nsteps) {
     CU(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
     h->diag_valid = true;
     h->force_valid = false;
-    if (err == PSC_ERR_TIMEOUT) return fail(err, "a bulk copy's bounded wait ran out during the step");
-    if (err) return fail(err, "non-finite background (NaN/Inf in a, a' or a'') during the step");
+    if (err) return fail(err, step_err_msg(err));
     h->force_valid = h->b.Fk != nullptr;
     return PSC_OK;
 }
@@ -1101,6 +1113,25 @@ int psc_selftest_bulk_wait(double limit_ms, int *status) {
     return PSC_OK;
 }
 
+int psc_test_wait_hook(psc_handle *h, double limit_ms, int plant_bytes) {
+    if (!h || !(limit_ms > 0.0) || limit_ms > 10000.0 || plant_bytes < 0 || plant_bytes > 4096)
+        return fail(PSC_ERR_ARG, "bad argument");
+    const psc::Geo &g = h->cfg.g;
+    const bool bulk = g.gw && g.reg && h->p0().precision == 32 &&
+                      ((size_t(1) << g.tlz_shift) * (size_t)g.H * h->csize) % 16 == 0;
+    if (plant_bytes && !bulk)
+        return fail(PSC_ERR_CONFIG, "the handle's GW Z pass does not stage its tiles by bulk copies");
+    for (int r = 0; r < h->R; ++r) {
+        psc::DevBG bg;
+        int rc;
+        if ((rc = read_bg(h, r, &bg))) return rc;
+        bg.wait_ns = (unsigned long long)(limit_ms * 1e6);
+        bg.wait_plant = plant_bytes;
+        if ((rc = write_bg(h, r, bg))) return rc;
+    }
+    return PSC_OK;
+}
+
 int psc_pass_bytes(psc_handle *h, double *bytes) {
     if (!h || !bytes) return fail(PSC_ERR_ARG, "bad argument");
     const psc::Geo &g = h->cfg.g;
@@ -1253,8 +1284,7 @@ int psc_batch_step(psc_batch *b, double dt, int nsteps) {
     for (psc_handle *h : b->groups) {
         h->diag_valid = true;
         const int err = read_err(h);
-        if (err == PSC_ERR_TIMEOUT) return fail(err, "a bulk copy's bounded wait ran out in a realization of the batch");
-        if (err) return fail(err, "non-finite background in a realization of the batch");
+        if (err) return fail(err, step_err_msg(err));
     }
     return PSC_OK;
 }
@@ -1321,6 +1351,7 @@ const char *psc_strerror(int code) {
     case PSC_ERR_CUDA: return "CUDA runtime error";
     case PSC_ERR_NONFINITE: return "non-finite background";
     case PSC_ERR_TIMEOUT: return "device-side wait timed out";
+    case PSC_ERR_DEVICE: return "device-side wait timed out with copies still outstanding (context unusable)";
     case PSC_ERR_STATE: return "call out of order";
     case PSC_ERR_NOMEM: return "out of device memory";
     case PSC_ERR_IO: return "file could not be written";

@@ -27,6 +27,11 @@ struct DevBG {
     double inv_nv;                  // 1 / (sites the <V> partials sum over): N^3, or N_pad^3 when padded
     int s, alpha, nf, nterms, mask, model, nbx, nbz;   // nbz: blocks of the <V> partials
     int stage, steps_left, err, pad;
+    // bounded device-side waits: the limit of one wait (1 s unless a test sets it), and a
+    // test hook: bytes a GW Z pass tile is told to expect that no copy delivers, so its
+    // wait runs out after the real copies have landed (0 = off)
+    unsigned long long wait_ns;
+    int wait_plant, pad2;
 };
 
 // Scalar state of the discrete adjoint (psc_adjoint.cu), resident in device memory

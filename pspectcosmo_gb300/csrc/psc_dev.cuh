@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "psc.h"
 #include "psc_bg.h"
 
 namespace psc {
@@ -258,9 +259,21 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity
         if (globaltimer_ns() - t0 > limit_ns) return false;
     }
 }
-// the limit of the waits on bulk copies: far above any copy's time, short enough that a
-// lost completion returns an error instead of holding the GPU
+// the default limit of the waits on bulk copies (DevBG::wait_ns): far above any copy's
+// time, short enough that a lost completion returns an error instead of holding the GPU
 constexpr unsigned long long kBulkWaitNs = 1000000000ull;
+// counts `bytes` of transactions as complete on bar's current phase, as an arriving copy does
+__device__ __forceinline__ void mbar_complete_tx(uint64_t *bar, unsigned bytes) {
+    asm volatile("mbarrier.complete_tx.relaxed.cta.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+// Error word of a device record: the first cause wins (a later failure does not overwrite
+// it), except that PSC_ERR_DEVICE, which says the context can no longer be trusted,
+// replaces a PSC_ERR_TIMEOUT.
+__device__ __forceinline__ void report_err(int *err, int code) {
+    const int old = atomicCAS(err, 0, code);
+    if (old == PSC_ERR_TIMEOUT && code == PSC_ERR_DEVICE) atomicCAS(err, PSC_ERR_TIMEOUT, code);
+}
 
 // ------------------------------------------------------------------ reductions
 // Block reduction of NV doubles; thread 0 stores out[i * stride + blockIdx.x].

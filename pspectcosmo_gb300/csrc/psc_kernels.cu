@@ -462,6 +462,9 @@ __global__ void __launch_bounds__(1024) k_scalar(DevBG *bg, const double *__rest
     bg += blockIdx.x;
     partKG += (size_t)blockIdx.x * pkg_stride;
     partV += (size_t)blockIdx.x * pv_stride;
+    // a failed step (a wait ran out, a non-finite background) keeps its background as the
+    // failure left it; evaluations of the state still run
+    if (bg->err && mode != SCALAR_EVAL && mode != SCALAR_EVAL_END) return;
     __shared__ double sums[NQ];
     const bool reduce = (mode == SCALAR_END || mode == SCALAR_EVAL_END);
     if (reduce) {
@@ -545,7 +548,7 @@ __global__ void __launch_bounds__(1024) k_scalar(DevBG *bg, const double *__rest
         V += v;
     }
     const double add_new = friedmann_add(bg, K, G, V);
-    if (!isfinite(add_new) || !isfinite(bg->a)) bg->err = PSC_ERR_NONFINITE;
+    if (!isfinite(add_new) || !isfinite(bg->a)) report_err(&bg->err, PSC_ERR_NONFINITE);
     if (mode == SCALAR_EVAL_END) {
         if (p == 0) bg->add = add_new;   // p == 1: diagnostics only, a'' kept as set by the caller
         return;
@@ -560,7 +563,7 @@ __global__ void __launch_bounds__(1024) k_scalar(DevBG *bg, const double *__rest
     bg->ad = bg->b;        // evolution.cpp:1196-1197
     bg->t += bg->dt;
     bg->steps_left -= 1;
-    if (!isfinite(bg->ad)) bg->err = PSC_ERR_NONFINITE;
+    if (!isfinite(bg->ad)) report_err(&bg->err, PSC_ERR_NONFINITE);
     if (bg->steps_left > 0) {
         bg->b = bg->ad;
         bg->ad_stale = bg->ad;

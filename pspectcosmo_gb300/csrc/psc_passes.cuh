@@ -613,6 +613,9 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
         partV += (size_t)blockIdx.z * g.pv_stride;
         bg += blockIdx.z;
     }
+    // a failed stage (an earlier wait ran out, or a non-finite background) leaves the rest
+    // of the step call without work: no further waits
+    if (bg->err) return;
     const int TL = 1 << g.tlz_shift, H = g.H, N = g.N;
     const int nf = g.nf;
     const int pin = 2 * nf;                         // input pairs of a line
@@ -636,6 +639,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
     const C *stA = stage + ((size_t)(fld * 3 + (kind ? 1 : 0)) * TL + t) * hs;
     const C *stB = stage + ((size_t)(fld * 3 + 2) * TL + t) * hs;
     const int ntiles = (g.lines_z + TL - 1) / TL;
+    const unsigned long long wait_ns = bg->wait_ns;
+    const unsigned plant = (unsigned)bg->wait_plant;   // test hook, 0 in normal runs
     if (bulk && threadIdx.x == 0) {
         mbar_init(&zbar, 1);
         mbar_fence_init();
@@ -650,7 +655,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
             if (threadIdx.x == 0 && tl < ntiles) {
                 const unsigned run = (unsigned)((size_t)TL * H * sizeof(C));
                 fence_proxy_async();   // the staging reads of the previous tile come first
-                mbar_arrive_expect_tx(&zbar, (unsigned)(nf * 3) * run);
+                mbar_arrive_expect_tx(&zbar, (unsigned)(nf * 3) * run + plant);
                 for (int a = 0; a < nf * 3; ++a) {
                     const int fl = a >= 3 ? 1 : 0, w = a - 3 * fl;
                     const C *src = (w == 0 ? TA : (w == 1 ? TB : TC)) + (long long)fl * g.modes +
@@ -695,12 +700,23 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
             const ZIdx<L> ix{(int)(grp * slot_elems + t * LS)};
             const long long lo = (long long)line * H;
             if (bulk) {
-                const bool ok = mbar_wait_bounded(&zbar, phase, kBulkWaitNs);
+                const bool ok = mbar_wait_bounded(&zbar, phase, wait_ns);
                 if (__syncthreads_or(!ok)) {
-                    // the copies did not complete in time: report it, give the copies in
-                    // flight one more bounded wait, and leave (the whole block together)
-                    if (threadIdx.x == 0) const_cast<DevBG *>(bg)->err = PSC_ERR_TIMEOUT;
-                    mbar_wait_bounded(&zbar, phase, kBulkWaitNs);
+                    // The tile's copies did not complete in time. Only this tile's copies can
+                    // be in flight (the next tile's are issued after this wait), and the block
+                    // must not leave while one of them can still write into its shared memory:
+                    // report the timeout, wait for them once more (bounded), and leave only
+                    // after they landed. If they never do, the copies may still write into
+                    // shared memory the SM gives to another block: PSC_ERR_DEVICE says the
+                    // context can no longer be trusted. With the test hook the planted bytes
+                    // are counted here, so the phase completes once the real copies have.
+                    int *err = &const_cast<DevBG *>(bg)->err;
+                    if (threadIdx.x == 0) {
+                        report_err(err, PSC_ERR_TIMEOUT);
+                        if (plant) mbar_complete_tx(&zbar, plant);
+                    }
+                    const bool landed = mbar_wait_bounded(&zbar, phase, wait_ns);
+                    if (__syncthreads_or(!landed) && threadIdx.x == 0) report_err(err, PSC_ERR_DEVICE);
                     return;
                 }
                 phase ^= 1u;

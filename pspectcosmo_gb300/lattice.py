@@ -34,6 +34,7 @@ PSC_ERR_TIMEOUT = -5
 PSC_ERR_STATE = -6
 PSC_ERR_NOMEM = -7
 PSC_ERR_IO = -8
+PSC_ERR_DEVICE = -9
 
 _lib = None
 
@@ -121,6 +122,8 @@ def load_library(path: str | None = None):
                                     ctypes.c_double, D, D, D]
     L.psc_slices.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, D,
                              ctypes.POINTER(ctypes.c_longlong)]
+    L.psc_selftest_bulk_wait.argtypes = [ctypes.c_double, ctypes.POINTER(ctypes.c_int)]
+    L.psc_test_wait_hook.argtypes = [P, ctypes.c_double, ctypes.c_int]
     L.psc_strerror.argtypes = [ctypes.c_int]
     L.psc_strerror.restype = ctypes.c_char_p
     L.psc_last_error.argtypes = []
@@ -136,7 +139,7 @@ def load_library(path: str | None = None):
                  "psc_set_state_padded", "psc_checkpoint_write", "psc_checkpoint_read",
                  "psc_h5_dataset_shape", "psc_h5_read_f64", "psc_analytic_begin", "psc_analytic_step",
                  "psc_analytic_background", "psc_analytic_modes", "psc_analytic_to_lattice",
-                 "psc_histograms_2d", "psc_slices"):
+                 "psc_histograms_2d", "psc_slices", "psc_selftest_bulk_wait", "psc_test_wait_hook"):
         getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L
