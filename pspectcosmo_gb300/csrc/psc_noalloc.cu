@@ -15,7 +15,6 @@
 // call's sums; each call clears them before use. Calls whose work overlaps on
 // the GPU (different streams, or different host threads) race on them.
 #include <cmath>
-#include <mutex>
 
 #include "../../include/psc.h"
 #include "psc_dev.cuh"
@@ -34,13 +33,6 @@ struct SpectraScratch {
     alignas(256) int counts[kCountInts];
 };
 static __device__ __align__(256) SpectraScratch g_spectra_scratch;
-
-// Device address of g_spectra_scratch per device, found once with
-// cudaGetSymbolAddress while that device is current. In host code the symbol
-// itself is only a host-side stand-in, never a device address.
-constexpr int kMaxDevices = 64;
-SpectraScratch *g_scratch_addr[kMaxDevices] = {};
-std::mutex g_scratch_mutex;
 
 int fail(int code, const char *msg) {
     psc::set_last_error(msg);
@@ -119,21 +111,26 @@ extern "C" int psc_spectra_noalloc(const psc_params *p, double a, double ad, con
     if (nb > kMaxBins) return fail(PSC_ERR_CONFIG, "psc_spectra_noalloc: too many bins");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
-        return fail(PSC_ERR_CUDA, "psc_spectra_noalloc: no current CUDA device");
-    SpectraScratch *scratch;
-    {
-        std::lock_guard<std::mutex> lock(g_scratch_mutex);
-        if (!g_scratch_addr[dev]) {
-            void *ptr = nullptr;
-            cudaError_t e = cudaGetSymbolAddress(&ptr, g_spectra_scratch);
-            if (e != cudaSuccess) return fail(PSC_ERR_CUDA, cudaGetErrorString(e));
-            g_scratch_addr[dev] = static_cast<SpectraScratch *>(ptr);
-        }
-        scratch = g_scratch_addr[dev];
+    if (cudaGetDevice(&dev) != cudaSuccess) return fail(PSC_ERR_CUDA, "psc_spectra_noalloc: no current CUDA device");
+    if (st) {
+        // the scratch address below is the current device's copy: the stream must be on it
+        int sdev = -1;
+        if (cudaStreamGetDevice(st, &sdev) != cudaSuccess)
+            return fail(PSC_ERR_ARG, "psc_spectra_noalloc: not a valid CUDA stream");
+        if (sdev != dev)
+            return fail(PSC_ERR_ARG, "psc_spectra_noalloc: the stream belongs to another device than the current one");
     }
+    // Device address of g_spectra_scratch on the current device. In host code the symbol
+    // itself is only a host-side stand-in, never a device address. The lookup is made on
+    // every call, so a context created anew on the device (after cudaDeviceReset) is served
+    // by its own copy; the first lookup in a context loads the library's device code there,
+    // which is the set-up that should come before any stream capture.
+    void *ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_spectra_scratch);
+    if (e != cudaSuccess) return fail(PSC_ERR_CUDA, cudaGetErrorString(e));
+    SpectraScratch *scratch = static_cast<SpectraScratch *>(ptr);
     // clear the accumulators this call uses (the previous call's sums are still there)
-    cudaError_t e = cudaMemsetAsync(scratch->sums, 0, sizeof(double) * 3 * nb * p->nflds, st);
+    e = cudaMemsetAsync(scratch->sums, 0, sizeof(double) * 3 * nb * p->nflds, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(scratch->counts, 0, sizeof(int) * nb * p->nflds, st);
     if (e != cudaSuccess) return fail(PSC_ERR_CUDA, cudaGetErrorString(e));
     const long long modes = (long long)p->N * p->N * (p->N / 2 + 1);

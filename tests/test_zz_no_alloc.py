@@ -6,7 +6,10 @@ accumulators in a fixed array inside the library and calls no cudaMalloc. This t
 it device copies of a lattice's state (made here with torch, as such a caller would
 provide them), calls it twice in a row through the C ABI, and checks both results
 against the handle-based psc_spectra: bin counts exactly, per-bin means to 1e-12 relative
-(the two differ only in the order of floating-point atomic additions).
+(the two differ only in the order of floating-point atomic additions). The second call
+must leave the device's free memory unchanged (cudaMemGetInfo before and after): it
+allocates nothing. Sizes 16^3 to 64^3, FP64 and FP32, on the default stream and on a
+stream of the caller's.
 
 This file sorts last so that a run stopping at its first failure has run every other test.
 """
@@ -26,15 +29,16 @@ def _noalloc(lib):
     return f
 
 
-@pytest.mark.parametrize("precision", [64, 32])
-def test_noalloc_spectra_match_handle_spectra(precision):
+@pytest.mark.parametrize("N,precision,own_stream", [(32, 64, False), (32, 32, False), (16, 64, True),
+                                                    (64, 32, True)])
+def test_noalloc_spectra_match_handle_spectra(N, precision, own_stream):
     torch = pytest.importorskip("torch")
     from pspectcosmo_gb300 import Lattice, load_library
     from pspectcosmo_gb300.params import Params
 
     lib = load_library()
     fn = _noalloc(lib)
-    p = Params.preheating(N=32, precision=precision)
+    p = Params.preheating(N=N, precision=precision)
     lat = Lattice(p)
     lat.initialize()
     lat.evolve(0.005, 4)
@@ -45,6 +49,8 @@ def test_noalloc_spectra_match_handle_spectra(precision):
     dev = torch.device("cuda:0")
     f_k = torch.from_numpy(st["f_k"]).to(cdt).to(dev).contiguous()
     pi_k = torch.from_numpy(st["pi_k"]).to(cdt).to(dev).contiguous()
+    stream = torch.cuda.Stream(device=dev) if own_stream else None
+    handle = ctypes.c_void_p(stream.cuda_stream) if own_stream else None
     nb = p.maxnumbins
     for call in range(2):
         numpoints = torch.full((p.nflds, nb), -1, dtype=torch.int32, device=dev)
@@ -52,10 +58,14 @@ def test_noalloc_spectra_match_handle_spectra(precision):
         pi2 = torch.full_like(f2, np.nan)
         n2 = torch.full_like(f2, np.nan)
         torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info(dev)[0]
         rc = fn(ctypes.byref(p), st["a"], st["ad"], f_k.data_ptr(), pi_k.data_ptr(), numpoints.data_ptr(),
-                f2.data_ptr(), pi2.data_ptr(), n2.data_ptr(), None)
+                f2.data_ptr(), pi2.data_ptr(), n2.data_ptr(), handle)
         assert rc == 0, lib.psc_last_error()
         torch.cuda.synchronize()
+        free_after = torch.cuda.mem_get_info(dev)[0]
+        if call == 1:   # the first call may load the library's device code into the context
+            assert free_after == free_before, f"device free memory changed by {free_before - free_after} bytes"
         assert np.array_equal(numpoints.cpu().numpy(), ref["numpoints"]), f"bin counts, call {call}"
         for name, got in (("f2", f2), ("pi2", pi2), ("n2", n2)):
             g = got.cpu().numpy()
@@ -63,6 +73,7 @@ def test_noalloc_spectra_match_handle_spectra(precision):
             assert np.all(np.isfinite(g)), name
             err = np.abs(g - r).max() / np.abs(r).max()
             assert err < 1e-12, f"{name} differs by {err:.3e} on call {call}"
+    lat.close()
 
 
 def test_noalloc_rejects_sizes_beyond_its_limit():
