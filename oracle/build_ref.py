@@ -27,8 +27,14 @@ import sys
 from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+# the reference checkout this recipe reads (PSC_REFERENCE_DIR overrides the default)
 REF = os.environ.get("PSC_REFERENCE_DIR", "/root/reference")
 OUT = os.path.join(HERE, "_ref")
+
+
+def reference_available() -> bool:
+    """True where the reference checkout exists (never on the GPU machine)."""
+    return os.path.isdir(REF)
 
 # name -> (model, overrides). Values are C++ source text.
 CONFIGS: dict[str, tuple[str, dict[str, str]]] = {

@@ -1,0 +1,170 @@
+"""Parity at the benchmark's own configuration: 256^3 two-field preheating (V = phi^2/2 +
+g^2 phi^2 chi^2/2, g^2 = 2.5e5, phi0 = 0.193, phidot0 = -0.142, kIR = 1) with gravitational
+waves, Yoshida-4, dt = 0.005 — the kernels bench.py times (the 256-point instantiations of
+every pass and the bulk-staged GW Z pass) against the FP64 oracle, which follows the
+reference's real-space step with GWs (evolution.cpp:607-694).
+
+* FP64 device path, one step (three Yoshida stages) from the oracle's initial state: fields
+  and the six u_ij, pi_u_ij within 1e-10 relative, and so are the fluctuation modes alone
+  (the zero mode left out: phi's zero mode, 0.193 N^3, would hide them); background within
+  1e-12, spectrum bin counts bit-exact, GW spectra, energies and rho_GW within 1e-10. The
+  spectra of phi are compared at the real-space tolerance (1e-7, n_k 1e-6): V'(phi0 + dphi)
+  is evaluated per site, so phi's fluctuation modes carry a rounding floor of about
+  eps phi0 / dphi that depends on the order of the FFT sums (measured on GB300: f2 3.4e-10,
+  pi2 2.0e-10, n_k 2.7e-7; chi, with no zero mode, 2e-14). The device's own initial
+  conditions equal the oracle's to 1e-12 first.
+* FP32 device path, same step: within the FP32 tolerances stated below.
+* FP64, 32^3 two-field + GW, Y4, 1000 steps (t = 5) against the oracle: the fields stay
+  within 1e-10 relative at every 100-step checkpoint.
+
+The oracle needs ~7 GB of host memory and ~30 s of host time at 256^3; it runs once for
+the module."""
+import numpy as np
+import pytest
+
+from golden_util import output_rows, rel
+
+pytestmark = pytest.mark.gpu
+
+DT = 0.005
+REALSPACE_SPEC_TOL = 1e-7
+REALSPACE_NK_TOL = 1e-6
+# FP32 tolerances after one step (measured on GB300, with margin; see the module text)
+FP32_FIELD_TOL = 1e-5
+FP32_FLUCT_TOL = 1e-4   # fluctuation modes alone (phi's rounding against phi0 shows here)
+FP32_BG_TOL = 1e-7
+FP32_ADD_TOL = 1e-5
+FP32_SPEC_TOL = 1e-4
+FP32_NK_TOL = 1e-3
+
+
+def _params(precision):
+    from pspectcosmo_gb300.params import Params
+
+    return Params.preheating(N=256, vv=4, spectral=0, with_gw=1, precision=precision)
+
+
+@pytest.fixture(scope="module")
+def headline(oracle_mod):
+    p = _params(64)
+    o = oracle_mod.Oracle(p)
+    o.init_ic()
+    init = dict(state=o.state_k(), bg=o.bg())
+    o.step(DT, 1)
+    fin = dict(state=o.state_k(), bg=o.bg(), rows=output_rows(o, p))
+    o.close()
+    return init, fin
+
+
+def _evolve_from(init, precision):
+    from pspectcosmo_gb300 import Lattice
+
+    p = _params(precision)
+    lat = Lattice(p)
+    f0, pi0, u0, pu0 = init["state"]
+    b = init["bg"]
+    lat.set_state(f0, pi0, b["a"], b["ad"], b["add"], u0, pu0)
+    lat.evolve(DT, 1)
+    return p, lat
+
+
+def _errors(lat, p, fin):
+    st = lat.get_state()
+    of, opi, ou, opu = fin["state"]
+    bg = fin["bg"]
+    e = dict(f_k=rel(st["f_k"], of), pi_k=rel(st["pi_k"], opi), u_k=rel(st["u_k"], ou), pi_u_k=rel(st["pi_u_k"], opu),
+             f_k_fluct=rel(st["f_k"][:, 1:], of[:, 1:]), pi_k_fluct=rel(st["pi_k"][:, 1:], opi[:, 1:]),
+             a=rel(st["a"], bg["a"]), ad=rel(st["ad"], bg["ad"]), add=rel(st["add"], bg["add"]))
+    rg, ro = output_rows(lat, p), fin["rows"]
+    counts_equal = True
+    for f in range(p.nflds):
+        a, b = rg[f"spectra_scalar_{f}"], ro[f"spectra_scalar_{f}"]
+        counts_equal &= bool(np.array_equal(a[:, 4], b[:, 4]))
+        for c, name in ((1, "f2"), (2, "pi2"), (3, "nk")):
+            e[f"{name}_{f}"] = rel(a[:, c], b[:, c])
+    a, b = rg["spectra_gws"], ro["spectra_gws"]
+    counts_equal &= bool(np.array_equal(a[:, 4], b[:, 4]))
+    e["h2"] = rel(a[:, 1], b[:, 1])
+    e["hdot2"] = rel(a[:, 2], b[:, 2])
+    eg, eo = rg["energies"], ro["energies"]
+    for k in ("K", "G", "V", "rho_gw"):
+        e[k] = rel(eg[k], eo[k])
+    return e, counts_equal
+
+
+def test_headline_fp64_one_step_matches_oracle(headline):
+    from pspectcosmo_gb300 import Lattice
+
+    init, fin = headline
+    p = _params(64)
+    lat = Lattice(p)
+    lat.initialize()
+    st = lat.get_state()
+    f0, pi0, u0, pu0 = init["state"]
+    for name, x, y in (("f_k", st["f_k"], f0), ("pi_k", st["pi_k"], pi0), ("u_k", st["u_k"], u0),
+                       ("pi_u_k", st["pi_u_k"], pu0)):
+        assert rel(x, y) < 1e-12, f"initial {name}"
+    lat.close()
+
+    p, lat = _evolve_from(init, 64)
+    e, counts_equal = _errors(lat, p, fin)
+    print("headline FP64 errors:", {k: f"{v:.2e}" for k, v in e.items()})
+    assert counts_equal, "bin counts must be bit-exact"
+    for k in ("f_k", "pi_k", "u_k", "pi_u_k", "f_k_fluct", "pi_k_fluct"):
+        assert e[k] < 1e-10, k
+    for k in ("a", "ad", "add"):
+        assert e[k] < 1e-12, k
+    assert e["f2_0"] < REALSPACE_SPEC_TOL and e["pi2_0"] < REALSPACE_SPEC_TOL and e["nk_0"] < REALSPACE_NK_TOL
+    for k in ("f2_1", "pi2_1", "nk_1", "h2", "hdot2", "K", "G", "V", "rho_gw"):
+        assert e[k] < 1e-10, k
+    lat.close()
+
+
+def test_headline_fp32_one_step_within_stated_tolerance(headline):
+    init, fin = headline
+    p, lat = _evolve_from(init, 32)
+    e, counts_equal = _errors(lat, p, fin)
+    print("headline FP32 errors:", {k: f"{v:.2e}" for k, v in e.items()})
+    assert counts_equal, "bin counts must be bit-exact"
+    for k in ("f_k", "pi_k", "u_k", "pi_u_k"):
+        assert e[k] < FP32_FIELD_TOL, k
+    assert e["f_k_fluct"] < FP32_FLUCT_TOL and e["pi_k_fluct"] < FP32_FLUCT_TOL
+    assert e["a"] < FP32_BG_TOL and e["ad"] < FP32_BG_TOL
+    assert e["add"] < FP32_ADD_TOL
+    for f in range(p.nflds):
+        assert e[f"f2_{f}"] < FP32_SPEC_TOL and e[f"pi2_{f}"] < FP32_SPEC_TOL, f"spectra of field {f}"
+        assert e[f"nk_{f}"] < FP32_NK_TOL, f"n_k of field {f}"
+    for k in ("h2", "hdot2", "K", "G", "V", "rho_gw"):
+        assert e[k] < FP32_SPEC_TOL, k
+    lat.close()
+
+
+def test_gw_two_field_1000_steps_32cubed_fp64(oracle_mod):
+    """Two-field preheating with GWs, Y4, FP64, 32^3, 1000 steps against the oracle: the
+    preheating dynamics amplify rounding differences, so the error is recorded at every
+    100-step checkpoint and must stay within 1e-10 relative throughout."""
+    from pspectcosmo_gb300 import Lattice
+    from pspectcosmo_gb300.params import Params
+
+    p = Params.preheating(N=32, vv=4, spectral=0, with_gw=1, precision=64)
+    o = oracle_mod.Oracle(p)
+    o.init_ic()
+    f0, pi0, u0, pu0 = o.state_k()
+    b = o.bg()
+    lat = Lattice(p)
+    lat.set_state(f0, pi0, b["a"], b["ad"], b["add"], u0, pu0)
+    track = []
+    for k in range(10):
+        lat.evolve(DT, 100)
+        o.step(DT, 100)
+        st = lat.get_state()
+        of, opi, ou, opu = o.state_k()
+        bg = o.bg()
+        err = max(rel(st["f_k"], of), rel(st["pi_k"], opi), rel(st["u_k"], ou), rel(st["pi_u_k"], opu))
+        track.append((100 * (k + 1), err, rel(st["a"], bg["a"])))
+    print("32^3 GW two-field FP64 vs oracle (step, field error, a error):",
+          [(s, f"{e:.2e}", f"{ea:.2e}") for s, e, ea in track])
+    for s, e, ea in track:
+        assert e < 1e-10, f"fields differ by {e:.3e} at step {s}"
+        assert ea < 1e-12, f"a differs by {ea:.3e} at step {s}"
+    lat.close()
