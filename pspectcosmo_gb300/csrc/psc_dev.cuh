@@ -72,6 +72,30 @@ __device__ __forceinline__ void model_potential(const ModelG<G> &m, const T *v, 
     }
 }
 
+// The potential terms of one site minus a reference value per term, accumulated in the
+// field precision: terms[t] += V_t(v) - ref[t], where ref holds the terms of the first
+// site the thread summed (set here when *count == 0). A plain FP32 sum of a thread's
+// sites adds a long run of nearly equal values (phi^2/2 of a lattice dominated by its
+// homogeneous mode), and its roundings do not cancel: at 256^3 two-field preheating <V>
+// came out 5e-7 high after one step, which a'' ~ (V - 2K) amplifies tenfold. Shifted, the
+// summands are the sites' small deviations. The reference depends on the state alone, so
+// resumed and uninterrupted runs sum identically. The caller adds count x ref in FP64.
+template <typename T, typename G>
+__device__ __forceinline__ void model_potential_shifted(const ModelG<G> &m, const T *v, T *ref, T *terms,
+                                                        int *count) {
+    const T p = v[0];
+    if (*count == 0) {
+        ref[0] = T(0.5) * p * p;
+        ref[1] = m.kind == 1 ? T(0.5) * (T)m.gsq * p * p * v[1] * v[1] : T(0);
+    }
+    ++*count;
+    terms[0] += fma(T(0.5) * p, p, -ref[0]);
+    if (m.kind == 1) {
+        const T c = v[1];
+        terms[1] += fma(T(0.5) * (T)m.gsq * p * p * c, c, -ref[1]);
+    }
+}
+
 // ------------------------------------------------------------------ FFT engine
 // cos/sin(2 pi k / 16): exact decimal expansions of the algebraic values.
 __host__ __device__ constexpr double cos16(int k) {

@@ -458,6 +458,9 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
     T pot_t[kMaxTerms] = {T(0), T(0)};
     double pot_d[kMaxTerms] = {0.0, 0.0};
     int nfold = 0;
+    // the sums run over V(site) - vref (model_potential_shifted), vref the thread's first site
+    T vref[kMaxTerms] = {T(0), T(0)};
+    int nsite = 0;
     prefetch(blockIdx.x);
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int line = tile * TL + t;
@@ -524,7 +527,7 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
 #pragma unroll
                 for (int fl = 0; fl < 2; ++fl) f[fl] = (fl < nf) ? (half ? in[fl].y : in[fl].x) : T(0);
                 model_dvdf<T>(mdl, f, vp, nf);
-                model_potential<T, T, T>(mdl, f, pot_t);
+                model_potential_shifted<T, T>(mdl, f, vref, pot_t, &nsite);
 #pragma unroll
                 for (int fl = 0; fl < 2; ++fl)
                     if (fl < nf) { if (half) out[fl].y = vp[fl]; else out[fl].x = vp[fl]; }
@@ -573,7 +576,7 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
     }
     cp_async_wait_all();
 #pragma unroll
-    for (int i = 0; i < kMaxTerms; ++i) pot_d[i] += (double)pot_t[i];
+    for (int i = 0; i < kMaxTerms; ++i) pot_d[i] += (double)pot_t[i] + (double)nsite * (double)vref[i];
     block_reduce_store_t<double, kMaxTerms>(pot_d, partV, gridDim.x, blockIdx.x);
 }
 
@@ -689,6 +692,9 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
     T pot_t[kMaxTerms] = {T(0), T(0)};
     double pot_d[kMaxTerms] = {0.0, 0.0};
     int nfold = 0;
+    // the sums run over V(site) - vref (model_potential_shifted), vref the thread's first site
+    T vref[kMaxTerms] = {T(0), T(0)};
+    int nsite = 0;
     if (STAGED) prefetch(blockIdx.x);
     unsigned phase = 0;   // parity of the bulk-copy phase the next tile completes
     for (int tile = blockIdx.x; tile < ntiles; tile = STAGED ? tile + gridDim.x : ntiles) {
@@ -784,7 +790,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
             }
             T vp[2] = {T(0), T(0)};
             model_dvdf<T>(mdl, f, vp, nf);
-            model_potential<T, T, T>(mdl, f, pot_t);
+            model_potential_shifted<T, T>(mdl, f, vref, pot_t, &nsite);
             T o[8];
             const int si[6] = {0, 0, 0, 1, 1, 2}, sj[6] = {0, 1, 2, 1, 2, 2};
             o[0] = vp[0];
@@ -879,7 +885,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
     }
     if (STAGED) cp_async_wait_all();
 #pragma unroll
-    for (int i = 0; i < kMaxTerms; ++i) pot_d[i] += (double)pot_t[i];
+    for (int i = 0; i < kMaxTerms; ++i) pot_d[i] += (double)pot_t[i] + (double)nsite * (double)vref[i];
     block_reduce_store_t<double, kMaxTerms>(pot_d, partV, gridDim.x, blockIdx.x);
 }
 

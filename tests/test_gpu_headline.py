@@ -5,14 +5,19 @@ every pass and the bulk-staged GW Z pass) against the FP64 oracle, which follows
 reference's real-space step with GWs (evolution.cpp:607-694).
 
 * FP64 device path, one step (three Yoshida stages) from the oracle's initial state: fields
-  and the six u_ij, pi_u_ij within 1e-10 relative, and so are the fluctuation modes alone
-  (the zero mode left out: phi's zero mode, 0.193 N^3, would hide them); background within
-  1e-12, spectrum bin counts bit-exact, GW spectra, energies and rho_GW within 1e-10. The
-  spectra of phi are compared at the real-space tolerance (1e-7, n_k 1e-6): V'(phi0 + dphi)
-  is evaluated per site, so phi's fluctuation modes carry a rounding floor of about
-  eps phi0 / dphi that depends on the order of the FFT sums (measured on GB300: f2 3.4e-10,
-  pi2 2.0e-10, n_k 2.7e-7; chi, with no zero mode, 2e-14). The device's own initial
-  conditions equal the oracle's to 1e-12 first.
+  and the six u_ij, pi_u_ij within 1e-10 relative; chi's modes one by one within 1e-10;
+  background within 1e-12, spectrum bin counts bit-exact, GW spectra, energies and rho_GW
+  within 1e-10.
+  phi is the exception, and the reason is arithmetic, not the method: at 256^3 its
+  fluctuations are ~9e-9 of phi0 = 0.193 in real space, and V'(phi0 + dphi) is evaluated per
+  site (as the reference does), so every fluctuation mode of V'_k carries a rounding floor
+  of eps phi0 / dphi relative to the largest one. Computing V'_k of the oracle's own
+  initial state with phi0 inside the real-space array and without it differs by 2.1e-6 in
+  the max norm over the fluctuation modes, in FP64 and with numpy's FFT. Two codes that
+  sum their FFTs in different orders differ by that much mode by mode (measured: f 1.4e-6,
+  pi 2.4e-6), while the binned spectra average it out (f2 3.4e-10, pi2 2.0e-10, n_k
+  2.7e-7). phi's modes are compared at 1e-5 and its spectra at the real-space tolerance
+  (1e-7, n_k 1e-6). The device's own initial conditions equal the oracle's to 1e-12 first.
 * FP32 device path, same step: within the FP32 tolerances stated below.
 * FP64, 32^3 two-field + GW, Y4, 1000 steps (t = 5) against the oracle: the fields stay
   within 1e-10 relative at every 100-step checkpoint.
@@ -28,10 +33,11 @@ pytestmark = pytest.mark.gpu
 
 DT = 0.005
 REALSPACE_SPEC_TOL = 1e-7
+PHI_FLUCT_TOL = 1e-5    # phi's fluctuation modes one by one: the FP64 floor of V'(phi0 + dphi)
 REALSPACE_NK_TOL = 1e-6
 # FP32 tolerances after one step (measured on GB300, with margin; see the module text)
 FP32_FIELD_TOL = 1e-5
-FP32_FLUCT_TOL = 1e-4   # fluctuation modes alone (phi's rounding against phi0 shows here)
+FP32_FLUCT_TOL = 1e-3   # phi's fluctuation modes one by one (the FP32 floor of V'(phi0 + dphi))
 FP32_BG_TOL = 1e-7
 FP32_ADD_TOL = 1e-5
 FP32_SPEC_TOL = 1e-4
@@ -73,7 +79,8 @@ def _errors(lat, p, fin):
     of, opi, ou, opu = fin["state"]
     bg = fin["bg"]
     e = dict(f_k=rel(st["f_k"], of), pi_k=rel(st["pi_k"], opi), u_k=rel(st["u_k"], ou), pi_u_k=rel(st["pi_u_k"], opu),
-             f_k_fluct=rel(st["f_k"][:, 1:], of[:, 1:]), pi_k_fluct=rel(st["pi_k"][:, 1:], opi[:, 1:]),
+             f_k_fluct=rel(st["f_k"][0, 1:], of[0, 1:]), pi_k_fluct=rel(st["pi_k"][0, 1:], opi[0, 1:]),
+             chi_f_k=rel(st["f_k"][1], of[1]), chi_pi_k=rel(st["pi_k"][1], opi[1]),
              a=rel(st["a"], bg["a"]), ad=rel(st["ad"], bg["ad"]), add=rel(st["add"], bg["add"]))
     rg, ro = output_rows(lat, p), fin["rows"]
     counts_equal = True
@@ -110,8 +117,9 @@ def test_headline_fp64_one_step_matches_oracle(headline):
     e, counts_equal = _errors(lat, p, fin)
     print("headline FP64 errors:", {k: f"{v:.2e}" for k, v in e.items()})
     assert counts_equal, "bin counts must be bit-exact"
-    for k in ("f_k", "pi_k", "u_k", "pi_u_k", "f_k_fluct", "pi_k_fluct"):
+    for k in ("f_k", "pi_k", "u_k", "pi_u_k", "chi_f_k", "chi_pi_k"):
         assert e[k] < 1e-10, k
+    assert e["f_k_fluct"] < PHI_FLUCT_TOL and e["pi_k_fluct"] < PHI_FLUCT_TOL
     for k in ("a", "ad", "add"):
         assert e[k] < 1e-12, k
     assert e["f2_0"] < REALSPACE_SPEC_TOL and e["pi2_0"] < REALSPACE_SPEC_TOL and e["nk_0"] < REALSPACE_NK_TOL
@@ -129,6 +137,7 @@ def test_headline_fp32_one_step_within_stated_tolerance(headline):
     for k in ("f_k", "pi_k", "u_k", "pi_u_k"):
         assert e[k] < FP32_FIELD_TOL, k
     assert e["f_k_fluct"] < FP32_FLUCT_TOL and e["pi_k_fluct"] < FP32_FLUCT_TOL
+    assert e["chi_f_k"] < FP32_FIELD_TOL and e["chi_pi_k"] < FP32_FIELD_TOL
     assert e["a"] < FP32_BG_TOL and e["ad"] < FP32_BG_TOL
     assert e["add"] < FP32_ADD_TOL
     for f in range(p.nflds):
