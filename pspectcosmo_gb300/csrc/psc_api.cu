@@ -385,7 +385,7 @@ cudaError_t enqueue_step(psc_handle *h, cudaStream_t st) {
 // the opening half kick of a call and the start of its first step
 cudaError_t enqueue_prologue(psc_handle *h, double dt, int nsteps, cudaStream_t st) {
     cudaError_t e = psc::launch_set_run(h->b.bg, h->R, dt, nsteps, st);
-    if (e == cudaSuccess) e = psc::launch_scalar(h->cfg, h->b, psc::SCALAR_PRIME, 0, st);
+    if (e == cudaSuccess) e = psc::launch_scalar(h->cfg, h->b, psc::SCALAR_PRIME, h->force_valid ? 1 : 0, st);
     // the force at the current (f, a) is the one the previous call's last kick kept: the
     // opening half kick needs no force evaluation then (same arithmetic, same bits)
     if (e == cudaSuccess)
@@ -586,6 +586,7 @@ int create_handle(const psc_params *ps, int R, psc_handle **out) {
         bg.inv_n3sq = bg.inv_n3 * bg.inv_n3;
         bg.inv_nv = bg.inv_n3;
         bg.wait_ns = psc::kBulkWaitNs;
+        bg.fp32 = q.precision == 32 ? 1 : 0;
         if (h->padded) {
             // <V> over the padded sites (kernel_a_k_pad, evolution.cpp:1624-1631)
             bg.nbz = h->cfgp.nbz;
@@ -620,6 +621,17 @@ int init_ic_host(psc_handle *h, int r, std::vector<double> &fk, std::vector<doub
     return PSC_OK;
 }
 
+// the homogeneous modes' FP64 shadow from FP64 host arrays ([nf][modes] interleaved complex)
+void shadow_from(psc::DevBG &bg, const double *f_k, const double *pi_k, int nf, long long modes) {
+    for (int f = 0; f < nf; ++f)
+        for (int c = 0; c < 2; ++c) {
+            bg.z0f[f][c] = f_k[2 * (size_t)f * modes + c];
+            bg.z0p[f][c] = pi_k[2 * (size_t)f * modes + c];
+        }
+    bg.zero64 = 1;
+    bg.z0pending = 0;
+}
+
 int init_ic(psc_handle *h) {
     const psc::Geo &g = h->cfg.g;
     const size_t n = (size_t)g.modes;
@@ -627,7 +639,8 @@ int init_ic(psc_handle *h) {
     int rc;
     for (int r = 0; r < h->R; ++r) {
         psc::ICInfo info;
-        if (h->p[r].seed >= 1 && !(psc::ic_setup(h->p[r]).k2c > 0.)) {
+        const bool on_device = h->p[r].seed >= 1 && !(psc::ic_setup(h->p[r]).k2c > 0.);
+        if (on_device) {
             // on the device: one thread per mode (initialize.cpp:686-749 by skip-ahead)
             if ((rc = psc::ic_device(h, r, &info))) return rc;
         } else {
@@ -649,6 +662,20 @@ int init_ic(psc_handle *h) {
         bg.add = info.add_printed;
         bg.t = 0.0;
         bg.err = 0;
+        if (on_device) {
+            // the homogeneous modes as the device generator computes them in FP64
+            // (initialize.cpp:760-765), before their rounding to the array precision
+            const psc::ICSetup s = psc::ic_setup(h->p[r]);
+            for (int f = 0; f < g.nf; ++f) {
+                bg.z0f[f][0] = s.f0[f] * s.n3;
+                bg.z0p[f][0] = s.aop * s.fd0[f] * s.n3;
+                bg.z0f[f][1] = bg.z0p[f][1] = 0.0;
+            }
+            bg.zero64 = 1;
+            bg.z0pending = 0;
+        } else {
+            shadow_from(bg, fk.data(), pk.data(), g.nf, g.modes);
+        }
         if ((rc = write_bg(h, r, bg))) return rc;
     }
     h->have_state = true;
@@ -675,6 +702,7 @@ int set_state(psc_handle *h, int r, const double *f_k, const double *pi_k, doubl
     bg.ad = ad;
     bg.add = add;
     bg.err = 0;
+    shadow_from(bg, f_k, pi_k, g.nf, g.modes);
     if ((rc = write_bg(h, r, bg))) return rc;
     h->have_state = true;
     h->diag_valid = false;
@@ -695,6 +723,12 @@ int get_state(psc_handle *h, int r, double *f_k, double *pi_k, double *a, double
     }
     psc::DevBG bg;
     if ((rc = read_bg(h, r, &bg))) return rc;
+    if (bg.zero64)   // the homogeneous modes at the precision the device evolves them in
+        for (int f = 0; f < g.nf; ++f)
+            for (int c = 0; c < 2; ++c) {
+                if (f_k) f_k[2 * (size_t)f * n + c] = bg.z0f[f][c];
+                if (pi_k) pi_k[2 * (size_t)f * n + c] = bg.z0p[f][c];
+            }
     if (a) *a = bg.a;
     if (ad) *ad = bg.ad;
     if (add) *add = bg.add;
@@ -999,6 +1033,7 @@ int psc_set_state_padded(psc_handle *h, int Nsrc, const double *f_k, const doubl
     }
     cudaFreeAsync(src, h->st);
     if (rc) return rc;
+    CU(psc::launch_zero_sync(h->cfg, h->b, h->st));
     CU(cudaStreamSynchronize(h->st));
     psc::DevBG bg;
     if ((rc = read_bg(h, 0, &bg))) return rc;

@@ -31,7 +31,18 @@ struct DevBG {
     // test hook: bytes a GW Z pass tile is told to expect that no copy delivers, so its
     // wait runs out after the real copies have landed (0 = off)
     unsigned long long wait_ns;
-    int wait_plant, pad2;
+    int wait_plant, fp32;           // fp32: the handle's arrays hold FP32 values
+    // FP64 shadow of each field's homogeneous mode f_k(0), pi_k(0) (re, im). The background
+    // kernel evolves it (drift when a stage begins, the kicks after the kick pass) and writes
+    // its rounding into the arrays, which every other kernel reads as before. Stored in FP32
+    // and re-rounded by each kick, the homogeneous mode random-walks: at 256^3 two-field
+    // preheating a(t) drifted 7.6e-7 from FP64 over 4000 steps and shifted the phases of the
+    // highest GW modes (3e-4 in hdot^2); with the mode pinned to FP64, 4e-8 and 3e-5.
+    double z0f[kMaxFields][2], z0p[kMaxFields][2];
+    double z0q[kMaxFields][2];      // the zero mode of V'_k as the last kick pass read it
+    double z0F[kMaxFields][2];      // the zero mode's force at the last synchronising kick
+    int zero64;                     // 1 when the shadow holds the state (set with the state)
+    int z0pending;                  // 1 after a kick pass, until the background kernel kicks
 };
 
 // Scalar state of the discrete adjoint (psc_adjoint.cu), resident in device memory

@@ -64,6 +64,8 @@ __global__ void __launch_bounds__(256) k_ifft_x(Geo g, cplx<T> *__restrict__ fk,
                 const C p = pk[a];
                 v.x += c * p.x;
                 v.y += c * p.y;
+                // the homogeneous mode: the background kernel's FP64 shadow, already drifted
+                if (a == off && bg->zero64) v = mk<T>((T)bg->z0f[blockIdx.y][0], (T)bg->z0f[blockIdx.y][1]);
                 fk[a] = v;
             }
         }
@@ -371,6 +373,13 @@ __global__ void __launch_bounds__(256) k_fft_x_final(Geo g, const cplx<T> *__res
             const T k2 = (T)(px * px + py * py + kz * kz);
             const long long a = off + n * stride + line;
             const C f = fk[a], p = pk[a], q = r[idx];
+            if (a == off && bg->zero64) {   // the homogeneous mode: kicked in FP64 by the background kernel
+                DevBG *bw = const_cast<DevBG *>(bg);
+                bw->z0q[job][0] = (double)q.x;
+                bw->z0q[job][1] = (double)q.y;
+                bw->z0pending = 1;
+                continue;
+            }
             // force (evolution.cpp:1124-1125)
             const T fl = -norm1 * kIR2 * k2;
             const C F = mk<T>(fl * f.x - norm2 * q.x, fl * f.y - norm2 * q.y);
@@ -417,6 +426,30 @@ __global__ void __launch_bounds__(256) k_fft_x_final(Geo g, const cplx<T> *__res
 }
 
 // ------------------------------------------------------------------ scalar background update
+// The homogeneous mode's FP64 shadow (DevBG::z0*): element 0 of field f's array, rounded
+// to the array's precision
+__device__ void zero_store(const DevBG *bg, void *arr, long long modes, int f, const double *v) {
+    if (bg->fp32) reinterpret_cast<float2 *>(arr)[(long long)f * modes] = make_float2((float)v[0], (float)v[1]);
+    else reinterpret_cast<double2 *>(arr)[(long long)f * modes] = make_double2(v[0], v[1]);
+}
+
+// The kicks of the last kick pass, applied to the shadow: F = -a^(3+alpha) V'_k(0) (no
+// gradient term at k = 0, kernel_field_k_nopad evolution.cpp:1124-1125), pf = p + c_close F
+// (synchronised: K0[f] = |pf|^2, the zero mode's term of the kinetic sum), p = pf + c_open F.
+__device__ void zero_kick(DevBG *bg, void *pk, long long modes, double *K0) {
+    for (int f = 0; f < bg->nf; ++f) {
+        const double F[2] = {-bg->norm2 * bg->z0q[f][0], -bg->norm2 * bg->z0q[f][1]};
+        const double pf[2] = {bg->z0p[f][0] + bg->c_close * F[0], bg->z0p[f][1] + bg->c_close * F[1]};
+        if (K0) K0[f] = pf[0] * pf[0] + pf[1] * pf[1];
+        for (int c = 0; c < 2; ++c) {
+            bg->z0p[f][c] = pf[c] + bg->c_open * F[c];
+            if (bg->c_open == 0.0) bg->z0F[f][c] = F[c];
+        }
+        zero_store(bg, pk, modes, f, bg->z0p[f]);
+    }
+    bg->z0pending = 0;
+}
+
 __device__ void begin_stage(DevBG *bg, int p) {
     const double w = bg->w[p], dt = bg->dt;
     const int al = bg->alpha;
@@ -434,6 +467,9 @@ __device__ void begin_stage(DevBG *bg, int p) {
     bg->apow = ipow(bg->a, al - 3);
     bg->a3 = ipow(bg->a, 3 - al);
     bg->stage = p;
+    if (bg->zero64)   // the drift of the homogeneous mode (the drift pass reads the shadow)
+        for (int f = 0; f < bg->nf; ++f)
+            for (int c = 0; c < 2; ++c) bg->z0f[f][c] += bg->c_drift * bg->z0p[f][c];
 }
 
 __device__ void eval_coeffs(DevBG *bg) {
@@ -454,14 +490,23 @@ __device__ double friedmann_add(const DevBG *bg, double K, double G, double V) {
     return 1. / 3. * bg->fs_over_mpl2 * ipow(bg->a, 1 + 2 * al) * ((al - 2) * K + al * G + (al + 1) * V);
 }
 
+// fk, pk: the realizations' field arrays (realization blockIdx.x at blockIdx.x fstride
+// elements), for the homogeneous mode's shadow. SCALAR_PRIME with p = 1: the opening half
+// kick uses the kept force.
 __global__ void __launch_bounds__(1024) k_scalar(DevBG *bg, const double *__restrict__ partKG,
                                                 const double *__restrict__ partV, int mode, int p, int pkg_stride,
-                                                int pv_stride) {
+                                                int pv_stride, void *fk, void *pk, long long fstride,
+                                                long long modes) {
     constexpr int NQ = 2 * kMaxFields + kMaxTerms;
     __shared__ double red[32][NQ];
     bg += blockIdx.x;
     partKG += (size_t)blockIdx.x * pkg_stride;
     partV += (size_t)blockIdx.x * pv_stride;
+    {
+        const size_t off = (size_t)blockIdx.x * fstride * (bg->fp32 ? sizeof(float2) : sizeof(double2));
+        fk = static_cast<char *>(fk) + off;
+        pk = static_cast<char *>(pk) + off;
+    }
     // a failed step (a wait ran out, a non-finite background) keeps its background as the
     // failure left it; evaluations of the state still run
     if (bg->err && mode != SCALAR_EVAL && mode != SCALAR_EVAL_END) return;
@@ -511,9 +556,15 @@ __global__ void __launch_bounds__(1024) k_scalar(DevBG *bg, const double *__rest
         __syncthreads();
     }
     if (threadIdx.x != 0) return;
+    const bool z0 = bg->zero64 != 0;
     if (mode == SCALAR_PRIME) {
         eval_coeffs(bg);
         bg->c_open = bg->w[0] * bg->dt / 2;
+        if (z0 && p)   // the opening half kick of the homogeneous mode from its kept force
+            for (int f = 0; f < bg->nf; ++f) {
+                for (int c = 0; c < 2; ++c) bg->z0p[f][c] += bg->c_open * bg->z0F[f][c];
+                zero_store(bg, pk, modes, f, bg->z0p[f]);
+            }
         return;
     }
     if (mode == SCALAR_EVAL) {
@@ -522,6 +573,7 @@ __global__ void __launch_bounds__(1024) k_scalar(DevBG *bg, const double *__rest
         return;
     }
     if (mode == SCALAR_BEGIN) {
+        if (z0 && bg->z0pending) zero_kick(bg, pk, modes, nullptr);   // the prologue's evaluated kick
         bg->b = bg->ad;
         bg->ad_stale = bg->ad;
         begin_stage(bg, 0);
@@ -531,8 +583,10 @@ __global__ void __launch_bounds__(1024) k_scalar(DevBG *bg, const double *__rest
     // V_E evolution.cpp:1077-1085)
     double K = 0, G = 0, V = 0;
     const double a = bg->a;
+    double K0[kMaxFields] = {0.0, 0.0};   // the homogeneous mode's kinetic term, from the shadow
+    if (z0 && bg->z0pending) zero_kick(bg, pk, modes, K0);
     for (int f = 0; f < bg->nf; ++f) {
-        const double k = .5 * sums[2 * f] / ipow(a, 6) * bg->inv_n3sq;
+        const double k = .5 * (sums[2 * f] + K0[f]) / ipow(a, 6) * bg->inv_n3sq;
         double grad = bg->kIR2 * sums[2 * f + 1];
         grad *= bg->inv_n3;
         grad /= 2.;
@@ -569,6 +623,32 @@ __global__ void __launch_bounds__(1024) k_scalar(DevBG *bg, const double *__rest
         bg->ad_stale = bg->ad;
         begin_stage(bg, 0);
     }
+}
+
+// the homogeneous modes' FP64 shadow taken from the arrays (after a device-side writer)
+__global__ void k_zero_sync(DevBG *bg, const void *fk, const void *pk, long long fstride, long long modes) {
+    if (threadIdx.x != 0) return;
+    bg += blockIdx.x;
+    const size_t cs = bg->fp32 ? sizeof(float2) : sizeof(double2);
+    const char *f = static_cast<const char *>(fk) + (size_t)blockIdx.x * fstride * cs;
+    const char *p = static_cast<const char *>(pk) + (size_t)blockIdx.x * fstride * cs;
+    for (int q = 0; q < bg->nf; ++q) {
+        const size_t o = (size_t)q * modes * cs;
+        if (bg->fp32) {
+            const float2 a = *reinterpret_cast<const float2 *>(f + o), b = *reinterpret_cast<const float2 *>(p + o);
+            bg->z0f[q][0] = a.x, bg->z0f[q][1] = a.y, bg->z0p[q][0] = b.x, bg->z0p[q][1] = b.y;
+        } else {
+            const double2 a = *reinterpret_cast<const double2 *>(f + o), b = *reinterpret_cast<const double2 *>(p + o);
+            bg->z0f[q][0] = a.x, bg->z0f[q][1] = a.y, bg->z0p[q][0] = b.x, bg->z0p[q][1] = b.y;
+        }
+    }
+    bg->zero64 = 1;
+    bg->z0pending = 0;
+}
+
+cudaError_t launch_zero_sync(const LaunchCfg &cfg, const Buffers &b, cudaStream_t st) {
+    k_zero_sync<<<cfg.R, 32, 0, st>>>(b.bg, b.fk, b.pk, cfg.g.fstride, cfg.g.modes);
+    return cudaGetLastError();
 }
 
 __global__ void k_set_run(DevBG *bg, int R, double dt, int nsteps) {
@@ -909,7 +989,8 @@ static cudaError_t launch_stage_t(const LaunchCfg &cfg, const Buffers &b, int dr
     else k_fft_x_final<T, false><<<gf, cfg.thr_xy, cfg.smem_xy, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw);
     mark(5);
     if (scalar_mode >= 0) {
-        k_scalar<<<cfg.R, 1024, 0, st>>>(b.bg, b.partKG, b.partV, scalar_mode, 1, cfg.g.pkg_stride, cfg.g.pv_stride);
+        k_scalar<<<cfg.R, 1024, 0, st>>>(b.bg, b.partKG, b.partV, scalar_mode, 1, cfg.g.pkg_stride, cfg.g.pv_stride,
+                                         b.fk, b.pk, cfg.g.fstride, cfg.g.modes);
         mark(6);
     }
     return cudaGetLastError();
@@ -932,7 +1013,8 @@ cudaError_t launch_stage(const LaunchCfg &cfg, const Buffers &b, int precision, 
 }
 
 cudaError_t launch_scalar(const LaunchCfg &cfg, const Buffers &b, int mode, int p, cudaStream_t st) {
-    k_scalar<<<cfg.R, 1024, 0, st>>>(b.bg, b.partKG, b.partV, mode, p, cfg.g.pkg_stride, cfg.g.pv_stride);
+    k_scalar<<<cfg.R, 1024, 0, st>>>(b.bg, b.partKG, b.partV, mode, p, cfg.g.pkg_stride, cfg.g.pv_stride, b.fk, b.pk,
+                                     cfg.g.fstride, cfg.g.modes);
     return cudaGetLastError();
 }
 
@@ -958,7 +1040,9 @@ __global__ void __launch_bounds__(256) k_open_kick(Geo g, cplx<T> *__restrict__ 
     }
     const T c_close = (T)bg->c_close, c_open = (T)bg->c_open;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < g.modes; m += stride) {
+    // the homogeneous mode of a field has its opening kick in the background kernel (FP64)
+    const long long m0 = (arr < g.nf && bg->zero64) ? 1 : 0;
+    for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x + m0; m < g.modes; m += stride) {
         const cplx<T> f = F[m], q = p[m];
         const cplx<T> pf = mk<T>(q.x + c_close * f.x, q.y + c_close * f.y);
         p[m] = mk<T>(pf.x + c_open * f.x, pf.y + c_open * f.y);

@@ -88,6 +88,8 @@ cudaError_t launch_stage_timed(const LaunchCfg &cfg, const Buffers &b, int preci
                                cudaEvent_t *ev, cudaStream_t st);
 cudaError_t launch_scalar(const LaunchCfg &cfg, const Buffers &b, int mode, int p, cudaStream_t st);
 cudaError_t launch_set_run(DevBG *bg, int R, double dt, int nsteps, cudaStream_t st);
+// The homogeneous modes' FP64 shadow (DevBG::z0f, z0p) read from the arrays' element 0.
+cudaError_t launch_zero_sync(const LaunchCfg &cfg, const Buffers &b, cudaStream_t st);
 // The opening half kick of a step call from the kept force: pi += c_open F (and pi_u).
 cudaError_t launch_open_kick(const LaunchCfg &cfg, const Buffers &b, int precision, cudaStream_t st);
 // Real-space view of nsrc complex arrays (c2r / N^3) into b.real (precision T).

@@ -50,6 +50,8 @@ __global__ void __launch_bounds__(kPadThreads) k_pad_scatter(cplx<T> *__restrict
             const cplx<T> p = pk[m];
             v.x += c * p.x;
             v.y += c * p.y;
+            // the homogeneous mode: the background kernel's FP64 shadow, already drifted
+            if (m == 0 && bg->zero64) v = mk<T>((T)bg->z0f[blockIdx.y][0], (T)bg->z0f[blockIdx.y][1]);
             src[m] = v;
         }
         T f = scale;
@@ -105,6 +107,13 @@ __global__ void __launch_bounds__(kPadThreads) k_pad_kick(const cplx<T> *__restr
         const int px = pcoord(i, N), py = pcoord(j, N);
         const T k2 = (T)(px * px + py * py + kz * kz);
         const C f = fk[m], p = pk[m];
+        if (m == 0 && bg->zero64) {   // the homogeneous mode: kicked in FP64 by the background kernel
+            DevBG *bw = const_cast<DevBG *>(bg);
+            bw->z0q[fld][0] = (double)q.x;
+            bw->z0q[fld][1] = (double)q.y;
+            bw->z0pending = 1;
+            continue;
+        }
         const T fl = -norm1 * kIR2 * k2;
         const C F = mk<T>(fl * f.x - norm2 * q.x, fl * f.y - norm2 * q.y);
         const C pf = mk<T>(p.x + c_close * F.x, p.y + c_close * F.y);

@@ -66,10 +66,14 @@ __global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_ifft_x(Ge
             C pv[16];
 #pragma unroll
             for (int r = 0; r < 16; ++r) pv[r] = valid ? pk[base + (long long)(j + r * RP::P) * stride] : mk<T>(0, 0);
+            // the homogeneous mode (element 0 of the line x = y = kz = 0) is the background
+            // kernel's FP64 shadow, already drifted
+            const bool z0 = line == 0 && j == 0 && bg->zero64;
 #pragma unroll
             for (int r = 0; r < 16; ++r) {
                 v[r].x += c * pv[r].x;
                 v[r].y += c * pv[r].y;
+                if (r == 0 && z0) v[0] = mk<T>((T)bg->z0f[blockIdx.y][0], (T)bg->z0f[blockIdx.y][1]);
                 if (valid) fk[base + (long long)(j + r * RP::P) * stride] = v[r];
             }
         }
@@ -285,6 +289,9 @@ __global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_fft_x_fin
     const int py = pcoord(y, N);
     if (field) {
         T accK = T(0), accG = T(0);   // per-thread partials (16 modes), FP64 across threads
+        // the homogeneous mode (n = 0 of line 0) is kicked by the background kernel in FP64:
+        // here its V'_k is handed over and it stays out of the partials
+        const bool z0 = line == 0 && bg->zero64;
         if (valid) {
             const bool mask = g.mask != 0;
             const T hub = (T)bg->hub, apow = (T)bg->apow, a3 = (T)bg->a3;
@@ -299,6 +306,18 @@ __global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_fft_x_fin
                     const T k2 = (T)(px * px + py * py + kz * kz);
                     const long long a = base + (long long)n * stride;
                     const C f = opA[ix(n)], p = opB[ix(n)], qv = v[q * RP::RL + r];
+                    if (z0 && n == 0) {
+                        DevBG *bw = const_cast<DevBG *>(bg);
+                        bw->z0q[job][0] = (double)qv.x;
+                        bw->z0q[job][1] = (double)qv.y;
+                        bw->z0pending = 1;
+                        if (tape_p) {   // the tape as the kick below would write it (k = 0: no -k^2 f term)
+                            tape_f[a] = f;
+                            tape_p[a] = mk<T>(p.x + c_close * (-norm2 * qv.x), p.y + c_close * (-norm2 * qv.y));
+                            tape_vp[a] = qv;
+                        }
+                        continue;
+                    }
                     // force (evolution.cpp:1124-1125)
                     const T fl = -norm1 * kIR2 * k2;
                     const C F = mk<T>(fl * f.x - norm2 * qv.x, fl * f.y - norm2 * qv.y);

@@ -7,9 +7,13 @@ reference keeps phi0 + dphi(x) in real space there, so its fluctuation spectra c
 rounding floor of ~eps * phi0 / dphi ~ 1e-9 per step that the k-space state does not
 have. FP32 device path (measured tolerances, written here so a regression shows):
 fields within 2e-4 relative of the oracle, a and a' within 1e-6, a'' within 1e-4
-(a'' = (fStar/MPl)^2 a (V - 2K)/3 cancels), P_f and P_pi within 1e-3, the occupation
-number n_k (|a^(alpha-3) pi + H f|^2 cancels for vacuum modes) within 1e-2; on the
-real-space path n_k is compared at 1e-6 for the same reason."""
+(a'' = (fStar/MPl)^2 a (V - 2K)/3 cancels), P_f and P_pi within 1e-4, the occupation
+number n_k (|a^(alpha-3) pi + H f|^2 cancels for vacuum modes) within 1e-3; on the
+real-space path n_k is compared at 1e-6 for the same reason. Two-field preheating runs on
+16^3 and 32^3 are held to 2e-3 for the spectra: their fluctuations are ~1e-8 of
+phi0 = 0.193, below FP32 resolution where V'(phi0 + dphi) is evaluated per site, and a bin of
+these small lattices holds too few modes to average that floor out (measured on GB300:
+P_f 3.7e-4 at 16^3, 9.0e-4 at 32^3; at 128^3 and 256^3 the same floor stays below 2e-6)."""
 import numpy as np
 import pytest
 
@@ -21,8 +25,9 @@ RUNS = ["spec1_n16", "spec1_n16_vv6", "spec1_n32_vv4", "spec1_n64_dt1e-4", "spec
         "gw1_n16_vv2", "gw2_n16_vv4"]
 
 FP32_FIELD_TOL = 2e-4
-FP32_SPEC_TOL = 1e-3
-FP32_NK_TOL = 1e-2
+FP32_SPEC_TOL = 1e-4
+FP32_NK_TOL = 1e-3
+FP32_SPEC_TOL_2F_SMALL = 2e-3   # two-field preheating on 16^3 / 32^3 (the FP32 floor of phi's fluctuations)
 FP32_BG_TOL = 1e-6
 FP32_ADD_TOL = 1e-4
 REALSPACE_SPEC_TOL = 1e-7
@@ -94,7 +99,9 @@ def test_fp32_within_stated_tolerance(oracle_mod, run):
     lat.evolve(meta["dt"], meta["nsteps"])
     o.step(meta["dt"], meta["nsteps"])
     _compare_state(lat, o, p, FP32_FIELD_TOL, FP32_BG_TOL, FP32_ADD_TOL)
-    _compare_outputs(lat, o, p, FP32_SPEC_TOL, FP32_NK_TOL)
+    small_two_field = p.nflds == 2 and p.N <= 32
+    tol = FP32_SPEC_TOL_2F_SMALL if small_two_field else FP32_SPEC_TOL
+    _compare_outputs(lat, o, p, tol, max(tol, FP32_NK_TOL))
 
 
 def test_fp64_against_reference_golden_directly(oracle_mod):
