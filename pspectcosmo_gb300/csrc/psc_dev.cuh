@@ -73,27 +73,33 @@ __device__ __forceinline__ void model_potential(const ModelG<G> &m, const T *v, 
 }
 
 // The potential terms of one site minus a reference value per term, accumulated in the
-// field precision: terms[t] += V_t(v) - ref[t], where ref holds the terms of the first
-// site the thread summed (set here when *count == 0). A plain FP32 sum of a thread's
-// sites adds a long run of nearly equal values (phi^2/2 of a lattice dominated by its
-// homogeneous mode), and its roundings do not cancel: at 256^3 two-field preheating <V>
-// came out 5e-7 high after one step, which a'' ~ (V - 2K) amplifies tenfold. Shifted, the
-// summands are the sites' small deviations. The reference depends on the state alone, so
-// resumed and uninterrupted runs sum identically. The caller adds count x ref in FP64.
+// field precision: terms[t] += V_t(v) - ref[t]. A plain FP32 sum of a thread's sites adds a
+// long run of nearly equal values (phi^2/2 of a lattice dominated by its homogeneous mode),
+// and its roundings do not cancel: at 256^3 two-field preheating <V> came out 5e-7 high
+// after one step, which a'' ~ (V - 2K) amplifies tenfold. Shifted by the terms of the
+// homogeneous fields (homogeneous_potential), the summands are the sites' small deviations.
+// The caller counts its sites and adds count x ref in FP64.
 template <typename T, typename G>
-__device__ __forceinline__ void model_potential_shifted(const ModelG<G> &m, const T *v, T *ref, T *terms,
-                                                        int *count) {
+__device__ __forceinline__ void model_potential_shifted(const ModelG<G> &m, const T *v, const T *ref, T *terms) {
     const T p = v[0];
-    if (*count == 0) {
-        ref[0] = T(0.5) * p * p;
-        ref[1] = m.kind == 1 ? T(0.5) * (T)m.gsq * p * p * v[1] * v[1] : T(0);
-    }
-    ++*count;
     terms[0] += fma(T(0.5) * p, p, -ref[0]);
     if (m.kind == 1) {
         const T c = v[1];
         terms[1] += fma(T(0.5) * (T)m.gsq * p * p * c, c, -ref[1]);
     }
+}
+
+// The potential terms of the homogeneous fields, the FP64 shadow of the zero modes over
+// N^3 (zero when the shadow is not set): a reference for model_potential_shifted that depends
+// on the state alone, so that resumed and uninterrupted runs sum identically.
+template <typename T, typename G>
+__device__ __forceinline__ void homogeneous_potential(const ModelG<G> &m, const DevBG *bg, T *ref) {
+    T f[kMaxFields] = {T(0), T(0)};
+    if (bg->zero64)
+        for (int q = 0; q < kMaxFields; ++q)
+            if (q < bg->nf) f[q] = (T)(bg->z0f[q][0] * bg->inv_n3);
+    ref[0] = T(0.5) * f[0] * f[0];
+    ref[1] = m.kind == 1 ? T(0.5) * (T)m.gsq * f[0] * f[0] * f[1] * f[1] : T(0);
 }
 
 // ------------------------------------------------------------------ FFT engine

@@ -66,15 +66,17 @@ __global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_ifft_x(Ge
             C pv[16];
 #pragma unroll
             for (int r = 0; r < 16; ++r) pv[r] = valid ? pk[base + (long long)(j + r * RP::P) * stride] : mk<T>(0, 0);
-            // the homogeneous mode (element 0 of the line x = y = kz = 0) is the background
-            // kernel's FP64 shadow, already drifted
-            const bool z0 = line == 0 && j == 0 && bg->zero64;
 #pragma unroll
             for (int r = 0; r < 16; ++r) {
                 v[r].x += c * pv[r].x;
                 v[r].y += c * pv[r].y;
-                if (r == 0 && z0) v[0] = mk<T>((T)bg->z0f[blockIdx.y][0], (T)bg->z0f[blockIdx.y][1]);
                 if (valid) fk[base + (long long)(j + r * RP::P) * stride] = v[r];
+            }
+            if (line == 0 && j == 0 && bg->zero64) {
+                // the homogeneous mode (element 0 of the line x = y = kz = 0) is the background
+                // kernel's FP64 shadow, already drifted
+                v[0] = mk<T>((T)bg->z0f[blockIdx.y][0], (T)bg->z0f[blockIdx.y][1]);
+                fk[base] = v[0];
             }
         }
         if (pass == 1) {
@@ -291,7 +293,7 @@ __global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_fft_x_fin
         T accK = T(0), accG = T(0);   // per-thread partials (16 modes), FP64 across threads
         // the homogeneous mode (n = 0 of line 0) is kicked by the background kernel in FP64:
         // here its V'_k is handed over and it stays out of the partials
-        const bool z0 = line == 0 && bg->zero64;
+        const bool z0 = line == 0 && j == 0 && bg->zero64;
         if (valid) {
             const bool mask = g.mask != 0;
             const T hub = (T)bg->hub, apow = (T)bg->apow, a3 = (T)bg->a3;
@@ -306,7 +308,7 @@ __global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_fft_x_fin
                     const T k2 = (T)(px * px + py * py + kz * kz);
                     const long long a = base + (long long)n * stride;
                     const C f = opA[ix(n)], p = opB[ix(n)], qv = v[q * RP::RL + r];
-                    if (z0 && n == 0) {
+                    if (q == 0 && r == 0 && z0) {   // n = 0 (out(0, 0, 0))
                         DevBG *bw = const_cast<DevBG *>(bg);
                         bw->z0q[job][0] = (double)qv.x;
                         bw->z0q[job][1] = (double)qv.y;
@@ -477,9 +479,12 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
     T pot_t[kMaxTerms] = {T(0), T(0)};
     double pot_d[kMaxTerms] = {0.0, 0.0};
     int nfold = 0;
-    // the sums run over V(site) - vref (model_potential_shifted), vref the thread's first site
-    T vref[kMaxTerms] = {T(0), T(0)};
-    int nsite = 0;
+    // the sums run over V(site) - vref (model_potential_shifted), vref the potential terms of
+    // the homogeneous fields (the FP64 shadow of the zero modes / N^3), a value of the state
+    // alone; vref is added back once per site summed (every tile gives a thread the same
+    // number of sites: the line count is a multiple of the tile's)
+    T vref[kMaxTerms];
+    homogeneous_potential<T>(mdl, bg, vref);
     prefetch(blockIdx.x);
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int line = tile * TL + t;
@@ -546,7 +551,7 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
 #pragma unroll
                 for (int fl = 0; fl < 2; ++fl) f[fl] = (fl < nf) ? (half ? in[fl].y : in[fl].x) : T(0);
                 model_dvdf<T>(mdl, f, vp, nf);
-                model_potential_shifted<T, T>(mdl, f, vref, pot_t, &nsite);
+                model_potential_shifted<T, T>(mdl, f, vref, pot_t);
 #pragma unroll
                 for (int fl = 0; fl < 2; ++fl)
                     if (fl < nf) { if (half) out[fl].y = vp[fl]; else out[fl].x = vp[fl]; }
@@ -595,7 +600,8 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
     }
     cp_async_wait_all();
 #pragma unroll
-    for (int i = 0; i < kMaxTerms; ++i) pot_d[i] += (double)pot_t[i] + (double)nsite * (double)vref[i];
+    const double nsite = (double)nfold * (2 * ((TL * M - 1 - (int)threadIdx.x) / (int)blockDim.x + 1));
+    for (int i = 0; i < kMaxTerms; ++i) pot_d[i] += (double)pot_t[i] + nsite * (double)vref[i];
     block_reduce_store_t<double, kMaxTerms>(pot_d, partV, gridDim.x, blockIdx.x);
 }
 
@@ -661,8 +667,6 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
     const C *stA = stage + ((size_t)(fld * 3 + (kind ? 1 : 0)) * TL + t) * hs;
     const C *stB = stage + ((size_t)(fld * 3 + 2) * TL + t) * hs;
     const int ntiles = (g.lines_z + TL - 1) / TL;
-    const unsigned long long wait_ns = bg->wait_ns;
-    const unsigned plant = (unsigned)bg->wait_plant;   // test hook, 0 in normal runs
     if (bulk && threadIdx.x == 0) {
         mbar_init(&zbar, 1);
         mbar_fence_init();
@@ -677,7 +681,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
             if (threadIdx.x == 0 && tl < ntiles) {
                 const unsigned run = (unsigned)((size_t)TL * H * sizeof(C));
                 fence_proxy_async();   // the staging reads of the previous tile come first
-                mbar_arrive_expect_tx(&zbar, (unsigned)(nf * 3) * run + plant);
+                // + the test hook's planted bytes (0 in normal runs)
+                mbar_arrive_expect_tx(&zbar, (unsigned)(nf * 3) * run + (unsigned)bg->wait_plant);
                 for (int a = 0; a < nf * 3; ++a) {
                     const int fl = a >= 3 ? 1 : 0, w = a - 3 * fl;
                     const C *src = (w == 0 ? TA : (w == 1 ? TB : TC)) + (long long)fl * g.modes +
@@ -711,9 +716,12 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
     T pot_t[kMaxTerms] = {T(0), T(0)};
     double pot_d[kMaxTerms] = {0.0, 0.0};
     int nfold = 0;
-    // the sums run over V(site) - vref (model_potential_shifted), vref the thread's first site
-    T vref[kMaxTerms] = {T(0), T(0)};
-    int nsite = 0;
+    // the sums run over V(site) - vref (model_potential_shifted), vref the potential terms of
+    // the homogeneous fields (the FP64 shadow of the zero modes / N^3), a value of the state
+    // alone; vref is added back once per site summed (every tile gives a thread the same
+    // number of sites: the line count is a multiple of the tile's)
+    T vref[kMaxTerms];
+    homogeneous_potential<T>(mdl, bg, vref);
     if (STAGED) prefetch(blockIdx.x);
     unsigned phase = 0;   // parity of the bulk-copy phase the next tile completes
     for (int tile = blockIdx.x; tile < ntiles; tile = STAGED ? tile + gridDim.x : ntiles) {
@@ -725,7 +733,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
             const ZIdx<L> ix{(int)(grp * slot_elems + t * LS)};
             const long long lo = (long long)line * H;
             if (bulk) {
-                const bool ok = mbar_wait_bounded(&zbar, phase, wait_ns);
+                const bool ok = mbar_wait_bounded(&zbar, phase, bg->wait_ns);
                 if (__syncthreads_or(!ok)) {
                     // The tile's copies did not complete in time. Only this tile's copies can
                     // be in flight (the next tile's are issued after this wait), and the block
@@ -738,9 +746,9 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
                     int *err = &const_cast<DevBG *>(bg)->err;
                     if (threadIdx.x == 0) {
                         report_err(err, PSC_ERR_TIMEOUT);
-                        if (plant) mbar_complete_tx(&zbar, plant);
+                        if (bg->wait_plant) mbar_complete_tx(&zbar, (unsigned)bg->wait_plant);
                     }
-                    const bool landed = mbar_wait_bounded(&zbar, phase, wait_ns);
+                    const bool landed = mbar_wait_bounded(&zbar, phase, bg->wait_ns);
                     if (__syncthreads_or(!landed) && threadIdx.x == 0) report_err(err, PSC_ERR_DEVICE);
                     return;
                 }
@@ -809,7 +817,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
             }
             T vp[2] = {T(0), T(0)};
             model_dvdf<T>(mdl, f, vp, nf);
-            model_potential_shifted<T, T>(mdl, f, vref, pot_t, &nsite);
+            model_potential_shifted<T, T>(mdl, f, vref, pot_t);
             T o[8];
             const int si[6] = {0, 0, 0, 1, 1, 2}, sj[6] = {0, 1, 2, 1, 2, 2};
             o[0] = vp[0];
@@ -904,7 +912,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
     }
     if (STAGED) cp_async_wait_all();
 #pragma unroll
-    for (int i = 0; i < kMaxTerms; ++i) pot_d[i] += (double)pot_t[i] + (double)nsite * (double)vref[i];
+    const double nsite = (double)nfold * ((TL * L - 1 - (int)threadIdx.x) / (int)blockDim.x + 1);
+    for (int i = 0; i < kMaxTerms; ++i) pot_d[i] += (double)pot_t[i] + nsite * (double)vref[i];
     block_reduce_store_t<double, kMaxTerms>(pot_d, partV, gridDim.x, blockIdx.x);
 }
 
