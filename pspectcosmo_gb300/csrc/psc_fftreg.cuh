@@ -44,7 +44,7 @@ struct RegPlan {
     __device__ __forceinline__ static int out(int j, int q, int r) { return (j * NBL + q) + r * NSL; }
 };
 
-template <typename C, int L, int DIR, int S, typename IX>
+template <typename C, int L, int DIR, int S, bool PK, typename IX>
 __device__ __forceinline__ void reg_stage(C (&v)[16], C *sm, const IX &ix, int j, const C *__restrict__ tw,
                                           int twmul, bool act) {
     constexpr int R = reg_rad(L, S), NS = reg_span(L, S), NB = 16 / R, LR = L / R;
@@ -63,7 +63,7 @@ __device__ __forceinline__ void reg_stage(C (&v)[16], C *sm, const IX &ix, int j
             if (DIR > 0) w.y = -w.y;
             u[r] = cmul(u[r], w);
         }
-        dft<R, DIR>(u);
+        dft<R, DIR, C, PK>(u);
 #pragma unroll
         for (int r = 0; r < R; ++r) v[q * R + r] = u[r];
     }
@@ -77,7 +77,7 @@ __device__ __forceinline__ void reg_stage(C (&v)[16], C *sm, const IX &ix, int j
                 for (int r = 0; r < R; ++r) sm[ix(idxD + r * NS)] = v[q * R + r];
             }
         }
-        reg_stage<C, L, DIR, S + 1>(v, sm, ix, j, tw, twmul, act);
+        reg_stage<C, L, DIR, S + 1, PK>(v, sm, ix, j, tw, twmul, act);
     }
 }
 
@@ -87,18 +87,18 @@ __device__ __forceinline__ void reg_stage(C (&v)[16], C *sm, const IX &ix, int j
 // synchronizes after any earlier use); on return the last stage has read it, so
 // the caller synchronizes again before writing it. `act` = false runs the
 // barriers without touching memory (threads without a line this round).
-// Twiddles: tw[q] = e^{-2 pi i q / (L twmul)}.
-template <typename C, int L, int DIR, typename IX>
+// Twiddles: tw[q] = e^{-2 pi i q / (L twmul)}. PK: packed FP32 butterflies (cadd_k).
+template <typename C, int L, int DIR, bool PK = false, typename IX>
 __device__ __forceinline__ void fft_reg(C (&v)[16], C *sm, const IX &ix, int j, const C *__restrict__ tw, int twmul,
                                         bool act = true) {
     static_assert(L >= 16 && (L & (L - 1)) == 0 && L <= 1024, "line length");
-    dft<16, DIR>(v);
+    dft<16, DIR, C, PK>(v);
     if constexpr (reg_nstages(L) > 1) {
         if (act) {
 #pragma unroll
             for (int r = 0; r < 16; ++r) sm[ix(j * 16 + r)] = v[r];
         }
-        reg_stage<C, L, DIR, 1>(v, sm, ix, j, tw, twmul, act);
+        reg_stage<C, L, DIR, 1, PK>(v, sm, ix, j, tw, twmul, act);
     }
 }
 

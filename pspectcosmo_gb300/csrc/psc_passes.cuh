@@ -520,12 +520,12 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
             }
             __syncthreads();   // every thread has read the staging area
             prefetch(tile + gridDim.x);
-            fft_reg<C, L, +1>(v, slots, ix, j, tw, N / L);
+            fft_reg<C, L, +1, true>(v, slots, ix, j, tw, N / L);
             __syncthreads();
 #pragma unroll
             for (int q = 0; q < RP::NBL; ++q)
 #pragma unroll
-                for (int r = 0; r < RP::RL; ++r) slots[ix(RP::out(j, q, r))] = cscale(v[q * RP::RL + r], inv_n3);
+                for (int r = 0; r < RP::RL; ++r) slots[ix(RP::out(j, q, r))] = cscale_k<true>(v[q * RP::RL + r], inv_n3);
         }
         __syncthreads();
 
@@ -574,7 +574,7 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
 #pragma unroll
         for (int r = 0; r < 16; ++r) v[r] = slots[ix(j + r * P)];
         __syncthreads();   // all loads precede the first exchange write
-        fft_reg<C, L, -1>(v, slots, ix, j, tw, N / L);
+        fft_reg<C, L, -1, true>(v, slots, ix, j, tw, N / L);
         {
             // the partners Z[M-k] by warp shuffle, X[k] straight out
             C *dst = QV + (long long)grp * g.modes + (long long)line * H;
@@ -585,8 +585,8 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
                     const int k = RP::out(j, q, r);
                     const C zk = v[q * RP::RL + r];
                     const C zc = partner_out<C, M>(v, j, q, r);
-                    const C ev = cscale(cadd(zk, zc), T(0.5));
-                    const C dd = cscale(csub(zk, zc), T(0.5));
+                    const C ev = cscale_k<true>(cadd_k<true>(zk, zc), T(0.5));
+                    const C dd = cscale_k<true>(csub_k<true>(zk, zc), T(0.5));
                     const C od = mk<T>(dd.y, -dd.x);
                     const C w = __ldg(&tw[k]);
                     if (valid) dst[k] = cadd(ev, cmul(w, od));
@@ -782,12 +782,12 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
                 __syncthreads();   // every staging read of this tile is done
                 prefetch(tile + gridDim.x);
             }
-            fft_reg<C, L, +1>(v, slots, ix, j, tw, N / L);
+            fft_reg<C, L, +1, true>(v, slots, ix, j, tw, N / L);
             __syncthreads();
 #pragma unroll
             for (int q = 0; q < RP::NBL; ++q)
 #pragma unroll
-                for (int r = 0; r < RP::RL; ++r) slots[ix(RP::out(j, q, r))] = cscale(v[q * RP::RL + r], inv_n3);
+                for (int r = 0; r < RP::RL; ++r) slots[ix(RP::out(j, q, r))] = cscale_k<true>(v[q * RP::RL + r], inv_n3);
         }
         __syncthreads();
         // 2. pointwise epilogue per site: V'(f), <V>, anisotropic stress
@@ -857,7 +857,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
 #pragma unroll
             for (int r = 0; r < 16; ++r) v[r] = act ? slots[ix(j + r * P)] : mk<T>(0, 0);
             __syncthreads();   // all loads of this round precede the first exchange write
-            fft_reg<C, L, -1>(v, slots, ix, j, tw, N / L, act);
+            fft_reg<C, L, -1, true>(v, slots, ix, j, tw, N / L, act);
             {
                 const int r0 = 2 * o, r1 = 2 * o + 1;
                 auto arr = [&](int ri) -> C * {
@@ -879,8 +879,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
                             const C zk = v[q * RP::RL + r];
                             const C zc = partner_out<C, L>(v, j, q, r);   // conj Z[N - k]
                             if (wr && k <= HL) {
-                                const C ev = cscale(cadd(zk, zc), T(0.5));
-                                const C dd = cscale(csub(zk, zc), T(0.5));
+                                const C ev = cscale_k<true>(cadd_k<true>(zk, zc), T(0.5));
+                                const C dd = cscale_k<true>(csub_k<true>(zk, zc), T(0.5));
                                 d0[k] = ev;
                                 if (d1) d1[k] = mk<T>(dd.y, -dd.x);
                             }
@@ -899,8 +899,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
                     if (wr) {
                         for (int k = j; k <= HL; k += P) {
                             const C zk = slots[ix(k)], zc = cconj(slots[ix((L - k) & (L - 1))]);
-                            const C ev = cscale(cadd(zk, zc), T(0.5));
-                            const C dd = cscale(csub(zk, zc), T(0.5));
+                            const C ev = cscale_k<true>(cadd_k<true>(zk, zc), T(0.5));
+                            const C dd = cscale_k<true>(csub_k<true>(zk, zc), T(0.5));
                             d0[k] = ev;
                             if (d1) d1[k] = mk<T>(dd.y, -dd.x);
                         }
