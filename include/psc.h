@@ -65,7 +65,9 @@ typedef struct psc_params {
     int expansion;          /* parameters.h:67   must be 2 (self-consistent Friedmann) for evolution */
     int simulate_inflation; /* parameters.h:17   fixed-amplitude ICs + R_Q2C mask in K, G */
     int spectral;           /* parameters.h:12   1: evolve_VV_k_nopad semantics, 0: evolve_VV (real space) */
-    int with_gw;            /* parameters.h:15   evolve the tensor perturbations u_ij (needs spectral = 0) */
+    int with_gw;            /* parameters.h:15   tensor perturbations u_ij: evolved on the real-space path
+                               (spectral = 0); on the spectral path they keep their initial values
+                               and appear in the GW spectra, as the reference does */
     int precision;          /* 64: FP64 state (the plain method) or 32: FP32 state, FP64 background */
     int model;              /* PSC_MODEL_* (model.h) */
     int seed;               /* parameters.h:65   Park-Miller seed (rand_uniform, initialize.cpp:13) */

@@ -42,6 +42,8 @@ CONFIGS: dict[str, tuple[str, dict[str, str]]] = {
     "spec1_n16": ("phi2", {"N": "16"}),
     "spec1_n32_vv4": ("phi2", {"N": "32", "VV": "4"}),
     "spec1_n16_vv6": ("phi2", {"N": "16", "VV": "6"}),
+    "spec1_n16_vv8": ("phi2", {"N": "16", "VV": "8"}),
+    "spec1_n16_vv10": ("phi2", {"N": "16", "VV": "10"}),
     "spec1_n64": ("phi2", {}),
     # two-field preheating (phi0 = 0.193 MPl, phidot0 = -0.142 m MPl, kIR = 1 m)
     "spec2_n16_vv4": ("phi2chi2", {
@@ -94,6 +96,14 @@ CONFIGS: dict[str, tuple[str, dict[str, str]]] = {
     }),
     "gw1_n16_vv2": ("phi2", {
         "N": "16", "VV": "2", "SPECTRAL_FLAG": "false", "WITH_GW": "true",
+    }),
+    # the spectral step with WITH_GW on: u_k is set by initialize_GW() and never evolved,
+    # and spectra() still writes the GW spectra of those modes
+    "specgw2_n16_vv4": ("phi2chi2", {
+        "N": "16", "VV": "4", "nflds": "2", "kIR": "1",
+        "SPECTRAL_FLAG": "true", "WITH_GW": "true",
+        "initfield[]": "{0.193 * MPl, 0.}",
+        "initderivs[]": "{-0.142e-6 * MPl * MPl, 0.}",
     }),
 }
 

@@ -506,6 +506,8 @@ int check(psc_handle *h, int obs) {
         return fail(PSC_ERR_CONFIG, "the adjoint differentiates the unmasked step (spectral = 0 or simulate_inflation = 0)");
     if (p.expansion != 2) return fail(PSC_ERR_CONFIG, "the adjoint needs self-consistent expansion (expansion = 2)");
     if (obs == PSC_OBS_RHO_GW && !p.with_gw) return fail(PSC_ERR_CONFIG, "the rho_GW observable needs with_gw = 1");
+    if (p.with_gw && p.spectral)
+        return fail(PSC_ERR_CONFIG, "the adjoint differentiates evolved GW tensors (spectral = 0 with GWs)");
     if (p.with_gw && h->cfg.g.N > 512) return fail(PSC_ERR_CONFIG, "the adjoint with GWs needs N <= 512");
     if (p.model == PSC_MODEL_PHI2CHI2 && !(p.gsq > 0)) return fail(PSC_ERR_CONFIG, "the adjoint needs gsq > 0");
     if (!h->have_state) return fail(PSC_ERR_STATE, "no state: call psc_init_ic or psc_set_state first");

@@ -120,8 +120,6 @@ int validate(const psc_params *p) {
     if (p->vv != 2 && p->vv != 4 && p->vv != 6 && p->vv != 8 && p->vv != 10)
         return fail(PSC_ERR_CONFIG, "vv must be 2, 4, 6, 8 or 10");
     if (p->precision != 32 && p->precision != 64) return fail(PSC_ERR_CONFIG, "precision must be 32 or 64");
-    if (p->with_gw && p->spectral)
-        return fail(PSC_ERR_CONFIG, "GWs are evolved on the real-space path only (spectral = 0), as in the reference");
     if (p->N_pad != 0) {
         if (!p->spectral || p->with_gw)
             return fail(PSC_ERR_CONFIG, "the padded step (N_pad) is the spectral step without GWs, as in the reference");
@@ -519,7 +517,7 @@ int create_handle(const psc_params *ps, int R, psc_handle **out) {
     // evaluates the opening force every call)
     if (g.reg || h->padded) {
         if ((rc = dalloc(h, &b.Fk, farr))) return bail(rc);
-        if (g.gw && (rc = dalloc(h, &b.Fu, garr))) return bail(rc);
+        if (g.gwev && (rc = dalloc(h, &b.Fu, garr))) return bail(rc);
     }
     if (h->padded) {
         // N_pad-grid arrays: padded spectra (zero outside the band, written in-band each
@@ -1152,7 +1150,7 @@ int psc_test_wait_hook(psc_handle *h, double limit_ms, int plant_bytes) {
     if (!h || !(limit_ms > 0.0) || limit_ms > 10000.0 || plant_bytes < 0 || plant_bytes > 4096)
         return fail(PSC_ERR_ARG, "bad argument");
     const psc::Geo &g = h->cfg.g;
-    const bool bulk = g.gw && g.reg && h->p0().precision == 32 &&
+    const bool bulk = g.gwev && g.reg && h->p0().precision == 32 &&
                       ((size_t(1) << g.tlz_shift) * (size_t)g.H * h->csize) % 16 == 0;
     if (plant_bytes && !bulk)
         return fail(PSC_ERR_CONFIG, "the handle's GW Z pass does not stage its tiles by bulk copies");
@@ -1171,7 +1169,7 @@ int psc_pass_bytes(psc_handle *h, double *bytes) {
     if (!h || !bytes) return fail(PSC_ERR_ARG, "bad argument");
     const psc::Geo &g = h->cfg.g;
     const double C = (double)g.modes * h->csize * h->R;
-    const int nf = g.nf, gw = g.gw;
+    const int nf = g.nf, gw = g.gwev;
     // X inverse: read f_k, pi_half; write f_k, TA [, TB]
     bytes[0] = nf * (4 + gw) * C;
     // Y inverse: read TA [, TB]; write TA [, TB, TC]

@@ -830,6 +830,7 @@ void plan(const psc_params &p, int R, LaunchCfg *cfg) {
     g.M = p.N / 2;
     g.nf = p.nflds;
     g.gw = p.with_gw ? 1 : 0;
+    g.gwev = (p.with_gw && !p.spectral) ? 1 : 0;
     g.model = p.model;
     g.nterms = p.model == PSC_MODEL_PHI2 ? 1 : 2;
     g.mask = (p.spectral && p.simulate_inflation) ? 1 : 0;
@@ -843,7 +844,7 @@ void plan(const psc_params &p, int R, LaunchCfg *cfg) {
     g.fstride = (long long)g.nf * g.modes;
     g.gstride = g.gw ? 6LL * g.modes : 0;
     const int csize = p.precision == 32 ? 8 : 16;
-    const int nin = g.nf * (g.gw ? 4 : 1), nout = g.nf + (g.gw ? 6 : 0);
+    const int nin = g.nf * (g.gwev ? 4 : 1), nout = g.nf + (g.gwev ? 6 : 0);
     const int nslot = nin > nout ? nin : nout;
     if (g.reg) {
         // register engine: P = L/16 threads per line, 256 threads per block (512 for FP32
@@ -868,8 +869,8 @@ void plan(const psc_params &p, int R, LaunchCfg *cfg) {
         // half-length lines, persistent (2 blocks per SM). With GWs (kr_zpass_gw): four
         // slots of N-point lines and, in FP32 (persistent, 3 blocks per SM, next tile
         // staged), the nf x 3 input lines of a tile; in FP64 one tile per block.
-        const bool gw_staged = g.gw && p.precision == 32;
-        if (g.gw)
+        const bool gw_staged = g.gwev && p.precision == 32;
+        if (g.gwev)
             cfg->smem_z = ((size_t)4 * tlz * (g.N + g.N / 16 + 1) +
                            (gw_staged ? (size_t)g.nf * 3 * tlz * (g.M + 2) : 0)) * csize;
         else
@@ -883,7 +884,7 @@ void plan(const psc_params &p, int R, LaunchCfg *cfg) {
         int per_sm = (int)(smem_sm / cfg->smem_z);
         if (per_sm > (gw_staged ? 3 : 2)) per_sm = gw_staged ? 3 : 2;
         if (per_sm < 1) per_sm = 1;
-        cfg->nbz = ((g.gw && !gw_staged) || ntiles < per_sm * sms) ? ntiles : per_sm * sms;
+        cfg->nbz = ((g.gwev && !gw_staged) || ntiles < per_sm * sms) ? ntiles : per_sm * sms;
         g.pkg_stride = 2 * kMaxFields * cfg->nbx;
         g.pv_stride = kMaxTerms * cfg->nbz;
         return;
@@ -955,7 +956,7 @@ static cudaError_t launch_stage_t(const LaunchCfg &cfg, const Buffers &b, int dr
         if (ev) cudaEventRecord(ev[i], st);
     };
     mark(0);
-    if (g.gw) {
+    if (g.gwev) {
         if (drift) k_ifft_x<T, true, true><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
         else k_ifft_x<T, true, false><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
         mark(1);
@@ -977,7 +978,7 @@ static cudaError_t launch_stage_t(const LaunchCfg &cfg, const Buffers &b, int dr
         al.rs[nj] = g.fstride;
         al.p[nj++] = QV + (long long)f * g.modes;
     }
-    if (g.gw)
+    if (g.gwev)
         for (int c = 0; c < 6; ++c) {
             al.rs[nj] = g.gstride;
             al.p[nj++] = QS + (long long)c * g.modes;
@@ -985,7 +986,7 @@ static cudaError_t launch_stage_t(const LaunchCfg &cfg, const Buffers &b, int dr
     k_fft_y<T><<<dim3(cfg.nbx, nj, R), cfg.thr_xy, cfg.smem_xy, st>>>(g, al, tw);
     mark(4);
     const dim3 gf(cfg.nbx, nj, R);
-    if (g.gw) k_fft_x_final<T, true><<<gf, cfg.thr_xy, cfg.smem_xy, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw);
+    if (g.gwev) k_fft_x_final<T, true><<<gf, cfg.thr_xy, cfg.smem_xy, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw);
     else k_fft_x_final<T, false><<<gf, cfg.thr_xy, cfg.smem_xy, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw);
     mark(5);
     if (scalar_mode >= 0) {
@@ -1051,7 +1052,7 @@ __global__ void __launch_bounds__(256) k_open_kick(Geo g, cplx<T> *__restrict__ 
 
 cudaError_t launch_open_kick(const LaunchCfg &cfg, const Buffers &b, int precision, cudaStream_t st) {
     const Geo &g = cfg.g;
-    const dim3 grid(2 * 152, g.nf + (g.gw ? 6 : 0), cfg.R);
+    const dim3 grid(2 * 152, g.nf + (g.gwev ? 6 : 0), cfg.R);
     if (precision == 32)
         k_open_kick<float><<<grid, 256, 0, st>>>(g, (float2 *)b.pk, (const float2 *)b.Fk, (float2 *)b.puk,
                                                  (const float2 *)b.Fu, b.bg);

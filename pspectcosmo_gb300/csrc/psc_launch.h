@@ -15,7 +15,9 @@ struct DevAdj;
 // Lattice geometry and tiling, passed by value to every pass kernel.
 struct Geo {
     int N, H, M;                 // edge, half-spectrum length N/2+1, N/2
-    int nf, gw, nterms, mask;    // fields, GW flag, potential terms, R_Q2C mask on
+    int nf, gw, nterms, mask;    // fields, GW tensors held, potential terms, R_Q2C mask on
+    int gwev;                    // the step evolves the GW tensors (the real-space path; on the
+                                 // spectral path they stay as initialised, as in the reference)
     int model;                   // PSC_MODEL_*
     int reg;                     // 1: register-engine passes (N >= 32), 0: generic shared-memory engine
     int tlx_shift, tlz_shift;    // log2 lines per tile: X/Y passes, Z pass

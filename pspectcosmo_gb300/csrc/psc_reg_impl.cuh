@@ -74,7 +74,7 @@ struct RegLaunch {
             if (ev) cudaEventRecord(ev[i], st);
         };
         mark(0);
-        if (g.gw) {
+        if (g.gwev) {
             if (drift) kr_ifft_x<T, N, true, true><<<gx, txy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
             else kr_ifft_x<T, N, true, false><<<gx, txy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
             mark(1);
@@ -98,7 +98,7 @@ struct RegLaunch {
             al.rs[nj] = g.fstride;
             al.p[nj++] = QV + (long long)f * g.modes;
         }
-        if (g.gw)
+        if (g.gwev)
             for (int c = 0; c < 6; ++c) {
                 al.rs[nj] = g.gstride;
                 al.p[nj++] = QS + (long long)c * g.modes;
@@ -106,7 +106,7 @@ struct RegLaunch {
         kr_fft_y<T, N><<<dim3(cfg.nbx, nj, R), txy, cfg.smem_xy, st>>>(g, al, tw);
         mark(4);
         const dim3 gf(cfg.nbx, nj, R);
-        if (g.gw)
+        if (g.gwev)
             kr_fft_x_final<T, N, true><<<gf, txy, cfg.smem_xf, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw,
                                                                       (C *)b.tape_f, (C *)b.tape_p, (C *)b.tape_vp,
                                                                       (C *)b.tape_pu, (C *)b.tape_fu, (C *)b.Fk,

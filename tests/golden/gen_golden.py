@@ -26,6 +26,9 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 RUNS = {
     "spec1_n16": ("spec1_n16", 20, 0.002, 10, True),
     "spec1_n16_vv6": ("spec1_n16_vv6", 10, 0.002, 5, True),
+    "spec1_n16_vv8": ("spec1_n16_vv8", 10, 0.002, 5, True),
+    "spec1_n16_vv10": ("spec1_n16_vv10", 10, 0.002, 5, True),
+    "specgw2_n16_vv4": ("specgw2_n16_vv4", 10, 0.005, 5, True),
     "spec1_n32_vv4": ("spec1_n32_vv4", 20, 0.001, 10, False),
     "spec1_n64_dt2e-3": ("spec1_n64", 1000, 0.002, 50, False),
     "spec1_n64_dt1e-4": ("spec1_n64", 200, 0.0001, 50, False),

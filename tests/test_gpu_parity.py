@@ -22,8 +22,8 @@ from golden_util import load, output_rows, params_for, rel
 
 pytestmark = pytest.mark.gpu
 
-RUNS = ["spec1_n16", "spec1_n16_vv6", "spec1_n32_vv4", "spec1_n64_dt1e-4", "spec2_n16_vv4", "spec2_n32_vv2",
-        "gw1_n16_vv2", "gw2_n16_vv4"]
+RUNS = ["spec1_n16", "spec1_n16_vv6", "spec1_n16_vv8", "spec1_n16_vv10", "spec1_n32_vv4", "spec1_n64_dt1e-4",
+        "spec2_n16_vv4", "spec2_n32_vv2", "gw1_n16_vv2", "gw2_n16_vv4", "specgw2_n16_vv4"]
 
 FP32_FIELD_TOL = 2e-4
 FP32_SPEC_TOL = 1e-4

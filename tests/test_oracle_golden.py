@@ -10,7 +10,7 @@ import pytest
 from golden_util import ALL_RUNS, load, output_rows, params_for, rel
 
 FAST = ["spec1_n16", "spec1_n16_vv6", "spec1_n32_vv4", "spec1_n64_dt1e-4", "spec2_n16_vv4", "spec2_n32_vv2",
-        "gw2_n16_vv4", "gw1_n16_vv2"]
+        "gw2_n16_vv4", "gw1_n16_vv2", "spec1_n16_vv8", "spec1_n16_vv10", "specgw2_n16_vv4"]
 
 
 @pytest.fixture(scope="module")
