@@ -211,8 +211,51 @@ def cpu_sample(p, dt, budget_s: float = 20.0, threads: int | None = None) -> dic
             break
     per_step = el / done * s
     return {"value": p.sites / per_step, "unit": "site-steps/s", "cores": threads, "kind": "port",
+            "stages_timed": done,
             "sample": f"{done} Yoshida stage(s) of the {p.N}^3 lattice ({s} per step) in {el:.1f} s, FP64 "
                       f"restatement (oracle/port) with {threads} threads"}
+
+
+REF_BENCH_CONFIG = "bench_gw2_n256_vv4"   # oracle/build_ref.py: the headline workload on the reference's code
+
+
+def reference_sample(p, dt, nsteps: int = 1) -> dict | None:
+    """The reference's OWN evolve_VV (its sources, prepared in oracle/_ref by
+    oracle/build_ref.py and compiled here against the FFTW API shim) timed for `nsteps` steps
+    of the headline workload on this host's cores: initial conditions, then the steps on the
+    wall clock. None when the prepared sources are absent or the build fails."""
+    if (p.N, p.nflds, p.with_gw, p.spectral, p.vv) != (256, 2, 1, 0, 4):
+        return None
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    try:
+        import build_ref
+
+        if not build_ref.prepared(REF_BENCH_CONFIG) and not build_ref.reference_available():
+            return None
+        exe = os.path.join(build_ref.OUT, REF_BENCH_CONFIG, "harness")
+        if not os.path.exists(exe) or os.path.getmtime(exe) < os.path.getmtime(
+                os.path.join(build_ref.OUT, REF_BENCH_CONFIG, "parameters.h")):
+            exe = build_ref.build(REF_BENCH_CONFIG)
+        import tempfile
+
+        with tempfile.TemporaryDirectory() as tmp:
+            env = dict(os.environ, PSC_HARNESS_STACK_GB="16")
+            # initialize() waits for a key press (initialize.cpp:681): give it one
+            r = subprocess.run([exe, "time", str(nsteps), repr(dt)], cwd=tmp, env=env, input="\n",
+                               capture_output=True, text=True, timeout=900)
+        line = [ln for ln in r.stdout.splitlines() if ln.startswith("steps ")]
+        if r.returncode != 0 or not line:
+            return None
+        f = line[-1].split()
+        sps, threads = float(f[5]), int(f[7])
+    except (Exception, SystemExit):
+        return None
+    return {"value": p.sites / sps, "unit": "site-steps/s", "cores": threads, "kind": "reference",
+            "steps_timed": nsteps,
+            "sample": f"{nsteps} step(s) ({p.stages} Yoshida stages each) of the {p.N}^3 lattice in {sps * nsteps:.1f} s: "
+                      f"the reference's own evolve_VV (evolution.cpp:607-694) and initialize(), compiled with "
+                      f"g++ -O2 against the FFTW API shim (FFTW is not installed); FFTs on {threads} threads, "
+                      f"the rest single-threaded as in the reference"}
 
 
 def run_reference(args):
@@ -220,10 +263,14 @@ def run_reference(args):
     if rank != 0:
         return
     p, dt, desc = make_params(args.config, args.precision)
-    budget = max(5.0, min(120.0, 8.0 * args.steps))
-    cs = cpu_sample(p, dt, budget_s=budget)
+    cs = reference_sample(p, dt, 1)
+    if cs is None:   # no prepared reference sources for this workload: the C restatement
+        budget = max(5.0, min(120.0, 8.0 * args.steps))
+        cs = cpu_sample(p, dt, budget_s=budget)
+    timed_steps = cs.get("steps_timed", cs.get("stages_timed", 0) / max(1, p.stages))
     line = {"impl": "reference", "metric": "site-steps/s", "value": cs["value"], "unit": "site-steps/s",
-            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "n_gpus": args.gpus, "steps": timed_steps, "steps_requested": args.steps, "warmup": 0,
+            "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (reference seeded ICs)",
             "config": {"workload": desc, "N": p.N, "nflds": p.nflds, "gw": bool(p.with_gw), "vv": p.vv,
                        "dt": dt, "parallelism": "cpu threads"},
@@ -560,6 +607,7 @@ def run_ours(args):
     if rank == 0:
         yard = None if big else fft_yardstick(lat, p)
         cpu = cpu_sample(p, dt, budget_s=20.0) if (world == 1 and not args.no_cpu and not big) else None
+        cpu_ref = reference_sample(p, dt, 1) if (world == 1 and not args.no_cpu and not big) else None
         line = {
             "metric": "site-steps/s", "value": value, "unit": "site-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -581,6 +629,7 @@ def run_ours(args):
             "fft_yardstick": yard,
             "fp32_vs_fp64_trajectory": traj,
             "cpu_baseline": cpu,
+            "cpu_baseline_reference": cpu_ref,
             "clocks": clk,
             "gpu_launches": gpu_launches,
         }
@@ -602,10 +651,10 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--fp64-steps", type=int, default=None,
                     help="also run FP32 and FP64 lattices this many steps side by side and report the errors "
-                         "(default: 2000 for preheat_gw_256, 0 otherwise)")
+                         "(default: 1000 for preheat_gw_256, 0 otherwise)")
     args = ap.parse_args()
     if args.fp64_steps is None:
-        args.fp64_steps = 2000 if args.config == "preheat_gw_256" else 0
+        args.fp64_steps = 1000 if args.config == "preheat_gw_256" else 0
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":

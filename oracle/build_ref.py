@@ -20,6 +20,7 @@ fixtures are generated. Usage: python oracle/build_ref.py [config ...]
 from __future__ import annotations
 
 import os
+import platform
 import re
 import shutil
 import subprocess
@@ -87,6 +88,14 @@ CONFIGS: dict[str, tuple[str, dict[str, str]]] = {
         "initfield[]": "{0.193 * MPl, 0.}",
         "initderivs[]": "{-0.142e-6 * MPl * MPl, 0.}",
     }),
+    # the benchmark workload on the reference's own code (timed, not dumped): 256^3 two-field
+    # preheating with GWs, Yoshida-4, real-space step
+    "bench_gw2_n256_vv4": ("phi2chi2", {
+        "N": "256", "VV": "4", "nflds": "2", "kIR": "1",
+        "SPECTRAL_FLAG": "false", "WITH_GW": "true",
+        "initfield[]": "{0.193 * MPl, 0.}",
+        "initderivs[]": "{-0.142e-6 * MPl * MPl, 0.}",
+    }),
     # real-space pseudo-spectral path with gravitational waves (evolve_VV)
     "gw2_n16_vv4": ("phi2chi2", {
         "N": "16", "VV": "4", "nflds": "2", "kIR": "1",
@@ -126,7 +135,15 @@ def make_parameters(text: str, overrides: dict[str, str]) -> str:
     return text
 
 
-def build(name: str) -> str:
+def prepared(name: str) -> bool:
+    """True when oracle/_ref/<name> holds the copied sources and headers (they travel with
+    the repository's working tree to a machine without the reference checkout)."""
+    d = os.path.join(OUT, name)
+    return all(os.path.exists(os.path.join(d, f)) for f in SOURCES + ["pspectcosmo.h", "parameters.h", "model.h"])
+
+
+def prepare(name: str) -> str:
+    """Steps 1-3: the reference's sources and the per-config headers into oracle/_ref/<name>."""
     model, overrides = CONFIGS[name]
     d = os.path.join(OUT, name)
     os.makedirs(d, exist_ok=True)
@@ -140,10 +157,24 @@ def build(name: str) -> str:
         shutil.copyfile(os.path.join(REF, "model.h"), os.path.join(d, "model.h"))
     else:
         shutil.copyfile(os.path.join(HERE, "models", f"model_{model}.h"), os.path.join(d, "model.h"))
+    return d
+
+
+def build(name: str) -> str:
+    """Steps 1-4: prepare (where the reference checkout exists) and compile; returns the
+    harness path. Without the checkout, compiles what prepare() left in oracle/_ref/<name>."""
+    d = os.path.join(OUT, name)
+    if reference_available():
+        prepare(name)
+    elif not prepared(name):
+        raise SystemExit(f"{d}: neither the reference checkout nor prepared sources")
 
     shim = os.path.join(HERE, "shim")
     cxx = ["g++", "-O2", "-std=c++17", "-fopenmp", "-w", "-I", d, "-I", shim,
            "-include", os.path.join(shim, "prec_override.h")]
+    if int(CONFIGS[name][1].get("N", "64")) >= 128:
+        # the reference's static N^3 arrays exceed the small code model's 2-4 GB of data
+        cxx.append("-mcmodel=large" if platform.machine() in ("aarch64", "arm64") else "-mcmodel=medium")
     objs = []
     jobs = []
     for s in SOURCES:

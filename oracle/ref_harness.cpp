@@ -27,7 +27,9 @@
  */
 #include "pspectcosmo.h"
 
+#include <omp.h>
 #include <pthread.h>
+#include <chrono>
 #include <algorithm>
 #include <complex>
 #include <vector>
@@ -161,6 +163,47 @@ static void *run(void *) {
     return nullptr;
 }
 
+// timing mode: initialize() [+ initialize_GW()], then g_nsteps steps of g_dt timed on the
+// wall clock, with no output; prints the seconds per step. The FFTs (the reference's only
+// threaded part, pspectcosmo.cpp:251) use every host core.
+static void *run_timing(void *) {
+    fftw_init_threads();
+    fftw_plan_with_nthreads(std::max(1, omp_get_max_threads()));
+    const size_t modes = (size_t)N * N * (N / 2 + 1);
+    Cache_Data_k = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes);
+    R_k = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes);
+    for (int fld = 0; fld < nflds; fld++) {
+        f_k[fld] = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes);
+        pi_k[fld] = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes);
+#if SPECTRAL_FLAG
+        pi_k_half[fld] = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes);
+        V_prime_k[fld] = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes);
+        kernel_f_k[fld] = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes);
+#endif
+    }
+#if WITH_GW
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            u_k[i][j] = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes);
+            pi_u_k[i][j] = (fftw_complex *)fftw_malloc(sizeof(fftw_complex) * modes);
+        }
+#endif
+    dt = g_dt;
+    t0 = 0.;
+    t = t0;
+    a = a0;
+    initialize();
+#if WITH_GW
+    initialize_GW();
+#endif
+    const auto t_start = std::chrono::steady_clock::now();
+    for (long s = 1; s <= g_nsteps; s++) step_once(g_dt);
+    const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+    std::printf("steps %ld seconds %.6f seconds_per_step %.6f threads %d a %.17g\n", g_nsteps, el,
+                el / (double)g_nsteps, omp_get_max_threads(), a);
+    return nullptr;
+}
+
 int reference_main();   // the reference's own main() (pspectcosmo.cpp:236), renamed at compile time
 
 static void *run_reference_main(void *) {
@@ -232,6 +275,21 @@ int main(int argc, char **argv) {
         return 0;
     }
 #endif
+    // the worker thread's stack: the real-space path keeps N^3 arrays on the stack
+    // (evolution.cpp:612, 441, 581); PSC_HARNESS_STACK_GB raises it for large lattices
+    const char *sgb = std::getenv("PSC_HARNESS_STACK_GB");
+    const size_t stack = (size_t)(sgb ? std::max(1, std::atoi(sgb)) : 2) << 30;
+    if (argc == 4 && std::string(argv[1]) == "time") {
+        g_nsteps = std::max(1L, std::atol(argv[2]));
+        g_dt = std::atof(argv[3]);
+        pthread_attr_t attr;
+        pthread_attr_init(&attr);
+        pthread_attr_setstacksize(&attr, stack);
+        pthread_t th;
+        if (pthread_create(&th, &attr, run_timing, nullptr) != 0) return 3;
+        pthread_join(th, nullptr);
+        return 0;
+    }
     if (argc == 2 && std::string(argv[1]) == "main") {
         // the reference's own driver: adaptive dt, output cadence (pspectcosmo.cpp:600-697)
         pthread_attr_t attr;
@@ -252,7 +310,7 @@ int main(int argc, char **argv) {
     if (g_every < 1) g_every = 1;
     pthread_attr_t attr;
     pthread_attr_init(&attr);
-    pthread_attr_setstacksize(&attr, (size_t)2 << 30);
+    pthread_attr_setstacksize(&attr, stack);
     pthread_t th;
     if (pthread_create(&th, &attr, run, nullptr) != 0) {
         std::fprintf(stderr, "cannot start worker thread\n");
