@@ -245,10 +245,12 @@ def reference_sample(p, dt, nsteps: int = 1) -> dict | None:
                                capture_output=True, text=True, timeout=900)
         line = [ln for ln in r.stdout.splitlines() if ln.startswith("steps ")]
         if r.returncode != 0 or not line:
+            print(f"reference harness failed (rc {r.returncode}): {r.stderr[-500:]}", file=sys.stderr)
             return None
         f = line[-1].split()
         sps, threads = float(f[5]), int(f[7])
-    except (Exception, SystemExit):
+    except (Exception, SystemExit) as e:
+        print(f"reference harness unavailable: {e!r}"[:800], file=sys.stderr)
         return None
     return {"value": p.sites / sps, "unit": "site-steps/s", "cores": threads, "kind": "reference",
             "steps_timed": nsteps,

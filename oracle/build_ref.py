@@ -172,9 +172,17 @@ def build(name: str) -> str:
     shim = os.path.join(HERE, "shim")
     cxx = ["g++", "-O2", "-std=c++17", "-fopenmp", "-w", "-I", d, "-I", shim,
            "-include", os.path.join(shim, "prec_override.h")]
+    link_extra, model_flags = [], []
     if int(CONFIGS[name][1].get("N", "64")) >= 128:
-        # the reference's static N^3 arrays exceed the small code model's 2-4 GB of data
-        cxx.append("-mcmodel=large" if platform.machine() in ("aarch64", "arm64") else "-mcmodel=medium")
+        # the reference's static N^3 arrays exceed the small code model's 2-4 GB of data; on
+        # aarch64 the large model exists only for position-dependent code. Every object of the
+        # program needs it (the shims' own statics end up beyond the arrays)
+        if platform.machine() in ("aarch64", "arm64"):
+            model_flags = ["-fno-pic", "-mcmodel=large"]
+            link_extra = ["-no-pie"]
+        else:
+            model_flags = ["-mcmodel=medium"]
+    cxx += model_flags
     objs = []
     jobs = []
     for s in SOURCES:
@@ -187,14 +195,15 @@ def build(name: str) -> str:
     objs.append(o)
     for src in (os.path.join(shim, "shim_fftw.c"), os.path.join(HERE, "fft64.c")):
         o = os.path.join(d, os.path.basename(src).replace(".c", ".o"))
-        jobs.append(["gcc", "-O2", "-std=c11", "-fopenmp", "-I", shim, "-c", src, "-o", o])
+        jobs.append(["gcc", "-O2", "-std=c11", "-fopenmp"] + model_flags + ["-I", shim, "-c", src, "-o", o])
         objs.append(o)
     with ThreadPoolExecutor(max_workers=os.cpu_count()) as ex:
         for r in ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), jobs):
             if r.returncode != 0:
                 raise SystemExit(f"compile failed:\n{' '.join(r.args)}\n{r.stderr}")
     exe = os.path.join(d, "harness")
-    r = subprocess.run(["g++", "-fopenmp", "-o", exe] + objs + ["-lm", "-lpthread"], capture_output=True, text=True)
+    r = subprocess.run(["g++", "-fopenmp"] + link_extra + ["-o", exe] + objs + ["-lm", "-lpthread"], capture_output=True,
+                       text=True)
     if r.returncode != 0:
         raise SystemExit(f"link failed:\n{r.stderr}")
     return exe
