@@ -57,8 +57,14 @@ CONFIGS = {
     "adjoint_128": (dict(kind="preheating", N=128, spectral=0, with_gw=1, vv=2), 0.005,
                     "adjoint of <chi^2> and rho_GW after 2000 steps: 128^3 two-field preheating + GW, "
                     "velocity Verlet, checkpoints every 100 steps"),
+    # the 1024^3 configuration's own check: FP32 1024^3 + GW from the 256^3 initial state
+    # prolonged spectrally (psc_set_state_padded), against the FP64 256^3 run on the same modes
+    # (bins |k| < 128 kIR, inside the 256^3 lattice), GW energy spectrum every 100 steps
+    "gw_modes_1024": (dict(kind="preheating", N=1024, spectral=0, with_gw=1, vv=4), 0.2 / (1024 * 3 ** 0.5 / 2),
+                      "1024^3 two-field preheating + GW (FP32) vs FP64 256^3 on the same modes, Yoshida-4"),
 }
 ADJ_STEPS, ADJ_EVERY = 2000, 100
+MODES_EVERY, MODES_OUTPUTS = 100, 2
 
 
 def ensemble_params(precision: int):
@@ -291,6 +297,9 @@ def run_ensemble(args):
     sites = sum(p.sites for p in ps)
     ens = Ensemble(ps)
     ens.initialize()
+    if not args.no_autotune:
+        ens.autotune(reps=2)
+    one_launch = ens.launch_mode(per_group=True if args.per_group else None)
     ens.evolve(dt, args.warmup)
     clocks = ClockSampler(local)
     barrier(dist)
@@ -307,12 +316,157 @@ def run_ensemble(args):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == 32 else "f64",
                 "data": "synthetic (reference seeded initial conditions per realization)",
                 "config": {"workload": desc, "realizations": len(ps), "groups": ens.groups, "sites": sites,
-                           "dt": dt, "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
-                "clocks": clk, "gpu_launches": 3 * 6 * 4 * args.steps}
+                           "dt": dt, "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                           "fft_shapes": "default" if args.no_autotune else "autotuned per group",
+                           "launches": "one per pass for all groups" if one_launch else "one per pass per group"},
+                "clocks": clk,
+                "gpu_launches": (1 if one_launch else ens.groups) * 6 * ps[0].stages * args.steps}
         print(json.dumps(line), flush=True)
     ens.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+def run_modes_check(args):
+    """GW energy spectrum of the 1024^3 FP32 lattice against an FP64 256^3 run on the same modes:
+    the 256^3 initial state (the reference's initialize() + initialize_GW()) is the 1024^3 state
+    by spectral prolongation (zero modes above the 256^3 band), both evolve with the 1024^3
+    step's dt, and the spectra_gws columns of the bins |k| < 128 kIR (every mode of the bin lies
+    in both lattices) are compared every MODES_EVERY steps, with rho_GW and a(t)."""
+    world, rank, local, dist = dist_setup()
+    import numpy as np
+    from pspectcosmo_gb300 import Lattice, build
+    from pspectcosmo_gb300.outputs import spectra_rows
+
+    build.build()
+    p, dt, desc = make_params(args.config, 32)
+    q = p.copy()
+    q.N, q.precision = 256, 64
+    small = Lattice(q)
+    small.initialize()
+    st = small.get_state()
+    big = Lattice(p)
+    big.set_state_padded(256, st["f_k"], st["pi_k"], st["a"], st["ad"], st["add"], st["u_k"], st["pi_u_k"])
+    del st
+    if not args.no_autotune:
+        big.autotune(reps=2)
+
+    def rows(lat, pp):
+        en = lat.energies()
+        return spectra_rows(pp, lat.background(), lat.spectra_raw(), en["total"]), en
+
+    points, big_ms = [], 0.0
+    clocks = ClockSampler(local)
+    clocks.start()
+    for k in range(1, MODES_OUTPUTS + 1):
+        big.evolve(dt, MODES_EVERY)
+        big_ms += big.last_step_ms()
+        small.evolve(dt, MODES_EVERY)
+        (rb, eb), (rs, es) = rows(big, p), rows(small, q)
+        # bin i (|k| in [i, i+1) kIR) is row i - 1 of both lattices' spectra; bins below 128 kIR
+        def inside(x):
+            return x[x[:, 0] < 128 * q.kIR]
+
+        gb, gs = inside(rb["spectra_gws"]), inside(rs["spectra_gws"])
+        pt = {"step": k * MODES_EVERY, "t": big.background()["t"]}
+        for c, name in ((1, "h2"), (2, "hdot2")):
+            d = np.abs(gb[:, c] - gs[:, c]).max() / np.abs(gs[:, c]).max()
+            pt[f"gw_{name}_rel_err"] = float(d)
+        for f in range(p.nflds):
+            a_, b_ = inside(rb[f"spectra_scalar_{f}"]), inside(rs[f"spectra_scalar_{f}"])
+            pt[f"P_f{f}_rel_err"] = float(np.abs(a_[:, 1] - b_[:, 1]).max() / np.abs(b_[:, 1]).max())
+        pt["rho_gw_rel_err"] = abs(eb["rho_gw"] - es["rho_gw"]) / abs(es["rho_gw"])
+        pt["a_rel_err"] = abs(big.background()["a"] - small.background()["a"]) / small.background()["a"]
+        points.append(pt)
+    clk = clocks.stop()
+    steps = MODES_EVERY * MODES_OUTPUTS
+    if rank == 0:
+        line = {"metric": "site-steps/s", "value": p.sites * steps / (big_ms / 1e3), "unit": "site-steps/s",
+                "n_gpus": 1, "steps": steps, "warmup": 0, "ms_per_step": big_ms / steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (reference seeded 256^3 initial conditions, prolonged)",
+                "config": {"workload": desc, "N": p.N, "nflds": p.nflds, "gw": True, "vv": p.vv, "dt": dt,
+                           "compared_bins": "|k| < 128 kIR", "output_every": MODES_EVERY},
+                "gw_spectrum_vs_fp64_256": points, "clocks": clk}
+        print(json.dumps(line), flush=True)
+    big.close()
+    small.close()
+
+
+def adjoint_check(lat, p, dt, st0, ndir):
+    """Accuracy of the FP32 adjoint at this configuration: directional derivatives of <chi^2> and
+    rho_GW along ndir random directions of (f_k, pi_k, u_k, pi_u_k, gsq) at t = 0, from the FP32
+    and FP64 adjoint gradients, against FP64 central differences of the product's forward map
+    (h = 1e-6 relative: each array's perturbation has mean modulus 1e-6 of the array's, gsq
+    moves by 1e-6 gsq times a standard normal)."""
+    import numpy as np
+    from pspectcosmo_gb300 import Lattice
+
+    q = p.copy()
+    q.precision = 64
+    keys = ("f_k", "pi_k", "u_k", "pi_u_k")
+    cur = [None]
+
+    def set64(st, gsq=None):
+        # an FP64 lattice holding st (a new one per coupling value: gsq is a run parameter)
+        if cur[0] is not None:
+            cur[0].close()
+        qq = q.copy()
+        if gsq is not None:
+            qq.gsq = gsq
+        cur[0] = Lattice(qq)
+        cur[0].set_state(*(st[k] for k in ("f_k", "pi_k", "a", "ad", "add", "u_k", "pi_u_k")))
+        return cur[0]
+
+    def reset32():
+        lat.set_state(*(st0[k] for k in ("f_k", "pi_k", "a", "ad", "add", "u_k", "pi_u_k")))
+
+    grads = {}
+    for name in ("chi2", "rho_gw"):
+        reset32()
+        g32 = lat.adjoint(name, dt, ADJ_STEPS, ADJ_EVERY)
+        g64 = set64(st0).adjoint(name, dt, ADJ_STEPS, ADJ_EVERY)
+        grads[name] = (g32, g64)
+    # rho_GW of the forward map's final state: the energies after a forward run equal the
+    # adjoint's rho_GW observable (checked on the unperturbed state)
+    l64 = set64(st0)
+    o_chi = l64.adjoint_forward("chi2", dt, ADJ_STEPS)
+    o_rho_e = l64.energies()["rho_gw"]
+    o_rho = set64(st0).adjoint_forward("rho_gw", dt, ADJ_STEPS)
+    rng = np.random.default_rng(2026)
+    N = p.N
+    dirs = []
+    for d in range(ndir):
+        v = {}
+        for k in keys:
+            base = st0[k]
+            x = np.fft.rfftn(rng.standard_normal((base.shape[0], N, N, N)), axes=(-3, -2, -1)).reshape(base.shape)
+            v[k] = x * (1e-6 * np.abs(base).mean() / np.abs(x).mean())
+        dg = 1e-6 * p.gsq * float(rng.standard_normal())
+        fd = {}
+        for sign in (1, -1):
+            st = dict(st0)
+            for k in keys:
+                st[k] = st0[k] + sign * v[k]
+            l64 = set64(st, gsq=p.gsq + sign * dg)
+            oc = l64.adjoint_forward("chi2", dt, ADJ_STEPS)
+            orho = l64.energies()["rho_gw"]
+            fd.setdefault("chi2", []).append(oc)
+            fd.setdefault("rho_gw", []).append(orho)
+        row = {"direction": d}
+        for name in ("chi2", "rho_gw"):
+            fdv = (fd[name][0] - fd[name][1]) / 2
+            for tag, g in zip(("fp32", "fp64"), grads[name]):
+                pred = sum(float(np.sum(np.real(np.conj(g["grad_" + k]) * v[k]))) for k in keys
+                           if g.get("grad_" + k) is not None) + float(g["grad_theta"][0]) * dg
+                row[f"{name}_{tag}_rel_err"] = abs(pred - fdv) / abs(fdv)
+            row[f"{name}_fd"] = fdv
+        dirs.append(row)
+    cur[0].close()
+    worst = {k: max(r[k] for r in dirs) for k in dirs[0] if k.endswith("rel_err")}
+    return {"directions": ndir, "h": "1e-6 relative", "O_chi2": o_chi, "O_rho_gw": o_rho,
+            "rho_gw_energies_vs_observable": abs(o_rho_e - o_rho) / abs(o_rho), "worst": worst,
+            "per_direction": dirs, "stated_tolerance": 1e-3}
 
 
 def run_adjoint(args):
@@ -364,6 +518,7 @@ def run_adjoint(args):
             lat.adjoint(name, dt, ADJ_STEPS, ADJ_EVERY)
     e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
     state_bytes = (2 * p.nflds + 12) * p.modes * 16
+    check = adjoint_check(lat, p, dt, st0, args.adj_check) if (args.adj_check > 0 and rank == 0) else None
     if rank == 0:
         line = {"metric": "site-steps/s", "value": value, "unit": "site-steps/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -386,6 +541,7 @@ def run_adjoint(args):
                 "roofline": None,
                 "cpu_baseline": None,
                 "clocks": clk,
+                "gradient_check": check,
                 "gpu_launches": int(ADJ_STEPS * p.stages * (2 * (2 * 6 + 11) + 13) + 32)}
         print(json.dumps(line), flush=True)
     lat.close()
@@ -460,6 +616,8 @@ def run_ours(args):
         return run_ensemble(args)
     if args.config == "adjoint_128":
         return run_adjoint(args)
+    if args.config == "gw_modes_1024":
+        return run_modes_check(args)
     world, rank, local, dist = dist_setup()
     from pspectcosmo_gb300 import Lattice, build
     from pspectcosmo_gb300.params import Params  # noqa: F401
@@ -468,6 +626,12 @@ def run_ours(args):
     p, dt, desc = make_params(args.config, args.precision)
     lat = Lattice(p)
     lat.initialize()
+    # FFT tile / grid shapes: the planner's defaults, then the autotuner's choice (timed on
+    # this state, before the warm-up)
+    shapes = {"default": list(lat.shapes)}
+    if not args.no_autotune:
+        tune = lat.autotune(reps=3)
+        shapes.update(chosen=list(tune["shape"]), from_cache=tune["from_cache"])
     # host copy of the initial state (the e2e input); at 1024^3 the FP64 host state would be
     # ~140 GB, so that size has no e2e leg and restarts from the device generator instead
     big = p.N >= 1024
@@ -619,7 +783,8 @@ def run_ours(args):
             "config": {"workload": desc, "N": p.N, "nflds": p.nflds, "gw": bool(p.with_gw), "vv": p.vv, "dt": dt,
                        "precision": f"fp{p.precision} fields, fp64 background/reductions",
                        "parallelism": f"replicas x{world}" if world > 1 else "single lattice",
-                       "l2": "arrays > 129 MB L2 (no flush needed)"},
+                       "l2": "arrays > 129 MB L2 (no flush needed)",
+                       "fft_shapes": shapes},
             "e2e": e2e,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
@@ -651,6 +816,12 @@ def main():
     ap.add_argument("--precision", type=int, default=32, choices=[32, 64])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the planner's default FFT tile shapes")
+    ap.add_argument("--per-group", action="store_true",
+                    help="ensemble_mixed: launch each size group's passes separately (default: one launch per pass)")
+    ap.add_argument("--adj-check", type=int, default=0,
+                    help="adjoint_128: also check the FP32 and FP64 gradients against FP64 central differences "
+                         "on this many random directions")
     ap.add_argument("--fp64-steps", type=int, default=None,
                     help="also run FP32 and FP64 lattices this many steps side by side and report the errors "
                          "(default: 1000 for preheat_gw_256, 0 otherwise)")

@@ -50,8 +50,15 @@ extern "C" {
                                    the CUDA context can no longer be trusted (destroy the handle and
                                    do no further GPU work in this process) */
 
-#define PSC_MODEL_PHI2 0      /* V = phi^2/2 (reference model.h:35-99) */
-#define PSC_MODEL_PHI2CHI2 1  /* V = phi^2/2 + gsq phi^2 chi^2 / 2 (two-field preheating) */
+#define PSC_MODEL_PHI2 0      /* V = phi^2/2 (reference model.h:35-99), built in */
+#define PSC_MODEL_PHI2CHI2 1  /* V = phi^2/2 + gsq phi^2 chi^2 / 2 (two-field preheating), built in */
+/* Model ids PSC_MODEL_USER + i: the model.h files compiled into the library (file i of the
+ * PSC_MODEL_H list at build time, by default every .h file in pspectcosmo_gb300/models/),
+ * each written in the reference's model interface (model.h:10-104) and evaluated on the
+ * device in the lattice's precision; psc_model_find gives the id of a file stem. */
+#define PSC_MODEL_USER 16
+#define PSC_MAX_FIELDS 4      /* nflds <= 4 (built-in models: 1 and 2) */
+#define PSC_MAX_TERMS 4       /* num_potential_terms <= 4 */
 
 /*
  * Run configuration: the reference's compile-time parameters.h / model.h surface as
@@ -59,7 +66,8 @@ extern "C" {
  */
 typedef struct psc_params {
     int N;                  /* parameters.h:22   points per lattice edge: power of two, 8..1024 */
-    int nflds;              /* parameters.h:20   number of scalar fields: 1 or 2 */
+    int nflds;              /* parameters.h:20   number of scalar fields: 1 .. PSC_MAX_FIELDS (GWs with more
+                               than two fields: N <= 512) */
     int vv;                 /* parameters.h:10   integrator: 2 (velocity Verlet), 4, 6, 8, 10 (Yoshida) */
     int alpha;              /* parameters.h:120  time variable exponent (0 = cosmic time) */
     int expansion;          /* parameters.h:67   must be 2 (self-consistent Friedmann) for evolution */
@@ -69,7 +77,7 @@ typedef struct psc_params {
                                (spectral = 0); on the spectral path they keep their initial values
                                and appear in the GW spectra, as the reference does */
     int precision;          /* 64: FP64 state (the plain method) or 32: FP32 state, FP64 background */
-    int model;              /* PSC_MODEL_* (model.h) */
+    int model;              /* model.h: PSC_MODEL_PHI2, PSC_MODEL_PHI2CHI2 or PSC_MODEL_USER + i */
     int seed;               /* parameters.h:65   Park-Miller seed (rand_uniform, initialize.cpp:13) */
     int N_pad;              /* parameters.h:13,23 PAD_FLAG / N_pad: 0 = off, else the padded grid of the
                                dealiased spectral step evolve_VV_k_pad (power of two, N < N_pad <= 1024,
@@ -80,13 +88,36 @@ typedef struct psc_params {
     double m_in_MPl;        /* parameters.h:110  mass in Planck units (omegaStar = m_in_MPl * fStar) */
     double fStar;           /* parameters.h:127  field unit (0 => MPl) */
     double epsilon;         /* parameters.h:39   R_Q2C threshold of the K, G mask */
-    double gsq;             /* two-field coupling g^2 in program units */
-    double initfield[2];    /* parameters.h:123  initial homogeneous fields */
-    double initderivs[2];   /* parameters.h:124  initial homogeneous field derivatives */
+    double gsq;             /* coupling g^2 of PSC_MODEL_PHI2CHI2 in program units (a user model
+                               holds its own couplings, as a model.h does) */
+    double initfield[PSC_MAX_FIELDS];    /* parameters.h:123  initial homogeneous fields */
+    double initderivs[PSC_MAX_FIELDS];   /* parameters.h:124  initial homogeneous field derivatives */
     double kcutoff;         /* parameters.h:30   initial low-pass cut (0 = none) */
 } psc_params;
 
 typedef struct psc_handle psc_handle;
+
+/* ---- the model surface (model.h). The reference compiles one model.h into its binary;
+ * this library compiles a list of them (see PSC_MODEL_USER) next to its two built-in
+ * models. psc_model_count: number of user models; psc_model_name: the name of a model id,
+ * the file stem for a user model and "builtin:phi2", "builtin:phi2chi2" for the built-ins
+ * (NULL for an unknown id); psc_model_find: the id of such a name (PSC_ERR_CONFIG when
+ * unknown); psc_model_nterms: num_potential_terms of a model id (0 when unknown). */
+int psc_model_count(void);
+const char *psc_model_name(int model);
+int psc_model_find(const char *name, int *model);
+int psc_model_nterms(int model);
+
+/* Evaluates the model of p (p->model, p->nflds, p->gsq, p->precision) at n field points
+ * (fields [n][nflds], FP64) the way the lattice does: dvdf [n][nflds] = dvdf(fld, f) (model.h
+ * dvdf, in the arithmetic of the lattice path of p->precision), terms [n][nterms] =
+ * potential_energy(term, f) (same arithmetic), mass_sq [n][nflds] = effective_mass(f) (FP64,
+ * as the initial conditions and spectra use it); any output may be NULL. on_device = 1
+ * evaluates on the current GPU (the device code the passes call), 0 on the host (the same
+ * model code compiled for the host). The reference's counterpart is a direct call of
+ * model.h's functions (evolution.cpp:1077-1109, initialize.cpp:644). */
+int psc_model_eval(const psc_params *p, int on_device, long long n, const double *fields, double *dvdf,
+                   double *terms, double *mass_sq);
 
 /* Fill *p with the reference's shipped parameters.h / model.h values (N = 64,
  * one field, VV = 2, kIR = 25, phi0 = 11, spectral path, FP64). */
@@ -155,6 +186,10 @@ int psc_energies(psc_handle *h, double *K, double *G, double *V, double *total, 
 /* meansvars() (output.cpp:380-461): per field <f>, a^(alpha-3)<pi>, <f^2>,
  * a^(2(alpha-3))<pi^2>, rms(f), a^(alpha-3) rms(pi); out has 6*nflds doubles. */
 int psc_means(psc_handle *h, double *out);
+
+/* <effective_mass(f(x))> over the lattice, the mass_sq_av of spectra() (output.cpp:566-580)
+ * that its occupation numbers n_k use; out has nflds doubles. */
+int psc_mass_sq_av(psc_handle *h, double *out);
 
 /* histograms() (output.cpp:1193-1297): for each field, the nbins frequencies of its
  * real-space values ([nflds][nbins], each count divided by the number of points
@@ -264,6 +299,26 @@ int psc_analytic_to_lattice(psc_handle *h);
  * the real-space buffer that psc_get_fields_real reads. */
 int psc_time_c2r(psc_handle *h, int reps, float *ms);
 
+/* FFT tile and grid shapes picked by measurement (no reference counterpart: the reference
+ * plans its FFTW transforms with FFTW_ESTIMATE). Times, on the handle's current state, every
+ * candidate shape of the register-engine passes (N >= 32): lines per tile of the X and Y passes
+ * (the default and two narrower tiles), and lines per tile x resident blocks per SM of the Z
+ * pass; each candidate runs reps + 1 stage evaluations with zero drift and kick coefficients
+ * (the state is left as it was). The fastest shapes stay in use for the handle (the step graph
+ * is captured again) and are cached per configuration (N, nflds, GWs, precision, batch size,
+ * user model, SM count) for the process and, when the environment variable PSC_TUNE_CACHE
+ * names a file, across processes; a cached configuration is applied without timing
+ * (*from_cache = 1). shape (may be NULL) receives {log2 X/Y lines per tile, log2 Z lines per
+ * tile, Z blocks per SM}, -1 where the handle has nothing to tune (N < 32, padded step).
+ * The shapes set the order of the K, G and <V> partial sums, so results differ from another
+ * shape's at the rounding of those reductions; a run with given shapes is reproducible. */
+int psc_autotune(psc_handle *h, int reps, int *shape, int *from_cache);
+/* The shapes in use ({-1, -1, -1} where nothing is tunable), and a given set of shapes (as
+ * psc_autotune reports them; each is clamped to its limits, -1 / 0 = the default), e.g. a
+ * choice recorded by an earlier run. */
+int psc_get_shapes(psc_handle *h, int *shape);
+int psc_set_shapes(psc_handle *h, const int *shape);
+
 /* Compulsory HBM bytes each of the PSC_NPASS passes moves per launch (the bytes
  * of the arrays it must read and write once), for roofline accounting. */
 int psc_pass_bytes(psc_handle *h, double *bytes);
@@ -296,8 +351,8 @@ int psc_test_wait_hook(psc_handle *h, double limit_ms, int plant_bytes);
  * counterpart and compose the ones above. psc_batch_create groups the n
  * realizations by configuration (all psc_params fields except seed, initfield,
  * initderivs, a0 and kcutoff must agree within a group; sizes may differ between
- * groups). Each group is advanced by one launch per pass for all its members, and
- * one CUDA graph holds a whole step of every group. Realizations are addressed by
+ * groups). One CUDA graph holds a whole step of every group (see psc_batch_launch_mode for
+ * how the groups' passes are launched). Realizations are addressed by
  * their index in the array given to psc_batch_create. */
 typedef struct psc_batch psc_batch;
 int psc_batch_create(const psc_params *per_realization, int n, psc_batch **out);
@@ -307,6 +362,16 @@ int psc_batch_groups(psc_batch *b);
 int psc_batch_init_ic(psc_batch *b);                      /* initialize() for every realization */
 int psc_batch_step(psc_batch *b, double dt, int nsteps);  /* nsteps steps of every realization */
 int psc_batch_last_step_ms(psc_batch *b, float *ms);
+int psc_batch_autotune(psc_batch *b, int reps);         /* psc_autotune for every group */
+/* How the groups' passes are launched. By default a batch whose groups all run the register
+ * engine at N <= 256 with 256-thread blocks, a built-in model, and one precision, GW setting
+ * and integrator advances with ONE launch per pass for all groups: persistent kernels over
+ * a work list of (group, realization, array, tile) (and one background launch per stage);
+ * other batches launch every group's passes on its own stream, the streams forked and joined
+ * in the step graph. per_group = 1 asks for the per-group launches, 0 for the default, -1
+ * leaves the choice; *one_launch_per_pass (may be NULL) receives 1 when the batched launches
+ * are in use. Both give each realization the results it has alone, bit for bit. */
+int psc_batch_launch_mode(psc_batch *b, int per_group, int *one_launch_per_pass);
 int psc_batch_set_state(psc_batch *b, int idx, const double *f_k, const double *pi_k, double a, double ad, double add,
                         const double *u_k, const double *pi_u_k);
 int psc_batch_get_state(psc_batch *b, int idx, double *f_k, double *pi_k, double *a, double *ad, double *add,

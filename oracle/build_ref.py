@@ -9,8 +9,9 @@ build:
      the per-config headers because pspectcosmo.h:24 includes "parameters.h" with quotes;
   2. parameters.h is the reference's own file with the named constants/macros replaced
      (regex on `const <type> NAME = ...;` and `#define NAME ...`);
-  3. model.h is the reference's own (single-field phi^2) or oracle/models/*.h (the
-     two-field model the benchmark configurations need, written in the same API);
+  3. model.h is the reference's own (single-field phi^2) or one of the model files of the
+     library's model surface, pspectcosmo_gb300/models/*.h (the two-field model the benchmark
+     configurations need, a three-field model; written in the same API);
   4. g++ compiles them against oracle/shim (FFTW/HDF5 API shims over oracle/fft64.c),
      with pspectcosmo.cpp's main renamed and oracle/ref_harness.cpp as the driver.
 
@@ -31,6 +32,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 # the reference checkout this recipe reads (PSC_REFERENCE_DIR overrides the default)
 REF = os.environ.get("PSC_REFERENCE_DIR", "/root/reference")
 OUT = os.path.join(HERE, "_ref")
+MODELS = os.path.join(os.path.dirname(HERE), "pspectcosmo_gb300", "models")
 
 
 def reference_available() -> bool:
@@ -96,6 +98,30 @@ CONFIGS: dict[str, tuple[str, dict[str, str]]] = {
         "initfield[]": "{0.193 * MPl, 0.}",
         "initderivs[]": "{-0.142e-6 * MPl * MPl, 0.}",
     }),
+    # three fields (pspectcosmo_gb300/models/three_field.h: phi, chi, sigma), the spectral step
+    # and the real-space step with GWs, at N = 16 (full state) and N = 32 (outputs)
+    "spec3_n16_vv4": ("three_field", {
+        "N": "16", "VV": "4", "nflds": "3", "kIR": "1",
+        "initfield[]": "{0.193 * MPl, 0., 0.01 * MPl}",
+        "initderivs[]": "{-0.142e-6 * MPl * MPl, 0., 0.}",
+    }),
+    "gw3_n16_vv4": ("three_field", {
+        "N": "16", "VV": "4", "nflds": "3", "kIR": "1",
+        "SPECTRAL_FLAG": "false", "WITH_GW": "true",
+        "initfield[]": "{0.193 * MPl, 0., 0.01 * MPl}",
+        "initderivs[]": "{-0.142e-6 * MPl * MPl, 0., 0.}",
+    }),
+    "gw3_n32_vv4": ("three_field", {
+        "N": "32", "VV": "4", "nflds": "3", "kIR": "1",
+        "SPECTRAL_FLAG": "false", "WITH_GW": "true",
+        "initfield[]": "{0.193 * MPl, 0., 0.01 * MPl}",
+        "initderivs[]": "{-0.142e-6 * MPl * MPl, 0., 0.}",
+    }),
+    "spec3_n32_vv2": ("three_field", {
+        "N": "32", "VV": "2", "nflds": "3", "kIR": "1",
+        "initfield[]": "{0.193 * MPl, 0., 0.01 * MPl}",
+        "initderivs[]": "{-0.142e-6 * MPl * MPl, 0., 0.}",
+    }),
     # real-space pseudo-spectral path with gravitational waves (evolve_VV)
     "gw2_n16_vv4": ("phi2chi2", {
         "N": "16", "VV": "4", "nflds": "2", "kIR": "1",
@@ -156,7 +182,7 @@ def prepare(name: str) -> str:
     if model == "phi2":
         shutil.copyfile(os.path.join(REF, "model.h"), os.path.join(d, "model.h"))
     else:
-        shutil.copyfile(os.path.join(HERE, "models", f"model_{model}.h"), os.path.join(d, "model.h"))
+        shutil.copyfile(os.path.join(MODELS, f"{model}.h"), os.path.join(d, "model.h"))
     return d
 
 

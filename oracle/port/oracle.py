@@ -17,7 +17,9 @@ SRC = [os.path.join(HERE, "psc_oracle.c"), os.path.join(os.path.dirname(HERE), "
 
 
 def build(force: bool = False) -> str:
-    newest = max(os.path.getmtime(s) for s in SRC + [os.path.join(HERE, "psc_oracle.h")])
+    # psc_oracle.h includes the library's psc.h for the psc_params layout
+    deps = SRC + [os.path.join(HERE, "psc_oracle.h"), os.path.join(HERE, "..", "..", "include", "psc.h")]
+    newest = max(os.path.getmtime(s) for s in deps)
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
         cmd = ["gcc", "-O2", "-std=c11", "-fopenmp", "-shared", "-fPIC"] + SRC + ["-o", LIB, "-lm"]
         subprocess.run(cmd, check=True)

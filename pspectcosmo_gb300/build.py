@@ -1,8 +1,10 @@
 """Build libpsc.so (the CUDA path and its C ABI) in-tree for sm_103a.
 
-Three translation units compiled in parallel with nvcc (the IC generator with the host
-compiler through nvcc), linked into pspectcosmo_gb300/libpsc.so. Rebuilds only when a
-source is newer than the library.
+The model.h files of the model surface (PSC_MODEL_H, default pspectcosmo_gb300/models/*.h)
+are first turned into _build/psc_user_models.cuh by model_adapter.py. The translation units
+compile in parallel with nvcc (the IC generator and the HDF5 writer with the host compiler
+through nvcc) and link into pspectcosmo_gb300/libpsc.so. Rebuilds only when a source, a
+model file or the generated header is newer than the library.
 """
 from __future__ import annotations
 
@@ -17,7 +19,9 @@ CSRC = os.path.join(HERE, "csrc")
 ROOT = os.path.dirname(HERE)
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpsc.so")
-SOURCES = ["psc_kernels.cu", "psc_reg_f32.cu", "psc_reg_f64.cu", "psc_api.cu", "psc_noalloc.cu", "psc_adjoint.cu",
+SOURCES = ["psc_kernels.cu", "psc_reg_f32.cu", "psc_reg_f64.cu", "psc_reg_user_f32.cu", "psc_reg_user_f64.cu",
+           "psc_batch_f32.cu", "psc_batch_f64.cu",
+           "psc_api.cu", "psc_noalloc.cu", "psc_adjoint.cu",
            "psc_ic_gpu.cu", "psc_outputs.cu", "psc_pad.cu", "psc_analytic.cu",
            "psc_ic.cpp", "psc_h5.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -30,18 +34,26 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found")
 
 
+USER_MODELS_H = os.path.join(BUILD, "psc_user_models.cuh")
+
+
 def _deps():
-    files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(ROOT, "include", "psc.h")]
+    files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(ROOT, "include", "psc.h"), USER_MODELS_H]
     return [f for f in files if os.path.isfile(f)]
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
+    sys.path.insert(0, HERE)
+    import model_adapter  # noqa: E402
+
+    sys.path.remove(HERE)
+    model_adapter.write(USER_MODELS_H)   # rewritten (newer) only when the model list or a model changed
     newest = max(os.path.getmtime(f) for f in _deps() + [os.path.abspath(__file__)])
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     cc = nvcc()
-    common = ["-std=c++17", "-O3", "-Xcompiler", "-fPIC", "-I", CSRC, "-I", os.path.join(ROOT, "include")]
+    common = ["-std=c++17", "-O3", "-Xcompiler", "-fPIC", "-I", CSRC, "-I", BUILD, "-I", os.path.join(ROOT, "include")]
     jobs = []
     objs = []
     for src in SOURCES:

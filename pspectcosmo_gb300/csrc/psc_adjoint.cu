@@ -509,6 +509,9 @@ int check(psc_handle *h, int obs) {
     if (p.with_gw && p.spectral)
         return fail(PSC_ERR_CONFIG, "the adjoint differentiates evolved GW tensors (spectral = 0 with GWs)");
     if (p.with_gw && h->cfg.g.N > 512) return fail(PSC_ERR_CONFIG, "the adjoint with GWs needs N <= 512");
+    if (psc::model_is_user(p.model))
+        return fail(PSC_ERR_CONFIG, "the adjoint differentiates the built-in models (V'' and the coupling derivatives are "
+                                    "written for them)");
     if (p.model == PSC_MODEL_PHI2CHI2 && !(p.gsq > 0)) return fail(PSC_ERR_CONFIG, "the adjoint needs gsq > 0");
     if (!h->have_state) return fail(PSC_ERR_STATE, "no state: call psc_init_ic or psc_set_state first");
     return PSC_OK;

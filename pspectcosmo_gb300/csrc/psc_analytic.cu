@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "psc_handle.h"
+#include "psc_model.h"
 
 namespace psc {
 namespace {
@@ -196,6 +197,10 @@ int analytic_begin(psc_handle *h) {
     if (h->R != 1) return fail(PSC_ERR_CONFIG, "the analytic phase runs on single-lattice handles");
     const psc_params &p = h->p0();
     if (p.expansion != 2) return fail(PSC_ERR_CONFIG, "the analytic phase needs expansion = 2");
+    // the linear mode equations use d2Vdf2(fld + fld2) (evolution.cpp:229), whose index names a
+    // field pair uniquely for the built-in models only
+    if (psc::model_is_user(p.model))
+        return fail(PSC_ERR_CONFIG, "the analytic phase runs the built-in models (PSC_MODEL_PHI2, PSC_MODEL_PHI2CHI2)");
     if (h->ana && h->ana_free) h->ana_free(h->ana);
     Analytic *an = new Analytic();
     h->ana = an;

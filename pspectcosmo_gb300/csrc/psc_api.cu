@@ -11,8 +11,10 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <new>
 #include <string>
 #include <tuple>
@@ -113,10 +115,13 @@ int dalloc(psc_handle *h, void **out, size_t bytes) {
 int validate(const psc_params *p) {
     if (!p) return fail(PSC_ERR_ARG, "null parameters");
     if (!pow2(p->N) || p->N < 8 || p->N > 1024) return fail(PSC_ERR_CONFIG, "N must be a power of two in [8, 1024]");
-    if (p->nflds < 1 || p->nflds > 2) return fail(PSC_ERR_CONFIG, "nflds must be 1 or 2");
+    if (p->nflds < 1 || p->nflds > PSC_MAX_FIELDS) return fail(PSC_ERR_CONFIG, "nflds must be 1 .. PSC_MAX_FIELDS (4)");
     if (p->model == PSC_MODEL_PHI2 && p->nflds != 1) return fail(PSC_ERR_CONFIG, "the phi^2 model has one field");
     if (p->model == PSC_MODEL_PHI2CHI2 && p->nflds != 2) return fail(PSC_ERR_CONFIG, "the phi^2 chi^2 model has two fields");
-    if (p->model != PSC_MODEL_PHI2 && p->model != PSC_MODEL_PHI2CHI2) return fail(PSC_ERR_CONFIG, "unknown model");
+    if (!psc::model_known(p->model)) return fail(PSC_ERR_CONFIG, "unknown model (not built in and not a compiled model.h)");
+    // the GW Z pass carries 2 nflds input line pairs of N/16 threads in a 256-thread block
+    if (p->with_gw && !p->spectral && p->N >= 32 && p->nflds * p->N > 2048)
+        return fail(PSC_ERR_CONFIG, "GWs with more than two fields need N <= 512 (three or four fields)");
     if (p->vv != 2 && p->vv != 4 && p->vv != 6 && p->vv != 8 && p->vv != 10)
         return fail(PSC_ERR_CONFIG, "vv must be 2, 4, 6, 8 or 10");
     if (p->precision != 32 && p->precision != 64) return fail(PSC_ERR_CONFIG, "precision must be 32 or 64");
@@ -504,9 +509,11 @@ int create_handle(const psc_params *ps, int R, psc_handle **out) {
     if ((rc = dalloc(h, &b.tw, (size_t)g.N * h->csize))) return bail(rc);
     if ((rc = dalloc(h, &tmp, sizeof(double) * (size_t)R * g.pkg_stride))) return bail(rc);
     b.partKG = static_cast<double *>(tmp);
+    h->partKG_cap = (size_t)R * g.pkg_stride;
     const size_t pv = h->padded ? std::max(g.pv_stride, h->cfgp.g.pv_stride) : g.pv_stride;
     if ((rc = dalloc(h, &tmp, sizeof(double) * (size_t)R * pv))) return bail(rc);
     b.partV = static_cast<double *>(tmp);
+    h->partV_cap = (size_t)R * pv;
     if ((rc = dalloc(h, &tmp, sizeof(double) * (g.nf * 3 + 2) * h->nb))) return bail(rc);
     b.spec = static_cast<double *>(tmp);
     if ((rc = dalloc(h, &tmp, sizeof(int) * (g.nf + 1) * h->nb))) return bail(rc);
@@ -531,6 +538,7 @@ int create_handle(const psc_params *ps, int R, psc_handle **out) {
             return bail(rc);
         bp.pk = bp.uk = bp.puk = bp.TB = bp.TC = bp.QS = nullptr;
         bp.Fk = bp.Fu = nullptr;
+        bp.tape_f = bp.tape_p = bp.tape_vp = bp.tape_fx = bp.tape_pu = bp.tape_fu = nullptr;
         CUB(cudaMemsetAsync(bp.fk, 0, parr, h->st));
     }
     CUB(cudaMemsetAsync(b.fk, 0, farr, h->st));
@@ -907,6 +915,198 @@ int means(psc_handle *h, int r, double *out) {
     return PSC_OK;
 }
 
+// ------------------------------------------------------------------ autotuner
+// Tile and grid shapes of the register-engine passes chosen by timing the candidates on the
+// handle's own buffers. Choices are cached per configuration in the process and, when
+// PSC_TUNE_CACHE names a file, across processes (one line per configuration).
+using TuneKey = std::tuple<int, int, int, int, int, int, int>;   // N, nflds, GW evolved, precision, R, user, SMs
+
+TuneKey tune_key(psc_handle *h) {
+    const psc::Geo &g = h->cfg.g;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return TuneKey(g.N, g.nf, g.gwev, h->p0().precision, h->R, psc::model_is_user(h->p0().model) ? 1 : 0, sms);
+}
+
+std::map<TuneKey, psc::TileChoice> &tune_cache() {
+    static std::map<TuneKey, psc::TileChoice> m;
+    return m;
+}
+std::mutex &tune_mutex() {
+    static std::mutex m;
+    return m;
+}
+
+void tune_cache_load() {
+    static bool loaded = false;
+    if (loaded) return;
+    loaded = true;
+    const char *path = std::getenv("PSC_TUNE_CACHE");
+    if (!path || !*path) return;
+    FILE *fh = std::fopen(path, "r");
+    if (!fh) return;
+    int k[7], c[3];
+    while (std::fscanf(fh, "%d %d %d %d %d %d %d %d %d %d", &k[0], &k[1], &k[2], &k[3], &k[4], &k[5], &k[6], &c[0],
+                       &c[1], &c[2]) == 10) {
+        psc::TileChoice tc;
+        tc.xy_shift = c[0];
+        tc.z_shift = c[1];
+        tc.z_per_sm = c[2];
+        tune_cache()[TuneKey(k[0], k[1], k[2], k[3], k[4], k[5], k[6])] = tc;
+    }
+    std::fclose(fh);
+}
+
+void tune_cache_store(const TuneKey &k, const psc::TileChoice &tc) {
+    tune_cache()[k] = tc;
+    const char *path = std::getenv("PSC_TUNE_CACHE");
+    if (!path || !*path) return;
+    FILE *fh = std::fopen(path, "a");
+    if (!fh) return;
+    std::fprintf(fh, "%d %d %d %d %d %d %d %d %d %d\n", std::get<0>(k), std::get<1>(k), std::get<2>(k), std::get<3>(k),
+                 std::get<4>(k), std::get<5>(k), std::get<6>(k), tc.xy_shift, tc.z_shift, tc.z_per_sm);
+    std::fclose(fh);
+}
+
+// Re-plan the handle with shapes tc: launch configuration, kernel attributes, partial-sum
+// buffers large enough for the new block counts, the block counts in the background records,
+// and a fresh step graph at the next step call.
+int apply_shapes(psc_handle *h, const psc::TileChoice &tc) {
+    psc::LaunchCfg c;
+    psc::plan(h->p0(), h->R, &c, &tc);
+    CU(psc::configure(c, h->p0().precision));
+    const size_t kg = (size_t)h->R * c.g.pkg_stride, pv = (size_t)h->R * c.g.pv_stride;
+    void *tmp = nullptr;
+    int rc;
+    if (kg > h->partKG_cap) {
+        if ((rc = dalloc(h, &tmp, sizeof(double) * kg))) return rc;
+        h->b.partKG = static_cast<double *>(tmp);
+        h->partKG_cap = kg;
+    }
+    if (pv > h->partV_cap) {
+        if ((rc = dalloc(h, &tmp, sizeof(double) * pv))) return rc;
+        h->b.partV = static_cast<double *>(tmp);
+        h->partV_cap = pv;
+    }
+    h->cfg = c;
+    for (int r = 0; r < h->R; ++r) {
+        psc::DevBG bg;
+        if ((rc = read_bg(h, r, &bg))) return rc;
+        bg.nbx = c.nbx;
+        bg.nbz = c.nbz;
+        if ((rc = write_bg(h, r, bg))) return rc;
+    }
+    if (h->gexec) {
+        cudaGraphExecDestroy(h->gexec);
+        h->gexec = nullptr;
+    }
+    return PSC_OK;
+}
+
+// Device time of each pass of `reps` stage evaluations (zero drift and kick coefficients:
+// the state is unchanged) with the current shapes.
+int time_stage(psc_handle *h, int reps, double *ms) {
+    cudaEvent_t ev[7];
+    for (int i = 0; i < 7; ++i) CU(cudaEventCreate(&ev[i]));
+    for (int i = 0; i < PSC_NPASS; ++i) ms[i] = 0;
+    psc::Buffers bt = h->b;
+    bt.Fk = bt.Fu = nullptr;
+    int rc = PSC_OK;
+    for (int r = 0; r < reps + 1 && rc == PSC_OK; ++r) {   // the first evaluation warms up
+        cudaError_t e = psc::launch_scalar(h->cfg, bt, psc::SCALAR_EVAL, 0, h->st);
+        if (e == cudaSuccess) e = psc::launch_stage_timed(h->cfg, bt, h->p0().precision, 1, psc::SCALAR_EVAL_END, ev, h->st);
+        if (e == cudaSuccess) e = cudaEventSynchronize(ev[6]);
+        for (int i = 0; i < PSC_NPASS && e == cudaSuccess && r > 0; ++i) {
+            float t = 0.f;
+            e = cudaEventElapsedTime(&t, ev[i], ev[i + 1]);
+            ms[i] += t / reps;
+        }
+        if (e != cudaSuccess) rc = fail(PSC_ERR_CUDA, cudaGetErrorString(e));
+    }
+    for (int i = 0; i < 7; ++i) cudaEventDestroy(ev[i]);
+    h->diag_valid = true;
+    return rc;
+}
+
+int autotune(psc_handle *h, int reps, int *shape, int *from_cache) {
+    const psc::Geo &g = h->cfg.g;
+    if (from_cache) *from_cache = 0;
+    if (!g.reg || h->padded) {   // the generic engine (N < 32) and the padded step keep their shapes
+        if (shape) shape[0] = shape[1] = shape[2] = -1;
+        return PSC_OK;
+    }
+    std::lock_guard<std::mutex> lock(tune_mutex());
+    tune_cache_load();
+    const TuneKey key = tune_key(h);
+    auto it = tune_cache().find(key);
+    psc::TileChoice best;
+    int rc;
+    if (it != tune_cache().end()) {
+        best = it->second;
+        if (from_cache) *from_cache = 1;
+    } else {
+        if (!h->have_state) return fail(PSC_ERR_STATE, "no state: the candidates are timed on the lattice's state");
+        psc::LaunchCfg def;
+        psc::plan(h->p0(), h->R, &def);
+        const psc::TileChoice d0 = def.tc;
+        double ms[PSC_NPASS];
+        // X and Y passes (one tile shape for all four): the default and two narrower tiles of at
+        // least four lines (32 contiguous bytes of an FP32 row)
+        double best_xy = 1e30;
+        for (int s = d0.xy_shift; s >= 2 && s >= d0.xy_shift - 2; --s) {
+            psc::TileChoice tc = d0;
+            tc.xy_shift = s;
+            if ((rc = apply_shapes(h, tc)) || (rc = time_stage(h, reps, ms))) return rc;
+            const double t = ms[0] + ms[1] + ms[3] + ms[4];
+            if (t < best_xy) {
+                best_xy = t;
+                best.xy_shift = s;
+            }
+        }
+        // Z pass: lines per tile x resident blocks per SM of the persistent forms
+        double best_z = 1e30;
+        for (int s = d0.z_shift; s >= 0 && s >= d0.z_shift - 2; --s)
+            for (int k = d0.z_per_sm; k >= 1; --k) {
+                psc::TileChoice tc = d0;
+                tc.z_shift = s;
+                tc.z_per_sm = k;
+                if ((rc = apply_shapes(h, tc)) || (rc = time_stage(h, reps, ms))) return rc;
+                if (ms[2] < best_z) {
+                    best_z = ms[2];
+                    best.z_shift = s;
+                    best.z_per_sm = k;
+                }
+            }
+        tune_cache_store(key, best);
+    }
+    if ((rc = apply_shapes(h, best))) return rc;
+    if (shape) {
+        shape[0] = h->cfg.tc.xy_shift;
+        shape[1] = h->cfg.tc.z_shift;
+        shape[2] = h->cfg.tc.z_per_sm;
+    }
+    return PSC_OK;
+}
+
+// mass_sq_av of spectra() (output.cpp:566-580): effective_mass at every site of the real-space
+// fields, summed in the reference's site order in FP64, over N^3
+int mass_sq_av(psc_handle *h, int r, double *out) {
+    const psc::Geo &g = h->cfg.g;
+    std::vector<double> f((size_t)g.sites * g.nf);
+    int rc = fields_real(h, r, f.data(), nullptr);
+    if (rc) return rc;
+    const psc_params &p = h->p[r];
+    double acc[PSC_MAX_FIELDS] = {}, pt[PSC_MAX_FIELDS] = {}, m2[PSC_MAX_FIELDS] = {};
+    for (long long i = 0; i < g.sites; ++i) {
+        for (int q = 0; q < g.nf; ++q) pt[q] = f[(size_t)q * g.sites + i];
+        model_effective_mass(p.model, p.gsq, m2, pt);
+        for (int q = 0; q < g.nf; ++q) acc[q] += m2[q];
+    }
+    for (int q = 0; q < g.nf; ++q) out[q] = acc[q] / (double)g.sites;
+    return PSC_OK;
+}
+
 }  // namespace hapi
 }  // namespace psc
 using namespace psc::hapi;
@@ -921,9 +1121,216 @@ struct psc_batch {
     cudaEvent_t fork = nullptr;
     cudaGraphExec_t gexec = nullptr;
     float last_ms = 0.f;
+    // one launch per pass for all groups (psc_batch.cuh): the work lists, and per pass the grid
+    // and dynamic shared memory of the batched kernel; `multi` when the batch qualifies and the
+    // caller has not asked for the per-group launches
+    bool multi = false, per_group = false;
+    psc::BatchTable bt{};
+    int grid[psc::kBatchPasses] = {};
+    size_t smem[psc::kBatchPasses] = {};
 };
 
+namespace {
+
+// The batched passes of psc_batch.cuh cover the register engine's line lengths 32 .. 256 with
+// 256-thread blocks, the built-in models and one precision, GW setting and integrator for all
+// groups; other batches launch every group's passes on its own stream.
+int batch_multi_setup(psc_batch *b) {
+    b->multi = false;
+    if (b->per_group || b->groups.empty() || (int)b->groups.size() > psc::kMaxBatchGroups) return PSC_OK;
+    const psc_handle *h0 = b->groups[0];
+    for (const psc_handle *h : b->groups) {
+        const psc::Geo &g = h->cfg.g;
+        if (!g.reg || g.N > 256 || h->padded || psc::model_is_user(h->p0().model) || h->cfg.thr_xy != 256 ||
+            h->cfg.thr_z != 256 || h->p0().precision != h0->p0().precision || g.gwev != h0->cfg.g.gwev || h->s != h0->s)
+            return PSC_OK;
+    }
+    psc::BatchTable &bt = b->bt;
+    bt = psc::BatchTable{};
+    bt.ngroups = (int)b->groups.size();
+    size_t smem[psc::kBatchPasses] = {0, 0, 0, 0, 0};
+    for (int gi = 0; gi < bt.ngroups; ++gi) {
+        const psc_handle *h = b->groups[gi];
+        const psc::LaunchCfg &c = h->cfg;
+        const psc::Geo &g = c.g;
+        psc::BatchGroup &G = bt.grp[gi];
+        G.g = g;
+        G.L = g.N;
+        G.nbx = c.nbx;
+        G.nbz = c.nbz;
+        G.R = h->R;
+        G.nj = g.nf + (g.gwev ? 6 : 0);
+        const psc::Buffers &B = h->b;
+        G.fk = B.fk; G.pk = B.pk; G.uk = B.uk; G.puk = B.puk;
+        G.TA = B.TA; G.TB = B.TB; G.TC = B.TC; G.QV = B.QV; G.QS = B.QS; G.tw = B.tw;
+        G.Fk = B.Fk; G.Fu = B.Fu; G.partKG = B.partKG; G.partV = B.partV; G.bg = B.bg;
+        int nj = 0;
+        for (int f = 0; f < g.nf; ++f) {
+            G.fwd.rs[nj] = g.fstride;
+            G.fwd.p[nj++] = static_cast<char *>(B.QV) + (size_t)f * g.modes * h->csize;
+        }
+        if (g.gwev)
+            for (int q = 0; q < 6; ++q) {
+                G.fwd.rs[nj] = g.gstride;
+                G.fwd.p[nj++] = static_cast<char *>(B.QS) + (size_t)q * g.modes * h->csize;
+            }
+        const int count[psc::kBatchPasses] = {c.nbx * g.nf * h->R, c.nbx * g.nf * h->R, c.nbz * h->R,
+                                              c.nbx * G.nj * h->R, c.nbx * G.nj * h->R};
+        for (int k = 0; k < psc::kBatchPasses; ++k) {
+            G.start[k] = bt.total[k];
+            bt.total[k] += count[k];
+        }
+        const size_t need[psc::kBatchPasses] = {c.smem_xy, g.gwev ? 3 * c.smem_xy : c.smem_xy, c.smem_z, c.smem_xy,
+                                                c.smem_xf};
+        for (int k = 0; k < psc::kBatchPasses; ++k) smem[k] = std::max(smem[k], need[k]);
+    }
+    int dev = 0, sms = 0;
+    CU(cudaGetDevice(&dev));
+    CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const bool f32 = h0->p0().precision == 32;
+    for (int k = 0; k < psc::kBatchPasses; ++k) {
+        int per_sm = 0;
+        for (int drift = 0; drift < (k == 0 ? 2 : 1); ++drift) {
+            const void *kern = f32 ? psc::reg_batch_kernel_f32(k, drift) : psc::reg_batch_kernel_f64(k, drift);
+            CU(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem[k]));
+            CU(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                    cudaSharedmemCarveoutMaxShared));
+            CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem[k]));
+        }
+        if (per_sm < 1) return PSC_OK;   // does not fit: per-group launches
+        b->smem[k] = smem[k];
+        b->grid[k] = std::min(bt.total[k], per_sm * sms);
+    }
+    b->multi = true;
+    return PSC_OK;
+}
+
+// the kernels of one step of every group: one launch per pass and one background launch per
+// stage for all groups
+cudaError_t enqueue_batch_step(psc_batch *b, cudaStream_t st) {
+    const bool f32 = b->groups[0]->p0().precision == 32;
+    cudaError_t e = cudaSuccess;
+    for (int p = 0; p < b->groups[0]->s && e == cudaSuccess; ++p) {
+        for (int k = 0; k < psc::kBatchPasses && e == cudaSuccess; ++k)
+            e = f32 ? psc::reg_batch_pass_f32(b->bt, k, k == 0, b->grid[k], b->smem[k], st)
+                    : psc::reg_batch_pass_f64(b->bt, k, k == 0, b->grid[k], b->smem[k], st);
+        if (e == cudaSuccess) e = psc::launch_scalar_batch(b->bt, p, st);
+    }
+    return e;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ model evaluation
+namespace {
+
+// dvdf, the potential terms (arithmetic T, the lattice path's) and the effective masses
+// (FP64) of one field point
+template <typename T>
+__host__ __device__ void model_point(int model, double gsq, int nf, const double *fv, double *dvdf, double *terms,
+                                     double *mass_sq) {
+    T v[psc::kMaxFields] = {}, out[psc::kMaxFields] = {}, t[psc::kMaxTerms] = {};
+    double vd[psc::kMaxFields] = {};
+    for (int q = 0; q < nf; ++q) {
+        v[q] = (T)fv[q];
+        vd[q] = fv[q];
+    }
+    const psc::ModelG<T> m{model, (T)gsq};
+    const int nt = psc::model_nterms(model);
+    if (dvdf) {
+        psc::model_dvdf<T, T, true>(m, v, out, nf);
+        for (int q = 0; q < nf; ++q) dvdf[q] = (double)out[q];
+    }
+    if (terms) {
+        psc::model_potential<T, T, T, true>(m, v, t);
+        for (int q = 0; q < nt; ++q) terms[q] = (double)t[q];
+    }
+    if (mass_sq) {
+        double m2[psc::kMaxFields] = {};
+        psc::model_effective_mass(model, gsq, m2, vd);
+        for (int q = 0; q < nf; ++q) mass_sq[q] = m2[q];
+    }
+}
+
+template <typename T>
+__global__ void k_model_eval(int model, double gsq, int nf, long long n, const double *fields, double *dvdf,
+                             double *terms, double *mass_sq) {
+    const int nt = psc::model_nterms(model);
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        model_point<T>(model, gsq, nf, fields + i * nf, dvdf ? dvdf + i * nf : nullptr, terms ? terms + i * nt : nullptr,
+                       mass_sq ? mass_sq + i * nf : nullptr);
+}
+
+}  // namespace
+
 extern "C" {
+
+int psc_model_count(void) { return psc::kUserModels; }
+
+const char *psc_model_name(int model) {
+    if (model == PSC_MODEL_PHI2) return "builtin:phi2";
+    if (model == PSC_MODEL_PHI2CHI2) return "builtin:phi2chi2";
+    if (psc::model_is_user(model)) return psc::kUserModelNames[model - PSC_MODEL_USER];
+    return nullptr;
+}
+
+int psc_model_find(const char *name, int *model) {
+    if (!name || !model) return fail(PSC_ERR_ARG, "null argument");
+    for (int id : {PSC_MODEL_PHI2, PSC_MODEL_PHI2CHI2})
+        if (std::strcmp(name, psc_model_name(id)) == 0) {
+            *model = id;
+            return PSC_OK;
+        }
+    for (int i = 0; i < psc::kUserModels; ++i)
+        if (std::strcmp(name, psc::kUserModelNames[i]) == 0) {
+            *model = PSC_MODEL_USER + i;
+            return PSC_OK;
+        }
+    return fail(PSC_ERR_CONFIG, (std::string("no model named ") + name + " in this build").c_str());
+}
+
+int psc_model_nterms(int model) { return psc::model_known(model) ? psc::model_nterms(model) : 0; }
+
+int psc_model_eval(const psc_params *p, int on_device, long long n, const double *fields, double *dvdf,
+                   double *terms, double *mass_sq) {
+    if (!p || !fields || n < 0) return fail(PSC_ERR_ARG, "bad argument");
+    if (!psc::model_known(p->model)) return fail(PSC_ERR_CONFIG, "unknown model");
+    if (p->nflds < 1 || p->nflds > PSC_MAX_FIELDS) return fail(PSC_ERR_CONFIG, "nflds must be 1 .. PSC_MAX_FIELDS");
+    if (p->precision != 32 && p->precision != 64) return fail(PSC_ERR_CONFIG, "precision must be 32 or 64");
+    const int nf = p->nflds, nt = psc::model_nterms(p->model);
+    if (n == 0) return PSC_OK;
+    if (!on_device) {
+        for (long long i = 0; i < n; ++i) {
+            double *d = dvdf ? dvdf + i * nf : nullptr, *t = terms ? terms + i * nt : nullptr;
+            double *m = mass_sq ? mass_sq + i * nf : nullptr;
+            if (p->precision == 32) model_point<float>(p->model, p->gsq, nf, fields + i * nf, d, t, m);
+            else model_point<double>(p->model, p->gsq, nf, fields + i * nf, d, t, m);
+        }
+        return PSC_OK;
+    }
+    const size_t fb = sizeof(double) * (size_t)n * nf, tb = sizeof(double) * (size_t)n * nt;
+    double *dev = nullptr;
+    CU(cudaMalloc(&dev, 3 * fb + tb));
+    double *df = dev, *dd = dev + (size_t)n * nf, *dm = dd + (size_t)n * nf, *dt = dm + (size_t)n * nf;
+    int rc = PSC_OK;
+    cudaError_t e = cudaMemcpy(df, fields, fb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        const int blocks = (int)std::min<long long>((n + 255) / 256, 4096);
+        if (p->precision == 32)
+            k_model_eval<float><<<blocks, 256>>>(p->model, p->gsq, nf, n, df, dd, dt, dm);
+        else
+            k_model_eval<double><<<blocks, 256>>>(p->model, p->gsq, nf, n, df, dd, dt, dm);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess && dvdf) e = cudaMemcpy(dvdf, dd, fb, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && terms) e = cudaMemcpy(terms, dt, tb, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && mass_sq) e = cudaMemcpy(mass_sq, dm, fb, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) rc = fail(PSC_ERR_CUDA, cudaGetErrorString(e));
+    cudaFree(dev);
+    return rc;
+}
+
 
 void psc_default_params(psc_params *p) {
     if (!p) return;
@@ -1110,6 +1517,30 @@ int psc_time_passes(psc_handle *h, int reps, float *ms) {
     return PSC_OK;
 }
 
+int psc_autotune(psc_handle *h, int reps, int *shape, int *from_cache) {
+    if (!h || reps < 1) return fail(PSC_ERR_ARG, "bad argument");
+    return autotune(h, reps, shape, from_cache);
+}
+
+int psc_set_shapes(psc_handle *h, const int *shape) {
+    if (!h || !shape) return fail(PSC_ERR_ARG, "null argument");
+    if (!h->cfg.g.reg || h->padded) return PSC_OK;
+    psc::TileChoice tc;
+    tc.xy_shift = shape[0];
+    tc.z_shift = shape[1];
+    tc.z_per_sm = shape[2];
+    return apply_shapes(h, tc);
+}
+
+int psc_get_shapes(psc_handle *h, int *shape) {
+    if (!h || !shape) return fail(PSC_ERR_ARG, "null argument");
+    const bool tunable = h->cfg.g.reg && !h->padded;
+    shape[0] = tunable ? h->cfg.tc.xy_shift : -1;
+    shape[1] = tunable ? h->cfg.tc.z_shift : -1;
+    shape[2] = tunable ? h->cfg.tc.z_per_sm : -1;
+    return PSC_OK;
+}
+
 // the bounded wait of the bulk-copy staging on an mbarrier whose transactions never
 // arrive: thread 0 expects 16 bytes that no copy delivers
 __global__ void k_bulk_wait_selftest(int *out, unsigned long long limit_ns) {
@@ -1206,6 +1637,11 @@ int psc_means(psc_handle *h, double *out) {
     return means(h, 0, out);
 }
 
+int psc_mass_sq_av(psc_handle *h, double *out) {
+    if (!h || !out) return fail(PSC_ERR_ARG, "null argument");
+    return mass_sq_av(h, 0, out);
+}
+
 // ------------------------------------------------------------------ batches
 int psc_batch_create(const psc_params *per_realization, int n, psc_batch **out) {
     if (!out || !per_realization || n < 1) return fail(PSC_ERR_ARG, "bad argument");
@@ -1253,7 +1689,22 @@ int psc_batch_create(const psc_params *per_realization, int n, psc_batch **out) 
     for (auto &e : b->join)
         if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
             return bail(fail(PSC_ERR_CUDA, "batch event creation failed"));
+    if (int rc = batch_multi_setup(b)) return bail(rc);
     *out = b;
+    return PSC_OK;
+}
+
+int psc_batch_launch_mode(psc_batch *b, int per_group, int *one_launch_per_pass) {
+    if (!b) return fail(PSC_ERR_ARG, "null batch");
+    if (per_group >= 0) {
+        b->per_group = per_group != 0;
+        if (int rc = batch_multi_setup(b)) return rc;
+        if (b->gexec) {
+            cudaGraphExecDestroy(b->gexec);
+            b->gexec = nullptr;
+        }
+    }
+    if (one_launch_per_pass) *one_launch_per_pass = b->multi ? 1 : 0;
     return PSC_OK;
 }
 
@@ -1304,7 +1755,8 @@ int psc_batch_step(psc_batch *b, double dt, int nsteps) {
     };
     if (!b->gexec) {
         CU(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
-        const cudaError_t err = fork_join([&](psc_handle *h) { return enqueue_step(h, h->st); });
+        const cudaError_t err = b->multi ? enqueue_batch_step(b, b->st)
+                                         : fork_join([&](psc_handle *h) { return enqueue_step(h, h->st); });
         int rc = instantiate(b->st, err, &b->gexec);
         if (rc) return rc;
     }
@@ -1318,6 +1770,20 @@ int psc_batch_step(psc_batch *b, double dt, int nsteps) {
         h->diag_valid = true;
         const int err = read_err(h);
         if (err) return fail(err, step_err_msg(err));
+    }
+    return PSC_OK;
+}
+
+int psc_batch_autotune(psc_batch *b, int reps) {
+    if (!b || reps < 1) return fail(PSC_ERR_ARG, "bad argument");
+    for (psc_handle *h : b->groups) {
+        int rc = autotune(h, reps, nullptr, nullptr);
+        if (rc) return rc;
+    }
+    if (int rc = batch_multi_setup(b)) return rc;   // the groups' shapes may have changed
+    if (b->gexec) {
+        cudaGraphExecDestroy(b->gexec);
+        b->gexec = nullptr;
     }
     return PSC_OK;
 }

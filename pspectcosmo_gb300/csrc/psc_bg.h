@@ -4,8 +4,8 @@
 namespace psc {
 
 constexpr int kMaxStages = 31;   // Yoshida-10 (pspectcosmo.h:295-297)
-constexpr int kMaxFields = 2;
-constexpr int kMaxTerms = 2;
+constexpr int kMaxFields = 4;   // PSC_MAX_FIELDS
+constexpr int kMaxTerms = 4;    // PSC_MAX_TERMS
 
 // FP64 background and per-stage coefficients, resident in device memory so a
 // captured step graph needs no host values. Mirrors the reference globals

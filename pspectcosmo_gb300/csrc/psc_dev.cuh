@@ -14,6 +14,7 @@
 
 #include "psc.h"
 #include "psc_bg.h"
+#include "psc_model.h"
 
 namespace psc {
 
@@ -56,20 +57,30 @@ template <bool PK, typename C, typename T> __device__ __forceinline__ C cscale_k
 
 
 // ------------------------------------------------------------------ model (model.h)
-// Device mirror of model.h: V, dV/dphi for the shipped phi^2 model
-// (model.h:35-82) and the two-field phi^2 chi^2 model written in the same API.
+// Per-site evaluation of the model in the arithmetic of the pass: V'(phi) and the potential
+// terms. The built-in models (PSC_MODEL_PHI2, model.h:35-99, and the two-field
+// phi^2 chi^2 model) are written out here; a user model (PSC_MODEL_USER + i) is its model.h
+// compiled in the same precision (psc_user_models.cuh). USER = false compiles the built-in
+// models only: the pass instantiations of the built-in models (nf <= 2) keep the code and
+// registers of the hand-written forms; USER = true adds the user models.
 // The coupling is held in the precision G of the arithmetic that uses it (the field
 // precision in the register engine: no per-site FP64 -> FP32 conversion).
 template <typename G = double>
 struct ModelG {
-    int kind;   // 0 = phi^2, 1 = phi^2 chi^2
+    int kind;   // PSC_MODEL_*
     G gsq;
 };
 using Model = ModelG<double>;
 
-template <typename T, typename G>
-__device__ __forceinline__ void model_dvdf(const ModelG<G> &m, const T *v, T *out, int nf) {
-    if (m.kind == 0) {
+template <typename T, typename G, bool USER = false>
+__host__ __device__ __forceinline__ void model_dvdf(const ModelG<G> &m, const T *v, T *out, int nf) {
+    if constexpr (USER) {
+        if (m.kind >= PSC_MODEL_USER) {
+            um_dvdf<T>(m.kind - PSC_MODEL_USER, v, out, nf);
+            return;
+        }
+    }
+    if (m.kind == PSC_MODEL_PHI2) {
         out[0] = v[0];
     } else {
         const T g = (T)m.gsq;
@@ -81,11 +92,20 @@ __device__ __forceinline__ void model_dvdf(const ModelG<G> &m, const T *v, T *ou
 // Accumulates in A: the field precision for the per-thread partial sums of the
 // register engine (a thread adds a handful of sites before the FP64 block sum),
 // double in the generic engine.
-template <typename T, typename A = double, typename G = double>
-__device__ __forceinline__ void model_potential(const ModelG<G> &m, const T *v, A *terms) {
+template <typename T, typename A = double, typename G = double, bool USER = false>
+__host__ __device__ __forceinline__ void model_potential(const ModelG<G> &m, const T *v, A *terms) {
+    if constexpr (USER) {
+        if (m.kind >= PSC_MODEL_USER) {
+            T t[kMaxTerms] = {};
+            um_potential<T>(m.kind - PSC_MODEL_USER, v, t);
+#pragma unroll
+            for (int i = 0; i < kMaxTerms; ++i) terms[i] += (A)t[i];
+            return;
+        }
+    }
     const A p = (A)v[0];
     terms[0] += A(0.5) * p * p;
-    if (m.kind == 1) {
+    if (m.kind == PSC_MODEL_PHI2CHI2) {
         const A c = (A)v[1];
         terms[1] += A(0.5) * (A)m.gsq * p * p * c * c;
     }
@@ -98,11 +118,20 @@ __device__ __forceinline__ void model_potential(const ModelG<G> &m, const T *v, 
 // after one step, which a'' ~ (V - 2K) amplifies tenfold. Shifted by the terms of the
 // homogeneous fields (homogeneous_potential), the summands are the sites' small deviations.
 // The caller counts its sites and adds count x ref in FP64.
-template <typename T, typename G>
-__device__ __forceinline__ void model_potential_shifted(const ModelG<G> &m, const T *v, const T *ref, T *terms) {
+template <typename T, typename G, bool USER = false>
+__host__ __device__ __forceinline__ void model_potential_shifted(const ModelG<G> &m, const T *v, const T *ref, T *terms) {
+    if constexpr (USER) {
+        if (m.kind >= PSC_MODEL_USER) {
+            T t[kMaxTerms] = {};
+            um_potential<T>(m.kind - PSC_MODEL_USER, v, t);
+#pragma unroll
+            for (int i = 0; i < kMaxTerms; ++i) terms[i] += t[i] - ref[i];
+            return;
+        }
+    }
     const T p = v[0];
     terms[0] += fma(T(0.5) * p, p, -ref[0]);
-    if (m.kind == 1) {
+    if (m.kind == PSC_MODEL_PHI2CHI2) {
         const T c = v[1];
         terms[1] += fma(T(0.5) * (T)m.gsq * p * p * c, c, -ref[1]);
     }
@@ -111,14 +140,21 @@ __device__ __forceinline__ void model_potential_shifted(const ModelG<G> &m, cons
 // The potential terms of the homogeneous fields, the FP64 shadow of the zero modes over
 // N^3 (zero when the shadow is not set): a reference for model_potential_shifted that depends
 // on the state alone, so that resumed and uninterrupted runs sum identically.
-template <typename T, typename G>
+template <typename T, typename G, bool USER = false>
 __device__ __forceinline__ void homogeneous_potential(const ModelG<G> &m, const DevBG *bg, T *ref) {
-    T f[kMaxFields] = {T(0), T(0)};
+    T f[kMaxFields] = {};
     if (bg->zero64)
         for (int q = 0; q < kMaxFields; ++q)
             if (q < bg->nf) f[q] = (T)(bg->z0f[q][0] * bg->inv_n3);
+    if constexpr (USER) {   // ref has kMaxTerms entries (two in the built-in instantiations)
+        for (int i = 0; i < kMaxTerms; ++i) ref[i] = T(0);
+        if (m.kind >= PSC_MODEL_USER) {
+            um_potential<T>(m.kind - PSC_MODEL_USER, f, ref);
+            return;
+        }
+    }
     ref[0] = T(0.5) * f[0] * f[0];
-    ref[1] = m.kind == 1 ? T(0.5) * (T)m.gsq * f[0] * f[0] * f[1] * f[1] : T(0);
+    ref[1] = m.kind == PSC_MODEL_PHI2CHI2 ? T(0.5) * (T)m.gsq * f[0] * f[0] * f[1] * f[1] : T(0);
 }
 
 // ------------------------------------------------------------------ FFT engine

@@ -33,6 +33,7 @@ struct psc_handle {
     double *xfer = nullptr;      // device FP64 scratch of the FP32 upload (one chunk)
     size_t xfer_elems = 0;
     std::vector<void *> allocs;
+    size_t partKG_cap = 0, partV_cap = 0;   // doubles held by b.partKG, b.partV (the autotuner may grow them)
     void *adj = nullptr;         // adjoint workspace (psc_adjoint.cu), owned by the handle
     void (*adj_free)(void *) = nullptr;
     void *ana = nullptr;         // analytic pre-lattice phase (psc_analytic.cu), owned by the handle

@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "psc_ic.h"
+#include "psc_model.h"
 
 namespace psc {
 namespace {
@@ -66,19 +67,12 @@ struct Ctx {
     }
 };
 
+// potential_energy / effective_mass of the run's model (model.h:36-100), FP64
 double potential_term(const psc_params &p, int term, const double *v) {
-    if (p.model == PSC_MODEL_PHI2 || term == 0) return 0.5 * pw2(v[0]);
-    return 0.5 * p.gsq * pw2(v[0]) * pw2(v[1]);
+    return model_potential_term(p.model, p.gsq, term, v);
 }
 
-void effective_mass(const psc_params &p, double *m2, const double *v) {
-    if (p.model == PSC_MODEL_PHI2) {
-        m2[0] = 1.;
-        return;
-    }
-    m2[0] = 1. + p.gsq * pw2(v[1]);
-    m2[1] = p.gsq * pw2(v[0]);
-}
+void effective_mass(const psc_params &p, double *m2, const double *v) { model_effective_mass(p.model, p.gsq, m2, v); }
 
 // one mode of one field (set_mode)
 void set_mode(Ctx &c, double p2, double m2, double *fk, double *pk, bool isReal) {
@@ -249,7 +243,7 @@ ICSetup ic_setup(const psc_params &p) {
     if (p.expansion > 0) {
         double fdsq = 0., pot = 0.;
         for (int fld = 0; fld < nf; fld++) fdsq += pw2(s.fd0[fld]);
-        const int nterms = p.model == PSC_MODEL_PHI2 ? 1 : 2;
+        const int nterms = model_nterms(p.model);
         for (int t = 0; t < nterms; t++) pot += potential_term(p, t, s.f0);
         double h = fdsq / 2.;
         h += pot;
@@ -277,7 +271,7 @@ ICInfo generate_ic(const psc_params &p, double *f_k, double *pi_k, double *u_k, 
     const int N = c.N, H = c.H, nf = p.nflds;
     const double dp2 = pw2(p.kIR);
     const long long M2 = 2 * c.modes;
-    double initial_f[2] = {0, 0}, initial_fd[2] = {0, 0}, mass_sq[2] = {0, 0};
+    double initial_f[PSC_MAX_FIELDS] = {}, initial_fd[PSC_MAX_FIELDS] = {}, mass_sq[PSC_MAX_FIELDS] = {};
     for (int fld = 0; fld < nf; fld++) {
         initial_f[fld] = p.initfield[fld] / c.fStar;
         initial_fd[fld] = p.initderivs[fld] / c.fStar / c.omegaStar;
@@ -289,7 +283,7 @@ ICInfo generate_ic(const psc_params &p, double *f_k, double *pi_k, double *u_k, 
     if (p.expansion > 0) {
         double fdsq = 0., pot = 0.;
         for (int fld = 0; fld < nf; fld++) fdsq += pw2(initial_fd[fld]);
-        const int nterms = p.model == PSC_MODEL_PHI2 ? 1 : 2;
+        const int nterms = model_nterms(p.model);
         for (int t = 0; t < nterms; t++) pot += potential_term(p, t, initial_f);
         double h = fdsq / 2.;
         h += pot;

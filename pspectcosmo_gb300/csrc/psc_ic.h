@@ -24,7 +24,7 @@ struct ICSetup {
     double norm_s;       // sqrt(DFDP): scalar mode amplitude factor
     double norm_gw;      // MPl omegaStar / fStar^2 (N/dx)^1.5: GW mode amplitude factor
     double n3;
-    double m2[2], f0[2], fd0[2];
+    double m2[PSC_MAX_FIELDS], f0[PSC_MAX_FIELDS], fd0[PSC_MAX_FIELDS];
     int seed;
     long long visits;    // modes visited per scalar field (initialize.cpp:686-749)
     int dpm;             // draws per scalar mode: 1 (fixed amplitude) or 4 (Rayleigh)

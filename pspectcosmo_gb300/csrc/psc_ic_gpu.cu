@@ -46,7 +46,7 @@ __device__ __forceinline__ unsigned long long pm_pow(unsigned long long n, const
 struct ICDev {
     int N, H, nf, model, gw, simulate_inflation, dpm;
     double k2c, dp2, kIR, gsq, a, hubble, aop, norm_s, norm_gw, n3;
-    double m2[2], f0[2], fd0[2];
+    double m2[PSC_MAX_FIELDS], f0[PSC_MAX_FIELDS], fd0[PSC_MAX_FIELDS];
     long long visits;
     unsigned long long x0;   // seed (>= 1)
     unsigned long long pw[64];
@@ -302,7 +302,7 @@ int ic_device(psc_handle *h, int r, ICInfo *info) {
     d.norm_s = s.norm_s;
     d.norm_gw = s.norm_gw;
     d.n3 = s.n3;
-    for (int q = 0; q < 2; ++q) {
+    for (int q = 0; q < PSC_MAX_FIELDS; ++q) {
         d.m2[q] = s.m2[q];
         d.f0[q] = s.f0[q];
         d.fd0[q] = s.fd0[q];

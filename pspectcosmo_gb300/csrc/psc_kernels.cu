@@ -247,21 +247,22 @@ __global__ void __launch_bounds__(256) k_zpass(Geo g, const cplx<T> *__restrict_
     Model mdl;
     mdl.kind = g.model;
     mdl.gsq = g.gsq;
-    double pot[kMaxTerms] = {0.0, 0.0};
+    double pot[kMaxTerms] = {};
+    constexpr int NIN = 4 * kMaxFields, NOUT = kMaxFields + 6;
     for (int idx = threadIdx.x; idx < TL * M; idx += blockDim.x) {
         const int t = idx & (TL - 1), k = idx >> sh;
         if (line0 + t >= g.lines_z) continue;
         const int e = k * LD + t;
-        C in[8];
+        C in[NIN];
 #pragma unroll
-        for (int o = 0; o < 8; ++o)
+        for (int o = 0; o < NIN; ++o)
             if (o < nin) in[o] = slots[(size_t)o * M * LD + e];
-        C out[8];
+        C out[NOUT];
 #pragma unroll
         for (int half = 0; half < 2; ++half) {
-            T f[2], vp[2];
+            T f[kMaxFields], vp[kMaxFields];
 #pragma unroll
-            for (int fl = 0; fl < 2; ++fl) {
+            for (int fl = 0; fl < kMaxFields; ++fl) {
                 if (fl < nf) {
                     const C c = in[GW ? fl * 4 : fl];
                     f[fl] = half ? c.y : c.x;
@@ -269,15 +270,15 @@ __global__ void __launch_bounds__(256) k_zpass(Geo g, const cplx<T> *__restrict_
                     f[fl] = T(0);
                 }
             }
-            model_dvdf<T>(mdl, f, vp, nf);
-            model_potential<T>(mdl, f, pot);
+            model_dvdf<T, double, true>(mdl, f, vp, nf);
+            model_potential<T, double, double, true>(mdl, f, pot);
 #pragma unroll
-            for (int fl = 0; fl < 2; ++fl)
+            for (int fl = 0; fl < kMaxFields; ++fl)
                 if (fl < nf) { if (half) out[fl].y = vp[fl]; else out[fl].x = vp[fl]; }
             if (GW) {
-                T d[2][3];
+                T d[kMaxFields][3];
 #pragma unroll
-                for (int fl = 0; fl < 2; ++fl)
+                for (int fl = 0; fl < kMaxFields; ++fl)
 #pragma unroll
                     for (int ax = 0; ax < 3; ++ax)
                         d[fl][ax] = (fl < nf) ? (half ? in[fl * 4 + 1 + ax].y : in[fl * 4 + 1 + ax].x) : T(0);
@@ -286,14 +287,14 @@ __global__ void __launch_bounds__(256) k_zpass(Geo g, const cplx<T> *__restrict_
                 for (int c = 0; c < 6; ++c) {
                     T sum = T(0);
 #pragma unroll
-                    for (int fl = 0; fl < 2; ++fl)
+                    for (int fl = 0; fl < kMaxFields; ++fl)
                         if (fl < nf) sum += T(2) * d[fl][si[c]] * d[fl][sj[c]];
                     if (half) out[nf + c].y = sum; else out[nf + c].x = sum;
                 }
             }
         }
 #pragma unroll
-        for (int o = 0; o < 8; ++o)
+        for (int o = 0; o < NOUT; ++o)
             if (o < nout) slots[(size_t)o * M * LD + e] = out[o];
     }
     block_reduce_store<kMaxTerms>(pot, partV, gridDim.x, blockIdx.x);
@@ -493,17 +494,18 @@ __device__ double friedmann_add(const DevBG *bg, double K, double G, double V) {
 // fk, pk: the realizations' field arrays (realization blockIdx.x at blockIdx.x fstride
 // elements), for the homogeneous mode's shadow. SCALAR_PRIME with p = 1: the opening half
 // kick uses the kept force.
-__global__ void __launch_bounds__(1024) k_scalar(DevBG *bg, const double *__restrict__ partKG,
-                                                const double *__restrict__ partV, int mode, int p, int pkg_stride,
-                                                int pv_stride, void *fk, void *pk, long long fstride,
-                                                long long modes) {
+// r: the realization (the block of one configuration's kernel; the batched background kernel
+// passes a realization of one of its configurations)
+__device__ __forceinline__ void k_scalar_body(unsigned r, DevBG *bg, const double *__restrict__ partKG,
+                                              const double *__restrict__ partV, int mode, int p, int pkg_stride,
+                                              int pv_stride, void *fk, void *pk, long long fstride, long long modes) {
     constexpr int NQ = 2 * kMaxFields + kMaxTerms;
     __shared__ double red[32][NQ];
-    bg += blockIdx.x;
-    partKG += (size_t)blockIdx.x * pkg_stride;
-    partV += (size_t)blockIdx.x * pv_stride;
+    bg += r;
+    partKG += (size_t)r * pkg_stride;
+    partV += (size_t)r * pv_stride;
     {
-        const size_t off = (size_t)blockIdx.x * fstride * (bg->fp32 ? sizeof(float2) : sizeof(double2));
+        const size_t off = (size_t)r * fstride * (bg->fp32 ? sizeof(float2) : sizeof(double2));
         fk = static_cast<char *>(fk) + off;
         pk = static_cast<char *>(pk) + off;
     }
@@ -623,6 +625,13 @@ __global__ void __launch_bounds__(1024) k_scalar(DevBG *bg, const double *__rest
         bg->ad_stale = bg->ad;
         begin_stage(bg, 0);
     }
+}
+
+__global__ void __launch_bounds__(1024) k_scalar(DevBG *bg, const double *__restrict__ partKG,
+                                                const double *__restrict__ partV, int mode, int p, int pkg_stride,
+                                                int pv_stride, void *fk, void *pk, long long fstride,
+                                                long long modes) {
+    k_scalar_body(blockIdx.x, bg, partKG, partV, mode, p, pkg_stride, pv_stride, fk, pk, fstride, modes);
 }
 
 // the homogeneous modes' FP64 shadow taken from the arrays (after a device-side writer)
@@ -822,7 +831,7 @@ static int ilog2i(int v) {
     return l;
 }
 
-void plan(const psc_params &p, int R, LaunchCfg *cfg) {
+void plan(const psc_params &p, int R, LaunchCfg *cfg, const TileChoice *tc) {
     Geo &g = cfg->g;
     cfg->R = R;
     g.N = p.N;
@@ -832,7 +841,7 @@ void plan(const psc_params &p, int R, LaunchCfg *cfg) {
     g.gw = p.with_gw ? 1 : 0;
     g.gwev = (p.with_gw && !p.spectral) ? 1 : 0;
     g.model = p.model;
-    g.nterms = p.model == PSC_MODEL_PHI2 ? 1 : 2;
+    g.nterms = model_nterms(p.model);
     g.mask = (p.spectral && p.simulate_inflation) ? 1 : 0;
     g.gsq = p.gsq;
     g.kIR = p.kIR;
@@ -854,24 +863,32 @@ void plan(const psc_params &p, int R, LaunchCfg *cfg) {
         const int xy_thr = (g.N >= 1024 && p.precision == 32) ? 512 : 256;
         int tl = xy_thr / P;
         while (tl > 1 && tl / 2 >= g.lines_x) tl /= 2;
+        if (tc && tc->xy_shift >= 0 && (1 << tc->xy_shift) < tl) tl = 1 << tc->xy_shift;
         g.tlx_shift = ilog2i(tl);
+        cfg->tc.xy_shift = g.tlx_shift;
         cfg->thr_xy = tl * P;
         cfg->smem_xy = (size_t)tl * g.N * csize;
         cfg->smem_xf = 3 * cfg->smem_xy;
         cfg->nbx = (g.lines_x + tl - 1) / tl;
         const int Pz = g.M / 16;
-        int tlz = 256 / (nin * Pz);
-        if (tlz < 1) tlz = 1;
+        int tlz = 1;   // lines per tile: the largest power of two with nin x tlz x Pz <= 256 threads
+        while (2 * tlz * nin * Pz <= 256) tlz *= 2;
+        if (tc && tc->z_shift >= 0 && (1 << tc->z_shift) < tlz) tlz = 1 << tc->z_shift;
         g.tlz_shift = ilog2i(tlz);
+        cfg->tc.z_shift = g.tlz_shift;
         g.ldz = 0;
         cfg->thr_z = nin * tlz * Pz;
         // Z pass shared memory. Without GWs (kr_zpass): nf work slots + nf staging slots of
         // half-length lines, persistent (2 blocks per SM). With GWs (kr_zpass_gw): four
         // slots of N-point lines and, in FP32 (persistent, 3 blocks per SM, next tile
         // staged), the nf x 3 input lines of a tile; in FP64 one tile per block.
+        // A user model (up to kMaxFields fields) runs the USER instantiations: nslot work
+        // slots (input pairs 2 nf, output pairs (nf + 7) / 2) and at most 2 blocks per SM.
         const bool gw_staged = g.gwev && p.precision == 32;
+        const bool user = model_is_user(p.model);
+        const int gw_slots = user ? ((2 * g.nf > (g.nf + 7) / 2) ? 2 * g.nf : (g.nf + 7) / 2) : 4;
         if (g.gwev)
-            cfg->smem_z = ((size_t)4 * tlz * (g.N + g.N / 16 + 1) +
+            cfg->smem_z = ((size_t)gw_slots * tlz * (g.N + g.N / 16 + 1) +
                            (gw_staged ? (size_t)g.nf * 3 * tlz * (g.M + 2) : 0)) * csize;
         else
             cfg->smem_z = (size_t)2 * g.nf * tlz * (g.M + g.M / 16 + 1) * csize;
@@ -882,8 +899,10 @@ void plan(const psc_params &p, int R, LaunchCfg *cfg) {
             sms = 152;
         const size_t smem_sm = 227 * 1024;
         int per_sm = (int)(smem_sm / cfg->smem_z);
-        if (per_sm > (gw_staged ? 3 : 2)) per_sm = gw_staged ? 3 : 2;
+        if (per_sm > ((gw_staged && !user) ? 3 : 2)) per_sm = (gw_staged && !user) ? 3 : 2;
+        if (tc && tc->z_per_sm > 0 && tc->z_per_sm < per_sm) per_sm = tc->z_per_sm;
         if (per_sm < 1) per_sm = 1;
+        cfg->tc.z_per_sm = per_sm;
         cfg->nbz = ((g.gwev && !gw_staged) || ntiles < per_sm * sms) ? ntiles : per_sm * sms;
         g.pkg_stride = 2 * kMaxFields * cfg->nbx;
         g.pv_stride = kMaxTerms * cfg->nbz;
@@ -1011,6 +1030,28 @@ cudaError_t launch_stage(const LaunchCfg &cfg, const Buffers &b, int precision, 
         return precision == 32 ? reg_stage_f32(cfg, b, drift, st, nullptr, -1)
                                : reg_stage_f64(cfg, b, drift, st, nullptr, -1);
     return precision == 32 ? launch_stage_t<float>(cfg, b, drift, st) : launch_stage_t<double>(cfg, b, drift, st);
+}
+
+// SCALAR_END of stage p for every realization of every configuration of a batch: block i is
+// realization i of the concatenated list (the groups' realizations in order). 1024 threads, as
+// k_scalar: the partial sums add up in the same order, so the background is the same bits.
+__global__ void __launch_bounds__(1024) k_scalar_batch(const __grid_constant__ BatchTable bt, int p) {
+    unsigned r = blockIdx.x;
+    int gi = 0;
+    while (gi + 1 < bt.ngroups && r >= (unsigned)bt.grp[gi].R) {
+        r -= (unsigned)bt.grp[gi].R;
+        ++gi;
+    }
+    const BatchGroup &G = bt.grp[gi];
+    k_scalar_body(r, G.bg, G.partKG, G.partV, SCALAR_END, p, G.g.pkg_stride, G.g.pv_stride, G.fk, G.pk, G.g.fstride,
+                  G.g.modes);
+}
+
+cudaError_t launch_scalar_batch(const BatchTable &bt, int p, cudaStream_t st) {
+    int n = 0;
+    for (int i = 0; i < bt.ngroups; ++i) n += bt.grp[i].R;
+    k_scalar_batch<<<n, 1024, 0, st>>>(bt, p);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_scalar(const LaunchCfg &cfg, const Buffers &b, int mode, int p, cudaStream_t st) {

@@ -33,8 +33,18 @@ struct Geo {
     int pkg_stride, pv_stride;
 };
 
+// Tile and grid shapes of the register-engine passes that the autotuner (psc_autotune)
+// chooses among; -1 / 0 = the planner's default. xy_shift: log2 lines per tile of the X and Y
+// passes (at most the default, which fills the passes' block size); z_shift: log2 lines per
+// tile of the Z pass (at most the default); z_per_sm: resident blocks per SM of the persistent
+// Z passes (1 .. the kernel's launch-bound minimum).
+struct TileChoice {
+    int xy_shift = -1, z_shift = -1, z_per_sm = 0;
+};
+
 struct LaunchCfg {
     Geo g;
+    TileChoice tc;               // the shapes in use (defaults resolved)
     int R;                       // realizations advanced together (1 for a single lattice)
     int thr_xy, thr_z;           // threads per block
     size_t smem_xy, smem_z;      // dynamic shared memory bytes
@@ -67,6 +77,36 @@ struct Buffers {
     void *Fk, *Fu;
 };
 
+// Up to eight arrays of the forward passes (V' of each field, then S_ab) with the realization
+// stride of each (elements).
+struct ArrList8 {
+    void *p[8];
+    long long rs[8];
+};
+
+// Batches of several configurations (lattice sizes) advanced by ONE launch per pass: the work
+// list of each pass is the concatenation of every configuration's blocks (group i owns the
+// items [start[pass], start[pass] + count)); a block of the batched kernel walks the items
+// blockIdx.x, blockIdx.x + gridDim.x, ... and runs each with its configuration's geometry and
+// buffers. Passes: 0 X inverse (+ drift), 1 Y inverse, 2 Z, 3 Y forward, 4 X forward + kick.
+constexpr int kMaxBatchGroups = 4;
+constexpr int kBatchPasses = 5;
+struct BatchGroup {
+    Geo g;
+    int L;                       // N: line length of the X / Y passes
+    int nbx, nbz, R, nj;         // X/Y blocks per array, Z blocks per realization, realizations, forward arrays
+    int start[kBatchPasses];     // first item of this group in each pass's work list
+    void *fk, *pk, *uk, *puk, *TA, *TB, *TC, *QV, *QS, *tw, *Fk, *Fu;
+    double *partKG, *partV;
+    DevBG *bg;
+    ArrList8 fwd;                // the forward passes' arrays
+};
+struct BatchTable {
+    int ngroups;
+    int total[kBatchPasses];     // items of each pass
+    BatchGroup grp[kMaxBatchGroups];
+};
+
 enum ScalarMode {
     SCALAR_PRIME = 0,   // coefficients for the opening half kick of a call
     SCALAR_BEGIN = 1,   // start of a step: b = ad, begin stage 0
@@ -75,8 +115,9 @@ enum ScalarMode {
     SCALAR_EVAL_END = 4 // reductions of an evaluation -> K, G, V, a''
 };
 
-// Tile sizes, block sizes and shared memory for R lattices of one configuration.
-void plan(const psc_params &p, int R, LaunchCfg *cfg);
+// Tile sizes, block sizes and shared memory for R lattices of one configuration; tc (may be
+// null) overrides the default shapes of the register engine within their limits.
+void plan(const psc_params &p, int R, LaunchCfg *cfg, const TileChoice *tc = nullptr);
 // Set the dynamic shared-memory limits of the kernels a configuration uses.
 cudaError_t configure(const LaunchCfg &cfg, int precision);
 
@@ -112,6 +153,22 @@ cudaError_t reg_stage_f32(const LaunchCfg &cfg, const Buffers &b, int drift, cud
                           int scalar_mode);
 cudaError_t reg_stage_f64(const LaunchCfg &cfg, const Buffers &b, int drift, cudaStream_t st, cudaEvent_t *ev,
                           int scalar_mode);
+// The fused Z pass for the user models (model.h files compiled in, up to PSC_MAX_FIELDS
+// fields): its shared-memory limits and its launch for R realizations.
+cudaError_t reg_configure_user_f32(const LaunchCfg &cfg);
+cudaError_t reg_configure_user_f64(const LaunchCfg &cfg);
+cudaError_t reg_zpass_user_f32(const LaunchCfg &cfg, const Buffers &b, cudaStream_t st, int R);
+cudaError_t reg_zpass_user_f64(const LaunchCfg &cfg, const Buffers &b, cudaStream_t st, int R);
+// One pass of a batch over all its configurations (BatchTable): grid blocks of 256 threads with
+// smem bytes of dynamic shared memory; the line lengths of the register engine up to 256.
+cudaError_t reg_batch_pass_f32(const BatchTable &bt, int pass, int drift, int grid, size_t smem, cudaStream_t st);
+cudaError_t reg_batch_pass_f64(const BatchTable &bt, int pass, int drift, int grid, size_t smem, cudaStream_t st);
+// The kernel behind reg_batch_pass_* (for occupancy queries and shared-memory limits).
+const void *reg_batch_kernel_f32(int pass, int drift);
+const void *reg_batch_kernel_f64(int pass, int drift);
+// The background update at the end of stage p for every realization of every configuration
+// of the batch (k_scalar's SCALAR_END), one launch.
+cudaError_t launch_scalar_batch(const BatchTable &bt, int p, cudaStream_t st);
 cudaError_t reg_pad_passes_f32(const LaunchCfg &cfg, const Buffers &b, cudaStream_t st);
 cudaError_t reg_pad_passes_f64(const LaunchCfg &cfg, const Buffers &b, cudaStream_t st);
 // The padded step's force evaluation (psc_pad.cu): drift (drift != 0) and padding of f_k

@@ -53,14 +53,22 @@ __global__ void __launch_bounds__(kOutThreads) k_deriv_axis(const cplx<T> *__res
 template <typename T>
 __global__ void __launch_bounds__(kOutThreads) k_snap_pot(const T *__restrict__ real, double *__restrict__ pot,
                                                           double *__restrict__ tot, long long sites, int model,
-                                                          double gsq) {
+                                                          double gsq, int nf) {
     const long long stride = (long long)gridDim.x * blockDim.x;
+    const int nt = model_nterms(model);
     for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < sites; s += stride) {
-        const double phi = (double)real[s];
-        double v = 0.0 + 0.5 * (phi * phi);
-        if (model == 1) {
-            const double chi = (double)real[sites + s];
-            v += 0.5 * gsq * (phi * phi) * (chi * chi);
+        double v = 0.0;
+        if (model_is_user(model)) {
+            double f[kMaxFields] = {};
+            for (int q = 0; q < nf; ++q) f[q] = (double)real[q * sites + s];
+            for (int t = 0; t < nt; ++t) v += model_potential_term(model, gsq, t, f);
+        } else {
+            const double phi = (double)real[s];
+            v += 0.5 * (phi * phi);
+            if (model == PSC_MODEL_PHI2CHI2) {
+                const double chi = (double)real[sites + s];
+                v += 0.5 * gsq * (phi * phi) * (chi * chi);
+            }
         }
         pot[s] = v;
         tot[s] = v;
@@ -464,7 +472,7 @@ int snapshot_t(psc_handle *h, int r, int want_fields, int with_energy, Sink &sin
     tot = work + g.sites;
     auto run = [&]() -> int {
         const T *real = static_cast<const T *>(h->b.real);
-        k_snap_pot<T><<<kOutBlocks, kOutThreads, 0, h->st>>>(real, work, tot, g.sites, g.model, g.gsq);
+        k_snap_pot<T><<<kOutBlocks, kOutThreads, 0, h->st>>>(real, work, tot, g.sites, g.model, g.gsq, g.nf);
         CU(cudaGetLastError());
         int rc2 = sink.energy(0, work);
         if (rc2) return rc2;

@@ -24,30 +24,49 @@ namespace psc {
 template <int L> constexpr int xy_threads() { return L >= 1024 ? 512 : 256; }
 template <int L> constexpr int xy_blocks(int k) { return L >= 1024 ? 1 : k; }
 
+// The block a pass body works on: its indices and the width of the grid along x (the stride
+// of the persistent Z passes). A kernel of one lattice (or of R realizations of one
+// configuration) passes its own blockIdx and gridDim; the batched kernels of several
+// configurations pass a block of one configuration's grid.
+// HwBlock reads the hardware indices where they are used (no registers held for them, as in a
+// kernel written with blockIdx); VBlock carries the indices of a block of another grid.
+struct HwBlock {
+    __device__ __forceinline__ unsigned x() const { return blockIdx.x; }
+    __device__ __forceinline__ unsigned y() const { return blockIdx.y; }
+    __device__ __forceinline__ unsigned z() const { return blockIdx.z; }
+    __device__ __forceinline__ unsigned gx() const { return gridDim.x; }
+};
+struct VBlock {
+    unsigned x_, y_, z_, gx_;
+    __device__ __forceinline__ unsigned x() const { return x_; }
+    __device__ __forceinline__ unsigned y() const { return y_; }
+    __device__ __forceinline__ unsigned z() const { return z_; }
+    __device__ __forceinline__ unsigned gx() const { return gx_; }
+};
+__device__ __forceinline__ HwBlock vblock_hw() { return HwBlock{}; }
+
 
 // ------------------------------------------------------------------ X inverse (+ drift, + x-derivative)
-template <typename T, int L, bool GW, bool DRIFT>
-__global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_ifft_x(Geo g, cplx<T> *__restrict__ fk, const cplx<T> *__restrict__ pk,
-                                                 cplx<T> *__restrict__ TA, cplx<T> *__restrict__ TB,
-                                                 const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw) {
+template <typename T, int L, bool GW, bool DRIFT, class VB>
+__device__ __forceinline__ void kr_ifft_x_body(const VB &vb, Geo g, cplx<T> *__restrict__ fk, const cplx<T> *__restrict__ pk, cplx<T> *__restrict__ TA, cplx<T> *__restrict__ TB, const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw) {
     using C = cplx<T>;
     using RP = RegPlan<L>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *sm = reinterpret_cast<C *>(smem_raw);
     {
-        const long long rf = (long long)blockIdx.z * g.fstride;
+        const long long rf = (long long)vb.z() * g.fstride;
         fk += rf;
         if (DRIFT) pk += rf;
         TA += rf;
         if (GW) TB += rf;
-        bg += blockIdx.z;
+        bg += vb.z();
     }
     const int sh = g.tlx_shift, TL = 1 << sh;
     const int t = threadIdx.x & (TL - 1), j = threadIdx.x >> sh;
-    const int line = blockIdx.x * TL + t;
+    const int line = vb.x() * TL + t;
     const bool valid = line < g.lines_x;
     const long long stride = g.lines_x;
-    const long long base = (long long)blockIdx.y * g.modes + line;
+    const long long base = (long long)vb.y() * g.modes + line;
     auto ix = [&](int n) { return n * TL + t; };
     const T c = DRIFT ? (T)bg->c_drift : T(0);
     const T kIR = GW ? (T)bg->kIR : T(0);
@@ -75,7 +94,7 @@ __global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_ifft_x(Ge
             if (line == 0 && j == 0 && bg->zero64) {
                 // the homogeneous mode (element 0 of the line x = y = kz = 0) is the background
                 // kernel's FP64 shadow, already drifted
-                v[0] = mk<T>((T)bg->z0f[blockIdx.y][0], (T)bg->z0f[blockIdx.y][1]);
+                v[0] = mk<T>((T)bg->z0f[vb.y()][0], (T)bg->z0f[vb.y()][1]);
                 fk[base] = v[0];
             }
         }
@@ -98,17 +117,24 @@ __global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_ifft_x(Ge
     }
 }
 
+template <typename T, int L, bool GW, bool DRIFT>
+__global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_ifft_x(Geo g, cplx<T> *__restrict__ fk, const cplx<T> *__restrict__ pk,
+                                                 cplx<T> *__restrict__ TA, cplx<T> *__restrict__ TB,
+                                                 const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw) {
+    kr_ifft_x_body<T, L, GW, DRIFT, HwBlock>(vblock_hw(), g, fk, pk, TA, TB, bg, tw);
+}
+
 // ------------------------------------------------------------------ Y passes
 // One transform of a tile of Y lines (l = x H + kz, element y at (x N + y) H + kz):
 // src -> dst (may alias), optional i k_y multiplier. Ends with a barrier.
-template <typename T, int L, int DIR>
-__device__ __forceinline__ void ry_tile(const Geo &g, const cplx<T> *src, cplx<T> *dst, bool deriv, T kIR, cplx<T> *sm,
-                                        const cplx<T> *__restrict__ tw) {
+template <typename T, int L, int DIR, class VB>
+__device__ __forceinline__ void ry_tile(const VB &vb, const Geo &g, const cplx<T> *src, cplx<T> *dst, bool deriv, T kIR,
+                                        cplx<T> *sm, const cplx<T> *__restrict__ tw) {
     using C = cplx<T>;
     using RP = RegPlan<L>;
     const int sh = g.tlx_shift, TL = 1 << sh;
     const int t = threadIdx.x & (TL - 1), j = threadIdx.x >> sh;
-    const int line = blockIdx.x * TL + t;
+    const int line = vb.x() * TL + t;
     const bool valid = line < g.lines_x;
     const int x = line / g.H, kz = line - x * g.H;
     const long long base = (long long)x * g.N * g.H + kz;
@@ -138,15 +164,13 @@ __device__ __forceinline__ void ry_tile(const Geo &g, const cplx<T> *src, cplx<T
     __syncthreads();
 }
 
-template <typename T, int L, bool GW>
-__global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_ifft_y(Geo g, cplx<T> *__restrict__ TA, cplx<T> *__restrict__ TB,
-                                                 cplx<T> *__restrict__ TC, const DevBG *__restrict__ bg,
-                                                 const cplx<T> *__restrict__ tw) {
+template <typename T, int L, bool GW, class VB>
+__device__ __forceinline__ void kr_ifft_y_body(const VB &vb, Geo g, cplx<T> *__restrict__ TA, cplx<T> *__restrict__ TB, cplx<T> *__restrict__ TC, const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw) {
     using C = cplx<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *sm = reinterpret_cast<C *>(smem_raw);
-    const long long off = (long long)blockIdx.y * g.modes + (long long)blockIdx.z * g.fstride;
-    bg += blockIdx.z;
+    const long long off = (long long)vb.y() * g.modes + (long long)vb.z() * g.fstride;
+    bg += vb.z();
     const T kIR = (T)bg->kIR;
     if (GW) {
         // This thread's TA and TB elements are copied into two shared staging tiles by
@@ -156,7 +180,7 @@ __global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_ifft_y(Ge
         using RP = RegPlan<L>;
         const int sh = g.tlx_shift, TL = 1 << sh;
         const int t = threadIdx.x & (TL - 1), j = threadIdx.x >> sh;
-        const int line = blockIdx.x * TL + t;
+        const int line = vb.x() * TL + t;
         const bool valid = line < g.lines_x;
         const int x = line / g.H, kz = line - x * g.H;
         const long long base = off + (long long)x * g.N * g.H + kz;
@@ -199,45 +223,42 @@ __global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_ifft_y(Ge
             }
         }
     } else {
-        ry_tile<T, L, +1>(g, TA + off, TA + off, false, kIR, sm, tw);
+        ry_tile<T, L, +1, VB>(vb, g, TA + off, TA + off, false, kIR, sm, tw);
     }
 }
 
-struct ArrList8 {
-    void *p[8];
-    long long rs[8];   // realization stride of each array (elements)
-};
+template <typename T, int L, bool GW>
+__global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_ifft_y(Geo g, cplx<T> *__restrict__ TA, cplx<T> *__restrict__ TB,
+                                                 cplx<T> *__restrict__ TC, const DevBG *__restrict__ bg,
+                                                 const cplx<T> *__restrict__ tw) {
+    kr_ifft_y_body<T, L, GW, HwBlock>(vblock_hw(), g, TA, TB, TC, bg, tw);
+}
+
+
+template <typename T, int L, class VB>
+__device__ __forceinline__ void kr_fft_y_body(const VB &vb, Geo g, const ArrList8 &arrs, const cplx<T> *__restrict__ tw) {
+    using C = cplx<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *sm = reinterpret_cast<C *>(smem_raw);
+    C *a = reinterpret_cast<C *>(arrs.p[vb.y()]) + (long long)vb.z() * arrs.rs[vb.y()];
+    ry_tile<T, L, -1, VB>(vb, g, a, a, false, T(0), sm, tw);
+}
 
 template <typename T, int L>
 __global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(3)) kr_fft_y(Geo g, const __grid_constant__ ArrList8 arrs,
                                                  const cplx<T> *__restrict__ tw) {
-    using C = cplx<T>;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    C *sm = reinterpret_cast<C *>(smem_raw);
-    C *a = reinterpret_cast<C *>(arrs.p[blockIdx.y]) + (long long)blockIdx.z * arrs.rs[blockIdx.y];
-    ry_tile<T, L, -1>(g, a, a, false, T(0), sm, tw);
+    kr_fft_y_body<T, L, HwBlock>(vblock_hw(), g, arrs, tw);
 }
 
 // ------------------------------------------------------------------ X forward + kick epilogue
-template <typename T, int L, bool GW>
-__global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_fft_x_final(Geo g, const cplx<T> *__restrict__ QV,
-                                                      const cplx<T> *__restrict__ QS, const cplx<T> *__restrict__ fk,
-                                                      cplx<T> *__restrict__ pk, cplx<T> *__restrict__ uk,
-                                                      cplx<T> *__restrict__ puk, double *__restrict__ partKG,
-                                                      const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw,
-                                                      cplx<T> *__restrict__ tape_f = nullptr,
-                                                      cplx<T> *__restrict__ tape_p = nullptr,
-                                                      cplx<T> *__restrict__ tape_vp = nullptr,
-                                                      cplx<T> *__restrict__ tape_pu = nullptr,
-                                                      cplx<T> *__restrict__ tape_fu = nullptr,
-                                                      cplx<T> *__restrict__ fcache = nullptr,
-                                                      cplx<T> *__restrict__ ucache = nullptr) {
+template <typename T, int L, bool GW, class VB>
+__device__ __forceinline__ void kr_fft_x_final_body(const VB &vb, Geo g, const cplx<T> *__restrict__ QV, const cplx<T> *__restrict__ QS, const cplx<T> *__restrict__ fk, cplx<T> *__restrict__ pk, cplx<T> *__restrict__ uk, cplx<T> *__restrict__ puk, double *__restrict__ partKG, const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw, cplx<T> *__restrict__ tape_f, cplx<T> *__restrict__ tape_p, cplx<T> *__restrict__ tape_vp, cplx<T> *__restrict__ tape_pu, cplx<T> *__restrict__ tape_fu, cplx<T> *__restrict__ fcache, cplx<T> *__restrict__ ucache) {
     using C = cplx<T>;
     using RP = RegPlan<L>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *sm = reinterpret_cast<C *>(smem_raw);
     {
-        const long long rf = (long long)blockIdx.z * g.fstride, rg = (long long)blockIdx.z * g.gstride;
+        const long long rf = (long long)vb.z() * g.fstride, rg = (long long)vb.z() * g.gstride;
         QV += rf;
         fk += rf;
         pk += rf;
@@ -248,14 +269,14 @@ __global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_fft_x_fin
             uk += rg;
             puk += rg;
         }
-        partKG += (size_t)blockIdx.z * g.pkg_stride;
-        bg += blockIdx.z;
+        partKG += (size_t)vb.z() * g.pkg_stride;
+        bg += vb.z();
     }
     const int sh = g.tlx_shift, TL = 1 << sh, N = g.N, H = g.H, M = g.M;
     const int t = threadIdx.x & (TL - 1), j = threadIdx.x >> sh;
-    const int line = blockIdx.x * TL + t;
+    const int line = vb.x() * TL + t;
     const bool valid = line < g.lines_x;
-    const int job = blockIdx.y;
+    const int job = vb.y();
     const bool field = job < g.nf;
     const long long off = (long long)(field ? job : job - g.nf) * g.modes;
     const C *src = (field ? QV : QS) + off;
@@ -346,7 +367,7 @@ __global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_fft_x_fin
                 }
         }
         T vals[2] = {accK, accG};
-        block_reduce_store_t<T, 2>(vals, partKG + (size_t)(2 * job) * gridDim.x, gridDim.x, blockIdx.x);
+        block_reduce_store_t<T, 2>(vals, partKG + (size_t)(2 * job) * vb.gx(), vb.gx(), vb.x());
     } else if (GW && valid) {
         const T c_drift = (T)bg->c_drift;
 #pragma unroll
@@ -376,6 +397,22 @@ __global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_fft_x_fin
                 }
             }
     }
+}
+
+template <typename T, int L, bool GW>
+__global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_fft_x_final(Geo g, const cplx<T> *__restrict__ QV,
+                                                      const cplx<T> *__restrict__ QS, const cplx<T> *__restrict__ fk,
+                                                      cplx<T> *__restrict__ pk, cplx<T> *__restrict__ uk,
+                                                      cplx<T> *__restrict__ puk, double *__restrict__ partKG,
+                                                      const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw,
+                                                      cplx<T> *__restrict__ tape_f = nullptr,
+                                                      cplx<T> *__restrict__ tape_p = nullptr,
+                                                      cplx<T> *__restrict__ tape_vp = nullptr,
+                                                      cplx<T> *__restrict__ tape_pu = nullptr,
+                                                      cplx<T> *__restrict__ tape_fu = nullptr,
+                                                      cplx<T> *__restrict__ fcache = nullptr,
+                                                      cplx<T> *__restrict__ ucache = nullptr) {
+    kr_fft_x_final_body<T, L, GW, HwBlock>(vblock_hw(), g, QV, QS, fk, pk, uk, puk, partKG, bg, tw, tape_f, tape_p, tape_vp, tape_pu, tape_fu, fcache, ucache);
 }
 
 // ------------------------------------------------------------------ fused Z pass
@@ -431,22 +468,22 @@ __device__ __forceinline__ C partner_out(const C (&v)[16], int j, int q, int r) 
 // the input lines of the next are copied into a staging area by cp.async (no register
 // round trip), so the HBM reads overlap the FFT work. Shared memory: nf work slots, then
 // nf staging slots, TL lines x LS complex each (a complex element holds the real sites
-// 2m, 2m+1). The GW form is kr_zpass_gw.
-template <typename T, int L>
-__global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restrict__ TA, cplx<T> *__restrict__ QV,
-                                                double *__restrict__ partV, const DevBG *__restrict__ bg,
-                                                const cplx<T> *__restrict__ tw, T *__restrict__ tape_fx = nullptr) {
+// 2m, 2m+1). The GW form is kr_zpass_gw. USER = false: the built-in models (nf <= 2);
+// USER = true: any model, up to kMaxFields fields and kMaxTerms potential terms.
+template <typename T, int L, bool USER, class VB>
+__device__ __forceinline__ void kr_zpass_body(const VB &vb, Geo g, const cplx<T> *__restrict__ TA, cplx<T> *__restrict__ QV, double *__restrict__ partV, const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw, T *__restrict__ tape_fx) {
     using C = cplx<T>;
     using RP = RegPlan<L>;
     constexpr int M = L, P = RP::P, LS = ZIdx<L>::LS;
+    constexpr int NF = USER ? kMaxFields : 2, NT = USER ? kMaxTerms : 2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *slots = reinterpret_cast<C *>(smem_raw);
     {
-        const long long rf = (long long)blockIdx.z * g.fstride;
+        const long long rf = (long long)vb.z() * g.fstride;
         TA += rf;
         QV += rf;
-        partV += (size_t)blockIdx.z * g.pv_stride;
-        bg += blockIdx.z;
+        partV += (size_t)vb.z() * g.pv_stride;
+        bg += vb.z();
     }
     const int sh = g.tlz_shift, TL = 1 << sh, H = g.H, N = g.N;
     const int nf = g.nf;
@@ -476,17 +513,17 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
     // <V> partial sums: up to 16 tiles' sites in the field precision, then folded into
     // FP64 (a persistent block walks thousands of tiles at N = 1024; a fold per tile
     // would put a conversion and an add per thread and tile on the narrow FP64 pipe)
-    T pot_t[kMaxTerms] = {T(0), T(0)};
-    double pot_d[kMaxTerms] = {0.0, 0.0};
+    T pot_t[NT] = {};
+    double pot_d[NT] = {};
     int nfold = 0;
     // the sums run over V(site) - vref (model_potential_shifted), vref the potential terms of
     // the homogeneous fields (the FP64 shadow of the zero modes / N^3), a value of the state
     // alone; vref is added back once per site summed (every tile gives a thread the same
     // number of sites: the line count is a multiple of the tile's)
-    T vref[kMaxTerms];
-    homogeneous_potential<T>(mdl, bg, vref);
-    prefetch(blockIdx.x);
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    T vref[NT];
+    homogeneous_potential<T, T, USER>(mdl, bg, vref);
+    prefetch(vb.x());
+    for (int tile = vb.x(); tile < ntiles; tile += vb.gx()) {
         const int line = tile * TL + t;
         const bool valid = line < g.lines_z;
         // 1. complex-to-real along z of field grp: pack X[k], X[M-k] into the M-point
@@ -519,7 +556,7 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
                 v[r] = mk<T>(s.x - td.y, s.y + td.x);
             }
             __syncthreads();   // every thread has read the staging area
-            prefetch(tile + gridDim.x);
+            prefetch(tile + vb.gx());
             fft_reg<C, L, +1, true>(v, slots, ix, j, tw, N / L);
             __syncthreads();
 #pragma unroll
@@ -535,34 +572,34 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
             const long long ln = (long long)tile * TL + tt;
             if (ln >= g.lines_z) continue;
             const int e = tt * LS + m + (m >> 4);
-            C in[2];
+            C in[NF];
 #pragma unroll
-            for (int o = 0; o < 2; ++o)
+            for (int o = 0; o < NF; ++o)
                 if (o < nf) in[o] = slots[o * slot_elems + e];
             if (tape_fx) {   // adjoint tape: the real fields (sites 2m, 2m+1 of the line)
 #pragma unroll
-                for (int fl = 0; fl < 2; ++fl)
+                for (int fl = 0; fl < NF; ++fl)
                     if (fl < nf) reinterpret_cast<C *>(tape_fx + fl * g.sites + ln * N)[m] = in[fl];
             }
-            C out[2];
+            C out[NF];
 #pragma unroll
             for (int half = 0; half < 2; ++half) {
-                T f[2], vp[2];
+                T f[NF], vp[NF];
 #pragma unroll
-                for (int fl = 0; fl < 2; ++fl) f[fl] = (fl < nf) ? (half ? in[fl].y : in[fl].x) : T(0);
-                model_dvdf<T>(mdl, f, vp, nf);
-                model_potential_shifted<T, T>(mdl, f, vref, pot_t);
+                for (int fl = 0; fl < NF; ++fl) f[fl] = (fl < nf) ? (half ? in[fl].y : in[fl].x) : T(0);
+                model_dvdf<T, T, USER>(mdl, f, vp, nf);
+                model_potential_shifted<T, T, USER>(mdl, f, vref, pot_t);
 #pragma unroll
-                for (int fl = 0; fl < 2; ++fl)
+                for (int fl = 0; fl < NF; ++fl)
                     if (fl < nf) { if (half) out[fl].y = vp[fl]; else out[fl].x = vp[fl]; }
             }
 #pragma unroll
-            for (int o = 0; o < 2; ++o)
+            for (int o = 0; o < NF; ++o)
                 if (o < nf) slots[o * slot_elems + e] = out[o];
         }
         if ((++nfold & 15) == 0) {
 #pragma unroll
-            for (int i = 0; i < kMaxTerms; ++i) {
+            for (int i = 0; i < NT; ++i) {
                 pot_d[i] += (double)pot_t[i];
                 pot_t[i] = T(0);
             }
@@ -601,8 +638,15 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
     cp_async_wait_all();
 #pragma unroll
     const double nsite = (double)nfold * (2 * ((TL * M - 1 - (int)threadIdx.x) / (int)blockDim.x + 1));
-    for (int i = 0; i < kMaxTerms; ++i) pot_d[i] += (double)pot_t[i] + nsite * (double)vref[i];
-    block_reduce_store_t<double, kMaxTerms>(pot_d, partV, gridDim.x, blockIdx.x);
+    for (int i = 0; i < NT; ++i) pot_d[i] += (double)pot_t[i] + nsite * (double)vref[i];
+    block_reduce_store_t<double, NT>(pot_d, partV, vb.gx(), vb.x());
+}
+
+template <typename T, int L, bool USER = false>
+__global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restrict__ TA, cplx<T> *__restrict__ QV,
+                                                double *__restrict__ partV, const DevBG *__restrict__ bg,
+                                                const cplx<T> *__restrict__ tw, T *__restrict__ tape_fx = nullptr) {
+    kr_zpass_body<T, L, USER, HwBlock>(vblock_hw(), g, TA, QV, partV, bg, tw, tape_fx);
 }
 
 // GW form of the Z pass on full-length line transforms. The eight real lines of a z line
@@ -619,27 +663,24 @@ __global__ void __launch_bounds__(256, 2) kr_zpass(Geo g, const cplx<T> *__restr
 // next tile are copied into a staging area by cp.async while the current one is
 // transformed. Otherwise one tile per block, inputs read straight from global memory.
 // Shared memory: four slots of TL lines x LS complex, then (STAGED) the staging area.
-template <typename T, int L, bool STAGED>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g, const cplx<T> *__restrict__ TA,
-                                                     const cplx<T> *__restrict__ TB, const cplx<T> *__restrict__ TC,
-                                                     cplx<T> *__restrict__ QV, cplx<T> *__restrict__ QS,
-                                                     double *__restrict__ partV, const DevBG *bg,
-                                                     const cplx<T> *__restrict__ tw, T *__restrict__ tape_fx) {
+template <typename T, int L, bool STAGED, bool USER, class VB>
+__device__ __forceinline__ void kr_zpass_gw_body(const VB &vb, Geo g, const cplx<T> *__restrict__ TA, const cplx<T> *__restrict__ TB, const cplx<T> *__restrict__ TC, cplx<T> *__restrict__ QV, cplx<T> *__restrict__ QS, double *__restrict__ partV, const DevBG *bg, const cplx<T> *__restrict__ tw, T *__restrict__ tape_fx) {
     using C = cplx<T>;
     using RP = RegPlan<L>;
     constexpr int P = RP::P, LS = ZIdx<L>::LS, HL = L / 2;
+    constexpr int NF = USER ? kMaxFields : 2, NT = USER ? kMaxTerms : 2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ uint64_t zbar;   // completion of a tile's bulk copies
     C *slots = reinterpret_cast<C *>(smem_raw);
     {
-        const long long rf = (long long)blockIdx.z * g.fstride, rg = (long long)blockIdx.z * g.gstride;
+        const long long rf = (long long)vb.z() * g.fstride, rg = (long long)vb.z() * g.gstride;
         TA += rf;
         TB += rf;
         TC += rf;
         QV += rf;
         QS += rg;
-        partV += (size_t)blockIdx.z * g.pv_stride;
-        bg += blockIdx.z;
+        partV += (size_t)vb.z() * g.pv_stride;
+        bg += vb.z();
     }
     // a failed stage (an earlier wait ran out, or a non-finite background) leaves the rest
     // of the step call without work: no further waits
@@ -647,6 +688,10 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
     const int TL = 1 << g.tlz_shift, H = g.H, N = g.N;
     const int nf = g.nf;
     const int pin = 2 * nf;                         // input pairs of a line
+    // output pairs (V' of each field, then the six S_ab, two by two) and work slots: four
+    // for up to two fields
+    const int pout = USER ? (nf + 7) / 2 : 4;
+    const int nslot = USER ? (pin > pout ? pin : pout) : 4;
     const int j = threadIdx.x % P;
     const int t = (threadIdx.x / P) & (TL - 1);
     const int grp = threadIdx.x / (P * TL);         // this thread's input pair in phase 1
@@ -655,7 +700,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
     // lines of one array in a tile are contiguous in global memory; when that run is a
     // multiple of 16 bytes (TL even in FP32) it is one bulk copy by the tensor memory
     // accelerator (line stride hs = H), otherwise warps copy it by cp.async (hs = H + 1).
-    C *stage = slots + 4 * slot_elems;
+    C *stage = slots + nslot * slot_elems;
     const bool bulk = STAGED && ((size_t)TL * H * sizeof(C)) % 16 == 0;
     const int hs = bulk ? H : H + 1;
     const T inv_n3 = (T)bg->inv_n3;
@@ -684,7 +729,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
                 // + the test hook's planted bytes (0 in normal runs)
                 mbar_arrive_expect_tx(&zbar, (unsigned)(nf * 3) * run + (unsigned)bg->wait_plant);
                 for (int a = 0; a < nf * 3; ++a) {
-                    const int fl = a >= 3 ? 1 : 0, w = a - 3 * fl;
+                    const int fl = USER ? a / 3 : (a >= 3 ? 1 : 0), w = a - 3 * fl;
                     const C *src = (w == 0 ? TA : (w == 1 ? TB : TC)) + (long long)fl * g.modes +
                                    (long long)tl * TL * H;
                     bulk_copy_g2s(stage + (size_t)a * TL * H, src, run, &zbar);
@@ -699,7 +744,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
                 const int a = li >> g.tlz_shift, tt = li & (TL - 1);
                 const long long ln = (long long)tl * TL + tt;
                 if (ln >= g.lines_z) continue;
-                const int fl = a >= 3 ? 1 : 0, w = a - 3 * fl;
+                const int fl = USER ? a / 3 : (a >= 3 ? 1 : 0), w = a - 3 * fl;
                 const C *src = (w == 0 ? TA : (w == 1 ? TB : TC)) + (long long)fl * g.modes + ln * H;
                 C *dst = stage + (size_t)li * hs;
                 for (int m = lane; m < H; m += 32) cp_async_elem(dst + m, src + m);
@@ -713,18 +758,18 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
     // <V> partial sums: up to 16 tiles' sites in the field precision, then folded into
     // FP64 (a persistent block walks thousands of tiles at N = 1024; a fold per tile
     // would put a conversion and an add per thread and tile on the narrow FP64 pipe)
-    T pot_t[kMaxTerms] = {T(0), T(0)};
-    double pot_d[kMaxTerms] = {0.0, 0.0};
+    T pot_t[NT] = {};
+    double pot_d[NT] = {};
     int nfold = 0;
     // the sums run over V(site) - vref (model_potential_shifted), vref the potential terms of
     // the homogeneous fields (the FP64 shadow of the zero modes / N^3), a value of the state
     // alone; vref is added back once per site summed (every tile gives a thread the same
     // number of sites: the line count is a multiple of the tile's)
-    T vref[kMaxTerms];
-    homogeneous_potential<T>(mdl, bg, vref);
-    if (STAGED) prefetch(blockIdx.x);
+    T vref[NT];
+    homogeneous_potential<T, T, USER>(mdl, bg, vref);
+    if (STAGED) prefetch(vb.x());
     unsigned phase = 0;   // parity of the bulk-copy phase the next tile completes
-    for (int tile = blockIdx.x; tile < ntiles; tile = STAGED ? tile + gridDim.x : ntiles) {
+    for (int tile = vb.x(); tile < ntiles; tile = STAGED ? tile + vb.gx() : ntiles) {
         const int line = tile * TL + t;
         const bool valid = line < g.lines_z;
         C v[16];
@@ -780,7 +825,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
             }
             if (STAGED) {
                 __syncthreads();   // every staging read of this tile is done
-                prefetch(tile + gridDim.x);
+                prefetch(tile + vb.gx());
             }
             fft_reg<C, L, +1, true>(v, slots, ix, j, tw, N / L);
             __syncthreads();
@@ -796,9 +841,9 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
             const long long ln = (long long)tile * TL + tt;
             if (ln >= g.lines_z) continue;
             const int e = tt * LS + z + (z >> 4);
-            T f[2], d[2][3];
+            T f[NF], d[NF][3];
 #pragma unroll
-            for (int fl = 0; fl < 2; ++fl) {
+            for (int fl = 0; fl < NF; ++fl) {
                 if (fl < nf) {
                     const C p0 = slots[(2 * fl) * slot_elems + e], p1 = slots[(2 * fl + 1) * slot_elems + e];
                     f[fl] = p0.x;
@@ -812,35 +857,56 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
             }
             if (tape_fx) {   // adjoint tape: the real fields
 #pragma unroll
-                for (int fl = 0; fl < 2; ++fl)
+                for (int fl = 0; fl < NF; ++fl)
                     if (fl < nf) tape_fx[fl * g.sites + ln * N + z] = f[fl];
             }
-            T vp[2] = {T(0), T(0)};
-            model_dvdf<T>(mdl, f, vp, nf);
-            model_potential_shifted<T, T>(mdl, f, vref, pot_t);
-            T o[8];
+            T vp[NF] = {};
+            model_dvdf<T, T, USER>(mdl, f, vp, nf);
+            model_potential_shifted<T, T, USER>(mdl, f, vref, pot_t);
             const int si[6] = {0, 0, 0, 1, 1, 2}, sj[6] = {0, 1, 2, 1, 2, 2};
-            o[0] = vp[0];
-            o[1] = vp[1];
+            if constexpr (!USER) {
+                T o[8];
+                o[0] = vp[0];
+                o[1] = vp[1];
 #pragma unroll
-            for (int c = 0; c < 6; ++c) {
-                T sum = T(0);
+                for (int c = 0; c < 6; ++c) {
+                    T sum = T(0);
 #pragma unroll
-                for (int fl = 0; fl < 2; ++fl)
-                    if (fl < nf) sum += T(2) * d[fl][si[c]] * d[fl][sj[c]];
-                o[2 + c] = sum;
+                    for (int fl = 0; fl < 2; ++fl)
+                        if (fl < nf) sum += T(2) * d[fl][si[c]] * d[fl][sj[c]];
+                    o[2 + c] = sum;
+                }
+                if (nf == 1) {   // V', S_00, ..., S_22, 0
+#pragma unroll
+                    for (int c = 1; c < 7; ++c) o[c] = o[c + 1];
+                    o[7] = T(0);
+                }
+#pragma unroll
+                for (int p = 0; p < 4; ++p) slots[p * slot_elems + e] = mk<T>(o[2 * p], o[2 * p + 1]);
+            } else {
+                // the products in order V'_0 .. V'_{nf-1}, S_00, ..., S_22, padded with 0
+                constexpr int NPO = (kMaxFields + 7) / 2;
+                T o[2 * NPO];
+#pragma unroll
+                for (int q = 0; q < 2 * NPO; ++q) o[q] = q < nf ? vp[q < NF ? q : 0] : T(0);
+#pragma unroll
+                for (int c = 0; c < 6; ++c) {
+                    T sum = T(0);
+#pragma unroll
+                    for (int fl = 0; fl < NF; ++fl)
+                        if (fl < nf) sum += T(2) * d[fl][si[c]] * d[fl][sj[c]];
+#pragma unroll
+                    for (int q = 0; q < 2 * NPO; ++q)
+                        if (q == nf + c) o[q] = sum;
+                }
+#pragma unroll
+                for (int p = 0; p < NPO; ++p)
+                    if (p < pout) slots[p * slot_elems + e] = mk<T>(o[2 * p], o[2 * p + 1]);
             }
-            if (nf == 1) {   // V', S_00, ..., S_22, 0
-#pragma unroll
-                for (int c = 1; c < 7; ++c) o[c] = o[c + 1];
-                o[7] = T(0);
-            }
-#pragma unroll
-            for (int p = 0; p < 4; ++p) slots[p * slot_elems + e] = mk<T>(o[2 * p], o[2 * p + 1]);
         }
         if ((++nfold & 15) == 0) {
 #pragma unroll
-            for (int i = 0; i < kMaxTerms; ++i) {
+            for (int i = 0; i < NT; ++i) {
                 pot_d[i] += (double)pot_t[i];
                 pot_t[i] = T(0);
             }
@@ -849,10 +915,10 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
 
         // 3. two real r2c per N-point forward transform of output pair o
         const int nreal = nf + 6;
-        const int rounds = (4 + pin - 1) / pin;
+        const int rounds = (pout + pin - 1) / pin;
         for (int it = 0; it < rounds; ++it) {
             const int o = grp + it * pin;
-            const bool act = o < 4;
+            const bool act = o < pout;
             const ZIdx<L> ix{(int)((act ? o : 0) * slot_elems + t * LS)};
 #pragma unroll
             for (int r = 0; r < 16; ++r) v[r] = act ? slots[ix(j + r * P)] : mk<T>(0, 0);
@@ -913,8 +979,17 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) kr_zpass_gw(Geo g
     if (STAGED) cp_async_wait_all();
 #pragma unroll
     const double nsite = (double)nfold * ((TL * L - 1 - (int)threadIdx.x) / (int)blockDim.x + 1);
-    for (int i = 0; i < kMaxTerms; ++i) pot_d[i] += (double)pot_t[i] + nsite * (double)vref[i];
-    block_reduce_store_t<double, kMaxTerms>(pot_d, partV, gridDim.x, blockIdx.x);
+    for (int i = 0; i < NT; ++i) pot_d[i] += (double)pot_t[i] + nsite * (double)vref[i];
+    block_reduce_store_t<double, NT>(pot_d, partV, vb.gx(), vb.x());
+}
+
+template <typename T, int L, bool STAGED, bool USER = false>
+__global__ void __launch_bounds__(256, (sizeof(T) == 4 && !USER) ? 3 : 2) kr_zpass_gw(Geo g, const cplx<T> *__restrict__ TA,
+                                                     const cplx<T> *__restrict__ TB, const cplx<T> *__restrict__ TC,
+                                                     cplx<T> *__restrict__ QV, cplx<T> *__restrict__ QS,
+                                                     double *__restrict__ partV, const DevBG *bg,
+                                                     const cplx<T> *__restrict__ tw, T *__restrict__ tape_fx) {
+    kr_zpass_gw_body<T, L, STAGED, USER, HwBlock>(vblock_hw(), g, TA, TB, TC, QV, QS, partV, bg, tw, tape_fx);
 }
 
 // ------------------------------------------------------------------ real-space view (c2r along z)

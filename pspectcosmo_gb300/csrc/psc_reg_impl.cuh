@@ -43,6 +43,11 @@ struct RegLaunch {
         SETA((kr_fft_x_final<T, N, true>), (int)cfg.smem_xf);
         SETA((kr_zpass<T, M>), sz);
         SETA((kr_zpass_gw<T, N, sizeof(T) == 4>), sz);
+        if (model_is_user(cfg.g.model)) {   // the Z passes of the user models (psc_reg_user_*.cu)
+            if constexpr (sizeof(T) == 4) e = reg_configure_user_f32(cfg);
+            else e = reg_configure_user_f64(cfg);
+            if (e != cudaSuccess) return e;
+        }
         SETA((kr_z_c2r_real<T, M>), (int)((256 / (M / 16)) * ZIdx<M>::LS * sizeof(C)));
         {
             int tl = 1, sh = 0;
@@ -59,6 +64,42 @@ struct RegLaunch {
         }
 #undef SETA
         return cudaSuccess;
+    }
+
+    // The fused Z pass of R realizations: kr_zpass_gw on the real-space path with GWs,
+    // kr_zpass otherwise. USER = true: the instantiations of the user models (up to
+    // kMaxFields fields), compiled in psc_reg_user_*.cu only.
+    template <bool USER>
+    static cudaError_t zpass(const LaunchCfg &cfg, const Buffers &b, cudaStream_t st, int R) {
+        const Geo &g = cfg.g;
+        const C *tw = reinterpret_cast<const C *>(b.tw);
+        C *TA = (C *)b.TA, *TB = (C *)b.TB, *TC = (C *)b.TC, *QV = (C *)b.QV, *QS = (C *)b.QS;
+        if (g.gwev)
+            kr_zpass_gw<T, N, sizeof(T) == 4, USER><<<dim3(cfg.nbz, 1, R), cfg.thr_z, cfg.smem_z, st>>>(
+                g, TA, TB, TC, QV, QS, b.partV, b.bg, tw, (T *)b.tape_fx);
+        else
+            kr_zpass<T, M, USER><<<dim3(cfg.nbz, 1, R), cfg.thr_z, cfg.smem_z, st>>>(g, TA, QV, b.partV, b.bg, tw,
+                                                                                  (T *)b.tape_fx);
+        return cudaGetLastError();
+    }
+    template <bool USER>
+    static cudaError_t configure_z(const LaunchCfg &cfg) {
+        const void *kz[2] = {(const void *)kr_zpass<T, M, USER>, (const void *)kr_zpass_gw<T, N, sizeof(T) == 4, USER>};
+        for (const void *k : kz) {
+            cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem_z);
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    }
+    static void zpass_any(const LaunchCfg &cfg, const Buffers &b, cudaStream_t st, int R) {
+        if (model_is_user(cfg.g.model)) {
+            if constexpr (sizeof(T) == 4) reg_zpass_user_f32(cfg, b, st, R);
+            else reg_zpass_user_f64(cfg, b, st, R);
+        } else {
+            zpass<false>(cfg, b, st, R);
+        }
     }
 
     static cudaError_t stage(const LaunchCfg &cfg, const Buffers &b, int drift, cudaStream_t st, cudaEvent_t *ev,
@@ -80,16 +121,14 @@ struct RegLaunch {
             mark(1);
             kr_ifft_y<T, N, true><<<gx, txy, 3 * cfg.smem_xy, st>>>(g, TA, TB, TC, b.bg, tw);
             mark(2);
-            kr_zpass_gw<T, N, sizeof(T) == 4><<<dim3(cfg.nbz, 1, R), tz, cfg.smem_z, st>>>(
-                g, TA, TB, TC, QV, QS, b.partV, b.bg, tw, (T *)b.tape_fx);
+            zpass_any(cfg, b, st, R);
         } else {
             if (drift) kr_ifft_x<T, N, false, true><<<gx, txy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
             else kr_ifft_x<T, N, false, false><<<gx, txy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
             mark(1);
             kr_ifft_y<T, N, false><<<gx, txy, cfg.smem_xy, st>>>(g, TA, TB, TC, b.bg, tw);
             mark(2);
-            kr_zpass<T, M><<<dim3(cfg.nbz, 1, R), tz, cfg.smem_z, st>>>(g, TA, QV, b.partV, b.bg, tw,
-                                                                      (T *)b.tape_fx);
+            zpass_any(cfg, b, st, R);
         }
         mark(3);
         ArrList8 al{};
@@ -134,8 +173,7 @@ struct RegLaunch {
         const dim3 gx(cfg.nbx, g.nf);
         kr_ifft_x<T, N, false, false><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, fk, nullptr, TA, nullptr, b.bg, tw);
         kr_ifft_y<T, N, false><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, TA, nullptr, nullptr, b.bg, tw);
-        kr_zpass<T, M><<<dim3(cfg.nbz, 1, 1), cfg.thr_z, cfg.smem_z, st>>>(g, TA, QV, b.partV, b.bg, tw,
-                                                                         (T *)nullptr);
+        zpass_any(cfg, b, st, 1);
         ArrList8 al{};
         for (int f = 0; f < g.nf; ++f) {
             al.rs[f] = g.fstride;
@@ -250,6 +288,17 @@ struct RegDispatch {
 };
 
 }  // namespace psc
+
+// The user-model Z passes of one precision (psc_reg_user_f32.cu, psc_reg_user_f64.cu).
+#define PSC_DEFINE_REG_USER_ENTRY(T, SUFFIX)                                                                     \
+    namespace psc {                                                                                              \
+    cudaError_t reg_configure_user_##SUFFIX(const LaunchCfg &cfg) {                                              \
+        return RegDispatch<T>::on(cfg.g.N, [&](auto L) { return decltype(L)::template configure_z<true>(cfg); }); \
+    }                                                                                                            \
+    cudaError_t reg_zpass_user_##SUFFIX(const LaunchCfg &cfg, const Buffers &b, cudaStream_t st, int R) {        \
+        return RegDispatch<T>::on(cfg.g.N, [&](auto L) { return decltype(L)::template zpass<true>(cfg, b, st, R); }); \
+    }                                                                                                            \
+    }
 
 #define PSC_DEFINE_REG_ENTRY(T, SUFFIX)                                                                          \
     namespace psc {                                                                                              \

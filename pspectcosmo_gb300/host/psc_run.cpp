@@ -18,7 +18,8 @@
 // Arguments are key=value pairs: preset=reference|preheating (the shipped parameters.h /
 // model.h, or two-field preheating), any psc_params field by its parameters.h name
 // (N, nflds, vv, spectral, with_gw, precision, model, seed, kIR, gsq, m_in_MPl, initfield0,
-// initderivs0, ...), and tf, tOutputFreq, tOutputInfreq, nsteps, dt, out, state.
+// initderivs0, ... initfield3, initderivs3), model_name (a model.h compiled into the library,
+// by file stem), and tf, tOutputFreq, tOutputInfreq, nsteps, dt, out, state.
 //
 // Build (one line): g++ -O2 -std=c++17 -I include pspectcosmo_gb300/host/psc_run.cpp
 //   -L pspectcosmo_gb300 -lpsc -Wl,-rpath,<dir of libpsc.so> -o psc_run
@@ -80,13 +81,16 @@ bool set_param(Run &r, const std::string &k, const std::string &v) {
     const DblField dbls[] = {{"kIR", &p.kIR},         {"a0", &p.a0},       {"MPl", &p.MPl},
                              {"m_in_MPl", &p.m_in_MPl}, {"fStar", &p.fStar}, {"epsilon", &p.epsilon},
                              {"gsq", &p.gsq},         {"kcutoff", &p.kcutoff}, {"initfield0", &p.initfield[0]},
-                             {"initfield1", &p.initfield[1]}, {"initderivs0", &p.initderivs[0]},
-                             {"initderivs1", &p.initderivs[1]}, {"tf", &r.tf}, {"tOutputFreq", &r.tOutputFreq},
+                             {"initfield1", &p.initfield[1]}, {"initfield2", &p.initfield[2]},
+                             {"initfield3", &p.initfield[3]}, {"initderivs0", &p.initderivs[0]},
+                             {"initderivs1", &p.initderivs[1]}, {"initderivs2", &p.initderivs[2]},
+                             {"initderivs3", &p.initderivs[3]}, {"tf", &r.tf}, {"tOutputFreq", &r.tOutputFreq},
                              {"tOutputInfreq", &r.tOutputInfreq}, {"dt", &r.dt}};
     for (const IntField &f : ints)
         if (k == f.name) return *f.dst = i, true;
     for (const DblField &f : dbls)
         if (k == f.name) return *f.dst = d, true;
+    if (k == "model_name") return psc_model_find(v.c_str(), &p.model) == PSC_OK;   // a compiled model.h by file stem
     if (k == "out") return r.out = v, true;
     if (k == "state") return r.state = v, true;
     return false;
@@ -148,11 +152,14 @@ class Writer {
         check(psc_means(h, m.data()), "psc_means");
         const double n3 = std::pow((double)p_.N, 3), fs = p_.fStar > 0 ? p_.fStar : p_.MPl;
         const double omega = p_.m_in_MPl * fs, L = 2 * kPi / p_.kIR;
-        // <effective_mass(f(x))> (output.cpp:571-580): the models' masses are linear in f^2
-        double m2[2] = {1.0, 0.0};
+        // <effective_mass(f(x))> (output.cpp:571-580): the built-in models' masses are linear in
+        // f^2; a model.h compiled in is evaluated at every site by the library
+        double m2[PSC_MAX_FIELDS] = {1.0, 0.0, 0.0, 0.0};
         if (p_.model == PSC_MODEL_PHI2CHI2) {
             m2[0] = 1.0 + p_.gsq * m[6 + 2];
             m2[1] = p_.gsq * m[2];
+        } else if (p_.model != PSC_MODEL_PHI2) {
+            check(psc_mass_sq_av(h, m2), "psc_mass_sq_av");
         }
         const double aop = std::pow(b.a, al - 3);
         for (int f = 0; f < nf; ++f) {

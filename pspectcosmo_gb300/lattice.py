@@ -124,6 +124,19 @@ def load_library(path: str | None = None):
                              ctypes.POINTER(ctypes.c_longlong)]
     L.psc_selftest_bulk_wait.argtypes = [ctypes.c_double, ctypes.POINTER(ctypes.c_int)]
     L.psc_test_wait_hook.argtypes = [P, ctypes.c_double, ctypes.c_int]
+    I3 = ctypes.POINTER(ctypes.c_int)
+    L.psc_autotune.argtypes = [P, ctypes.c_int, I3, I3]
+    L.psc_get_shapes.argtypes = [P, I3]
+    L.psc_set_shapes.argtypes = [P, I3]
+    L.psc_batch_autotune.argtypes = [P, ctypes.c_int]
+    L.psc_batch_launch_mode.argtypes = [P, ctypes.c_int, I3]
+    L.psc_model_count.argtypes = []
+    L.psc_model_name.argtypes = [ctypes.c_int]
+    L.psc_model_name.restype = ctypes.c_char_p
+    L.psc_model_find.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
+    L.psc_model_nterms.argtypes = [ctypes.c_int]
+    L.psc_model_eval.argtypes = [PP, ctypes.c_int, ctypes.c_longlong, D, D, D, D]
+    L.psc_mass_sq_av.argtypes = [P, D]
     L.psc_strerror.argtypes = [ctypes.c_int]
     L.psc_strerror.restype = ctypes.c_char_p
     L.psc_last_error.argtypes = []
@@ -139,7 +152,9 @@ def load_library(path: str | None = None):
                  "psc_set_state_padded", "psc_checkpoint_write", "psc_checkpoint_read",
                  "psc_h5_dataset_shape", "psc_h5_read_f64", "psc_analytic_begin", "psc_analytic_step",
                  "psc_analytic_background", "psc_analytic_modes", "psc_analytic_to_lattice",
-                 "psc_histograms_2d", "psc_slices", "psc_selftest_bulk_wait", "psc_test_wait_hook"):
+                 "psc_histograms_2d", "psc_slices", "psc_selftest_bulk_wait", "psc_test_wait_hook",
+                 "psc_model_count", "psc_model_find", "psc_model_nterms", "psc_model_eval", "psc_mass_sq_av",
+                 "psc_autotune", "psc_get_shapes", "psc_set_shapes", "psc_batch_autotune", "psc_batch_launch_mode"):
         getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L
@@ -183,6 +198,36 @@ def h5_read(path: str, name: str) -> np.ndarray:
     out = np.empty(shape, dtype=np.float64)
     _check(L.psc_h5_read_f64(os.fsencode(path), name.encode(), _dp(out), out.size), "psc_h5_read_f64")
     return out
+
+
+def model_id(name: str) -> int:
+    """The model id of a model.h compiled into the library (its file stem) or of a built-in
+    model ("builtin:phi2", "builtin:phi2chi2")."""
+    L = load_library()
+    mid = ctypes.c_int()
+    _check(L.psc_model_find(name.encode(), ctypes.byref(mid)), "psc_model_find")
+    return mid.value
+
+
+def model_names() -> dict:
+    """{id: name} of every model of this build."""
+    L = load_library()
+    ids = [0, 1] + [16 + i for i in range(L.psc_model_count())]
+    return {i: L.psc_model_name(i).decode() for i in ids}
+
+
+def model_eval(params: Params, fields, on_device: bool = True) -> dict:
+    """dvdf, the potential terms and effective_mass of params' model at the field points
+    fields[n][nflds] (psc_model_eval): in the lattice's arithmetic, on the GPU or the host."""
+    L = load_library()
+    x = np.ascontiguousarray(fields, np.float64).reshape(-1, params.nflds)
+    n = x.shape[0]
+    nt = L.psc_model_nterms(params.model)
+    d = np.zeros((n, params.nflds))
+    t = np.zeros((n, nt))
+    m = np.zeros((n, params.nflds))
+    _check(L.psc_model_eval(ctypes.byref(params), int(on_device), n, _dp(x), _dp(d), _dp(t), _dp(m)), "psc_model_eval")
+    return dict(dvdf=d, terms=t, mass_sq=m)
 
 
 def generate_ic(params: Params):
@@ -296,6 +341,27 @@ class Lattice:
         _check(self._L.psc_last_step_ms(self._h, ctypes.byref(v)), "psc_last_step_ms")
         return v.value
 
+    # -- FFT tile / grid shapes -----------------------------------------------
+    def autotune(self, reps: int = 3) -> dict:
+        """Time the candidate tile and grid shapes of the passes on the current state and keep
+        the fastest (psc_autotune). Returns shape = (log2 X/Y lines per tile, log2 Z lines per
+        tile, Z blocks per SM) and from_cache."""
+        sh = (ctypes.c_int * 3)()
+        fc = ctypes.c_int()
+        _check(self._L.psc_autotune(self._h, int(reps), sh, ctypes.byref(fc)), "psc_autotune")
+        return dict(shape=tuple(sh), from_cache=bool(fc.value))
+
+    @property
+    def shapes(self) -> tuple:
+        sh = (ctypes.c_int * 3)()
+        _check(self._L.psc_get_shapes(self._h, sh), "psc_get_shapes")
+        return tuple(sh)
+
+    @shapes.setter
+    def shapes(self, value):
+        sh = (ctypes.c_int * 3)(*[int(x) for x in value])
+        _check(self._L.psc_set_shapes(self._h, sh), "psc_set_shapes")
+
     # -- adjoint --------------------------------------------------------------
     def adjoint_chi2(self, dt: float, nsteps: int, every: int = 0, fields: bool = True) -> dict:
         """O = <chi^2> after nsteps and its gradient with respect to the current state.
@@ -401,6 +467,13 @@ class Lattice:
     def means(self) -> np.ndarray:
         out = np.zeros((self.p.nflds, 6))
         _check(self._L.psc_means(self._h, _dp(out)), "psc_means")
+        return out
+
+    def mass_sq_av(self) -> np.ndarray:
+        """<effective_mass(f(x))> over the lattice ([nflds]), the mass_sq_av of spectra()
+        (output.cpp:566-580)."""
+        out = np.zeros(self.p.nflds)
+        _check(self._L.psc_mass_sq_av(self._h, _dp(out)), "psc_mass_sq_av")
         return out
 
     def histograms(self, nbins: int = 256, hmin: float = 0.0, hmax: float = 0.0) -> dict:
@@ -542,6 +615,19 @@ class Ensemble:
 
     def evolve(self, dt: float, nsteps: int = 1):
         _check(self._L.psc_batch_step(self._h, float(dt), int(nsteps)), "psc_batch_step")
+
+    def autotune(self, reps: int = 3):
+        """psc_autotune for every same-configuration group (psc_batch_autotune)."""
+        _check(self._L.psc_batch_autotune(self._h, int(reps)), "psc_batch_autotune")
+
+    def launch_mode(self, per_group: bool | None = None) -> bool:
+        """True when the batch advances with one launch per pass for all its groups
+        (psc_batch_launch_mode); per_group=True asks for the per-group launches, False for the
+        default, None leaves the choice."""
+        v = ctypes.c_int()
+        _check(self._L.psc_batch_launch_mode(self._h, -1 if per_group is None else int(per_group), ctypes.byref(v)),
+               "psc_batch_launch_mode")
+        return bool(v.value)
 
     def last_step_ms(self) -> float:
         v = ctypes.c_float()

@@ -18,25 +18,35 @@ import os
 
 import numpy as np
 
-from .params import MODEL_PHI2, Params
+from .params import MODEL_PHI2, MODEL_PHI2CHI2, Params
 
 
 def mass_sq_av(p: Params, means: np.ndarray) -> np.ndarray:
-    """<effective_mass(f(x))> over the lattice (output.cpp:571-580); the models'
-    effective masses are linear in the squared fields, so <f^2> suffices."""
+    """<effective_mass(f(x))> over the lattice (output.cpp:571-580) for the built-in models:
+    their effective masses are linear in the squared fields, so <f^2> suffices. A user model
+    (model.h compiled in) takes it from Lattice.mass_sq_av(), evaluated at every site."""
     if p.model == MODEL_PHI2:
         return np.array([1.0])
     phi2, chi2 = means[0, 2], means[1, 2]
     return np.array([1.0 + p.gsq * chi2, p.gsq * phi2])
 
 
-def spectra_rows(p: Params, bg: dict, raw: dict, total: float, means: np.ndarray | None = None) -> dict:
+def spectra_rows(p: Params, bg: dict, raw: dict, total: float, means: np.ndarray | None = None,
+                 mass_sq: np.ndarray | None = None) -> dict:
+    """The rows of spectra_scalar_<fld> and spectra_gws (output.cpp:690-705, 1040-1062); the
+    occupation numbers use mass_sq (the lattice mean of effective_mass) when given, else the
+    built-in models' mean from `means`."""
     a, ad, al = bg["a"], bg["ad"], p.alpha
     n3 = float(p.sites)
     nb = p.maxnumbins
     a_of_pi = a ** (al - 3)
     out = {}
-    m2 = mass_sq_av(p, means) if means is not None else (np.array([1.0]) if p.model == MODEL_PHI2 else None)
+    if mass_sq is not None:
+        m2 = np.asarray(mass_sq)
+    elif p.model in (MODEL_PHI2, MODEL_PHI2CHI2):
+        m2 = mass_sq_av(p, means) if means is not None else (np.array([1.0]) if p.model == MODEL_PHI2 else None)
+    else:
+        m2 = None
     for f in range(p.nflds):
         rows = []
         for i in range(1, nb):
@@ -320,7 +330,8 @@ class TextWriter:
         p = self.p
         bg = lat.background()
         en = lat.energies()
-        rows = spectra_rows(p, bg, lat.spectra_raw(), en["total"], lat.means())
+        user = p.model not in (MODEL_PHI2, MODEL_PHI2CHI2)
+        rows = spectra_rows(p, bg, lat.spectra_raw(), en["total"], lat.means(), lat.mass_sq_av() if user else None)
         for f in range(p.nflds):
             with self._open(f"spectra_scalar_{f}") as fh:
                 for r in rows[f"spectra_scalar_{f}"]:

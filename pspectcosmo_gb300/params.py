@@ -14,6 +14,8 @@ import math
 
 MODEL_PHI2 = 0
 MODEL_PHI2CHI2 = 1
+MODEL_USER = 16      # model id of the first model.h compiled into the library (psc_model_find)
+MAX_FIELDS = 4
 
 
 class Params(ctypes.Structure):
@@ -37,8 +39,8 @@ class Params(ctypes.Structure):
         ("fStar", ctypes.c_double),
         ("epsilon", ctypes.c_double),
         ("gsq", ctypes.c_double),
-        ("initfield", ctypes.c_double * 2),
-        ("initderivs", ctypes.c_double * 2),
+        ("initfield", ctypes.c_double * MAX_FIELDS),
+        ("initderivs", ctypes.c_double * MAX_FIELDS),
         ("kcutoff", ctypes.c_double),
     ]
 
@@ -85,6 +87,25 @@ class Params(ctypes.Structure):
         p.initfield[1] = 0.0
         p.initderivs[0] = -0.142e-6 * p.MPl * p.MPl
         p.initderivs[1] = 0.0
+        return p.update(**overrides)
+
+    @classmethod
+    def user_model(cls, name: str, nflds: int, initfield=(), initderivs=(), **overrides) -> "Params":
+        """A run of the model.h file `name` (its file stem) compiled into the library: the
+        two-field preheating setup with that model, nflds fields and the given homogeneous
+        initial values (the rest zero)."""
+        from .lattice import model_id
+
+        p = cls.preheating()
+        p.model = model_id(name)
+        p.nflds = nflds
+        for i in range(MAX_FIELDS):
+            p.initfield[i] = initfield[i] if i < len(initfield) else 0.0
+            p.initderivs[i] = initderivs[i] if i < len(initderivs) else 0.0
+        if not initfield:
+            p.initfield[0] = 0.193 * p.MPl
+        if not initderivs:
+            p.initderivs[0] = -0.142e-6 * p.MPl * p.MPl
         return p.update(**overrides)
 
     def update(self, **overrides) -> "Params":
@@ -139,7 +160,13 @@ class Params(ctypes.Structure):
 
     @property
     def num_potential_terms(self) -> int:
-        return 1 if self.model == MODEL_PHI2 else 2
+        if self.model == MODEL_PHI2:
+            return 1
+        if self.model == MODEL_PHI2CHI2:
+            return 2
+        from .lattice import load_library
+
+        return int(load_library().psc_model_nterms(self.model))
 
     @property
     def stages(self) -> int:

@@ -40,6 +40,10 @@ RUNS = {
     "pad2_n16_vv4": ("pad2_n16_vv4", 20, 0.005, 10, True),
     "gw2_n16_vv4": ("gw2_n16_vv4", 10, 0.005, 5, True),
     "gw1_n16_vv2": ("gw1_n16_vv2", 10, 0.002, 5, True),
+    "spec3_n16_vv4": ("spec3_n16_vv4", 20, 0.005, 10, True),
+    "gw3_n16_vv4": ("gw3_n16_vv4", 10, 0.005, 5, True),
+    "spec3_n32_vv2": ("spec3_n32_vv2", 40, 0.005, 20, False),
+    "gw3_n32_vv4": ("gw3_n32_vv4", 10, 0.005, 5, False),
 }
 
 
@@ -196,6 +200,9 @@ def generate(run: str) -> str:
         else:
             out["ic_f_k"] = ic["f_k"][:, :4096]
             out["ic_pi_k"] = ic["pi_k"][:, :4096]
+            if ic["gw"]:
+                out["ic_u_k"] = out["ic_u_k"][:, :4096]
+                out["ic_pi_u_k"] = out["ic_pi_u_k"][:, :4096]
         out["meta"] = np.array(json.dumps(meta))
     path = os.path.join(HERE, f"{run}.npz")
     np.savez_compressed(path, **out)

@@ -25,6 +25,10 @@ def params_for(meta: dict, precision: int = 64) -> Params:
     c = meta["config"]
     if c.startswith(("spec1", "gw1", "pad1", "anal1")):
         p = Params.reference_default(N=meta["N"])
+    elif c.startswith(("spec3", "gw3")):
+        # the three-field model file (pspectcosmo_gb300/models/three_field.h) compiled in
+        p = Params.user_model("three_field", 3, initfield=(0.193, 0.0, 0.01), initderivs=(-0.142e-6, 0.0, 0.0),
+                              N=meta["N"])
     else:
         p = Params.preheating(N=meta["N"])
     p.vv = int(c.split("vv")[1]) if "vv" in c else 2
@@ -47,7 +51,8 @@ def output_rows(engine, p: Params) -> dict:
     raw = engine.spectra_raw() if hasattr(engine, "spectra_raw") else engine.spectra()
     en = engine.energies()
     means = engine.means()
-    rows = spectra_rows(p, bg, raw, en["total"], means)
+    mass_sq = engine.mass_sq_av() if p.model not in (0, 1) else None
+    rows = spectra_rows(p, bg, raw, en["total"], means, mass_sq)
     rows["energies"] = en
     rows["means"] = means
     rows["bg"] = bg

@@ -1,6 +1,7 @@
-"""Batched ensembles: realizations of uneven lattice sizes advanced together (one launch
-per pass per size group, one graph per step) must give exactly what each realization
-gives on its own, and match the oracle."""
+"""Batched ensembles: realizations of uneven lattice sizes advanced together (one graph per
+step; on the register engine one launch per pass for all size groups, otherwise one launch
+per pass per group) must give exactly what each realization gives on its own, and match the
+oracle."""
 import numpy as np
 import pytest
 
@@ -73,6 +74,7 @@ def test_batch_with_gw_equals_individual_lattices(precision):
           for i, N in enumerate((32, 32, 32, 64, 64))]
     ens = Ensemble(ps)
     assert ens.groups == 2
+    assert ens.launch_mode()   # one launch per pass for both groups
     ens.initialize()
     ens.evolve(0.005, 4)
     for idx, p in enumerate(ps):
@@ -84,3 +86,46 @@ def test_batch_with_gw_equals_individual_lattices(precision):
             assert np.array_equal(a[k], b[k]), (idx, k)
         assert a["a"] == b["a"] and a["ad"] == b["ad"] and a["add"] == b["add"], idx
         lat.close()
+
+
+def _mixed(precision):
+    from pspectcosmo_gb300.params import Params
+
+    rng = np.random.default_rng(7)
+    ps = []
+    for N, count in ((32, 4), (64, 3), (128, 1), (256, 1)):
+        for _ in range(count):
+            ps.append(Params.reference_default(N=N, vv=4, seed=1 + len(ps), precision=precision,
+                                               initfield=[float(rng.uniform(10, 12)), 0.0]))
+    return ps
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_one_launch_per_pass_equals_individual_lattices(precision):
+    """Four size groups (32^3 .. 256^3) in one launch per pass: every realization equals the
+    lattice advanced alone, bit for bit, and the per-group launches give the same bits."""
+    from pspectcosmo_gb300 import Ensemble, Lattice
+
+    ps = _mixed(precision)
+    ens = Ensemble(ps)
+    assert ens.groups == 4 and ens.launch_mode()
+    ens.initialize()
+    ens.evolve(1e-4, 5)
+    states = [ens.get_state(i) for i in range(len(ps))]
+    for idx in (0, 3, 4, 7, 8):
+        lat = Lattice(ps[idx])
+        lat.initialize()
+        lat.evolve(1e-4, 5)
+        a, b = states[idx], lat.get_state()
+        assert np.array_equal(a["f_k"], b["f_k"]) and np.array_equal(a["pi_k"], b["pi_k"]), idx
+        assert a["a"] == b["a"] and a["ad"] == b["ad"] and a["add"] == b["add"], idx
+        lat.close()
+    ens.close()
+    per = Ensemble(ps)
+    assert not per.launch_mode(per_group=True)
+    per.initialize()
+    per.evolve(1e-4, 5)
+    for idx in (1, 5, 8):
+        b = per.get_state(idx)
+        assert np.array_equal(states[idx]["f_k"], b["f_k"]) and states[idx]["a"] == b["a"], idx
+    per.close()
