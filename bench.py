@@ -299,7 +299,7 @@ def run_ensemble(args):
     ens.initialize()
     if not args.no_autotune:
         ens.autotune(reps=2)
-    one_launch = ens.launch_mode(per_group=True if args.per_group else None)
+    one_launch = ens.launch_mode(per_group=False if args.one_launch else None)
     ens.evolve(dt, args.warmup)
     clocks = ClockSampler(local)
     barrier(dist)
@@ -817,8 +817,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--no-autotune", action="store_true", help="keep the planner's default FFT tile shapes")
-    ap.add_argument("--per-group", action="store_true",
-                    help="ensemble_mixed: launch each size group's passes separately (default: one launch per pass)")
+    ap.add_argument("--one-launch", action="store_true",
+                    help="ensemble_mixed: one launch per pass for all size groups (default: per-group launches)")
     ap.add_argument("--adj-check", type=int, default=0,
                     help="adjoint_128: also check the FP32 and FP64 gradients against FP64 central differences "
                          "on this many random directions")

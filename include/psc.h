@@ -363,14 +363,16 @@ int psc_batch_init_ic(psc_batch *b);                      /* initialize() for ev
 int psc_batch_step(psc_batch *b, double dt, int nsteps);  /* nsteps steps of every realization */
 int psc_batch_last_step_ms(psc_batch *b, float *ms);
 int psc_batch_autotune(psc_batch *b, int reps);         /* psc_autotune for every group */
-/* How the groups' passes are launched. By default a batch whose groups all run the register
- * engine at N <= 256 with 256-thread blocks, a built-in model, and one precision, GW setting
- * and integrator advances with ONE launch per pass for all groups: persistent kernels over
- * a work list of (group, realization, array, tile) (and one background launch per stage);
- * other batches launch every group's passes on its own stream, the streams forked and joined
- * in the step graph. per_group = 1 asks for the per-group launches, 0 for the default, -1
- * leaves the choice; *one_launch_per_pass (may be NULL) receives 1 when the batched launches
- * are in use. Both give each realization the results it has alone, bit for bit. */
+/* How the groups' passes are launched. By default every group's passes run on its own
+ * stream, the streams forked and joined inside the step graph. per_group = 0 asks for ONE
+ * launch per pass for all groups instead: persistent kernels over a work list of (group,
+ * realization, array, tile), and one background launch per stage; it applies when every
+ * group runs the register engine at N <= 256 with 256-thread blocks, a built-in model, and
+ * one precision, GW setting and integrator (at most four groups). per_group = 1 restores the
+ * default, -1 leaves the choice; *one_launch_per_pass (may be NULL) receives 1 when the
+ * batched launches are in use. Both give each realization the results it has alone, bit for
+ * bit. (On the mixed 32^3 / 64^3 / 128^3 ensemble the per-group launches are the faster:
+ * their streams fill each other's kernel tails.) */
 int psc_batch_launch_mode(psc_batch *b, int per_group, int *one_launch_per_pass);
 int psc_batch_set_state(psc_batch *b, int idx, const double *f_k, const double *pi_k, double a, double ad, double add,
                         const double *u_k, const double *pi_u_k);

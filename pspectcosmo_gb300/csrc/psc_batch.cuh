@@ -25,8 +25,8 @@ __device__ __forceinline__ void batch_item(const BatchGroup &G, unsigned w) {
         const unsigned nbx = (unsigned)G.nbx, nf = (unsigned)g.nf, rest = w / nbx;
         const VBlock vb{w - rest * nbx, rest % nf, rest / nf, nbx};
         if constexpr (PASS == 0) {
-            if (g.gwev) kr_ifft_x_body<T, L, true, DRIFT, VBlock>(vb, g, fk, pk, TA, TB, G.bg, tw);
-            else kr_ifft_x_body<T, L, false, DRIFT, VBlock>(vb, g, fk, pk, TA, TB, G.bg, tw);
+            if (g.gwev) kr_ifft_x_body<T, L, true, DRIFT, VBlock>(vb, g, fk, pk, TA, TB, G.bg, tw, nullptr);
+            else kr_ifft_x_body<T, L, false, DRIFT, VBlock>(vb, g, fk, pk, TA, TB, G.bg, tw, nullptr);
         } else {
             if (g.gwev) kr_ifft_y_body<T, L, true, VBlock>(vb, g, TA, TB, TC, G.bg, tw);
             else kr_ifft_y_body<T, L, false, VBlock>(vb, g, TA, TB, TC, G.bg, tw);
@@ -49,10 +49,10 @@ __device__ __forceinline__ void batch_item(const BatchGroup &G, unsigned w) {
         } else {
             if (g.gwev)
                 kr_fft_x_final_body<T, L, true, VBlock>(vb, g, QV, QS, fk, pk, uk, puk, G.partKG, G.bg, tw, nullptr,
-                                                        nullptr, nullptr, nullptr, nullptr, (C *)G.Fk, (C *)G.Fu);
+                                                        nullptr, nullptr, nullptr, nullptr, (C *)G.Fk, (C *)G.Fu, nullptr);
             else
                 kr_fft_x_final_body<T, L, false, VBlock>(vb, g, QV, QS, fk, pk, uk, puk, G.partKG, G.bg, tw, nullptr,
-                                                         nullptr, nullptr, nullptr, nullptr, (C *)G.Fk, nullptr);
+                                                         nullptr, nullptr, nullptr, nullptr, (C *)G.Fk, nullptr, nullptr);
         }
     }
 }

@@ -9,6 +9,7 @@
 // (evolution.cpp:1150, 1176) is applied in the Z-pass epilogue.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -332,6 +333,18 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsign
                      smem_addr(dst)),
                  "l"(src), "r"(bytes), "r"(smem_addr(bar))
                  : "memory");
+}
+// Tiled tensor copy global -> shared by the tensor memory accelerator: the box of the tensor
+// map at coordinates (c0, c1, c2, c3), innermost first, written to dst (128-byte aligned) in
+// the box's row-major order and completed on an mbarrier. map is the address of a
+// __grid_constant__ kernel parameter.
+__device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
+                                            uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+        "%5}], [%6];\n" ::"r"(smem_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_addr(bar))
+        : "memory");
 }
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
     unsigned ok;

@@ -34,6 +34,7 @@ struct psc_handle {
     size_t xfer_elems = 0;
     std::vector<void *> allocs;
     size_t partKG_cap = 0, partV_cap = 0;   // doubles held by b.partKG, b.partV (the autotuner may grow them)
+    psc::XTma xtma{};            // tensor maps of the X forward + kick operands (b.xtma points here when on)
     void *adj = nullptr;         // adjoint workspace (psc_adjoint.cu), owned by the handle
     void (*adj_free)(void *) = nullptr;
     void *ana = nullptr;         // analytic pre-lattice phase (psc_analytic.cu), owned by the handle
@@ -49,6 +50,7 @@ struct psc_handle {
 namespace psc {
 namespace hapi {
 int fail(int code, const std::string &msg);
+void encode_xtma(psc_handle *h);
 int dalloc(psc_handle *h, void **out, size_t bytes);
 int upload(psc_handle *h, void *dst, const double *src, size_t ncplx);
 int download_real(psc_handle *h, double *dst, const void *src, size_t count);

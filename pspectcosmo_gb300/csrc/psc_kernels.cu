@@ -868,7 +868,8 @@ void plan(const psc_params &p, int R, LaunchCfg *cfg, const TileChoice *tc) {
         cfg->tc.xy_shift = g.tlx_shift;
         cfg->thr_xy = tl * P;
         cfg->smem_xy = (size_t)tl * g.N * csize;
-        cfg->smem_xf = 3 * cfg->smem_xy;
+        cfg->smem_xf = 3 * cfg->smem_xy + 128;   // + the alignment of the TMA operand tiles
+        cfg->smem_xi = 3 * cfg->smem_xy + 128;
         cfg->nbx = (g.lines_x + tl - 1) / tl;
         const int Pz = g.M / 16;
         int tlz = 1;   // lines per tile: the largest power of two with nin x tlz x Pz <= 256 threads
@@ -918,6 +919,7 @@ void plan(const psc_params &p, int R, LaunchCfg *cfg, const TileChoice *tc) {
     cfg->thr_xy = 256;
     cfg->smem_xy = (size_t)2 * tl * g.N * csize;
     cfg->smem_xf = cfg->smem_xy;
+    cfg->smem_xi = cfg->smem_xy;
     cfg->nbx = (g.lines_x + tl - 1) / tl;
     // Z pass: TLz lines, two H-row buffers + nslot M-row real-line slots.
     int tlz = 32;

@@ -2,6 +2,7 @@
 // the CUDA kernels (psc_kernels.cu). No CUDA C++ device code here.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -11,6 +12,7 @@ namespace psc {
 
 struct DevBG;
 struct DevAdj;
+struct XTma;
 
 // Lattice geometry and tiling, passed by value to every pass kernel.
 struct Geo {
@@ -49,6 +51,7 @@ struct LaunchCfg {
     int thr_xy, thr_z;           // threads per block
     size_t smem_xy, smem_z;      // dynamic shared memory bytes
     size_t smem_xf;              // X forward + kick pass (exchange tile + two prefetched operand tiles)
+    size_t smem_xi;              // X inverse pass with tensor-map staging (exchange tile + f_k and pi tiles)
     int nbx;                     // blocks of the X / Y passes (per array)
     int nbz;                     // blocks of the Z pass
 };
@@ -75,6 +78,17 @@ struct Buffers {
     // [nf][modes] and a^(1+alpha)(-k^2 u + S) of the GW [6][modes]. The opening half kick of
     // the next step call uses it instead of a force evaluation (null: not kept)
     void *Fk, *Fu;
+    const XTma *xtma;            // host copy of the kick operands' tensor maps (null: cp.async staging)
+};
+
+// Tensor maps of the X forward + kick pass's operand tiles (TMA): f_k, pi_k as
+// {lines, x, field, realization} and u_k, pi_u_k as {lines, x, component, realization}, in
+// 8-byte elements, box {lines per tile, N, 1, 1}. on = 0: the pass stages its operands by
+// cp.async instead (N > 256, batched launches, or no tensor-map encoder).
+struct XTma {
+    CUtensorMap fk, pk, uk, puk;
+    int on;
+    int xi;   // the X inverse pass stages f_k and pi too (FP32: its two tiles keep two blocks per SM)
 };
 
 // Up to eight arrays of the forward passes (V' of each field, then S_ab) with the realization

@@ -48,7 +48,7 @@ __device__ __forceinline__ HwBlock vblock_hw() { return HwBlock{}; }
 
 // ------------------------------------------------------------------ X inverse (+ drift, + x-derivative)
 template <typename T, int L, bool GW, bool DRIFT, class VB>
-__device__ __forceinline__ void kr_ifft_x_body(const VB &vb, Geo g, cplx<T> *__restrict__ fk, const cplx<T> *__restrict__ pk, cplx<T> *__restrict__ TA, cplx<T> *__restrict__ TB, const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw) {
+__device__ __forceinline__ void kr_ifft_x_body(const VB &vb, Geo g, cplx<T> *__restrict__ fk, const cplx<T> *__restrict__ pk, cplx<T> *__restrict__ TA, cplx<T> *__restrict__ TB, const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw, const XTma *tma) {
     using C = cplx<T>;
     using RP = RegPlan<L>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -70,6 +70,39 @@ __device__ __forceinline__ void kr_ifft_x_body(const VB &vb, Geo g, cplx<T> *__r
     auto ix = [&](int n) { return n * TL + t; };
     const T c = DRIFT ? (T)bg->c_drift : T(0);
     const T kIR = GW ? (T)bg->kIR : T(0);
+    // With tensor maps (tma): the tile of f_k (and, drifting, of pi_half) comes into shared
+    // memory by tiled copies of the tensor memory accelerator, issued by one thread and landing
+    // on an mbarrier (128-byte aligned tiles: the launch adds 128 bytes of shared memory);
+    // the drift updates the staged f_k too, so the GW derivative pass reads it from there.
+    // Otherwise every thread loads its elements from global memory.
+    __shared__ uint64_t ibar;
+    const bool use_tma = tma != nullptr;
+    C *opF = nullptr, *opP = nullptr;
+    if (use_tma) {
+        // a failed stage: no further waits (the block decides as one)
+        if (__syncthreads_or(threadIdx.x == 0 && bg->err != 0)) return;
+        opF = reinterpret_cast<C *>((reinterpret_cast<uintptr_t>(sm + TL * L) + 127) & ~(uintptr_t)127);
+        opP = opF + TL * L;
+        if (threadIdx.x == 0) {
+            mbar_init(&ibar, 1);
+            mbar_fence_init();
+            mbar_arrive_expect_tx(&ibar, (DRIFT ? 2u : 1u) * (unsigned)(TL * L * sizeof(C)));
+            const int w8 = (int)(sizeof(C) / 8), c0 = (int)(vb.x() * TL) * w8;
+            tma_load_4d(opF, &tma->fk, c0, 0, (int)vb.y(), (int)vb.z(), &ibar);
+            if (DRIFT) tma_load_4d(opP, &tma->pk, c0, 0, (int)vb.y(), (int)vb.z(), &ibar);
+        }
+        __syncthreads();   // the mbarrier is initialised before any thread waits on it
+        // bounded wait, as the X forward + kick pass's: a timeout is reported, the copies in
+        // flight are waited for once more, and the block leaves only after they landed
+        const bool ok = mbar_wait_bounded(&ibar, 0, bg->wait_ns);
+        if (__syncthreads_or(!ok)) {
+            int *err = &const_cast<DevBG *>(bg)->err;
+            if (threadIdx.x == 0) report_err(err, PSC_ERR_TIMEOUT);
+            const bool landed = mbar_wait_bounded(&ibar, 0, bg->wait_ns);
+            if (__syncthreads_or(!landed) && threadIdx.x == 0) report_err(err, PSC_ERR_DEVICE);
+            return;
+        }
+    }
     // pass 0: (drifted) f -> TA; with GWs pass 1: i k_x f -> TB (one copy of the
     // transform code for both keeps the register allocation spill-free)
 #pragma unroll 1
@@ -79,23 +112,36 @@ __device__ __forceinline__ void kr_ifft_x_body(const VB &vb, Geo g, cplx<T> *__r
         // read-modify-write of f_k through one pointer would otherwise keep each load
         // behind the previous store (no alias proof at run-time strides)
         C v[16];
+        if (use_tma) {
 #pragma unroll
-        for (int r = 0; r < 16; ++r) v[r] = valid ? fk[base + (long long)(j + r * RP::P) * stride] : mk<T>(0, 0);
+            for (int r = 0; r < 16; ++r) v[r] = opF[ix(j + r * RP::P)];
+        } else {
+#pragma unroll
+            for (int r = 0; r < 16; ++r) v[r] = valid ? fk[base + (long long)(j + r * RP::P) * stride] : mk<T>(0, 0);
+        }
         if (pass == 0 && DRIFT) {
             C pv[16];
+            if (use_tma) {
 #pragma unroll
-            for (int r = 0; r < 16; ++r) pv[r] = valid ? pk[base + (long long)(j + r * RP::P) * stride] : mk<T>(0, 0);
+                for (int r = 0; r < 16; ++r) pv[r] = opP[ix(j + r * RP::P)];
+            } else {
+#pragma unroll
+                for (int r = 0; r < 16; ++r)
+                    pv[r] = valid ? pk[base + (long long)(j + r * RP::P) * stride] : mk<T>(0, 0);
+            }
 #pragma unroll
             for (int r = 0; r < 16; ++r) {
                 v[r].x += c * pv[r].x;
                 v[r].y += c * pv[r].y;
                 if (valid) fk[base + (long long)(j + r * RP::P) * stride] = v[r];
+                if (GW && use_tma) opF[ix(j + r * RP::P)] = v[r];   // this thread's own elements
             }
             if (line == 0 && j == 0 && bg->zero64) {
                 // the homogeneous mode (element 0 of the line x = y = kz = 0) is the background
                 // kernel's FP64 shadow, already drifted
                 v[0] = mk<T>((T)bg->z0f[vb.y()][0], (T)bg->z0f[vb.y()][1]);
                 fk[base] = v[0];
+                if (GW && use_tma) opF[ix(0)] = v[0];
             }
         }
         if (pass == 1) {
@@ -120,8 +166,10 @@ __device__ __forceinline__ void kr_ifft_x_body(const VB &vb, Geo g, cplx<T> *__r
 template <typename T, int L, bool GW, bool DRIFT>
 __global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_ifft_x(Geo g, cplx<T> *__restrict__ fk, const cplx<T> *__restrict__ pk,
                                                  cplx<T> *__restrict__ TA, cplx<T> *__restrict__ TB,
-                                                 const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw) {
-    kr_ifft_x_body<T, L, GW, DRIFT, HwBlock>(vblock_hw(), g, fk, pk, TA, TB, bg, tw);
+                                                 const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw,
+                                                 const __grid_constant__ XTma tma = XTma{}) {
+    kr_ifft_x_body<T, L, GW, DRIFT, HwBlock>(vblock_hw(), g, fk, pk, TA, TB, bg, tw,
+                                             (tma.on && tma.xi) ? &tma : nullptr);
 }
 
 // ------------------------------------------------------------------ Y passes
@@ -252,11 +300,12 @@ __global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(3)) kr_fft_y(Geo
 
 // ------------------------------------------------------------------ X forward + kick epilogue
 template <typename T, int L, bool GW, class VB>
-__device__ __forceinline__ void kr_fft_x_final_body(const VB &vb, Geo g, const cplx<T> *__restrict__ QV, const cplx<T> *__restrict__ QS, const cplx<T> *__restrict__ fk, cplx<T> *__restrict__ pk, cplx<T> *__restrict__ uk, cplx<T> *__restrict__ puk, double *__restrict__ partKG, const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw, cplx<T> *__restrict__ tape_f, cplx<T> *__restrict__ tape_p, cplx<T> *__restrict__ tape_vp, cplx<T> *__restrict__ tape_pu, cplx<T> *__restrict__ tape_fu, cplx<T> *__restrict__ fcache, cplx<T> *__restrict__ ucache) {
+__device__ __forceinline__ void kr_fft_x_final_body(const VB &vb, Geo g, const cplx<T> *__restrict__ QV, const cplx<T> *__restrict__ QS, const cplx<T> *__restrict__ fk, cplx<T> *__restrict__ pk, cplx<T> *__restrict__ uk, cplx<T> *__restrict__ puk, double *__restrict__ partKG, const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw, cplx<T> *__restrict__ tape_f, cplx<T> *__restrict__ tape_p, cplx<T> *__restrict__ tape_vp, cplx<T> *__restrict__ tape_pu, cplx<T> *__restrict__ tape_fu, cplx<T> *__restrict__ fcache, cplx<T> *__restrict__ ucache, const XTma *tma) {
     using C = cplx<T>;
     using RP = RegPlan<L>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *sm = reinterpret_cast<C *>(smem_raw);
+    __shared__ uint64_t xbar;   // completion of the operand tiles' tensor copies (TMA)
     {
         const long long rf = (long long)vb.z() * g.fstride, rg = (long long)vb.z() * g.gstride;
         QV += rf;
@@ -283,26 +332,63 @@ __device__ __forceinline__ void kr_fft_x_final_body(const VB &vb, Geo g, const c
     const long long stride = g.lines_x;
     const long long base = off + line;
     auto ix = [&](int n) { return n * TL + t; };
-    // Prefetch the kick operands (f_k, pi_half or u_k, pi_u_half) of this tile
-    // into shared memory with cp.async, overlapping their latency with the FFT.
-    C *opA = sm + TL * L, *opB = opA + TL * L;
+    // Prefetch the kick operands (f_k, pi_half or u_k, pi_u_half) of this tile into shared
+    // memory, overlapping their latency with the FFT: with tensor maps (tma), two tiled copies
+    // by the tensor memory accelerator issued by one thread, landing on an mbarrier (the tiles
+    // 128-byte aligned: the launch adds 128 bytes of shared memory for it); otherwise each
+    // thread copies its own elements with cp.async.
+    const bool use_tma = tma != nullptr;
+    C *opA = sm + TL * L;
+    if (use_tma) opA = reinterpret_cast<C *>((reinterpret_cast<uintptr_t>(opA) + 127) & ~(uintptr_t)127);
+    C *opB = opA + TL * L;
     const C *gA = field ? fk : uk, *gB = field ? pk : puk;
-    if (valid) {
-#pragma unroll
-        for (int r = 0; r < 16; ++r) {
-            const int n = RP::out(j, r / RP::RL, r % RP::RL);
-            const long long a = base + (long long)n * stride;
-            cp_async_elem(opA + ix(n), gA + a);
-            cp_async_elem(opB + ix(n), gB + a);
+    if (use_tma) {
+        // a failed stage: no further waits (one thread reads the error word, so that the block
+        // decides as one while another block may be writing it)
+        if (__syncthreads_or(threadIdx.x == 0 && bg->err != 0)) return;
+        if (threadIdx.x == 0) {
+            mbar_init(&xbar, 1);
+            mbar_fence_init();
+            mbar_arrive_expect_tx(&xbar, 2u * (unsigned)(TL * L * sizeof(C)));
+            const int w8 = (int)(sizeof(C) / 8), arr = field ? job : job - g.nf;
+            const CUtensorMap *ma = field ? &tma->fk : &tma->uk, *mb = field ? &tma->pk : &tma->puk;
+            tma_load_4d(opA, ma, (int)(vb.x() * TL) * w8, 0, arr, (int)vb.z(), &xbar);
+            tma_load_4d(opB, mb, (int)(vb.x() * TL) * w8, 0, arr, (int)vb.z(), &xbar);
         }
+        // (the transform's barriers order the mbarrier's initialisation before the waits below)
+    } else {
+        if (valid) {
+#pragma unroll
+            for (int r = 0; r < 16; ++r) {
+                const int n = RP::out(j, r / RP::RL, r % RP::RL);
+                const long long a = base + (long long)n * stride;
+                cp_async_elem(opA + ix(n), gA + a);
+                cp_async_elem(opB + ix(n), gB + a);
+            }
+        }
+        cp_async_commit();
     }
-    cp_async_commit();
     C v[16];
 #pragma unroll
     for (int r = 0; r < 16; ++r)
         v[r] = valid ? src[(long long)(j + r * RP::P) * stride + line] : mk<T>(0, 0);
     fft_reg<C, L, -1>(v, sm, ix, j, tw, N / L);
-    cp_async_wait_all();
+    if (use_tma) {
+        // every thread waits for the tiles (bounded). If they did not land in time: report the
+        // timeout, wait once more for the copies in flight (bounded) so that the block never
+        // leaves while one can still write into its shared memory, and leave; if they never
+        // land, PSC_ERR_DEVICE (the context can no longer be trusted)
+        const bool ok = mbar_wait_bounded(&xbar, 0, bg->wait_ns);
+        if (__syncthreads_or(!ok)) {
+            int *err = &const_cast<DevBG *>(bg)->err;
+            if (threadIdx.x == 0) report_err(err, PSC_ERR_TIMEOUT);
+            const bool landed = mbar_wait_bounded(&xbar, 0, bg->wait_ns);
+            if (__syncthreads_or(!landed) && threadIdx.x == 0) report_err(err, PSC_ERR_DEVICE);
+            return;
+        }
+    } else {
+        cp_async_wait_all();
+    }
 
     const T norm1 = (T)bg->norm1, norm2 = (T)bg->norm2, kIR2 = (T)bg->kIR2;
     const T c_close = (T)bg->c_close, c_open = (T)bg->c_open;
@@ -411,8 +497,9 @@ __global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_fft_x_fin
                                                       cplx<T> *__restrict__ tape_pu = nullptr,
                                                       cplx<T> *__restrict__ tape_fu = nullptr,
                                                       cplx<T> *__restrict__ fcache = nullptr,
-                                                      cplx<T> *__restrict__ ucache = nullptr) {
-    kr_fft_x_final_body<T, L, GW, HwBlock>(vblock_hw(), g, QV, QS, fk, pk, uk, puk, partKG, bg, tw, tape_f, tape_p, tape_vp, tape_pu, tape_fu, fcache, ucache);
+                                                      cplx<T> *__restrict__ ucache = nullptr,
+                                                      const __grid_constant__ XTma tma = XTma{}) {
+    kr_fft_x_final_body<T, L, GW, HwBlock>(vblock_hw(), g, QV, QS, fk, pk, uk, puk, partKG, bg, tw, tape_f, tape_p, tape_vp, tape_pu, tape_fu, fcache, ucache, tma.on ? &tma : nullptr);
 }
 
 // ------------------------------------------------------------------ fused Z pass
@@ -683,8 +770,9 @@ __device__ __forceinline__ void kr_zpass_gw_body(const VB &vb, Geo g, const cplx
         bg += vb.z();
     }
     // a failed stage (an earlier wait ran out, or a non-finite background) leaves the rest
-    // of the step call without work: no further waits
-    if (bg->err) return;
+    // of the step call without work: no further waits. One thread reads the error word, so
+    // that the block decides as one while another block may be writing it.
+    if (__syncthreads_or(threadIdx.x == 0 && bg->err != 0)) return;
     const int TL = 1 << g.tlz_shift, H = g.H, N = g.N;
     const int nf = g.nf;
     const int pin = 2 * nf;                         // input pairs of a line

@@ -32,10 +32,10 @@ struct RegLaunch {
     e = cudaFuncSetAttribute((const void *)(kern), cudaFuncAttributePreferredSharedMemoryCarveout,         \
                              cudaSharedmemCarveoutMaxShared);                                               \
     if (e != cudaSuccess) return e;
-        SETA((kr_ifft_x<T, N, false, true>), sxy);
-        SETA((kr_ifft_x<T, N, true, true>), sxy);
-        SETA((kr_ifft_x<T, N, false, false>), sxy);
-        SETA((kr_ifft_x<T, N, true, false>), sxy);
+        SETA((kr_ifft_x<T, N, false, true>), (int)cfg.smem_xi);
+        SETA((kr_ifft_x<T, N, true, true>), (int)cfg.smem_xi);
+        SETA((kr_ifft_x<T, N, false, false>), (int)cfg.smem_xi);
+        SETA((kr_ifft_x<T, N, true, false>), (int)cfg.smem_xi);
         SETA((kr_ifft_y<T, N, false>), sxy);
         SETA((kr_ifft_y<T, N, true>), 3 * sxy);   // exchange tile + TA and TB staging tiles
         SETA((kr_fft_y<T, N>), sxy);
@@ -114,17 +114,20 @@ struct RegLaunch {
         auto mark = [&](int i) {
             if (ev) cudaEventRecord(ev[i], st);
         };
+        // the X passes' operand tiles by tensor copies where the handle has tensor maps
+        const XTma xt = (b.xtma && b.xtma->on) ? *b.xtma : XTma{};
+        const size_t sxi = (xt.on && xt.xi) ? cfg.smem_xi : cfg.smem_xy;
         mark(0);
         if (g.gwev) {
-            if (drift) kr_ifft_x<T, N, true, true><<<gx, txy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
-            else kr_ifft_x<T, N, true, false><<<gx, txy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
+            if (drift) kr_ifft_x<T, N, true, true><<<gx, txy, sxi, st>>>(g, fk, pk, TA, TB, b.bg, tw, xt);
+            else kr_ifft_x<T, N, true, false><<<gx, txy, sxi, st>>>(g, fk, pk, TA, TB, b.bg, tw, xt);
             mark(1);
             kr_ifft_y<T, N, true><<<gx, txy, 3 * cfg.smem_xy, st>>>(g, TA, TB, TC, b.bg, tw);
             mark(2);
             zpass_any(cfg, b, st, R);
         } else {
-            if (drift) kr_ifft_x<T, N, false, true><<<gx, txy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
-            else kr_ifft_x<T, N, false, false><<<gx, txy, cfg.smem_xy, st>>>(g, fk, pk, TA, TB, b.bg, tw);
+            if (drift) kr_ifft_x<T, N, false, true><<<gx, txy, sxi, st>>>(g, fk, pk, TA, TB, b.bg, tw, xt);
+            else kr_ifft_x<T, N, false, false><<<gx, txy, sxi, st>>>(g, fk, pk, TA, TB, b.bg, tw, xt);
             mark(1);
             kr_ifft_y<T, N, false><<<gx, txy, cfg.smem_xy, st>>>(g, TA, TB, TC, b.bg, tw);
             mark(2);
@@ -149,11 +152,11 @@ struct RegLaunch {
             kr_fft_x_final<T, N, true><<<gf, txy, cfg.smem_xf, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw,
                                                                       (C *)b.tape_f, (C *)b.tape_p, (C *)b.tape_vp,
                                                                       (C *)b.tape_pu, (C *)b.tape_fu, (C *)b.Fk,
-                                                                      (C *)b.Fu);
+                                                                      (C *)b.Fu, xt);
         else
             kr_fft_x_final<T, N, false><<<gf, txy, cfg.smem_xf, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw,
                                                                        (C *)b.tape_f, (C *)b.tape_p, (C *)b.tape_vp,
-                                                                       nullptr, nullptr, (C *)b.Fk, nullptr);
+                                                                       nullptr, nullptr, (C *)b.Fk, nullptr, xt);
         mark(5);
         if (scalar_mode >= 0) {
             cudaError_t e = launch_scalar(cfg, b, scalar_mode, 1, st);

@@ -74,7 +74,7 @@ def test_batch_with_gw_equals_individual_lattices(precision):
           for i, N in enumerate((32, 32, 32, 64, 64))]
     ens = Ensemble(ps)
     assert ens.groups == 2
-    assert ens.launch_mode()   # one launch per pass for both groups
+    assert ens.launch_mode(per_group=False)   # one launch per pass for both groups
     ens.initialize()
     ens.evolve(0.005, 4)
     for idx, p in enumerate(ps):
@@ -108,7 +108,7 @@ def test_one_launch_per_pass_equals_individual_lattices(precision):
 
     ps = _mixed(precision)
     ens = Ensemble(ps)
-    assert ens.groups == 4 and ens.launch_mode()
+    assert ens.groups == 4 and not ens.launch_mode() and ens.launch_mode(per_group=False)
     ens.initialize()
     ens.evolve(1e-4, 5)
     states = [ens.get_state(i) for i in range(len(ps))]

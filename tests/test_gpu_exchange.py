@@ -1,8 +1,9 @@
 """State exchange through the C ABI (psc_set_state / psc_get_state) at the benchmark's size.
 
 The FP32 upload copies the caller's FP64 arrays through a 16 Mi-double device scratch and
-rounds on the device; the download copies in up to 16 chunks and widens on the host cores,
-or, into page-locked buffers, widens on the device and copies the FP64 values straight in.
+rounds on the device; the download copies in up to 16 chunks and widens on the host cores.
+Page-locked host buffers mapped into the device (cudaHostAlloc, torch's pin_memory) are read
+and written by the rounding and widening kernels directly, in one pass over the link.
 At 256^3 with GWs every array group spans several chunks of both. A round trip must give
 exactly the FP32 rounding of the input (round to nearest even, as a host cast), except the
 fields' homogeneous modes f_k(0), pi_k(0), which the device keeps in FP64 and returns
