@@ -24,7 +24,10 @@ sys.path.insert(0, ROOT)
 from pspectcosmo_gb300 import model_adapter  # noqa: E402
 
 MODELS = os.path.join(ROOT, "pspectcosmo_gb300", "models")
-REF_MODEL = os.path.join(os.environ.get("PSC_REFERENCE_DIR", "/root/reference"), "model.h")
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import build_ref  # noqa: E402  (the oracle's recipe names the reference checkout)
+
+REF_MODEL = os.path.join(build_ref.REF, "model.h")
 NPTS = 64
 
 CASES = [("phi2", os.path.join(MODELS, "phi2.h"), 1), ("phi2chi2", os.path.join(MODELS, "phi2chi2.h"), 2),
