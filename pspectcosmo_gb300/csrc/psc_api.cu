@@ -1014,8 +1014,11 @@ void encode_xtma(psc_handle *h) {
                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
     };
-    bool ok = make(&h->xtma.fk, h->b.fk, g.nf, g.fstride) && make(&h->xtma.pk, h->b.pk, g.nf, g.fstride);
-    if (ok && g.gwev) ok = make(&h->xtma.uk, h->b.uk, 6, g.gstride) && make(&h->xtma.puk, h->b.puk, 6, g.gstride);
+    bool ok = make(&h->xtma.fk, h->b.fk, g.nf, g.fstride) && make(&h->xtma.pk, h->b.pk, g.nf, g.fstride) &&
+              make(&h->xtma.qv, h->b.QV, g.nf, g.fstride);
+    if (ok && g.gwev)
+        ok = make(&h->xtma.uk, h->b.uk, 6, g.gstride) && make(&h->xtma.puk, h->b.puk, 6, g.gstride) &&
+             make(&h->xtma.qs, h->b.QS, 6, g.gstride);
     if (!ok) {
         h->xtma = psc::XTma{};
         return;

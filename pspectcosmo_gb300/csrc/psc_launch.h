@@ -81,12 +81,13 @@ struct Buffers {
     const XTma *xtma;            // host copy of the kick operands' tensor maps (null: cp.async staging)
 };
 
-// Tensor maps of the X forward + kick pass's operand tiles (TMA): f_k, pi_k as
-// {lines, x, field, realization} and u_k, pi_u_k as {lines, x, component, realization}, in
-// 8-byte elements, box {lines per tile, N, 1, 1}. on = 0: the pass stages its operands by
+// Tensor maps of the X passes' tiles (TMA): f_k, pi_k, QV as {lines, x, field, realization}
+// and u_k, pi_u_k, QS as {lines, x, component, realization}, in 8-byte elements, box {lines
+// per tile, N, 1, 1}. on = 0: the pass stages its operands by
 // cp.async instead (N > 256, batched launches, or no tensor-map encoder).
 struct XTma {
     CUtensorMap fk, pk, uk, puk;
+    CUtensorMap qv, qs;   // the forward passes' V'_k and S_k arrays: the X forward's input tiles
     int on;
     int xi;   // the X inverse pass stages f_k and pi too (FP32: its two tiles keep two blocks per SM)
 };

@@ -305,7 +305,7 @@ __device__ __forceinline__ void kr_fft_x_final_body(const VB &vb, Geo g, const c
     using RP = RegPlan<L>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *sm = reinterpret_cast<C *>(smem_raw);
-    __shared__ uint64_t xbar;   // completion of the operand tiles' tensor copies (TMA)
+    __shared__ uint64_t qbar, xbar;   // completion of the input tile's / operand tiles' tensor copies (TMA)
     {
         const long long rf = (long long)vb.z() * g.fstride, rg = (long long)vb.z() * g.gstride;
         QV += rf;
@@ -338,24 +338,45 @@ __device__ __forceinline__ void kr_fft_x_final_body(const VB &vb, Geo g, const c
     // 128-byte aligned: the launch adds 128 bytes of shared memory for it); otherwise each
     // thread copies its own elements with cp.async.
     const bool use_tma = tma != nullptr;
+    // with tensor maps the three tiles (the transform's input, then the two operands) sit
+    // 128-byte aligned from the start of the buffer: the input tile doubles as the exchange
+    // buffer once every thread holds its elements
+    if (use_tma) sm = reinterpret_cast<C *>((reinterpret_cast<uintptr_t>(sm) + 127) & ~(uintptr_t)127);
     C *opA = sm + TL * L;
-    if (use_tma) opA = reinterpret_cast<C *>((reinterpret_cast<uintptr_t>(opA) + 127) & ~(uintptr_t)127);
     C *opB = opA + TL * L;
     const C *gA = field ? fk : uk, *gB = field ? pk : puk;
+    C v[16];
     if (use_tma) {
         // a failed stage: no further waits (one thread reads the error word, so that the block
         // decides as one while another block may be writing it)
         if (__syncthreads_or(threadIdx.x == 0 && bg->err != 0)) return;
         if (threadIdx.x == 0) {
+            mbar_init(&qbar, 1);
             mbar_init(&xbar, 1);
             mbar_fence_init();
+            const int w8 = (int)(sizeof(C) / 8), arr = field ? job : job - g.nf, c0 = (int)(vb.x() * TL) * w8;
+            mbar_arrive_expect_tx(&qbar, (unsigned)(TL * L * sizeof(C)));
+            tma_load_4d(sm, field ? &tma->qv : &tma->qs, c0, 0, arr, (int)vb.z(), &qbar);
             mbar_arrive_expect_tx(&xbar, 2u * (unsigned)(TL * L * sizeof(C)));
-            const int w8 = (int)(sizeof(C) / 8), arr = field ? job : job - g.nf;
             const CUtensorMap *ma = field ? &tma->fk : &tma->uk, *mb = field ? &tma->pk : &tma->puk;
-            tma_load_4d(opA, ma, (int)(vb.x() * TL) * w8, 0, arr, (int)vb.z(), &xbar);
-            tma_load_4d(opB, mb, (int)(vb.x() * TL) * w8, 0, arr, (int)vb.z(), &xbar);
+            tma_load_4d(opA, ma, c0, 0, arr, (int)vb.z(), &xbar);
+            tma_load_4d(opB, mb, c0, 0, arr, (int)vb.z(), &xbar);
         }
-        // (the transform's barriers order the mbarrier's initialisation before the waits below)
+        __syncthreads();   // the mbarriers are initialised before any thread waits on them
+        const bool ok = mbar_wait_bounded(&qbar, 0, bg->wait_ns);
+        if (__syncthreads_or(!ok)) {
+            // the input tile did not land in time: report it, wait once more (bounded) for all
+            // three tiles still in flight so that none can write into shared memory after the
+            // block has left, and leave (PSC_ERR_DEVICE when they never land)
+            int *err = &const_cast<DevBG *>(bg)->err;
+            if (threadIdx.x == 0) report_err(err, PSC_ERR_TIMEOUT);
+            const bool landed = mbar_wait_bounded(&qbar, 0, bg->wait_ns) && mbar_wait_bounded(&xbar, 0, bg->wait_ns);
+            if (__syncthreads_or(!landed) && threadIdx.x == 0) report_err(err, PSC_ERR_DEVICE);
+            return;
+        }
+#pragma unroll
+        for (int r = 0; r < 16; ++r) v[r] = sm[ix(j + r * RP::P)];
+        __syncthreads();   // every thread holds its elements before the transform reuses the tile
     } else {
         if (valid) {
 #pragma unroll
@@ -367,11 +388,10 @@ __device__ __forceinline__ void kr_fft_x_final_body(const VB &vb, Geo g, const c
             }
         }
         cp_async_commit();
-    }
-    C v[16];
 #pragma unroll
-    for (int r = 0; r < 16; ++r)
-        v[r] = valid ? src[(long long)(j + r * RP::P) * stride + line] : mk<T>(0, 0);
+        for (int r = 0; r < 16; ++r)
+            v[r] = valid ? src[(long long)(j + r * RP::P) * stride + line] : mk<T>(0, 0);
+    }
     fft_reg<C, L, -1>(v, sm, ix, j, tw, N / L);
     if (use_tma) {
         // every thread waits for the tiles (bounded). If they did not land in time: report the
