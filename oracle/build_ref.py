@@ -122,6 +122,19 @@ CONFIGS: dict[str, tuple[str, dict[str, str]]] = {
         "initfield[]": "{0.193 * MPl, 0., 0.01 * MPl}",
         "initderivs[]": "{-0.142e-6 * MPl * MPl, 0., 0.}",
     }),
+    # four fields (pspectcosmo_gb300/models/four_field.h), the real-space step with GWs
+    "gw4_n16_vv2": ("four_field", {
+        "N": "16", "VV": "2", "nflds": "4", "kIR": "1",
+        "SPECTRAL_FLAG": "false", "WITH_GW": "true",
+        "initfield[]": "{0.193 * MPl, 0., 0., 0.}",
+        "initderivs[]": "{-0.142e-6 * MPl * MPl, 0., 0., 0.}",
+    }),
+    "gw4_n32_vv2": ("four_field", {
+        "N": "32", "VV": "2", "nflds": "4", "kIR": "1",
+        "SPECTRAL_FLAG": "false", "WITH_GW": "true",
+        "initfield[]": "{0.193 * MPl, 0., 0., 0.}",
+        "initderivs[]": "{-0.142e-6 * MPl * MPl, 0., 0., 0.}",
+    }),
     # real-space pseudo-spectral path with gravitational waves (evolve_VV)
     "gw2_n16_vv4": ("phi2chi2", {
         "N": "16", "VV": "4", "nflds": "2", "kIR": "1",

@@ -153,11 +153,8 @@ __global__ void __launch_bounds__(256) k_ifft_y(Geo g, cplx<T> *__restrict__ TA,
     }
 }
 
-// Forward Y pass in place over a list of arrays (blockIdx.y selects the array).
-struct ArrList {
-    void *p[8];
-    long long rs[8];
-};
+// Forward Y pass in place over a list of arrays (blockIdx.y selects the array; ArrList,
+// psc_launch.h, holds up to PSC_MAX_FIELDS + 6 of them).
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_fft_y(Geo g, ArrList arrs, const cplx<T> *__restrict__ tw) {

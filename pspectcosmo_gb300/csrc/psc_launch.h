@@ -92,11 +92,12 @@ struct XTma {
     int xi;   // the X inverse pass stages f_k and pi too (FP32: its two tiles keep two blocks per SM)
 };
 
-// Up to eight arrays of the forward passes (V' of each field, then S_ab) with the realization
-// stride of each (elements).
-struct ArrList8 {
-    void *p[8];
-    long long rs[8];
+// The arrays of the forward passes (V' of each field, then the six S_ab: up to
+// PSC_MAX_FIELDS + 6) with the realization stride of each (elements).
+constexpr int kMaxArrays = PSC_MAX_FIELDS + 6;
+struct ArrList {
+    void *p[kMaxArrays];
+    long long rs[kMaxArrays];
 };
 
 // Batches of several configurations (lattice sizes) advanced by ONE launch per pass: the work
@@ -114,7 +115,7 @@ struct BatchGroup {
     void *fk, *pk, *uk, *puk, *TA, *TB, *TC, *QV, *QS, *tw, *Fk, *Fu;
     double *partKG, *partV;
     DevBG *bg;
-    ArrList8 fwd;                // the forward passes' arrays
+    ArrList fwd;                // the forward passes' arrays
 };
 struct BatchTable {
     int ngroups;

@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_ifft_y(Ge
 
 
 template <typename T, int L, class VB>
-__device__ __forceinline__ void kr_fft_y_body(const VB &vb, Geo g, const ArrList8 &arrs, const cplx<T> *__restrict__ tw) {
+__device__ __forceinline__ void kr_fft_y_body(const VB &vb, Geo g, const ArrList &arrs, const cplx<T> *__restrict__ tw) {
     using C = cplx<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *sm = reinterpret_cast<C *>(smem_raw);
@@ -293,7 +293,7 @@ __device__ __forceinline__ void kr_fft_y_body(const VB &vb, Geo g, const ArrList
 }
 
 template <typename T, int L>
-__global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(3)) kr_fft_y(Geo g, const __grid_constant__ ArrList8 arrs,
+__global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(3)) kr_fft_y(Geo g, const __grid_constant__ ArrList arrs,
                                                  const cplx<T> *__restrict__ tw) {
     kr_fft_y_body<T, L, HwBlock>(vblock_hw(), g, arrs, tw);
 }
@@ -1578,7 +1578,7 @@ __global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_fft_x_gwa
 // last pass of the padded step's r2c on the padded grid, whose kick runs on the
 // lattice grid afterwards.
 template <typename T, int L>
-__global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(3)) kr_fft_x_plain(Geo g, const __grid_constant__ ArrList8 arrs,
+__global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(3)) kr_fft_x_plain(Geo g, const __grid_constant__ ArrList arrs,
                                                        const cplx<T> *__restrict__ tw) {
     using C = cplx<T>;
     using RP = RegPlan<L>;

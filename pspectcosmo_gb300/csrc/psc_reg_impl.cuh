@@ -134,7 +134,7 @@ struct RegLaunch {
             zpass_any(cfg, b, st, R);
         }
         mark(3);
-        ArrList8 al{};
+        ArrList al{};
         int nj = 0;
         for (int f = 0; f < g.nf; ++f) {
             al.rs[nj] = g.fstride;
@@ -177,7 +177,7 @@ struct RegLaunch {
         kr_ifft_x<T, N, false, false><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, fk, nullptr, TA, nullptr, b.bg, tw);
         kr_ifft_y<T, N, false><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, TA, nullptr, nullptr, b.bg, tw);
         zpass_any(cfg, b, st, 1);
-        ArrList8 al{};
+        ArrList al{};
         for (int f = 0; f < g.nf; ++f) {
             al.rs[f] = g.fstride;
             al.p[f] = QV + (long long)f * g.modes;
@@ -226,7 +226,7 @@ struct RegLaunch {
         const int nbz = adj_z_blocks(N, g.nf);
         kr_zpass_adj<T, M><<<nbz, g.nf * (M / 16) * tl, (size_t)g.nf * tl * ZIdx<M>::LS * sizeof(C), st>>>(
             g, TA, (const T *)fx_tape, QV, part, ad, tw, sh);
-        ArrList8 al{};
+        ArrList al{};
         for (int f = 0; f < g.nf; ++f) al.p[f] = QV + (long long)f * g.modes;
         kr_fft_y<T, N><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, al, tw);
         kr_fft_x_adj<T, N><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, QV, (const C *)Mk, (const C *)f_tape, (C *)Lf, ad,
@@ -254,7 +254,7 @@ struct RegLaunch {
         const size_t smem = (size_t)pin * tl * ZIdx<N>::LS * sizeof(C);
         kr_zpass_adj_gw<T, N><<<(g.lines_z + tl - 1) / tl, pin * P * tl, smem, st>>>(g, TA, TB, TC, QS, (C *)Tarr, tw,
                                                                                     sh);
-        ArrList8 al{};
+        ArrList al{};
         for (int i = 0; i < 3 * g.nf; ++i) al.p[i] = (C *)Tarr + (long long)i * g.modes;
         kr_fft_y<T, N><<<dim3(cfg.nbx, 3 * g.nf), cfg.thr_xy, cfg.smem_xy, st>>>(g, al, tw);
         kr_fft_x_gwadj<T, N><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, (const C *)Tarr, (C *)Lf, ad, tw);

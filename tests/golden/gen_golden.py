@@ -44,6 +44,8 @@ RUNS = {
     "gw3_n16_vv4": ("gw3_n16_vv4", 10, 0.005, 5, True),
     "spec3_n32_vv2": ("spec3_n32_vv2", 40, 0.005, 20, False),
     "gw3_n32_vv4": ("gw3_n32_vv4", 10, 0.005, 5, False),
+    "gw4_n16_vv2": ("gw4_n16_vv2", 10, 0.005, 5, True),
+    "gw4_n32_vv2": ("gw4_n32_vv2", 10, 0.005, 5, False),
 }
 
 

@@ -2,8 +2,8 @@
 
 * The device compilation of every user model equals its host compilation (psc_model_eval)
   to FP64 / FP32 rounding (the device fuses multiply-adds).
-* Three fields (pspectcosmo_gb300/models/three_field.h) against the reference's own code built
-  with that model.h and nflds = 3 (golden fixtures): the spectral step and the real-space step
+* Three and four fields (pspectcosmo_gb300/models/three_field.h, four_field.h) against the
+  reference's own code built with that model.h and nflds = 3 or 4 (golden fixtures): the spectral step and the real-space step
   with GWs at 16^3 (the generic engine; full final state) and at 32^3 (the register engine's
   user-model Z passes; outputs at every output step). FP64 at the bars of the two-field runs:
   states 1e-10, spectra 1e-10 (spectral) or 1e-7 (real space, the reference's rounding floor
@@ -31,7 +31,7 @@ def _lattice(p):
     return Lattice(p)
 
 
-@pytest.mark.parametrize("name,nf", [("phi2", 1), ("phi2chi2", 2), ("three_field", 3)])
+@pytest.mark.parametrize("name,nf", [("phi2", 1), ("phi2chi2", 2), ("three_field", 3), ("four_field", 4)])
 @pytest.mark.parametrize("precision", [64, 32])
 def test_device_model_equals_host_model(name, nf, precision):
     from pspectcosmo_gb300 import Params
@@ -69,9 +69,9 @@ def _compare_rows(rows, g, blk, p, tol, tol_nk, tol_e):
             assert rel(got[:, c], ref[:, c]) < tol, f"GW spectra column {c}"
 
 
-@pytest.mark.parametrize("run", ["spec3_n16_vv4", "gw3_n16_vv4"])
-def test_three_fields_fp64_match_reference_16(run):
-    """Three fields, 16^3, from the device initial conditions: ICs, final state and outputs
+@pytest.mark.parametrize("run", ["spec3_n16_vv4", "gw3_n16_vv4", "gw4_n16_vv2"])
+def test_user_models_fp64_match_reference_16(run):
+    """Three or four fields, 16^3, from the device initial conditions: ICs, final state and outputs
     against the reference's own run."""
     g, meta = load(run)
     p = params_for(meta, 64)
@@ -100,9 +100,9 @@ def test_three_fields_fp64_match_reference_16(run):
     lat.close()
 
 
-@pytest.mark.parametrize("run", ["spec3_n32_vv2", "gw3_n32_vv4"])
-def test_three_fields_fp64_match_reference_32(run):
-    """Three fields, 32^3 (register engine, user-model Z passes), FP64: outputs at every output
+@pytest.mark.parametrize("run", ["spec3_n32_vv2", "gw3_n32_vv4", "gw4_n32_vv2"])
+def test_user_models_fp64_match_reference_32(run):
+    """Three or four fields, 32^3 (register engine, user-model Z passes), FP64: outputs at every output
     step of the reference's run."""
     g, meta = load(run)
     p = params_for(meta, 64)
@@ -214,3 +214,27 @@ def test_user_model_limits():
         lat.adjoint_chi2(0.005, 2)
     assert e.value.code == PSC_ERR_CONFIG
     lat.close()
+
+
+def test_user_model_batch_equals_individual_lattices():
+    """Realizations of a model.h compiled in (three fields, GW, 32^3 and 64^3 groups) advanced
+    as a batch equal the lattices advanced alone, bit for bit."""
+    from pspectcosmo_gb300 import Ensemble, Lattice, Params
+
+    ps = [Params.user_model("three_field", 3, initfield=(0.193, 0.0, 0.01), initderivs=(-0.142e-6, 0.0, 0.0),
+                            N=N, vv=4, spectral=0, with_gw=1, seed=1 + i, precision=32)
+          for i, N in enumerate((32, 32, 64))]
+    ens = Ensemble(ps)
+    assert ens.groups == 2
+    ens.initialize()
+    ens.evolve(0.005, 3)
+    for idx, p in enumerate(ps):
+        lat = _lattice(p)
+        lat.initialize()
+        lat.evolve(0.005, 3)
+        a, b = ens.get_state(idx), lat.get_state()
+        for k in ("f_k", "pi_k", "u_k", "pi_u_k"):
+            assert np.array_equal(a[k], b[k]), (idx, k)
+        assert a["a"] == b["a"], idx
+        lat.close()
+    ens.close()

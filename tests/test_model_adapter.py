@@ -31,7 +31,7 @@ REF_MODEL = os.path.join(build_ref.REF, "model.h")
 NPTS = 64
 
 CASES = [("phi2", os.path.join(MODELS, "phi2.h"), 1), ("phi2chi2", os.path.join(MODELS, "phi2chi2.h"), 2),
-         ("three_field", os.path.join(MODELS, "three_field.h"), 3)]
+         ("three_field", os.path.join(MODELS, "three_field.h"), 3), ("four_field", os.path.join(MODELS, "four_field.h"), 4)]
 
 HARNESS = r"""
 #include <cmath>
@@ -177,16 +177,17 @@ def test_user_model_ids_and_limits():
     L = load_library()
     names = model_names()
     assert names[0] == "builtin:phi2" and names[1] == "builtin:phi2chi2"
-    assert {"phi2", "phi2chi2", "three_field"} <= set(names.values())
+    assert {"phi2", "phi2chi2", "three_field", "four_field"} <= set(names.values())
     for mid, nm in names.items():
         assert L.psc_model_nterms(mid) == {"builtin:phi2": 1, "builtin:phi2chi2": 2, "phi2": 1, "phi2chi2": 2,
-                                           "three_field": 3}.get(nm, L.psc_model_nterms(mid))
+                                           "three_field": 3, "four_field": 4}.get(nm, L.psc_model_nterms(mid))
     assert L.psc_model_nterms(99) == 0
 
 
-@pytest.mark.parametrize("run", ["spec3_n16_vv4", "gw3_n16_vv4", "spec3_n32_vv2", "gw3_n32_vv4"])
-def test_three_field_initial_conditions_match_reference(run):
-    """initialize() of the reference built with three_field.h and nflds = 3 against the
+@pytest.mark.parametrize("run", ["spec3_n16_vv4", "gw3_n16_vv4", "spec3_n32_vv2", "gw3_n32_vv4", "gw4_n16_vv2",
+                                 "gw4_n32_vv2"])
+def test_user_model_initial_conditions_match_reference(run):
+    """initialize() of the reference built with three_field.h (nflds = 3) or four_field.h (4) against the
     library's host generator with the same model compiled in: the scalar modes use the model's
     effective_mass (initialize.cpp:644), the background its potential_energy (:654)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
