@@ -122,6 +122,12 @@ CONFIGS: dict[str, tuple[str, dict[str, str]]] = {
         "initfield[]": "{0.193 * MPl, 0., 0.01 * MPl}",
         "initderivs[]": "{-0.142e-6 * MPl * MPl, 0., 0.}",
     }),
+    # three fields on the padded (dealiased) spectral step
+    "pad3_n16_vv4": ("three_field", {
+        "N": "16", "VV": "4", "nflds": "3", "kIR": "1", "PAD_FLAG": "true", "N_pad": "32",
+        "initfield[]": "{0.193 * MPl, 0., 0.01 * MPl}",
+        "initderivs[]": "{-0.142e-6 * MPl * MPl, 0., 0.}",
+    }),
     # four fields (pspectcosmo_gb300/models/four_field.h), the real-space step with GWs
     "gw4_n16_vv2": ("four_field", {
         "N": "16", "VV": "2", "nflds": "4", "kIR": "1",

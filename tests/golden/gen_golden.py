@@ -45,6 +45,7 @@ RUNS = {
     "spec3_n32_vv2": ("spec3_n32_vv2", 40, 0.005, 20, False),
     "gw3_n32_vv4": ("gw3_n32_vv4", 10, 0.005, 5, False),
     "gw4_n16_vv2": ("gw4_n16_vv2", 10, 0.005, 5, True),
+    "pad3_n16_vv4": ("pad3_n16_vv4", 20, 0.005, 10, True),
     "gw4_n32_vv2": ("gw4_n32_vv2", 10, 0.005, 5, False),
 }
 

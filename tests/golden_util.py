@@ -28,7 +28,7 @@ def params_for(meta: dict, precision: int = 64) -> Params:
     elif c.startswith("gw4"):
         p = Params.user_model("four_field", 4, initfield=(0.193, 0.0, 0.0, 0.0),
                               initderivs=(-0.142e-6, 0.0, 0.0, 0.0), N=meta["N"])
-    elif c.startswith(("spec3", "gw3")):
+    elif c.startswith(("spec3", "gw3", "pad3")):
         # the three-field model file (pspectcosmo_gb300/models/three_field.h) compiled in
         p = Params.user_model("three_field", 3, initfield=(0.193, 0.0, 0.01), initderivs=(-0.142e-6, 0.0, 0.0),
                               N=meta["N"])

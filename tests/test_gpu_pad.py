@@ -1,7 +1,7 @@
 """The padded (dealiased) spectral step and the spectral prolongation on the device.
 
 * FP64 padded step (N = 16, N_pad = 32) against the reference's own evolve_VV_k_pad
-  (golden runs pad1_n16, pad2_n16_vv4): initial a'' (kernel_a_k_pad) to 1e-12, the state
+  (golden runs pad1_n16, pad2_n16_vv4, and pad3_n16_vv4 with the three-field model.h): initial a'' (kernel_a_k_pad) to 1e-12, the state
   after 20 steps to 1e-10 of its largest mode and, for the two-field model where the
   padding changes the result, the fluctuation modes (all but k = 0) to 1e-8 of theirs
   (the unpadded step differs from the padded one by ~5e-7 there).
@@ -39,7 +39,7 @@ def _padded(run, precision=64):
     return g, meta, p, Lattice(p)
 
 
-@pytest.mark.parametrize("run", ["pad1_n16", "pad2_n16_vv4"])
+@pytest.mark.parametrize("run", ["pad1_n16", "pad2_n16_vv4", "pad3_n16_vv4"])
 def test_padded_step_matches_reference(run):
     g, meta, p, lat = _padded(run)
     lat.initialize()

@@ -185,7 +185,7 @@ def test_user_model_ids_and_limits():
 
 
 @pytest.mark.parametrize("run", ["spec3_n16_vv4", "gw3_n16_vv4", "spec3_n32_vv2", "gw3_n32_vv4", "gw4_n16_vv2",
-                                 "gw4_n32_vv2"])
+                                 "gw4_n32_vv2", "pad3_n16_vv4"])
 def test_user_model_initial_conditions_match_reference(run):
     """initialize() of the reference built with three_field.h (nflds = 3) or four_field.h (4) against the
     library's host generator with the same model compiled in: the scalar modes use the model's
