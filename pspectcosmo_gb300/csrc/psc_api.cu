@@ -407,6 +407,9 @@ psc::Buffers buffers_of(psc_handle *h, int r) {
         b.QS = goff(h, h->b.QS, r);
     }
     b.bg = h->b.bg + r;
+    // the tensor maps describe all R realizations at once: a single-lattice view has none
+    b.xtma = nullptr;
+    b.ytma = nullptr;
     return b;
 }
 
@@ -993,39 +996,79 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     return fn;
 }
 
-// The X forward + kick pass's operand tiles as tensor maps: an array group of the handle
-// (na arrays of `modes` complex, realization stride rstride) as {lines_x, N, na, R} in 8-byte
-// elements (an FP64 complex is two), box {lines per tile, N, 1, 1}. Register engine, N <= 256
-// (a box edge is at most 256), single-lattice or batch handles alike; otherwise off.
+// The tensor maps of the handle's passes (TMA staging), re-encoded whenever the tile shape
+// changes. Register engine, N <= 256 (a box edge is at most 256), single-lattice or batch
+// handles alike (the realization is a map dimension); otherwise, or when the handle's mask
+// (psc_set_tensor_maps) leaves a group out, that group is off and its passes load directly.
+// X passes: an array group (na arrays of `modes` complex, realization stride rstride) as
+// {lines_x, N, na, R} in 8-byte elements (an FP64 complex is two), box {lines per tile, N, 1, 1}.
+// Y forward pass (FP32): V' and S_ab as {2 H, N N/2, na, R} (rows of two y; YTma,
+// psc_launch.h), boxes {TL, N/2, 1, 1} (even rows) and {TL + 2, N/2, 1, 1} (odd rows); on for
+// the sizes with the tensor-map instantiation (N = 128, 256) when TL divides N/2 and a box row
+// is a multiple of 16 bytes.
 void encode_xtma(psc_handle *h) {
     h->xtma = psc::XTma{};
+    h->ytma = psc::YTma{};
     h->b.xtma = nullptr;
+    h->b.ytma = nullptr;
     const psc::Geo &g = h->cfg.g;
     auto enc = tensor_map_encoder();
     if (!enc || !g.reg || g.N > 256 || h->padded) return;
     const cuuint64_t w = h->csize / 8, TL = 1u << g.tlx_shift;
-    auto make = [&](CUtensorMap *m, void *base, int na, long long rstride) -> bool {
-        const cuuint64_t dims[4] = {(cuuint64_t)g.lines_x * w, (cuuint64_t)g.N, (cuuint64_t)na, (cuuint64_t)h->R};
-        const cuuint64_t strides[3] = {(cuuint64_t)g.lines_x * h->csize, (cuuint64_t)g.modes * h->csize,
-                                       (cuuint64_t)(rstride > 0 ? rstride : g.modes * na) * h->csize};
-        const cuuint32_t box[4] = {(cuuint32_t)(TL * w), (cuuint32_t)g.N, 1, 1};
+    auto map4 = [&](CUtensorMap *m, void *base, const cuuint64_t (&dims)[4], const cuuint64_t (&strides)[3],
+                    cuuint32_t box0, cuuint32_t box1) -> bool {
+        const cuuint32_t box[4] = {box0, box1, 1, 1};
         const cuuint32_t es[4] = {1, 1, 1, 1};
         return enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 4, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
     };
-    bool ok = make(&h->xtma.fk, h->b.fk, g.nf, g.fstride) && make(&h->xtma.pk, h->b.pk, g.nf, g.fstride) &&
-              make(&h->xtma.qv, h->b.QV, g.nf, g.fstride);
-    if (ok && g.gwev)
-        ok = make(&h->xtma.uk, h->b.uk, 6, g.gstride) && make(&h->xtma.puk, h->b.puk, 6, g.gstride) &&
-             make(&h->xtma.qs, h->b.QS, 6, g.gstride);
-    if (!ok) {
-        h->xtma = psc::XTma{};
-        return;
+    auto rs = [&](long long rstride, int na) {
+        return (cuuint64_t)(rstride > 0 ? rstride : g.modes * na) * h->csize;
+    };
+    if (h->tmap_mask & PSC_TMAP_X) {
+        auto make = [&](CUtensorMap *m, void *base, int na, long long rstride) -> bool {
+            const cuuint64_t dims[4] = {(cuuint64_t)g.lines_x * w, (cuuint64_t)g.N, (cuuint64_t)na, (cuuint64_t)h->R};
+            const cuuint64_t strides[3] = {(cuuint64_t)g.lines_x * h->csize, (cuuint64_t)g.modes * h->csize,
+                                           rs(rstride, na)};
+            return map4(m, base, dims, strides, (cuuint32_t)(TL * w), (cuuint32_t)g.N);
+        };
+        bool ok = make(&h->xtma.fk, h->b.fk, g.nf, g.fstride) && make(&h->xtma.pk, h->b.pk, g.nf, g.fstride) &&
+                  make(&h->xtma.qv, h->b.QV, g.nf, g.fstride);
+        if (ok && g.gwev)
+            ok = make(&h->xtma.uk, h->b.uk, 6, g.gstride) && make(&h->xtma.puk, h->b.puk, 6, g.gstride) &&
+                 make(&h->xtma.qs, h->b.QS, 6, g.gstride);
+        if (ok) {
+            h->xtma.on = 1;
+            h->xtma.xi = h->csize == 8 ? 1 : 0;   // FP64: three 64 KB tiles would leave one block per SM
+            h->b.xtma = &h->xtma;
+        } else {
+            h->xtma = psc::XTma{};
+        }
     }
-    h->xtma.on = 1;
-    h->xtma.xi = h->csize == 8 ? 1 : 0;   // FP64: three 64 KB tiles would leave one block per SM
-    h->b.xtma = &h->xtma;
+    const cuuint64_t ox = w == 1 ? 1 : 0;   // FP32: the odd rows' box starts one element early
+    const bool yfits = w == 1 && psc::y_pipe_size(g.N) && TL <= (cuuint64_t)g.M && (TL * w * 8) % 16 == 0 &&
+                       (TL + 2 * ox) * w <= 256 && g.M <= 256;
+    if ((h->tmap_mask & PSC_TMAP_Y) && yfits) {
+        auto make = [&](CUtensorMap *me, CUtensorMap *mo, void *base, int na, long long rstride) -> bool {
+            const cuuint64_t dims[4] = {(cuuint64_t)(2 * g.H) * w, (cuuint64_t)g.N * g.M, (cuuint64_t)na,
+                                        (cuuint64_t)h->R};
+            const cuuint64_t strides[3] = {(cuuint64_t)(2 * g.H) * h->csize, (cuuint64_t)g.modes * h->csize,
+                                           rs(rstride, na)};
+            return map4(me, base, dims, strides, (cuuint32_t)(TL * w), (cuuint32_t)g.M) &&
+                   map4(mo, base, dims, strides, (cuuint32_t)((TL + 2 * ox) * w), (cuuint32_t)g.M);
+        };
+        psc::YTma &y = h->ytma;
+        bool ok = make(&y.ae, &y.ao, h->b.QV, g.nf, g.fstride);
+        if (ok && g.gwev) ok = make(&y.be, &y.bo, h->b.QS, 6, g.gstride);
+        if (ok) {
+            y.na = g.nf;
+            y.on = 1;
+            h->b.ytma = &h->ytma;
+        } else {
+            h->ytma = psc::YTma{};
+        }
+    }
 }
 
 // ------------------------------------------------------------------ autotuner
@@ -1647,6 +1690,24 @@ int psc_set_shapes(psc_handle *h, const int *shape) {
     return apply_shapes(h, tc);
 }
 
+int psc_set_tensor_maps(psc_handle *h, int mask) {
+    if (!h) return fail(PSC_ERR_ARG, "null handle");
+    if (mask & ~(PSC_TMAP_X | PSC_TMAP_Y)) return fail(PSC_ERR_ARG, "unknown tensor-map group");
+    h->tmap_mask = mask;
+    encode_xtma(h);
+    if (h->gexec) {   // the step graph holds the maps of its launches
+        cudaGraphExecDestroy(h->gexec);
+        h->gexec = nullptr;
+    }
+    return PSC_OK;
+}
+
+int psc_get_tensor_maps(psc_handle *h, int *mask) {
+    if (!h || !mask) return fail(PSC_ERR_ARG, "null argument");
+    *mask = (h->b.xtma ? PSC_TMAP_X : 0) | (h->b.ytma ? PSC_TMAP_Y : 0);
+    return PSC_OK;
+}
+
 int psc_get_shapes(psc_handle *h, int *shape) {
     if (!h || !shape) return fail(PSC_ERR_ARG, "null argument");
     const bool tunable = h->cfg.g.reg && !h->padded;
@@ -1692,23 +1753,37 @@ int psc_selftest_bulk_wait(double limit_ms, int *status) {
     return PSC_OK;
 }
 
-int psc_test_wait_hook(psc_handle *h, double limit_ms, int plant_bytes) {
-    if (!h || !(limit_ms > 0.0) || limit_ms > 10000.0 || plant_bytes < 0 || plant_bytes > 4096)
+int psc_test_wait_hook_pass(psc_handle *h, double limit_ms, int plant_bytes, int pass) {
+    if (!h || !(limit_ms > 0.0) || limit_ms > 10000.0 || plant_bytes < 0 || plant_bytes > 4096 || pass < 0 ||
+        pass > 4)
         return fail(PSC_ERR_ARG, "bad argument");
     const psc::Geo &g = h->cfg.g;
-    const bool bulk = g.gwev && g.reg && h->p0().precision == 32 &&
-                      ((size_t(1) << g.tlz_shift) * (size_t)g.H * h->csize) % 16 == 0;
-    if (plant_bytes && !bulk)
-        return fail(PSC_ERR_CONFIG, "the handle's GW Z pass does not stage its tiles by bulk copies");
+    bool staged = false;
+    switch (pass) {
+    case 0: staged = h->b.xtma && h->xtma.xi; break;                 // X inverse (FP32 tensor maps)
+    case 1: staged = false; break;                                   // Y inverse (direct loads)
+    case 3: staged = h->b.ytma != nullptr; break;                    // Y forward (tensor maps)
+    case 2:                                                          // GW Z pass (bulk copies)
+        staged = g.gwev && g.reg && h->p0().precision == 32 &&
+                 ((size_t(1) << g.tlz_shift) * (size_t)g.H * h->csize) % 16 == 0;
+        break;
+    default: staged = h->b.xtma != nullptr; break;                   // X forward + kick (tensor maps)
+    }
+    if (plant_bytes && !staged) return fail(PSC_ERR_CONFIG, "the handle's pass does not stage its tiles by bulk copies");
     for (int r = 0; r < h->R; ++r) {
         psc::DevBG bg;
         int rc;
         if ((rc = read_bg(h, r, &bg))) return rc;
         bg.wait_ns = (unsigned long long)(limit_ms * 1e6);
         bg.wait_plant = plant_bytes;
+        bg.wait_plant_pass = pass;
         if ((rc = write_bg(h, r, bg))) return rc;
     }
     return PSC_OK;
+}
+
+int psc_test_wait_hook(psc_handle *h, double limit_ms, int plant_bytes) {
+    return psc_test_wait_hook_pass(h, limit_ms, plant_bytes, 2);
 }
 
 int psc_pass_bytes(psc_handle *h, double *bytes) {

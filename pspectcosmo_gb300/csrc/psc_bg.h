@@ -28,10 +28,12 @@ struct DevBG {
     int s, alpha, nf, nterms, mask, model, nbx, nbz;   // nbz: blocks of the <V> partials
     int stage, steps_left, err, pad;
     // bounded device-side waits: the limit of one wait (1 s unless a test sets it), and a
-    // test hook: bytes a GW Z pass tile is told to expect that no copy delivers, so its
+    // test hook: bytes every staged tile of pass wait_plant_pass (PSC_NPASS order: 0 X
+    // inverse, 2 Z, 3 Y forward, 4 X forward) is told to expect that no copy delivers, so its
     // wait runs out after the real copies have landed (0 = off)
     unsigned long long wait_ns;
     int wait_plant, fp32;           // fp32: the handle's arrays hold FP32 values
+    int wait_plant_pass, pad2;
     // FP64 shadow of each field's homogeneous mode f_k(0), pi_k(0) (re, im). The background
     // kernel evolves it (drift when a stage begins, the kicks after the kick pass) and writes
     // its rounding into the arrays, which every other kernel reads as before. Stored in FP32

@@ -378,6 +378,10 @@ __device__ __forceinline__ void mbar_complete_tx(uint64_t *bar, unsigned bytes) 
     asm volatile("mbarrier.complete_tx.relaxed.cta.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes)
                  : "memory");
 }
+// The test hook's planted bytes for a staged tile of pass `pass` (0 in normal runs).
+__device__ __forceinline__ unsigned planted(const DevBG *bg, int pass) {
+    return bg->wait_plant_pass == pass ? (unsigned)bg->wait_plant : 0u;
+}
 // Error word of a device record: the first cause wins (a later failure does not overwrite
 // it), except that PSC_ERR_DEVICE, which says the context can no longer be trusted,
 // replaces a PSC_ERR_TIMEOUT.

@@ -867,6 +867,8 @@ void plan(const psc_params &p, int R, LaunchCfg *cfg, const TileChoice *tc) {
         cfg->smem_xy = (size_t)tl * g.N * csize;
         cfg->smem_xf = 3 * cfg->smem_xy + 128;   // + the alignment of the TMA operand tiles
         cfg->smem_xi = 3 * cfg->smem_xy + 128;
+        // a Y tile staged by tensor copies: TL even rows and TL + 2 odd rows (FP32) of N/2
+        cfg->smem_ys = (size_t)(tl + (csize == 8 ? 1 : 0)) * g.N * csize;
         cfg->nbx = (g.lines_x + tl - 1) / tl;
         const int Pz = g.M / 16;
         int tlz = 1;   // lines per tile: the largest power of two with nin x tlz x Pz <= 256 threads
@@ -895,6 +897,7 @@ void plan(const psc_params &p, int R, LaunchCfg *cfg, const TileChoice *tc) {
         if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
                                                       cudaSuccess || sms <= 0)
             sms = 152;
+        cfg->sms = sms;
         const size_t smem_sm = 227 * 1024;
         int per_sm = (int)(smem_sm / cfg->smem_z);
         if (per_sm > ((gw_staged && !user) ? 3 : 2)) per_sm = (gw_staged && !user) ? 3 : 2;
@@ -917,6 +920,7 @@ void plan(const psc_params &p, int R, LaunchCfg *cfg, const TileChoice *tc) {
     cfg->smem_xy = (size_t)2 * tl * g.N * csize;
     cfg->smem_xf = cfg->smem_xy;
     cfg->smem_xi = cfg->smem_xy;
+    cfg->smem_ys = 0;
     cfg->nbx = (g.lines_x + tl - 1) / tl;
     // Z pass: TLz lines, two H-row buffers + nslot M-row real-line slots.
     int tlz = 32;

@@ -13,6 +13,7 @@ namespace psc {
 struct DevBG;
 struct DevAdj;
 struct XTma;
+struct YTma;
 
 // Lattice geometry and tiling, passed by value to every pass kernel.
 struct Geo {
@@ -52,8 +53,10 @@ struct LaunchCfg {
     size_t smem_xy, smem_z;      // dynamic shared memory bytes
     size_t smem_xf;              // X forward + kick pass (exchange tile + two prefetched operand tiles)
     size_t smem_xi;              // X inverse pass with tensor-map staging (exchange tile + f_k and pi tiles)
+    size_t smem_ys;              // one array's tile of a Y pass staged by tensor copies (even + odd rows)
     int nbx;                     // blocks of the X / Y passes (per array)
     int nbz;                     // blocks of the Z pass
+    int sms = 0;                 // SMs of the device (the persistent passes' waves)
 };
 
 // Device buffers of one lattice. Complex arrays hold cplx<T> of the handle's
@@ -79,6 +82,7 @@ struct Buffers {
     // the next step call uses it instead of a force evaluation (null: not kept)
     void *Fk, *Fu;
     const XTma *xtma;            // host copy of the kick operands' tensor maps (null: cp.async staging)
+    const YTma *ytma;            // the Y forward pass's tensor maps (V', S_ab); null: direct loads
 };
 
 // Tensor maps of the X passes' tiles (TMA): f_k, pi_k, QV as {lines, x, field, realization}
@@ -91,6 +95,23 @@ struct XTma {
     int on;
     int xi;   // the X inverse pass stages f_k and pi too (FP32: its two tiles keep two blocks per SM)
 };
+
+// Tensor maps of the Y passes' tiles (TMA). A Y line's element stride is H = N/2 + 1 complex,
+// in FP32 8 H bytes, never a multiple of 16, so an array is mapped as rows of two y (pairs):
+// {2 H, N N / 2, array, realization} in 8-byte elements (an FP64 complex being two), pair stride
+// 16 H bytes. A tile of TL consecutive kz < N/2 at one x is two boxes of N/2 pairs: the even
+// rows {TL, N/2} at kz0, the odd rows at H + kz0; in FP32 that start is odd, so the odd box
+// starts one element earlier (H - 1 + kz0, even) and is TL + 2 wide (a multiple of 16 bytes).
+// The FP32 Y forward pass uses them (in FP64 the staging measured no faster): a* map the fields'
+// V' (the first na arrays of the pass), b* the six S_ab. on = 0: direct loads. (The Y inverse
+// pass keeps its direct loads: staged this way it measured slower.)
+struct YTma {
+    CUtensorMap ae, ao, be, bo;   // even-row and odd-row boxes of the two array groups
+    int na;
+    int on;
+};
+// the lattice sizes whose Y forward pass has its tensor-map instantiation (FP32)
+constexpr bool y_pipe_size(int N) { return N == 128 || N == 256; }
 
 // The arrays of the forward passes (V' of each field, then the six S_ab: up to
 // PSC_MAX_FIELDS + 6) with the realization stride of each (elements).

@@ -86,7 +86,7 @@ __device__ __forceinline__ void kr_ifft_x_body(const VB &vb, Geo g, cplx<T> *__r
         if (threadIdx.x == 0) {
             mbar_init(&ibar, 1);
             mbar_fence_init();
-            mbar_arrive_expect_tx(&ibar, (DRIFT ? 2u : 1u) * (unsigned)(TL * L * sizeof(C)));
+            mbar_arrive_expect_tx(&ibar, (DRIFT ? 2u : 1u) * (unsigned)(TL * L * sizeof(C)) + planted(bg, 0));
             const int w8 = (int)(sizeof(C) / 8), c0 = (int)(vb.x() * TL) * w8;
             tma_load_4d(opF, &tma->fk, c0, 0, (int)vb.y(), (int)vb.z(), &ibar);
             if (DRIFT) tma_load_4d(opP, &tma->pk, c0, 0, (int)vb.y(), (int)vb.z(), &ibar);
@@ -97,7 +97,10 @@ __device__ __forceinline__ void kr_ifft_x_body(const VB &vb, Geo g, cplx<T> *__r
         const bool ok = mbar_wait_bounded(&ibar, 0, bg->wait_ns);
         if (__syncthreads_or(!ok)) {
             int *err = &const_cast<DevBG *>(bg)->err;
-            if (threadIdx.x == 0) report_err(err, PSC_ERR_TIMEOUT);
+            if (threadIdx.x == 0) {
+                report_err(err, PSC_ERR_TIMEOUT);
+                if (planted(bg, 0)) mbar_complete_tx(&ibar, planted(bg, 0));   // the test hook's bytes
+            }
             const bool landed = mbar_wait_bounded(&ibar, 0, bg->wait_ns);
             if (__syncthreads_or(!landed) && threadIdx.x == 0) report_err(err, PSC_ERR_DEVICE);
             return;
@@ -223,8 +226,10 @@ __device__ __forceinline__ void kr_ifft_y_body(const VB &vb, Geo g, cplx<T> *__r
     if (GW) {
         // This thread's TA and TB elements are copied into two shared staging tiles by
         // cp.async at once (every load in flight together, TA read from HBM once); then
-        // three transforms from the tiles: d/dy TA -> TC, TA -> TA, TB -> TB (one copy of
-        // the transform code keeps the register allocation spill-free).
+        // three transforms from the tiles: d/dy TA -> TC, TA -> TA, TB -> TB (one copy of the
+        // transform code keeps the register allocation spill-free). (Staged by tensor copies
+        // instead, as the Y forward pass is, this pass measured slower on GB300: 0.215 against
+        // 0.201 ms at 256^3.)
         using RP = RegPlan<L>;
         const int sh = g.tlx_shift, TL = 1 << sh;
         const int t = threadIdx.x & (TL - 1), j = threadIdx.x >> sh;
@@ -298,6 +303,170 @@ __global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(3)) kr_fft_y(Geo
     kr_fft_y_body<T, L, HwBlock>(vblock_hw(), g, arrs, tw);
 }
 
+// Y forward pass staged by tensor maps (YTma, psc_launch.h). Its tiles: the first N (N/2)/TL
+// hold TL consecutive kz < N/2 of one x plane, staged by two tensor copies (the even and the
+// odd rows); the last N/TL hold the kz = N/2 column of TL consecutive x, staged by each
+// thread's cp.async copies into the same layout. Together they cover the N H lines in the
+// same number of tiles as kr_fft_y (TL divides N/2), and every line is transformed alike.
+struct YTile {
+    int x, kz;     // this thread's line
+    int x0, kz0;   // the tile's first line
+    bool column;   // a kz = N/2 tile
+};
+
+// Staged tile of one array: the even rows y = 2p as [p][TL], then the odd rows y = 2p + 1 as
+// [p][TL + 2 OX] from element OX on. OX = 1 in FP32, where the odd rows' box starts one element
+// before kz0 (its start must be a multiple of 16 bytes), 0 in FP64.
+template <typename C> __host__ __device__ constexpr int y_ox() { return sizeof(C) == 8 ? 1 : 0; }
+template <typename C>
+__device__ __forceinline__ int y_slot(int n, int t, int TL, int M) {
+    constexpr int OX = y_ox<C>();
+    return (n & 1) ? TL * M + (n >> 1) * (TL + 2 * OX) + OX + t : (n >> 1) * TL + t;
+}
+// A thread's elements n = j + r P (P = L/16, even) all have the parity of j, so their slots
+// are s0 + r sp: y_slot(j) + r (P/2) (row pitch).
+template <typename C, int L>
+__device__ __forceinline__ void y_slots(int j, int t, int TL, int M, int &s0, int &sp) {
+    constexpr int P = RegPlan<L>::P, OX = y_ox<C>();
+    s0 = y_slot<C>(j, t, TL, M);
+    sp = (P / 2) * ((j & 1) ? TL + 2 * OX : TL);
+}
+// elements of one staged array tile: (2 TL + 2 OX) rows of N/2
+template <typename C> __device__ __forceinline__ int y_stage_elems(int TL, int N) { return (TL + y_ox<C>()) * N; }
+
+// Thread 0: the two tensor copies of plane tile y of array `arr`, realization z, into st
+// (128-byte aligned), completing on bar.
+template <typename C>
+__device__ __forceinline__ void y_issue(C *st, const CUtensorMap *me, const CUtensorMap *mo, const YTile &y,
+                                        const Geo &g, int arr, int z, uint64_t *bar) {
+    constexpr int OX = y_ox<C>(), W = (int)(sizeof(C) / 8);
+    const int q0 = y.x0 * g.M;
+    tma_load_4d(st, me, y.kz0 * W, q0, arr, z, bar);
+    tma_load_4d(st + (g.M << g.tlx_shift), mo, (g.H + y.kz0) * W - OX, q0, arr, z, bar);
+}
+
+// Each thread of a column tile copies its own elements of array src (cp.async) into the
+// staged layout.
+template <typename C, int L>
+__device__ __forceinline__ void y_column_async(C *st, const C *src, const YTile &y, int t, int j, const Geo &g) {
+    using RP = RegPlan<L>;
+    int s0, sp;
+    y_slots<C, L>(j, t, 1 << g.tlx_shift, g.M, s0, sp);
+    const C *p = src + (long long)y.x * g.N * g.H + y.kz + (long long)j * g.H;
+#pragma unroll
+    for (int r = 0; r < 16; ++r) cp_async_elem(st + s0 + r * sp, p + (long long)r * RP::P * g.H);
+}
+
+// Y forward pass, FP32 tensor-map form, persistent and pipelined: one wave of blocks (two per
+// SM; three, at 80 registers, measured slower) walks the items w = (tile, array, realization),
+// tile fastest. While an item's tile is transformed, thread 0 has already issued the tensor
+// copies of the block's next item into the other of two staging buffers (the current one
+// doubles as the exchange buffer), so each tile's load overlaps the previous tile's transform.
+// Column tiles (kz = N/2) are staged by the block's own cp.async copies when their turn comes.
+// Same transform per line: the bits of kr_fft_y.
+template <typename T, int L>
+__global__ void __launch_bounds__(256, 2) kr_fft_y_pipe(Geo g, const __grid_constant__ ArrList arrs,
+                                                       const cplx<T> *__restrict__ tw, const DevBG *bg,
+                                                       const __grid_constant__ YTma ym, int nj, int R) {
+    using C = cplx<T>;
+    using RP = RegPlan<L>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ uint64_t bar[2];   // completion of the tensor copies into staging buffer 0 / 1
+    const int sh = g.tlx_shift, TL = 1 << sh;
+    const int t = threadIdx.x & (TL - 1), j = threadIdx.x >> sh;
+    const unsigned per = (unsigned)(g.M >> sh), nplane = (unsigned)g.N * per, nbx = nplane + (unsigned)(g.N >> sh);
+    const unsigned total = nbx * (unsigned)nj * (unsigned)R;
+    const int se = y_stage_elems<C>(TL, g.N);
+    C *S0 = reinterpret_cast<C *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
+    auto ix = [&](int n) { return n * TL + t; };
+    // thread 0: the two tensor copies of plane-tile item w into st, on br
+    auto issue = [&](unsigned w, C *st, uint64_t *br) {
+        const unsigned b = w % nbx, rest = w / nbx;
+        const int jy = (int)(rest % (unsigned)nj), z = (int)(rest / (unsigned)nj);
+        const bool first = jy < ym.na;
+        YTile y;
+        y.x0 = (int)(b / per);
+        y.kz0 = (int)(b - (unsigned)y.x0 * per) << sh;
+        fence_proxy_async();   // the previous use of st (staging reads, exchange) comes first
+        mbar_arrive_expect_tx(br, (unsigned)(se * sizeof(C)) + planted(bg + z, 3));
+        y_issue(st, first ? &ym.ae : &ym.be, first ? &ym.ao : &ym.bo, y, g, first ? jy : jy - ym.na, z, br);
+    };
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_fence_init();
+    }
+    // a failed stage: no work (one thread reads the error words; the barrier also makes the
+    // initialised mbarriers visible to every thread)
+    bool failed = false;
+    if (threadIdx.x == 0)
+        for (int z = 0; z < R; ++z) failed |= bg[z].err != 0;
+    if (__syncthreads_or(failed)) return;
+    unsigned w = blockIdx.x;
+    if (threadIdx.x == 0 && w < total && w % nbx < nplane) issue(w, S0, &bar[0]);
+    unsigned phase = 0;   // bit i: parity of the next completion of bar[i]
+    int cur = 0;
+    for (; w < total; w += gridDim.x, cur ^= 1) {
+        const unsigned wn = w + gridDim.x;
+        C *Sc = S0 + cur * se;
+        const bool next_tma = wn < total && wn % nbx < nplane;
+        if (threadIdx.x == 0 && next_tma) issue(wn, S0 + (cur ^ 1) * se, &bar[cur ^ 1]);
+        const unsigned b = w % nbx, rest = w / nbx;
+        const int jy = (int)(rest % (unsigned)nj), z = (int)(rest / (unsigned)nj);
+        C *a = reinterpret_cast<C *>(arrs.p[jy]) + (long long)z * arrs.rs[jy];
+        YTile y;
+        if (b < nplane) {
+            y.x0 = (int)(b / per);
+            y.x = y.x0;
+            y.kz = ((int)(b - (unsigned)y.x0 * per) << sh) + t;
+            y.column = false;
+        } else {
+            y.x = ((int)(b - nplane) << sh) + t;
+            y.kz = g.M;
+            y.column = true;
+        }
+        if (y.column) {
+            y_column_async<C, L>(Sc, a, y, t, j, g);
+            cp_async_commit();
+            cp_async_wait_all();   // own elements only
+        } else {
+            const bool ok = mbar_wait_bounded(&bar[cur], (phase >> cur) & 1u, bg[z].wait_ns);
+            if (__syncthreads_or(!ok)) {
+                // report the timeout, count the test hook's planted bytes, wait once more
+                // (bounded) for every copy still in flight (this tile's and the next one's)
+                // and leave; PSC_ERR_DEVICE when they never land
+                int *err = &const_cast<DevBG *>(bg)[z].err;
+                const int zn = next_tma ? (int)(wn / nbx / (unsigned)nj) : 0;
+                if (threadIdx.x == 0) {
+                    report_err(err, PSC_ERR_TIMEOUT);
+                    if (planted(bg + z, 3)) mbar_complete_tx(&bar[cur], planted(bg + z, 3));
+                    if (next_tma && planted(bg + zn, 3)) mbar_complete_tx(&bar[cur ^ 1], planted(bg + zn, 3));
+                }
+                bool landed = mbar_wait_bounded(&bar[cur], (phase >> cur) & 1u, bg[z].wait_ns);
+                if (next_tma)
+                    landed = mbar_wait_bounded(&bar[cur ^ 1], (phase >> (cur ^ 1)) & 1u, bg[z].wait_ns) && landed;
+                if (__syncthreads_or(!landed) && threadIdx.x == 0) report_err(err, PSC_ERR_DEVICE);
+                return;
+            }
+            phase ^= 1u << cur;
+        }
+        int s0, sp;
+        y_slots<C, L>(j, t, TL, g.M, s0, sp);
+        C v[16];
+#pragma unroll
+        for (int r = 0; r < 16; ++r) v[r] = Sc[s0 + r * sp];
+        __syncthreads();   // every thread holds its elements before the transform reuses the tile
+        fft_reg<C, L, -1>(v, Sc, ix, j, tw, g.N / L);
+        const long long base = (long long)y.x * g.N * g.H + y.kz;
+#pragma unroll
+        for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+            for (int r = 0; r < RP::RL; ++r) a[base + (long long)RP::out(j, q, r) * g.H] = v[q * RP::RL + r];
+        __syncthreads();   // the exchange reads are done before the buffer is refilled
+    }
+}
+
+
 // ------------------------------------------------------------------ X forward + kick epilogue
 template <typename T, int L, bool GW, class VB>
 __device__ __forceinline__ void kr_fft_x_final_body(const VB &vb, Geo g, const cplx<T> *__restrict__ QV, const cplx<T> *__restrict__ QS, const cplx<T> *__restrict__ fk, cplx<T> *__restrict__ pk, cplx<T> *__restrict__ uk, cplx<T> *__restrict__ puk, double *__restrict__ partKG, const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw, cplx<T> *__restrict__ tape_f, cplx<T> *__restrict__ tape_p, cplx<T> *__restrict__ tape_vp, cplx<T> *__restrict__ tape_pu, cplx<T> *__restrict__ tape_fu, cplx<T> *__restrict__ fcache, cplx<T> *__restrict__ ucache, const XTma *tma) {
@@ -355,7 +524,7 @@ __device__ __forceinline__ void kr_fft_x_final_body(const VB &vb, Geo g, const c
             mbar_init(&xbar, 1);
             mbar_fence_init();
             const int w8 = (int)(sizeof(C) / 8), arr = field ? job : job - g.nf, c0 = (int)(vb.x() * TL) * w8;
-            mbar_arrive_expect_tx(&qbar, (unsigned)(TL * L * sizeof(C)));
+            mbar_arrive_expect_tx(&qbar, (unsigned)(TL * L * sizeof(C)) + planted(bg, 4));
             tma_load_4d(sm, field ? &tma->qv : &tma->qs, c0, 0, arr, (int)vb.z(), &qbar);
             mbar_arrive_expect_tx(&xbar, 2u * (unsigned)(TL * L * sizeof(C)));
             const CUtensorMap *ma = field ? &tma->fk : &tma->uk, *mb = field ? &tma->pk : &tma->puk;
@@ -369,7 +538,10 @@ __device__ __forceinline__ void kr_fft_x_final_body(const VB &vb, Geo g, const c
             // three tiles still in flight so that none can write into shared memory after the
             // block has left, and leave (PSC_ERR_DEVICE when they never land)
             int *err = &const_cast<DevBG *>(bg)->err;
-            if (threadIdx.x == 0) report_err(err, PSC_ERR_TIMEOUT);
+            if (threadIdx.x == 0) {
+                report_err(err, PSC_ERR_TIMEOUT);
+                if (planted(bg, 4)) mbar_complete_tx(&qbar, planted(bg, 4));   // the test hook's bytes
+            }
             const bool landed = mbar_wait_bounded(&qbar, 0, bg->wait_ns) && mbar_wait_bounded(&xbar, 0, bg->wait_ns);
             if (__syncthreads_or(!landed) && threadIdx.x == 0) report_err(err, PSC_ERR_DEVICE);
             return;
@@ -835,7 +1007,7 @@ __device__ __forceinline__ void kr_zpass_gw_body(const VB &vb, Geo g, const cplx
                 const unsigned run = (unsigned)((size_t)TL * H * sizeof(C));
                 fence_proxy_async();   // the staging reads of the previous tile come first
                 // + the test hook's planted bytes (0 in normal runs)
-                mbar_arrive_expect_tx(&zbar, (unsigned)(nf * 3) * run + (unsigned)bg->wait_plant);
+                mbar_arrive_expect_tx(&zbar, (unsigned)(nf * 3) * run + planted(bg, 2));
                 for (int a = 0; a < nf * 3; ++a) {
                     const int fl = USER ? a / 3 : (a >= 3 ? 1 : 0), w = a - 3 * fl;
                     const C *src = (w == 0 ? TA : (w == 1 ? TB : TC)) + (long long)fl * g.modes +
@@ -899,7 +1071,7 @@ __device__ __forceinline__ void kr_zpass_gw_body(const VB &vb, Geo g, const cplx
                     int *err = &const_cast<DevBG *>(bg)->err;
                     if (threadIdx.x == 0) {
                         report_err(err, PSC_ERR_TIMEOUT);
-                        if (bg->wait_plant) mbar_complete_tx(&zbar, (unsigned)bg->wait_plant);
+                        if (planted(bg, 2)) mbar_complete_tx(&zbar, planted(bg, 2));
                     }
                     const bool landed = mbar_wait_bounded(&zbar, phase, bg->wait_ns);
                     if (__syncthreads_or(!landed) && threadIdx.x == 0) report_err(err, PSC_ERR_DEVICE);

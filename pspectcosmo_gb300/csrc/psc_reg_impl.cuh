@@ -12,6 +12,8 @@ template <typename T, int N>
 struct RegLaunch {
     using C = cplx<T>;
     static constexpr int M = N / 2;
+    // the Y forward pass staged by tensor maps (kr_fft_y_pipe): FP32, N = 128 and 256
+    static constexpr bool kYPipe = sizeof(T) == 4 && y_pipe_size(N);
 
     static void gw_adj_tile(int nf, int *tl, int *sh);
     // the scalar adjoint Z pass (adj_z_tile / adj_z_blocks, psc_launch.h)
@@ -39,6 +41,9 @@ struct RegLaunch {
         SETA((kr_ifft_y<T, N, false>), sxy);
         SETA((kr_ifft_y<T, N, true>), 3 * sxy);   // exchange tile + TA and TB staging tiles
         SETA((kr_fft_y<T, N>), sxy);
+        if constexpr (kYPipe) {   // the Y forward staged by tensor maps: two 128-byte aligned buffers
+            SETA((kr_fft_y_pipe<T, N>), 2 * (int)cfg.smem_ys + 128);
+        }
         SETA((kr_fft_x_final<T, N, false>), (int)cfg.smem_xf);
         SETA((kr_fft_x_final<T, N, true>), (int)cfg.smem_xf);
         SETA((kr_zpass<T, M>), sz);
@@ -117,6 +122,9 @@ struct RegLaunch {
         // the X passes' operand tiles by tensor copies where the handle has tensor maps
         const XTma xt = (b.xtma && b.xtma->on) ? *b.xtma : XTma{};
         const size_t sxi = (xt.on && xt.xi) ? cfg.smem_xi : cfg.smem_xy;
+        // the Y forward pass's tiles by tensor copies where the handle has tensor maps for them
+        // (the encoder gives them only to FP32 and the sizes with the tensor-map instantiation)
+        const bool ypl = kYPipe && b.ytma && b.ytma->on;
         mark(0);
         if (g.gwev) {
             if (drift) kr_ifft_x<T, N, true, true><<<gx, txy, sxi, st>>>(g, fk, pk, TA, TB, b.bg, tw, xt);
@@ -145,7 +153,14 @@ struct RegLaunch {
                 al.rs[nj] = g.gstride;
                 al.p[nj++] = QS + (long long)c * g.modes;
             }
-        kr_fft_y<T, N><<<dim3(cfg.nbx, nj, R), txy, cfg.smem_xy, st>>>(g, al, tw);
+        if (!ypl) {
+            kr_fft_y<T, N><<<dim3(cfg.nbx, nj, R), txy, cfg.smem_xy, st>>>(g, al, tw);
+        } else if constexpr (kYPipe) {
+            // persistent and pipelined: two blocks per SM walk the items
+            const long long items = (long long)cfg.nbx * nj * R;
+            const int grid = (int)(items < 2LL * cfg.sms ? items : 2LL * cfg.sms);
+            kr_fft_y_pipe<T, N><<<grid, txy, 2 * cfg.smem_ys + 128, st>>>(g, al, tw, b.bg, *b.ytma, nj, R);
+        }
         mark(4);
         const dim3 gf(cfg.nbx, nj, R);
         if (g.gwev)

@@ -124,10 +124,13 @@ def load_library(path: str | None = None):
                              ctypes.POINTER(ctypes.c_longlong)]
     L.psc_selftest_bulk_wait.argtypes = [ctypes.c_double, ctypes.POINTER(ctypes.c_int)]
     L.psc_test_wait_hook.argtypes = [P, ctypes.c_double, ctypes.c_int]
+    L.psc_test_wait_hook_pass.argtypes = [P, ctypes.c_double, ctypes.c_int, ctypes.c_int]
     I3 = ctypes.POINTER(ctypes.c_int)
     L.psc_autotune.argtypes = [P, ctypes.c_int, I3, I3]
     L.psc_get_shapes.argtypes = [P, I3]
     L.psc_set_shapes.argtypes = [P, I3]
+    L.psc_set_tensor_maps.argtypes = [P, ctypes.c_int]
+    L.psc_get_tensor_maps.argtypes = [P, I3]
     L.psc_batch_autotune.argtypes = [P, ctypes.c_int]
     L.psc_batch_launch_mode.argtypes = [P, ctypes.c_int, I3]
     L.psc_model_count.argtypes = []
@@ -152,9 +155,10 @@ def load_library(path: str | None = None):
                  "psc_set_state_padded", "psc_checkpoint_write", "psc_checkpoint_read",
                  "psc_h5_dataset_shape", "psc_h5_read_f64", "psc_analytic_begin", "psc_analytic_step",
                  "psc_analytic_background", "psc_analytic_modes", "psc_analytic_to_lattice",
-                 "psc_histograms_2d", "psc_slices", "psc_selftest_bulk_wait", "psc_test_wait_hook",
+                 "psc_histograms_2d", "psc_slices", "psc_selftest_bulk_wait", "psc_test_wait_hook", "psc_test_wait_hook_pass",
                  "psc_model_count", "psc_model_find", "psc_model_nterms", "psc_model_eval", "psc_mass_sq_av",
-                 "psc_autotune", "psc_get_shapes", "psc_set_shapes", "psc_batch_autotune", "psc_batch_launch_mode"):
+                 "psc_autotune", "psc_get_shapes", "psc_set_shapes", "psc_batch_autotune", "psc_batch_launch_mode",
+                 "psc_set_tensor_maps", "psc_get_tensor_maps"):
         getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L
@@ -361,6 +365,19 @@ class Lattice:
     def shapes(self, value):
         sh = (ctypes.c_int * 3)(*[int(x) for x in value])
         _check(self._L.psc_set_shapes(self._h, sh), "psc_set_shapes")
+
+    TMAP_X, TMAP_Y = 1, 2
+
+    @property
+    def tensor_maps(self) -> int:
+        """The pass groups that stage their tiles by tensor maps (TMAP_X | TMAP_Y bits)."""
+        m = ctypes.c_int()
+        _check(self._L.psc_get_tensor_maps(self._h, ctypes.byref(m)), "psc_get_tensor_maps")
+        return m.value
+
+    @tensor_maps.setter
+    def tensor_maps(self, mask: int):
+        _check(self._L.psc_set_tensor_maps(self._h, int(mask)), "psc_set_tensor_maps")
 
     # -- adjoint --------------------------------------------------------------
     def adjoint_chi2(self, dt: float, nsteps: int, every: int = 0, fields: bool = True) -> dict:
