@@ -38,7 +38,7 @@ extern "C" {
 #endif
 
 #define PSC_OK 0
-#define PSC_ERR_CONFIG (-1)     /* unsupported parameter (N not a power of two in [8,1024], ...) */
+#define PSC_ERR_CONFIG (-1)     /* unsupported parameter (N outside the sizes below, ...) */
 #define PSC_ERR_ARG (-2)        /* null pointer / bad argument */
 #define PSC_ERR_CUDA (-3)       /* a CUDA runtime call failed */
 #define PSC_ERR_NONFINITE (-4)  /* the on-device finite check tripped (NaN/Inf in the background) */
@@ -65,7 +65,9 @@ extern "C" {
  * run-time values. Field names follow parameters.h.
  */
 typedef struct psc_params {
-    int N;                  /* parameters.h:22   points per lattice edge: power of two, 8..1024 */
+    int N;                  /* parameters.h:22   points per lattice edge: a power of two in 8..1024 (the
+                               register FFT engine from 32 on), or an even size in 8..512 whose prime
+                               factors are 2, 3, 5, 7 (e.g. 24, 40, 56, 96; the generic engine) */
     int nflds;              /* parameters.h:20   number of scalar fields: 1 .. PSC_MAX_FIELDS (GWs with more
                                than two fields: N <= 512) */
     int vv;                 /* parameters.h:10   integrator: 2 (velocity Verlet), 4, 6, 8, 10 (Yoshida) */
@@ -81,7 +83,7 @@ typedef struct psc_params {
     int seed;               /* parameters.h:65   Park-Miller seed (rand_uniform, initialize.cpp:13) */
     int N_pad;              /* parameters.h:13,23 PAD_FLAG / N_pad: 0 = off, else the padded grid of the
                                dealiased spectral step evolve_VV_k_pad (power of two, N < N_pad <= 1024,
-                               spectral = 1, no GWs) */
+                               N a power of two, spectral = 1, no GWs) */
     double kIR;             /* parameters.h:27   smallest lattice wavenumber (program units) */
     double a0;              /* parameters.h:29   initial scale factor */
     double MPl;             /* parameters.h:121  Planck mass */

@@ -141,6 +141,23 @@ CONFIGS: dict[str, tuple[str, dict[str, str]]] = {
         "initfield[]": "{0.193 * MPl, 0., 0., 0.}",
         "initderivs[]": "{-0.142e-6 * MPl * MPl, 0., 0., 0.}",
     }),
+    # lattice sizes that are not powers of two (FFTW takes any N; here the generic engine's
+    # mixed radices 3, 5, 7)
+    "spec1_n24_vv4": ("phi2", {"N": "24", "VV": "4"}),
+    "spec2_n20_vv2": ("phi2chi2", {
+        "N": "20", "VV": "2", "nflds": "2", "kIR": "1",
+        "initfield[]": "{0.193 * MPl, 0.}",
+        "initderivs[]": "{-0.142e-6 * MPl * MPl, 0.}",
+    }),
+    "gw2_n24_vv4": ("phi2chi2", {
+        "N": "24", "VV": "4", "nflds": "2", "kIR": "1",
+        "SPECTRAL_FLAG": "false", "WITH_GW": "true",
+        "initfield[]": "{0.193 * MPl, 0.}",
+        "initderivs[]": "{-0.142e-6 * MPl * MPl, 0.}",
+    }),
+    "gw1_n28_vv2": ("phi2", {
+        "N": "28", "VV": "2", "SPECTRAL_FLAG": "false", "WITH_GW": "true",
+    }),
     # real-space pseudo-spectral path with gravitational waves (evolve_VV)
     "gw2_n16_vv4": ("phi2chi2", {
         "N": "16", "VV": "4", "nflds": "2", "kIR": "1",

@@ -1,8 +1,10 @@
 /*
- * fft64 — FP64 power-of-two FFTs for the CPU oracle (test infrastructure only).
- * Conventions: see fft64.h. Algorithm: iterative radix-2 decimation-in-time
- * Cooley-Tukey on a contiguous copy of each line, twiddles e^{-2 pi i k/n}
- * from libm cos/sin cached per length; real transforms of length n use the
+ * fft64 — FP64 FFTs for the CPU oracle (test infrastructure only).
+ * Conventions: see fft64.h. Algorithm: for power-of-two lengths, iterative
+ * radix-2 decimation-in-time Cooley-Tukey on a contiguous copy of each line;
+ * for other lengths, recursive mixed-radix decimation in time by the smallest
+ * prime factor (a prime length is a direct DFT). Twiddles e^{-2 pi i k/n} from
+ * libm cos/sin, cached per length; real transforms of (even) length n use the
  * standard half-length packing (x[2m] + i x[2m+1]) with a split step.
  */
 #include "fft64.h"
@@ -18,6 +20,8 @@
 static const double PI = 3.14159265358979323846264338327950288;
 
 static double *g_tw[32];      /* g_tw[l]: n = 2^l, n/2 complex e^{-2 pi i k/n} */
+#define NP2_MAX 8192
+static double *g_twn[NP2_MAX + 1]; /* other lengths n: n complex e^{-2 pi i k/n} */
 static pthread_mutex_t g_tw_lock = PTHREAD_MUTEX_INITIALIZER;
 static int g_threads = 0;
 
@@ -27,7 +31,31 @@ static int ilog2(int n) {
     return l;
 }
 
+static int is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+static const double *twiddles_np2(int n) {
+    double *t = __atomic_load_n(&g_twn[n], __ATOMIC_ACQUIRE);
+    if (t) return t;
+    pthread_mutex_lock(&g_tw_lock);
+    t = g_twn[n];
+    if (!t) {
+        t = (double *)malloc(sizeof(double) * 2 * n);
+        for (int k = 0; k < n; k++) {
+            double ang = 2.0 * PI * (double)k / (double)n;
+            t[2 * k] = cos(ang);
+            t[2 * k + 1] = -sin(ang);
+        }
+        __atomic_store_n(&g_twn[n], t, __ATOMIC_RELEASE);
+    }
+    pthread_mutex_unlock(&g_tw_lock);
+    return t;
+}
+
 static const double *twiddles(int n) {
+    if (!is_pow2(n)) {
+        if (n > NP2_MAX) abort();
+        return twiddles_np2(n);
+    }
     int l = ilog2(n);
     double *t = __atomic_load_n(&g_tw[l], __ATOMIC_ACQUIRE);
     if (t) return t;
@@ -57,9 +85,59 @@ int fft64_get_threads(void) {
 #endif
 }
 
+static int smallest_factor(int n) {
+    for (int p = 2; p * p <= n; p++)
+        if (n % p == 0) return p;
+    return n;
+}
+
+/* y[0..n) = DFT of the n complex values x[0], x[xs], ... (any n): p = smallest prime
+ * factor of n; the p sub-transforms of length m = n/p of the subsequences x[r xs p^0 ...]
+ * go to y[r m ..], then Y[k + q m] = sum_r w^{r (k + q m)} Y_r[k]. tw: the table of length
+ * n0 (a multiple of n), used at stride n0/n; sign -1 forward, +1 backward. */
+static void dft_mixed(const double *x, ptrdiff_t xs, double *y, int n, int sign, const double *tw, int n0) {
+    if (n == 1) {
+        y[0] = x[0];
+        y[1] = x[1];
+        return;
+    }
+    const int p = smallest_factor(n), m = n / p, ts = n0 / n;
+    double *sub = (double *)malloc(sizeof(double) * 2 * n);
+    if (m == 1) {
+        for (int r = 0; r < p; r++) {
+            sub[2 * r] = x[2 * r * xs];
+            sub[2 * r + 1] = x[2 * r * xs + 1];
+        }
+    } else {
+        for (int r = 0; r < p; r++) dft_mixed(x + 2 * r * xs, xs * p, sub + 2 * r * m, m, sign, tw, n0);
+    }
+    for (int k = 0; k < m; k++)
+        for (int q = 0; q < p; q++) {
+            const int kk = k + q * m;
+            double ar = 0.0, ai = 0.0;
+            for (int r = 0; r < p; r++) {
+                const int e = (int)(((long)r * kk) % n) * ts;
+                const double wr = tw[2 * e], wi = (sign < 0 ? 1.0 : -1.0) * tw[2 * e + 1];
+                const double vr = sub[2 * (r * m + k)], vi = sub[2 * (r * m + k) + 1];
+                ar += vr * wr - vi * wi;
+                ai += vr * wi + vi * wr;
+            }
+            y[2 * kk] = ar;
+            y[2 * kk + 1] = ai;
+        }
+    free(sub);
+}
+
 /* contiguous in-place transform of n complex values */
 static void fft_contig(double *x, int n, int sign) {
     if (n <= 1) return;
+    if (!is_pow2(n)) {
+        double *in = (double *)malloc(sizeof(double) * 2 * n);
+        memcpy(in, x, sizeof(double) * 2 * n);
+        dft_mixed(in, 1, x, n, sign, twiddles(n), n);
+        free(in);
+        return;
+    }
     /* bit reversal */
     for (int i = 1, j = 0; i < n; i++) {
         int bit = n >> 1;

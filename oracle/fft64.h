@@ -13,8 +13,9 @@
  * parts of X[0] and X[N/2]; a 3-D real transform of a row-major [n0][n1][n2]
  * array produces [n0][n1][n2/2+1] with the last index fastest.
  *
- * Lengths must be powers of two (>= 2). Multi-line transforms run on all host
- * threads with OpenMP when it is enabled at compile time.
+ * Any length >= 2 (power-of-two lengths by radix-2, others mixed-radix up to
+ * 8192); real transforms need an even length. Multi-line transforms run on all
+ * host threads with OpenMP when it is enabled at compile time.
  */
 #ifndef PSC_ORACLE_FFT64_H
 #define PSC_ORACLE_FFT64_H

@@ -19,11 +19,10 @@ struct psc_shim_plan {
     void *in, *out;
 };
 
-static int is_pow2(int n) { return n >= 2 && (n & (n - 1)) == 0; }
-
+/* fft64 takes any length up to 8192; its real transforms need an even length */
 static void check_len(int n) {
-    if (!is_pow2(n)) {
-        fprintf(stderr, "fftw shim: length %d is not a power of two >= 2\n", n);
+    if (n < 2 || n % 2 != 0 || n > 8192) {
+        fprintf(stderr, "fftw shim: length %d is not an even length in [2, 8192]\n", n);
         exit(2);
     }
 }

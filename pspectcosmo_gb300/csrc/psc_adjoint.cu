@@ -501,7 +501,7 @@ int check(psc_handle *h, int obs) {
     if (h->R != 1) return fail(PSC_ERR_CONFIG, "the adjoint works on single-lattice handles");
     if (h->padded) return fail(PSC_ERR_CONFIG, "the adjoint differentiates the unpadded step (N_pad = 0)");
     h->force_valid = false;   // the reverse sweep rewrites the stage buffers
-    if (h->cfg.g.N < 32) return fail(PSC_ERR_CONFIG, "the adjoint needs N >= 32");
+    if (!h->cfg.g.reg) return fail(PSC_ERR_CONFIG, "the adjoint needs the register engine (a power-of-two N >= 32)");
     if (h->cfg.g.mask)
         return fail(PSC_ERR_CONFIG, "the adjoint differentiates the unmasked step (spectral = 0 or simulate_inflation = 0)");
     if (p.expansion != 2) return fail(PSC_ERR_CONFIG, "the adjoint needs self-consistent expansion (expansion = 2)");

@@ -79,6 +79,13 @@ const double kW10[31] = {
     0.50180317558723140279,  0.0036303931544595926879, -0.48159895600253002870};
 
 bool pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+// n has no prime factor above 7 (the generic engine's radices 2, 3, 5, 7)
+bool smooth7(int n) {
+    if (n < 1) return false;
+    for (int p : {2, 3, 5, 7})
+        while (n % p == 0) n /= p;
+    return n == 1;
+}
 
 constexpr double kPi = 3.14159265358979323846;
 
@@ -116,7 +123,11 @@ int dalloc(psc_handle *h, void **out, size_t bytes) {
 
 int validate(const psc_params *p) {
     if (!p) return fail(PSC_ERR_ARG, "null parameters");
-    if (!pow2(p->N) || p->N < 8 || p->N > 1024) return fail(PSC_ERR_CONFIG, "N must be a power of two in [8, 1024]");
+    // powers of two up to 1024 (the register engine from 32 on); other even sizes up to 512 with
+    // prime factors 2, 3, 5, 7 on the generic engine (FFTW, which the reference uses, takes any N)
+    if (p->N < 8 || !(pow2(p->N) ? p->N <= 1024 : (p->N % 2 == 0 && smooth7(p->N) && p->N <= 512)))
+        return fail(PSC_ERR_CONFIG,
+                    "N must be a power of two in [8, 1024] or an even size in [8, 512] with prime factors 2, 3, 5, 7");
     if (p->nflds < 1 || p->nflds > PSC_MAX_FIELDS) return fail(PSC_ERR_CONFIG, "nflds must be 1 .. PSC_MAX_FIELDS (4)");
     if (p->model == PSC_MODEL_PHI2 && p->nflds != 1) return fail(PSC_ERR_CONFIG, "the phi^2 model has one field");
     if (p->model == PSC_MODEL_PHI2CHI2 && p->nflds != 2) return fail(PSC_ERR_CONFIG, "the phi^2 chi^2 model has two fields");
@@ -130,8 +141,9 @@ int validate(const psc_params *p) {
     if (p->N_pad != 0) {
         if (!p->spectral || p->with_gw)
             return fail(PSC_ERR_CONFIG, "the padded step (N_pad) is the spectral step without GWs, as in the reference");
-        if (!pow2(p->N_pad) || p->N_pad <= p->N || p->N_pad > 1024 || p->N_pad < 32)
-            return fail(PSC_ERR_CONFIG, "N_pad must be a power of two with N < N_pad <= 1024 and N_pad >= 32");
+        if (!pow2(p->N_pad) || !pow2(p->N) || p->N_pad <= p->N || p->N_pad > 1024 || p->N_pad < 32)
+            return fail(PSC_ERR_CONFIG,
+                        "the padded step needs power-of-two N and N_pad with N < N_pad <= 1024 and N_pad >= 32");
     }
     if (p->expansion < 0 || p->expansion > 2) return fail(PSC_ERR_CONFIG, "expansion must be 0, 1 or 2");
     if (!(p->kIR > 0) || !(p->MPl > 0) || !(p->m_in_MPl > 0) || !(p->a0 > 0))

@@ -237,6 +237,61 @@ __device__ __forceinline__ void dft(C (&v)[R]) {
     }
 }
 
+// cos/sin(2 pi k / R) for the odd radices R = 3, 5, 7 of the generic engine (lattice sizes
+// that are not powers of two): decimal expansions of the algebraic values, k = 0 .. R/2.
+__host__ __device__ constexpr double cos_odd(int R, int k) {
+    return R == 3 ? (k == 0 ? 1.0 : -0.5)
+         : R == 5 ? (k == 0 ? 1.0 : k == 1 ? 0.30901699437494742410 : -0.80901699437494742410)
+                  : (k == 0 ? 1.0 : k == 1 ? 0.62348980185873353053 : k == 2 ? -0.22252093395631440429
+                                                                               : -0.90096886790241912624);
+}
+__host__ __device__ constexpr double sin_odd(int R, int k) {
+    return R == 3 ? (k == 0 ? 0.0 : 0.86602540378443864676)
+         : R == 5 ? (k == 0 ? 0.0 : k == 1 ? 0.95105651629515357212 : 0.58778525229247312917)
+                  : (k == 0 ? 0.0 : k == 1 ? 0.78183148246802980871 : k == 2 ? 0.97492791218182360702
+                                                                               : 0.43388373911755812048);
+}
+
+// In-register R-point DFT for odd prime R (3, 5, 7), direction DIR: the symmetric form
+// Y[k] = v0 + sum_{m=1}^{(R-1)/2} [(v_m + v_{R-m}) cos(2 pi k m / R)
+//        + DIR i (v_m - v_{R-m}) sin(2 pi k m / R)], with compile-time constants.
+template <int R, int DIR, typename C>
+__device__ __forceinline__ void dft_odd(C (&v)[R]) {
+    using T = decltype(v[0].x);
+    constexpr int H2 = R / 2;
+    C s[H2 + 1], d[H2 + 1];
+#pragma unroll
+    for (int m = 1; m <= H2; ++m) {
+        s[m] = mk<T>(v[m].x + v[R - m].x, v[m].y + v[R - m].y);
+        d[m] = mk<T>(v[m].x - v[R - m].x, v[m].y - v[R - m].y);
+    }
+    C y[R];
+    y[0] = v[0];
+#pragma unroll
+    for (int m = 1; m <= H2; ++m) {
+        y[0].x += s[m].x;
+        y[0].y += s[m].y;
+    }
+#pragma unroll
+    for (int k = 1; k <= H2; ++k) {
+        T ar = v[0].x, ai = v[0].y, br = T(0), bi = T(0);
+#pragma unroll
+        for (int m = 1; m <= H2; ++m) {
+            const int q = (k * m) % R, qq = q <= H2 ? q : R - q;
+            const T c = (T)cos_odd(R, qq), sn = (T)(q <= H2 ? sin_odd(R, qq) : -sin_odd(R, qq));
+            ar += c * s[m].x;
+            ai += c * s[m].y;
+            br += sn * d[m].x;
+            bi += sn * d[m].y;
+        }
+        // DIR i (br + i bi) = DIR (-bi + i br)
+        y[k] = mk<T>(ar - T(DIR) * bi, ai + T(DIR) * br);
+        y[R - k] = mk<T>(ar + T(DIR) * bi, ai - T(DIR) * br);
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k) v[k] = y[k];
+}
+
 // One Stockham autosort stage (radix R, span Ns) over a tile of TL lines of
 // length L held in shared memory as s[n * LD + t] (element n of line t).
 // Twiddles come from tw[q] = e^{-2 pi i q / Ntw}, the table of the lattice
@@ -251,7 +306,7 @@ __device__ __forceinline__ void stockham_stage(const C *__restrict__ src, C *__r
     for (int b = threadIdx.x; b < nb; b += blockDim.x) {
         const int t = b & (TL - 1);
         const int j = b >> tl_shift;
-        const int jm = j & (Ns - 1);
+        const int jm = j % Ns;
         C v[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) v[r] = src[(j + r * LR) * LD + t];
@@ -263,35 +318,48 @@ __device__ __forceinline__ void stockham_stage(const C *__restrict__ src, C *__r
                 v[r] = cmul(v[r], w);
             }
         }
-        dft<R, DIR>(v);
+        if constexpr (R == 3 || R == 5 || R == 7) dft_odd<R, DIR>(v);
+        else dft<R, DIR>(v);
         const int idxD = (j - jm) * R + jm;
 #pragma unroll
         for (int r = 0; r < R; ++r) dst[(idxD + r * Ns) * LD + t] = v[r];
     }
 }
 
-// Transform all TL lines of a tile (length L, power of two >= 2). Ping-pongs
-// between a and b; returns the buffer holding the result. Begins and ends
-// with a block barrier.
+// Transform all TL lines of a tile (length L >= 2 with prime factors 2, 3, 5, 7: radix 16,
+// 8, 4, 2 while L's power of two lasts, then 3, 5, 7). Ping-pongs between a and b; returns
+// the buffer holding the result. Begins and ends with a block barrier.
 template <typename C, int DIR>
 __device__ C *fft_tile(C *a, C *b, int L, int tl_shift, int LD, const C *__restrict__ tw, int Ntw) {
     C *src = a, *dst = b;
     int Ns = 1, rem = L;
     while (rem > 1) {
         __syncthreads();
-        if (rem >= 16) {
+        int R;
+        if (rem % 16 == 0) {
             stockham_stage<C, 16, DIR>(src, dst, L, Ns, tl_shift, LD, tw, Ntw);
-            Ns *= 16; rem >>= 4;
-        } else if (rem == 8) {
+            R = 16;
+        } else if (rem % 8 == 0) {
             stockham_stage<C, 8, DIR>(src, dst, L, Ns, tl_shift, LD, tw, Ntw);
-            Ns *= 8; rem >>= 3;
-        } else if (rem == 4) {
+            R = 8;
+        } else if (rem % 4 == 0) {
             stockham_stage<C, 4, DIR>(src, dst, L, Ns, tl_shift, LD, tw, Ntw);
-            Ns *= 4; rem >>= 2;
-        } else {
+            R = 4;
+        } else if (rem % 2 == 0) {
             stockham_stage<C, 2, DIR>(src, dst, L, Ns, tl_shift, LD, tw, Ntw);
-            Ns *= 2; rem >>= 1;
+            R = 2;
+        } else if (rem % 3 == 0) {
+            stockham_stage<C, 3, DIR>(src, dst, L, Ns, tl_shift, LD, tw, Ntw);
+            R = 3;
+        } else if (rem % 5 == 0) {
+            stockham_stage<C, 5, DIR>(src, dst, L, Ns, tl_shift, LD, tw, Ntw);
+            R = 5;
+        } else {
+            stockham_stage<C, 7, DIR>(src, dst, L, Ns, tl_shift, LD, tw, Ntw);
+            R = 7;
         }
+        Ns *= R;
+        rem /= R;
         C *x = src; src = dst; dst = x;
     }
     __syncthreads();

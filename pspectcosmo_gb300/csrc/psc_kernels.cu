@@ -846,7 +846,9 @@ void plan(const psc_params &p, int R, LaunchCfg *cfg, const TileChoice *tc) {
     g.lines_z = g.N * g.N;
     g.modes = (long long)g.N * g.N * g.H;
     g.sites = (long long)g.N * g.N * g.N;
-    g.reg = g.N >= 32 ? 1 : 0;
+    // the register engine: power-of-two lines from 32 on; the generic engine takes the rest
+    // (N = 8, 16 and the sizes with factors 3, 5, 7)
+    g.reg = (g.N >= 32 && (g.N & (g.N - 1)) == 0) ? 1 : 0;
     g.fstride = (long long)g.nf * g.modes;
     g.gstride = g.gw ? 6LL * g.modes : 0;
     const int csize = p.precision == 32 ? 8 : 16;
@@ -909,9 +911,11 @@ void plan(const psc_params &p, int R, LaunchCfg *cfg, const TileChoice *tc) {
         g.pv_stride = kMaxTerms * cfg->nbz;
         return;
     }
-    // generic engine: a tile of TL lines x N elements, two ping-pong buffers of
-    // <= 32 KiB each
-    int tl = (32768 / csize) / g.N;
+    // generic engine: a tile of TL lines x N elements (TL a power of two: the kernels take
+    // a line's index and element from the low and high bits of a thread index), two
+    // ping-pong buffers of <= 32 KiB each
+    int tl = 1;
+    while (2 * tl <= (32768 / csize) / g.N) tl *= 2;
     if (tl < 4) tl = 4;
     if (tl > 256) tl = 256;
     while (tl > 1 && tl / 2 >= g.lines_x) tl /= 2;

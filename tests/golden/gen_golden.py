@@ -47,6 +47,10 @@ RUNS = {
     "gw4_n16_vv2": ("gw4_n16_vv2", 10, 0.005, 5, True),
     "pad3_n16_vv4": ("pad3_n16_vv4", 20, 0.005, 10, True),
     "gw4_n32_vv2": ("gw4_n32_vv2", 10, 0.005, 5, False),
+    "spec1_n24_vv4": ("spec1_n24_vv4", 20, 0.002, 10, True),
+    "spec2_n20_vv2": ("spec2_n20_vv2", 20, 0.005, 10, True),
+    "gw2_n24_vv4": ("gw2_n24_vv4", 10, 0.005, 5, True),
+    "gw1_n28_vv2": ("gw1_n28_vv2", 10, 0.002, 5, False),
 }
 
 

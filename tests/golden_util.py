@@ -12,7 +12,8 @@ from pspectcosmo_gb300.params import Params
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 ALL_RUNS = ["spec1_n16", "spec1_n16_vv6", "spec1_n16_vv8", "spec1_n16_vv10", "spec1_n32_vv4", "spec1_n64_dt1e-4",
-            "spec1_n64_dt2e-3", "spec2_n16_vv4", "spec2_n32_vv2", "gw2_n16_vv4", "gw1_n16_vv2", "specgw2_n16_vv4"]
+            "spec1_n64_dt2e-3", "spec2_n16_vv4", "spec2_n32_vv2", "gw2_n16_vv4", "gw1_n16_vv2", "specgw2_n16_vv4",
+            "spec1_n24_vv4", "spec2_n20_vv2", "gw2_n24_vv4", "gw1_n28_vv2"]
 
 
 def load(run: str):

@@ -1,4 +1,5 @@
-"""The oracle's FP64 FFT (the FFTW stand-in) against numpy.fft and a direct DFT."""
+"""The oracle's FP64 FFT (the FFTW stand-in) against numpy.fft and a direct DFT: power-of-two
+lengths (radix 2) and the mixed-radix lengths of other lattice sizes (factors 2, 3, 5, 7)."""
 import ctypes
 
 import numpy as np
@@ -19,7 +20,7 @@ def _p(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
 
-@pytest.mark.parametrize("n", [2, 4, 8, 16, 64, 256, 1024])
+@pytest.mark.parametrize("n", [2, 4, 8, 16, 64, 256, 1024, 3, 6, 12, 20, 24, 28, 30, 42, 49, 96, 210, 480])
 def test_line_vs_direct_dft(fft, n):
     rng = np.random.default_rng(n)
     x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
@@ -33,7 +34,8 @@ def test_line_vs_direct_dft(fft, n):
     assert np.allclose(z, np.fft.ifft(x) * n, rtol=0, atol=1e-12 * np.abs(x).sum())
 
 
-@pytest.mark.parametrize("shape", [(8, 8, 8), (16, 16, 16), (32, 32, 32), (8, 16, 32)])
+@pytest.mark.parametrize("shape", [(8, 8, 8), (16, 16, 16), (32, 32, 32), (8, 16, 32), (12, 12, 12), (20, 20, 20),
+                                   (24, 24, 24), (28, 28, 28), (30, 12, 42)])
 def test_3d_real_transforms_match_numpy(fft, shape):
     rng = np.random.default_rng(sum(shape))
     x = rng.standard_normal(shape)

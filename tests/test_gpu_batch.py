@@ -129,3 +129,29 @@ def test_one_launch_per_pass_equals_individual_lattices(precision):
         b = per.get_state(idx)
         assert np.array_equal(states[idx]["f_k"], b["f_k"]) and states[idx]["a"] == b["a"], idx
     per.close()
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_mixed_radix_group_equals_individual_lattices(precision):
+    """A batch with a group at a size that is not a power of two (24^3: the generic engine's
+    radix 3) beside a register-engine group (32^3), GWs on: every realization equals the
+    same lattice advanced alone, bit for bit."""
+    from pspectcosmo_gb300 import Ensemble, Lattice
+    from pspectcosmo_gb300.params import Params
+
+    ps = [Params.preheating(N=N, vv=4, spectral=0, with_gw=1, seed=1 + i, precision=precision)
+          for i, N in enumerate((24, 24, 32))]
+    ens = Ensemble(ps)
+    assert ens.groups == 2
+    ens.initialize()
+    ens.evolve(0.005, 3)
+    for idx, p in enumerate(ps):
+        lat = Lattice(p)
+        lat.initialize()
+        lat.evolve(0.005, 3)
+        a, b = ens.get_state(idx), lat.get_state()
+        for k in ("f_k", "pi_k", "u_k", "pi_u_k"):
+            assert np.array_equal(a[k], b[k]), (idx, k)
+        assert a["a"] == b["a"] and a["ad"] == b["ad"] and a["add"] == b["add"], idx
+        lat.close()
+    ens.close()

@@ -18,6 +18,8 @@ CASES = {
     "single_field_rayleigh_n16": ("default", dict(N=16, simulate_inflation=0, spectral=0)),
     "two_field_gw_fixed_amplitude": ("preheating", dict(N=32, spectral=0, with_gw=1)),
     "two_field_gw_rayleigh_n64": ("preheating", dict(N=64, spectral=0, with_gw=1, simulate_inflation=0, seed=7)),
+    # a lattice size that is not a power of two (24 = 8 x 3)
+    "two_field_gw_fixed_amplitude_n24": ("preheating", dict(N=24, spectral=0, with_gw=1)),
 }
 
 

@@ -23,7 +23,9 @@ from golden_util import load, output_rows, params_for, rel
 pytestmark = pytest.mark.gpu
 
 RUNS = ["spec1_n16", "spec1_n16_vv6", "spec1_n16_vv8", "spec1_n16_vv10", "spec1_n32_vv4", "spec1_n64_dt1e-4",
-        "spec2_n16_vv4", "spec2_n32_vv2", "gw1_n16_vv2", "gw2_n16_vv4", "specgw2_n16_vv4"]
+        "spec2_n16_vv4", "spec2_n32_vv2", "gw1_n16_vv2", "gw2_n16_vv4", "specgw2_n16_vv4",
+        # sizes that are not powers of two: the generic engine's mixed radices 3, 5, 7
+        "spec1_n24_vv4", "spec2_n20_vv2", "gw2_n24_vv4", "gw1_n28_vv2"]
 
 FP32_FIELD_TOL = 2e-4
 FP32_SPEC_TOL = 1e-4
@@ -33,6 +35,11 @@ FP32_BG_TOL = 1e-6
 FP32_ADD_TOL = 1e-4
 REALSPACE_SPEC_TOL = 1e-7
 REALSPACE_NK_TOL = 1e-6
+# n_k on the spectral path at the mixed-radix sizes: its bins sum |pi_k + (a'/a) f_k|^2, a
+# difference that cancels to ~1e-7 of its terms for these super-horizon modes, so a change of
+# summation order in the transforms (radix 8 then 3 on the device, 2 then 3 in the oracle) shows
+# at ~2e-10 relative (measured 1.7e-10 at 24^3 after 20 steps) while the states agree to 1e-10
+SPECTRAL_NK_TOL_MIXED = 1e-9
 
 
 def _pair(oracle_mod, run, precision):
@@ -88,7 +95,7 @@ def test_fp64_matches_oracle(oracle_mod, run):
     o.step(meta["dt"], meta["nsteps"])
     _compare_state(lat, o, p, 1e-10, 1e-12)
     if p.spectral:
-        _compare_outputs(lat, o, p, 1e-10)
+        _compare_outputs(lat, o, p, 1e-10, 1e-10 if p.N & (p.N - 1) == 0 else SPECTRAL_NK_TOL_MIXED)
     else:
         _compare_outputs(lat, o, p, REALSPACE_SPEC_TOL, REALSPACE_NK_TOL)
     assert abs(lat.t - meta["nsteps"] * meta["dt"]) < 1e-12
