@@ -82,8 +82,8 @@ typedef struct psc_params {
     int model;              /* model.h: PSC_MODEL_PHI2, PSC_MODEL_PHI2CHI2 or PSC_MODEL_USER + i */
     int seed;               /* parameters.h:65   Park-Miller seed (rand_uniform, initialize.cpp:13) */
     int N_pad;              /* parameters.h:13,23 PAD_FLAG / N_pad: 0 = off, else the padded grid of the
-                               dealiased spectral step evolve_VV_k_pad (power of two, N < N_pad <= 1024,
-                               N a power of two, spectral = 1, no GWs) */
+                               dealiased spectral step evolve_VV_k_pad (N < N_pad, a size N may take,
+                               spectral = 1, no GWs) */
     double kIR;             /* parameters.h:27   smallest lattice wavenumber (program units) */
     double a0;              /* parameters.h:29   initial scale factor */
     double MPl;             /* parameters.h:121  Planck mass */

@@ -122,6 +122,14 @@ CONFIGS: dict[str, tuple[str, dict[str, str]]] = {
         "initfield[]": "{0.193 * MPl, 0., 0.01 * MPl}",
         "initderivs[]": "{-0.142e-6 * MPl * MPl, 0., 0.}",
     }),
+    # the padded step with padded grids that are not powers of two (ratio 1.5), and both sizes
+    # mixed-radix
+    "pad1_n16_np24": ("phi2", {"N": "16", "PAD_FLAG": "true", "N_pad": "24"}),
+    "pad2_n20_vv4_np30": ("phi2chi2", {
+        "N": "20", "VV": "4", "nflds": "2", "kIR": "1", "PAD_FLAG": "true", "N_pad": "30",
+        "initfield[]": "{0.193 * MPl, 0.}",
+        "initderivs[]": "{-0.142e-6 * MPl * MPl, 0.}",
+    }),
     # three fields on the padded (dealiased) spectral step
     "pad3_n16_vv4": ("three_field", {
         "N": "16", "VV": "4", "nflds": "3", "kIR": "1", "PAD_FLAG": "true", "N_pad": "32",

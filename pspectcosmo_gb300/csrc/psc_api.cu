@@ -141,9 +141,11 @@ int validate(const psc_params *p) {
     if (p->N_pad != 0) {
         if (!p->spectral || p->with_gw)
             return fail(PSC_ERR_CONFIG, "the padded step (N_pad) is the spectral step without GWs, as in the reference");
-        if (!pow2(p->N_pad) || !pow2(p->N) || p->N_pad <= p->N || p->N_pad > 1024 || p->N_pad < 32)
-            return fail(PSC_ERR_CONFIG,
-                        "the padded step needs power-of-two N and N_pad with N < N_pad <= 1024 and N_pad >= 32");
+        // N_pad: a size psc_create takes for N, above N (the register engine at N_pad when it is a
+        // power of two >= 32, the generic engine otherwise)
+        if (p->N_pad <= p->N ||
+            !(pow2(p->N_pad) ? p->N_pad <= 1024 : (p->N_pad % 2 == 0 && smooth7(p->N_pad) && p->N_pad <= 512)))
+            return fail(PSC_ERR_CONFIG, "N_pad must be above N and a lattice size psc_create takes for N");
     }
     if (p->expansion < 0 || p->expansion > 2) return fail(PSC_ERR_CONFIG, "expansion must be 0, 1 or 2");
     if (!(p->kIR > 0) || !(p->MPl > 0) || !(p->m_in_MPl > 0) || !(p->a0 > 0))

@@ -167,6 +167,29 @@ __global__ void __launch_bounds__(256) k_fft_y(Geo g, ArrList arrs, const cplx<T
     ypass_tile<T, -1>(g, a, a, false, T(0), b0, b1, tw);
 }
 
+// X-axis forward pass of the arrays of a list, no epilogue (the padded step's r2c at N_pad)
+template <typename T>
+__global__ void __launch_bounds__(256) k_fft_x_plain(Geo g, ArrList arrs, const cplx<T> *__restrict__ tw) {
+    using C = cplx<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int sh = g.tlx_shift, TL = 1 << sh, N = g.N;
+    C *b0 = reinterpret_cast<C *>(smem_raw);
+    C *b1 = b0 + TL * N;
+    C *a = reinterpret_cast<C *>(arrs.p[blockIdx.y]) + (long long)blockIdx.z * arrs.rs[blockIdx.y];
+    const int line0 = blockIdx.x * TL;
+    const long long stride = g.lines_x;
+    const int total = TL * N;
+    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+        const int t = idx & (TL - 1), n = idx >> sh, line = line0 + t;
+        b0[idx] = (line < g.lines_x) ? a[n * stride + line] : mk<T>(0, 0);
+    }
+    const C *r = fft_tile<C, -1>(b0, b1, N, sh, TL, tw, N);
+    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+        const int t = idx & (TL - 1), n = idx >> sh, line = line0 + t;
+        if (line < g.lines_x) a[n * stride + line] = r[idx];
+    }
+}
+
 // ------------------------------------------------------------------ fused Z pass
 // Shared memory: b0, b1 (H rows x ldz) and nslot real-line slots (M rows x ldz,
 // a complex element holding the two real sites 2m and 2m+1).
@@ -959,6 +982,7 @@ static cudaError_t configure_t(const LaunchCfg &cfg) {
     SETA((k_fft_x_final<T, false>), sxy);
     SETA((k_fft_x_final<T, true>), sxy);
     SETA((k_z_c2r_real<T>), sz);
+    SETA((k_fft_x_plain<T>), sxy);
 #undef SETA
     return cudaSuccess;
 }
@@ -1021,6 +1045,34 @@ static cudaError_t launch_stage_t(const LaunchCfg &cfg, const Buffers &b, int dr
         mark(6);
     }
     return cudaGetLastError();
+}
+
+// The transforms of the padded step on the generic engine (N_pad not a power of two, or below
+// 32), as RegLaunch::pad_passes: c2r of the padded spectra b.fk with the lattice's 1/N^3 (the
+// background record's inv_n3), V'(f_pad) and the <V> partials over the padded sites, r2c into
+// b.QV.
+template <typename T>
+static cudaError_t pad_passes_t(const LaunchCfg &cfg, const Buffers &b, cudaStream_t st) {
+    using C = cplx<T>;
+    const Geo &g = cfg.g;
+    const C *tw = reinterpret_cast<const C *>(b.tw);
+    C *fk = (C *)b.fk, *TA = (C *)b.TA, *QV = (C *)b.QV;
+    const dim3 gx(cfg.nbx, g.nf);
+    k_ifft_x<T, false, false><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, fk, nullptr, TA, nullptr, b.bg, tw);
+    k_ifft_y<T, false><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, TA, nullptr, nullptr, b.bg, tw);
+    k_zpass<T, false><<<cfg.nbz, cfg.thr_z, cfg.smem_z, st>>>(g, TA, nullptr, nullptr, QV, nullptr, b.partV, b.bg, tw);
+    ArrList al{};
+    for (int f = 0; f < g.nf; ++f) {
+        al.rs[f] = g.fstride;
+        al.p[f] = QV + (long long)f * g.modes;
+    }
+    k_fft_y<T><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, al, tw);
+    k_fft_x_plain<T><<<gx, cfg.thr_xy, cfg.smem_xy, st>>>(g, al, tw);
+    return cudaGetLastError();
+}
+
+cudaError_t generic_pad_passes(const LaunchCfg &cfg, const Buffers &b, int precision, cudaStream_t st) {
+    return precision == 32 ? pad_passes_t<float>(cfg, b, st) : pad_passes_t<double>(cfg, b, st);
 }
 
 cudaError_t launch_stage_timed(const LaunchCfg &cfg, const Buffers &b, int precision, int drift, int scalar_mode,

@@ -206,6 +206,7 @@ const void *reg_batch_kernel_f64(int pass, int drift);
 // The background update at the end of stage p for every realization of every configuration
 // of the batch (k_scalar's SCALAR_END), one launch.
 cudaError_t launch_scalar_batch(const BatchTable &bt, int p, cudaStream_t st);
+cudaError_t generic_pad_passes(const LaunchCfg &cfg, const Buffers &b, int precision, cudaStream_t st);
 cudaError_t reg_pad_passes_f32(const LaunchCfg &cfg, const Buffers &b, cudaStream_t st);
 cudaError_t reg_pad_passes_f64(const LaunchCfg &cfg, const Buffers &b, cudaStream_t st);
 // The padded step's force evaluation (psc_pad.cu): drift (drift != 0) and padding of f_k

@@ -5,7 +5,8 @@
 //   padding()          evolution.cpp:1271-1443  f_k (N) -> f_k_pad (N_pad), zero outside the
 //                       band |k_x|, |k_y|, k_z <= N/2, every Nyquist index (x, y or z = N/2)
 //                       split over its +-N/2 images with a factor 1/2 per Nyquist axis;
-//   c2r at N_pad / N^3, V'(f_pad), r2c at N_pad     (the register-engine passes at N_pad);
+//   c2r at N_pad / N^3, V'(f_pad), r2c at N_pad     (the register-engine passes at N_pad, or
+//                       the generic engine's where N_pad is not a power of two >= 32);
 //   extract_padding()  evolution.cpp:1446-1609  V'_k_pad -> V'_k, Nyquist entries taken from
 //                       the +N/2 image times 2 per Nyquist axis, divided by (N_pad/N)^3;
 //   kernel_field_k_pad evolution.cpp:1643-1682  the force, then the kicks as in the unpadded
@@ -16,6 +17,7 @@
 // padded entries outside the band are zero once and never written again.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <string>
 #include <vector>
 
@@ -77,7 +79,7 @@ template <typename T, typename C_ = cplx<T>>
 __global__ void __launch_bounds__(kPadThreads) k_pad_kick(const cplx<T> *__restrict__ qvp, const cplx<T> *__restrict__ fk,
                                                           cplx<T> *__restrict__ pk, double *__restrict__ partKG,
                                                           int N, int Np, long long modes, long long modes_p,
-                                                          T inv_ratio3, const DevBG *__restrict__ bg,
+                                                          T ratio3, const DevBG *__restrict__ bg,
                                                           C_ *__restrict__ fcache) {
     using C = cplx<T>;
     const int H = N / 2 + 1, Hp = Np / 2 + 1, h = N / 2;
@@ -101,9 +103,9 @@ __global__ void __launch_bounds__(kPadThreads) k_pad_kick(const cplx<T> *__restr
         if (i == h) g *= T(2);
         if (j == h) g *= T(2);
         if (kz == h) g *= T(2);
-        // x 2 per Nyquist axis, / (N_pad/N)^3 (a power of two: its reciprocal is exact)
-        q.x = q.x * g * inv_ratio3;
-        q.y = q.y * g * inv_ratio3;
+        // x 2 per Nyquist axis, / (N_pad/N)^3 (evolution.cpp:1602)
+        q.x = q.x * g / ratio3;
+        q.y = q.y * g / ratio3;
         const int px = pcoord(i, N), py = pcoord(j, N);
         const T k2 = (T)(px * px + py * py + kz * kz);
         const C f = fk[m], p = pk[m];
@@ -141,12 +143,15 @@ cudaError_t pad_stage_t(const LaunchCfg &cfg, const LaunchCfg &cfgp, const Buffe
                                                               gp.modes, T(1), b.bg);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    e = sizeof(T) == 4 ? reg_pad_passes_f32(cfgp, bp, st) : reg_pad_passes_f64(cfgp, bp, st);
+    if (gp.reg)
+        e = sizeof(T) == 4 ? reg_pad_passes_f32(cfgp, bp, st) : reg_pad_passes_f64(cfgp, bp, st);
+    else
+        e = generic_pad_passes(cfgp, bp, sizeof(T) == 4 ? 32 : 64, st);
     if (e != cudaSuccess) return e;
-    // extract_padding divides by pow(N_pad / N, 3): an exact power of two here
-    const double r = (double)gp.N / (double)g.N;
+    // extract_padding divides by pow((double)N_pad / N, 3) (evolution.cpp:1602)
+    const double r3 = std::pow((double)gp.N / (double)g.N, 3);
     k_pad_kick<T><<<grid, kPadThreads, 0, st>>>((const C *)bp.QV, (const C *)b.fk, (C *)b.pk, b.partKG, g.N, gp.N,
-                                                g.modes, gp.modes, (T)(1.0 / (r * r * r)), b.bg, (C *)b.Fk);
+                                                g.modes, gp.modes, (T)r3, b.bg, (C *)b.Fk);
     return cudaGetLastError();
 }
 

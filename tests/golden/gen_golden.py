@@ -51,6 +51,8 @@ RUNS = {
     "spec2_n20_vv2": ("spec2_n20_vv2", 20, 0.005, 10, True),
     "gw2_n24_vv4": ("gw2_n24_vv4", 10, 0.005, 5, True),
     "gw1_n28_vv2": ("gw1_n28_vv2", 10, 0.002, 5, False),
+    "pad1_n16_np24": ("pad1_n16_np24", 20, 0.002, 10, True),
+    "pad2_n20_vv4_np30": ("pad2_n20_vv4_np30", 20, 0.005, 10, True),
 }
 
 

@@ -2,6 +2,7 @@
 from __future__ import annotations
 
 import json
+import re
 import os
 
 import numpy as np
@@ -35,7 +36,8 @@ def params_for(meta: dict, precision: int = 64) -> Params:
                               N=meta["N"])
     else:
         p = Params.preheating(N=meta["N"])
-    p.vv = int(c.split("vv")[1]) if "vv" in c else 2
+    m = re.search(r"vv(\d+)", c)
+    p.vv = int(m.group(1)) if m else 2
     p.spectral = meta["spectral"]
     p.with_gw = meta["gw"]
     p.precision = precision

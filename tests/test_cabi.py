@@ -45,7 +45,7 @@ def test_params_struct_layout_matches_header(psc_lib):
 
 
 @pytest.mark.parametrize("bad", [dict(N=44), dict(N=15), dict(N=768), dict(N=2048), dict(N=4), dict(nflds=3),
-                                 dict(vv=3), dict(precision=16), dict(with_gw=1, N_pad=32), dict(N=24, N_pad=64),
+                                 dict(vv=3), dict(precision=16), dict(with_gw=1, N_pad=32), dict(N=16, N_pad=44),
                                  dict(kIR=0.0), dict(model=1)])
 def test_invalid_configurations_are_rejected(psc_lib, bad):
     from pspectcosmo_gb300.params import Params

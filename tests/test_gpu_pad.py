@@ -1,7 +1,8 @@
 """The padded (dealiased) spectral step and the spectral prolongation on the device.
 
-* FP64 padded step (N = 16, N_pad = 32) against the reference's own evolve_VV_k_pad
-  (golden runs pad1_n16, pad2_n16_vv4, and pad3_n16_vv4 with the three-field model.h): initial a'' (kernel_a_k_pad) to 1e-12, the state
+* FP64 padded step (N = 16, N_pad = 32; N = 16, N_pad = 24; N = 20, N_pad = 30) against the
+  reference's own evolve_VV_k_pad (golden runs pad1_n16, pad2_n16_vv4, pad3_n16_vv4 with the
+  three-field model.h, pad1_n16_np24, pad2_n20_vv4_np30): initial a'' (kernel_a_k_pad) to 1e-12, the state
   after 20 steps to 1e-10 of its largest mode and, for the two-field model where the
   padding changes the result, the fluctuation modes (all but k = 0) to 1e-8 of theirs
   (the unpadded step differs from the padded one by ~5e-7 there).
@@ -18,6 +19,7 @@
   bound (~1.57), and the FP32 rounding noise there grows by orders of magnitude per step.
 """
 import os
+import re
 import sys
 
 import numpy as np
@@ -35,11 +37,14 @@ def _padded(run, precision=64):
 
     g, meta = load(run)
     p = params_for(meta, precision)
-    p.N_pad = 2 * p.N
+    m = re.search(r"np(\d+)", run)
+    p.N_pad = int(m.group(1)) if m else 2 * p.N
     return g, meta, p, Lattice(p)
 
 
-@pytest.mark.parametrize("run", ["pad1_n16", "pad2_n16_vv4", "pad3_n16_vv4"])
+# pad1_n16_np24: a padded grid that is not a power of two (24^3, the generic engine, ratio 1.5);
+# pad2_n20_vv4_np30: both grids mixed-radix (20^3 and 30^3)
+@pytest.mark.parametrize("run", ["pad1_n16", "pad2_n16_vv4", "pad3_n16_vv4", "pad1_n16_np24", "pad2_n20_vv4_np30"])
 def test_padded_step_matches_reference(run):
     g, meta, p, lat = _padded(run)
     lat.initialize()

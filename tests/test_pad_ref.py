@@ -34,7 +34,9 @@ def scatter_map(src, Ns, Nd, scale=1.0):
 
 
 def extract_map(pad, N, Np):
-    """k_pad_kick's read of V'_k_pad: the +N/2 image, x 2 per Nyquist axis, / (Np/N)^3."""
+    """k_pad_kick's read of V'_k_pad: the +N/2 image, x 2 per Nyquist axis, / (Np/N)^3 (a
+    division, as evolution.cpp:1602: exact for power-of-two ratios, rounded as the reference
+    rounds for the others)."""
     h = N // 2
     p = pad.reshape(Np, Np, Np // 2 + 1)
     out = np.zeros((N, N, h + 1), dtype=p.dtype)
@@ -44,18 +46,18 @@ def extract_map(pad, N, Np):
                 I = i if i <= h else Np - (N - i)
                 J = j if j <= h else Np - (N - j)
                 g = (2 if i == h else 1) * (2 if j == h else 1) * (2 if kz == h else 1)
-                out[i, j, kz] = p[I, J, kz] * g * (1.0 / (Np / N) ** 3)
+                out[i, j, kz] = p[I, J, kz] * g / (Np / N) ** 3
     return out
 
 
-@pytest.mark.parametrize("N,Np", [(4, 8), (8, 16), (8, 32), (16, 32)])
+@pytest.mark.parametrize("N,Np", [(4, 8), (8, 16), (8, 32), (16, 32), (8, 12), (12, 20), (16, 24)])
 def test_scatter_map_is_padding(N, Np):
     rng = np.random.default_rng(N * Np)
     fk = rng.standard_normal((N, N, N // 2 + 1)) + 1j * rng.standard_normal((N, N, N // 2 + 1))
     assert np.array_equal(scatter_map(fk, N, Np), pad_ref.padding(fk, N, Np))
 
 
-@pytest.mark.parametrize("N,Np", [(4, 8), (8, 16), (8, 32), (16, 32)])
+@pytest.mark.parametrize("N,Np", [(4, 8), (8, 16), (8, 32), (16, 32), (8, 12), (12, 20), (16, 24)])
 def test_extract_map_is_extract_padding(N, Np):
     rng = np.random.default_rng(N + Np)
     fkp = rng.standard_normal((Np, Np, Np // 2 + 1)) + 1j * rng.standard_normal((Np, Np, Np // 2 + 1))
