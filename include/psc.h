@@ -321,9 +321,9 @@ int psc_autotune(psc_handle *h, int reps, int *shape, int *from_cache);
 int psc_get_shapes(psc_handle *h, int *shape);
 int psc_set_shapes(psc_handle *h, const int *shape);
 
-/* Tile staging by tensor maps (TMA; no reference counterpart). The register-engine passes of
- * N <= 256 stage their tiles in shared memory with tiled tensor copies: PSC_TMAP_X, the X
- * inverse (FP32) and the X forward + kick pass (input and operand tiles); PSC_TMAP_Y, the FP32 Y
+/* Tile staging by tensor maps (TMA; no reference counterpart). The register-engine passes
+ * stage their tiles in shared memory with tiled tensor copies: PSC_TMAP_X, the X inverse (FP32)
+ * and the X forward + kick pass (input and operand tiles, every N >= 32); PSC_TMAP_Y, the FP32 Y
  * forward pass at N = 128 and 256 (where a tile's lines divide N/2; persistent, the next tile's
  * copies in flight during the current transform). Without them each thread loads its own
  * elements. Both forms give bit-identical results. psc_set_tensor_maps allows the groups in mask

@@ -1011,11 +1011,12 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 }
 
 // The tensor maps of the handle's passes (TMA staging), re-encoded whenever the tile shape
-// changes. Register engine, N <= 256 (a box edge is at most 256), single-lattice or batch
-// handles alike (the realization is a map dimension); otherwise, or when the handle's mask
-// (psc_set_tensor_maps) leaves a group out, that group is off and its passes load directly.
+// changes. Register engine, single-lattice or batch handles alike (the realization is a map
+// dimension); otherwise, or when the handle's mask (psc_set_tensor_maps) leaves a group out,
+// that group is off and its passes load directly.
 // X passes: an array group (na arrays of `modes` complex, realization stride rstride) as
-// {lines_x, N, na, R} in 8-byte elements (an FP64 complex is two), box {lines per tile, N, 1, 1}.
+// {lines_x, N, na, R} in 8-byte elements (an FP64 complex is two), box {lines per tile,
+// min(N, 256), 1, 1} (a box edge is at most 256: a tile of N > 256 points is N/256 boxes).
 // Y forward pass (FP32): V' and S_ab as {2 H, N N/2, na, R} (rows of two y; YTma,
 // psc_launch.h), boxes {TL, N/2, 1, 1} (even rows) and {TL + 2, N/2, 1, 1} (odd rows); on for
 // the sizes with the tensor-map instantiation (N = 128, 256) when TL divides N/2 and a box row
@@ -1027,7 +1028,7 @@ void encode_xtma(psc_handle *h) {
     h->b.ytma = nullptr;
     const psc::Geo &g = h->cfg.g;
     auto enc = tensor_map_encoder();
-    if (!enc || !g.reg || g.N > 256 || h->padded) return;
+    if (!enc || !g.reg || h->padded) return;
     const cuuint64_t w = h->csize / 8, TL = 1u << g.tlx_shift;
     auto map4 = [&](CUtensorMap *m, void *base, const cuuint64_t (&dims)[4], const cuuint64_t (&strides)[3],
                     cuuint32_t box0, cuuint32_t box1) -> bool {
@@ -1045,7 +1046,7 @@ void encode_xtma(psc_handle *h) {
             const cuuint64_t dims[4] = {(cuuint64_t)g.lines_x * w, (cuuint64_t)g.N, (cuuint64_t)na, (cuuint64_t)h->R};
             const cuuint64_t strides[3] = {(cuuint64_t)g.lines_x * h->csize, (cuuint64_t)g.modes * h->csize,
                                            rs(rstride, na)};
-            return map4(m, base, dims, strides, (cuuint32_t)(TL * w), (cuuint32_t)g.N);
+            return map4(m, base, dims, strides, (cuuint32_t)(TL * w), (cuuint32_t)std::min(g.N, 256));
         };
         bool ok = make(&h->xtma.fk, h->b.fk, g.nf, g.fstride) && make(&h->xtma.pk, h->b.pk, g.nf, g.fstride) &&
                   make(&h->xtma.qv, h->b.QV, g.nf, g.fstride);

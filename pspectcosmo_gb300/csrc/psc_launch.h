@@ -87,8 +87,9 @@ struct Buffers {
 
 // Tensor maps of the X passes' tiles (TMA): f_k, pi_k, QV as {lines, x, field, realization}
 // and u_k, pi_u_k, QS as {lines, x, component, realization}, in 8-byte elements, box {lines
-// per tile, N, 1, 1}. on = 0: the pass stages its operands by
-// cp.async instead (N > 256, batched launches, or no tensor-map encoder).
+// per tile, min(N, 256), 1, 1} (N/256 boxes per tile above 256). on = 0: the pass stages its
+// operands by cp.async instead (batched launches, the generic engine, or no tensor-map
+// encoder).
 struct XTma {
     CUtensorMap fk, pk, uk, puk;
     CUtensorMap qv, qs;   // the forward passes' V'_k and S_k arrays: the X forward's input tiles

@@ -45,6 +45,17 @@ struct VBlock {
 };
 __device__ __forceinline__ HwBlock vblock_hw() { return HwBlock{}; }
 
+// One X-pass tile (TL lines x L points, line fastest) of array `arr`, realization z, by tensor
+// copies from the map m (box {TL lines, XB x}): L / XB boxes stacked along x, since a box edge
+// is at most 256 (XB = min(L, 256)). c0: the tile's first line in 8-byte elements.
+template <int L, typename C>
+__device__ __forceinline__ void x_tile_tma(C *dst, const CUtensorMap *m, int c0, int TL, int arr, int z,
+                                           uint64_t *bar) {
+    constexpr int XB = L < 256 ? L : 256;
+#pragma unroll
+    for (int x0 = 0; x0 < L; x0 += XB) tma_load_4d(dst + x0 * TL, m, c0, x0, arr, z, bar);
+}
+
 
 // ------------------------------------------------------------------ X inverse (+ drift, + x-derivative)
 template <typename T, int L, bool GW, bool DRIFT, class VB>
@@ -88,8 +99,8 @@ __device__ __forceinline__ void kr_ifft_x_body(const VB &vb, Geo g, cplx<T> *__r
             mbar_fence_init();
             mbar_arrive_expect_tx(&ibar, (DRIFT ? 2u : 1u) * (unsigned)(TL * L * sizeof(C)) + planted(bg, 0));
             const int w8 = (int)(sizeof(C) / 8), c0 = (int)(vb.x() * TL) * w8;
-            tma_load_4d(opF, &tma->fk, c0, 0, (int)vb.y(), (int)vb.z(), &ibar);
-            if (DRIFT) tma_load_4d(opP, &tma->pk, c0, 0, (int)vb.y(), (int)vb.z(), &ibar);
+            x_tile_tma<L>(opF, &tma->fk, c0, TL, (int)vb.y(), (int)vb.z(), &ibar);
+            if (DRIFT) x_tile_tma<L>(opP, &tma->pk, c0, TL, (int)vb.y(), (int)vb.z(), &ibar);
         }
         __syncthreads();   // the mbarrier is initialised before any thread waits on it
         // bounded wait, as the X forward + kick pass's: a timeout is reported, the copies in
@@ -525,11 +536,11 @@ __device__ __forceinline__ void kr_fft_x_final_body(const VB &vb, Geo g, const c
             mbar_fence_init();
             const int w8 = (int)(sizeof(C) / 8), arr = field ? job : job - g.nf, c0 = (int)(vb.x() * TL) * w8;
             mbar_arrive_expect_tx(&qbar, (unsigned)(TL * L * sizeof(C)) + planted(bg, 4));
-            tma_load_4d(sm, field ? &tma->qv : &tma->qs, c0, 0, arr, (int)vb.z(), &qbar);
+            x_tile_tma<L>(sm, field ? &tma->qv : &tma->qs, c0, TL, arr, (int)vb.z(), &qbar);
             mbar_arrive_expect_tx(&xbar, 2u * (unsigned)(TL * L * sizeof(C)));
             const CUtensorMap *ma = field ? &tma->fk : &tma->uk, *mb = field ? &tma->pk : &tma->puk;
-            tma_load_4d(opA, ma, c0, 0, arr, (int)vb.z(), &xbar);
-            tma_load_4d(opB, mb, c0, 0, arr, (int)vb.z(), &xbar);
+            x_tile_tma<L>(opA, ma, c0, TL, arr, (int)vb.z(), &xbar);
+            x_tile_tma<L>(opB, mb, c0, TL, arr, (int)vb.z(), &xbar);
         }
         __syncthreads();   // the mbarriers are initialised before any thread waits on them
         const bool ok = mbar_wait_bounded(&qbar, 0, bg->wait_ns);

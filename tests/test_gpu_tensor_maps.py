@@ -1,4 +1,5 @@
-"""Tile staging by tensor maps (TMA). The X passes (X inverse in FP32, X forward + kick) and,
+"""Tile staging by tensor maps (TMA). The X passes (X inverse in FP32, X forward + kick; above
+N = 256 a tile is N/256 boxes along x) and,
 in FP32 at N = 128 and 256, the Y forward pass (persistent and pipelined) stage their tiles in
 shared memory by tiled tensor copies; with the maps switched off (psc_set_tensor_maps) every
 thread loads its own elements.
@@ -35,7 +36,7 @@ def _same(a, b, gw):
 
 
 @pytest.mark.parametrize("N,precision,gw,want", [(256, 32, 1, X | Y), (128, 64, 1, X), (128, 32, 0, X | Y),
-                                                  (64, 32, 1, X), (16, 32, 1, 0)])
+                                                  (64, 32, 1, X), (16, 32, 1, 0), (512, 32, 1, X), (24, 32, 1, 0)])
 def test_groups_in_use(N, precision, gw, want):
     from pspectcosmo_gb300 import Lattice
 
@@ -53,7 +54,8 @@ def test_groups_in_use(N, precision, gw, want):
 
 
 @pytest.mark.parametrize("N,precision,gw,shift", [(256, 32, 1, -1), (128, 32, 1, -1), (128, 64, 1, -1),
-                                                  (256, 64, 0, -1), (128, 32, 0, -1), (256, 32, 1, 2)])
+                                                  (256, 64, 0, -1), (128, 32, 0, -1), (256, 32, 1, 2),
+                                                  (512, 32, 1, -1), (512, 64, 1, -1)])
 def test_every_form_gives_the_same_bits(N, precision, gw, shift):
     from pspectcosmo_gb300 import Lattice
 
