@@ -324,7 +324,7 @@ int psc_set_shapes(psc_handle *h, const int *shape);
 /* Tile staging by tensor maps (TMA; no reference counterpart). The register-engine passes
  * stage their tiles in shared memory with tiled tensor copies: PSC_TMAP_X, the X inverse (FP32)
  * and the X forward + kick pass (input and operand tiles, every N >= 32); PSC_TMAP_Y, the FP32 Y
- * forward pass at N = 128 and 256 (where a tile's lines divide N/2; persistent, the next tile's
+ * forward pass at N = 128 .. 1024 (where a tile's lines divide N/2; persistent, the next tile's
  * copies in flight during the current transform). Without them each thread loads its own
  * elements. Both forms give bit-identical results. psc_set_tensor_maps allows the groups in mask
  * (both by default; a group also needs a fitting shape); psc_get_tensor_maps reports the groups

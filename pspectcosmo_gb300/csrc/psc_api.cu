@@ -1018,9 +1018,9 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 // {lines_x, N, na, R} in 8-byte elements (an FP64 complex is two), box {lines per tile,
 // min(N, 256), 1, 1} (a box edge is at most 256: a tile of N > 256 points is N/256 boxes).
 // Y forward pass (FP32): V' and S_ab as {2 H, N N/2, na, R} (rows of two y; YTma,
-// psc_launch.h), boxes {TL, N/2, 1, 1} (even rows) and {TL + 2, N/2, 1, 1} (odd rows); on for
-// the sizes with the tensor-map instantiation (N = 128, 256) when TL divides N/2 and a box row
-// is a multiple of 16 bytes.
+// psc_launch.h), boxes {TL, min(N/2, 256), 1, 1} (even rows) and {TL + 2, min(N/2, 256), 1, 1}
+// (odd rows); on for the sizes with the tensor-map instantiation (N = 128 .. 1024) when TL
+// divides N/2 and a box row is a multiple of 16 bytes.
 void encode_xtma(psc_handle *h) {
     h->xtma = psc::XTma{};
     h->ytma = psc::YTma{};
@@ -1063,15 +1063,16 @@ void encode_xtma(psc_handle *h) {
     }
     const cuuint64_t ox = w == 1 ? 1 : 0;   // FP32: the odd rows' box starts one element early
     const bool yfits = w == 1 && psc::y_pipe_size(g.N) && TL <= (cuuint64_t)g.M && (TL * w * 8) % 16 == 0 &&
-                       (TL + 2 * ox) * w <= 256 && g.M <= 256;
+                       (TL + 2 * ox) * w <= 256;
     if ((h->tmap_mask & PSC_TMAP_Y) && yfits) {
         auto make = [&](CUtensorMap *me, CUtensorMap *mo, void *base, int na, long long rstride) -> bool {
             const cuuint64_t dims[4] = {(cuuint64_t)(2 * g.H) * w, (cuuint64_t)g.N * g.M, (cuuint64_t)na,
                                         (cuuint64_t)h->R};
             const cuuint64_t strides[3] = {(cuuint64_t)(2 * g.H) * h->csize, (cuuint64_t)g.modes * h->csize,
                                            rs(rstride, na)};
-            return map4(me, base, dims, strides, (cuuint32_t)(TL * w), (cuuint32_t)g.M) &&
-                   map4(mo, base, dims, strides, (cuuint32_t)((TL + 2 * ox) * w), (cuuint32_t)g.M);
+            const cuuint32_t yb = (cuuint32_t)std::min(g.M, 256);   // pairs per box
+            return map4(me, base, dims, strides, (cuuint32_t)(TL * w), yb) &&
+                   map4(mo, base, dims, strides, (cuuint32_t)((TL + 2 * ox) * w), yb);
         };
         psc::YTma &y = h->ytma;
         bool ok = make(&y.ae, &y.ao, h->b.QV, g.nf, g.fstride);

@@ -100,7 +100,8 @@ struct XTma {
 // Tensor maps of the Y passes' tiles (TMA). A Y line's element stride is H = N/2 + 1 complex,
 // in FP32 8 H bytes, never a multiple of 16, so an array is mapped as rows of two y (pairs):
 // {2 H, N N / 2, array, realization} in 8-byte elements (an FP64 complex being two), pair stride
-// 16 H bytes. A tile of TL consecutive kz < N/2 at one x is two boxes of N/2 pairs: the even
+// 16 H bytes. A tile of TL consecutive kz < N/2 at one x is two boxes of N/2 pairs (each split
+// into boxes of 256 pairs above N = 512, a box edge being at most 256): the even
 // rows {TL, N/2} at kz0, the odd rows at H + kz0; in FP32 that start is odd, so the odd box
 // starts one element earlier (H - 1 + kz0, even) and is TL + 2 wide (a multiple of 16 bytes).
 // The FP32 Y forward pass uses them (in FP64 the staging measured no faster): a* map the fields'
@@ -112,7 +113,7 @@ struct YTma {
     int on;
 };
 // the lattice sizes whose Y forward pass has its tensor-map instantiation (FP32)
-constexpr bool y_pipe_size(int N) { return N == 128 || N == 256; }
+constexpr bool y_pipe_size(int N) { return N == 128 || N == 256 || N == 512 || N == 1024; }
 
 // The arrays of the forward passes (V' of each field, then the six S_ab: up to
 // PSC_MAX_FIELDS + 6) with the realization stride of each (elements).

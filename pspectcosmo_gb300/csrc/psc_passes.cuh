@@ -345,15 +345,20 @@ __device__ __forceinline__ void y_slots(int j, int t, int TL, int M, int &s0, in
 // elements of one staged array tile: (2 TL + 2 OX) rows of N/2
 template <typename C> __device__ __forceinline__ int y_stage_elems(int TL, int N) { return (TL + y_ox<C>()) * N; }
 
-// Thread 0: the two tensor copies of plane tile y of array `arr`, realization z, into st
-// (128-byte aligned), completing on bar.
-template <typename C>
+// Thread 0: the tensor copies of plane tile y of array `arr`, realization z, into st (128-byte
+// aligned), completing on bar: the even rows, then the odd rows, each in boxes of
+// YB = min(N/2, 256) pairs (a box edge is at most 256).
+template <typename C, int L>
 __device__ __forceinline__ void y_issue(C *st, const CUtensorMap *me, const CUtensorMap *mo, const YTile &y,
                                         const Geo &g, int arr, int z, uint64_t *bar) {
-    constexpr int OX = y_ox<C>(), W = (int)(sizeof(C) / 8);
-    const int q0 = y.x0 * g.M;
-    tma_load_4d(st, me, y.kz0 * W, q0, arr, z, bar);
-    tma_load_4d(st + (g.M << g.tlx_shift), mo, (g.H + y.kz0) * W - OX, q0, arr, z, bar);
+    constexpr int OX = y_ox<C>(), W = (int)(sizeof(C) / 8), M = L / 2, YB = M < 256 ? M : 256;
+    const int TL = 1 << g.tlx_shift, q0 = y.x0 * M;
+    C *odd = st + TL * M;
+#pragma unroll
+    for (int p0 = 0; p0 < M; p0 += YB) {
+        tma_load_4d(st + p0 * TL, me, y.kz0 * W, q0 + p0, arr, z, bar);
+        tma_load_4d(odd + p0 * (TL + 2 * OX), mo, (g.H + y.kz0) * W - OX, q0 + p0, arr, z, bar);
+    }
 }
 
 // Each thread of a column tile copies its own elements of array src (cp.async) into the
@@ -369,14 +374,15 @@ __device__ __forceinline__ void y_column_async(C *st, const C *src, const YTile 
 }
 
 // Y forward pass, FP32 tensor-map form, persistent and pipelined: one wave of blocks (two per
-// SM; three, at 80 registers, measured slower) walks the items w = (tile, array, realization),
+// SM, one for 1024-point lines; three, at 80 registers, measured slower) walks the items
+// w = (tile, array, realization),
 // tile fastest. While an item's tile is transformed, thread 0 has already issued the tensor
 // copies of the block's next item into the other of two staging buffers (the current one
 // doubles as the exchange buffer), so each tile's load overlaps the previous tile's transform.
 // Column tiles (kz = N/2) are staged by the block's own cp.async copies when their turn comes.
 // Same transform per line: the bits of kr_fft_y.
 template <typename T, int L>
-__global__ void __launch_bounds__(256, 2) kr_fft_y_pipe(Geo g, const __grid_constant__ ArrList arrs,
+__global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_fft_y_pipe(Geo g, const __grid_constant__ ArrList arrs,
                                                        const cplx<T> *__restrict__ tw, const DevBG *bg,
                                                        const __grid_constant__ YTma ym, int nj, int R) {
     using C = cplx<T>;
@@ -400,7 +406,7 @@ __global__ void __launch_bounds__(256, 2) kr_fft_y_pipe(Geo g, const __grid_cons
         y.kz0 = (int)(b - (unsigned)y.x0 * per) << sh;
         fence_proxy_async();   // the previous use of st (staging reads, exchange) comes first
         mbar_arrive_expect_tx(br, (unsigned)(se * sizeof(C)) + planted(bg + z, 3));
-        y_issue(st, first ? &ym.ae : &ym.be, first ? &ym.ao : &ym.bo, y, g, first ? jy : jy - ym.na, z, br);
+        y_issue<C, L>(st, first ? &ym.ae : &ym.be, first ? &ym.ao : &ym.bo, y, g, first ? jy : jy - ym.na, z, br);
     };
     if (threadIdx.x == 0) {
         mbar_init(&bar[0], 1);

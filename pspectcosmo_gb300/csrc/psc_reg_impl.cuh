@@ -12,7 +12,7 @@ template <typename T, int N>
 struct RegLaunch {
     using C = cplx<T>;
     static constexpr int M = N / 2;
-    // the Y forward pass staged by tensor maps (kr_fft_y_pipe): FP32, N = 128 and 256
+    // the Y forward pass staged by tensor maps (kr_fft_y_pipe): FP32, N = 128 .. 1024
     static constexpr bool kYPipe = sizeof(T) == 4 && y_pipe_size(N);
 
     static void gw_adj_tile(int nf, int *tl, int *sh);
@@ -156,9 +156,9 @@ struct RegLaunch {
         if (!ypl) {
             kr_fft_y<T, N><<<dim3(cfg.nbx, nj, R), txy, cfg.smem_xy, st>>>(g, al, tw);
         } else if constexpr (kYPipe) {
-            // persistent and pipelined: two blocks per SM walk the items
-            const long long items = (long long)cfg.nbx * nj * R;
-            const int grid = (int)(items < 2LL * cfg.sms ? items : 2LL * cfg.sms);
+            // persistent and pipelined: two blocks per SM (one for 1024-point lines) walk the items
+            const long long items = (long long)cfg.nbx * nj * R, wave = (long long)xy_blocks<N>(2) * cfg.sms;
+            const int grid = (int)(items < wave ? items : wave);
             kr_fft_y_pipe<T, N><<<grid, txy, 2 * cfg.smem_ys + 128, st>>>(g, al, tw, b.bg, *b.ytma, nj, R);
         }
         mark(4);

@@ -36,7 +36,7 @@ def _same(a, b, gw):
 
 
 @pytest.mark.parametrize("N,precision,gw,want", [(256, 32, 1, X | Y), (128, 64, 1, X), (128, 32, 0, X | Y),
-                                                  (64, 32, 1, X), (16, 32, 1, 0), (512, 32, 1, X), (24, 32, 1, 0)])
+                                                  (64, 32, 1, X), (16, 32, 1, 0), (512, 32, 1, X | Y), (24, 32, 1, 0)])
 def test_groups_in_use(N, precision, gw, want):
     from pspectcosmo_gb300 import Lattice
 
