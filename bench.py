@@ -786,7 +786,8 @@ def run_ours(args):
                        "parallelism": f"replicas x{world}" if world > 1 else "single lattice",
                        "l2": "arrays > 129 MB L2 (no flush needed)",
                        "fft_shapes": shapes,
-                       "tensor_map_staging": {"x_passes": bool(lat.tensor_maps & 1), "y_passes": bool(lat.tensor_maps & 2)}},
+                       "tensor_map_staging": {"x_passes": bool(lat.tensor_maps & 1), "y_forward": bool(lat.tensor_maps & 2),
+                                              "y_inverse": bool(lat.tensor_maps & 4)}},
             "e2e": e2e,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
@@ -819,8 +820,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--no-autotune", action="store_true", help="keep the planner's default FFT tile shapes")
-    ap.add_argument("--tensor-maps", type=int, default=3, choices=[0, 1, 2, 3],
-                    help="pass groups that stage their tiles by tensor maps: 1 X passes, 2 Y passes (default both)")
+    ap.add_argument("--tensor-maps", type=int, default=3, choices=range(8),
+                    help="pass groups that stage their tiles by tensor maps: 1 X passes, 2 Y passes (default both), "
+                         "4 the pipelined GW Y inverse pass below N = 1024")
     ap.add_argument("--one-launch", action="store_true",
                     help="ensemble_mixed: one launch per pass for all size groups (default: per-group launches)")
     ap.add_argument("--adj-check", type=int, default=0,

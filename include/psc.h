@@ -325,12 +325,15 @@ int psc_set_shapes(psc_handle *h, const int *shape);
  * stage their tiles in shared memory with tiled tensor copies: PSC_TMAP_X, the X inverse (FP32)
  * and the X forward + kick pass (input and operand tiles, every N >= 32); PSC_TMAP_Y, the FP32 Y
  * forward pass at N = 128 .. 1024 (where a tile's lines divide N/2; persistent, the next tile's
- * copies in flight during the current transform). Without them each thread loads its own
+ * copies in flight during the current transform) and, at N = 1024, the FP32 GW Y inverse pass in
+ * the same pipelined form (it measured slower at 256); PSC_TMAP_YINV (with PSC_TMAP_Y) takes that
+ * form at every size from 128 on (tests, timing). Without them each thread loads its own
  * elements. Both forms give bit-identical results. psc_set_tensor_maps allows the groups in mask
  * (both by default; a group also needs a fitting shape); psc_get_tensor_maps reports the groups
  * in use. */
 #define PSC_TMAP_X 1
 #define PSC_TMAP_Y 2
+#define PSC_TMAP_YINV 4
 int psc_set_tensor_maps(psc_handle *h, int mask);
 int psc_get_tensor_maps(psc_handle *h, int *mask);
 
@@ -359,12 +362,13 @@ int psc_selftest_bulk_wait(double limit_ms, int *status);
  * PSC_ERR_CONFIG when plant_bytes > 0 and the handle's GW Z pass does not stage its tiles by
  * bulk copies (FP32 GW runs with an even number of lines per tile do). */
 int psc_test_wait_hook(psc_handle *h, double limit_ms, int plant_bytes);
-/* The same hook on the tensor-map waits of another pass (PSC_NPASS order: 0 X inverse, 2 the
- * GW Z pass as above, 3 Y forward, 4 X forward + kick): every tile that pass stages by tensor
- * copies expects plant_bytes more than its copies deliver, waits out the limit, counts the
- * planted bytes itself and leaves; psc_step returns PSC_ERR_TIMEOUT. PSC_ERR_CONFIG when
- * plant_bytes > 0 and the handle's pass does not stage its tiles that way (psc_get_tensor_maps;
- * the X inverse stages by tensor maps in FP32 only; the Y inverse, pass 1, never does). */
+/* The same hook on the tensor-map waits of another pass (PSC_NPASS order: 0 X inverse, 1 Y
+ * inverse, 2 the GW Z pass as above, 3 Y forward, 4 X forward + kick): every tile that pass
+ * stages by tensor copies expects plant_bytes more than its copies deliver, waits out the limit,
+ * counts the planted bytes itself and leaves; psc_step returns PSC_ERR_TIMEOUT. PSC_ERR_CONFIG
+ * when plant_bytes > 0 and the handle's pass does not stage its tiles that way
+ * (psc_get_tensor_maps; the X inverse stages by tensor maps in FP32 only, the Y inverse with GWs
+ * in FP32 only). */
 int psc_test_wait_hook_pass(psc_handle *h, double limit_ms, int plant_bytes, int pass);
 
 /* ---------------------------------------------------------------- batches

@@ -29,8 +29,8 @@ struct DevBG {
     int stage, steps_left, err, pad;
     // bounded device-side waits: the limit of one wait (1 s unless a test sets it), and a
     // test hook: bytes every staged tile of pass wait_plant_pass (PSC_NPASS order: 0 X
-    // inverse, 2 Z, 3 Y forward, 4 X forward) is told to expect that no copy delivers, so its
-    // wait runs out after the real copies have landed (0 = off)
+    // inverse, 1 Y inverse, 2 Z, 3 Y forward, 4 X forward) is told to expect that no copy
+    // delivers, so its wait runs out after the real copies have landed (0 = off)
     unsigned long long wait_ns;
     int wait_plant, fp32;           // fp32: the handle's arrays hold FP32 values
     int wait_plant_pass, pad2;

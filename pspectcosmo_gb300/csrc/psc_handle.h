@@ -36,6 +36,7 @@ struct psc_handle {
     size_t partKG_cap = 0, partV_cap = 0;   // doubles held by b.partKG, b.partV (the autotuner may grow them)
     psc::XTma xtma{};            // tensor maps of the X forward + kick operands (b.xtma points here when on)
     psc::YTma ytma{};            // tensor maps of the Y forward tiles (b.ytma points here when on)
+    psc::YTma ytma_i{};          // tensor maps of the GW Y inverse tiles (b.ytma_i)
     int tmap_mask = PSC_TMAP_X | PSC_TMAP_Y;   // passes allowed to stage their tiles by tensor maps
     void *adj = nullptr;         // adjoint workspace (psc_adjoint.cu), owned by the handle
     void (*adj_free)(void *) = nullptr;

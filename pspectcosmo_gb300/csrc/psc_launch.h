@@ -83,6 +83,7 @@ struct Buffers {
     void *Fk, *Fu;
     const XTma *xtma;            // host copy of the kick operands' tensor maps (null: cp.async staging)
     const YTma *ytma;            // the Y forward pass's tensor maps (V', S_ab); null: direct loads
+    const YTma *ytma_i;          // the GW Y inverse pass's tensor maps (TA, TB); null: direct loads
 };
 
 // Tensor maps of the X passes' tiles (TMA): f_k, pi_k, QV as {lines, x, field, realization}
@@ -105,8 +106,8 @@ struct XTma {
 // rows {TL, N/2} at kz0, the odd rows at H + kz0; in FP32 that start is odd, so the odd box
 // starts one element earlier (H - 1 + kz0, even) and is TL + 2 wide (a multiple of 16 bytes).
 // The FP32 Y forward pass uses them (in FP64 the staging measured no faster): a* map the fields'
-// V' (the first na arrays of the pass), b* the six S_ab. on = 0: direct loads. (The Y inverse
-// pass keeps its direct loads: staged this way it measured slower.)
+// V' (the first na arrays of the pass), b* the six S_ab; and the FP32 GW Y inverse pass in its
+// pipelined form: a* TA, b* TB of each field. on = 0: direct loads.
 struct YTma {
     CUtensorMap ae, ao, be, bo;   // even-row and odd-row boxes of the two array groups
     int na;

@@ -484,6 +484,159 @@ __global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_fft_y_pip
 }
 
 
+// Y inverse pass with GWs, FP32 tensor-map form, persistent and pipelined: one wave of blocks
+// walks the items w = (tile, field, realization), tile fastest, with the Y forward pass's tiles
+// (row-pair boxes; the kz = N/2 column by the threads' own cp.async copies). An item's TA and TB
+// tiles sit in one staging buffer each; the block transforms TB -> TB first, then
+// d/dy TA -> TC and TA -> TA, through a separate exchange buffer. As soon as a buffer's last
+// transform has read it, thread 0 refills it with the block's next item (TB after the first
+// transform, TA after the third), so each tile's load overlaps the transforms that follow.
+// Same transform per line: the bits of kr_ifft_y.
+template <typename T, int L>
+__global__ void __launch_bounds__(xy_threads<L>(), xy_blocks<L>(2)) kr_ifft_y_pipe(Geo g, cplx<T> *__restrict__ TA,
+                                                       cplx<T> *__restrict__ TB, cplx<T> *__restrict__ TC,
+                                                       const DevBG *bg, const cplx<T> *__restrict__ tw,
+                                                       const __grid_constant__ YTma ym, int R) {
+    using C = cplx<T>;
+    using RP = RegPlan<L>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ uint64_t barA, barB;   // completion of the tensor copies into the TA / TB buffer
+    const int sh = g.tlx_shift, TL = 1 << sh;
+    const int t = threadIdx.x & (TL - 1), j = threadIdx.x >> sh;
+    const unsigned per = (unsigned)(g.M >> sh), nplane = (unsigned)g.N * per, nbx = nplane + (unsigned)(g.N >> sh);
+    const unsigned nf = (unsigned)g.nf, total = nbx * nf * (unsigned)R;
+    const int se = y_stage_elems<C>(TL, g.N);
+    C *stA = reinterpret_cast<C *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
+    C *stB = stA + se, *xb = stB + se;
+    auto ix = [&](int n) { return n * TL + t; };
+    unsigned plantA = 0, plantB = 0;   // thread 0: the test hook's bytes in the pending copies
+    // thread 0: the tensor copies of plane-tile item w's array (maps me, mo) into st, on br
+    auto issue = [&](unsigned w, C *st, const CUtensorMap *me, const CUtensorMap *mo, uint64_t *br) -> unsigned {
+        const unsigned b = w % nbx, rest = w / nbx;
+        const int jy = (int)(rest % nf), z = (int)(rest / nf);
+        YTile y;
+        y.x0 = (int)(b / per);
+        y.kz0 = (int)(b - (unsigned)y.x0 * per) << sh;
+        const unsigned plant = planted(bg + z, 1);
+        fence_proxy_async();   // the previous reads of st come first
+        mbar_arrive_expect_tx(br, (unsigned)(se * sizeof(C)) + plant);
+        y_issue<C, L>(st, me, mo, y, g, jy, z, br);
+        return plant;
+    };
+    if (threadIdx.x == 0) {
+        mbar_init(&barA, 1);
+        mbar_init(&barB, 1);
+        mbar_fence_init();
+    }
+    // a failed stage: no work (one thread reads the error words; the barrier also makes the
+    // initialised mbarriers visible to every thread)
+    bool failed = false;
+    if (threadIdx.x == 0)
+        for (int z = 0; z < R; ++z) failed |= bg[z].err != 0;
+    if (__syncthreads_or(failed)) return;
+    unsigned w = blockIdx.x;
+    bool pendA = false, pendB = false;   // copies in flight into the TA / TB buffer (every thread)
+    unsigned pa = 0, pb = 0;             // parities of the next completions of barA / barB
+    if (w < total && w % nbx < nplane) {
+        if (threadIdx.x == 0) {
+            plantB = issue(w, stB, &ym.be, &ym.bo, &barB);
+            plantA = issue(w, stA, &ym.ae, &ym.ao, &barA);
+        }
+        pendA = pendB = true;
+    }
+    // every thread waits (bounded) for the copies into one buffer. On a timeout the block
+    // reports it, counts the test hook's planted bytes, waits once more (bounded) for every copy
+    // still in flight and returns false (PSC_ERR_DEVICE when they never land).
+    auto wait = [&](uint64_t *br, unsigned par, int z) -> bool {
+        if (!__syncthreads_or(!mbar_wait_bounded(br, par, bg[z].wait_ns))) return true;
+        int *err = &const_cast<DevBG *>(bg)[z].err;
+        if (threadIdx.x == 0) {
+            report_err(err, PSC_ERR_TIMEOUT);
+            if (pendA && plantA) mbar_complete_tx(&barA, plantA);
+            if (pendB && plantB) mbar_complete_tx(&barB, plantB);
+        }
+        bool landed = true;
+        if (pendA) landed = mbar_wait_bounded(&barA, pa, bg[z].wait_ns) && landed;
+        if (pendB) landed = mbar_wait_bounded(&barB, pb, bg[z].wait_ns) && landed;
+        if (__syncthreads_or(!landed) && threadIdx.x == 0) report_err(err, PSC_ERR_DEVICE);
+        return false;
+    };
+    for (; w < total; w += gridDim.x) {
+        const unsigned wn = w + gridDim.x;
+        const bool next_tma = wn < total && wn % nbx < nplane;
+        const unsigned b = w % nbx, rest = w / nbx;
+        const int jy = (int)(rest % nf), z = (int)(rest / nf);
+        YTile y;
+        if (b < nplane) {
+            y.x0 = (int)(b / per);
+            y.x = y.x0;
+            y.kz = ((int)(b - (unsigned)y.x0 * per) << sh) + t;
+            y.column = false;
+        } else {
+            y.x = ((int)(b - nplane) << sh) + t;
+            y.kz = g.M;
+            y.column = true;
+        }
+        const long long off = (long long)jy * g.modes + (long long)z * g.fstride;
+        if (y.column) {
+            // nothing is in flight into the buffers (this item issued no copies)
+            y_column_async<C, L>(stA, TA + off, y, t, j, g);
+            y_column_async<C, L>(stB, TB + off, y, t, j, g);
+            cp_async_commit();
+            cp_async_wait_all();   // own elements only
+            __syncthreads();       // the previous item's last exchange reads are done
+        }
+        const T kIR = (T)bg[z].kIR;
+        int s0, sp;
+        y_slots<C, L>(j, t, TL, g.M, s0, sp);
+        const long long base = off + (long long)y.x * g.N * g.H + y.kz;
+#pragma unroll 1
+        for (int k = 0; k < 3; ++k) {
+            // k = 0: TB -> TB; 1: d/dy TA -> TC; 2: TA -> TA
+            if (k) __syncthreads();   // the exchange buffer is free again (k = 0: the wait's barrier)
+            if (!y.column && k < 2) {
+                if (!wait(k == 0 ? &barB : &barA, k == 0 ? pb : pa, z)) return;
+                if (k == 0) {
+                    pb ^= 1u;
+                    pendB = false;
+                } else {
+                    pa ^= 1u;
+                    pendA = false;
+                }
+            }
+            const C *st = k == 0 ? stB : stA;
+            C v[16];
+#pragma unroll
+            for (int r = 0; r < 16; ++r) {
+                const int n = j + r * RP::P;
+                C e = st[s0 + r * sp];
+                if (k == 1) {
+                    const T ky = (n == (g.N >> 1)) ? T(0) : kIR * (T)pcoord(n, g.N);
+                    e = mk<T>(-ky * e.y, ky * e.x);
+                }
+                v[r] = e;
+            }
+            fft_reg<C, L, +1>(v, xb, ix, j, tw, g.N / L);
+            C *dst = k == 0 ? TB : (k == 1 ? TC : TA);
+#pragma unroll
+            for (int q = 0; q < RP::NBL; ++q)
+#pragma unroll
+                for (int r = 0; r < RP::RL; ++r) dst[base + (long long)RP::out(j, q, r) * g.H] = v[q * RP::RL + r];
+            // every thread has passed the transform's barriers, so every read of the buffer
+            // this transform used is done: refill it with the next item's tile
+            if (next_tma && k != 1) {
+                if (threadIdx.x == 0) {
+                    if (k == 0) plantB = issue(wn, stB, &ym.be, &ym.bo, &barB);
+                    else plantA = issue(wn, stA, &ym.ae, &ym.ao, &barA);
+                }
+                if (k == 0) pendB = true;
+                else pendA = true;
+            }
+        }
+    }
+}
+
+
 // ------------------------------------------------------------------ X forward + kick epilogue
 template <typename T, int L, bool GW, class VB>
 __device__ __forceinline__ void kr_fft_x_final_body(const VB &vb, Geo g, const cplx<T> *__restrict__ QV, const cplx<T> *__restrict__ QS, const cplx<T> *__restrict__ fk, cplx<T> *__restrict__ pk, cplx<T> *__restrict__ uk, cplx<T> *__restrict__ puk, double *__restrict__ partKG, const DevBG *__restrict__ bg, const cplx<T> *__restrict__ tw, cplx<T> *__restrict__ tape_f, cplx<T> *__restrict__ tape_p, cplx<T> *__restrict__ tape_vp, cplx<T> *__restrict__ tape_pu, cplx<T> *__restrict__ tape_fu, cplx<T> *__restrict__ fcache, cplx<T> *__restrict__ ucache, const XTma *tma) {

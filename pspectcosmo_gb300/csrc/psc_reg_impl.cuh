@@ -41,8 +41,9 @@ struct RegLaunch {
         SETA((kr_ifft_y<T, N, false>), sxy);
         SETA((kr_ifft_y<T, N, true>), 3 * sxy);   // exchange tile + TA and TB staging tiles
         SETA((kr_fft_y<T, N>), sxy);
-        if constexpr (kYPipe) {   // the Y forward staged by tensor maps: two 128-byte aligned buffers
+        if constexpr (kYPipe) {   // the Y passes staged by tensor maps: 128-byte aligned buffers
             SETA((kr_fft_y_pipe<T, N>), 2 * (int)cfg.smem_ys + 128);
+            SETA((kr_ifft_y_pipe<T, N>), 2 * (int)cfg.smem_ys + sxy + 128);   // + the exchange tile
         }
         SETA((kr_fft_x_final<T, N, false>), (int)cfg.smem_xf);
         SETA((kr_fft_x_final<T, N, true>), (int)cfg.smem_xf);
@@ -130,7 +131,18 @@ struct RegLaunch {
             if (drift) kr_ifft_x<T, N, true, true><<<gx, txy, sxi, st>>>(g, fk, pk, TA, TB, b.bg, tw, xt);
             else kr_ifft_x<T, N, true, false><<<gx, txy, sxi, st>>>(g, fk, pk, TA, TB, b.bg, tw, xt);
             mark(1);
-            kr_ifft_y<T, N, true><<<gx, txy, 3 * cfg.smem_xy, st>>>(g, TA, TB, TC, b.bg, tw);
+            bool ipiped = false;
+            if constexpr (kYPipe) {
+                if (b.ytma_i && b.ytma_i->on) {
+                    // persistent and pipelined: two blocks per SM (one for 1024-point lines)
+                    const long long items = (long long)cfg.nbx * g.nf * R, wave = (long long)xy_blocks<N>(2) * cfg.sms;
+                    const int grid = (int)(items < wave ? items : wave);
+                    kr_ifft_y_pipe<T, N><<<grid, txy, 2 * cfg.smem_ys + cfg.smem_xy + 128, st>>>(g, TA, TB, TC, b.bg, tw,
+                                                                                              *b.ytma_i, R);
+                    ipiped = true;
+                }
+            }
+            if (!ipiped) kr_ifft_y<T, N, true><<<gx, txy, 3 * cfg.smem_xy, st>>>(g, TA, TB, TC, b.bg, tw);
             mark(2);
             zpass_any(cfg, b, st, R);
         } else {

@@ -366,11 +366,11 @@ class Lattice:
         sh = (ctypes.c_int * 3)(*[int(x) for x in value])
         _check(self._L.psc_set_shapes(self._h, sh), "psc_set_shapes")
 
-    TMAP_X, TMAP_Y = 1, 2
+    TMAP_X, TMAP_Y, TMAP_YINV = 1, 2, 4
 
     @property
     def tensor_maps(self) -> int:
-        """The pass groups that stage their tiles by tensor maps (TMAP_X | TMAP_Y bits)."""
+        """The pass groups that stage their tiles by tensor maps (TMAP_X | TMAP_Y | TMAP_YINV bits)."""
         m = ctypes.c_int()
         _check(self._L.psc_get_tensor_maps(self._h, ctypes.byref(m)), "psc_get_tensor_maps")
         return m.value

@@ -1,12 +1,13 @@
 """Tile staging by tensor maps (TMA). The X passes (X inverse in FP32, X forward + kick; above
 N = 256 a tile is N/256 boxes along x) and,
-in FP32 at N = 128 and 256, the Y forward pass (persistent and pipelined) stage their tiles in
-shared memory by tiled tensor copies; with the maps switched off (psc_set_tensor_maps) every
+in FP32 at N = 128 .. 1024, the Y forward pass (persistent and pipelined; the GW Y inverse pass
+in the same form at 1024, or on request) stage their tiles in shared memory by tiled tensor
+copies; with the maps switched off (psc_set_tensor_maps) every
 thread loads its own elements.
 The staging only changes where a value is read from, so every form must give the same bits:
 fields, GW tensors and background after a few steps, from the same state, with the same tile
-shapes. The Y forward pass's tensor-map form also walks its tiles in another order (TL
-consecutive kz of one x plane, then the kz = N/2 column), which must not change a bit either.
+shapes. The Y passes' tensor-map forms also walk their tiles in another order (TL consecutive
+kz of one x plane, then the kz = N/2 column), which must not change a bit either.
 Each pass's bounded waits are driven to run out (the test hook plants bytes that no copy
 delivers; every copy lands in valid memory): psc_step returns PSC_ERR_TIMEOUT and the handle
 then evolves exactly as a fresh one."""
@@ -17,7 +18,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-X, Y = 1, 2
+X, Y, YI = 1, 2, 4
 PSC_ERR_CONFIG = -1
 PSC_ERR_TIMEOUT = -5
 KEYS = ("f_k", "pi_k", "u_k", "pi_u_k")
@@ -49,7 +50,10 @@ def test_groups_in_use(N, precision, gw, want):
     lat.tensor_maps = X | Y
     assert lat.tensor_maps == want
     L = lat._L
-    assert L.psc_set_tensor_maps(lat._h, 4) != 0   # an unknown group
+    assert L.psc_set_tensor_maps(lat._h, 8) != 0   # an unknown group
+    if want & Y and gw:   # the pipelined GW Y inverse pass on request
+        lat.tensor_maps = X | Y | YI
+        assert lat.tensor_maps == X | Y | YI
     lat.close()
 
 
@@ -66,13 +70,13 @@ def test_every_form_gives_the_same_bits(N, precision, gw, shift):
     lat.initialize()
     s0 = lat.get_state()
     out = {}
-    for mask in (X | Y, Y, X, 0):
+    for mask in (X | Y | YI, X | Y, Y, X, 0):
         lat.tensor_maps = mask
         lat.set_state(s0["f_k"], s0["pi_k"], s0["a"], s0["ad"], s0["add"], s0.get("u_k"), s0.get("pi_u_k"))
         lat.evolve(0.005, 3)
         out[mask] = lat.get_state()
     lat.close()
-    for mask in (X | Y, Y, X):
+    for mask in (X | Y | YI, X | Y, Y, X):
         _same(out[mask], out[0], gw)
 
 
@@ -96,7 +100,7 @@ def test_batch_realizations_with_tensor_maps_equal_single_lattices():
     ens.close()
 
 
-@pytest.mark.parametrize("pas", [0, 2, 3, 4], ids=["x_inverse", "zpass", "y_forward", "x_forward"])
+@pytest.mark.parametrize("pas", [0, 1, 2, 3, 4], ids=["x_inverse", "y_inverse", "zpass", "y_forward", "x_forward"])
 def test_each_staged_wait_runs_out_and_the_handle_recovers(pas):
     from pspectcosmo_gb300 import Lattice, PscError
 
@@ -110,6 +114,7 @@ def test_each_staged_wait_runs_out_and_the_handle_recovers(pas):
 
     lat = Lattice(p)
     L = lat._L
+    lat.tensor_maps = X | Y | YI   # the Y inverse pass pipelined at this size too
     lat.set_state(s0["f_k"], s0["pi_k"], s0["a"], s0["ad"], s0["add"], s0["u_k"], s0["pi_u_k"])
     assert L.psc_test_wait_hook_pass(lat._h, ctypes.c_double(20.0), 16, pas) == 0
     with pytest.raises(PscError) as ei:
@@ -124,7 +129,4 @@ def test_each_staged_wait_runs_out_and_the_handle_recovers(pas):
     rc = L.psc_test_wait_hook_pass(lat._h, ctypes.c_double(20.0), 16, pas)
     assert rc == (0 if pas == 2 else PSC_ERR_CONFIG)
     L.psc_test_wait_hook_pass(lat._h, ctypes.c_double(1000.0), 0, pas)
-    # the Y inverse pass loads directly in every form
-    lat.tensor_maps = X | Y
-    assert L.psc_test_wait_hook_pass(lat._h, ctypes.c_double(20.0), 16, 1) == PSC_ERR_CONFIG
     lat.close()
