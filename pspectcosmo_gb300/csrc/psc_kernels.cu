@@ -905,10 +905,11 @@ void plan(const psc_params &p, int R, LaunchCfg *cfg, const TileChoice *tc) {
         cfg->thr_z = nin * tlz * Pz;
         // Z pass shared memory. Without GWs (kr_zpass): nf work slots + nf staging slots of
         // half-length lines, persistent (2 blocks per SM). With GWs (kr_zpass_gw): four
-        // slots of N-point lines and, in FP32 (persistent, 3 blocks per SM, next tile
+        // slots of N-point lines and, in FP32 (persistent, 2 blocks per SM at up to 128
+        // registers: 0.384 against 0.402 ms at 3 blocks and 80 registers, 256^3; next tile
         // staged), the nf x 3 input lines of a tile; in FP64 one tile per block.
         // A user model (up to kMaxFields fields) runs the USER instantiations: nslot work
-        // slots (input pairs 2 nf, output pairs (nf + 7) / 2) and at most 2 blocks per SM.
+        // slots (input pairs 2 nf, output pairs (nf + 7) / 2).
         const bool gw_staged = g.gwev && p.precision == 32;
         const bool user = model_is_user(p.model);
         const int gw_slots = user ? ((2 * g.nf > (g.nf + 7) / 2) ? 2 * g.nf : (g.nf + 7) / 2) : 4;
@@ -925,7 +926,7 @@ void plan(const psc_params &p, int R, LaunchCfg *cfg, const TileChoice *tc) {
         cfg->sms = sms;
         const size_t smem_sm = 227 * 1024;
         int per_sm = (int)(smem_sm / cfg->smem_z);
-        if (per_sm > ((gw_staged && !user) ? 3 : 2)) per_sm = (gw_staged && !user) ? 3 : 2;
+        if (per_sm > 2) per_sm = 2;   // the Z passes' launch bounds
         if (tc && tc->z_per_sm > 0 && tc->z_per_sm < per_sm) per_sm = tc->z_per_sm;
         if (per_sm < 1) per_sm = 1;
         cfg->tc.z_per_sm = per_sm;

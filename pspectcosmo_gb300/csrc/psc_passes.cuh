@@ -1434,7 +1434,7 @@ __device__ __forceinline__ void kr_zpass_gw_body(const VB &vb, Geo g, const cplx
 }
 
 template <typename T, int L, bool STAGED, bool USER = false>
-__global__ void __launch_bounds__(256, (sizeof(T) == 4 && !USER) ? 3 : 2) kr_zpass_gw(Geo g, const cplx<T> *__restrict__ TA,
+__global__ void __launch_bounds__(256, 2) kr_zpass_gw(Geo g, const cplx<T> *__restrict__ TA,
                                                      const cplx<T> *__restrict__ TB, const cplx<T> *__restrict__ TC,
                                                      cplx<T> *__restrict__ QV, cplx<T> *__restrict__ QS,
                                                      double *__restrict__ partV, const DevBG *bg,
