@@ -516,6 +516,10 @@ __device__ double friedmann_add(const DevBG *bg, double K, double G, double V) {
 // kick uses the kept force.
 // r: the realization (the block of one configuration's kernel; the batched background kernel
 // passes a realization of one of its configurations)
+// threads of the background kernel's block (the reduction of the block partials; the rest is
+// one thread's FP64 arithmetic): 256 against 1024 cut its FP64 shuffle trees by four
+constexpr int kScalarThreads = 256;
+
 __device__ __forceinline__ void k_scalar_body(unsigned r, DevBG *bg, const double *__restrict__ partKG,
                                               const double *__restrict__ partV, int mode, int p, int pkg_stride,
                                               int pv_stride, void *fk, void *pk, long long fstride, long long modes) {
@@ -553,9 +557,13 @@ __device__ __forceinline__ void k_scalar_body(unsigned r, DevBG *bg, const doubl
 #pragma unroll
             for (int q = 0; q < kMaxTerms; ++q)
                 if (q < nt) acc[2 * kMaxFields + q] += partV[(size_t)q * nbz + i];
+        // only the live quantities (2 nf field sums, nt terms) go through the shuffle trees:
+        // on this part's narrow FP64 pipe the trees of every slot dominated the kernel
+        auto live = [&](int q) { return q < 2 * kMaxFields ? q < 2 * nf : q - 2 * kMaxFields < nt; };
 #pragma unroll
         for (int q = 0; q < NQ; ++q)
-            for (int o = 16; o > 0; o >>= 1) acc[q] += __shfl_down_sync(0xffffffffu, acc[q], o);
+            if (live(q))
+                for (int o = 16; o > 0; o >>= 1) acc[q] += __shfl_down_sync(0xffffffffu, acc[q], o);
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
         if (lane == 0)
 #pragma unroll
@@ -564,6 +572,7 @@ __device__ __forceinline__ void k_scalar_body(unsigned r, DevBG *bg, const doubl
         if (warp == 0) {
 #pragma unroll
             for (int q = 0; q < NQ; ++q) {
+                if (!live(q)) continue;
                 double x = lane < nw ? red[lane][q] : 0.0;
                 for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
                 if (lane == 0) {
@@ -647,7 +656,7 @@ __device__ __forceinline__ void k_scalar_body(unsigned r, DevBG *bg, const doubl
     }
 }
 
-__global__ void __launch_bounds__(1024) k_scalar(DevBG *bg, const double *__restrict__ partKG,
+__global__ void __launch_bounds__(kScalarThreads) k_scalar(DevBG *bg, const double *__restrict__ partKG,
                                                 const double *__restrict__ partV, int mode, int p, int pkg_stride,
                                                 int pv_stride, void *fk, void *pk, long long fstride,
                                                 long long modes) {
@@ -1041,7 +1050,7 @@ static cudaError_t launch_stage_t(const LaunchCfg &cfg, const Buffers &b, int dr
     else k_fft_x_final<T, false><<<gf, cfg.thr_xy, cfg.smem_xy, st>>>(g, QV, QS, fk, pk, uk, puk, b.partKG, b.bg, tw);
     mark(5);
     if (scalar_mode >= 0) {
-        k_scalar<<<cfg.R, 1024, 0, st>>>(b.bg, b.partKG, b.partV, scalar_mode, 1, cfg.g.pkg_stride, cfg.g.pv_stride,
+        k_scalar<<<cfg.R, kScalarThreads, 0, st>>>(b.bg, b.partKG, b.partV, scalar_mode, 1, cfg.g.pkg_stride, cfg.g.pv_stride,
                                          b.fk, b.pk, cfg.g.fstride, cfg.g.modes);
         mark(6);
     }
@@ -1093,9 +1102,10 @@ cudaError_t launch_stage(const LaunchCfg &cfg, const Buffers &b, int precision, 
 }
 
 // SCALAR_END of stage p for every realization of every configuration of a batch: block i is
-// realization i of the concatenated list (the groups' realizations in order). 1024 threads, as
-// k_scalar: the partial sums add up in the same order, so the background is the same bits.
-__global__ void __launch_bounds__(1024) k_scalar_batch(const __grid_constant__ BatchTable bt, int p) {
+// realization i of the concatenated list (the groups' realizations in order). kScalarThreads
+// threads, as k_scalar: the partial sums add up in the same order, so the background is the
+// same bits.
+__global__ void __launch_bounds__(kScalarThreads) k_scalar_batch(const __grid_constant__ BatchTable bt, int p) {
     unsigned r = blockIdx.x;
     int gi = 0;
     while (gi + 1 < bt.ngroups && r >= (unsigned)bt.grp[gi].R) {
@@ -1110,12 +1120,12 @@ __global__ void __launch_bounds__(1024) k_scalar_batch(const __grid_constant__ B
 cudaError_t launch_scalar_batch(const BatchTable &bt, int p, cudaStream_t st) {
     int n = 0;
     for (int i = 0; i < bt.ngroups; ++i) n += bt.grp[i].R;
-    k_scalar_batch<<<n, 1024, 0, st>>>(bt, p);
+    k_scalar_batch<<<n, kScalarThreads, 0, st>>>(bt, p);
     return cudaGetLastError();
 }
 
 cudaError_t launch_scalar(const LaunchCfg &cfg, const Buffers &b, int mode, int p, cudaStream_t st) {
-    k_scalar<<<cfg.R, 1024, 0, st>>>(b.bg, b.partKG, b.partV, mode, p, cfg.g.pkg_stride, cfg.g.pv_stride, b.fk, b.pk,
+    k_scalar<<<cfg.R, kScalarThreads, 0, st>>>(b.bg, b.partKG, b.partV, mode, p, cfg.g.pkg_stride, cfg.g.pv_stride, b.fk, b.pk,
                                      cfg.g.fstride, cfg.g.modes);
     return cudaGetLastError();
 }
