@@ -58,6 +58,22 @@ def test_invalid_configurations_are_rejected(psc_lib, bad):
     assert psc_lib.psc_strerror(rc) == b"unsupported configuration"
 
 
+@pytest.mark.parametrize("ok", [dict(N=24), dict(N=20), dict(N=28), dict(N=96), dict(N=480), dict(N=1024),
+                                dict(N=16, N_pad=24), dict(N=20, N_pad=30), dict(N=32, N_pad=64)])
+def test_accepted_sizes_pass_validation(psc_lib, ok):
+    """Even N up to 512 with prime factors 2, 3, 5, 7 (and such an N_pad above N) pass the
+    parameter checks: psc_create fails only where no GPU is present (a CUDA error, not
+    PSC_ERR_CONFIG)."""
+    from pspectcosmo_gb300.params import Params
+
+    p = Params.reference_default(**ok)
+    h = ctypes.c_void_p()
+    rc = psc_lib.psc_create(ctypes.byref(p), ctypes.byref(h))
+    assert rc != -1, psc_lib.psc_last_error()
+    if rc == 0:
+        psc_lib.psc_destroy(h)
+
+
 def test_null_arguments(psc_lib):
     h = ctypes.c_void_p()
     assert psc_lib.psc_create(None, ctypes.byref(h)) == -2
